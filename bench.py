@@ -1,0 +1,320 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 CKKS engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl nexus|reference] [--workload NAME]
+
+Prints ONE JSON line (rank 0).  Workloads:
+
+  ntt   Batched forward negacyclic NTT at N=2^16 over 24 primes of 60 bits
+        (CoeffModulus::Create(65536, 24 x 60)), 64 ciphertexts x 2 polynomials
+        of uniform residues = 3072 limb-NTTs per step, one engine call per
+        step.  Inputs (1.5 GiB) are larger than L2, so no flush is needed.
+
+`--impl reference` times the CPU restatement of SEAL's NTT (the oracle port,
+all host threads) on a bounded sample of the same workload.  Under torchrun
+(N>1) every rank runs an independent replica (the path has no exchange step),
+the timed region is bracketed by barriers and the slowest rank's time is used.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def _peak_hbm():
+    try:
+        d = json.loads(MEASURED_PEAKS.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def _profile_traffic(name: str):
+    """Per-launch DRAM bytes recorded from ncu in profiles/<name>.txt."""
+    p = ROOT / "profiles" / f"{name}.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.idx = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- NTT workload
+
+NTT_LOGN = 16
+NTT_PRIMES = 24
+NTT_CTS = 64
+NTT_POLYS = 2
+
+
+def ntt_config():
+    return {"workload": "ntt_forward_n65536_l24_64ct", "N": 1 << NTT_LOGN, "primes": NTT_PRIMES,
+            "prime_bits": 60, "ciphertexts": NTT_CTS, "polys_per_ct": NTT_POLYS,
+            "limb_ntts_per_step": NTT_CTS * NTT_POLYS * NTT_PRIMES, "parallelism": "replicas",
+            "l2": "inputs 1.5 GiB > L2, no flush"}
+
+
+def run_ntt_gpu(args, rank, world):
+    import numpy as np
+    import torch
+
+    import nexus_gb300 as ng
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = 1 << NTT_LOGN
+    qs = ng.create_coeff_modulus(n, [60] * NTT_PRIMES)
+    ctx = ng.Context(NTT_LOGN, qs)
+    limbs = NTT_CTS * NTT_POLYS * NTT_PRIMES
+    g = torch.Generator(device=dev).manual_seed(1234 + rank)
+    qd = torch.tensor(qs, dtype=torch.int64, device=dev).view(1, NTT_PRIMES, 1)
+    x = torch.randint(0, 2**62, (NTT_CTS * NTT_POLYS, NTT_PRIMES, n), generator=g, device=dev,
+                      dtype=torch.int64) % qd
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        ctx.ntt_forward(x, 0, NTT_PRIMES, stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize(dev)
+        t0.record(stream)
+        for i in range(args.steps):
+            evs[i][0].record(stream)
+            step()
+            evs[i][1].record(stream)
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+    barrier(world)
+    total_ms = t0.elapsed_time(t1)
+    total_ms = max_over_ranks(total_ms, world)
+    per_launch_ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+    # end to end through the public API: pinned host -> device, NTT, device -> host
+    e2e_steps = max(1, min(args.steps, 5))
+    host_in = torch.empty_like(x, device="cpu").pin_memory()
+    host_in.copy_(x)
+    host_out = torch.empty_like(host_in).pin_memory()
+    dbuf = torch.empty_like(x)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        dbuf.copy_(host_in, non_blocking=True)
+        ctx.ntt_forward(dbuf, 0, NTT_PRIMES, stream)
+        host_out.copy_(dbuf, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), world)
+    nbytes = x.numel() * 8
+
+    units = limbs * args.steps * world
+    value = units / (total_ms / 1e3)
+    alg_bytes = 2 * 8 * n * limbs
+    peak, peak_kind = _peak_hbm()
+    achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
+    res = {
+        "metric": "ntt_limb_throughput_n65536",
+        "value": value,
+        "unit": "limb-NTT/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic uniform residues (seeded)",
+        "config": ntt_config(),
+        "roofline": {
+            "kernel": "nexus_ntt_forward (k_fwd_cols + k_fwd_rows)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": alg_bytes,
+            "traffic": _profile_traffic("ntt_forward_n65536_l24_64ct"),
+        },
+        "e2e": {"value": limbs * e2e_steps * world / (e2e_ms / 1e3), "unit": "limb-NTT/s",
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+        "clocks": clk.summary(),
+        "gpu_launches": 2 * args.steps,
+    }
+    if rank == 0 and world == 1:
+        res["cpu_baseline"] = cpu_ntt_sample(budget_s=args.cpu_seconds)
+    return res
+
+
+def cpu_ntt_sample(budget_s: float = 10.0, threads: int | None = None):
+    """Oracle port of SEAL's NTT on the host cores over a bounded sample."""
+    import numpy as np
+
+    from oracle import pyoracle as po
+    n = 1 << NTT_LOGN
+    qs = po.create_coeff_modulus(n, [60] * NTT_PRIMES)
+    oc = po.OracleContext(NTT_LOGN, qs)
+    threads = threads or po.default_threads()
+    rng = np.random.default_rng(99)
+    polys = max(2, threads // 4)
+    x = po.random_residues(rng, (polys, NTT_PRIMES, n), qs)
+    done = 0
+    t0 = time.perf_counter()
+    while True:
+        po.lib().or_ntt_batch(oc._h, x.ctypes.data_as(po.u64p), polys, 0, NTT_PRIMES, 0, threads)
+        done += polys * NTT_PRIMES
+        el = time.perf_counter() - t0
+        if el >= budget_s:
+            break
+    return {"value": done / el, "unit": "limb-NTT/s", "cores": threads, "kind": "port",
+            "sample": f"{done} limb-NTTs (N=2^16, 60-bit primes) in {el:.1f} s"}
+
+
+# ----------------------------------------------------------------------------- plumbing
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["nexus", "reference"], default="nexus")
+    ap.add_argument("--workload", choices=["ntt"], default="ntt")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ntt-cts", type=int, default=NTT_CTS,
+                    help="ciphertexts per step (smaller values are for profiling captures only)")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    global NTT_CTS
+    NTT_CTS = args.ntt_cts
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        t_steps = []
+        cfg = ntt_config()
+        for i in range(args.warmup + args.steps):
+            r = cpu_ntt_sample(budget_s=max(1.0, args.cpu_seconds / max(1, args.steps)))
+            if i >= args.warmup:
+                t_steps.append(r)
+        value = statistics.mean(r["value"] for r in t_steps)
+        cores = t_steps[0]["cores"]
+        res = {
+            "impl": "reference", "metric": "ntt_limb_throughput_n65536", "value": value, "unit": "limb-NTT/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": cfg["limb_ntts_per_step"] / value * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic uniform residues (seeded)", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": "limb-NTT/s", "cores": cores, "kind": "port",
+                             "sample": "per step: " + t_steps[0]["sample"]},
+            "e2e": {"value": value, "unit": "limb-NTT/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(res), flush=True)
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    res = run_ntt_gpu(args, rank, world)
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

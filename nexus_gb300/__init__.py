@@ -1,0 +1,9 @@
+"""nexus_gb300: a GB300-native CKKS evaluation engine for NEXUS's
+encrypted-inference hot path.
+
+The compute path is hand-written sm_103a CUDA behind the C ABI declared in
+``include/nexus_gb300.h``; this package holds the build script and a thin
+ctypes layer used by the tests and the benchmark.
+"""
+from ._lib import NexusError, check, lib  # noqa: F401
+from .context import Context, create_coeff_modulus  # noqa: F401

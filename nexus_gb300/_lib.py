@@ -1,0 +1,52 @@
+"""ctypes binding of libnexus_gb300.so (the C ABI in include/nexus_gb300.h).
+
+The shared library is built in-tree by :mod:`nexus_gb300.build`.  Loading
+fails loudly when it is missing: there is no CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_LIB_PATH = Path(__file__).resolve().parent / "libnexus_gb300.so"
+_lib = None
+
+u64p = C.POINTER(C.c_uint64)
+
+# (name, restype, argtypes) of every exported entry point
+SIGNATURES = [
+    ("nexus_last_error", C.c_char_p, []),
+    ("nexus_create_coeff_modulus", C.c_int, [C.c_uint64, C.POINTER(C.c_int), C.c_int, u64p]),
+    ("nexus_context_create", C.c_int, [C.c_int, u64p, C.c_int, C.POINTER(C.c_void_p)]),
+    ("nexus_context_destroy", C.c_int, [C.c_void_p]),
+    ("nexus_context_get_psi", C.c_int, [C.c_void_p, u64p]),
+    ("nexus_ntt_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int, C.c_int, C.c_void_p]),
+    ("nexus_ntt_inverse", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int, C.c_int, C.c_void_p]),
+]
+
+
+class NexusError(RuntimeError):
+    pass
+
+
+def lib():
+    """Return the loaded library, loading it on first use."""
+    global _lib
+    if _lib is None:
+        if not _LIB_PATH.exists():
+            raise NexusError(
+                f"{_LIB_PATH} is missing: build it with `python -m nexus_gb300.build` "
+                "(the engine has no CPU fallback)")
+        l = C.CDLL(str(_LIB_PATH))
+        for name, res, args in SIGNATURES:
+            f = getattr(l, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = l
+    return _lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != 0:
+        msg = lib().nexus_last_error().decode(errors="replace")
+        raise NexusError(f"{what}: {msg}" if what else msg)

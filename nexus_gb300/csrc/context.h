@@ -1,0 +1,52 @@
+// Engine context: the RNS prime chain of one CKKS parameter set and the
+// device tables every kernel reads (twiddles, Barrett ratios, n^{-1}).
+//
+// Prime order follows SEAL's key level (context.cpp): indices 0..k-2 are the
+// data primes q_0..q_{L-1}; index k-1 is the special prime used only inside
+// key switching.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "modarith.cuh"
+
+namespace nexus {
+
+struct Context {
+    int logn = 0;
+    uint64_t n = 0;
+    int k = 0;                       // primes including the special prime
+    int device = 0;
+    std::vector<uint64_t> q;         // host copy of the primes
+    std::vector<uint64_t> psi;       // minimal primitive 2N-th roots
+    std::vector<PrimeConst> pc;      // host copy of the per-prime constants
+
+    PrimeConst *d_pc = nullptr;      // [k]
+    // Forward twiddles: tw_fwd[j*n + i] = {psi_j^{bitrev(i)}, Shoup quotient}.
+    // This is the power table of SEAL's NTTTables (util/ntt.cpp:270-278).
+    ulonglong2 *d_tw_fwd = nullptr;  // [k][n]
+    // Inverse twiddles indexed like the forward table:
+    // tw_inv[j*n + i] = {psi_j^{-bitrev(i)}, Shoup quotient}.
+    ulonglong2 *d_tw_inv = nullptr;  // [k][n]
+
+    // Split of the two-pass NTT: n = n1 * n2 (rows x columns).
+    int log_n1 = 0, log_n2 = 0;
+};
+
+// Host helpers shared by the translation units.
+uint64_t host_mulmod(uint64_t a, uint64_t b, uint64_t q);
+uint64_t host_powmod(uint64_t a, uint64_t e, uint64_t q);
+uint64_t host_invmod(uint64_t a, uint64_t q);
+uint64_t host_shoup(uint64_t w, uint64_t q);
+
+// Thread-local error text behind nexus_last_error().
+void set_error(const std::string &msg);
+
+}  // namespace nexus
+
+struct nexus_context {
+    nexus::Context c;
+};

@@ -1,0 +1,320 @@
+// Batched negacyclic RNS NTT / INTT over [poly][limb][N] uint64 residues.
+//
+// The transform is the one SEAL computes in ntt_negacyclic_harvey /
+// inverse_ntt_negacyclic_harvey (util/ntt.cpp:394-470, util/dwthandler.h:94-290
+// in SEAL-4.1-bs): input in natural order, output in bit-reversed order, with
+// psi the minimal primitive 2N-th root.  Because the transform is a linear map
+// over Z_q and both sides reduce to [0, q), any exact evaluation of it gives
+// SEAL's words; this file evaluates it as two passes over an n1 x n2 view of
+// each limb (row index r = i / n2, column c = i % n2):
+//
+//   pass 1 (columns): the first log2(n1) Cooley-Tukey stages only pair rows of
+//     one column, and the stage with m blocks uses twiddle W[m + block];
+//   pass 2 (rows): the remaining log2(n2) stages stay inside one contiguous
+//     row r, and the local stage with m blocks uses W[(n1 + r) * m + block].
+//
+// Each thread holds 16 residues in registers; 4 butterfly stages run in
+// registers, the thread group exchanges through shared memory, and the next
+// log2(T) stages run in registers again.  Butterflies are Harvey's lazy
+// Shoup butterflies (values in [0,4q) forward, [0,2q) inverse).
+#include <cstdio>
+#include <stdexcept>
+
+#include "context.h"
+#include "ntt.h"
+
+namespace nexus {
+
+namespace {
+
+constexpr int kE = 16;          // residues per thread
+constexpr int kThreads = 256;   // threads per CTA
+
+__device__ __forceinline__ void ct_bfly(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q, uint64_t q2)
+{
+    uint64_t u = csub(x, q2);
+    uint64_t v = mul_shoup_lazy(y, w.x, w.y, q);
+    x = u + v;
+    y = u + q2 - v;
+}
+
+__device__ __forceinline__ void gs_bfly(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q, uint64_t q2)
+{
+    uint64_t u = x, v = y;
+    x = csub(u + v, q2);
+    y = mul_shoup_lazy(u + q2 - v, w.x, w.y, q);
+}
+
+// Forward stages whose pairs are (k, k+h) inside the thread, residues at
+// sub-transform positions s = t + T*k.  Stage with pair distance h has
+// m = E/(2h) blocks and block index k/(2h).
+__device__ __forceinline__ void fwd_regs_strided(uint64_t (&x)[kE], const ulonglong2 *__restrict__ W, uint64_t B,
+                                                 uint64_t q, uint64_t q2)
+{
+#pragma unroll
+    for (int h = kE / 2; h >= 1; h >>= 1) {
+        const int m = kE / (2 * h);
+#pragma unroll
+        for (int k = 0; k < kE; ++k) {
+            if (k & h) continue;
+            ulonglong2 w = __ldg(&W[B * m + k / (2 * h)]);
+            ct_bfly(x[k], x[k + h], w, q, q2);
+        }
+    }
+}
+
+// Forward stages with gaps T/2 .. 1 on residues at s = E*t + k.
+template <int T>
+__device__ __forceinline__ void fwd_regs_blocked(uint64_t (&x)[kE], const ulonglong2 *__restrict__ W, uint64_t B,
+                                                 int t, uint64_t q, uint64_t q2)
+{
+    constexpr int S = kE * T;
+#pragma unroll
+    for (int g = T / 2; g >= 1; g >>= 1) {
+        const int m = S / (2 * g);
+        const uint64_t base = B * m + (uint64_t)(kE * t) / (2 * g);
+#pragma unroll
+        for (int k = 0; k < kE; ++k) {
+            if (k & g) continue;
+            ulonglong2 w = __ldg(&W[base + k / (2 * g)]);
+            ct_bfly(x[k], x[k + g], w, q, q2);
+        }
+    }
+}
+
+// Inverse of fwd_regs_blocked: gaps 1 .. T/2, Gentleman-Sande butterflies.
+template <int T>
+__device__ __forceinline__ void inv_regs_blocked(uint64_t (&x)[kE], const ulonglong2 *__restrict__ W, uint64_t B,
+                                                 int t, uint64_t q, uint64_t q2)
+{
+    constexpr int S = kE * T;
+#pragma unroll
+    for (int g = 1; g <= T / 2; g <<= 1) {
+        const int m = S / (2 * g);
+        const uint64_t base = B * m + (uint64_t)(kE * t) / (2 * g);
+#pragma unroll
+        for (int k = 0; k < kE; ++k) {
+            if (k & g) continue;
+            ulonglong2 w = __ldg(&W[base + k / (2 * g)]);
+            gs_bfly(x[k], x[k + g], w, q, q2);
+        }
+    }
+}
+
+// Inverse of fwd_regs_strided: pair distances 1 .. E/2.
+__device__ __forceinline__ void inv_regs_strided(uint64_t (&x)[kE], const ulonglong2 *__restrict__ W, uint64_t B,
+                                                 uint64_t q, uint64_t q2)
+{
+#pragma unroll
+    for (int h = 1; h <= kE / 2; h <<= 1) {
+        const int m = kE / (2 * h);
+#pragma unroll
+        for (int k = 0; k < kE; ++k) {
+            if (k & h) continue;
+            ulonglong2 w = __ldg(&W[B * m + k / (2 * h)]);
+            gs_bfly(x[k], x[k + h], w, q, q2);
+        }
+    }
+}
+
+__device__ __forceinline__ int swz(int s) { return s + (s >> 4); }
+
+// ---------------------------------------------------------------- forward
+
+// Pass 1: size-2^LOGS transforms down the columns.  Output stays in [0,4q).
+template <int LOGS>
+__global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
+                                                       const PrimeConst *__restrict__ pc, int logn, int limb_begin,
+                                                       int limb_count)
+{
+    constexpr int S = 1 << LOGS, T = S / kE, C = kThreads / T;
+    __shared__ uint64_t sm[S * C];
+    const int n2 = 1 << (logn - LOGS);
+    const int tiles = n2 / C;
+    const size_t pl = blockIdx.x / tiles;
+    const int col0 = (blockIdx.x % tiles) * C;
+    const int prime = limb_begin + (int)(pl % (size_t)limb_count);
+    const uint64_t q = pc[prime].q, q2 = q << 1;
+    const ulonglong2 *W = tw + ((size_t)prime << logn);
+    uint64_t *p = data + (pl << logn) + col0;
+    const int c = threadIdx.x % C, t = threadIdx.x / C;
+
+    uint64_t x[kE];
+#pragma unroll
+    for (int k = 0; k < kE; ++k) x[k] = p[(size_t)(t + T * k) * n2 + c];
+    fwd_regs_strided(x, W, 1, q, q2);
+#pragma unroll
+    for (int k = 0; k < kE; ++k) sm[(t + T * k) * C + c] = x[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kE; ++k) x[k] = sm[(kE * t + k) * C + c];
+    fwd_regs_blocked<T>(x, W, 1, t, q, q2);
+#pragma unroll
+    for (int k = 0; k < kE; ++k) p[(size_t)(kE * t + k) * n2 + c] = x[k];
+}
+
+// Pass 2: size-2^LOGS transforms along contiguous rows, then the final
+// reduction [0,4q) -> [0,q).
+template <int LOGS>
+__global__ void __launch_bounds__(kThreads) k_fwd_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
+                                                       const PrimeConst *__restrict__ pc, int logn, int limb_begin,
+                                                       int limb_count)
+{
+    constexpr int S = 1 << LOGS, T = S / kE, R = kThreads / T, SP = S + S / 16;
+    __shared__ uint64_t sm[R * SP];
+    const int log_n1 = logn - LOGS;
+    const int rr = threadIdx.x / T, t = threadIdx.x % T;
+    const size_t grow = (size_t)blockIdx.x * R + rr;
+    const size_t pl = grow >> log_n1;
+    const uint64_t r = grow & ((1u << log_n1) - 1);
+    const int prime = limb_begin + (int)(pl % (size_t)limb_count);
+    const uint64_t q = pc[prime].q, q2 = q << 1;
+    const ulonglong2 *W = tw + ((size_t)prime << logn);
+    uint64_t *p = data + grow * S;
+    uint64_t *srow = sm + rr * SP;
+    const uint64_t B = (1ull << log_n1) + r;
+
+    uint64_t x[kE];
+#pragma unroll
+    for (int k = 0; k < kE; ++k) x[k] = p[t + T * k];
+    fwd_regs_strided(x, W, B, q, q2);
+#pragma unroll
+    for (int k = 0; k < kE; ++k) srow[swz(t + T * k)] = x[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kE; ++k) x[k] = srow[swz(kE * t + k)];
+    fwd_regs_blocked<T>(x, W, B, t, q, q2);
+#pragma unroll
+    for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = csub(csub(x[k], q2), q);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kE; ++k) p[t + T * k] = srow[swz(t + T * k)];
+}
+
+// ---------------------------------------------------------------- inverse
+
+// Inverse pass A: rows first (undoing pass 2).  Output in [0,2q).
+template <int LOGS>
+__global__ void __launch_bounds__(kThreads) k_inv_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
+                                                       const PrimeConst *__restrict__ pc, int logn, int limb_begin,
+                                                       int limb_count)
+{
+    constexpr int S = 1 << LOGS, T = S / kE, R = kThreads / T, SP = S + S / 16;
+    __shared__ uint64_t sm[R * SP];
+    const int log_n1 = logn - LOGS;
+    const int rr = threadIdx.x / T, t = threadIdx.x % T;
+    const size_t grow = (size_t)blockIdx.x * R + rr;
+    const size_t pl = grow >> log_n1;
+    const uint64_t r = grow & ((1u << log_n1) - 1);
+    const int prime = limb_begin + (int)(pl % (size_t)limb_count);
+    const uint64_t q = pc[prime].q, q2 = q << 1;
+    const ulonglong2 *W = tw + ((size_t)prime << logn);
+    uint64_t *p = data + grow * S;
+    uint64_t *srow = sm + rr * SP;
+    const uint64_t B = (1ull << log_n1) + r;
+
+    uint64_t x[kE];
+#pragma unroll
+    for (int k = 0; k < kE; ++k) srow[swz(t + T * k)] = p[t + T * k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kE; ++k) x[k] = srow[swz(kE * t + k)];
+    inv_regs_blocked<T>(x, W, B, t, q, q2);
+#pragma unroll
+    for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = x[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kE; ++k) x[k] = srow[swz(t + T * k)];
+    inv_regs_strided(x, W, B, q, q2);
+#pragma unroll
+    for (int k = 0; k < kE; ++k) p[t + T * k] = x[k];
+}
+
+// Inverse pass B: columns (undoing pass 1), then n^{-1} and reduction to [0,q).
+template <int LOGS>
+__global__ void __launch_bounds__(kThreads) k_inv_cols(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
+                                                       const PrimeConst *__restrict__ pc, int logn, int limb_begin,
+                                                       int limb_count)
+{
+    constexpr int S = 1 << LOGS, T = S / kE, C = kThreads / T;
+    __shared__ uint64_t sm[S * C];
+    const int n2 = 1 << (logn - LOGS);
+    const int tiles = n2 / C;
+    const size_t pl = blockIdx.x / tiles;
+    const int col0 = (blockIdx.x % tiles) * C;
+    const int prime = limb_begin + (int)(pl % (size_t)limb_count);
+    const PrimeConst P = pc[prime];
+    const uint64_t q = P.q, q2 = q << 1;
+    const ulonglong2 *W = tw + ((size_t)prime << logn);
+    uint64_t *p = data + (pl << logn) + col0;
+    const int c = threadIdx.x % C, t = threadIdx.x / C;
+
+    uint64_t x[kE];
+#pragma unroll
+    for (int k = 0; k < kE; ++k) x[k] = p[(size_t)(kE * t + k) * n2 + c];
+    inv_regs_blocked<T>(x, W, 1, t, q, q2);
+#pragma unroll
+    for (int k = 0; k < kE; ++k) sm[(kE * t + k) * C + c] = x[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kE; ++k) x[k] = sm[(t + T * k) * C + c];
+    inv_regs_strided(x, W, 1, q, q2);
+#pragma unroll
+    for (int k = 0; k < kE; ++k) p[(size_t)(t + T * k) * n2 + c] = mul_shoup(x[k], P.inv_n, P.inv_n_q, q);
+}
+
+template <int L1, int L2>
+void launch_fwd(const Context &c, uint64_t *d, size_t n_polys, int lb, int lc, cudaStream_t s)
+{
+    const size_t limbs = n_polys * (size_t)lc;
+    constexpr int C = kThreads / ((1 << L1) / kE);
+    constexpr int R = kThreads / ((1 << L2) / kE);
+    const unsigned g1 = (unsigned)(limbs * ((1u << L2) / C));
+    const unsigned g2 = (unsigned)(limbs * ((1u << L1) / R));
+    k_fwd_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lb, lc);
+    k_fwd_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lb, lc);
+}
+
+template <int L1, int L2>
+void launch_inv(const Context &c, uint64_t *d, size_t n_polys, int lb, int lc, cudaStream_t s)
+{
+    const size_t limbs = n_polys * (size_t)lc;
+    constexpr int C = kThreads / ((1 << L1) / kE);
+    constexpr int R = kThreads / ((1 << L2) / kE);
+    const unsigned g1 = (unsigned)(limbs * ((1u << L2) / C));
+    const unsigned g2 = (unsigned)(limbs * ((1u << L1) / R));
+    k_inv_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lb, lc);
+    k_inv_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lb, lc);
+}
+
+}  // namespace
+
+void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, int limb_begin, int limb_end, cudaStream_t s)
+{
+    const int lc = limb_end - limb_begin;
+    if (n_polys == 0 || lc == 0) return;
+    switch (c.logn) {
+    case 12: launch_fwd<6, 6>(c, d, n_polys, limb_begin, lc, s); break;
+    case 13: launch_fwd<6, 7>(c, d, n_polys, limb_begin, lc, s); break;
+    case 14: launch_fwd<7, 7>(c, d, n_polys, limb_begin, lc, s); break;
+    case 15: launch_fwd<7, 8>(c, d, n_polys, limb_begin, lc, s); break;
+    case 16: launch_fwd<8, 8>(c, d, n_polys, limb_begin, lc, s); break;
+    default: throw std::invalid_argument("unsupported log_n");
+    }
+}
+
+void ntt_inverse(const Context &c, uint64_t *d, size_t n_polys, int limb_begin, int limb_end, cudaStream_t s)
+{
+    const int lc = limb_end - limb_begin;
+    if (n_polys == 0 || lc == 0) return;
+    switch (c.logn) {
+    case 12: launch_inv<6, 6>(c, d, n_polys, limb_begin, lc, s); break;
+    case 13: launch_inv<6, 7>(c, d, n_polys, limb_begin, lc, s); break;
+    case 14: launch_inv<7, 7>(c, d, n_polys, limb_begin, lc, s); break;
+    case 15: launch_inv<7, 8>(c, d, n_polys, limb_begin, lc, s); break;
+    case 16: launch_inv<8, 8>(c, d, n_polys, limb_begin, lc, s); break;
+    default: throw std::invalid_argument("unsupported log_n");
+    }
+}
+
+}  // namespace nexus

@@ -1,0 +1,44 @@
+"""The C ABI library loads without a GPU and exports every declared symbol."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions():
+    names = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*[A-Za-z_][\w\s\*]*?\b(nexus_\w+)\s*\(", text, flags=re.M):
+            names.append(m.group(1))
+    return sorted(set(names))
+
+
+def test_headers_declare_entry_points():
+    names = declared_functions()
+    assert "nexus_ntt_forward" in names and "nexus_context_create" in names
+
+
+def test_library_exports_every_declared_symbol():
+    from nexus_gb300 import _lib
+    lib = _lib.lib()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    bound = {name for name, _, _ in _lib.SIGNATURES}
+    assert set(declared_functions()) <= bound, set(declared_functions()) - bound
+
+
+def test_context_rejects_bad_arguments_without_gpu():
+    # argument validation happens before any CUDA call
+    from nexus_gb300 import _lib
+    lib = _lib.lib()
+    h = ctypes.c_void_p()
+    arr = (ctypes.c_uint64 * 2)(3, 5)
+    assert lib.nexus_context_create(5, arr, 2, ctypes.byref(h)) != 0
+    assert b"log_n" in lib.nexus_last_error()
+    assert lib.nexus_ntt_forward(None, None, 1, 0, 1, None) != 0
+    assert b"null" in lib.nexus_last_error()
