@@ -263,6 +263,7 @@ def max_over_ranks(v: float, world: int) -> float:
 
 
 def main():
+    global NTT_CTS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -270,11 +271,10 @@ def main():
     ap.add_argument("--impl", choices=["nexus", "reference"], default="nexus")
     ap.add_argument("--workload", choices=["ntt"], default="ntt")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--ntt-cts", type=int, default=NTT_CTS,
+    ap.add_argument("--ntt-cts", type=int, default=64,
                     help="ciphertexts per step (smaller values are for profiling captures only)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
-    global NTT_CTS
     NTT_CTS = args.ntt_cts
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

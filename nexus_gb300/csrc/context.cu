@@ -8,6 +8,12 @@
 
 #include "context.h"
 
+#define CK(call)                                                                      \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e_));      \
+    } while (0)
+
 namespace nexus {
 
 typedef unsigned __int128 u128;
@@ -89,6 +95,40 @@ static uint32_t bitrev(uint32_t x, int bits)
     return r;
 }
 
+uint64_t *Context::get_scratch(size_t words)
+{
+    if (words > scratch_words) {
+        // growing frees the old arena, which synchronises with pending work
+        if (scratch) CK(cudaFree(scratch));
+        scratch = nullptr;
+        scratch_words = 0;
+        CK(cudaMalloc(&scratch, words * sizeof(uint64_t)));
+        scratch_words = words;
+    }
+    return scratch;
+}
+
+// GaloisTool::generate_table_ntt (util/galois.cpp:18-52): slot i of the
+// permuted polynomial reads slot table[i] of the input.
+const uint32_t *Context::galois_table(uint32_t elt)
+{
+    auto it = galois_tables.find(elt);
+    if (it != galois_tables.end()) return it->second;
+    if (!(elt & 1) || elt >= 2 * n) throw std::invalid_argument("Galois element is not valid");
+    std::vector<uint32_t> t(n);
+    const uint32_t mask = (uint32_t)n - 1;
+    for (uint64_t i = n; i < 2 * n; ++i) {
+        uint32_t rev = bitrev((uint32_t)i, logn + 1);
+        uint64_t raw = ((uint64_t)elt * rev) >> 1;
+        t[i - n] = bitrev((uint32_t)(raw & mask), logn);
+    }
+    uint32_t *d = nullptr;
+    CK(cudaMalloc(&d, sizeof(uint32_t) * n));
+    CK(cudaMemcpy(d, t.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+    galois_tables[elt] = d;
+    return d;
+}
+
 static thread_local std::string g_last_error;
 void set_error(const std::string &msg) { g_last_error = msg; }
 
@@ -97,12 +137,6 @@ void set_error(const std::string &msg) { g_last_error = msg; }
 using namespace nexus;
 
 extern "C" const char *nexus_last_error(void) { return nexus::g_last_error.c_str(); }
-
-#define CK(call)                                                                      \
-    do {                                                                              \
-        cudaError_t e_ = (call);                                                      \
-        if (e_ != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e_));      \
-    } while (0)
 
 extern "C" int nexus_context_create(int log_n, const uint64_t *moduli, int n_moduli, nexus_context **out)
 {
@@ -160,6 +194,15 @@ extern "C" int nexus_context_create(int log_n, const uint64_t *moduli, int n_mod
             pc.inv_n_q = host_shoup(pc.inv_n, q);
             c.pc.push_back(pc);
         }
+        c.inv_q.assign((size_t)n_moduli * n_moduli, make_ulonglong2(0, 0));
+        for (int a = 0; a < n_moduli; ++a)
+            for (int b = 0; b < n_moduli; ++b)
+                if (a != b) {
+                    uint64_t v = host_invmod(c.q[a] % c.q[b], c.q[b]);
+                    c.inv_q[(size_t)a * n_moduli + b] = make_ulonglong2(v, host_shoup(v, c.q[b]));
+                }
+        CK(cudaMalloc(&c.d_inv_q, sizeof(ulonglong2) * c.inv_q.size()));
+        CK(cudaMemcpy(c.d_inv_q, c.inv_q.data(), sizeof(ulonglong2) * c.inv_q.size(), cudaMemcpyHostToDevice));
         CK(cudaMalloc(&c.d_pc, sizeof(PrimeConst) * n_moduli));
         CK(cudaMemcpy(c.d_pc, c.pc.data(), sizeof(PrimeConst) * n_moduli, cudaMemcpyHostToDevice));
         CK(cudaMalloc(&c.d_tw_fwd, sizeof(ulonglong2) * fwd.size()));
@@ -171,6 +214,7 @@ extern "C" int nexus_context_create(int log_n, const uint64_t *moduli, int n_mod
         cudaFree(c.d_pc);
         cudaFree(c.d_tw_fwd);
         cudaFree(c.d_tw_inv);
+        cudaFree(c.d_inv_q);
         delete h;
         return -1;
     }
@@ -184,6 +228,9 @@ extern "C" int nexus_context_destroy(nexus_context *h)
     cudaFree(h->c.d_pc);
     cudaFree(h->c.d_tw_fwd);
     cudaFree(h->c.d_tw_inv);
+    cudaFree(h->c.d_inv_q);
+    cudaFree(h->c.scratch);
+    for (auto &kv : h->c.galois_tables) cudaFree(kv.second);
     delete h;
     return 0;
 }

@@ -8,6 +8,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <map>
 #include <vector>
 #include <cuda_runtime.h>
 
@@ -34,6 +35,22 @@ struct Context {
 
     // Split of the two-pass NTT: n = n1 * n2 (rows x columns).
     int log_n1 = 0, log_n2 = 0;
+
+    // inv_q[a*k + b] = {q_a^{-1} mod q_b, Shoup quotient} (0 on the diagonal);
+    // rescale divides by q_{l-1}, ModDown by the special prime q_{k-1}.
+    ulonglong2 *d_inv_q = nullptr;   // [k][k]
+    std::vector<ulonglong2> inv_q;   // host copy
+
+    // Galois permutation tables in the NTT domain, one per element, built on
+    // first use (GaloisTool::generate_table_ntt, util/galois.cpp:18-52).
+    std::map<uint32_t, uint32_t *> galois_tables;
+
+    // Scratch arena reused by every multi-kernel operation; operations on one
+    // context are stream-ordered and must not run concurrently.
+    uint64_t *scratch = nullptr;
+    size_t scratch_words = 0;
+    uint64_t *get_scratch(size_t words);
+    const uint32_t *galois_table(uint32_t elt);
 };
 
 // Host helpers shared by the translation units.

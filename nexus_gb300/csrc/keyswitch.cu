@@ -1,0 +1,154 @@
+// Key switching with one special prime and one digit per data prime, the
+// decomposition of SEAL's Evaluator::switch_key_inplace (evaluator.cpp:2724-3022
+// in SEAL-4.1-bs), so the output words equal SEAL's.
+//
+//   1. INTT of the target's l limbs (coefficient form, each in [0, q_j)).
+//   2. ModUp: digit j is reduced into every prime of {q_0..q_{l-1}, p} and
+//      transformed: D[j][i] = NTT_i(t_j mod q_i).  (For i == j this equals the
+//      target limb SEAL reuses.)
+//   3. Inner product with the key, 128-bit accumulation, one Barrett
+//      reduction: P[k][i] = sum_j D[j][i] * key[j][k][i] mod q_i.
+//   4. ModDown with rounding: ct[k][i] += (P[k][i] - NTT_i(((INTT_p(P[k][p]) + p/2)
+//      mod p) - p/2)) * p^{-1} mod q_i.
+#include <stdexcept>
+
+#include "context.h"
+#include "ntt.h"
+#include "ops.h"
+
+namespace nexus {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+inline unsigned grid_for(size_t n)
+{
+    size_t g = (n + kBlock - 1) / kBlock;
+    return (unsigned)(g > 1048576 ? 1048576 : g);
+}
+
+// D[j][i'][n] = t[j][n] mod q(i') for i' in [0, l], q(l) = special prime
+__global__ void k_modup_spread(const uint64_t *__restrict__ t, uint64_t *__restrict__ D,
+                               const PrimeConst *__restrict__ pc, int l, int sp, int logn, size_t total)
+{
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(x >> logn);
+        const size_t n = x & (((size_t)1 << logn) - 1);
+        const uint64_t v = t[x];
+        const uint64_t qj = pc[j].q;
+        uint64_t *o = D + ((size_t)j * (l + 1) << logn) + n;
+        for (int i = 0; i <= l; ++i) {
+            const PrimeConst P = pc[i == l ? sp : i];
+            o[(size_t)i << logn] = (P.q < qj) ? barrett_64(v, P.q, P.r1) : v;
+        }
+    }
+}
+
+__device__ __forceinline__ void mac128(uint64_t &lo, uint64_t &hi, uint64_t a, uint64_t b)
+{
+    asm("mad.lo.cc.u64 %0, %2, %3, %0;\n\tmadc.hi.u64 %1, %2, %3, %1;" : "+l"(lo), "+l"(hi) : "l"(a), "l"(b));
+}
+
+// P[k][i'][n] = sum_j D[j][i'][n] * key[j][k][kidx(i')][n] mod q(i')
+__global__ void k_ks_inner(const uint64_t *__restrict__ D, const uint64_t *__restrict__ key, uint64_t *__restrict__ P,
+                           const PrimeConst *__restrict__ pc, int l, int K, int logn, size_t total)
+{
+    const size_t N = (size_t)1 << logn;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(x >> logn);  // 0..l
+        const size_t n = x & (N - 1);
+        const int kidx = (i == l) ? K - 1 : i;
+        const PrimeConst P0 = pc[kidx];
+        uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
+        const uint64_t *d = D + ((size_t)i << logn) + n;
+        const uint64_t *k0 = key + ((size_t)kidx << logn) + n;
+        const size_t dstride = (size_t)(l + 1) << logn;
+        const size_t kstride = (size_t)2 * K << logn;
+        const size_t kcomp = (size_t)K << logn;
+        for (int j = 0; j < l; ++j) {
+            const uint64_t dv = d[j * dstride];
+            mac128(lo0, hi0, dv, k0[j * kstride]);
+            mac128(lo1, hi1, dv, k0[j * kstride + kcomp]);
+        }
+        P[((size_t)i << logn) + n] = barrett_128(lo0, hi0, P0.q, P0.r0, P0.r1);
+        P[((size_t)(l + 1 + i) << logn) + n] = barrett_128(lo1, hi1, P0.q, P0.r0, P0.r1);
+    }
+}
+
+// ct[k][i] += (P[k][i] - T[k][i]) * p^{-1} mod q_i ; T[k][i] in [0, q_i)
+__global__ void k_moddown_finish(uint64_t *__restrict__ ct, const uint64_t *__restrict__ P,
+                                 const uint64_t *__restrict__ T, const PrimeConst *__restrict__ pc,
+                                 const ulonglong2 *__restrict__ inv_p, int l, int logn, size_t total)
+{
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = x >> logn;             // k*l + i
+        const size_t n = x & (((size_t)1 << logn) - 1);
+        const int k = (int)(row / l), i = (int)(row % l);
+        const uint64_t q = pc[i].q;
+        const ulonglong2 w = inv_p[i];
+        const uint64_t pv = P[(((size_t)k * (l + 1) + i) << logn) + n];
+        const uint64_t v = mul_shoup(pv + q - T[x], w.x, w.y, q);
+        ct[x] = csub(ct[x] + v, q);
+    }
+}
+
+}  // namespace
+
+void switch_key(Context &c, uint64_t *ct, int l, const uint64_t *target, const uint64_t *key, cudaStream_t s)
+{
+    if (l < 1 || l > c.k - 1) throw std::invalid_argument("switch_key: level out of range");
+    const size_t N = c.n;
+    const int sp = c.k - 1;
+    // scratch: t[l] | D[l][l+1] | P[2][l+1] | T[2][l] | last[2]
+    const size_t words = N * ((size_t)l + (size_t)l * (l + 1) + 2 * (size_t)(l + 1) + 2 * (size_t)l + 2);
+    uint64_t *t = c.get_scratch(words);
+    uint64_t *D = t + (size_t)l * N;
+    uint64_t *P = D + (size_t)l * (l + 1) * N;
+    uint64_t *T = P + 2 * (size_t)(l + 1) * N;
+    uint64_t *last = T + 2 * (size_t)l * N;
+
+    cudaMemcpyAsync(t, target, sizeof(uint64_t) * l * N, cudaMemcpyDeviceToDevice, s);
+    ntt_inverse(c, t, 1, LimbMap{l, 0, -1}, s);
+    size_t tot = (size_t)l * N;
+    k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot);
+    ntt_forward(c, D, l, LimbMap{l + 1, 0, sp}, s);
+    tot = (size_t)(l + 1) * N;
+    k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, tot);
+    // ModDown: special limbs of both components to coefficient form
+    cudaMemcpyAsync(last, P + (size_t)l * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(last + N, P + (size_t)(2 * l + 1) * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
+    ntt_inverse(c, last, 2, LimbMap{1, sp, -1}, s);
+    launch_round_spread(c, last, T, 2, sp, l, s);
+    ntt_forward(c, T, 2, LimbMap{l, 0, -1}, s);
+    tot = (size_t)2 * l * N;
+    k_moddown_finish<<<grid_for(tot), kBlock, 0, s>>>(ct, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn, tot);
+}
+
+void relinearize(Context &c, const uint64_t *ct3, int l, const uint64_t *key, uint64_t *out2, cudaStream_t s)
+{
+    const size_t N = c.n;
+    // the c2 input must survive until the key switch has read it
+    uint64_t *c2 = nullptr;
+    if (cudaMallocAsync(&c2, sizeof(uint64_t) * l * N, s) != cudaSuccess) throw std::runtime_error("cudaMallocAsync");
+    cudaMemcpyAsync(c2, ct3 + (size_t)2 * l * N, sizeof(uint64_t) * l * N, cudaMemcpyDeviceToDevice, s);
+    if (out2 != ct3) cudaMemcpyAsync(out2, ct3, sizeof(uint64_t) * 2 * l * N, cudaMemcpyDeviceToDevice, s);
+    switch_key(c, out2, l, c2, key, s);
+    cudaFreeAsync(c2, s);
+}
+
+void apply_galois(Context &c, const uint64_t *ct, int l, uint32_t elt, const uint64_t *key, uint64_t *out,
+                  cudaStream_t s)
+{
+    const size_t N = c.n;
+    uint64_t *tmp = nullptr;
+    if (cudaMallocAsync(&tmp, sizeof(uint64_t) * 2 * l * N, s) != cudaSuccess)
+        throw std::runtime_error("cudaMallocAsync");
+    galois_permute(c, ct, 2, l, elt, tmp, s);
+    cudaMemcpyAsync(out, tmp, sizeof(uint64_t) * l * N, cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(out + (size_t)l * N, 0, sizeof(uint64_t) * l * N, s);
+    switch_key(c, out, l, tmp + (size_t)l * N, key, s);
+    cudaFreeAsync(tmp, s);
+}
+
+}  // namespace nexus

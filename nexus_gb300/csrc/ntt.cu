@@ -124,8 +124,7 @@ __device__ __forceinline__ int swz(int s) { return s + (s >> 4); }
 // Pass 1: size-2^LOGS transforms down the columns.  Output stays in [0,4q).
 template <int LOGS>
 __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
-                                                       const PrimeConst *__restrict__ pc, int logn, int limb_begin,
-                                                       int limb_count)
+                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
 {
     constexpr int S = 1 << LOGS, T = S / kE, C = kThreads / T;
     __shared__ uint64_t sm[S * C];
@@ -133,7 +132,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
     const int tiles = n2 / C;
     const size_t pl = blockIdx.x / tiles;
     const int col0 = (blockIdx.x % tiles) * C;
-    const int prime = limb_begin + (int)(pl % (size_t)limb_count);
+    const int prime = lm.prime((int)(pl % (size_t)lm.count));
     const uint64_t q = pc[prime].q, q2 = q << 1;
     const ulonglong2 *W = tw + ((size_t)prime << logn);
     uint64_t *p = data + (pl << logn) + col0;
@@ -157,8 +156,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
 // reduction [0,4q) -> [0,q).
 template <int LOGS>
 __global__ void __launch_bounds__(kThreads) k_fwd_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
-                                                       const PrimeConst *__restrict__ pc, int logn, int limb_begin,
-                                                       int limb_count)
+                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
 {
     constexpr int S = 1 << LOGS, T = S / kE, R = kThreads / T, SP = S + S / 16;
     __shared__ uint64_t sm[R * SP];
@@ -167,7 +165,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_rows(uint64_t *__restrict__ da
     const size_t grow = (size_t)blockIdx.x * R + rr;
     const size_t pl = grow >> log_n1;
     const uint64_t r = grow & ((1u << log_n1) - 1);
-    const int prime = limb_begin + (int)(pl % (size_t)limb_count);
+    const int prime = lm.prime((int)(pl % (size_t)lm.count));
     const uint64_t q = pc[prime].q, q2 = q << 1;
     const ulonglong2 *W = tw + ((size_t)prime << logn);
     uint64_t *p = data + grow * S;
@@ -196,8 +194,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_rows(uint64_t *__restrict__ da
 // Inverse pass A: rows first (undoing pass 2).  Output in [0,2q).
 template <int LOGS>
 __global__ void __launch_bounds__(kThreads) k_inv_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
-                                                       const PrimeConst *__restrict__ pc, int logn, int limb_begin,
-                                                       int limb_count)
+                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
 {
     constexpr int S = 1 << LOGS, T = S / kE, R = kThreads / T, SP = S + S / 16;
     __shared__ uint64_t sm[R * SP];
@@ -206,7 +203,7 @@ __global__ void __launch_bounds__(kThreads) k_inv_rows(uint64_t *__restrict__ da
     const size_t grow = (size_t)blockIdx.x * R + rr;
     const size_t pl = grow >> log_n1;
     const uint64_t r = grow & ((1u << log_n1) - 1);
-    const int prime = limb_begin + (int)(pl % (size_t)limb_count);
+    const int prime = lm.prime((int)(pl % (size_t)lm.count));
     const uint64_t q = pc[prime].q, q2 = q << 1;
     const ulonglong2 *W = tw + ((size_t)prime << logn);
     uint64_t *p = data + grow * S;
@@ -233,8 +230,7 @@ __global__ void __launch_bounds__(kThreads) k_inv_rows(uint64_t *__restrict__ da
 // Inverse pass B: columns (undoing pass 1), then n^{-1} and reduction to [0,q).
 template <int LOGS>
 __global__ void __launch_bounds__(kThreads) k_inv_cols(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
-                                                       const PrimeConst *__restrict__ pc, int logn, int limb_begin,
-                                                       int limb_count)
+                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
 {
     constexpr int S = 1 << LOGS, T = S / kE, C = kThreads / T;
     __shared__ uint64_t sm[S * C];
@@ -242,7 +238,7 @@ __global__ void __launch_bounds__(kThreads) k_inv_cols(uint64_t *__restrict__ da
     const int tiles = n2 / C;
     const size_t pl = blockIdx.x / tiles;
     const int col0 = (blockIdx.x % tiles) * C;
-    const int prime = limb_begin + (int)(pl % (size_t)limb_count);
+    const int prime = lm.prime((int)(pl % (size_t)lm.count));
     const PrimeConst P = pc[prime];
     const uint64_t q = P.q, q2 = q << 1;
     const ulonglong2 *W = tw + ((size_t)prime << logn);
@@ -264,57 +260,65 @@ __global__ void __launch_bounds__(kThreads) k_inv_cols(uint64_t *__restrict__ da
 }
 
 template <int L1, int L2>
-void launch_fwd(const Context &c, uint64_t *d, size_t n_polys, int lb, int lc, cudaStream_t s)
+void launch_fwd(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s)
 {
-    const size_t limbs = n_polys * (size_t)lc;
+    const size_t limbs = n_polys * (size_t)lm.count;
     constexpr int C = kThreads / ((1 << L1) / kE);
     constexpr int R = kThreads / ((1 << L2) / kE);
     const unsigned g1 = (unsigned)(limbs * ((1u << L2) / C));
     const unsigned g2 = (unsigned)(limbs * ((1u << L1) / R));
-    k_fwd_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lb, lc);
-    k_fwd_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lb, lc);
+    k_fwd_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm);
+    k_fwd_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm);
 }
 
 template <int L1, int L2>
-void launch_inv(const Context &c, uint64_t *d, size_t n_polys, int lb, int lc, cudaStream_t s)
+void launch_inv(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s)
 {
-    const size_t limbs = n_polys * (size_t)lc;
+    const size_t limbs = n_polys * (size_t)lm.count;
     constexpr int C = kThreads / ((1 << L1) / kE);
     constexpr int R = kThreads / ((1 << L2) / kE);
     const unsigned g1 = (unsigned)(limbs * ((1u << L2) / C));
     const unsigned g2 = (unsigned)(limbs * ((1u << L1) / R));
-    k_inv_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lb, lc);
-    k_inv_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lb, lc);
+    k_inv_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lm);
+    k_inv_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lm);
 }
 
 }  // namespace
 
-void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, int limb_begin, int limb_end, cudaStream_t s)
+void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s)
 {
-    const int lc = limb_end - limb_begin;
-    if (n_polys == 0 || lc == 0) return;
+    if (n_polys == 0 || lm.count == 0) return;
     switch (c.logn) {
-    case 12: launch_fwd<6, 6>(c, d, n_polys, limb_begin, lc, s); break;
-    case 13: launch_fwd<6, 7>(c, d, n_polys, limb_begin, lc, s); break;
-    case 14: launch_fwd<7, 7>(c, d, n_polys, limb_begin, lc, s); break;
-    case 15: launch_fwd<7, 8>(c, d, n_polys, limb_begin, lc, s); break;
-    case 16: launch_fwd<8, 8>(c, d, n_polys, limb_begin, lc, s); break;
+    case 12: launch_fwd<6, 6>(c, d, n_polys, lm, s); break;
+    case 13: launch_fwd<6, 7>(c, d, n_polys, lm, s); break;
+    case 14: launch_fwd<7, 7>(c, d, n_polys, lm, s); break;
+    case 15: launch_fwd<7, 8>(c, d, n_polys, lm, s); break;
+    case 16: launch_fwd<8, 8>(c, d, n_polys, lm, s); break;
     default: throw std::invalid_argument("unsupported log_n");
     }
 }
 
-void ntt_inverse(const Context &c, uint64_t *d, size_t n_polys, int limb_begin, int limb_end, cudaStream_t s)
+void ntt_inverse(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s)
 {
-    const int lc = limb_end - limb_begin;
-    if (n_polys == 0 || lc == 0) return;
+    if (n_polys == 0 || lm.count == 0) return;
     switch (c.logn) {
-    case 12: launch_inv<6, 6>(c, d, n_polys, limb_begin, lc, s); break;
-    case 13: launch_inv<6, 7>(c, d, n_polys, limb_begin, lc, s); break;
-    case 14: launch_inv<7, 7>(c, d, n_polys, limb_begin, lc, s); break;
-    case 15: launch_inv<7, 8>(c, d, n_polys, limb_begin, lc, s); break;
-    case 16: launch_inv<8, 8>(c, d, n_polys, limb_begin, lc, s); break;
+    case 12: launch_inv<6, 6>(c, d, n_polys, lm, s); break;
+    case 13: launch_inv<6, 7>(c, d, n_polys, lm, s); break;
+    case 14: launch_inv<7, 7>(c, d, n_polys, lm, s); break;
+    case 15: launch_inv<7, 8>(c, d, n_polys, lm, s); break;
+    case 16: launch_inv<8, 8>(c, d, n_polys, lm, s); break;
     default: throw std::invalid_argument("unsupported log_n");
     }
+}
+
+void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, int limb_begin, int limb_end, cudaStream_t s)
+{
+    ntt_forward(c, d, n_polys, LimbMap{limb_end - limb_begin, limb_begin, -1}, s);
+}
+
+void ntt_inverse(const Context &c, uint64_t *d, size_t n_polys, int limb_begin, int limb_end, cudaStream_t s)
+{
+    ntt_inverse(c, d, n_polys, LimbMap{limb_end - limb_begin, limb_begin, -1}, s);
 }
 
 }  // namespace nexus

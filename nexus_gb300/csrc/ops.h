@@ -1,0 +1,50 @@
+// Internal CKKS operations on device arrays in SEAL's layout.  A ciphertext
+// with `limbs` limbs uses data primes 0..limbs-1; polynomials are [limbs][N],
+// ciphertexts [size][limbs][N], key-switching keys [K-1][2][K][N] with
+// K = ctx.k (every prime of the key level).  All functions only enqueue work
+// on `s`; multi-kernel operations share the context's scratch arena.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "context.h"
+
+namespace nexus {
+
+// element-wise, over [polys][limbs][N]
+void poly_add(const Context &c, const uint64_t *a, const uint64_t *b, int polys, int limbs, uint64_t *out,
+              cudaStream_t s);
+void poly_sub(const Context &c, const uint64_t *a, const uint64_t *b, int polys, int limbs, uint64_t *out,
+              cudaStream_t s);
+void poly_negate(const Context &c, const uint64_t *a, int polys, int limbs, uint64_t *out, cudaStream_t s);
+// out[p] = ct[p] * pt for every polynomial p of ct (pt is one [limbs][N] polynomial)
+void poly_mul_plain(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *pt, uint64_t *out,
+                    cudaStream_t s);
+// out[p] = ct[p] + pt (pt broadcast); used for add_plain
+void poly_add_plain(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *pt, int sub,
+                    uint64_t *out, cudaStream_t s);
+// out[p][l] = ct[p][l] * scalar[l] mod q_l (per-limb scalar from host)
+void poly_mul_scalar(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *scalars,
+                     uint64_t *out, cudaStream_t s);
+
+// ckks_multiply / ckks_square tensor: out3 = (a0 b0, a0 b1 + a1 b0, a1 b1)
+void tensor(const Context &c, const uint64_t *a, const uint64_t *b, int limbs, uint64_t *out3, cudaStream_t s);
+
+// divide_and_round_q_last_ntt over every polynomial: [size][limbs] -> [size][limbs-1]
+void rescale(const Context &c, const uint64_t *in, int size, int limbs, uint64_t *out, cudaStream_t s);
+
+// NTT-domain automorphism of [polys][limbs][N]
+void galois_permute(Context &c, const uint64_t *in, int polys, int limbs, uint32_t elt, uint64_t *out,
+                    cudaStream_t s);
+
+// switch_key_inplace: ct[2][limbs] += key-switch(target[limbs])
+void switch_key(Context &c, uint64_t *ct, int limbs, const uint64_t *target, const uint64_t *key, cudaStream_t s);
+
+// relinearize a size-3 ciphertext into out2 (may alias ct3)
+void relinearize(Context &c, const uint64_t *ct3, int limbs, const uint64_t *key, uint64_t *out2, cudaStream_t s);
+
+// apply_galois_inplace: permute both polynomials, key-switch the second
+void apply_galois(Context &c, const uint64_t *ct, int limbs, uint32_t elt, const uint64_t *key, uint64_t *out,
+                  cudaStream_t s);
+
+}  // namespace nexus

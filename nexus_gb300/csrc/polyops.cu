@@ -1,0 +1,287 @@
+// Element-wise RNS kernels, rescale and the NTT-domain automorphism.
+//
+// Every result is the fully reduced residue SEAL produces for the same
+// operation (references are to the SEAL-4.1-bs tree bundled with NEXUS).
+#include <stdexcept>
+
+#include "context.h"
+#include "ntt.h"
+#include "ops.h"
+
+namespace nexus {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+inline unsigned grid_for(size_t pairs)
+{
+    size_t g = (pairs + kBlock - 1) / kBlock;
+    return (unsigned)(g > 1048576 ? 1048576 : g);
+}
+
+// Iterate residue pairs (2 consecutive coefficients of one limb) over
+// [rows][N]; `limb` is the limb index of the row within its polynomial.
+#define FOR_PAIRS(total_pairs)                                                            \
+    for (size_t pi = (size_t)blockIdx.x * blockDim.x + threadIdx.x; pi < (total_pairs);  \
+         pi += (size_t)gridDim.x * blockDim.x)
+
+__device__ __forceinline__ uint64_t add_mod(uint64_t a, uint64_t b, uint64_t q) { return csub(a + b, q); }
+__device__ __forceinline__ uint64_t sub_mod(uint64_t a, uint64_t b, uint64_t q) { return csub(a + q - b, q); }
+
+__global__ void k_add_sub(const ulonglong2 *__restrict__ a, const ulonglong2 *__restrict__ b, ulonglong2 *out,
+                          const PrimeConst *__restrict__ pc, int limbs, int logn, size_t pairs, int sub)
+{
+    FOR_PAIRS(pairs)
+    {
+        const int limb = (int)((pi >> (logn - 1)) % (size_t)limbs);
+        const uint64_t q = pc[limb].q;
+        ulonglong2 x = a[pi], y = b[pi];
+        if (sub) {
+            x.x = sub_mod(x.x, y.x, q);
+            x.y = sub_mod(x.y, y.y, q);
+        } else {
+            x.x = add_mod(x.x, y.x, q);
+            x.y = add_mod(x.y, y.y, q);
+        }
+        out[pi] = x;
+    }
+}
+
+__global__ void k_negate(const ulonglong2 *__restrict__ a, ulonglong2 *out, const PrimeConst *__restrict__ pc,
+                         int limbs, int logn, size_t pairs)
+{
+    FOR_PAIRS(pairs)
+    {
+        const int limb = (int)((pi >> (logn - 1)) % (size_t)limbs);
+        const uint64_t q = pc[limb].q;
+        ulonglong2 x = a[pi];
+        x.x = x.x ? q - x.x : 0;
+        x.y = x.y ? q - x.y : 0;
+        out[pi] = x;
+    }
+}
+
+// out[p][l] = ct[p][l] (*|+|-) pt[l]
+__global__ void k_plain(const ulonglong2 *__restrict__ ct, const ulonglong2 *__restrict__ pt, ulonglong2 *out,
+                        const PrimeConst *__restrict__ pc, int limbs, int logn, size_t pairs, int op)
+{
+    const size_t pt_pairs = ((size_t)limbs << logn) >> 1;
+    FOR_PAIRS(pairs)
+    {
+        const int limb = (int)((pi >> (logn - 1)) % (size_t)limbs);
+        const PrimeConst P = pc[limb];
+        ulonglong2 x = ct[pi], y = pt[pi % pt_pairs];
+        if (op == 0) {
+            x.x = mul_mod(x.x, y.x, P.q, P.r0, P.r1);
+            x.y = mul_mod(x.y, y.y, P.q, P.r0, P.r1);
+        } else if (op == 1) {
+            x.x = add_mod(x.x, y.x, P.q);
+            x.y = add_mod(x.y, y.y, P.q);
+        } else {
+            x.x = sub_mod(x.x, y.x, P.q);
+            x.y = sub_mod(x.y, y.y, P.q);
+        }
+        out[pi] = x;
+    }
+}
+
+struct LimbScalars {
+    ulonglong2 w[64];  // {scalar mod q_l, Shoup quotient}
+};
+
+__global__ void k_mul_scalar(const ulonglong2 *__restrict__ ct, const LimbScalars sc, ulonglong2 *out,
+                             const PrimeConst *__restrict__ pc, int limbs, int logn, size_t pairs)
+{
+    FOR_PAIRS(pairs)
+    {
+        const int limb = (int)((pi >> (logn - 1)) % (size_t)limbs);
+        const uint64_t q = pc[limb].q;
+        const ulonglong2 w = sc.w[limb];
+        ulonglong2 x = ct[pi];
+        x.x = mul_shoup(x.x, w.x, w.y, q);
+        x.y = mul_shoup(x.y, w.x, w.y, q);
+        out[pi] = x;
+    }
+}
+
+// ckks_multiply (evaluator.cpp:770-850): out3 = (a0 b0, a0 b1 + a1 b0, a1 b1)
+__global__ void k_tensor(const ulonglong2 *__restrict__ a, const ulonglong2 *__restrict__ b, ulonglong2 *out,
+                         const PrimeConst *__restrict__ pc, int limbs, int logn)
+{
+    const size_t poly_pairs = ((size_t)limbs << logn) >> 1;
+    FOR_PAIRS(poly_pairs)
+    {
+        const int limb = (int)(pi >> (logn - 1));
+        const PrimeConst P = pc[limb];
+        const ulonglong2 x0 = a[pi], x1 = a[pi + poly_pairs], y0 = b[pi], y1 = b[pi + poly_pairs];
+        ulonglong2 o0, o1, o2;
+        o0.x = mul_mod(x0.x, y0.x, P.q, P.r0, P.r1);
+        o0.y = mul_mod(x0.y, y0.y, P.q, P.r0, P.r1);
+        o2.x = mul_mod(x1.x, y1.x, P.q, P.r0, P.r1);
+        o2.y = mul_mod(x1.y, y1.y, P.q, P.r0, P.r1);
+        o1.x = add_mod(mul_mod(x0.x, y1.x, P.q, P.r0, P.r1), mul_mod(x1.x, y0.x, P.q, P.r0, P.r1), P.q);
+        o1.y = add_mod(mul_mod(x0.y, y1.y, P.q, P.r0, P.r1), mul_mod(x1.y, y0.y, P.q, P.r0, P.r1), P.q);
+        out[pi] = o0;
+        out[pi + poly_pairs] = o1;
+        out[pi + 2 * poly_pairs] = o2;
+    }
+}
+
+// copy limb `which` of each of `polys` polynomials ([polys][limbs][N]) into dst[polys][N]
+__global__ void k_gather_limb(const ulonglong2 *__restrict__ src, ulonglong2 *dst, int limbs, int which, int logn,
+                              size_t pairs)
+{
+    const size_t half = (size_t)1 << (logn - 1);
+    FOR_PAIRS(pairs)
+    {
+        const size_t p = pi / half, i = pi % half;
+        dst[pi] = src[(p * limbs + which) * half + i];
+    }
+}
+
+// From the inverse-transformed dropped limb x (in [0, q_last)), build for every
+// remaining prime q_i the value ((x + h) mod q_last) mod q_i + (q_i - h mod q_i)
+// with h = floor(q_last / 2): the rounding correction of
+// divide_and_round_q_last_ntt_inplace (util/rns.cpp:857-884) and of the
+// ModDown step of switch_key_inplace (evaluator.cpp:2966-2985).
+__global__ void k_round_spread(const uint64_t *__restrict__ last, uint64_t *__restrict__ out,
+                               const PrimeConst *__restrict__ pc, int last_prime, int out_limbs, int logn,
+                               size_t total)
+{
+    const uint64_t ql = pc[last_prime].q, h = ql >> 1;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t p = t >> logn, n = t & (((size_t)1 << logn) - 1);
+        const uint64_t x = csub(last[t] + h, ql);
+        uint64_t *o = out + (p * out_limbs << logn) + n;
+        for (int i = 0; i < out_limbs; ++i) {
+            const PrimeConst P = pc[i];
+            const uint64_t xr = (P.q < ql) ? barrett_64(x, P.q, P.r1) : x;
+            const uint64_t hr = (P.q < ql) ? barrett_64(h, P.q, P.r1) : h;
+            o[(size_t)i << logn] = xr + (P.q - hr);
+        }
+    }
+}
+
+// out[p][i] = (in[p][i] - t[p][i]) * q_last^{-1} mod q_i   (t in [0, q_i))
+__global__ void k_rescale_finish(const ulonglong2 *__restrict__ in, const ulonglong2 *__restrict__ t,
+                                 ulonglong2 *out, const PrimeConst *__restrict__ pc,
+                                 const ulonglong2 *__restrict__ inv_row, int limbs, int logn, size_t pairs)
+{
+    const size_t half = (size_t)1 << (logn - 1);
+    const int ol = limbs - 1;
+    FOR_PAIRS(pairs)
+    {
+        const size_t row = pi / half, i = pi % half;
+        const size_t p = row / ol;
+        const int l = (int)(row % ol);
+        const uint64_t q = pc[l].q;
+        const ulonglong2 w = inv_row[l];
+        const ulonglong2 x = in[(p * limbs + l) * half + i], y = t[pi];
+        ulonglong2 r;
+        r.x = mul_shoup(x.x + q - y.x, w.x, w.y, q);
+        r.y = mul_shoup(x.y + q - y.y, w.x, w.y, q);
+        out[pi] = r;
+    }
+}
+
+__global__ void k_permute(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
+                          const uint32_t *__restrict__ tab, int logn, size_t total)
+{
+    const size_t mask = ((size_t)1 << logn) - 1;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t base = t & ~mask;
+        out[t] = in[base + tab[t & mask]];
+    }
+}
+
+}  // namespace
+
+static size_t pairs_of(const Context &c, int polys, int limbs) { return ((size_t)polys * limbs * c.n) >> 1; }
+
+void poly_add(const Context &c, const uint64_t *a, const uint64_t *b, int polys, int limbs, uint64_t *out,
+              cudaStream_t s)
+{
+    size_t pr = pairs_of(c, polys, limbs);
+    k_add_sub<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)a, (const ulonglong2 *)b, (ulonglong2 *)out, c.d_pc,
+                                               limbs, c.logn, pr, 0);
+}
+
+void poly_sub(const Context &c, const uint64_t *a, const uint64_t *b, int polys, int limbs, uint64_t *out,
+              cudaStream_t s)
+{
+    size_t pr = pairs_of(c, polys, limbs);
+    k_add_sub<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)a, (const ulonglong2 *)b, (ulonglong2 *)out, c.d_pc,
+                                               limbs, c.logn, pr, 1);
+}
+
+void poly_negate(const Context &c, const uint64_t *a, int polys, int limbs, uint64_t *out, cudaStream_t s)
+{
+    size_t pr = pairs_of(c, polys, limbs);
+    k_negate<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)a, (ulonglong2 *)out, c.d_pc, limbs, c.logn, pr);
+}
+
+void poly_mul_plain(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *pt, uint64_t *out,
+                    cudaStream_t s)
+{
+    size_t pr = pairs_of(c, polys, limbs);
+    k_plain<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)ct, (const ulonglong2 *)pt, (ulonglong2 *)out, c.d_pc,
+                                             limbs, c.logn, pr, 0);
+}
+
+void poly_add_plain(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *pt, int sub,
+                    uint64_t *out, cudaStream_t s)
+{
+    size_t pr = pairs_of(c, polys, limbs);
+    k_plain<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)ct, (const ulonglong2 *)pt, (ulonglong2 *)out, c.d_pc,
+                                             limbs, c.logn, pr, sub ? 2 : 1);
+}
+
+void poly_mul_scalar(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *scalars,
+                     uint64_t *out, cudaStream_t s)
+{
+    // host scalars (already reduced mod q_l) travel as a kernel parameter
+    if (limbs > 64) throw std::invalid_argument("at most 64 limbs");
+    LimbScalars w;
+    for (int l = 0; l < limbs; ++l) w.w[l] = make_ulonglong2(scalars[l], host_shoup(scalars[l], c.q[l]));
+    size_t pr = pairs_of(c, polys, limbs);
+    k_mul_scalar<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)ct, w, (ulonglong2 *)out, c.d_pc, limbs, c.logn,
+                                                  pr);
+}
+
+void tensor(const Context &c, const uint64_t *a, const uint64_t *b, int limbs, uint64_t *out3, cudaStream_t s)
+{
+    size_t pr = pairs_of(c, 1, limbs);
+    k_tensor<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)a, (const ulonglong2 *)b, (ulonglong2 *)out3, c.d_pc,
+                                              limbs, c.logn);
+}
+
+void rescale(const Context &c_in, const uint64_t *in, int size, int limbs, uint64_t *out, cudaStream_t s)
+{
+    if (limbs < 2) throw std::invalid_argument("rescale needs at least two limbs");
+    Context &c = const_cast<Context &>(c_in);
+    const size_t n = c.n;
+    uint64_t *last = c.get_scratch((size_t)size * n * limbs);
+    uint64_t *t = last + (size_t)size * n;
+    size_t pr = ((size_t)size * n) >> 1;
+    k_gather_limb<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, (ulonglong2 *)last, limbs, limbs - 1, c.logn,
+                                                   pr);
+    ntt_inverse(c, last, size, LimbMap{1, limbs - 1, -1}, s);
+    size_t tot = (size_t)size * n;
+    k_round_spread<<<grid_for(tot), kBlock, 0, s>>>(last, t, c.d_pc, limbs - 1, limbs - 1, c.logn, tot);
+    ntt_forward(c, t, size, LimbMap{limbs - 1, 0, -1}, s);
+    pr = pairs_of(c, size, limbs - 1);
+    k_rescale_finish<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, (const ulonglong2 *)t, (ulonglong2 *)out,
+                                                      c.d_pc, c.d_inv_q + (size_t)(limbs - 1) * c.k, limbs, c.logn,
+                                                      pr);
+}
+
+void galois_permute(Context &c, const uint64_t *in, int polys, int limbs, uint32_t elt, uint64_t *out,
+                    cudaStream_t s)
+{
+    const uint32_t *tab = c.galois_table(elt);
+    size_t tot = (size_t)polys * limbs * c.n;
+    k_permute<<<grid_for(tot), kBlock, 0, s>>>(in, out, tab, c.logn, tot);
+}
+
+}  // namespace nexus

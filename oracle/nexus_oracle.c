@@ -560,7 +560,7 @@ void or_galois_table_ntt(int logn, uint32_t elt, uint32_t *out)
     }
 }
 
-/* GaloisTool::get_elt_from_step (util/galois.cpp:53-90), generator 3 */
+/* GaloisTool::get_elt_from_step (util/galois.cpp:53-90); the generator is 5 (util/galois.h:169) */
 uint32_t or_galois_elt_from_step(int logn, int step)
 {
     uint32_t n = 1u << logn;
@@ -571,7 +571,7 @@ uint32_t or_galois_elt_from_step(int logn, int step)
     pos &= (uint32_t)(m - 1);
     int s = neg ? (int)(n >> 1) - (int)pos : (int)pos;
     uint64_t elt = 1;
-    while (s--) { elt *= 3; elt &= m - 1; }
+    while (s--) { elt *= 5; elt &= m - 1; }
     return (uint32_t)elt;
 }
 

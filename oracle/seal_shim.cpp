@@ -1,0 +1,317 @@
+// seal_shim.cpp -- TEST INFRASTRUCTURE.  A C ABI over the public API of the
+// SEAL-4.1-bs fork bundled with NEXUS, so the tests can run the real library
+// on the same inputs as the CPU restatement and the CUDA engine.  Built only
+// where the NEXUS sources are present (oracle/build_ref.py); the engine never
+// links it.
+//
+// Every array uses SEAL's own layout ([size][limbs][N], NTT form).
+#include <algorithm>
+#include <array>
+#include <complex>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "seal/seal.h"
+#include "seal/util/ntt.h"
+#include "seal/util/rlwe.h"
+
+using namespace seal;
+
+namespace {
+
+std::string g_err;
+
+struct Shim {
+    std::unique_ptr<SEALContext> ctx;
+    std::unique_ptr<CKKSEncoder> enc;
+    std::unique_ptr<Evaluator> ev;
+    std::unique_ptr<KeyGenerator> kg;
+    std::unique_ptr<SecretKey> sk;
+    std::unique_ptr<PublicKey> pk;
+    std::unique_ptr<RelinKeys> rk;
+    std::unique_ptr<GaloisKeys> gk;
+    std::unique_ptr<Encryptor> encryptor;
+    std::unique_ptr<Decryptor> decryptor;
+    size_t n = 0;
+    int k = 0;
+};
+
+parms_id_type pid_for_limbs(const Shim &s, int limbs)
+{
+    auto cd = s.ctx->key_context_data();
+    while (cd) {
+        if ((int)cd->parms().coeff_modulus().size() == limbs) return cd->parms_id();
+        cd = cd->next_context_data();
+    }
+    throw std::invalid_argument("no level with that many primes");
+}
+
+void load_ct(const Shim &s, Ciphertext &ct, const uint64_t *in, int size, int limbs, double scale)
+{
+    ct.resize(*s.ctx, pid_for_limbs(s, limbs), size);
+    std::memcpy(ct.data(), in, sizeof(uint64_t) * size * limbs * s.n);
+    ct.is_ntt_form() = true;
+    ct.scale() = scale;
+}
+
+void store_ct(const Shim &s, const Ciphertext &ct, uint64_t *out)
+{
+    std::memcpy(out, ct.data(), sizeof(uint64_t) * ct.size() * ct.coeff_modulus_size() * s.n);
+}
+
+void copy_kswitch(const Shim &s, const std::vector<PublicKey> &kv, uint64_t *out)
+{
+    size_t per = 2 * (size_t)s.k * s.n;
+    for (size_t j = 0; j < kv.size(); ++j) std::memcpy(out + j * per, kv[j].data().data(), sizeof(uint64_t) * per);
+}
+
+}  // namespace
+
+#define GUARD(...)                          \
+    try {                                   \
+        __VA_ARGS__;                        \
+    } catch (const std::exception &e) {     \
+        g_err = e.what();                   \
+        return -1;                          \
+    }                                       \
+    return 0;
+
+extern "C" {
+
+const char *sr_last_error() { return g_err.c_str(); }
+
+// CKKS context over explicit primes (data primes, then the special prime),
+// no security check, optional sparse secret (hamming_weight > 0), seeded
+// Blake2xb PRNG so keys and encryptions are reproducible.
+void *sr_create(int logn, const uint64_t *moduli, int k, uint64_t seed, int hamming_weight)
+{
+    try {
+        auto *s = new Shim();
+        EncryptionParameters parms(scheme_type::ckks);
+        s->n = size_t(1) << logn;
+        s->k = k;
+        parms.set_poly_modulus_degree(s->n);
+        std::vector<Modulus> mods;
+        for (int i = 0; i < k; ++i) mods.emplace_back(moduli[i]);
+        parms.set_coeff_modulus(mods);
+        if (hamming_weight > 0) parms.set_secret_key_hamming_weight(hamming_weight);
+        prng_seed_type sd{};
+        sd[0] = seed;
+        parms.set_random_generator(std::make_shared<Blake2xbPRNGFactory>(sd));
+        s->ctx.reset(new SEALContext(parms, true, sec_level_type::none));
+        if (!s->ctx->parameters_set()) throw std::invalid_argument(s->ctx->parameter_error_message());
+        s->enc.reset(new CKKSEncoder(*s->ctx));
+        s->ev.reset(new Evaluator(*s->ctx, *s->enc));
+        return s;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return nullptr;
+    }
+}
+
+void sr_destroy(void *h) { delete static_cast<Shim *>(h); }
+
+// Secret key, public key, relinearization key and Galois keys for `steps`.
+int sr_keygen(void *h, const int *steps, int nsteps)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        s.kg.reset(new KeyGenerator(*s.ctx));
+        s.sk.reset(new SecretKey(s.kg->secret_key()));
+        s.pk.reset(new PublicKey());
+        s.kg->create_public_key(*s.pk);
+        s.rk.reset(new RelinKeys());
+        s.kg->create_relin_keys(*s.rk);
+        s.gk.reset(new GaloisKeys());
+        if (nsteps > 0) s.kg->create_galois_keys(std::vector<int>(steps, steps + nsteps), *s.gk);
+        s.encryptor.reset(new Encryptor(*s.ctx, *s.pk));
+        s.decryptor.reset(new Decryptor(*s.ctx, *s.sk));
+    })
+}
+
+int sr_export_secret(void *h, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD(std::memcpy(out, s.sk->data().data(), sizeof(uint64_t) * s.k * s.n))
+}
+
+// relinearization key: [K-1][2][K][N]
+int sr_export_relin(void *h, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD(copy_kswitch(s, s.rk->key(2), out))
+}
+
+int sr_export_galois(void *h, uint32_t elt, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD(copy_kswitch(s, s.gk->key(elt), out))
+}
+
+int sr_galois_elt(void *h, int step, uint32_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD(*out = s.ctx->key_context_data()->galois_tool()->get_elt_from_step(step))
+}
+
+// ntt_negacyclic_harvey / inverse on `count` limbs of one prime
+int sr_ntt(int logn, uint64_t q, uint64_t *data, size_t count, int inverse)
+{
+    GUARD({
+        util::NTTTables t(logn, Modulus(q));
+        size_t n = size_t(1) << logn;
+        for (size_t i = 0; i < count; ++i) {
+            if (inverse) util::inverse_ntt_negacyclic_harvey(data + i * n, t);
+            else util::ntt_negacyclic_harvey(data + i * n, t);
+        }
+    })
+}
+
+int sr_rescale(void *h, const uint64_t *in, int size, int limbs, double scale, uint64_t *out, double *out_scale)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Ciphertext ct;
+        load_ct(s, ct, in, size, limbs, scale);
+        s.ev->rescale_to_next_inplace(ct);
+        store_ct(s, ct, out);
+        *out_scale = ct.scale();
+    })
+}
+
+int sr_multiply(void *h, const uint64_t *a, const uint64_t *b, int limbs, uint64_t *out3)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Ciphertext x, y;
+        load_ct(s, x, a, 2, limbs, 1.0);
+        load_ct(s, y, b, 2, limbs, 1.0);
+        s.ev->multiply_inplace(x, y);
+        store_ct(s, x, out3);
+    })
+}
+
+int sr_relinearize(void *h, const uint64_t *in3, int limbs, uint64_t *out2)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Ciphertext x;
+        load_ct(s, x, in3, 3, limbs, 1.0);
+        s.ev->relinearize_inplace(x, *s.rk);
+        store_ct(s, x, out2);
+    })
+}
+
+int sr_rotate(void *h, const uint64_t *in, int limbs, int step, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Ciphertext x;
+        load_ct(s, x, in, 2, limbs, 1.0);
+        s.ev->rotate_vector_inplace(x, step, *s.gk);
+        store_ct(s, x, out);
+    })
+}
+
+int sr_conjugate(void *h, const uint64_t *in, int limbs, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Ciphertext x;
+        load_ct(s, x, in, 2, limbs, 1.0);
+        s.ev->complex_conjugate_inplace(x, *s.gk);
+        store_ct(s, x, out);
+    })
+}
+
+int sr_multiply_plain(void *h, const uint64_t *ct, int size, int limbs, const uint64_t *pt, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Ciphertext x;
+        load_ct(s, x, ct, size, limbs, 1.0);
+        Plaintext p;
+        p.parms_id() = parms_id_zero;
+        p.resize(s.n * limbs);
+        std::memcpy(p.data(), pt, sizeof(uint64_t) * s.n * limbs);
+        p.parms_id() = pid_for_limbs(s, limbs);
+        p.scale() = 1.0;
+        s.ev->multiply_plain_inplace(x, p);
+        store_ct(s, x, out);
+    })
+}
+
+// CKKSEncoder::encode of n complex values (re, im) at `scale` for a level
+// with `limbs` primes; writes [limbs][N].
+int sr_encode(void *h, const double *re, const double *im, size_t nvals, double scale, int limbs, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        std::vector<std::complex<double>> v(nvals);
+        for (size_t i = 0; i < nvals; ++i) v[i] = {re[i], im ? im[i] : 0.0};
+        Plaintext p;
+        s.enc->encode(v, pid_for_limbs(s, limbs), scale, p);
+        std::memcpy(out, p.data(), sizeof(uint64_t) * s.n * limbs);
+    })
+}
+
+// CKKSEncoder::encode(double) -- the scalar path
+int sr_encode_scalar(void *h, double value, double scale, int limbs, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Plaintext p;
+        s.enc->encode(value, pid_for_limbs(s, limbs), scale, p);
+        std::memcpy(out, p.data(), sizeof(uint64_t) * s.n * limbs);
+    })
+}
+
+// decode of a plaintext [limbs][N] into nvals complex values
+int sr_decode(void *h, const uint64_t *pt, int limbs, double scale, double *re, double *im, size_t nvals)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Plaintext p;
+        p.resize(s.n * limbs);
+        std::memcpy(p.data(), pt, sizeof(uint64_t) * s.n * limbs);
+        p.parms_id() = pid_for_limbs(s, limbs);
+        p.scale() = scale;
+        std::vector<std::complex<double>> v;
+        s.enc->decode(p, v);
+        for (size_t i = 0; i < nvals && i < v.size(); ++i) {
+            re[i] = v[i].real();
+            if (im) im[i] = v[i].imag();
+        }
+    })
+}
+
+int sr_encrypt(void *h, const double *vals, size_t nvals, double scale, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        std::vector<double> v(vals, vals + nvals);
+        Plaintext p;
+        s.enc->encode(v, scale, p);
+        Ciphertext c;
+        s.encryptor->encrypt(p, c);
+        store_ct(s, c, out);
+    })
+}
+
+int sr_decrypt(void *h, const uint64_t *ct, int limbs, double scale, double *out, size_t nvals)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Ciphertext c;
+        load_ct(s, c, ct, 2, limbs, scale);
+        Plaintext p;
+        s.decryptor->decrypt(c, p);
+        std::vector<double> v;
+        s.enc->decode(p, v);
+        for (size_t i = 0; i < nvals && i < v.size(); ++i) out[i] = v[i];
+    })
+}
+
+}  // extern "C"
