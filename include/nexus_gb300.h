@@ -71,6 +71,80 @@ int nexus_ntt_forward(nexus_context *ctx, uint64_t *d_data, size_t n_polys, int 
 int nexus_ntt_inverse(nexus_context *ctx, uint64_t *d_data, size_t n_polys, int limb_begin, int limb_end,
                       void *stream);
 
+/* ------------------------------------------------------------------ */
+/* CKKS ciphertext arithmetic (NTT form, limbs = data primes 0..limbs-1) */
+/* ------------------------------------------------------------------ */
+
+/*
+ * Tensor product of two size-2 ciphertexts a, b [2][limbs][N] into the
+ * size-3 ciphertext out3 [3][limbs][N] (no relinearization).
+ * Replaces: Evaluator::multiply_inplace -> ckks_multiply
+ *   (native/src/seal/evaluator.cpp:770-850); Phantom tensor_prod_2x2_rns_poly
+ *   (cuda/thirdparty/phantom-fhe/src/polymath.cu:468).
+ */
+int nexus_multiply(nexus_context *ctx, const uint64_t *d_a, const uint64_t *d_b, int limbs, uint64_t *d_out3,
+                   void *stream);
+
+/*
+ * Rescale: divide every polynomial of d_in [size][limbs][N] by the last prime
+ * with rounding; d_out is [size][limbs-1][N] and must not overlap d_in.
+ * Replaces: Evaluator::rescale_to_next -> RNSTool::divide_and_round_q_last_ntt_inplace
+ *   (native/src/seal/evaluator.cpp:1682, util/rns.cpp:830-905); Phantom
+ *   rescale_to_next (cuda/thirdparty/phantom-fhe/src/rns.cu:1157).
+ */
+int nexus_rescale(nexus_context *ctx, const uint64_t *d_in, int size, int limbs, uint64_t *d_out, void *stream);
+
+/*
+ * Key switching: d_ct [2][limbs][N] += switch(d_target [limbs][N]) under the
+ * key-switching key d_key [n_moduli-1][2][n_moduli][N] (SEAL's KSwitchKeys
+ * layout: one PublicKey per data prime at the key level).
+ * Replaces: Evaluator::switch_key_inplace (native/src/seal/evaluator.cpp:2724-3022);
+ *   Phantom keyswitch_inplace (cuda/thirdparty/phantom-fhe/src/eval_key_switch.cu:93).
+ */
+int nexus_switch_key(nexus_context *ctx, uint64_t *d_ct, int limbs, const uint64_t *d_target, const uint64_t *d_key,
+                     void *stream);
+
+/*
+ * Relinearize the size-3 ciphertext d_ct3 into d_out2 [2][limbs][N]
+ * (d_out2 may equal d_ct3).
+ * Replaces: Evaluator::relinearize_inplace -> relinearize_internal
+ *   (native/src/seal/evaluator.cpp:1345-1400).
+ */
+int nexus_relinearize(nexus_context *ctx, const uint64_t *d_ct3, int limbs, const uint64_t *d_relin_key,
+                      uint64_t *d_out2, void *stream);
+
+/*
+ * Apply the automorphism X -> X^galois_elt and switch back to the secret key.
+ * Replaces: Evaluator::apply_galois_inplace (native/src/seal/evaluator.cpp:2563-2665);
+ *   rotate_vector / complex_conjugate use it with the element of a step.
+ */
+int nexus_apply_galois(nexus_context *ctx, const uint64_t *d_ct, int limbs, uint32_t galois_elt,
+                       const uint64_t *d_galois_key, uint64_t *d_out, void *stream);
+
+/*
+ * Galois element of a slot rotation by `step` (0 = complex conjugation).
+ * Replaces: GaloisTool::get_elt_from_step (native/src/seal/util/galois.cpp:53-90).
+ */
+int nexus_galois_elt_from_step(int log_n, int step, uint32_t *out);
+
+/* out = a + b / a - b / -a over [polys][limbs][N].
+ * Replaces: Evaluator::add_inplace / sub_inplace / negate_inplace
+ *   (native/src/seal/evaluator.cpp:155, 263, 130). */
+int nexus_add(nexus_context *ctx, const uint64_t *d_a, const uint64_t *d_b, int polys, int limbs, uint64_t *d_out,
+              void *stream);
+int nexus_sub(nexus_context *ctx, const uint64_t *d_a, const uint64_t *d_b, int polys, int limbs, uint64_t *d_out,
+              void *stream);
+int nexus_negate(nexus_context *ctx, const uint64_t *d_a, int polys, int limbs, uint64_t *d_out, void *stream);
+
+/* Every polynomial of d_ct [size][limbs][N] times (op 0), plus (op 1) or minus
+ * (op 2) the plaintext d_pt [limbs][N].
+ * Replaces: Evaluator::multiply_plain_inplace -> multiply_plain_ntt
+ *   (native/src/seal/evaluator.cpp:2154, 2336-2373), add_plain_inplace (:1938),
+ *   sub_plain_inplace (:2046); the plaintext is added to component 0 only,
+ *   so callers pass size = 1 for op 1 and 2. */
+int nexus_plain_op(nexus_context *ctx, const uint64_t *d_ct, int size, int limbs, const uint64_t *d_pt, int op,
+                   uint64_t *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -65,3 +65,46 @@ class Context:
         n_polys = t.numel() // ((limb_end - limb_begin) * self.n)
         check(lib().nexus_ntt_inverse(self._h, t.data_ptr(), n_polys, limb_begin, limb_end, _stream_ptr(stream)),
               "nexus_ntt_inverse")
+
+    # ---- ciphertext arithmetic on device tensors (SEAL layout) -----------
+    def multiply(self, a, b, out3, stream=None):
+        check(lib().nexus_multiply(self._h, a.data_ptr(), b.data_ptr(), a.shape[-2], out3.data_ptr(),
+                                   _stream_ptr(stream)), "nexus_multiply")
+
+    def rescale(self, ct, out, stream=None):
+        size, limbs = ct.shape[0], ct.shape[1]
+        check(lib().nexus_rescale(self._h, ct.data_ptr(), size, limbs, out.data_ptr(), _stream_ptr(stream)),
+              "nexus_rescale")
+
+    def switch_key(self, ct, target, key, stream=None):
+        check(lib().nexus_switch_key(self._h, ct.data_ptr(), ct.shape[1], target.data_ptr(), key.data_ptr(),
+                                     _stream_ptr(stream)), "nexus_switch_key")
+
+    def relinearize(self, ct3, key, out2, stream=None):
+        check(lib().nexus_relinearize(self._h, ct3.data_ptr(), ct3.shape[1], key.data_ptr(), out2.data_ptr(),
+                                      _stream_ptr(stream)), "nexus_relinearize")
+
+    def apply_galois(self, ct, elt, key, out, stream=None):
+        check(lib().nexus_apply_galois(self._h, ct.data_ptr(), ct.shape[1], int(elt), key.data_ptr(),
+                                       out.data_ptr(), _stream_ptr(stream)), "nexus_apply_galois")
+
+    def galois_elt(self, step: int) -> int:
+        e = C.c_uint32()
+        check(lib().nexus_galois_elt_from_step(self.log_n, int(step), C.byref(e)), "galois_elt")
+        return e.value
+
+    def add(self, a, b, out, stream=None):
+        check(lib().nexus_add(self._h, a.data_ptr(), b.data_ptr(), a.shape[0], a.shape[1], out.data_ptr(),
+                              _stream_ptr(stream)), "nexus_add")
+
+    def sub(self, a, b, out, stream=None):
+        check(lib().nexus_sub(self._h, a.data_ptr(), b.data_ptr(), a.shape[0], a.shape[1], out.data_ptr(),
+                              _stream_ptr(stream)), "nexus_sub")
+
+    def negate(self, a, out, stream=None):
+        check(lib().nexus_negate(self._h, a.data_ptr(), a.shape[0], a.shape[1], out.data_ptr(), _stream_ptr(stream)),
+              "nexus_negate")
+
+    def plain_op(self, ct, pt, op: int, out, stream=None):
+        check(lib().nexus_plain_op(self._h, ct.data_ptr(), ct.shape[0], ct.shape[1], pt.data_ptr(), op,
+                                   out.data_ptr(), _stream_ptr(stream)), "nexus_plain_op")

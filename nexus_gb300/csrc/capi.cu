@@ -7,6 +7,7 @@
 #include "../../include/nexus_gb300.h"
 #include "context.h"
 #include "ntt.h"
+#include "ops.h"
 
 using namespace nexus;
 
@@ -58,4 +59,135 @@ extern "C" int nexus_ntt_inverse(nexus_context *ctx, uint64_t *d_data, size_t n_
         return fail(fn, e.what());
     }
     return check_launch(fn);
+}
+
+namespace {
+
+int check_ct(const char *fn, const nexus_context *ctx, int limbs, int min_limbs = 1)
+{
+    if (!ctx) return fail(fn, "null context");
+    if (limbs < min_limbs || limbs > ctx->c.k - 1)
+        return fail(fn, "limbs must be in [" + std::to_string(min_limbs) + ", n_moduli-1]");
+    return 0;
+}
+
+template <class F>
+int guarded(const char *fn, F &&f)
+{
+    try {
+        f();
+    } catch (const std::exception &e) {
+        return fail(fn, e.what());
+    }
+    return check_launch(fn);
+}
+
+}  // namespace
+
+extern "C" int nexus_multiply(nexus_context *ctx, const uint64_t *a, const uint64_t *b, int limbs, uint64_t *out3,
+                              void *stream)
+{
+    static const char *fn = "nexus_multiply";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!a || !b || !out3) return fail(fn, "null argument");
+    return guarded(fn, [&] { tensor(ctx->c, a, b, limbs, out3, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_rescale(nexus_context *ctx, const uint64_t *in, int size, int limbs, uint64_t *out, void *stream)
+{
+    static const char *fn = "nexus_rescale";
+    if (check_ct(fn, ctx, limbs, 2)) return -1;
+    if (!in || !out || size < 1) return fail(fn, "null argument or size < 1");
+    const size_t n = ctx->c.n;
+    if (out < in + (size_t)size * limbs * n && in < out + (size_t)size * (limbs - 1) * n)
+        return fail(fn, "d_out must not overlap d_in");
+    return guarded(fn, [&] { rescale(ctx->c, in, size, limbs, out, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_switch_key(nexus_context *ctx, uint64_t *ct, int limbs, const uint64_t *target,
+                                const uint64_t *key, void *stream)
+{
+    static const char *fn = "nexus_switch_key";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!ct || !target || !key) return fail(fn, "null argument");
+    return guarded(fn, [&] { switch_key(ctx->c, ct, limbs, target, key, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_relinearize(nexus_context *ctx, const uint64_t *ct3, int limbs, const uint64_t *key,
+                                 uint64_t *out2, void *stream)
+{
+    static const char *fn = "nexus_relinearize";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!ct3 || !key || !out2) return fail(fn, "null argument");
+    return guarded(fn, [&] { relinearize(ctx->c, ct3, limbs, key, out2, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_apply_galois(nexus_context *ctx, const uint64_t *ct, int limbs, uint32_t elt, const uint64_t *key,
+                                  uint64_t *out, void *stream)
+{
+    static const char *fn = "nexus_apply_galois";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!ct || !key || !out) return fail(fn, "null argument");
+    if (!(elt & 1) || elt >= 2 * ctx->c.n) return fail(fn, "Galois element is not valid");
+    return guarded(fn, [&] { apply_galois(ctx->c, ct, limbs, elt, key, out, (cudaStream_t)stream); });
+}
+
+// GaloisTool::get_elt_from_step (util/galois.cpp:53-90), generator 5
+extern "C" int nexus_galois_elt_from_step(int log_n, int step, uint32_t *out)
+{
+    static const char *fn = "nexus_galois_elt_from_step";
+    if (!out || log_n < 1 || log_n > 17) return fail(fn, "bad arguments");
+    const uint32_t n = 1u << log_n;
+    const uint64_t m = 2ull * n;
+    if (step == 0) {
+        *out = (uint32_t)(m - 1);
+        return 0;
+    }
+    const bool neg = step < 0;
+    uint32_t pos = (uint32_t)(neg ? -(int64_t)step : step);
+    if (pos >= (n >> 1)) return fail(fn, "step count too large");
+    int e = neg ? (int)(n >> 1) - (int)pos : (int)pos;
+    uint64_t g = 1;
+    while (e--) g = (g * 5) & (m - 1);
+    *out = (uint32_t)g;
+    return 0;
+}
+
+extern "C" int nexus_add(nexus_context *ctx, const uint64_t *a, const uint64_t *b, int polys, int limbs, uint64_t *out,
+                         void *stream)
+{
+    static const char *fn = "nexus_add";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!a || !b || !out || polys < 1) return fail(fn, "null argument");
+    return guarded(fn, [&] { poly_add(ctx->c, a, b, polys, limbs, out, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_sub(nexus_context *ctx, const uint64_t *a, const uint64_t *b, int polys, int limbs, uint64_t *out,
+                         void *stream)
+{
+    static const char *fn = "nexus_sub";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!a || !b || !out || polys < 1) return fail(fn, "null argument");
+    return guarded(fn, [&] { poly_sub(ctx->c, a, b, polys, limbs, out, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_negate(nexus_context *ctx, const uint64_t *a, int polys, int limbs, uint64_t *out, void *stream)
+{
+    static const char *fn = "nexus_negate";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!a || !out || polys < 1) return fail(fn, "null argument");
+    return guarded(fn, [&] { poly_negate(ctx->c, a, polys, limbs, out, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_plain_op(nexus_context *ctx, const uint64_t *ct, int size, int limbs, const uint64_t *pt, int op,
+                              uint64_t *out, void *stream)
+{
+    static const char *fn = "nexus_plain_op";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!ct || !pt || !out || size < 1) return fail(fn, "null argument");
+    if (op < 0 || op > 2) return fail(fn, "op must be 0 (multiply), 1 (add) or 2 (sub)");
+    return guarded(fn, [&] {
+        if (op == 0) poly_mul_plain(ctx->c, ct, size, limbs, pt, out, (cudaStream_t)stream);
+        else poly_add_plain(ctx->c, ct, size, limbs, pt, op == 2, out, (cudaStream_t)stream);
+    });
 }

@@ -276,6 +276,13 @@ void rescale(const Context &c_in, const uint64_t *in, int size, int limbs, uint6
                                                       pr);
 }
 
+void launch_round_spread(const Context &c, const uint64_t *last, uint64_t *out, int polys, int last_prime,
+                         int out_limbs, cudaStream_t s)
+{
+    size_t tot = (size_t)polys * c.n;
+    k_round_spread<<<grid_for(tot), kBlock, 0, s>>>(last, out, c.d_pc, last_prime, out_limbs, c.logn, tot);
+}
+
 void galois_permute(Context &c, const uint64_t *in, int polys, int limbs, uint32_t elt, uint64_t *out,
                     cudaStream_t s)
 {
