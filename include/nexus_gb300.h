@@ -145,6 +145,50 @@ int nexus_negate(nexus_context *ctx, const uint64_t *d_a, int polys, int limbs, 
 int nexus_plain_op(nexus_context *ctx, const uint64_t *d_ct, int size, int limbs, const uint64_t *d_pt, int op,
                    uint64_t *d_out, void *stream);
 
+/* ------------------------------------------------------------------ */
+/* CKKS encoding                                                        */
+/* ------------------------------------------------------------------ */
+
+/*
+ * Encode nvals (<= N/2) complex slot values (re[i] + i*im[i]; im may be NULL)
+ * at `scale` into the NTT-form plaintext d_out [limbs][N].  The FP64 special
+ * FFT runs on the host and reproduces SEAL's rounding; the RNS forward NTT
+ * runs on the GPU.  Returns after d_out is written.
+ * Replaces: CKKSEncoder::encode(vector<complex<double>>, parms_id, scale, Plaintext&)
+ *   -> encode_internal (native/src/seal/ckks.h:457-640); Phantom
+ *   PhantomCKKSEncoder::encode (cuda/thirdparty/phantom-fhe/src/ckks.cu:89).
+ */
+int nexus_encode(nexus_context *ctx, const double *re, const double *im, size_t nvals, double scale, int limbs,
+                 uint64_t *d_out, void *stream);
+
+/*
+ * Residues of round(value * scale) in each of the first `limbs` primes
+ * (host array per_limb[limbs]).  In NTT form SEAL's scalar plaintext holds this
+ * residue in every coefficient, so multiplying by it is a per-limb scalar
+ * product (nexus_multiply_scalar).
+ * Replaces: CKKSEncoder::encode(double, parms_id, scale, Plaintext&)
+ *   (native/src/seal/ckks.cpp:75-205).
+ */
+int nexus_encode_scalar(nexus_context *ctx, double value, double scale, int limbs, uint64_t *per_limb);
+
+/*
+ * d_out [polys][limbs][N] = d_in * per_limb[l] mod q_l (host scalars < q_l).
+ * Replaces: multiply_plain with a scalar-encoded plaintext
+ *   (native/src/seal/evaluator.cpp:2336-2373 with a constant plaintext).
+ */
+int nexus_multiply_scalar(nexus_context *ctx, const uint64_t *d_in, int polys, int limbs, const uint64_t *per_limb,
+                          uint64_t *d_out, void *stream);
+
+/*
+ * Decode the NTT-form plaintext d_pt [limbs][N] at `scale` into nvals slot
+ * values (re, im host arrays; im may be NULL).  sparse_slots = 0 decodes all
+ * N/2 slots; otherwise coefficients outside the sparse subring are zeroed as
+ * in the bootstrapping fork of SEAL.
+ * Replaces: CKKSEncoder::decode -> decode_internal (native/src/seal/ckks.h:640-760).
+ */
+int nexus_decode(nexus_context *ctx, const uint64_t *d_pt, int limbs, double scale, double *re, double *im,
+                 size_t nvals, size_t sparse_slots, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,6 +32,12 @@ SIGNATURES = [
     ("nexus_add", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     ("nexus_sub", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     ("nexus_negate", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    ("nexus_encode", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_double, C.c_int, C.c_void_p,
+                               C.c_void_p]),
+    ("nexus_encode_scalar", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, u64p]),
+    ("nexus_multiply_scalar", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, u64p, C.c_void_p, C.c_void_p]),
+    ("nexus_decode", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_size_t,
+                               C.c_size_t, C.c_void_p]),
     ("nexus_plain_op", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
 ]

@@ -24,6 +24,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
     "--expt-relaxed-constexpr", "-I", str(ROOT / "include"), "-I", str(CSRC),
+    # host FP64 (the CKKS encoder FFT) must not be contracted into FMAs: SEAL's
+    # rounding is reproduced operation by operation
+    "-Xcompiler", "-ffp-contract=off",
 ]
 
 

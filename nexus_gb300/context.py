@@ -108,3 +108,31 @@ class Context:
     def plain_op(self, ct, pt, op: int, out, stream=None):
         check(lib().nexus_plain_op(self._h, ct.data_ptr(), ct.shape[0], ct.shape[1], pt.data_ptr(), op,
                                    out.data_ptr(), _stream_ptr(stream)), "nexus_plain_op")
+
+    # ---- encoding ----------------------------------------------------------
+    def encode(self, values, scale: float, limbs: int, out, stream=None):
+        v = np.asarray(values)
+        re = np.ascontiguousarray(v.real, dtype=np.float64)
+        im = np.ascontiguousarray(v.imag, dtype=np.float64) if np.iscomplexobj(v) else None
+        check(lib().nexus_encode(self._h, re.ctypes.data, None if im is None else im.ctypes.data, re.size,
+                                 float(scale), limbs, out.data_ptr(), _stream_ptr(stream)), "nexus_encode")
+
+    def encode_scalar(self, value: float, scale: float, limbs: int) -> np.ndarray:
+        out = np.zeros(limbs, dtype=np.uint64)
+        check(lib().nexus_encode_scalar(self._h, float(value), float(scale), limbs,
+                                        out.ctypes.data_as(C.POINTER(C.c_uint64))), "nexus_encode_scalar")
+        return out
+
+    def multiply_scalar(self, ct, per_limb, out, stream=None):
+        pl = np.ascontiguousarray(per_limb, dtype=np.uint64)
+        check(lib().nexus_multiply_scalar(self._h, ct.data_ptr(), ct.shape[0], ct.shape[1],
+                                          pl.ctypes.data_as(C.POINTER(C.c_uint64)), out.data_ptr(),
+                                          _stream_ptr(stream)), "nexus_multiply_scalar")
+
+    def decode(self, pt, scale: float, nvals: int | None = None, sparse_slots: int = 0, stream=None):
+        nvals = nvals or self.n // 2
+        re = np.zeros(nvals)
+        im = np.zeros(nvals)
+        check(lib().nexus_decode(self._h, pt.data_ptr(), pt.shape[-2], float(scale), re.ctypes.data, im.ctypes.data,
+                                 nvals, sparse_slots, _stream_ptr(stream)), "nexus_decode")
+        return re + 1j * im

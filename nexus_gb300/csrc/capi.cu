@@ -8,6 +8,10 @@
 #include "context.h"
 #include "ntt.h"
 #include "ops.h"
+#include "encoder.h"
+
+#include <complex>
+#include <vector>
 
 using namespace nexus;
 
@@ -189,5 +193,86 @@ extern "C" int nexus_plain_op(nexus_context *ctx, const uint64_t *ct, int size, 
     return guarded(fn, [&] {
         if (op == 0) poly_mul_plain(ctx->c, ct, size, limbs, pt, out, (cudaStream_t)stream);
         else poly_add_plain(ctx->c, ct, size, limbs, pt, op == 2, out, (cudaStream_t)stream);
+    });
+}
+
+namespace {
+
+Encoder &encoder_of(nexus_context *ctx)
+{
+    if (!ctx->enc) ctx->enc = new Encoder(ctx->c);
+    return *ctx->enc;
+}
+
+}  // namespace
+
+extern "C" int nexus_encode(nexus_context *ctx, const double *re, const double *im, size_t nvals, double scale,
+                            int limbs, uint64_t *d_out, void *stream)
+{
+    static const char *fn = "nexus_encode";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if ((!re && nvals) || !d_out) return fail(fn, "null argument");
+    return guarded(fn, [&] {
+        Encoder &e = encoder_of(ctx);
+        std::vector<std::complex<double>> v(nvals);
+        for (size_t i = 0; i < nvals; ++i) v[i] = {re[i], im ? im[i] : 0.0};
+        std::vector<uint64_t> host((size_t)limbs * ctx->c.n);
+        e.encode(v.data(), nvals, scale, limbs, host.data());
+        cudaStream_t s = (cudaStream_t)stream;
+        if (cudaMemcpyAsync(d_out, host.data(), host.size() * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+            throw std::runtime_error("upload failed");
+        ntt_forward(ctx->c, d_out, 1, 0, limbs, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) throw std::runtime_error("stream synchronize failed");
+    });
+}
+
+extern "C" int nexus_encode_scalar(nexus_context *ctx, double value, double scale, int limbs, uint64_t *per_limb)
+{
+    static const char *fn = "nexus_encode_scalar";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!per_limb) return fail(fn, "null argument");
+    try {
+        encoder_of(ctx).encode_scalar(value, scale, limbs, per_limb);
+    } catch (const std::exception &e) {
+        return fail(fn, e.what());
+    }
+    return 0;
+}
+
+extern "C" int nexus_multiply_scalar(nexus_context *ctx, const uint64_t *in, int polys, int limbs,
+                                     const uint64_t *per_limb, uint64_t *out, void *stream)
+{
+    static const char *fn = "nexus_multiply_scalar";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!in || !per_limb || !out || polys < 1) return fail(fn, "null argument");
+    for (int l = 0; l < limbs; ++l)
+        if (per_limb[l] >= ctx->c.q[l]) return fail(fn, "scalar not reduced mod q_l");
+    return guarded(fn, [&] { poly_mul_scalar(ctx->c, in, polys, limbs, per_limb, out, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_decode(nexus_context *ctx, const uint64_t *d_pt, int limbs, double scale, double *re,
+                            double *im, size_t nvals, size_t sparse_slots, void *stream)
+{
+    static const char *fn = "nexus_decode";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!d_pt || !re) return fail(fn, "null argument");
+    if (scale <= 0) return fail(fn, "scale out of bounds");
+    return guarded(fn, [&] {
+        Encoder &e = encoder_of(ctx);
+        const size_t n = ctx->c.n;
+        cudaStream_t s = (cudaStream_t)stream;
+        uint64_t *tmp = ctx->c.get_scratch((size_t)limbs * n);
+        cudaMemcpyAsync(tmp, d_pt, (size_t)limbs * n * 8, cudaMemcpyDeviceToDevice, s);
+        ntt_inverse(ctx->c, tmp, 1, 0, limbs, s);
+        std::vector<uint64_t> host((size_t)limbs * n);
+        if (cudaMemcpyAsync(host.data(), tmp, host.size() * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            throw std::runtime_error("download failed");
+        std::vector<std::complex<double>> v(nvals);
+        e.decode(host.data(), limbs, scale, v.data(), nvals, sparse_slots);
+        for (size_t i = 0; i < nvals; ++i) {
+            re[i] = v[i].real();
+            if (im) im[i] = v[i].imag();
+        }
     });
 }

@@ -7,6 +7,7 @@
 #include <stdexcept>
 
 #include "context.h"
+#include "encoder.h"
 
 #define CK(call)                                                                      \
     do {                                                                              \
@@ -231,6 +232,7 @@ extern "C" int nexus_context_destroy(nexus_context *h)
     cudaFree(h->c.d_inv_q);
     cudaFree(h->c.scratch);
     for (auto &kv : h->c.galois_tables) cudaFree(kv.second);
+    delete h->enc;
     delete h;
     return 0;
 }

@@ -64,6 +64,11 @@ void set_error(const std::string &msg);
 
 }  // namespace nexus
 
+namespace nexus {
+class Encoder;
+}
+
 struct nexus_context {
     nexus::Context c;
+    nexus::Encoder *enc = nullptr;  // built on first encode/decode
 };

@@ -9,6 +9,7 @@
 
 namespace nexus {
 
+#if defined(__CUDACC__)
 // Shoup multiplication: w < q, wq = floor(w * 2^64 / q).  For any x < 2^64
 // the result is congruent to x*w mod q and lies in [0, 2q).
 __device__ __forceinline__ uint64_t mul_shoup_lazy(uint64_t x, uint64_t w, uint64_t wq, uint64_t q)
@@ -57,6 +58,8 @@ __device__ __forceinline__ uint64_t barrett_64(uint64_t x, uint64_t q, uint64_t 
     uint64_t t = __umul64hi(x, r1);
     return csub(x - t * q, q);
 }
+
+#endif  // __CUDACC__
 
 // Per-prime constants stored on the device.
 struct PrimeConst {

@@ -45,6 +45,14 @@ def main():
     rot1_low = s.rotate(np.ascontiguousarray(ct_a[:, :1]), 1)
     pt = s.encode(vp, scale, 2)
     mulplain = s.multiply_plain(ct_a, pt)
+    vc = rng.uniform(-1, 1, n // 2) + 1j * rng.uniform(-1, 1, n // 2)
+    pt_complex = s.encode(vc, 2.0 ** 35, 2)
+    pt_short = s.encode(vp[:100], 2.0 ** 20, 1)
+    scalar_vals = np.array([0.0, 1.0, -1.0, 0.5, -3.75, 1e-3, 123.456, -0.011])
+    scalar_scales = np.array([2.0 ** 30, 2.0 ** 40, 2.0 ** 45.5, 2.0 ** 20, 2.0 ** 30, 2.0 ** 50, 2.0 ** 30,
+                              2.0 ** 60])
+    scalar_pts = np.stack([s.encode_scalar(v, sc, 2)[:, 0] for v, sc in zip(scalar_vals, scalar_scales)])
+    decoded = s.decode(pt, scale)
     x = po.random_residues(rng, (2, 3, n), qs)
     ntt = np.stack([np.stack([pr.ntt(log_n, qs[j], x[p, j]) for j in range(3)]) for p in range(2)])
     out = Path(__file__).parent / "ckks_n4096.npz"
@@ -54,7 +62,17 @@ def main():
              galois_key_conj=s.galois_key(e0), galois_elts=np.array([e1, e3, e0], dtype=np.uint32),
              ct_a=ct_a, ct_b=ct_b, mul3=mul3, relin=relin, rescaled=rescaled, rot1=rot1, rotm3=rotm3,
              conj=conj, rot1_low=rot1_low, pt=pt, mulplain=mulplain, ntt_in=x, ntt_out=ntt,
-             secret_key=s.secret_key())
+             secret_key=s.secret_key(), values_c=vc, pt_complex=pt_complex, pt_short=pt_short,
+             scalar_vals=scalar_vals, scalar_scales=scalar_scales, scalar_pts=scalar_pts, decoded=decoded)
+    # one large-ring encode pins the N = 2^16 root table (2^17-th roots of unity)
+    log_n2, n2 = 16, 1 << 16
+    qs2 = po.create_coeff_modulus(n2, [60, 50, 60])
+    s2 = pr.SealRef(log_n2, qs2, seed=1)
+    v2 = np.random.default_rng(7).uniform(-1, 1, n2 // 2)
+    out2 = Path(__file__).parent / "ckks_encode_n65536.npz"
+    np.savez(out2, log_n=log_n2, moduli=np.array(qs2, dtype=np.uint64), values=v2,
+             pt=s2.encode(v2, 2.0 ** 40, 2), decoded=s2.decode(s2.encode(v2, 2.0 ** 40, 2), 2.0 ** 40))
+    print(out2, out2.stat().st_size)
     print(out, out.stat().st_size)
 
 
