@@ -105,6 +105,26 @@ int nexus_switch_key(nexus_context *ctx, uint64_t *d_ct, int limbs, const uint64
                      void *stream);
 
 /*
+ * Key switching that allocates nothing: the same operation and output words
+ * as nexus_switch_key, for callers that cannot let the library call
+ * cudaMalloc/cudaFree (their device memory is owned by another runtime's
+ * pool, or the implicit device synchronisation of an allocation is not
+ * allowed where they call).  Temporaries live in a fixed device array of
+ * 2^21 uint64 words (16 MiB) inside the library, which every GPU that loads
+ * the library holds until the process exits; requests needing more than
+ * N*(limbs^2 + 6*limbs + 4) > 2^21 words are rejected with an error.  The
+ * first call on a device looks up the array's address (cudaGetSymbolAddress)
+ * with the context's device current; make that first call before any stream
+ * capture.  All calls share the array, so calls whose work overlaps on the
+ * GPU (different streams, no ordering) race; every word is written before it
+ * is read, so no clearing is needed between calls.
+ * No counterpart in the reference: SEAL and Phantom allocate their key-switch
+ * temporaries from a memory pool on every call.
+ */
+int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *d_ct, int limbs, const uint64_t *d_target,
+                             const uint64_t *d_key, void *stream);
+
+/*
  * Relinearize the size-3 ciphertext d_ct3 into d_out2 [2][limbs][N]
  * (d_out2 may equal d_ct3).
  * Replaces: Evaluator::relinearize_inplace -> relinearize_internal

@@ -10,7 +10,9 @@
 //      reduction: P[k][i] = sum_j D[j][i] * key[j][k][i] mod q_i.
 //   4. ModDown with rounding: ct[k][i] += (P[k][i] - NTT_i(((INTT_p(P[k][p]) + p/2)
 //      mod p) - p/2)) * p^{-1} mod q_i.
+#include <mutex>
 #include <stdexcept>
+#include <string>
 
 #include "context.h"
 #include "ntt.h"
@@ -152,3 +154,104 @@ void apply_galois(Context &c, const uint64_t *ct, int l, uint32_t elt, const uin
 }
 
 }  // namespace nexus
+
+// ---------------------------------------------------------------------------
+// Key switching that allocates nothing.
+//
+// nexus_switch_key takes its temporaries from the context's scratch arena,
+// which is allocated (and regrown) with cudaMalloc/cudaFree on first use.
+// Some callers cannot allow that: a host program whose device memory is
+// entirely owned by another runtime's pool, or a serving loop in which the
+// implicit device-wide synchronisation of cudaMalloc/cudaFree would stall
+// other streams.  nexus_switch_key_noalloc gives them the same operation with
+// its temporaries in a fixed device array that is part of the library image:
+// every GPU that loads the library reserves kNoAllocWords * 8 bytes (16 MiB)
+// for it until the process exits.  The caller still passes the ciphertext,
+// the target and the key.  The array holds N * (l^2 + 6l + 4) words for
+// ring degree N and l data limbs; larger requests are rejected.
+using namespace nexus;
+
+namespace {
+
+constexpr size_t kNoAllocWords = size_t(1) << 21;
+static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocWords];
+
+std::mutex g_noalloc_mu;
+uint64_t *g_noalloc_addr[64] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (with that device current) and cached.
+uint64_t *noalloc_scratch_on_current_device()
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) throw std::runtime_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= 64) throw std::runtime_error("device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) throw std::runtime_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_noalloc_addr[dev] = static_cast<uint64_t *>(p);
+    }
+    return g_noalloc_addr[dev];
+}
+
+}  // namespace
+
+extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l, const uint64_t *target,
+                                        const uint64_t *key, void *stream)
+{
+    static const char *fn = "nexus_switch_key_noalloc";
+    if (!ctx || !ct || !target || !key) {
+        set_error(std::string(fn) + ": null argument");
+        return -1;
+    }
+    const Context &c = ctx->c;
+    if (l < 1 || l > c.k - 1) {
+        set_error(std::string(fn) + ": limbs must be in [1, n_moduli-1]");
+        return -1;
+    }
+    const size_t N = c.n;
+    const size_t words = N * ((size_t)l * l + 6 * (size_t)l + 4);
+    if (words > kNoAllocWords) {
+        set_error(std::string(fn) + ": needs " + std::to_string(words) + " scratch words (N*(l^2+6l+4)), the fixed " +
+                  "device buffer holds " + std::to_string(kNoAllocWords));
+        return -1;
+    }
+    try {
+        int dev = -1;
+        if (cudaGetDevice(&dev) != cudaSuccess || dev != c.device)
+            throw std::runtime_error("the context's device must be current");
+        uint64_t *t = noalloc_scratch_on_current_device();
+        // same layout and kernel sequence as switch_key(); every scratch word
+        // is written before it is read, so nothing needs clearing
+        cudaStream_t s = (cudaStream_t)stream;
+        const int sp = c.k - 1;
+        uint64_t *D = t + (size_t)l * N;
+        uint64_t *P = D + (size_t)l * (l + 1) * N;
+        uint64_t *T = P + 2 * (size_t)(l + 1) * N;
+        uint64_t *last = T + 2 * (size_t)l * N;
+        cudaMemcpyAsync(t, target, sizeof(uint64_t) * l * N, cudaMemcpyDeviceToDevice, s);
+        ntt_inverse(c, t, 1, LimbMap{l, 0, -1}, s);
+        size_t tot = (size_t)l * N;
+        k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot);
+        ntt_forward(c, D, l, LimbMap{l + 1, 0, sp}, s);
+        tot = (size_t)(l + 1) * N;
+        k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, tot);
+        cudaMemcpyAsync(last, P + (size_t)l * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(last + N, P + (size_t)(2 * l + 1) * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
+        ntt_inverse(c, last, 2, LimbMap{1, sp, -1}, s);
+        launch_round_spread(c, last, T, 2, sp, l, s);
+        ntt_forward(c, T, 2, LimbMap{l, 0, -1}, s);
+        tot = (size_t)2 * l * N;
+        k_moddown_finish<<<grid_for(tot), kBlock, 0, s>>>(ct, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn,
+                                                           tot);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
+    } catch (const std::exception &e) {
+        set_error(std::string(fn) + ": " + e.what());
+        return -1;
+    }
+    return 0;
+}
