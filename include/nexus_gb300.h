@@ -166,6 +166,39 @@ int nexus_plain_op(nexus_context *ctx, const uint64_t *d_ct, int size, int limbs
                    uint64_t *d_out, void *stream);
 
 /* ------------------------------------------------------------------ */
+/* Keys, encryption, decryption (test/benchmark keys: the sampler is a  */
+/* seeded counter hash, not a cryptographic generator; deployed keys are */
+/* made by the client with SEAL and imported in the same layout)         */
+/* ------------------------------------------------------------------ */
+
+/* Ternary secret key (hamming_weight > 0: exactly that many +-1
+ * coefficients, the NEXUS fork's sparse secret) in NTT form, d_sk [n_moduli][N].
+ * Replaces: KeyGenerator::generate_sk (native/src/seal/keygenerator.cpp:56). */
+int nexus_keygen_secret(nexus_context *ctx, uint64_t seed, int hamming_weight, uint64_t *d_sk, void *stream);
+
+/* Relinearization key for s^2, d_key [n_moduli-1][2][n_moduli][N].
+ * Replaces: KeyGenerator::create_relin_keys (native/src/seal/keygenerator.cpp:124)
+ *   over generate_one_kswitch_key (:303-336). */
+int nexus_keygen_relin(nexus_context *ctx, const uint64_t *d_sk, uint64_t seed, uint64_t *d_key, void *stream);
+
+/* Galois key for X -> X^galois_elt (same layout).
+ * Replaces: KeyGenerator::create_galois_keys (native/src/seal/keygenerator.cpp:164). */
+int nexus_keygen_galois(nexus_context *ctx, const uint64_t *d_sk, uint32_t galois_elt, uint64_t seed,
+                        uint64_t *d_key, void *stream);
+
+/* Symmetric encryption of the NTT-form plaintext d_pt [limbs][N] (NULL:
+ * encryption of zero) into d_ct [2][limbs][N].
+ * Replaces: Encryptor::encrypt_symmetric -> encrypt_zero_symmetric
+ *   (native/src/seal/encryptor.cpp:176, util/rlwe.cpp:311). */
+int nexus_encrypt_symmetric(nexus_context *ctx, const uint64_t *d_sk, const uint64_t *d_pt, int limbs, uint64_t seed,
+                            uint64_t *d_ct, void *stream);
+
+/* d_pt [limbs][N] = c0 + c1 s (+ c2 s^2 for size 3), NTT form.
+ * Replaces: Decryptor::decrypt (native/src/seal/decryptor.cpp:78). */
+int nexus_decrypt(nexus_context *ctx, const uint64_t *d_sk, const uint64_t *d_ct, int size, int limbs,
+                  uint64_t *d_pt, void *stream);
+
+/* ------------------------------------------------------------------ */
 /* CKKS encoding                                                        */
 /* ------------------------------------------------------------------ */
 

@@ -136,3 +136,41 @@ class Context:
         check(lib().nexus_decode(self._h, pt.data_ptr(), pt.shape[-2], float(scale), re.ctypes.data, im.ctypes.data,
                                  nvals, sparse_slots, _stream_ptr(stream)), "nexus_decode")
         return re + 1j * im
+
+    # ---- keys, encryption, decryption ---------------------------------------
+    def _empty(self, *shape):
+        import torch
+        return torch.empty(shape, dtype=torch.int64, device="cuda")
+
+    def keygen_secret(self, seed: int, hamming_weight: int = 0, stream=None):
+        sk = self._empty(len(self.moduli), self.n)
+        check(lib().nexus_keygen_secret(self._h, int(seed), int(hamming_weight), sk.data_ptr(), _stream_ptr(stream)),
+              "nexus_keygen_secret")
+        return sk
+
+    def keygen_relin(self, sk, seed: int, stream=None):
+        k = len(self.moduli)
+        key = self._empty(k - 1, 2, k, self.n)
+        check(lib().nexus_keygen_relin(self._h, sk.data_ptr(), int(seed), key.data_ptr(), _stream_ptr(stream)),
+              "nexus_keygen_relin")
+        return key
+
+    def keygen_galois(self, sk, elt: int, seed: int, stream=None):
+        k = len(self.moduli)
+        key = self._empty(k - 1, 2, k, self.n)
+        check(lib().nexus_keygen_galois(self._h, sk.data_ptr(), int(elt), int(seed), key.data_ptr(),
+                                        _stream_ptr(stream)), "nexus_keygen_galois")
+        return key
+
+    def encrypt_symmetric(self, sk, pt, limbs: int, seed: int, stream=None):
+        ct = self._empty(2, limbs, self.n)
+        check(lib().nexus_encrypt_symmetric(self._h, sk.data_ptr(), None if pt is None else pt.data_ptr(), limbs,
+                                            int(seed), ct.data_ptr(), _stream_ptr(stream)), "nexus_encrypt_symmetric")
+        return ct
+
+    def decrypt(self, sk, ct, stream=None):
+        size, limbs = ct.shape[0], ct.shape[1]
+        pt = self._empty(limbs, self.n)
+        check(lib().nexus_decrypt(self._h, sk.data_ptr(), ct.data_ptr(), size, limbs, pt.data_ptr(),
+                                  _stream_ptr(stream)), "nexus_decrypt")
+        return pt

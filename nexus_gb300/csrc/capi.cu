@@ -276,3 +276,47 @@ extern "C" int nexus_decode(nexus_context *ctx, const uint64_t *d_pt, int limbs,
         }
     });
 }
+
+extern "C" int nexus_keygen_secret(nexus_context *ctx, uint64_t seed, int hamming_weight, uint64_t *d_sk,
+                                   void *stream)
+{
+    static const char *fn = "nexus_keygen_secret";
+    if (!ctx || !d_sk) return fail(fn, "null argument");
+    if (hamming_weight < 0) return fail(fn, "hamming_weight must be >= 0");
+    return guarded(fn, [&] { keygen_secret(ctx->c, seed, hamming_weight, d_sk, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_keygen_relin(nexus_context *ctx, const uint64_t *d_sk, uint64_t seed, uint64_t *d_key,
+                                  void *stream)
+{
+    static const char *fn = "nexus_keygen_relin";
+    if (!ctx || !d_sk || !d_key) return fail(fn, "null argument");
+    return guarded(fn, [&] { keygen_relin(ctx->c, d_sk, seed, d_key, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_keygen_galois(nexus_context *ctx, const uint64_t *d_sk, uint32_t elt, uint64_t seed,
+                                   uint64_t *d_key, void *stream)
+{
+    static const char *fn = "nexus_keygen_galois";
+    if (!ctx || !d_sk || !d_key) return fail(fn, "null argument");
+    if (!(elt & 1) || elt >= 2 * ctx->c.n) return fail(fn, "Galois element is not valid");
+    return guarded(fn, [&] { keygen_galois(ctx->c, d_sk, elt, seed, d_key, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_encrypt_symmetric(nexus_context *ctx, const uint64_t *d_sk, const uint64_t *d_pt, int limbs,
+                                       uint64_t seed, uint64_t *d_ct, void *stream)
+{
+    static const char *fn = "nexus_encrypt_symmetric";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!d_sk || !d_ct) return fail(fn, "null argument");
+    return guarded(fn, [&] { encrypt_symmetric(ctx->c, d_sk, d_pt, limbs, seed, d_ct, (cudaStream_t)stream); });
+}
+
+extern "C" int nexus_decrypt(nexus_context *ctx, const uint64_t *d_sk, const uint64_t *d_ct, int size, int limbs,
+                             uint64_t *d_pt, void *stream)
+{
+    static const char *fn = "nexus_decrypt";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (!d_sk || !d_ct || !d_pt || size < 2 || size > 3) return fail(fn, "null argument or size not 2 or 3");
+    return guarded(fn, [&] { decrypt(ctx->c, d_sk, d_ct, size, limbs, d_pt, (cudaStream_t)stream); });
+}

@@ -52,4 +52,14 @@ void relinearize(Context &c, const uint64_t *ct3, int limbs, const uint64_t *key
 void apply_galois(Context &c, const uint64_t *ct, int limbs, uint32_t elt, const uint64_t *key, uint64_t *out,
                   cudaStream_t s);
 
+// key generation / symmetric encryption / decryption (sampling.cu)
+void keygen_secret(Context &c, uint64_t seed, int hamming_weight, uint64_t *sk, cudaStream_t s);
+void keygen_kswitch(Context &c, const uint64_t *sk, const uint64_t *new_key, uint64_t seed, uint64_t *key,
+                    cudaStream_t s);
+void keygen_relin(Context &c, const uint64_t *sk, uint64_t seed, uint64_t *key, cudaStream_t s);
+void keygen_galois(Context &c, const uint64_t *sk, uint32_t elt, uint64_t seed, uint64_t *key, cudaStream_t s);
+void encrypt_symmetric(Context &c, const uint64_t *sk, const uint64_t *m, int limbs, uint64_t seed, uint64_t *ct,
+                       cudaStream_t s);
+void decrypt(Context &c, const uint64_t *sk, const uint64_t *ct, int size, int limbs, uint64_t *m, cudaStream_t s);
+
 }  // namespace nexus
