@@ -652,3 +652,221 @@ void or_add_sub(const or_ctx *c, const uint64_t *a, const uint64_t *b, int size,
 uint64_t or_mulmod(uint64_t a, uint64_t b, uint64_t q) { return mulmod(a, b, q); }
 uint64_t or_invmod(uint64_t a, uint64_t q) { return invmod(a, q); }
 int or_is_prime(uint64_t n) { return is_prime_u64(n); }
+
+/* ------------------------------------------------------------------ */
+/* CKKS encoder                                                         */
+/* ------------------------------------------------------------------ */
+/* The complex FFT below restates CKKSEncoder (ckks.cpp:13-70), the root
+ * table of ComplexRoots (util/croots.cpp) and DWTHandler over complex<double>
+ * (util/dwthandler.h).  Products are written as (ac - bd, ad + bc), the
+ * rounding of std::complex<double> multiplication without contraction; the
+ * file is compiled with -ffp-contract=off. */
+#include <math.h>
+
+typedef struct { double re, im; } cplx;
+
+static cplx cmul(cplx a, cplx b) { cplx r = {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; return r; }
+static cplx cadd(cplx a, cplx b) { cplx r = {a.re + b.re, a.im + b.im}; return r; }
+static cplx csubc(cplx a, cplx b) { cplx r = {a.re - b.re, a.im - b.im}; return r; }
+static cplx cscale(cplx a, double s) { cplx r = {a.re * s, a.im * s}; return r; }
+
+typedef struct {
+    int logn;
+    size_t n, slots;
+    uint32_t *index_map;
+    cplx *root_powers, *inv_root_powers;
+} or_encoder;
+
+static cplx root_get(const cplx *tab, size_t m, size_t index)
+{
+    index &= m - 1;
+    if (index <= m / 8) return tab[index];
+    if (index <= m / 4) { cplx a = tab[m / 4 - index]; cplx r = {a.im, a.re}; return r; }
+    if (index <= m / 2) { cplx a = root_get(tab, m, m / 2 - index); cplx r = {-a.re, a.im}; return r; }
+    if (index <= 3 * m / 4) { cplx a = root_get(tab, m, index - m / 2); cplx r = {-a.re, -a.im}; return r; }
+    { cplx a = root_get(tab, m, m - index); cplx r = {a.re, -a.im}; return r; }
+}
+
+or_encoder *or_encoder_create(int logn)
+{
+    or_encoder *e = (or_encoder *)calloc(1, sizeof(or_encoder));
+    size_t n = (size_t)1 << logn, m = n << 1;
+    e->logn = logn; e->n = n; e->slots = n / 2;
+    e->index_map = (uint32_t *)malloc(sizeof(uint32_t) * n);
+    uint64_t pos = 1;
+    for (size_t i = 0; i < e->slots; i++) {
+        uint64_t i1 = (pos - 1) >> 1, i2 = (m - pos - 1) >> 1;
+        e->index_map[i] = reverse_bits((uint32_t)i1, logn);
+        e->index_map[e->slots | i] = reverse_bits((uint32_t)i2, logn);
+        pos = (pos * 5) & (m - 1);
+    }
+    const double PI_ = 3.1415926535897932384626433832795028842;
+    cplx *tab = (cplx *)malloc(sizeof(cplx) * (m / 8 + 1));
+    for (size_t i = 0; i <= m / 8; i++) {
+        double th = 2 * PI_ * (double)i / (double)m;
+        tab[i].re = cos(th);
+        tab[i].im = sin(th);
+    }
+    e->root_powers = (cplx *)calloc(n, sizeof(cplx));
+    e->inv_root_powers = (cplx *)calloc(n, sizeof(cplx));
+    for (size_t i = 1; i < n; i++) {
+        e->root_powers[i] = root_get(tab, m, reverse_bits((uint32_t)i, logn));
+        cplx a = root_get(tab, m, reverse_bits((uint32_t)(i - 1), logn) + 1);
+        a.im = -a.im;
+        e->inv_root_powers[i] = a;
+    }
+    free(tab);
+    return e;
+}
+
+void or_encoder_destroy(or_encoder *e)
+{
+    if (!e) return;
+    free(e->index_map); free(e->root_powers); free(e->inv_root_powers); free(e);
+}
+
+/* total_coeff_modulus_bit_count of the first `limbs` primes */
+static int prod_bits(const or_ctx *c, int limbs)
+{
+    uint64_t p[70] = {0};
+    p[0] = 1;
+    for (int i = 0; i < limbs; i++) {
+        u128 carry = 0;
+        for (int w = 0; w <= limbs; w++) {
+            u128 t = (u128)p[w] * c->q[i] + carry;
+            p[w] = (uint64_t)t;
+            carry = t >> 64;
+        }
+    }
+    for (int w = limbs; w >= 0; w--)
+        if (p[w]) return w * 64 + (64 - __builtin_clzll(p[w]));
+    return 0;
+}
+
+static uint64_t words_mod(const uint64_t *w, int count, uint64_t q)
+{
+    u128 r = 0;
+    for (int i = count - 1; i >= 0; i--) r = ((r << 64) | w[i]) % q;
+    return (uint64_t)r;
+}
+
+/* CKKSEncoder::encode_internal for complex values (ckks.h:457-640); output
+ * in NTT form [limbs][N].  Returns 0, -1 "scale out of bounds", -2 "encoded
+ * values are too large", -3 "values_size is too large". */
+int or_encode(const or_ctx *c, const or_encoder *e, const double *re, const double *im, size_t nvals, double scale,
+              int limbs, uint64_t *out)
+{
+    size_t n = e->n;
+    if (nvals > e->slots) return -3;
+    int tb = prod_bits(c, limbs);
+    if (scale <= 0 || ((int)log2(scale) + 1 >= tb)) return -1;
+    cplx *v = (cplx *)calloc(n, sizeof(cplx));
+    for (size_t i = 0; i < nvals; i++) {
+        cplx a = {re[i], im ? im[i] : 0.0};
+        v[e->index_map[i]] = a;
+        a.im = -a.im;
+        v[e->index_map[i + e->slots]] = a;
+    }
+    double fix = scale / (double)n;
+    /* transform_from_rev with the scalar in the last stage */
+    size_t gap = 1, m = n >> 1;
+    const cplx *rt = e->inv_root_powers;
+    for (; m > 1; m >>= 1) {
+        size_t off = 0;
+        for (size_t i = 0; i < m; i++) {
+            cplx r = *++rt;
+            cplx *x = v + off, *y = x + gap;
+            for (size_t j = 0; j < gap; j++) {
+                cplx u = x[j], w = y[j];
+                x[j] = cadd(u, w);
+                y[j] = cmul(csubc(u, w), r);
+            }
+            off += gap << 1;
+        }
+        gap <<= 1;
+    }
+    {
+        cplx r = *++rt;
+        cplx sr = cscale(r, fix);
+        for (size_t j = 0; j < gap; j++) {
+            cplx u = v[j], w = v[j + gap];
+            v[j] = cscale(cadd(u, w), fix);
+            v[j + gap] = cmul(csubc(u, w), sr);
+        }
+    }
+    double max_coeff = 0;
+    for (size_t i = 0; i < n; i++) if (fabs(v[i].re) > max_coeff) max_coeff = fabs(v[i].re);
+    int max_bits = (int)ceil(log2(max_coeff > 1.0 ? max_coeff : 1.0)) + 1;
+    if (max_bits >= tb) { free(v); return -2; }
+    double two64 = pow(2.0, 64);
+    for (size_t i = 0; i < n; i++) {
+        double cd = round(v[i].re);
+        int neg = signbit(cd) != 0;
+        cd = fabs(cd);
+        uint64_t w[40];
+        int cnt = 0;
+        if (max_bits <= 64) { w[0] = (uint64_t)cd; cnt = 1; }
+        else if (max_bits <= 128) { w[0] = (uint64_t)fmod(cd, two64); w[1] = (uint64_t)(cd / two64); cnt = 2; }
+        else { while (cd >= 1 && cnt < 40) { w[cnt++] = (uint64_t)fmod(cd, two64); cd /= two64; } }
+        for (int j = 0; j < limbs; j++) {
+            uint64_t q = c->q[j];
+            uint64_t r = cnt ? words_mod(w, cnt, q) : 0;
+            if (neg && r) r = q - r;
+            out[(size_t)j * n + i] = r;
+        }
+    }
+    free(v);
+    for (int j = 0; j < limbs; j++) ntt_full(out + (size_t)j * n, c, j);
+    return 0;
+}
+
+/* CKKSEncoder::encode_internal(double) (ckks.cpp:75-205): per-limb residue of
+ * round(value * scale).  Returns 0, -1 scale out of bounds, -2 too large. */
+int or_encode_scalar(const or_ctx *c, double value, double scale, int limbs, uint64_t *per_limb)
+{
+    int tb = prod_bits(c, limbs);
+    if (scale <= 0 || ((int)log2(scale) >= tb)) return -1;
+    value *= scale;
+    int cb = (int)log2(fabs(value)) + 2;
+    if (cb >= tb) return -2;
+    double two64 = pow(2.0, 64);
+    double cd = round(value);
+    int neg = signbit(cd) != 0;
+    cd = fabs(cd);
+    uint64_t w[40];
+    int cnt = 0;
+    if (cb <= 64) { w[0] = (uint64_t)fabs(cd); cnt = 1; }
+    else if (cb <= 128) { w[0] = (uint64_t)fmod(cd, two64); w[1] = (uint64_t)(cd / two64); cnt = 2; }
+    else { while (cd >= 1 && cnt < 40) { w[cnt++] = (uint64_t)fmod(cd, two64); cd /= two64; } }
+    for (int j = 0; j < limbs; j++) {
+        uint64_t q = c->q[j];
+        uint64_t r = cnt ? words_mod(w, cnt, q) : 0;
+        if (neg && r) r = q - r;
+        per_limb[j] = r;
+    }
+    return 0;
+}
+
+/* out[p][l] = in[p][l] * s[l] mod q_l */
+void or_multiply_scalar(const or_ctx *c, const uint64_t *in, int polys, int limbs, const uint64_t *s, uint64_t *out)
+{
+    size_t n = c->n;
+    for (int p = 0; p < polys; p++)
+        for (int l = 0; l < limbs; l++) {
+            size_t o = ((size_t)p * limbs + l) * n;
+            for (size_t t = 0; t < n; t++) out[o + t] = mulmod(in[o + t], s[l], c->q[l]);
+        }
+}
+
+/* out[l] = in[l] (+|-) s[l] on one polynomial (add_plain of a scalar plaintext) */
+void or_add_scalar(const or_ctx *c, const uint64_t *in, int limbs, const uint64_t *s, int sub, uint64_t *out)
+{
+    size_t n = c->n;
+    for (int l = 0; l < limbs; l++) {
+        uint64_t q = c->q[l];
+        for (size_t t = 0; t < n; t++) {
+            uint64_t x = in[(size_t)l * n + t];
+            out[(size_t)l * n + t] = sub ? (x >= s[l] ? x - s[l] : x + q - s[l]) : (x + s[l] >= q ? x + s[l] - q : x + s[l]);
+        }
+    }
+}

@@ -59,6 +59,15 @@ def lib():
         for f in ("or_mulmod", "or_invmod"):
             getattr(l, f).restype = C.c_uint64
             getattr(l, f).argtypes = [C.c_uint64, C.c_uint64, C.c_uint64][: 3 if f == "or_mulmod" else 2]
+        l.or_encoder_create.restype = C.c_void_p
+        l.or_encoder_create.argtypes = [C.c_int]
+        l.or_encoder_destroy.argtypes = [C.c_void_p]
+        l.or_encode.restype = C.c_int
+        l.or_encode.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_double, C.c_int, u64p]
+        l.or_encode_scalar.restype = C.c_int
+        l.or_encode_scalar.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int, u64p]
+        l.or_multiply_scalar.argtypes = [C.c_void_p, u64p, C.c_int, C.c_int, u64p, u64p]
+        l.or_add_scalar.argtypes = [C.c_void_p, u64p, C.c_int, u64p, C.c_int, u64p]
         l.or_is_prime.restype = C.c_int
         l.or_is_prime.argtypes = [C.c_uint64]
         _lib = l
@@ -107,6 +116,9 @@ class OracleContext:
             raise MemoryError("or_ctx_create failed")
 
     def __del__(self):
+        if getattr(self, "_enc", None):
+            lib().or_encoder_destroy(self._enc)
+            self._enc = None
         if getattr(self, "_h", None):
             lib().or_ctx_destroy(self._h)
             self._h = None
@@ -175,6 +187,44 @@ class OracleContext:
         out = np.zeros_like(ct)
         lib().or_multiply_plain(self._h, _p(np.ascontiguousarray(ct)), size, ell, _p(np.ascontiguousarray(pt)),
                                 _p(out))
+        return out
+
+    # CKKSEncoder::encode (ckks.h:457-640) -> NTT-form [limbs][N]
+    _ENC_ERR = {-1: "scale out of bounds", -2: "encoded values are too large", -3: "values_size is too large"}
+
+    def encode(self, values, scale, limbs):
+        if not hasattr(self, "_enc"):
+            self._enc = lib().or_encoder_create(self.log_n)
+        v = np.asarray(values)
+        re = np.ascontiguousarray(v.real, dtype=np.float64)
+        im = np.ascontiguousarray(v.imag, dtype=np.float64) if np.iscomplexobj(v) else None
+        out = np.zeros((limbs, self.n), dtype=np.uint64)
+        rc = lib().or_encode(self._h, self._enc, re.ctypes.data, None if im is None else im.ctypes.data, re.size,
+                             float(scale), limbs, _p(out))
+        if rc:
+            raise ValueError(self._ENC_ERR[rc])
+        return out
+
+    # CKKSEncoder::encode(double) (ckks.cpp:75-205): per-limb residues
+    def encode_scalar(self, value, scale, limbs):
+        out = np.zeros(limbs, dtype=np.uint64)
+        rc = lib().or_encode_scalar(self._h, float(value), float(scale), limbs, _p(out))
+        if rc:
+            raise ValueError({-1: "scale out of bounds", -2: "encoded value is too large"}[rc])
+        return out
+
+    def multiply_scalar(self, ct, per_limb):
+        ct = np.ascontiguousarray(ct, dtype=np.uint64)
+        out = np.zeros_like(ct)
+        s = np.ascontiguousarray(per_limb, dtype=np.uint64)
+        lib().or_multiply_scalar(self._h, _p(ct), ct.shape[0], ct.shape[1], _p(s), _p(out))
+        return out
+
+    def add_scalar(self, poly, per_limb, sub=False):
+        poly = np.ascontiguousarray(poly, dtype=np.uint64)
+        out = np.zeros_like(poly)
+        s = np.ascontiguousarray(per_limb, dtype=np.uint64)
+        lib().or_add_scalar(self._h, _p(poly), poly.shape[0], _p(s), 1 if sub else 0, _p(out))
         return out
 
     def add(self, a, b):
