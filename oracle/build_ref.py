@@ -24,6 +24,11 @@ OUT = HERE / "_ref"
 NEXUS_TREE = Path(os.environ.get("NEXUS_REFERENCE", "/root/reference"))
 SEAL_SRC = NEXUS_TREE / "thirdparty" / "SEAL-4.1-bs" / "native" / "src"
 LIB = OUT / "libseal_shim.so"
+# NEXUS's operators on SEAL (src/ in the NEXUS tree).  src/ckks_evaluator.cpp
+# names compr_mode_type::zstd (a deprecated helper); zstd is compiled out of
+# SEAL here, so that one enumerator is mapped to `none` with -Dzstd=none.
+NEXUS_SRC = NEXUS_TREE / "src"
+NEXUS_OPS = ["ckks_evaluator.cpp", "gelu.cpp", "softmax.cpp", "layer_norm.cpp"]
 
 CONFIG_ON = ["SEAL_USE_STD_BYTE", "SEAL_USE_SHARED_MUTEX", "SEAL_USE_IF_CONSTEXPR", "SEAL_USE_MAYBE_UNUSED",
              "SEAL_USE_NODISCARD", "SEAL_USE_STD_FOR_EACH_N", "SEAL_USE_INTRIN", "SEAL_USE___INT128",
@@ -61,11 +66,14 @@ def build(jobs: int | None = None) -> Path:
     objdir = OUT / "obj"
     objdir.mkdir(exist_ok=True)
     srcs = sorted((SEAL_SRC / "seal").glob("*.cpp")) + sorted((SEAL_SRC / "seal" / "util").glob("*.cpp")) + \
-        sorted((SEAL_SRC / "seal" / "util").glob("*.c")) + [HERE / "seal_shim.cpp"]
-    inc = ["-I", str(OUT / "include"), "-I", str(SEAL_SRC)]
+        sorted((SEAL_SRC / "seal" / "util").glob("*.c")) + [NEXUS_SRC / f for f in NEXUS_OPS] + \
+        [HERE / "seal_shim.cpp"]
+    inc = ["-I", str(OUT / "include"), "-I", str(SEAL_SRC), "-I", str(NEXUS_SRC)]
     todo, objs = [], []
     for s in srcs:
         o = objdir / (s.parent.name + "_" + s.name + ".o")
+        if s.parent == NEXUS_SRC:
+            o = objdir / ("nexus_" + s.name + ".o")
         objs.append(o)
         if not o.exists() or o.stat().st_mtime < s.stat().st_mtime:
             todo.append((s, o))
@@ -76,6 +84,8 @@ def build(jobs: int | None = None) -> Path:
             cmd = ["gcc", "-O2", "-fPIC", "-std=c11"] + inc + ["-c", str(s), "-o", str(o)]
         else:
             cmd = ["g++", "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off"] + inc + ["-c", str(s), "-o", str(o)]
+            if s.parent == NEXUS_SRC:
+                cmd.insert(1, "-Dzstd=none")
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
             raise RuntimeError(f"compile failed: {s}\n{r.stderr[-4000:]}")

@@ -55,6 +55,8 @@ def lib():
         l.sr_decode.argtypes = [C.c_void_p, u64p, C.c_int, C.c_double, f64p, f64p, C.c_size_t]
         l.sr_encrypt.argtypes = [C.c_void_p, f64p, C.c_size_t, C.c_double, u64p]
         l.sr_decrypt.argtypes = [C.c_void_p, u64p, C.c_int, C.c_double, f64p, C.c_size_t]
+        l.sr_nexus_op.argtypes = [C.c_void_p, C.c_int, u64p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
+                                  C.c_double, u64p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
         _lib = l
     return _lib
 
@@ -180,3 +182,14 @@ class SealRef:
         out = np.zeros(nvals)
         _ck(lib().sr_decrypt(self._h, _p(np.ascontiguousarray(ct)), ct.shape[1], scale, _p(out), nvals))
         return out
+
+    OPS = {"gelu": 0, "softmax": 1, "layer_norm": 2, "sgn_eval": 3, "exp": 4, "inverse": 5, "invert_sqrt": 6}
+
+    def nexus_op(self, op, ct, scale, base_scale, a1=0, a2=0, f=0.0):
+        """Run NEXUS's own operator (src/*.cpp compiled against this SEAL)."""
+        out = np.zeros((2, self.k - 1, self.n), np.uint64)
+        ol = C.c_int()
+        osc = C.c_double()
+        _ck(lib().sr_nexus_op(self._h, self.OPS[op], _p(np.ascontiguousarray(ct)), ct.shape[1], scale, base_scale,
+                              a1, a2, f, _p(out), C.byref(ol), C.byref(osc)))
+        return np.ascontiguousarray(out.reshape(-1)[: 2 * ol.value * self.n].reshape(2, ol.value, self.n)), osc.value

@@ -14,6 +14,12 @@
 #include <vector>
 
 #include "seal/seal.h"
+
+// NEXUS's own operators (src/*.h in the NEXUS tree), compiled from source
+#include "ckks_evaluator.h"
+#include "gelu.h"
+#include "layer_norm.h"
+#include "softmax.h"
 #include "seal/util/ntt.h"
 #include "seal/util/rlwe.h"
 
@@ -311,6 +317,35 @@ int sr_decrypt(void *h, const uint64_t *ct, int limbs, double scale, double *out
         std::vector<double> v;
         s.enc->decode(p, v);
         for (size_t i = 0; i < nvals && i < v.size(); ++i) out[i] = v[i];
+    })
+}
+
+// Run one NEXUS operator on a ciphertext [2][limbs][N] at in_scale with the
+// shim's keys: op 0 GeLUEvaluator::gelu, 1 SoftmaxEvaluator::softmax(len=a1),
+// 2 LNEvaluator::layer_norm(len=a1), 3 CKKSEvaluator::sgn_eval(a1, a2, f),
+// 4 exp, 5 inverse(iter=a1), 6 invert_sqrt(a1, a2).  `base_scale` is the
+// CKKSEvaluator's scale.  Writes the output and its limbs/scale.
+int sr_nexus_op(void *h, int op, const uint64_t *in, int limbs, double in_scale, double base_scale, int a1, int a2,
+                double f, uint64_t *out, int *out_limbs, double *out_scale)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Ciphertext x, res;
+        load_ct(s, x, in, 2, limbs, in_scale);
+        CKKSEvaluator ck(*s.ctx, *s.encryptor, *s.decryptor, *s.enc, *s.ev, base_scale, *s.rk, *s.gk);
+        switch (op) {
+        case 0: { GeLUEvaluator g(ck); g.gelu(x, res); break; }
+        case 1: { SoftmaxEvaluator sm(ck); sm.softmax(x, res, a1); break; }
+        case 2: { LNEvaluator ln(ck); ln.layer_norm(x, res, a1); break; }
+        case 3: res = ck.sgn_eval(x, a1, a2, f); break;
+        case 4: res = ck.exp(x); break;
+        case 5: res = ck.inverse(x, a1); break;
+        case 6: res = ck.invert_sqrt(x, a1, a2); break;
+        default: throw std::invalid_argument("unknown op");
+        }
+        store_ct(s, res, out);
+        *out_limbs = (int)res.coeff_modulus_size();
+        *out_scale = res.scale();
     })
 }
 

@@ -1,0 +1,79 @@
+"""NEXUS operators: the oracle restatement (oracle/nexus_l3.py) against NEXUS's
+own src/*.cpp compiled against the real SEAL-4.1-bs, on SEAL's keys and
+ciphertexts.  Word-for-word equality of the output ciphertext and its scale.
+Skipped where the SEAL/NEXUS reference build is unavailable."""
+import numpy as np
+import pytest
+
+from oracle import nexus_l3 as L
+from oracle import pyoracle as po
+from oracle import pyref as pr
+
+pytestmark = pytest.mark.skipif(not pr.available(), reason="SEAL reference build unavailable")
+
+LOG_N = 13
+N = 1 << LOG_N
+SCALE = 2.0 ** 40
+STEPS = [-128, 128] + [2 ** i for i in range(7)] + [-(2 ** i) for i in range(7)]
+
+
+@pytest.fixture(scope="module")
+def env():
+    qs = po.create_coeff_modulus(N, [58] + [40] * 24 + [58])
+    s = pr.SealRef(LOG_N, qs, seed=5, steps=STEPS)
+    oc = po.OracleContext(LOG_N, qs)
+    gk = {s.galois_elt(st): s.galois_key(s.galois_elt(st)) for st in STEPS}
+    ev = L.Evaluator(oc, s.relin_key(), gk)
+    return s, L.CKKSEvaluator(ev, SCALE)
+
+
+def _check(got, want):
+    data, scale = want
+    assert got.scale == scale
+    assert np.array_equal(got.data, data)
+
+
+def test_gelu(env):
+    s, ck = env
+    ct = s.encrypt(np.random.default_rng(0).uniform(-5, 5, N // 2), SCALE)
+    _check(L.gelu(ck, L.Ct(ct, SCALE)), s.nexus_op("gelu", ct, SCALE, SCALE))
+
+
+def test_softmax(env):
+    s, ck = env
+    ct = s.encrypt(np.random.default_rng(1).uniform(-5, 0, N // 2), SCALE)
+    _check(L.softmax(ck, L.Ct(ct, SCALE), 128), s.nexus_op("softmax", ct, SCALE, SCALE, a1=128))
+
+
+def test_layer_norm(env):
+    s, ck = env
+    ct = s.encrypt(np.random.default_rng(2).uniform(-1, 1, N // 2), SCALE)
+    _check(L.layer_norm(ck, L.Ct(ct, SCALE), 128), s.nexus_op("layer_norm", ct, SCALE, SCALE, a1=128))
+
+
+@pytest.mark.parametrize("op,args", [("sgn_eval", (2, 2, 0.5)), ("sgn_eval", (1, 3, 1.0)), ("exp", ()),
+                                     ("inverse", (4,)), ("invert_sqrt", (5, 2)), ("invert_sqrt", (4, 1))])
+def test_primitives(env, op, args):
+    s, ck = env
+    lo, hi = {"sgn_eval": (-1, 1), "exp": (-4, 0), "inverse": (0.1, 1.9), "invert_sqrt": (0.01, 5)}[op]
+    ct = s.encrypt(np.random.default_rng(3).uniform(lo, hi, N // 2), SCALE)
+    x = L.Ct(ct, SCALE)
+    if op == "sgn_eval":
+        got = ck.sgn_eval(x, *args)
+        want = s.nexus_op(op, ct, SCALE, SCALE, a1=args[0], a2=args[1], f=args[2])
+    elif op == "exp":
+        got, want = ck.exp(x), s.nexus_op(op, ct, SCALE, SCALE)
+    elif op == "inverse":
+        got, want = ck.inverse(x, *args), s.nexus_op(op, ct, SCALE, SCALE, a1=args[0])
+    else:
+        got, want = ck.invert_sqrt(x, *args), s.nexus_op(op, ct, SCALE, SCALE, a1=args[0], a2=args[1])
+    _check(got, want)
+
+
+def test_naf_and_multi_rotation(env):
+    """rotate by a step without its own key: SEAL's NAF decomposition"""
+    s, ck = env
+    ct = s.encrypt(np.random.default_rng(4).uniform(-1, 1, N // 2), SCALE)
+    for step in (3, 7, 100, -5):
+        assert np.array_equal(ck.ev.rotate(L.Ct(ct, SCALE), step).data, s.rotate(ct, step))
+    assert L.naf(7) == [-1, 8] and L.naf(-6) == [2, -8]
