@@ -242,6 +242,56 @@ int nexus_multiply_scalar(nexus_context *ctx, const uint64_t *d_in, int polys, i
 int nexus_decode(nexus_context *ctx, const uint64_t *d_pt, int limbs, double scale, double *re, double *im,
                  size_t nvals, size_t sparse_slots, void *stream);
 
+/* ------------------------------------------------------------------ */
+/* NEXUS operators (src/ckks_evaluator.cpp, gelu.cpp, softmax.cpp,      */
+/* layer_norm.cpp in the NEXUS tree) on the engine                      */
+/* ------------------------------------------------------------------ */
+
+typedef struct nexus_evaluator nexus_evaluator;
+typedef struct nexus_ciphertext nexus_ciphertext;
+
+/*
+ * Evaluator with SEAL's semantics plus NEXUS's CKKSEvaluator at base scale
+ * `scale`; d_relin_key (SEAL layout, caller-owned) may be NULL when no
+ * multiplication is evaluated.  All work is enqueued on `stream`.
+ * Replaces: CKKSEvaluator(SEALContext&, Encryptor&, Decryptor&, CKKSEncoder&,
+ *   Evaluator&, double scale, RelinKeys&, GaloisKeys&) (src/ckks_evaluator.h:52-86)
+ *   and nexus::CKKSEvaluator (cuda/src/ckks_evaluator.cuh:457-481).
+ */
+int nexus_evaluator_create(nexus_context *ctx, double scale, const uint64_t *d_relin_key, void *stream,
+                           nexus_evaluator **out);
+int nexus_evaluator_destroy(nexus_evaluator *ev);
+/* Register the Galois key of one element (caller-owned, SEAL layout).
+ * Replaces: the GaloisKeys& held by CKKSEvaluator (src/ckks_evaluator.h:42). */
+int nexus_evaluator_add_galois_key(nexus_evaluator *ev, uint32_t galois_elt, const uint64_t *d_key);
+
+/* Ciphertext objects owned by the engine ([size][limbs][N] on the device).
+ * Replaces: seal::Ciphertext / PhantomCiphertext. */
+int nexus_ciphertext_create(nexus_context *ctx, nexus_ciphertext **out);
+int nexus_ciphertext_destroy(nexus_ciphertext *ct);
+/* copy size x limbs x N words from host (from_host = 1) or device memory */
+int nexus_ciphertext_load(nexus_ciphertext *ct, const uint64_t *src, int size, int limbs, double scale, int from_host,
+                          void *stream);
+int nexus_ciphertext_info(const nexus_ciphertext *ct, int *size, int *limbs, double *scale, uint64_t **d_data);
+int nexus_ciphertext_store(const nexus_ciphertext *ct, uint64_t *dst, int to_host, void *stream);
+
+/* GeLUEvaluator::gelu(x, res) (src/gelu.cpp:5-111); x is mod-switched in
+ * place as in the original. */
+int nexus_gelu(nexus_evaluator *ev, nexus_ciphertext *x, nexus_ciphertext *res);
+/* SoftmaxEvaluator::softmax(x, res, len) (src/softmax.cpp:6-42); x is updated in place. */
+int nexus_softmax(nexus_evaluator *ev, nexus_ciphertext *x, int len, nexus_ciphertext *res);
+/* LNEvaluator::layer_norm(x, res, len) (src/layer_norm.cpp:6-33); x is updated in place. */
+int nexus_layer_norm(nexus_evaluator *ev, nexus_ciphertext *x, int len, nexus_ciphertext *res);
+
+/* CKKSEvaluator primitives (src/ckks_evaluator.cpp):
+ *   NEXUS_OP_SGN_EVAL     sgn_eval(x, d_g = a1, d_f = a2, sgn_factor = f)   :181-212
+ *   NEXUS_OP_EXP          exp(x)                                            :534-548
+ *   NEXUS_OP_INVERSE      inverse(x, iter = a1)                             :487-509
+ *   NEXUS_OP_INVERT_SQRT  invert_sqrt(x, d_newt = a1, d_gold = a2)          :480-485 */
+enum { NEXUS_OP_SGN_EVAL = 0, NEXUS_OP_EXP = 1, NEXUS_OP_INVERSE = 2, NEXUS_OP_INVERT_SQRT = 3 };
+int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext *x, int a1, int a2, double f,
+                  nexus_ciphertext *res);
+
 #ifdef __cplusplus
 }
 #endif

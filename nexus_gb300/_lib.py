@@ -45,6 +45,20 @@ SIGNATURES = [
     ("nexus_multiply_scalar", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, u64p, C.c_void_p, C.c_void_p]),
     ("nexus_decode", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.c_size_t,
                                C.c_size_t, C.c_void_p]),
+    ("nexus_evaluator_create", C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("nexus_evaluator_destroy", C.c_int, [C.c_void_p]),
+    ("nexus_evaluator_add_galois_key", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    ("nexus_ciphertext_create", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("nexus_ciphertext_destroy", C.c_int, [C.c_void_p]),
+    ("nexus_ciphertext_load", C.c_int,
+     [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p]),
+    ("nexus_ciphertext_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_void_p)]),
+    ("nexus_ciphertext_store", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("nexus_gelu", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("nexus_softmax", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("nexus_layer_norm", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("nexus_ckks_op", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_void_p]),
     ("nexus_plain_op", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
 ]

@@ -1,0 +1,178 @@
+// C ABI of the NEXUS operator layer: ciphertext handles, an evaluator bound
+// to caller-owned keys, and the CKKSEvaluator / GELU / softmax / LayerNorm
+// operators (declared in include/nexus_gb300.h).
+#include <stdexcept>
+#include <string>
+
+#include "../../include/nexus_gb300.h"
+#include "ckks.h"
+#include "nexus_ops.h"
+
+using namespace nexus;
+
+struct nexus_evaluator {
+    nexus_context *ctx;
+    Evaluator ev;
+    CKKSEvaluator ck;
+    nexus_evaluator(nexus_context *c, double scale) : ctx(c), ev(c->c), ck(ev, scale) {}
+};
+
+struct nexus_ciphertext {
+    nexus_context *ctx;
+    Ciphertext ct;
+};
+
+namespace {
+
+int fail(const char *fn, const std::string &msg)
+{
+    set_error(std::string(fn) + ": " + msg);
+    return -1;
+}
+
+template <class F>
+int guarded(const char *fn, F &&f)
+{
+    try {
+        f();
+    } catch (const std::exception &e) {
+        return fail(fn, e.what());
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(fn, cudaGetErrorString(e));
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int nexus_evaluator_create(nexus_context *ctx, double scale, const uint64_t *d_relin_key, void *stream,
+                                      nexus_evaluator **out)
+{
+    static const char *fn = "nexus_evaluator_create";
+    if (!ctx || !out) return fail(fn, "null argument");
+    *out = nullptr;
+    return guarded(fn, [&] {
+        auto *e = new nexus_evaluator(ctx, scale);
+        e->ev.set_stream((cudaStream_t)stream);
+        e->ev.relin_key = d_relin_key;
+        *out = e;
+    });
+}
+
+extern "C" int nexus_evaluator_destroy(nexus_evaluator *ev)
+{
+    delete ev;
+    return 0;
+}
+
+extern "C" int nexus_evaluator_add_galois_key(nexus_evaluator *ev, uint32_t galois_elt, const uint64_t *d_key)
+{
+    static const char *fn = "nexus_evaluator_add_galois_key";
+    if (!ev || !d_key) return fail(fn, "null argument");
+    if (!(galois_elt & 1) || galois_elt >= 2 * ev->ctx->c.n) return fail(fn, "Galois element is not valid");
+    ev->ev.galois_keys[galois_elt] = d_key;
+    return 0;
+}
+
+extern "C" int nexus_ciphertext_create(nexus_context *ctx, nexus_ciphertext **out)
+{
+    if (!ctx || !out) return fail("nexus_ciphertext_create", "null argument");
+    *out = new nexus_ciphertext{ctx, Ciphertext()};
+    return 0;
+}
+
+extern "C" int nexus_ciphertext_destroy(nexus_ciphertext *ct)
+{
+    delete ct;
+    return 0;
+}
+
+extern "C" int nexus_ciphertext_load(nexus_ciphertext *ct, const uint64_t *src, int size, int limbs, double scale,
+                                     int from_host, void *stream)
+{
+    static const char *fn = "nexus_ciphertext_load";
+    if (!ct || !src) return fail(fn, "null argument");
+    if (size < 2 || size > 3 || limbs < 1 || limbs > ct->ctx->c.k - 1) return fail(fn, "bad size or limbs");
+    return guarded(fn, [&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        ct->ct.resize(ct->ctx->c, size, limbs, s);
+        ct->ct.scale() = scale;
+        const size_t bytes = (size_t)size * limbs * ct->ctx->c.n * 8;
+        if (cudaMemcpyAsync(ct->ct.data(), src, bytes, from_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                            s) != cudaSuccess)
+            throw std::runtime_error("copy failed");
+    });
+}
+
+extern "C" int nexus_ciphertext_info(const nexus_ciphertext *ct, int *size, int *limbs, double *scale,
+                                     uint64_t **d_data)
+{
+    if (!ct) return fail("nexus_ciphertext_info", "null argument");
+    if (size) *size = ct->ct.size();
+    if (limbs) *limbs = ct->ct.limbs();
+    if (scale) *scale = ct->ct.scale();
+    if (d_data) *d_data = ct->ct.data();
+    return 0;
+}
+
+extern "C" int nexus_ciphertext_store(const nexus_ciphertext *ct, uint64_t *dst, int to_host, void *stream)
+{
+    static const char *fn = "nexus_ciphertext_store";
+    if (!ct || !dst) return fail(fn, "null argument");
+    return guarded(fn, [&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        const size_t bytes = (size_t)ct->ct.size() * ct->ct.limbs() * ct->ctx->c.n * 8;
+        if (cudaMemcpyAsync(dst, ct->ct.data(), bytes, to_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                            s) != cudaSuccess)
+            throw std::runtime_error("copy failed");
+        if (to_host && cudaStreamSynchronize(s) != cudaSuccess) throw std::runtime_error("synchronize failed");
+    });
+}
+
+extern "C" int nexus_gelu(nexus_evaluator *ev, nexus_ciphertext *x, nexus_ciphertext *res)
+{
+    static const char *fn = "nexus_gelu";
+    if (!ev || !x || !res) return fail(fn, "null argument");
+    return guarded(fn, [&] {
+        GeLUEvaluator g(ev->ck);
+        g.gelu(x->ct, res->ct);
+    });
+}
+
+extern "C" int nexus_softmax(nexus_evaluator *ev, nexus_ciphertext *x, int len, nexus_ciphertext *res)
+{
+    static const char *fn = "nexus_softmax";
+    if (!ev || !x || !res) return fail(fn, "null argument");
+    if (len < 1 || (len & (len - 1))) return fail(fn, "len must be a power of two");
+    return guarded(fn, [&] {
+        SoftmaxEvaluator sm(ev->ck);
+        sm.softmax(x->ct, res->ct, len);
+    });
+}
+
+extern "C" int nexus_layer_norm(nexus_evaluator *ev, nexus_ciphertext *x, int len, nexus_ciphertext *res)
+{
+    static const char *fn = "nexus_layer_norm";
+    if (!ev || !x || !res) return fail(fn, "null argument");
+    if (len < 1 || (len & (len - 1))) return fail(fn, "len must be a power of two");
+    return guarded(fn, [&] {
+        LNEvaluator ln(ev->ck);
+        ln.layer_norm(x->ct, res->ct, len);
+    });
+}
+
+extern "C" int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext *x, int a1, int a2, double f,
+                             nexus_ciphertext *res)
+{
+    static const char *fn = "nexus_ckks_op";
+    if (!ev || !x || !res) return fail(fn, "null argument");
+    return guarded(fn, [&] {
+        switch (op) {
+        case NEXUS_OP_SGN_EVAL: res->ct = ev->ck.sgn_eval(x->ct, a1, a2, f); break;
+        case NEXUS_OP_EXP: res->ct = ev->ck.exp(x->ct); break;
+        case NEXUS_OP_INVERSE: res->ct = ev->ck.inverse(x->ct, a1); break;
+        case NEXUS_OP_INVERT_SQRT: res->ct = ev->ck.invert_sqrt(x->ct, a1, a2); break;
+        default: throw std::invalid_argument("unknown op");
+        }
+    });
+}

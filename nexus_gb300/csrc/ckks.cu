@@ -1,0 +1,441 @@
+// C++ evaluator with SEAL's semantics over the engine's kernels (see ckks.h).
+// Error conditions and their messages follow SEAL's Evaluator
+// (evaluator.cpp in SEAL-4.1-bs) so NEXUS's code paths fail where SEAL's do.
+#include <cmath>
+#include <complex>
+#include <cstring>
+
+#include "ckks.h"
+#include "encoder.h"
+#include "ntt.h"
+#include "ops.h"
+
+namespace nexus {
+
+static void ck(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------- buffers
+
+void DeviceBuffer::reserve(size_t words, cudaStream_t s)
+{
+    if (words <= words_ && p_) return;
+    release();
+    ck(cudaMallocAsync(&p_, words * sizeof(uint64_t), s), "cudaMallocAsync");
+    words_ = words;
+    s_ = s;
+}
+
+void DeviceBuffer::release()
+{
+    if (p_) cudaFreeAsync(p_, s_);
+    p_ = nullptr;
+    words_ = 0;
+}
+
+void Ciphertext::resize(const Context &c, int size, int limbs, cudaStream_t s)
+{
+    n_ = c.n;
+    s_ = s;
+    buf_.reserve((size_t)size * limbs * c.n, s);
+    size_ = size;
+    limbs_ = limbs;
+}
+
+Ciphertext::Ciphertext(const Ciphertext &o) { *this = o; }
+
+Ciphertext &Ciphertext::operator=(const Ciphertext &o)
+{
+    if (this == &o) return *this;
+    if (o.empty()) {
+        buf_.release();
+        size_ = limbs_ = 0;
+        scale_ = o.scale_;
+        return *this;
+    }
+    n_ = o.n_;
+    s_ = o.s_;
+    buf_.reserve((size_t)o.size_ * o.limbs_ * o.n_, s_);
+    size_ = o.size_;
+    limbs_ = o.limbs_;
+    scale_ = o.scale_;
+    ck(cudaMemcpyAsync(buf_.get(), o.buf_.get(), (size_t)size_ * limbs_ * n_ * 8, cudaMemcpyDeviceToDevice, s_),
+       "copy ciphertext");
+    return *this;
+}
+
+Plaintext::Plaintext(const Plaintext &o) { *this = o; }
+
+Plaintext &Plaintext::operator=(const Plaintext &o)
+{
+    if (this == &o) return *this;
+    scalar_ = o.scalar_;
+    limbs_ = o.limbs_;
+    scale_ = o.scale_;
+    res_ = o.res_;
+    n_ = o.n_;
+    s_ = o.s_;
+    if (o.scalar_ || !o.buf_.get()) {
+        buf_.release();
+    } else {
+        buf_.reserve((size_t)limbs_ * n_, s_);
+        ck(cudaMemcpyAsync(buf_.get(), o.buf_.get(), (size_t)limbs_ * n_ * 8, cudaMemcpyDeviceToDevice, s_),
+           "copy plaintext");
+    }
+    return *this;
+}
+
+void Plaintext::set_scalar(std::vector<uint64_t> r, double scale)
+{
+    scalar_ = true;
+    res_ = std::move(r);
+    limbs_ = (int)res_.size();
+    scale_ = scale;
+    buf_.release();
+}
+
+void Plaintext::set_vector(const Context &c, int limbs, double scale, cudaStream_t s)
+{
+    scalar_ = false;
+    limbs_ = limbs;
+    scale_ = scale;
+    res_.clear();
+    n_ = c.n;
+    s_ = s;
+    buf_.reserve((size_t)limbs * c.n, s);
+}
+
+void Plaintext::drop_to(int limbs, cudaStream_t s, const Context &c)
+{
+    if (limbs > limbs_) throw std::invalid_argument("cannot switch to higher level modulus");
+    if (limbs == limbs_) return;
+    if (scalar_) {
+        res_.resize(limbs);
+    } else {
+        DeviceBuffer nb;
+        nb.reserve((size_t)limbs * c.n, s);
+        ck(cudaMemcpyAsync(nb.get(), buf_.get(), (size_t)limbs * c.n * 8, cudaMemcpyDeviceToDevice, s), "drop limbs");
+        buf_ = std::move(nb);
+    }
+    limbs_ = limbs;
+}
+
+// ---------------------------------------------------------------- helpers
+
+bool are_close(double a, double b)
+{
+    // util::are_close (util/common.h:569-573)
+    double sf = std::max(std::max(std::fabs(a), std::fabs(b)), 1.0);
+    return std::fabs(a - b) < std::numeric_limits<double>::epsilon() * sf;
+}
+
+std::vector<int> naf(int value)
+{
+    // util::naf (util/numth.h:22-42)
+    std::vector<int> res;
+    bool sign = value < 0;
+    value = std::abs(value);
+    for (int i = 0; value; ++i) {
+        int zi = (value & 1) ? 2 - (value & 3) : 0;
+        value = (value - zi) >> 1;
+        if (zi) res.push_back((sign ? -zi : zi) * (1 << i));
+    }
+    return res;
+}
+
+Evaluator::Evaluator(Context &c, cudaStream_t s) : c_(c), s_(s)
+{
+    enc_ = new Encoder(c);
+    bits_.assign(c.k + 1, 0);
+    for (int l = 1; l <= c.k; ++l) {
+        // bit count of prod_{i<l} q_i (ContextData::total_coeff_modulus_bit_count)
+        std::vector<uint64_t> p(l + 1, 0);
+        p[0] = 1;
+        for (int i = 0; i < l; ++i) {
+            unsigned __int128 carry = 0;
+            for (auto &w : p) {
+                unsigned __int128 t = (unsigned __int128)w * c.q[i] + carry;
+                w = (uint64_t)t;
+                carry = t >> 64;
+            }
+        }
+        int b = 0;
+        for (int w = l; w >= 0; --w)
+            if (p[w]) {
+                b = w * 64 + (64 - __builtin_clzll(p[w]));
+                break;
+            }
+        bits_[l] = b;
+    }
+}
+
+Evaluator::~Evaluator() { delete enc_; }
+
+int Evaluator::total_bits(int limbs) const { return bits_.at(limbs); }
+
+void Evaluator::check_scale(double scale, int limbs) const
+{
+    // is_scale_within_bounds (evaluator.cpp:29-47)
+    if (scale <= 0 || (int)std::log2(scale) >= total_bits(limbs)) throw std::invalid_argument("scale out of bounds");
+}
+
+uint32_t Evaluator::galois_elt(int step) const
+{
+    // GaloisTool::get_elt_from_step (util/galois.cpp:53-90)
+    const uint32_t n = (uint32_t)c_.n;
+    const uint64_t m = 2ull * n;
+    if (step == 0) return (uint32_t)(m - 1);
+    bool neg = step < 0;
+    uint32_t pos = (uint32_t)std::abs(step);
+    if (pos >= (n >> 1)) throw std::invalid_argument("step count too large");
+    int e = neg ? (int)(n >> 1) - (int)pos : (int)pos;
+    uint64_t g = 1;
+    while (e--) g = (g * 5) & (m - 1);
+    return (uint32_t)g;
+}
+
+// ---------------------------------------------------------------- encoding
+
+void Evaluator::encode(const std::vector<double> &values, int limbs, double scale, Plaintext &out)
+{
+    if (limbs < 1 || limbs > top_limbs()) throw std::invalid_argument("parms_id is not valid for encryption parameters");
+    std::vector<std::complex<double>> v(values.size());
+    for (size_t i = 0; i < values.size(); ++i) v[i] = values[i];
+    std::vector<uint64_t> host((size_t)limbs * c_.n);
+    enc_->encode(v.data(), v.size(), scale, limbs, host.data());
+    out.set_vector(c_, limbs, scale, s_);
+    ck(cudaMemcpyAsync(out.mutable_data(), host.data(), host.size() * 8, cudaMemcpyHostToDevice, s_), "upload");
+    ck(cudaStreamSynchronize(s_), "encode");  // host buffer lifetime
+    ntt_forward(c_, out.mutable_data(), 1, 0, limbs, s_);
+}
+
+void Evaluator::encode(double value, int limbs, double scale, Plaintext &out)
+{
+    if (limbs < 1 || limbs > top_limbs()) throw std::invalid_argument("parms_id is not valid for encryption parameters");
+    std::vector<uint64_t> r(limbs);
+    enc_->encode_scalar(value, scale, limbs, r.data());
+    out.set_scalar(std::move(r), scale);
+}
+
+std::vector<double> Evaluator::decode(const Plaintext &pt)
+{
+    if (pt.is_scalar()) throw std::invalid_argument("decode of a scalar plaintext");
+    const size_t n = c_.n;
+    std::vector<uint64_t> host((size_t)pt.limbs() * n);
+    uint64_t *tmp = c_.get_scratch(host.size());
+    ck(cudaMemcpyAsync(tmp, pt.data(), host.size() * 8, cudaMemcpyDeviceToDevice, s_), "copy");
+    ntt_inverse(c_, tmp, 1, 0, pt.limbs(), s_);
+    ck(cudaMemcpyAsync(host.data(), tmp, host.size() * 8, cudaMemcpyDeviceToHost, s_), "download");
+    ck(cudaStreamSynchronize(s_), "decode");
+    std::vector<std::complex<double>> v(n / 2);
+    enc_->decode(host.data(), pt.limbs(), pt.scale(), v.data(), n / 2, 0);
+    std::vector<double> out(n / 2);
+    for (size_t i = 0; i < n / 2; ++i) out[i] = v[i].real();
+    return out;
+}
+
+// ---------------------------------------------------------------- levels
+
+void Evaluator::mod_switch_to_inplace(Ciphertext &ct, int limbs)
+{
+    // mod_switch_to_inplace / mod_switch_drop_to_next (evaluator.cpp:1483-1546, 1630)
+    if (limbs > ct.limbs()) throw std::invalid_argument("cannot switch to higher level modulus");
+    if (limbs == ct.limbs()) return;
+    if (limbs < 1) throw std::invalid_argument("end of modulus switching chain reached");
+    Ciphertext out;
+    out.resize(c_, ct.size(), limbs, s_);
+    out.scale() = ct.scale();
+    const size_t row = c_.n * 8;
+    ck(cudaMemcpy2DAsync(out.data(), limbs * row, ct.data(), ct.limbs() * row, limbs * row, ct.size(),
+                         cudaMemcpyDeviceToDevice, s_),
+       "drop limbs");
+    ct = std::move(out);
+}
+
+void Evaluator::mod_switch_to_inplace(Plaintext &pt, int limbs) { pt.drop_to(limbs, s_, c_); }
+
+void Evaluator::rescale_to_next_inplace(Ciphertext &ct)
+{
+    // rescale_to_next -> mod_switch_scale_to_next (evaluator.cpp:1402-1480, 1682)
+    if (ct.limbs() < 2) throw std::invalid_argument("end of modulus switching chain reached");
+    const double scale = ct.scale() / (double)c_.q[ct.limbs() - 1];
+    check_scale(scale, ct.limbs() - 1);
+    Ciphertext out;
+    out.resize(c_, ct.size(), ct.limbs() - 1, s_);
+    rescale(c_, ct.data(), ct.size(), ct.limbs(), out.data(), s_);
+    out.scale() = scale;
+    ct = std::move(out);
+}
+
+// ---------------------------------------------------------------- arithmetic
+
+void Evaluator::multiply_inplace(Ciphertext &a, const Ciphertext &b)
+{
+    // multiply_inplace -> ckks_multiply (evaluator.cpp:770-850)
+    if (a.limbs() != b.limbs()) throw std::invalid_argument("encrypted1 and encrypted2 parameter mismatch");
+    if (a.size() != 2 || b.size() != 2) throw std::invalid_argument("multiply expects size-2 ciphertexts");
+    const double scale = a.scale() * b.scale();
+    check_scale(scale, a.limbs());
+    Ciphertext out;
+    out.resize(c_, 3, a.limbs(), s_);
+    tensor(c_, a.data(), b.data(), a.limbs(), out.data(), s_);
+    out.scale() = scale;
+    a = std::move(out);
+}
+
+void Evaluator::multiply(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest)
+{
+    if (&b == &dest) {
+        multiply_inplace(dest, a);
+    } else {
+        if (&a != &dest) dest = a;
+        multiply_inplace(dest, b);
+    }
+}
+
+void Evaluator::relinearize_inplace(Ciphertext &ct)
+{
+    // relinearize_internal (evaluator.cpp:1345-1400)
+    if (ct.size() == 2) return;
+    if (!relin_key) throw std::invalid_argument("relin_keys is not valid for encryption parameters");
+    Ciphertext out;
+    out.resize(c_, 2, ct.limbs(), s_);
+    relinearize(c_, ct.data(), ct.limbs(), relin_key, out.data(), s_);
+    out.scale() = ct.scale();
+    ct = std::move(out);
+}
+
+static void check_same(const Ciphertext &a, const Ciphertext &b)
+{
+    if (a.limbs() != b.limbs()) throw std::invalid_argument("encrypted1 and encrypted2 parameter mismatch");
+    if (!are_close(a.scale(), b.scale())) throw std::invalid_argument("scale mismatch");
+    if (a.size() != b.size()) throw std::invalid_argument("ciphertext sizes differ");
+}
+
+void Evaluator::add_inplace(Ciphertext &a, const Ciphertext &b)
+{
+    check_same(a, b);
+    poly_add(c_, a.data(), b.data(), a.size(), a.limbs(), a.data(), s_);
+}
+
+void Evaluator::add(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest)
+{
+    if (&b == &dest) {
+        add_inplace(dest, a);
+    } else {
+        if (&a != &dest) dest = a;
+        add_inplace(dest, b);
+    }
+}
+
+void Evaluator::sub_inplace(Ciphertext &a, const Ciphertext &b)
+{
+    check_same(a, b);
+    poly_sub(c_, a.data(), b.data(), a.size(), a.limbs(), a.data(), s_);
+}
+
+void Evaluator::sub(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest)
+{
+    if (&b == &dest) {
+        sub_inplace(dest, a);
+        negate_inplace(dest);
+    } else {
+        if (&a != &dest) dest = a;
+        sub_inplace(dest, b);
+    }
+}
+
+void Evaluator::negate_inplace(Ciphertext &a) { poly_negate(c_, a.data(), a.size(), a.limbs(), a.data(), s_); }
+
+void Evaluator::negate(const Ciphertext &a, Ciphertext &dest)
+{
+    if (&a != &dest) dest = a;
+    negate_inplace(dest);
+}
+
+void Evaluator::plain_arith(Ciphertext &ct, const Plaintext &pt, bool sub)
+{
+    // add_plain_inplace / sub_plain_inplace (evaluator.cpp:1938, 2046)
+    if (ct.limbs() != pt.limbs()) throw std::invalid_argument("encrypted and plain parameter mismatch");
+    if (!are_close(ct.scale(), pt.scale())) throw std::invalid_argument("scale mismatch");
+    if (pt.is_scalar())
+        poly_add_scalar(c_, ct.data(), ct.limbs(), pt.residues().data(), sub ? 1 : 0, ct.data(), s_);
+    else
+        poly_add_plain(c_, ct.data(), 1, ct.limbs(), pt.data(), sub ? 1 : 0, ct.data(), s_);
+}
+
+void Evaluator::add_plain_inplace(Ciphertext &ct, const Plaintext &pt) { plain_arith(ct, pt, false); }
+void Evaluator::sub_plain_inplace(Ciphertext &ct, const Plaintext &pt) { plain_arith(ct, pt, true); }
+
+void Evaluator::add_plain(const Ciphertext &ct, const Plaintext &pt, Ciphertext &dest)
+{
+    if (&ct != &dest) dest = ct;
+    add_plain_inplace(dest, pt);
+}
+
+void Evaluator::sub_plain(const Ciphertext &ct, const Plaintext &pt, Ciphertext &dest)
+{
+    if (&ct != &dest) dest = ct;
+    sub_plain_inplace(dest, pt);
+}
+
+void Evaluator::multiply_plain_inplace(Ciphertext &ct, const Plaintext &pt)
+{
+    // multiply_plain_inplace -> multiply_plain_ntt (evaluator.cpp:2154, 2336-2373)
+    if (ct.limbs() != pt.limbs()) throw std::invalid_argument("encrypted and plain parameter mismatch");
+    const double scale = ct.scale() * pt.scale();
+    check_scale(scale, ct.limbs());
+    if (pt.is_scalar())
+        poly_mul_scalar(c_, ct.data(), ct.size(), ct.limbs(), pt.residues().data(), ct.data(), s_);
+    else
+        poly_mul_plain(c_, ct.data(), ct.size(), ct.limbs(), pt.data(), ct.data(), s_);
+    ct.scale() = scale;
+}
+
+void Evaluator::multiply_plain(const Ciphertext &ct, const Plaintext &pt, Ciphertext &dest)
+{
+    if (&ct != &dest) dest = ct;
+    multiply_plain_inplace(dest, pt);
+}
+
+// ---------------------------------------------------------------- rotations
+
+void Evaluator::apply_galois_inplace(Ciphertext &ct, uint32_t elt)
+{
+    // apply_galois_inplace (evaluator.cpp:2563-2665)
+    auto it = galois_keys.find(elt);
+    if (it == galois_keys.end()) throw std::invalid_argument("Galois key not present");
+    if (ct.size() != 2) throw std::invalid_argument("encrypted size must be 2");
+    Ciphertext out;
+    out.resize(c_, 2, ct.limbs(), s_);
+    apply_galois(c_, ct.data(), ct.limbs(), elt, it->second, out.data(), s_);
+    out.scale() = ct.scale();
+    ct = std::move(out);
+}
+
+void Evaluator::rotate_vector_inplace(Ciphertext &ct, int steps)
+{
+    // rotate_internal with the NAF fallback (evaluator.cpp:2667-2722)
+    if (steps == 0) return;
+    const uint32_t elt = galois_elt(steps);
+    if (galois_keys.count(elt)) {
+        apply_galois_inplace(ct, elt);
+        return;
+    }
+    std::vector<int> parts = naf(steps);
+    if (parts.size() == 1) throw std::invalid_argument("Galois key not present");
+    for (int st : parts)
+        if ((size_t)std::abs(st) != (c_.n >> 1)) rotate_vector_inplace(ct, st);
+}
+
+void Evaluator::rotate_vector(const Ciphertext &ct, int steps, Ciphertext &dest)
+{
+    if (&ct != &dest) dest = ct;
+    rotate_vector_inplace(dest, steps);
+}
+
+void Evaluator::complex_conjugate_inplace(Ciphertext &ct) { apply_galois_inplace(ct, galois_elt(0)); }
+
+}  // namespace nexus

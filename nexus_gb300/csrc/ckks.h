@@ -1,0 +1,185 @@
+// C++ host layer over the engine's kernels: ciphertext / plaintext objects in
+// device memory and an evaluator with SEAL's semantics (scale bookkeeping,
+// level dropping, NAF rotations, the same error conditions), so NEXUS's
+// operators can be written against it call for call.
+//
+// Levels are identified by their number of data limbs (SEAL's parms_id).
+// Every operation is enqueued on the evaluator's stream; device memory comes
+// from the stream-ordered allocator (cudaMallocAsync pool).
+#pragma once
+#include <cstdint>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "context.h"
+
+namespace nexus {
+
+class Encoder;
+
+// Device buffer owned by one object, freed stream-ordered.
+class DeviceBuffer {
+public:
+    DeviceBuffer() = default;
+    ~DeviceBuffer() { release(); }
+    DeviceBuffer(const DeviceBuffer &) = delete;
+    DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+    DeviceBuffer(DeviceBuffer &&o) noexcept { swap(o); }
+    DeviceBuffer &operator=(DeviceBuffer &&o) noexcept
+    {
+        if (this != &o) {
+            release();
+            swap(o);
+        }
+        return *this;
+    }
+    void reserve(size_t words, cudaStream_t s);
+    void release();
+    uint64_t *get() const { return p_; }
+    size_t capacity() const { return words_; }
+
+private:
+    void swap(DeviceBuffer &o) noexcept
+    {
+        std::swap(p_, o.p_);
+        std::swap(words_, o.words_);
+        std::swap(s_, o.s_);
+    }
+    uint64_t *p_ = nullptr;
+    size_t words_ = 0;
+    cudaStream_t s_ = nullptr;
+};
+
+class Ciphertext {
+public:
+    Ciphertext() = default;
+    Ciphertext(const Ciphertext &o);
+    Ciphertext &operator=(const Ciphertext &o);
+    Ciphertext(Ciphertext &&) noexcept = default;
+    Ciphertext &operator=(Ciphertext &&) noexcept = default;
+
+    // allocate for size x limbs (contents undefined)
+    void resize(const Context &c, int size, int limbs, cudaStream_t s);
+    uint64_t *data() const { return buf_.get(); }
+    uint64_t *poly(int i) const { return buf_.get() + (size_t)i * limbs_ * n_; }
+    int size() const { return size_; }
+    int limbs() const { return limbs_; }
+    size_t n() const { return n_; }
+    double &scale() { return scale_; }
+    double scale() const { return scale_; }
+    cudaStream_t stream() const { return s_; }
+    bool empty() const { return size_ == 0; }
+
+private:
+    DeviceBuffer buf_;
+    int size_ = 0, limbs_ = 0;
+    size_t n_ = 0;
+    double scale_ = 1.0;
+    cudaStream_t s_ = nullptr;
+};
+
+// A vector-encoded plaintext lives on the device ([limbs][N], NTT form); a
+// scalar-encoded one (SEAL's encode(double)) is one residue per limb, which
+// SEAL stores in every coefficient of its NTT form.
+class Plaintext {
+public:
+    Plaintext() = default;
+    Plaintext(const Plaintext &o);
+    Plaintext &operator=(const Plaintext &o);
+    Plaintext(Plaintext &&) noexcept = default;
+    Plaintext &operator=(Plaintext &&) noexcept = default;
+    bool is_scalar() const { return scalar_; }
+    int limbs() const { return limbs_; }
+    double &scale() { return scale_; }
+    double scale() const { return scale_; }
+    const uint64_t *data() const { return buf_.get(); }
+    const std::vector<uint64_t> &residues() const { return res_; }
+
+    void set_scalar(std::vector<uint64_t> r, double scale);
+    void set_vector(const Context &c, int limbs, double scale, cudaStream_t s);  // allocates; caller fills data
+    uint64_t *mutable_data() { return buf_.get(); }
+    // keep the first `limbs` limbs (mod_switch_to for a plaintext)
+    void drop_to(int limbs, cudaStream_t s, const Context &c);
+
+private:
+    bool scalar_ = true;
+    int limbs_ = 0;
+    double scale_ = 1.0;
+    std::vector<uint64_t> res_;
+    DeviceBuffer buf_;
+    size_t n_ = 0;
+    cudaStream_t s_ = nullptr;
+};
+
+class Evaluator {
+public:
+    Evaluator(Context &c, cudaStream_t s = nullptr);
+    ~Evaluator();
+    Context &context() { return c_; }
+    cudaStream_t stream() const { return s_; }
+    void set_stream(cudaStream_t s) { s_ = s; }
+    size_t slot_count() const { return c_.n / 2; }
+    int top_limbs() const { return c_.k - 1; }
+    uint64_t modulus(int i) const { return c_.q[i]; }
+
+    // keys (device pointers owned by the caller, SEAL layout [K-1][2][K][N])
+    const uint64_t *relin_key = nullptr;
+    std::map<uint32_t, const uint64_t *> galois_keys;
+
+    // CKKSEncoder
+    void encode(const std::vector<double> &values, int limbs, double scale, Plaintext &out);
+    void encode(double value, int limbs, double scale, Plaintext &out);  // scalar path
+    void encode(double value, double scale, Plaintext &out) { encode(value, top_limbs(), scale, out); }
+    std::vector<double> decode(const Plaintext &pt);
+
+    // level management
+    void mod_switch_to_inplace(Ciphertext &ct, int limbs);
+    void mod_switch_to_inplace(Plaintext &pt, int limbs);
+    void mod_switch_to_next_inplace(Ciphertext &ct) { mod_switch_to_inplace(ct, ct.limbs() - 1); }
+    void rescale_to_next_inplace(Ciphertext &ct);
+
+    // arithmetic
+    void multiply_inplace(Ciphertext &a, const Ciphertext &b);
+    void multiply(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest);
+    void square_inplace(Ciphertext &a) { multiply_inplace(a, a); }
+    void square(const Ciphertext &a, Ciphertext &dest) { multiply(a, a, dest); }
+    void relinearize_inplace(Ciphertext &ct);
+    void add_inplace(Ciphertext &a, const Ciphertext &b);
+    void add(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest);
+    void sub_inplace(Ciphertext &a, const Ciphertext &b);
+    void sub(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest);
+    void negate_inplace(Ciphertext &a);
+    void negate(const Ciphertext &a, Ciphertext &dest);
+    void add_plain_inplace(Ciphertext &ct, const Plaintext &pt);
+    void add_plain(const Ciphertext &ct, const Plaintext &pt, Ciphertext &dest);
+    void sub_plain_inplace(Ciphertext &ct, const Plaintext &pt);
+    void sub_plain(const Ciphertext &ct, const Plaintext &pt, Ciphertext &dest);
+    void multiply_plain_inplace(Ciphertext &ct, const Plaintext &pt);
+    void multiply_plain(const Ciphertext &ct, const Plaintext &pt, Ciphertext &dest);
+
+    // rotations
+    void apply_galois_inplace(Ciphertext &ct, uint32_t elt);
+    void rotate_vector_inplace(Ciphertext &ct, int steps);
+    void rotate_vector(const Ciphertext &ct, int steps, Ciphertext &dest);
+    void complex_conjugate_inplace(Ciphertext &ct);
+    uint32_t galois_elt(int step) const;
+
+    int total_bits(int limbs) const;
+
+private:
+    void check_scale(double scale, int limbs) const;
+    void plain_arith(Ciphertext &ct, const Plaintext &pt, bool sub);
+    Context &c_;
+    cudaStream_t s_;
+    Encoder *enc_ = nullptr;
+    std::vector<int> bits_;
+};
+
+bool are_close(double a, double b);
+std::vector<int> naf(int value);
+
+}  // namespace nexus

@@ -161,6 +161,13 @@ extern "C" int nexus_context_create(int log_n, const uint64_t *moduli, int n_mod
         c.n = 1ull << log_n;
         c.k = n_moduli;
         CK(cudaGetDevice(&c.device));
+        // keep memory freed by stream-ordered deallocation in the pool: the
+        // evaluator allocates and frees ciphertexts on every operation
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, c.device) == cudaSuccess) {
+            uint64_t threshold = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+        }
         c.q.assign(moduli, moduli + n_moduli);
         c.log_n1 = log_n / 2;
         c.log_n2 = log_n - c.log_n1;

@@ -27,6 +27,10 @@ void poly_add_plain(const Context &c, const uint64_t *ct, int polys, int limbs, 
 void poly_mul_scalar(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *scalars,
                      uint64_t *out, cudaStream_t s);
 
+// out = in (+|-) per-limb scalar, one polynomial [limbs][N] (add_plain of a scalar plaintext)
+void poly_add_scalar(const Context &c, const uint64_t *in, int limbs, const uint64_t *scalars, int sub, uint64_t *out,
+                     cudaStream_t s);
+
 // ckks_multiply / ckks_square tensor: out3 = (a0 b0, a0 b1 + a1 b0, a1 b1)
 void tensor(const Context &c, const uint64_t *a, const uint64_t *b, int limbs, uint64_t *out3, cudaStream_t s);
 

@@ -105,6 +105,26 @@ __global__ void k_mul_scalar(const ulonglong2 *__restrict__ ct, const LimbScalar
     }
 }
 
+// out[l] = in[l] (+|-) sc[l] over one polynomial [limbs][N]
+__global__ void k_add_scalar(const ulonglong2 *__restrict__ in, const LimbScalars sc, ulonglong2 *out,
+                             const PrimeConst *__restrict__ pc, int logn, size_t pairs, int sub)
+{
+    FOR_PAIRS(pairs)
+    {
+        const int limb = (int)(pi >> (logn - 1));
+        const uint64_t q = pc[limb].q, w = sc.w[limb].x;
+        ulonglong2 x = in[pi];
+        if (sub) {
+            x.x = sub_mod(x.x, w, q);
+            x.y = sub_mod(x.y, w, q);
+        } else {
+            x.x = add_mod(x.x, w, q);
+            x.y = add_mod(x.y, w, q);
+        }
+        out[pi] = x;
+    }
+}
+
 // ckks_multiply (evaluator.cpp:770-850): out3 = (a0 b0, a0 b1 + a1 b0, a1 b1)
 __global__ void k_tensor(const ulonglong2 *__restrict__ a, const ulonglong2 *__restrict__ b, ulonglong2 *out,
                          const PrimeConst *__restrict__ pc, int limbs, int logn)
@@ -247,6 +267,17 @@ void poly_mul_scalar(const Context &c, const uint64_t *ct, int polys, int limbs,
     size_t pr = pairs_of(c, polys, limbs);
     k_mul_scalar<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)ct, w, (ulonglong2 *)out, c.d_pc, limbs, c.logn,
                                                   pr);
+}
+
+void poly_add_scalar(const Context &c, const uint64_t *in, int limbs, const uint64_t *scalars, int sub, uint64_t *out,
+                     cudaStream_t s)
+{
+    if (limbs > 64) throw std::invalid_argument("at most 64 limbs");
+    LimbScalars w;
+    for (int l = 0; l < limbs; ++l) w.w[l] = make_ulonglong2(scalars[l], 0);
+    size_t pr = pairs_of(c, 1, limbs);
+    k_add_scalar<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, w, (ulonglong2 *)out, c.d_pc, c.logn, pr,
+                                                  sub);
 }
 
 void tensor(const Context &c, const uint64_t *a, const uint64_t *b, int limbs, uint64_t *out3, cudaStream_t s)
