@@ -28,7 +28,7 @@ LIB = OUT / "libseal_shim.so"
 # names compr_mode_type::zstd (a deprecated helper); zstd is compiled out of
 # SEAL here, so that one enumerator is mapped to `none` with -Dzstd=none.
 NEXUS_SRC = NEXUS_TREE / "src"
-NEXUS_OPS = ["ckks_evaluator.cpp", "gelu.cpp", "softmax.cpp", "layer_norm.cpp"]
+NEXUS_OPS = ["ckks_evaluator.cpp", "gelu.cpp", "softmax.cpp", "layer_norm.cpp", "matrix_mul.cpp"]
 
 CONFIG_ON = ["SEAL_USE_STD_BYTE", "SEAL_USE_SHARED_MUTEX", "SEAL_USE_IF_CONSTEXPR", "SEAL_USE_MAYBE_UNUSED",
              "SEAL_USE_NODISCARD", "SEAL_USE_STD_FOR_EACH_N", "SEAL_USE_INTRIN", "SEAL_USE___INT128",

@@ -468,3 +468,73 @@ def layer_norm(ck: CKKSEvaluator, x: Ct, length: int) -> Ct:
     res = ck.invert_sqrt(res, 4, 2)
     x = ev.mod_switch_to(x, res.limbs)
     return ev.rescale(ev.relinearize(ev.multiply(res, x)))
+
+
+def negacyclic_shift(coeffs: np.ndarray, index: int, q_per_limb) -> np.ndarray:
+    """negacyclic_shift_poly_coeffmod (util/polyarithsmallmod.cpp:319-370) on
+    coefficient-form residues [..., limbs, N]: multiply by X^index mod X^N+1."""
+    n = coeffs.shape[-1]
+    out = np.empty_like(coeffs)
+    raw = np.arange(n, dtype=np.int64) + index
+    dst = raw & (n - 1)
+    neg = (raw & n) != 0
+    q = np.array(q_per_limb, dtype=np.uint64).reshape((-1, 1))
+    val = np.where(neg & (coeffs != 0), q - coeffs, coeffs)
+    out[..., dst] = val
+    return out
+
+
+class MMEvaluator:
+    """NEXUS's MMEvaluator (src/matrix_mul.cpp) on the oracle: the ciphertext
+    expansion tree and the ct x pt accumulation, generalised from the
+    hard-coded 768 x 64 shape to R x K."""
+
+    def __init__(self, ck: CKKSEvaluator):
+        self.ck = ck
+        self.ev = ck.ev
+        n = self.ev.n
+        # ckks->rots (src/ckks_evaluator.h:83-85): Galois elements (N + 2^i) / 2^i
+        self.rots = [(n + 2 ** i) // 2 ** i for i in range(int(math.ceil(math.log2(n))))]
+
+    # src/matrix_mul.cpp:131-172
+    def multiply_power_of_x(self, ct: Ct, index: int) -> Ct:
+        oc = self.ev.oc
+        limbs = ct.limbs
+        coeffs = oc.ntt(ct.data, 0, limbs, inverse=True)
+        shifted = negacyclic_shift(coeffs, index, self.ev.q[:limbs])
+        return Ct(oc.ntt(shifted, 0, limbs), ct.scale)
+
+    # src/matrix_mul.cpp:101-129
+    def expand_ciphertext(self, ct: Ct, m: int) -> list:
+        ev = self.ev
+        n = ev.n
+        logm = int(math.ceil(math.log2(m)))
+        temp = [ct]
+        for i in range(logm):
+            newtemp = [None] * (2 * len(temp))
+            index_raw = (n << 1) - (1 << i)
+            index = (index_raw * self.rots[i]) % (n << 1)
+            for a in range(len(temp)):
+                rotated = ev.apply_galois(temp[a], self.rots[i])
+                newtemp[a] = ev.add(temp[a], rotated)
+                shifted = self.multiply_power_of_x(temp[a], index_raw)
+                rshift = self.multiply_power_of_x(rotated, index)
+                newtemp[a + len(temp)] = ev.add(shifted, rshift)
+            temp = newtemp
+        return temp
+
+    # src/matrix_mul.cpp:174-246 after the expansion: output r = sum_k leaf[r*K+k] * pts[k],
+    # scale times the expansion factor, rescaled down to one prime
+    def accumulate(self, leaves: list, pts: list, rows: int, cols: int, factor: float) -> list:
+        ev = self.ev
+        res = []
+        for r in range(rows):
+            terms = [ev.multiply_plain(leaves[r * cols + k], pts[k]) for k in range(cols)]
+            acc = terms[0]
+            for t in terms[1:]:
+                acc = ev.add(acc, t)
+            acc.scale *= factor
+            while acc.limbs > 1:
+                acc = ev.rescale(acc)
+            res.append(acc)
+        return res

@@ -57,6 +57,10 @@ def lib():
         l.sr_decrypt.argtypes = [C.c_void_p, u64p, C.c_int, C.c_double, f64p, C.c_size_t]
         l.sr_nexus_op.argtypes = [C.c_void_p, C.c_int, u64p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
                                   C.c_double, u64p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        l.sr_galois_keys_from_elts.argtypes = [C.c_void_p, C.POINTER(C.c_uint32), C.c_int]
+        l.sr_mm_compress.argtypes = [C.c_void_p, f64p, C.c_double, u64p, f64p]
+        l.sr_mm_power_of_x.argtypes = [C.c_void_p, u64p, C.c_int, C.c_int, u64p]
+        l.sr_mm_expand.argtypes = [C.c_void_p, u64p, C.c_int, C.c_double, C.c_uint32, u64p]
         _lib = l
     return _lib
 
@@ -193,3 +197,24 @@ class SealRef:
         _ck(lib().sr_nexus_op(self._h, self.OPS[op], _p(np.ascontiguousarray(ct)), ct.shape[1], scale, base_scale,
                               a1, a2, f, _p(out), C.byref(ol), C.byref(osc)))
         return np.ascontiguousarray(out.reshape(-1)[: 2 * ol.value * self.n].reshape(2, ol.value, self.n)), osc.value
+
+    def galois_keys_from_elts(self, elts):
+        arr = (C.c_uint32 * len(elts))(*elts)
+        _ck(lib().sr_galois_keys_from_elts(self._h, arr, len(elts)))
+
+    def mm_compress(self, values, scale):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        out = np.zeros((2, self.k - 1, self.n), np.uint64)
+        sc = C.c_double()
+        _ck(lib().sr_mm_compress(self._h, _p(v), scale, _p(out), C.byref(sc)))
+        return out, sc.value
+
+    def mm_power_of_x(self, ct, index):
+        out = np.zeros_like(ct)
+        _ck(lib().sr_mm_power_of_x(self._h, _p(np.ascontiguousarray(ct)), ct.shape[1], index, _p(out)))
+        return out
+
+    def mm_expand(self, ct, scale, m):
+        out = np.zeros((m, 2, ct.shape[1], self.n), np.uint64)
+        _ck(lib().sr_mm_expand(self._h, _p(np.ascontiguousarray(ct)), ct.shape[1], scale, m, _p(out)))
+        return out

@@ -20,6 +20,10 @@
 #include "gelu.h"
 #include "layer_norm.h"
 #include "softmax.h"
+// MMEvaluator keeps its expansion steps private; the shim calls them directly
+#define private public
+#include "matrix_mul.h"
+#undef private
 #include "seal/util/ntt.h"
 #include "seal/util/rlwe.h"
 
@@ -346,6 +350,61 @@ int sr_nexus_op(void *h, int op, const uint64_t *in, int limbs, double in_scale,
         store_ct(s, res, out);
         *out_limbs = (int)res.coeff_modulus_size();
         *out_scale = res.scale();
+    })
+}
+
+// Galois keys for explicit elements (the MatMul expansion uses elements, not steps)
+int sr_galois_keys_from_elts(void *h, const uint32_t *elts, int n)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        s.gk.reset(new GaloisKeys());
+        s.kg->create_galois_keys(std::vector<uint32_t>(elts, elts + n), *s.gk);
+    })
+}
+
+// MMEvaluator::enc_compress_ciphertext (src/matrix_mul.cpp:58-99): N values -> ct at the top level
+int sr_mm_compress(void *h, const double *vals, double scale, uint64_t *out, double *out_scale)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        CKKSEvaluator ck(*s.ctx, *s.encryptor, *s.decryptor, *s.enc, *s.ev, scale, *s.rk, *s.gk);
+        MMEvaluator mm(ck);
+        std::vector<double> v(vals, vals + s.n);
+        Ciphertext ct;
+        mm.enc_compress_ciphertext(v, ct);
+        store_ct(s, ct, out);
+        *out_scale = ct.scale();
+    })
+}
+
+// MMEvaluator::multiply_power_of_x (src/matrix_mul.cpp:131-172)
+int sr_mm_power_of_x(void *h, const uint64_t *in, int limbs, int index, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        CKKSEvaluator ck(*s.ctx, *s.encryptor, *s.decryptor, *s.enc, *s.ev, 1.0, *s.rk, *s.gk);
+        MMEvaluator mm(ck);
+        Ciphertext x, d;
+        load_ct(s, x, in, 2, limbs, 1.0);
+        mm.multiply_power_of_x(x, d, index);
+        store_ct(s, d, out);
+    })
+}
+
+// MMEvaluator::expand_ciphertext (src/matrix_mul.cpp:101-129) with m leaves,
+// galois elements ckks->rots; out [m][2][limbs][N]
+int sr_mm_expand(void *h, const uint64_t *in, int limbs, double scale, uint32_t m, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        CKKSEvaluator ck(*s.ctx, *s.encryptor, *s.decryptor, *s.enc, *s.ev, 1.0, *s.rk, *s.gk);
+        MMEvaluator mm(ck);
+        Ciphertext x;
+        load_ct(s, x, in, 2, limbs, scale);
+        auto leaves = mm.expand_ciphertext(x, m, *s.gk, ck.rots);
+        size_t per = 2 * (size_t)limbs * s.n;
+        for (size_t i = 0; i < leaves.size(); ++i) std::memcpy(out + i * per, leaves[i].data(), per * 8);
     })
 }
 

@@ -77,3 +77,33 @@ def test_naf_and_multi_rotation(env):
     for step in (3, 7, 100, -5):
         assert np.array_equal(ck.ev.rotate(L.Ct(ct, SCALE), step).data, s.rotate(ct, step))
     assert L.naf(7) == [-1, 8] and L.naf(-6) == [2, -8]
+
+
+@pytest.fixture(scope="module")
+def mm_env():
+    log_n, n = 13, 1 << 13
+    qs = po.create_coeff_modulus(n, [60, 40, 60])
+    s = pr.SealRef(log_n, qs, seed=9)
+    rots = [(n + 2 ** i) // 2 ** i for i in range(log_n)]
+    s.galois_keys_from_elts(rots)
+    oc = po.OracleContext(log_n, qs)
+    ev = L.Evaluator(oc, s.relin_key(), {e: s.galois_key(e) for e in rots})
+    return s, L.MMEvaluator(L.CKKSEvaluator(ev, SCALE)), n
+
+
+def test_matmul_power_of_x(mm_env):
+    s, mm, n = mm_env
+    ct, sc = s.mm_compress(np.random.default_rng(0).uniform(-1, 1, n), SCALE)
+    for idx in (0, 1, 5, n - 1, n, n + 3, 2 * n - 1):
+        assert np.array_equal(s.mm_power_of_x(ct, idx), mm.multiply_power_of_x(L.Ct(ct, sc), idx).data)
+
+
+@pytest.mark.parametrize("m", [2, 16, 64])
+def test_matmul_expand(mm_env, m):
+    s, mm, n = mm_env
+    ct, sc = s.mm_compress(np.random.default_rng(m).uniform(-1, 1, n), SCALE)
+    want = s.mm_expand(ct, sc, m)
+    got = mm.expand_ciphertext(L.Ct(ct, sc), m)
+    assert len(got) == m
+    for i in range(m):
+        assert np.array_equal(want[i], got[i].data), i
