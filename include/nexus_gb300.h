@@ -292,6 +292,37 @@ enum { NEXUS_OP_SGN_EVAL = 0, NEXUS_OP_EXP = 1, NEXUS_OP_INVERSE = 2, NEXUS_OP_I
 int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext *x, int a1, int a2, double f,
                   nexus_ciphertext *res);
 
+/* ------------------------------------------------------------------ */
+/* MatMul (src/matrix_mul.cpp in the NEXUS tree)                        */
+/* ------------------------------------------------------------------ */
+
+/* Coefficient packing of the MatMul's compressed operand: coefficient i of
+ * the plaintext is round(values[i] * scale) (i < n <= N, the rest zero),
+ * reduced into the first `limbs` primes and transformed to NTT form.
+ * Replaces: the packing loop of MMEvaluator::enc_compress_ciphertext
+ *   (src/matrix_mul.cpp:72-96, there with scale 1e10 and two primes). */
+int nexus_encode_coefficients(nexus_context *ctx, const double *values, size_t n, double scale, int limbs,
+                              uint64_t *d_out, void *stream);
+
+/* MMEvaluator::multiply_power_of_x (src/matrix_mul.cpp:131-172): res = x * X^index. */
+int nexus_mm_power_of_x(nexus_evaluator *ev, nexus_ciphertext *x, int index, nexus_ciphertext *res);
+
+/* MMEvaluator::expand_ciphertext (src/matrix_mul.cpp:101-129) with the Galois
+ * keys of the elements (N + 2^i) / 2^i registered on ev: the m leaves are
+ * written to d_out [m][2][limbs][N]. */
+int nexus_mm_expand(nexus_evaluator *ev, const nexus_ciphertext *x, uint32_t m, uint64_t *d_out);
+
+/* MMEvaluator::matrix_mul (src/matrix_mul.cpp:174-246), generalised from
+ * 768 x 64: the n_compressed ciphertexts hold a rows x cols matrix flattened
+ * row-major in their coefficients; d_pts [cols][limbs][N] are NTT-form
+ * plaintexts at pt_scale.  res[r] (rows handles, filled) = sum_k
+ * leaf(r*cols + k) * pt_k with scale multiplied by `factor` (the expansion
+ * multiplies by N), rescaled to one prime.  Leaves are accumulated as they are
+ * produced and never all held in memory. */
+int nexus_matrix_mul(nexus_evaluator *ev, nexus_ciphertext *const *compressed, int n_compressed,
+                     const uint64_t *d_pts, double pt_scale, int rows, int cols, double factor,
+                     nexus_ciphertext *const *res);
+
 #ifdef __cplusplus
 }
 #endif

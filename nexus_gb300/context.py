@@ -174,3 +174,8 @@ class Context:
         check(lib().nexus_decrypt(self._h, sk.data_ptr(), ct.data_ptr(), size, limbs, pt.data_ptr(),
                                   _stream_ptr(stream)), "nexus_decrypt")
         return pt
+
+    def encode_coefficients(self, values, scale: float, limbs: int, out, stream=None):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        check(lib().nexus_encode_coefficients(self._h, v.ctypes.data, v.size, float(scale), limbs, out.data_ptr(),
+                                              _stream_ptr(stream)), "nexus_encode_coefficients")

@@ -10,6 +10,7 @@
 #include "ops.h"
 #include "encoder.h"
 
+#include <cmath>
 #include <complex>
 #include <vector>
 
@@ -319,4 +320,34 @@ extern "C" int nexus_decrypt(nexus_context *ctx, const uint64_t *d_sk, const uin
     if (check_ct(fn, ctx, limbs)) return -1;
     if (!d_sk || !d_ct || !d_pt || size < 2 || size > 3) return fail(fn, "null argument or size not 2 or 3");
     return guarded(fn, [&] { decrypt(ctx->c, d_sk, d_ct, size, limbs, d_pt, (cudaStream_t)stream); });
+}
+
+// coefficient packing of MMEvaluator::enc_compress_ciphertext (src/matrix_mul.cpp:72-96)
+extern "C" int nexus_encode_coefficients(nexus_context *ctx, const double *values, size_t n, double scale, int limbs,
+                                         uint64_t *d_out, void *stream)
+{
+    static const char *fn = "nexus_encode_coefficients";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if ((!values && n) || !d_out) return fail(fn, "null argument");
+    if (n > ctx->c.n) return fail(fn, "more values than coefficients");
+    return guarded(fn, [&] {
+        const size_t N = ctx->c.n;
+        std::vector<uint64_t> host((size_t)limbs * N, 0);
+        for (size_t i = 0; i < n; ++i) {
+            const double cd = std::round(values[i] * scale);
+            const bool neg = std::signbit(cd);
+            const double mag = std::fabs(cd);
+            if (mag >= 18446744073709551616.0) throw std::invalid_argument("coefficient does not fit in 64 bits");
+            const uint64_t cu = (uint64_t)mag;
+            for (int j = 0; j < limbs; ++j) {
+                uint64_t r = cu % ctx->c.q[j];
+                host[(size_t)j * N + i] = (neg && r) ? ctx->c.q[j] - r : r;
+            }
+        }
+        cudaStream_t s = (cudaStream_t)stream;
+        if (cudaMemcpyAsync(d_out, host.data(), host.size() * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+            throw std::runtime_error("upload failed");
+        ntt_forward(ctx->c, d_out, 1, 0, limbs, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) throw std::runtime_error("stream synchronize failed");
+    });
 }

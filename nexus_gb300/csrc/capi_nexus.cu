@@ -176,3 +176,47 @@ extern "C" int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext
         }
     });
 }
+
+extern "C" int nexus_mm_power_of_x(nexus_evaluator *ev, nexus_ciphertext *x, int index, nexus_ciphertext *res)
+{
+    static const char *fn = "nexus_mm_power_of_x";
+    if (!ev || !x || !res) return fail(fn, "null argument");
+    return guarded(fn, [&] {
+        MMEvaluator mm(ev->ck);
+        mm.multiply_power_of_x(x->ct, res->ct, index);
+    });
+}
+
+extern "C" int nexus_mm_expand(nexus_evaluator *ev, const nexus_ciphertext *x, uint32_t m, uint64_t *d_out)
+{
+    static const char *fn = "nexus_mm_expand";
+    if (!ev || !x || !d_out) return fail(fn, "null argument");
+    if (m < 1 || (m & (m - 1)) || m > ev->ctx->c.n) return fail(fn, "m must be a power of two <= N");
+    return guarded(fn, [&] {
+        MMEvaluator mm(ev->ck);
+        auto leaves = mm.expand_ciphertext(x->ct, m);
+        const size_t per = (size_t)2 * x->ct.limbs() * ev->ctx->c.n;
+        for (size_t i = 0; i < leaves.size(); ++i)
+            cudaMemcpyAsync(d_out + i * per, leaves[i].data(), per * 8, cudaMemcpyDeviceToDevice, ev->ev.stream());
+    });
+}
+
+extern "C" int nexus_matrix_mul(nexus_evaluator *ev, nexus_ciphertext *const *compressed, int n_compressed,
+                                const uint64_t *d_pts, double pt_scale, int rows, int cols, double factor,
+                                nexus_ciphertext *const *res)
+{
+    static const char *fn = "nexus_matrix_mul";
+    if (!ev || !compressed || !d_pts || !res || n_compressed < 1) return fail(fn, "null argument");
+    for (int i = 0; i < n_compressed; ++i)
+        if (!compressed[i]) return fail(fn, "null compressed ciphertext");
+    for (int r = 0; r < rows; ++r)
+        if (!res[r]) return fail(fn, "null result handle");
+    return guarded(fn, [&] {
+        MMEvaluator mm(ev->ck);
+        std::vector<const Ciphertext *> cp;
+        for (int i = 0; i < n_compressed; ++i) cp.push_back(&compressed[i]->ct);
+        std::vector<Ciphertext> out;
+        mm.matrix_mul(cp, d_pts, pt_scale, rows, cols, factor, out);
+        for (int r = 0; r < rows; ++r) res[r]->ct = std::move(out[r]);
+    });
+}

@@ -30,16 +30,18 @@ inline unsigned grid_for(size_t n)
     return (unsigned)(g > 1048576 ? 1048576 : g);
 }
 
-// D[j][i'][n] = t[j][n] mod q(i') for i' in [0, l], q(l) = special prime
+// D[b][j][i'][n] = t[b][j][n] mod q(i') for i' in [0, l], q(l) = special prime;
+// rows of t are (b, j) pairs, b < batch
 __global__ void k_modup_spread(const uint64_t *__restrict__ t, uint64_t *__restrict__ D,
                                const PrimeConst *__restrict__ pc, int l, int sp, int logn, size_t total)
 {
     for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
-        const int j = (int)(x >> logn);
+        const size_t row = x >> logn;
+        const int j = (int)(row % (size_t)l);
         const size_t n = x & (((size_t)1 << logn) - 1);
         const uint64_t v = t[x];
         const uint64_t qj = pc[j].q;
-        uint64_t *o = D + ((size_t)j * (l + 1) << logn) + n;
+        uint64_t *o = D + ((row * (l + 1)) << logn) + n;
         for (int i = 0; i <= l; ++i) {
             const PrimeConst P = pc[i == l ? sp : i];
             o[(size_t)i << logn] = (P.q < qj) ? barrett_64(v, P.q, P.r1) : v;
@@ -52,18 +54,20 @@ __device__ __forceinline__ void mac128(uint64_t &lo, uint64_t &hi, uint64_t a, u
     asm("mad.lo.cc.u64 %0, %2, %3, %0;\n\tmadc.hi.u64 %1, %2, %3, %1;" : "+l"(lo), "+l"(hi) : "l"(a), "l"(b));
 }
 
-// P[k][i'][n] = sum_j D[j][i'][n] * key[j][k][kidx(i')][n] mod q(i')
+// P[b][k][i'][n] = sum_j D[b][j][i'][n] * key[j][k][kidx(i')][n] mod q(i')
 __global__ void k_ks_inner(const uint64_t *__restrict__ D, const uint64_t *__restrict__ key, uint64_t *__restrict__ P,
                            const PrimeConst *__restrict__ pc, int l, int K, int logn, size_t total)
 {
     const size_t N = (size_t)1 << logn;
     for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
-        const int i = (int)(x >> logn);  // 0..l
+        const size_t row = x >> logn;            // b*(l+1) + i
+        const size_t b = row / (size_t)(l + 1);
+        const int i = (int)(row % (size_t)(l + 1));
         const size_t n = x & (N - 1);
         const int kidx = (i == l) ? K - 1 : i;
         const PrimeConst P0 = pc[kidx];
         uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
-        const uint64_t *d = D + ((size_t)i << logn) + n;
+        const uint64_t *d = D + ((b * l * (l + 1) + i) << logn) + n;
         const uint64_t *k0 = key + ((size_t)kidx << logn) + n;
         const size_t dstride = (size_t)(l + 1) << logn;
         const size_t kstride = (size_t)2 * K << logn;
@@ -73,12 +77,14 @@ __global__ void k_ks_inner(const uint64_t *__restrict__ D, const uint64_t *__res
             mac128(lo0, hi0, dv, k0[j * kstride]);
             mac128(lo1, hi1, dv, k0[j * kstride + kcomp]);
         }
-        P[((size_t)i << logn) + n] = barrett_128(lo0, hi0, P0.q, P0.r0, P0.r1);
-        P[((size_t)(l + 1 + i) << logn) + n] = barrett_128(lo1, hi1, P0.q, P0.r0, P0.r1);
+        uint64_t *pb = P + ((b * 2 * (l + 1)) << logn);
+        pb[((size_t)i << logn) + n] = barrett_128(lo0, hi0, P0.q, P0.r0, P0.r1);
+        pb[((size_t)(l + 1 + i) << logn) + n] = barrett_128(lo1, hi1, P0.q, P0.r0, P0.r1);
     }
 }
 
-// ct[k][i] += (P[k][i] - T[k][i]) * p^{-1} mod q_i ; T[k][i] in [0, q_i)
+// ct[kb][i] += (P[kb][i] - T[kb][i]) * p^{-1} mod q_i with kb = 2*b + k over the
+// batch; T[kb][i] in [0, q_i)
 __global__ void k_moddown_finish(uint64_t *__restrict__ ct, const uint64_t *__restrict__ P,
                                  const uint64_t *__restrict__ T, const PrimeConst *__restrict__ pc,
                                  const ulonglong2 *__restrict__ inv_p, int l, int logn, size_t total)
@@ -97,34 +103,41 @@ __global__ void k_moddown_finish(uint64_t *__restrict__ ct, const uint64_t *__re
 
 }  // namespace
 
-void switch_key(Context &c, uint64_t *ct, int l, const uint64_t *target, const uint64_t *key, cudaStream_t s)
+void switch_key_batch(Context &c, uint64_t *ct, int batch, int l, const uint64_t *target, const uint64_t *key,
+                      cudaStream_t s)
 {
     if (l < 1 || l > c.k - 1) throw std::invalid_argument("switch_key: level out of range");
-    const size_t N = c.n;
+    if (batch < 1) return;
+    const size_t N = c.n, B = (size_t)batch;
     const int sp = c.k - 1;
-    // scratch: t[l] | D[l][l+1] | P[2][l+1] | T[2][l] | last[2]
-    const size_t words = N * ((size_t)l + (size_t)l * (l + 1) + 2 * (size_t)(l + 1) + 2 * (size_t)l + 2);
+    // scratch per ciphertext: t[l] | D[l][l+1] | P[2][l+1] | T[2][l] | last[2]
+    const size_t words = B * N * ((size_t)l + (size_t)l * (l + 1) + 2 * (size_t)(l + 1) + 2 * (size_t)l + 2);
     uint64_t *t = c.get_scratch(words);
-    uint64_t *D = t + (size_t)l * N;
-    uint64_t *P = D + (size_t)l * (l + 1) * N;
-    uint64_t *T = P + 2 * (size_t)(l + 1) * N;
-    uint64_t *last = T + 2 * (size_t)l * N;
+    uint64_t *D = t + B * l * N;
+    uint64_t *P = D + B * l * (l + 1) * N;
+    uint64_t *T = P + B * 2 * (l + 1) * N;
+    uint64_t *last = T + B * 2 * l * N;
 
-    cudaMemcpyAsync(t, target, sizeof(uint64_t) * l * N, cudaMemcpyDeviceToDevice, s);
-    ntt_inverse(c, t, 1, LimbMap{l, 0, -1}, s);
-    size_t tot = (size_t)l * N;
+    cudaMemcpyAsync(t, target, sizeof(uint64_t) * B * l * N, cudaMemcpyDeviceToDevice, s);
+    ntt_inverse(c, t, B, LimbMap{l, 0, -1}, s);
+    size_t tot = B * l * N;
     k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot);
-    ntt_forward(c, D, l, LimbMap{l + 1, 0, sp}, s);
-    tot = (size_t)(l + 1) * N;
+    ntt_forward(c, D, B * l, LimbMap{l + 1, 0, sp}, s);
+    tot = B * (l + 1) * N;
     k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, tot);
-    // ModDown: special limbs of both components to coefficient form
-    cudaMemcpyAsync(last, P + (size_t)l * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(last + N, P + (size_t)(2 * l + 1) * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
-    ntt_inverse(c, last, 2, LimbMap{1, sp, -1}, s);
-    launch_round_spread(c, last, T, 2, sp, l, s);
-    ntt_forward(c, T, 2, LimbMap{l, 0, -1}, s);
-    tot = (size_t)2 * l * N;
+    // ModDown: the special limb of every (ciphertext, component) to coefficient form
+    cudaMemcpy2DAsync(last, N * 8, P + (size_t)l * N, (size_t)(l + 1) * N * 8, N * 8, 2 * B,
+                      cudaMemcpyDeviceToDevice, s);
+    ntt_inverse(c, last, 2 * B, LimbMap{1, sp, -1}, s);
+    launch_round_spread(c, last, T, (int)(2 * B), sp, l, s);
+    ntt_forward(c, T, 2 * B, LimbMap{l, 0, -1}, s);
+    tot = B * 2 * l * N;
     k_moddown_finish<<<grid_for(tot), kBlock, 0, s>>>(ct, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn, tot);
+}
+
+void switch_key(Context &c, uint64_t *ct, int l, const uint64_t *target, const uint64_t *key, cudaStream_t s)
+{
+    switch_key_batch(c, ct, 1, l, target, key, s);
 }
 
 void relinearize(Context &c, const uint64_t *ct3, int l, const uint64_t *key, uint64_t *out2, cudaStream_t s)

@@ -69,4 +69,26 @@ private:
     CKKSEvaluator *ckks;
 };
 
+// MMEvaluator (src/matrix_mul.{h,cpp}): ct x pt MatMul through the ciphertext
+// expansion tree; see matmul.cu for the GPU form.
+class MMEvaluator {
+public:
+    explicit MMEvaluator(CKKSEvaluator &ckks);
+    std::vector<uint32_t> rots;  // ckks->rots: Galois elements (N + 2^i) / 2^i
+
+    void multiply_power_of_x(Ciphertext &encrypted, Ciphertext &destination, int index);
+    std::vector<Ciphertext> expand_ciphertext(const Ciphertext &encrypted, uint32_t m);
+    // res[r] = sum_k leaf(r*cols + k) * pts[k] over the expanded compressed
+    // ciphertexts, scale *= factor, rescaled to one prime
+    void matrix_mul(const std::vector<Ciphertext> &compressed, const std::vector<Plaintext> &pts, int rows, int cols,
+                    double factor, std::vector<Ciphertext> &res, int subtree_depth = 6);
+    // the same with the plaintexts already stacked on the device, d_pts[cols][l][N] at pt_scale
+    void matrix_mul(const std::vector<const Ciphertext *> &compressed, const uint64_t *d_pts, double pt_scale,
+                    int rows, int cols, double factor, std::vector<Ciphertext> &res, int subtree_depth = 6);
+
+private:
+    const uint64_t *key_for(uint32_t elt) const;
+    CKKSEvaluator *ckks;
+};
+
 }  // namespace nexus

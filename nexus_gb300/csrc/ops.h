@@ -49,6 +49,11 @@ void galois_permute(Context &c, const uint64_t *in, int polys, int limbs, uint32
 // switch_key_inplace: ct[2][limbs] += key-switch(target[limbs])
 void switch_key(Context &c, uint64_t *ct, int limbs, const uint64_t *target, const uint64_t *key, cudaStream_t s);
 
+// the same for `batch` ciphertexts ct[batch][2][limbs] and targets[batch][limbs]
+// sharing one key (the key is read once per launch, not once per ciphertext)
+void switch_key_batch(Context &c, uint64_t *ct, int batch, int limbs, const uint64_t *target, const uint64_t *key,
+                      cudaStream_t s);
+
 // relinearize a size-3 ciphertext into out2 (may alias ct3)
 void relinearize(Context &c, const uint64_t *ct3, int limbs, const uint64_t *key, uint64_t *out2, cudaStream_t s);
 

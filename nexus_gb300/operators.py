@@ -120,3 +120,25 @@ class Evaluator:
 
     def invert_sqrt(self, x, d_newt=5, d_gold=2):
         return self._op(OP_INVERT_SQRT, x, d_newt, d_gold)
+
+    # ---- MatMul (src/matrix_mul.cpp) ------------------------------------------
+    def mm_power_of_x(self, x: Ciphertext, index: int) -> Ciphertext:
+        res = Ciphertext(self.ctx)
+        check(lib().nexus_mm_power_of_x(self._h, x.handle, int(index), res.handle), "nexus_mm_power_of_x")
+        return res
+
+    def mm_expand(self, x: Ciphertext, m: int):
+        import torch
+        _, limbs, _, _ = x.info()
+        out = torch.empty((m, 2, limbs, self.ctx.n), dtype=torch.int64, device="cuda")
+        check(lib().nexus_mm_expand(self._h, x.handle, int(m), out.data_ptr()), "nexus_mm_expand")
+        return out
+
+    def matrix_mul(self, compressed, pts, pt_scale: float, rows: int, cols: int, factor: float):
+        """compressed: list of Ciphertext; pts: CUDA int64 tensor [cols][limbs][N]."""
+        comp = (C.c_void_p * len(compressed))(*[c.handle.value for c in compressed])
+        res = [Ciphertext(self.ctx) for _ in range(rows)]
+        out = (C.c_void_p * rows)(*[r.handle.value for r in res])
+        check(lib().nexus_matrix_mul(self._h, comp, len(compressed), pts.data_ptr(), float(pt_scale), int(rows),
+                                     int(cols), float(factor), out), "nexus_matrix_mul")
+        return res
