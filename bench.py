@@ -5,6 +5,15 @@
 
 Prints ONE JSON line (rank 0).  Workloads:
 
+  matmul (default) NEXUS's ct x pt MatMul at the BERT-base shape: an encrypted
+        128 x 768 input of N(0,1), coefficient-packed into 2 ciphertexts,
+        times plaintext weights 768 x 768 of N(0, 0.02) plus a bias of 768,
+        at N = 2^16 with primes {60, 40, 60} (one 60-bit special prime), scale
+        2^40; one step = one full MatMul (expansion tree of 2 x 65535 Galois
+        key switches, 98304 ct x pt products, 128 rescales, bias).  Weights
+        (768 MB of plaintexts) and keys stay resident; the working set is far
+        larger than L2, so no flush is needed.
+
   ntt   Batched forward negacyclic NTT at N=2^16 over 24 primes of 60 bits
         (CoeffModulus::Create(65536, 24 x 60)), 64 ciphertexts x 2 polynomials
         of uniform residues = 3072 limb-NTTs per step, one engine call per
@@ -244,6 +253,215 @@ def cpu_ntt_sample(budget_s: float = 10.0, threads: int | None = None):
             "sample": f"{done} limb-NTTs (N=2^16, 60-bit primes) in {el:.1f} s"}
 
 
+# ----------------------------------------------------------------------------- MatMul workload
+
+MM_LOGN = 16
+MM_ROWS, MM_COLS, MM_OUT = 128, 768, 768
+MM_PT_SCALE = 2.0 ** 40
+MM_PACK_SCALE = 1e10  # enc_compress_ciphertext's fixed scale
+
+
+def mm_config():
+    return {"workload": "matmul_bert_128x768x768_n65536", "N": 1 << MM_LOGN, "moduli_bits": [60, 40, 60],
+            "X": [MM_ROWS, MM_COLS], "W": [MM_COLS, MM_OUT], "bias": MM_OUT, "compressed_cts": 2,
+            "galois_keys": MM_LOGN, "parallelism": "replicas",
+            "l2": "working set (768 MB of weight plaintexts + expansion) far above L2, no flush"}
+
+
+def run_mm_gpu(args, rank, world):
+    import numpy as np
+    import torch
+
+    import nexus_gb300 as ng
+    from nexus_gb300.operators import Ciphertext, Evaluator
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = 1 << MM_LOGN
+    qs = ng.create_coeff_modulus(n, [60, 40, 60])
+    ctx = ng.Context(MM_LOGN, qs)
+    sk = ctx.keygen_secret(seed=11 + rank)
+    rots = [(n + 2 ** i) // 2 ** i for i in range(MM_LOGN)]
+    gks = {e: ctx.keygen_galois(sk, e, seed=100 + i) for i, e in enumerate(rots)}
+    ev = Evaluator(ctx, MM_PT_SCALE, None, gks)
+    rng = np.random.default_rng(2024 + rank)
+    X = rng.normal(0, 1, (MM_ROWS, MM_COLS))
+    W = rng.normal(0, 0.02, (MM_COLS, MM_OUT))
+    b = rng.normal(0, 0.02, MM_OUT)
+    pts = torch.empty((MM_COLS, 2, n), dtype=torch.int64, device=dev)
+    for k in range(MM_COLS):
+        ctx.encode(W[k], MM_PT_SCALE, 2, pts[k])
+    flat = X.reshape(-1)
+    packs, host_packs = [], []
+    for i in range((flat.size + n - 1) // n):
+        ct = ctx.encrypt_symmetric(sk, None, 2, 50 + i)
+        pt = torch.empty((2, n), dtype=torch.int64, device=dev)
+        ctx.encode_coefficients(flat[i * n:(i + 1) * n], MM_PACK_SCALE, 2, pt)
+        c0 = ct[0:1].clone()
+        ctx.plain_op(c0, pt, 1, ct[0:1])
+        packs.append(Ciphertext.from_device(ctx, ct, MM_PACK_SCALE))
+        host_packs.append(ct.cpu().numpy().view(np.uint64).copy())
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        return ev.matrix_mul(packs, pts, MM_PT_SCALE, MM_ROWS, MM_COLS, float(n), bias=b)
+
+    for _ in range(args.warmup):
+        res = step()
+    torch.cuda.synchronize(dev)
+    # accuracy of the last warm-up result against FP64 X.W + b (a few rows)
+    Y = X @ W + b
+    err = 0.0
+    for r in (0, 63, 127):
+        dec = ctx.decode(ctx.decrypt(sk, res[r].to_device()), res[r].scale).real[:MM_OUT]
+        err = max(err, float(np.max(np.abs(dec - Y[r]))))
+    del res
+    barrier(world)
+    l0 = ng.kernel_launches()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize(dev)
+        t0.record(stream)
+        for _ in range(args.steps):
+            res = step()
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = ng.kernel_launches() - l0
+    barrier(world)
+    total_ms = max_over_ranks(t0.elapsed_time(t1), world)
+    del res
+
+    # one instrumented step: CUDA events around every NTT launch
+    ctx.ntt_timing_begin()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    res = step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ntt_ms, ntt_calls, ntt_limbs = ctx.ntt_timing_end()
+    instr_ms = e0.elapsed_time(e1)
+    del res
+
+    # end to end through the C ABI: packed ciphertexts from pinned host memory,
+    # MatMul, all 128 output ciphertexts back to the host
+    e2e_steps = max(1, min(args.steps, 3))
+    h_in = [torch.from_numpy(hp.view(np.int64)).pin_memory() for hp in host_packs]
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    w0 = time.perf_counter()
+    out_bytes = 0
+    for _ in range(e2e_steps):
+        loaded = []
+        for hp in h_in:
+            c = Ciphertext(ctx)
+            ng.check(ng.lib().nexus_ciphertext_load(c.handle, hp.data_ptr(), hp.shape[0], hp.shape[1],
+                                                    MM_PACK_SCALE, 1, None), "load")
+            loaded.append(c)
+        out = ev.matrix_mul(loaded, pts, MM_PT_SCALE, MM_ROWS, MM_COLS, float(n), bias=b)
+        out_bytes = 0
+        for c in out:
+            a = c.to_numpy()
+            out_bytes += a.nbytes
+    torch.cuda.synchronize(dev)
+    e2e_s = max_over_ranks(time.perf_counter() - w0, world)
+    in_bytes = sum(hp.nbytes for hp in host_packs)
+
+    step_ms = total_ms / args.steps
+    value = world * args.steps / (total_ms / 1e3)
+    peak, peak_kind = _peak_hbm()
+    ntt_avg_ms = ntt_ms / max(1, ntt_calls)
+    alg_bytes_per_call = 16.0 * n * ntt_limbs / max(1, ntt_calls)
+    achieved = alg_bytes_per_call / (ntt_avg_ms / 1e3) / 1e9
+    res = {
+        "metric": "bert_matmul_128x768x768_throughput",
+        "value": value,
+        "unit": "matmul/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic: X ~ N(0,1), W ~ N(0,0.02), b ~ N(0,0.02), seeded; engine-generated keys",
+        "config": mm_config(),
+        "accuracy": {"max_abs_err_vs_fp64": err, "rows_checked": [0, 63, 127]},
+        "roofline": {
+            "kernel": "nexus NTT launches inside the MatMul (k_fwd/k_inv cols+rows)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": alg_bytes_per_call,
+            "avg_launch_ms": ntt_avg_ms, "launches_per_step": ntt_calls, "limb_ntts_per_step": ntt_limbs,
+            "share_of_step": ntt_ms / instr_ms,
+            "traffic": _profile_traffic("matmul_bert_128x768x768_n65536"),
+        },
+        "e2e": {"value": world * e2e_steps / e2e_s, "unit": "matmul/s", "h2d_bytes_per_step": in_bytes,
+                "d2h_bytes_per_step": out_bytes},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+    }
+    if rank == 0 and world == 1:
+        res["cpu_baseline"] = cpu_mm_sample(workers=1, depth=args.cpu_depth)
+    return res
+
+
+def _mm_cpu_worker(args):
+    """Expand one subtree of `depth` levels of the MatMul tree with the oracle
+    port at N=2^16 and accumulate its leaves; returns (seconds, nodes, macs)."""
+    depth, seed = args
+    import numpy as np
+
+    from oracle import nexus_l3 as L
+    from oracle import pyoracle as po
+    n = 1 << MM_LOGN
+    qs = po.create_coeff_modulus(n, [60, 40, 60])
+    oc = po.OracleContext(MM_LOGN, qs)
+    rng = np.random.default_rng(seed)
+    rots = [(n + 2 ** i) // 2 ** i for i in range(MM_LOGN)]
+    # random keys cost exactly what real ones do (no decryption happens here)
+    keys = {e: po.random_residues(rng, (2, 2, 3, n), qs) for e in rots[:depth]}
+    ev = L.Evaluator(oc, None, keys)
+    mm = L.MMEvaluator(L.CKKSEvaluator(ev, MM_PT_SCALE))
+    ct = L.Ct(po.random_residues(rng, (2, 2, n), qs[:2]), MM_PACK_SCALE)
+    pts = [L.Pt(MM_PT_SCALE, data=po.random_residues(rng, (2, n), qs[:2])) for _ in range(1 << depth)]
+    t = time.perf_counter()
+    leaves = mm.expand_ciphertext(ct, 1 << depth)
+    t_exp = time.perf_counter() - t
+    t = time.perf_counter()
+    acc = ev.multiply_plain(leaves[0], pts[0])
+    for i in range(1, len(leaves)):
+        acc = ev.add(acc, ev.multiply_plain(leaves[i], pts[i]))
+    t_mac = time.perf_counter() - t
+    return t_exp, (1 << depth) - 1, t_mac, len(leaves)
+
+
+def cpu_mm_sample(workers: int = 1, depth: int = 7):
+    """The oracle port on the host cores: a bounded sample (one expansion
+    subtree per worker plus its leaf accumulation), extrapolated to the full
+    BERT-shape MatMul (2 x 65535 tree nodes, 98304 leaf products)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    n = 1 << MM_LOGN
+    w0 = time.perf_counter()
+    if workers <= 1:
+        outs = [_mm_cpu_worker((depth, 0))]
+    else:
+        with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            outs = list(ex.map(_mm_cpu_worker, [(depth, i) for i in range(workers)]))
+    wall = time.perf_counter() - w0
+    t_node = statistics.mean(o[0] / o[1] for o in outs)
+    t_mac = statistics.mean(o[2] / o[3] for o in outs)
+    total_1 = 2 * (n - 1) * t_node + MM_ROWS * MM_COLS * t_mac
+    value = workers / total_1
+    return {"value": value, "unit": "matmul/s", "cores": workers, "kind": "port",
+            "sample": f"{workers} worker(s) x one {1 << depth}-leaf expansion subtree + accumulation at N=2^16 "
+                      f"({wall:.1f} s wall; {t_node * 1e3:.1f} ms/node, {t_mac * 1e3:.2f} ms/leaf product), "
+                      f"extrapolated to 2 x 65535 nodes + 98304 products"}
+
+
 # ----------------------------------------------------------------------------- plumbing
 
 def barrier(world):
@@ -266,19 +484,48 @@ def main():
     global NTT_CTS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["nexus", "reference"], default="nexus")
-    ap.add_argument("--workload", choices=["ntt"], default="ntt")
+    ap.add_argument("--workload", choices=["matmul", "ntt"], default="matmul")
+    ap.add_argument("--cpu-depth", type=int, default=7, help="expansion-subtree depth of the MatMul CPU sample")
+    ap.add_argument("--mm-rows", type=int, default=128,
+                    help="rows of the encrypted input (smaller values are for profiling captures only)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ntt-cts", type=int, default=64,
                     help="ciphertexts per step (smaller values are for profiling captures only)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     NTT_CTS = args.ntt_cts
+    global MM_ROWS
+    MM_ROWS = args.mm_rows
+    if args.steps is None:
+        args.steps = 5 if args.workload == "matmul" else 20
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+
+    if args.impl == "reference" and args.workload == "matmul":
+        if rank != 0:
+            return
+        workers = max(1, os.cpu_count() or 1)
+        vals = []
+        for i in range(args.warmup + args.steps):
+            r = cpu_mm_sample(workers=workers, depth=max(3, args.cpu_depth - 2))
+            if i >= args.warmup:
+                vals.append(r)
+        value = statistics.mean(r["value"] for r in vals)
+        res = {
+            "impl": "reference", "metric": "bert_matmul_128x768x768_throughput", "value": value, "unit": "matmul/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (random residues; cost is data-independent)", "config": mm_config(),
+            "cpu_baseline": {"value": value, "unit": "matmul/s", "cores": workers, "kind": "port",
+                             "sample": "per step: " + vals[0]["sample"]},
+            "e2e": {"value": value, "unit": "matmul/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(res), flush=True)
+        return
 
     if args.impl == "reference":
         if rank != 0:
@@ -308,7 +555,7 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
-    res = run_ntt_gpu(args, rank, world)
+    res = run_mm_gpu(args, rank, world) if args.workload == "matmul" else run_ntt_gpu(args, rank, world)
     if rank == 0:
         print(json.dumps(res), flush=True)
     if world > 1:

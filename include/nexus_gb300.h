@@ -26,6 +26,11 @@ typedef struct nexus_context nexus_context;
 /* Message of the calling thread's last failed call ("" if none). */
 const char *nexus_last_error(void);
 
+/* Number of GPU kernels this library has launched in the process so far
+ * (for benchmarks that report their own launch counts).  No counterpart in
+ * the reference. */
+uint64_t nexus_kernel_launches(void);
+
 /*
  * Primes for a coefficient modulus: out[i] is a prime of bit_sizes[i] bits,
  * congruent to 1 mod 2*poly_degree, chosen exactly as SEAL chooses them.
@@ -70,6 +75,15 @@ int nexus_ntt_forward(nexus_context *ctx, uint64_t *d_data, size_t n_polys, int 
  */
 int nexus_ntt_inverse(nexus_context *ctx, uint64_t *d_data, size_t n_polys, int limb_begin, int limb_end,
                       void *stream);
+
+/*
+ * Measurement hooks: between begin and end every NTT call (forward or
+ * inverse, any caller) on this context records a CUDA event pair on its
+ * stream; end synchronises and returns the summed device time, the number of
+ * calls and the number of limb-NTTs.  No counterpart in the reference.
+ */
+int nexus_ntt_timing_begin(nexus_context *ctx);
+int nexus_ntt_timing_end(nexus_context *ctx, double *total_ms, uint64_t *calls, uint64_t *limbs);
 
 /* ------------------------------------------------------------------ */
 /* CKKS ciphertext arithmetic (NTT form, limbs = data primes 0..limbs-1) */
@@ -317,11 +331,13 @@ int nexus_mm_expand(nexus_evaluator *ev, const nexus_ciphertext *x, uint32_t m, 
  * row-major in their coefficients; d_pts [cols][limbs][N] are NTT-form
  * plaintexts at pt_scale.  res[r] (rows handles, filled) = sum_k
  * leaf(r*cols + k) * pt_k with scale multiplied by `factor` (the expansion
- * multiplies by N), rescaled to one prime.  Leaves are accumulated as they are
- * produced and never all held in memory. */
+ * multiplies by N), rescaled to one prime; bias (bias_len slot values, may
+ * be NULL) is then encoded at the output level and scale and added to every
+ * row.  Leaves are accumulated as they are produced and never all held in
+ * memory. */
 int nexus_matrix_mul(nexus_evaluator *ev, nexus_ciphertext *const *compressed, int n_compressed,
-                     const uint64_t *d_pts, double pt_scale, int rows, int cols, double factor,
-                     nexus_ciphertext *const *res);
+                     const uint64_t *d_pts, double pt_scale, int rows, int cols, double factor, const double *bias,
+                     int bias_len, nexus_ciphertext *const *res);
 
 #ifdef __cplusplus
 }

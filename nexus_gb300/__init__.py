@@ -6,4 +6,4 @@ The compute path is hand-written sm_103a CUDA behind the C ABI declared in
 ctypes layer used by the tests and the benchmark.
 """
 from ._lib import NexusError, check, lib  # noqa: F401
-from .context import Context, create_coeff_modulus  # noqa: F401
+from .context import Context, create_coeff_modulus, kernel_launches  # noqa: F401

@@ -16,12 +16,16 @@ u64p = C.POINTER(C.c_uint64)
 # (name, restype, argtypes) of every exported entry point
 SIGNATURES = [
     ("nexus_last_error", C.c_char_p, []),
+    ("nexus_kernel_launches", C.c_uint64, []),
     ("nexus_create_coeff_modulus", C.c_int, [C.c_uint64, C.POINTER(C.c_int), C.c_int, u64p]),
     ("nexus_context_create", C.c_int, [C.c_int, u64p, C.c_int, C.POINTER(C.c_void_p)]),
     ("nexus_context_destroy", C.c_int, [C.c_void_p]),
     ("nexus_context_get_psi", C.c_int, [C.c_void_p, u64p]),
     ("nexus_ntt_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int, C.c_int, C.c_void_p]),
     ("nexus_ntt_inverse", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int, C.c_int, C.c_void_p]),
+    ("nexus_ntt_timing_begin", C.c_int, [C.c_void_p]),
+    ("nexus_ntt_timing_end", C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64),
+                                       C.POINTER(C.c_uint64)]),
     ("nexus_multiply", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     ("nexus_rescale", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     ("nexus_switch_key", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -64,7 +68,7 @@ SIGNATURES = [
     ("nexus_mm_power_of_x", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("nexus_mm_expand", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     ("nexus_matrix_mul", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_int, C.c_int,
-                                   C.c_double, C.c_void_p]),
+                                   C.c_double, C.c_void_p, C.c_int, C.c_void_p]),
     ("nexus_plain_op", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
 ]

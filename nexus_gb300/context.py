@@ -179,3 +179,16 @@ class Context:
         v = np.ascontiguousarray(values, dtype=np.float64)
         check(lib().nexus_encode_coefficients(self._h, v.ctypes.data, v.size, float(scale), limbs, out.data_ptr(),
                                               _stream_ptr(stream)), "nexus_encode_coefficients")
+
+    # ---- measurement ---------------------------------------------------------
+    def ntt_timing_begin(self):
+        check(lib().nexus_ntt_timing_begin(self._h), "nexus_ntt_timing_begin")
+
+    def ntt_timing_end(self):
+        ms, calls, limbs = C.c_double(), C.c_uint64(), C.c_uint64()
+        check(lib().nexus_ntt_timing_end(self._h, C.byref(ms), C.byref(calls), C.byref(limbs)), "nexus_ntt_timing_end")
+        return ms.value, calls.value, limbs.value
+
+
+def kernel_launches() -> int:
+    return int(lib().nexus_kernel_launches())

@@ -351,3 +351,39 @@ extern "C" int nexus_encode_coefficients(nexus_context *ctx, const double *value
         if (cudaStreamSynchronize(s) != cudaSuccess) throw std::runtime_error("stream synchronize failed");
     });
 }
+
+extern "C" int nexus_ntt_timing_begin(nexus_context *ctx)
+{
+    if (!ctx) return fail("nexus_ntt_timing_begin", "null context");
+    for (auto e : ctx->c.ntt_events) cudaEventDestroy(e);
+    ctx->c.ntt_events.clear();
+    ctx->c.ntt_limbs.clear();
+    ctx->c.ntt_timing = true;
+    return 0;
+}
+
+extern "C" int nexus_ntt_timing_end(nexus_context *ctx, double *total_ms, uint64_t *calls, uint64_t *limbs)
+{
+    static const char *fn = "nexus_ntt_timing_end";
+    if (!ctx) return fail(fn, "null context");
+    Context &c = ctx->c;
+    c.ntt_timing = false;
+    double ms = 0;
+    uint64_t nl = 0;
+    const size_t n = c.ntt_events.size() / 2;
+    for (size_t i = 0; i < n; ++i) {
+        float t = 0;
+        if (cudaEventSynchronize(c.ntt_events[2 * i + 1]) != cudaSuccess ||
+            cudaEventElapsedTime(&t, c.ntt_events[2 * i], c.ntt_events[2 * i + 1]) != cudaSuccess)
+            return fail(fn, "event timing failed");
+        ms += t;
+        nl += c.ntt_limbs[i];
+    }
+    for (auto e : c.ntt_events) cudaEventDestroy(e);
+    c.ntt_events.clear();
+    c.ntt_limbs.clear();
+    if (total_ms) *total_ms = ms;
+    if (calls) *calls = n;
+    if (limbs) *limbs = nl;
+    return 0;
+}

@@ -203,7 +203,7 @@ extern "C" int nexus_mm_expand(nexus_evaluator *ev, const nexus_ciphertext *x, u
 
 extern "C" int nexus_matrix_mul(nexus_evaluator *ev, nexus_ciphertext *const *compressed, int n_compressed,
                                 const uint64_t *d_pts, double pt_scale, int rows, int cols, double factor,
-                                nexus_ciphertext *const *res)
+                                const double *bias, int bias_len, nexus_ciphertext *const *res)
 {
     static const char *fn = "nexus_matrix_mul";
     if (!ev || !compressed || !d_pts || !res || n_compressed < 1) return fail(fn, "null argument");
@@ -217,6 +217,7 @@ extern "C" int nexus_matrix_mul(nexus_evaluator *ev, nexus_ciphertext *const *co
         for (int i = 0; i < n_compressed; ++i) cp.push_back(&compressed[i]->ct);
         std::vector<Ciphertext> out;
         mm.matrix_mul(cp, d_pts, pt_scale, rows, cols, factor, out);
+        if (bias && bias_len > 0) mm.add_bias(out, std::vector<double>(bias, bias + bias_len));
         for (int r = 0; r < rows; ++r) res[r]->ct = std::move(out[r]);
     });
 }

@@ -130,6 +130,8 @@ const uint32_t *Context::galois_table(uint32_t elt)
     return d;
 }
 
+std::atomic<uint64_t> g_kernel_launches{0};
+
 static thread_local std::string g_last_error;
 void set_error(const std::string &msg) { g_last_error = msg; }
 
@@ -138,6 +140,8 @@ void set_error(const std::string &msg) { g_last_error = msg; }
 using namespace nexus;
 
 extern "C" const char *nexus_last_error(void) { return nexus::g_last_error.c_str(); }
+
+extern "C" uint64_t nexus_kernel_launches(void) { return nexus::g_kernel_launches.load(); }
 
 extern "C" int nexus_context_create(int log_n, const uint64_t *moduli, int n_moduli, nexus_context **out)
 {

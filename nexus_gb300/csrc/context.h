@@ -5,6 +5,7 @@
 // data primes q_0..q_{L-1}; index k-1 is the special prime used only inside
 // key switching.
 #pragma once
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -51,7 +52,18 @@ struct Context {
     size_t scratch_words = 0;
     uint64_t *get_scratch(size_t words);
     const uint32_t *galois_table(uint32_t elt);
+
+    // Optional CUDA-event timing of every NTT launch (nexus_ntt_timing_*):
+    // each forward/inverse call records an event pair on its stream.
+    mutable bool ntt_timing = false;
+    mutable std::vector<cudaEvent_t> ntt_events;   // start, stop, start, stop, ...
+    mutable std::vector<size_t> ntt_limbs;        // limbs per recorded call
 };
+
+// Count of kernels this library has launched (process-wide); read through
+// nexus_kernel_launches() so benchmarks can report their own launches.
+extern std::atomic<uint64_t> g_kernel_launches;
+#define NEXUS_LAUNCHED() (nexus::g_kernel_launches.fetch_add(1, std::memory_order_relaxed))
 
 // Host helpers shared by the translation units.
 uint64_t host_mulmod(uint64_t a, uint64_t b, uint64_t q);

@@ -121,10 +121,10 @@ void switch_key_batch(Context &c, uint64_t *ct, int batch, int l, const uint64_t
     cudaMemcpyAsync(t, target, sizeof(uint64_t) * B * l * N, cudaMemcpyDeviceToDevice, s);
     ntt_inverse(c, t, B, LimbMap{l, 0, -1}, s);
     size_t tot = B * l * N;
-    k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot);
+    k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot); NEXUS_LAUNCHED();
     ntt_forward(c, D, B * l, LimbMap{l + 1, 0, sp}, s);
     tot = B * (l + 1) * N;
-    k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, tot);
+    k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, tot); NEXUS_LAUNCHED();
     // ModDown: the special limb of every (ciphertext, component) to coefficient form
     cudaMemcpy2DAsync(last, N * 8, P + (size_t)l * N, (size_t)(l + 1) * N * 8, N * 8, 2 * B,
                       cudaMemcpyDeviceToDevice, s);
@@ -132,7 +132,7 @@ void switch_key_batch(Context &c, uint64_t *ct, int batch, int l, const uint64_t
     launch_round_spread(c, last, T, (int)(2 * B), sp, l, s);
     ntt_forward(c, T, 2 * B, LimbMap{l, 0, -1}, s);
     tot = B * 2 * l * N;
-    k_moddown_finish<<<grid_for(tot), kBlock, 0, s>>>(ct, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn, tot);
+    k_moddown_finish<<<grid_for(tot), kBlock, 0, s>>>(ct, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn, tot); NEXUS_LAUNCHED();
 }
 
 void switch_key(Context &c, uint64_t *ct, int l, const uint64_t *target, const uint64_t *key, cudaStream_t s)
@@ -248,10 +248,10 @@ extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l,
         cudaMemcpyAsync(t, target, sizeof(uint64_t) * l * N, cudaMemcpyDeviceToDevice, s);
         ntt_inverse(c, t, 1, LimbMap{l, 0, -1}, s);
         size_t tot = (size_t)l * N;
-        k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot);
+        k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot); NEXUS_LAUNCHED();
         ntt_forward(c, D, l, LimbMap{l + 1, 0, sp}, s);
         tot = (size_t)(l + 1) * N;
-        k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, tot);
+        k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, tot); NEXUS_LAUNCHED();
         cudaMemcpyAsync(last, P + (size_t)l * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(last + N, P + (size_t)(2 * l + 1) * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
         ntt_inverse(c, last, 2, LimbMap{1, sp, -1}, s);
@@ -259,7 +259,7 @@ extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l,
         ntt_forward(c, T, 2, LimbMap{l, 0, -1}, s);
         tot = (size_t)2 * l * N;
         k_moddown_finish<<<grid_for(tot), kBlock, 0, s>>>(ct, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn,
-                                                           tot);
+                                                           tot); NEXUS_LAUNCHED();
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
     } catch (const std::exception &e) {

@@ -155,7 +155,7 @@ static void expand_level(Context &c, const uint64_t *nodes, int count, int l, in
     cudaFreeAsync(tgt, s);
     const size_t total = (size_t)count * per;
     k_expand_combine<<<grid_for(total), kBlock, 0, s>>>(nodes, rot, next, next + (size_t)count * per, c.d_pc,
-                                                         c.d_tw_fwd, l, c.logn, idx_raw, idx, total);
+                                                         c.d_tw_fwd, l, c.logn, idx_raw, idx, total); NEXUS_LAUNCHED();
 }
 
 // ---------------------------------------------------------------- MMEvaluator
@@ -187,7 +187,7 @@ void MMEvaluator::multiply_power_of_x(Ciphertext &encrypted, Ciphertext &destina
     out.scale() = encrypted.scale();
     const size_t total = (size_t)encrypted.size() * encrypted.limbs() * c.n;
     k_mul_monomial<<<grid_for(total), kBlock, 0, ev.stream()>>>(encrypted.data(), out.data(), c.d_pc, c.d_tw_fwd,
-                                                                 encrypted.limbs(), c.logn, k, total);
+                                                                 encrypted.limbs(), c.logn, k, total); NEXUS_LAUNCHED();
     destination = std::move(out);
 }
 
@@ -304,7 +304,7 @@ void MMEvaluator::matrix_mul(const std::vector<const Ciphertext *> &compressed, 
             const int rows_here = r_last - r_first + 1;
             const size_t total = (size_t)rows_here * per;
             k_mm_accumulate<<<grid_for(total), kBlock, 0, s>>>(cur.get(), d_pts, out.get(), c.d_pc, l, logn, d,
-                                                                sidx, (int)ci, cols, r_first, rows_here, total);
+                                                                sidx, (int)ci, cols, r_first, rows_here, total); NEXUS_LAUNCHED();
         }
     }
     const double scale = compressed[0]->scale() * pt_scale * factor;
@@ -316,6 +316,15 @@ void MMEvaluator::matrix_mul(const std::vector<const Ciphertext *> &compressed, 
         res[r].scale() = scale;
         while (res[r].limbs() > 1) ev.rescale_to_next_inplace(res[r]);
     }
+}
+
+void MMEvaluator::add_bias(std::vector<Ciphertext> &res, const std::vector<double> &bias)
+{
+    if (res.empty() || bias.empty()) return;
+    Evaluator &ev = *ckks->evaluator;
+    Plaintext b;
+    ev.encode(bias, res[0].limbs(), res[0].scale(), b);
+    for (auto &ct : res) ev.add_plain_inplace(ct, b);
 }
 
 }  // namespace nexus

@@ -85,6 +85,8 @@ public:
     // the same with the plaintexts already stacked on the device, d_pts[cols][l][N] at pt_scale
     void matrix_mul(const std::vector<const Ciphertext *> &compressed, const uint64_t *d_pts, double pt_scale,
                     int rows, int cols, double factor, std::vector<Ciphertext> &res, int subtree_depth = 6);
+    // optional bias: res[r] += encode(bias) at the output level and scale
+    void add_bias(std::vector<Ciphertext> &res, const std::vector<double> &bias);
 
 private:
     const uint64_t *key_for(uint32_t elt) const;

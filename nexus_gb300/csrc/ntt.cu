@@ -267,8 +267,8 @@ void launch_fwd(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaS
     constexpr int R = kThreads / ((1 << L2) / kE);
     const unsigned g1 = (unsigned)(limbs * ((1u << L2) / C));
     const unsigned g2 = (unsigned)(limbs * ((1u << L1) / R));
-    k_fwd_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm);
-    k_fwd_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm);
+    k_fwd_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm); NEXUS_LAUNCHED();
+    k_fwd_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm); NEXUS_LAUNCHED();
 }
 
 template <int L1, int L2>
@@ -279,15 +279,27 @@ void launch_inv(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaS
     constexpr int R = kThreads / ((1 << L2) / kE);
     const unsigned g1 = (unsigned)(limbs * ((1u << L2) / C));
     const unsigned g2 = (unsigned)(limbs * ((1u << L1) / R));
-    k_inv_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lm);
-    k_inv_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lm);
+    k_inv_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lm); NEXUS_LAUNCHED();
+    k_inv_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lm); NEXUS_LAUNCHED();
 }
 
 }  // namespace
 
+static void timing_mark(const Context &c, cudaStream_t s)
+{
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, s);
+    c.ntt_events.push_back(e);
+}
+
 void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s)
 {
     if (n_polys == 0 || lm.count == 0) return;
+    if (c.ntt_timing) {
+        timing_mark(c, s);
+        c.ntt_limbs.push_back(n_polys * lm.count);
+    }
     switch (c.logn) {
     case 12: launch_fwd<6, 6>(c, d, n_polys, lm, s); break;
     case 13: launch_fwd<6, 7>(c, d, n_polys, lm, s); break;
@@ -296,11 +308,16 @@ void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cuda
     case 16: launch_fwd<8, 8>(c, d, n_polys, lm, s); break;
     default: throw std::invalid_argument("unsupported log_n");
     }
+    if (c.ntt_timing) timing_mark(c, s);
 }
 
 void ntt_inverse(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s)
 {
     if (n_polys == 0 || lm.count == 0) return;
+    if (c.ntt_timing) {
+        timing_mark(c, s);
+        c.ntt_limbs.push_back(n_polys * lm.count);
+    }
     switch (c.logn) {
     case 12: launch_inv<6, 6>(c, d, n_polys, lm, s); break;
     case 13: launch_inv<6, 7>(c, d, n_polys, lm, s); break;
@@ -309,6 +326,7 @@ void ntt_inverse(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cuda
     case 16: launch_inv<8, 8>(c, d, n_polys, lm, s); break;
     default: throw std::invalid_argument("unsupported log_n");
     }
+    if (c.ntt_timing) timing_mark(c, s);
 }
 
 void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, int limb_begin, int limb_end, cudaStream_t s)

@@ -224,7 +224,7 @@ void poly_add(const Context &c, const uint64_t *a, const uint64_t *b, int polys,
 {
     size_t pr = pairs_of(c, polys, limbs);
     k_add_sub<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)a, (const ulonglong2 *)b, (ulonglong2 *)out, c.d_pc,
-                                               limbs, c.logn, pr, 0);
+                                               limbs, c.logn, pr, 0); NEXUS_LAUNCHED();
 }
 
 void poly_sub(const Context &c, const uint64_t *a, const uint64_t *b, int polys, int limbs, uint64_t *out,
@@ -232,13 +232,13 @@ void poly_sub(const Context &c, const uint64_t *a, const uint64_t *b, int polys,
 {
     size_t pr = pairs_of(c, polys, limbs);
     k_add_sub<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)a, (const ulonglong2 *)b, (ulonglong2 *)out, c.d_pc,
-                                               limbs, c.logn, pr, 1);
+                                               limbs, c.logn, pr, 1); NEXUS_LAUNCHED();
 }
 
 void poly_negate(const Context &c, const uint64_t *a, int polys, int limbs, uint64_t *out, cudaStream_t s)
 {
     size_t pr = pairs_of(c, polys, limbs);
-    k_negate<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)a, (ulonglong2 *)out, c.d_pc, limbs, c.logn, pr);
+    k_negate<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)a, (ulonglong2 *)out, c.d_pc, limbs, c.logn, pr); NEXUS_LAUNCHED();
 }
 
 void poly_mul_plain(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *pt, uint64_t *out,
@@ -246,7 +246,7 @@ void poly_mul_plain(const Context &c, const uint64_t *ct, int polys, int limbs, 
 {
     size_t pr = pairs_of(c, polys, limbs);
     k_plain<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)ct, (const ulonglong2 *)pt, (ulonglong2 *)out, c.d_pc,
-                                             limbs, c.logn, pr, 0);
+                                             limbs, c.logn, pr, 0); NEXUS_LAUNCHED();
 }
 
 void poly_add_plain(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *pt, int sub,
@@ -254,7 +254,7 @@ void poly_add_plain(const Context &c, const uint64_t *ct, int polys, int limbs, 
 {
     size_t pr = pairs_of(c, polys, limbs);
     k_plain<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)ct, (const ulonglong2 *)pt, (ulonglong2 *)out, c.d_pc,
-                                             limbs, c.logn, pr, sub ? 2 : 1);
+                                             limbs, c.logn, pr, sub ? 2 : 1); NEXUS_LAUNCHED();
 }
 
 void poly_mul_scalar(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *scalars,
@@ -266,7 +266,7 @@ void poly_mul_scalar(const Context &c, const uint64_t *ct, int polys, int limbs,
     for (int l = 0; l < limbs; ++l) w.w[l] = make_ulonglong2(scalars[l], host_shoup(scalars[l], c.q[l]));
     size_t pr = pairs_of(c, polys, limbs);
     k_mul_scalar<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)ct, w, (ulonglong2 *)out, c.d_pc, limbs, c.logn,
-                                                  pr);
+                                                  pr); NEXUS_LAUNCHED();
 }
 
 void poly_add_scalar(const Context &c, const uint64_t *in, int limbs, const uint64_t *scalars, int sub, uint64_t *out,
@@ -277,14 +277,14 @@ void poly_add_scalar(const Context &c, const uint64_t *in, int limbs, const uint
     for (int l = 0; l < limbs; ++l) w.w[l] = make_ulonglong2(scalars[l], 0);
     size_t pr = pairs_of(c, 1, limbs);
     k_add_scalar<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, w, (ulonglong2 *)out, c.d_pc, c.logn, pr,
-                                                  sub);
+                                                  sub); NEXUS_LAUNCHED();
 }
 
 void tensor(const Context &c, const uint64_t *a, const uint64_t *b, int limbs, uint64_t *out3, cudaStream_t s)
 {
     size_t pr = pairs_of(c, 1, limbs);
     k_tensor<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)a, (const ulonglong2 *)b, (ulonglong2 *)out3, c.d_pc,
-                                              limbs, c.logn);
+                                              limbs, c.logn); NEXUS_LAUNCHED();
 }
 
 void rescale(const Context &c_in, const uint64_t *in, int size, int limbs, uint64_t *out, cudaStream_t s)
@@ -296,22 +296,22 @@ void rescale(const Context &c_in, const uint64_t *in, int size, int limbs, uint6
     uint64_t *t = last + (size_t)size * n;
     size_t pr = ((size_t)size * n) >> 1;
     k_gather_limb<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, (ulonglong2 *)last, limbs, limbs - 1, c.logn,
-                                                   pr);
+                                                   pr); NEXUS_LAUNCHED();
     ntt_inverse(c, last, size, LimbMap{1, limbs - 1, -1}, s);
     size_t tot = (size_t)size * n;
-    k_round_spread<<<grid_for(tot), kBlock, 0, s>>>(last, t, c.d_pc, limbs - 1, limbs - 1, c.logn, tot);
+    k_round_spread<<<grid_for(tot), kBlock, 0, s>>>(last, t, c.d_pc, limbs - 1, limbs - 1, c.logn, tot); NEXUS_LAUNCHED();
     ntt_forward(c, t, size, LimbMap{limbs - 1, 0, -1}, s);
     pr = pairs_of(c, size, limbs - 1);
     k_rescale_finish<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, (const ulonglong2 *)t, (ulonglong2 *)out,
                                                       c.d_pc, c.d_inv_q + (size_t)(limbs - 1) * c.k, limbs, c.logn,
-                                                      pr);
+                                                      pr); NEXUS_LAUNCHED();
 }
 
 void launch_round_spread(const Context &c, const uint64_t *last, uint64_t *out, int polys, int last_prime,
                          int out_limbs, cudaStream_t s)
 {
     size_t tot = (size_t)polys * c.n;
-    k_round_spread<<<grid_for(tot), kBlock, 0, s>>>(last, out, c.d_pc, last_prime, out_limbs, c.logn, tot);
+    k_round_spread<<<grid_for(tot), kBlock, 0, s>>>(last, out, c.d_pc, last_prime, out_limbs, c.logn, tot); NEXUS_LAUNCHED();
 }
 
 void galois_permute(Context &c, const uint64_t *in, int polys, int limbs, uint32_t elt, uint64_t *out,
@@ -319,7 +319,7 @@ void galois_permute(Context &c, const uint64_t *in, int polys, int limbs, uint32
 {
     const uint32_t *tab = c.galois_table(elt);
     size_t tot = (size_t)polys * limbs * c.n;
-    k_permute<<<grid_for(tot), kBlock, 0, s>>>(in, out, tab, c.logn, tot);
+    k_permute<<<grid_for(tot), kBlock, 0, s>>>(in, out, tab, c.logn, tot); NEXUS_LAUNCHED();
 }
 
 }  // namespace nexus

@@ -168,7 +168,7 @@ void keygen_secret(Context &c, uint64_t seed, int hamming_weight, uint64_t *sk, 
     int8_t *d = nullptr;
     if (cudaMalloc(&d, N) != cudaSuccess) throw std::runtime_error("cudaMalloc");
     cudaMemcpy(d, v.data(), N, cudaMemcpyHostToDevice);
-    k_small_to_rns<<<grid_for(N), kBlock, 0, s>>>(d, sk, c.d_pc, c.k, c.logn);
+    k_small_to_rns<<<grid_for(N), kBlock, 0, s>>>(d, sk, c.d_pc, c.k, c.logn); NEXUS_LAUNCHED();
     ntt_forward(c, sk, 1, 0, c.k, s);
     cudaStreamSynchronize(s);
     cudaFree(d);
@@ -186,11 +186,11 @@ void keygen_kswitch(Context &c, const uint64_t *sk, const uint64_t *new_key, uin
         uint64_t *b = key + (size_t)j * 2 * K * N;
         uint64_t *a = b + (size_t)K * N;
         size_t tot = (size_t)K * N;
-        k_uniform<<<grid_for(tot), kBlock, 0, s>>>(a, c.d_pc, LimbMap{K, 0, -1}, c.logn, tot, seed, 2 * j + 1);
-        k_cbd<<<grid_for(N), kBlock, 0, s>>>(e, c.d_pc, LimbMap{K, 0, -1}, c.logn, N, seed, 2 * j + 2);
+        k_uniform<<<grid_for(tot), kBlock, 0, s>>>(a, c.d_pc, LimbMap{K, 0, -1}, c.logn, tot, seed, 2 * j + 1); NEXUS_LAUNCHED();
+        k_cbd<<<grid_for(N), kBlock, 0, s>>>(e, c.d_pc, LimbMap{K, 0, -1}, c.logn, N, seed, 2 * j + 2); NEXUS_LAUNCHED();
         ntt_forward(c, e, 1, 0, K, s);
         const uint64_t factor = p % c.q[j];
-        k_kswitch_row<<<grid_for(tot), kBlock, 0, s>>>(b, a, e, sk, new_key, c.d_pc, K, j, factor, c.logn);
+        k_kswitch_row<<<grid_for(tot), kBlock, 0, s>>>(b, a, e, sk, new_key, c.d_pc, K, j, factor, c.logn); NEXUS_LAUNCHED();
     }
 }
 
@@ -199,7 +199,7 @@ void keygen_relin(Context &c, const uint64_t *sk, uint64_t seed, uint64_t *key, 
     uint64_t *sq = nullptr;
     const size_t words = (size_t)c.k * c.n;
     if (cudaMallocAsync(&sq, words * 8, s) != cudaSuccess) throw std::runtime_error("cudaMallocAsync");
-    k_square<<<grid_for(words), kBlock, 0, s>>>(sq, sk, c.d_pc, c.logn, words);
+    k_square<<<grid_for(words), kBlock, 0, s>>>(sq, sk, c.d_pc, c.logn, words); NEXUS_LAUNCHED();
     keygen_kswitch(c, sk, sq, seed, key, s);
     cudaFreeAsync(sq, s);
 }
@@ -223,16 +223,16 @@ void encrypt_symmetric(Context &c, const uint64_t *sk, const uint64_t *m, int li
     uint64_t *e = c.get_scratch((size_t)limbs * N);
     uint64_t *a = ct + (size_t)limbs * N;
     size_t tot = (size_t)limbs * N;
-    k_uniform<<<grid_for(tot), kBlock, 0, s>>>(a, c.d_pc, LimbMap{limbs, 0, -1}, c.logn, tot, seed, 1ull << 40);
-    k_cbd<<<grid_for(N), kBlock, 0, s>>>(e, c.d_pc, LimbMap{limbs, 0, -1}, c.logn, N, seed, (1ull << 40) + 1);
+    k_uniform<<<grid_for(tot), kBlock, 0, s>>>(a, c.d_pc, LimbMap{limbs, 0, -1}, c.logn, tot, seed, 1ull << 40); NEXUS_LAUNCHED();
+    k_cbd<<<grid_for(N), kBlock, 0, s>>>(e, c.d_pc, LimbMap{limbs, 0, -1}, c.logn, N, seed, (1ull << 40) + 1); NEXUS_LAUNCHED();
     ntt_forward(c, e, 1, 0, limbs, s);
-    k_encrypt_sym<<<grid_for(tot), kBlock, 0, s>>>(ct, a, e, m, sk, c.d_pc, limbs, c.logn);
+    k_encrypt_sym<<<grid_for(tot), kBlock, 0, s>>>(ct, a, e, m, sk, c.d_pc, limbs, c.logn); NEXUS_LAUNCHED();
 }
 
 void decrypt(Context &c, const uint64_t *sk, const uint64_t *ct, int size, int limbs, uint64_t *m, cudaStream_t s)
 {
     size_t tot = (size_t)limbs * c.n;
-    k_decrypt<<<grid_for(tot), kBlock, 0, s>>>(m, ct, size, sk, c.d_pc, limbs, c.logn);
+    k_decrypt<<<grid_for(tot), kBlock, 0, s>>>(m, ct, size, sk, c.d_pc, limbs, c.logn); NEXUS_LAUNCHED();
 }
 
 }  // namespace nexus

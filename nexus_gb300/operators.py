@@ -134,11 +134,13 @@ class Evaluator:
         check(lib().nexus_mm_expand(self._h, x.handle, int(m), out.data_ptr()), "nexus_mm_expand")
         return out
 
-    def matrix_mul(self, compressed, pts, pt_scale: float, rows: int, cols: int, factor: float):
-        """compressed: list of Ciphertext; pts: CUDA int64 tensor [cols][limbs][N]."""
+    def matrix_mul(self, compressed, pts, pt_scale: float, rows: int, cols: int, factor: float, bias=None):
+        """compressed: list of Ciphertext; pts: CUDA int64 tensor [cols][limbs][N]; bias: slot values or None."""
         comp = (C.c_void_p * len(compressed))(*[c.handle.value for c in compressed])
         res = [Ciphertext(self.ctx) for _ in range(rows)]
         out = (C.c_void_p * rows)(*[r.handle.value for r in res])
+        b = None if bias is None else np.ascontiguousarray(bias, dtype=np.float64)
         check(lib().nexus_matrix_mul(self._h, comp, len(compressed), pts.data_ptr(), float(pt_scale), int(rows),
-                                     int(cols), float(factor), out), "nexus_matrix_mul")
+                                     int(cols), float(factor), None if b is None else b.ctypes.data,
+                                     0 if b is None else b.size, out), "nexus_matrix_mul")
         return res
