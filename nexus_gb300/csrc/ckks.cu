@@ -211,6 +211,37 @@ void Evaluator::encode(const std::vector<double> &values, int limbs, double scal
     ntt_forward(c_, out.mutable_data(), 1, 0, limbs, s_);
 }
 
+void Evaluator::encode(const std::vector<std::complex<double>> &values, int limbs, double scale, Plaintext &out)
+{
+    if (limbs < 1 || limbs > top_limbs()) throw std::invalid_argument("parms_id is not valid for encryption parameters");
+    std::vector<uint64_t> host((size_t)limbs * c_.n);
+    enc_->encode(values.data(), values.size(), scale, limbs, host.data());
+    out.set_vector(c_, limbs, scale, s_);
+    ck(cudaMemcpyAsync(out.mutable_data(), host.data(), host.size() * 8, cudaMemcpyHostToDevice, s_), "upload");
+    ck(cudaStreamSynchronize(s_), "encode");
+    ntt_forward(c_, out.mutable_data(), 1, 0, limbs, s_);
+}
+
+void Evaluator::encode_then_drop(const std::vector<std::complex<double>> &values, int limbs, double scale,
+                                 Plaintext &out)
+{
+    if (limbs < 1 || limbs > top_limbs()) throw std::invalid_argument("cannot switch to higher level modulus");
+    std::vector<uint64_t> host((size_t)limbs * c_.n);
+    enc_->encode(values.data(), values.size(), scale, limbs, host.data(), top_limbs());
+    out.set_vector(c_, limbs, scale, s_);
+    ck(cudaMemcpyAsync(out.mutable_data(), host.data(), host.size() * 8, cudaMemcpyHostToDevice, s_), "upload");
+    ck(cudaStreamSynchronize(s_), "encode");
+    ntt_forward(c_, out.mutable_data(), 1, 0, limbs, s_);
+}
+
+void Evaluator::encode_then_drop(double value, int limbs, double scale, Plaintext &out)
+{
+    if (limbs < 1 || limbs > top_limbs()) throw std::invalid_argument("cannot switch to higher level modulus");
+    std::vector<uint64_t> r(limbs);
+    enc_->encode_scalar(value, scale, limbs, r.data(), top_limbs());
+    out.set_scalar(std::move(r), scale);
+}
+
 void Evaluator::encode(double value, int limbs, double scale, Plaintext &out)
 {
     if (limbs < 1 || limbs > top_limbs()) throw std::invalid_argument("parms_id is not valid for encryption parameters");
@@ -398,6 +429,137 @@ void Evaluator::multiply_plain(const Ciphertext &ct, const Plaintext &pt, Cipher
 {
     if (&ct != &dest) dest = ct;
     multiply_plain_inplace(dest, pt);
+}
+
+// ---------------------------------------------------------------- fork ops
+
+// add_const_inplace / multiply_const_inplace / multiply_vector_inplace
+// (evaluator.cpp:395-418): encode at the ciphertext's scale on the top level,
+// drop to its level, then add / multiply
+void Evaluator::add_const_inplace(Ciphertext &ct, double value)
+{
+    Plaintext p;
+    encode_then_drop(value, ct.limbs(), ct.scale(), p);
+    add_plain_inplace(ct, p);
+}
+
+void Evaluator::multiply_const_inplace(Ciphertext &ct, double value)
+{
+    Plaintext p;
+    encode_then_drop(value, ct.limbs(), ct.scale(), p);
+    multiply_plain_inplace(ct, p);
+}
+
+void Evaluator::multiply_const(const Ciphertext &ct, double value, Ciphertext &dest)
+{
+    if (&ct != &dest) dest = ct;
+    multiply_const_inplace(dest, value);
+}
+
+void Evaluator::multiply_vector_inplace_reduced_error(Ciphertext &ct, const std::vector<std::complex<double>> &values)
+{
+    Plaintext p;
+    encode_then_drop(values, ct.limbs(), ct.scale(), p);
+    multiply_plain_inplace(ct, p);
+}
+
+void Evaluator::multiply_vector_reduced_error(const Ciphertext &ct, const std::vector<std::complex<double>> &values,
+                                              Ciphertext &dest)
+{
+    if (&ct != &dest) dest = ct;
+    multiply_vector_inplace_reduced_error(dest, values);
+}
+
+// The level matching of add/sub/multiply_inplace_reduced_error
+// (evaluator.cpp:420-590): the higher ciphertext is multiplied by
+// lo.scale * q_top / hi.scale^2, given scale lo.scale * q_top, rescaled and
+// dropped to lo's level.
+Ciphertext Evaluator::adjust_down(const Ciphertext &hi, const Ciphertext &lo)
+{
+    const double q_top = (double)c_.q[hi.limbs() - 1];
+    const double scale_adjust = lo.scale() * q_top / (hi.scale() * hi.scale());
+    Ciphertext adj;
+    multiply_const(hi, scale_adjust, adj);
+    adj.scale() = lo.scale() * q_top;
+    rescale_to_next_inplace(adj);
+    mod_switch_to_inplace(adj, lo.limbs());
+    return adj;
+}
+
+void Evaluator::add_inplace_reduced_error(Ciphertext &a, const Ciphertext &b)
+{
+    if (a.limbs() == b.limbs()) {
+        a.scale() = b.scale();
+        add_inplace(a, b);
+    } else if (a.limbs() < b.limbs()) {
+        Ciphertext adj = adjust_down(b, a);
+        a.scale() = adj.scale();
+        add_inplace(a, adj);
+    } else {
+        Ciphertext adj = adjust_down(a, b);
+        adj.scale() = b.scale();
+        add(adj, b, a);
+    }
+}
+
+void Evaluator::sub_inplace_reduced_error(Ciphertext &a, const Ciphertext &b)
+{
+    if (a.limbs() == b.limbs()) {
+        a.scale() = b.scale();
+        sub_inplace(a, b);
+    } else if (a.limbs() < b.limbs()) {
+        Ciphertext adj = adjust_down(b, a);
+        a.scale() = adj.scale();
+        sub_inplace(a, adj);
+    } else {
+        Ciphertext adj = adjust_down(a, b);
+        adj.scale() = b.scale();
+        sub(adj, b, a);
+    }
+}
+
+void Evaluator::multiply_inplace_reduced_error(Ciphertext &a, const Ciphertext &b)
+{
+    if (a.limbs() == b.limbs()) {
+        a.scale() = b.scale();
+        multiply_inplace(a, b);
+    } else if (a.limbs() < b.limbs()) {
+        Ciphertext adj = adjust_down(b, a);
+        a.scale() = adj.scale();
+        multiply_inplace(a, adj);
+    } else {
+        Ciphertext adj = adjust_down(a, b);
+        adj.scale() = b.scale();
+        multiply(adj, b, a);
+    }
+    relinearize_inplace(a);
+}
+
+void Evaluator::add_reduced_error(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest)
+{
+    if (&b == &dest) {
+        add_inplace_reduced_error(dest, a);
+    } else {
+        if (&a != &dest) dest = a;
+        add_inplace_reduced_error(dest, b);
+    }
+}
+
+void Evaluator::sub_reduced_error(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest)
+{
+    Ciphertext bb = b;  // b may alias dest
+    if (&a != &dest) dest = a;
+    sub_inplace_reduced_error(dest, bb);
+}
+
+void Evaluator::multiply_reduced_error(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest)
+{
+    if (&b == &dest) {
+        multiply_inplace_reduced_error(dest, a);
+    } else {
+        if (&a != &dest) dest = a;
+        multiply_inplace_reduced_error(dest, b);
+    }
 }
 
 // ---------------------------------------------------------------- rotations

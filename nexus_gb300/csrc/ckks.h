@@ -7,6 +7,7 @@
 // Every operation is enqueued on the evaluator's stream; device memory comes
 // from the stream-ordered allocator (cudaMallocAsync pool).
 #pragma once
+#include <complex>
 #include <cstdint>
 #include <map>
 #include <stdexcept>
@@ -134,6 +135,10 @@ public:
     void encode(const std::vector<double> &values, int limbs, double scale, Plaintext &out);
     void encode(double value, int limbs, double scale, Plaintext &out);  // scalar path
     void encode(double value, double scale, Plaintext &out) { encode(value, top_limbs(), scale, out); }
+    void encode(const std::vector<std::complex<double>> &values, int limbs, double scale, Plaintext &out);
+    // SEAL's encode(..., scale) at the top level followed by mod_switch_to(limbs)
+    void encode_then_drop(const std::vector<std::complex<double>> &values, int limbs, double scale, Plaintext &out);
+    void encode_then_drop(double value, int limbs, double scale, Plaintext &out);
     std::vector<double> decode(const Plaintext &pt);
 
     // level management
@@ -161,6 +166,22 @@ public:
     void multiply_plain_inplace(Ciphertext &ct, const Plaintext &pt);
     void multiply_plain(const Ciphertext &ct, const Plaintext &pt, Ciphertext &dest);
 
+    // constant / vector ops of the bootstrapping fork of SEAL (evaluator.cpp:395-418)
+    void add_const_inplace(Ciphertext &ct, double value);
+    void multiply_const_inplace(Ciphertext &ct, double value);
+    void multiply_const(const Ciphertext &ct, double value, Ciphertext &dest);
+    void multiply_vector_inplace_reduced_error(Ciphertext &ct, const std::vector<std::complex<double>> &values);
+    void multiply_vector_reduced_error(const Ciphertext &ct, const std::vector<std::complex<double>> &values,
+                                       Ciphertext &dest);
+    // reduced-error level matching (Kim et al., CT-RSA'22; evaluator.cpp:420-590)
+    void add_inplace_reduced_error(Ciphertext &a, const Ciphertext &b);
+    void sub_inplace_reduced_error(Ciphertext &a, const Ciphertext &b);
+    void multiply_inplace_reduced_error(Ciphertext &a, const Ciphertext &b);
+    void add_reduced_error(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest);
+    void sub_reduced_error(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest);
+    void multiply_reduced_error(const Ciphertext &a, const Ciphertext &b, Ciphertext &dest);
+    void double_inplace(Ciphertext &ct) { add_inplace(ct, ct); }
+
     // rotations
     void apply_galois_inplace(Ciphertext &ct, uint32_t elt);
     void rotate_vector_inplace(Ciphertext &ct, int steps);
@@ -173,6 +194,9 @@ public:
 private:
     void check_scale(double scale, int limbs) const;
     void plain_arith(Ciphertext &ct, const Plaintext &pt, bool sub);
+    // the scale adjustment shared by the *_reduced_error ops: bring the higher
+    // ciphertext `hi` down to lo's level at lo's scale
+    Ciphertext adjust_down(const Ciphertext &hi, const Ciphertext &lo);
     Context &c_;
     cudaStream_t s_;
     Encoder *enc_ = nullptr;

@@ -164,14 +164,14 @@ static uint64_t reduce_words(const uint64_t *w, int count, uint64_t q)
     return (uint64_t)r;
 }
 
-void Encoder::encode(const std::complex<double> *values, size_t nvals, double scale, int limbs,
-                     uint64_t *out) const
+void Encoder::encode(const std::complex<double> *values, size_t nvals, double scale, int limbs, uint64_t *out,
+                     int check_limbs) const
 {
     const Context &c = ctx_;
     const size_t n = c.n;
     if (nvals > slots_) throw std::invalid_argument("values_size is too large");
     if (limbs < 1 || limbs > c.k - 1) throw std::invalid_argument("limbs out of range");
-    const int tb = total_bits(c, limbs);
+    const int tb = total_bits(c, check_limbs > 0 ? check_limbs : limbs);
     if (scale <= 0 || ((int)std::log2(scale) + 1 >= tb)) throw std::invalid_argument("scale out of bounds");
     std::vector<std::complex<double>> v(n, std::complex<double>(0, 0));
     for (size_t i = 0; i < nvals; ++i) {
@@ -216,10 +216,10 @@ void Encoder::encode(const std::complex<double> *values, size_t nvals, double sc
 // CKKSEncoder::encode_internal(double) (ckks.cpp:75-205): the constant
 // polynomial round(value*scale); in NTT form every coefficient of limb j holds
 // the same residue, returned here per limb.
-void Encoder::encode_scalar(double value, double scale, int limbs, uint64_t *per_limb) const
+void Encoder::encode_scalar(double value, double scale, int limbs, uint64_t *per_limb, int check_limbs) const
 {
     const Context &c = ctx_;
-    const int tb = total_bits(c, limbs);
+    const int tb = total_bits(c, check_limbs > 0 ? check_limbs : limbs);
     if (scale <= 0 || ((int)std::log2(scale) >= tb)) throw std::invalid_argument("scale out of bounds");
     value *= scale;
     const int cb = (int)std::log2(std::fabs(value)) + 2;

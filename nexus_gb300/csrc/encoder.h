@@ -13,9 +13,13 @@ public:
     explicit Encoder(const Context &c);
     // values[nvals] (nvals <= N/2) at `scale` into coefficient-form residues
     // out[limbs][N] (the caller applies the forward NTT)
-    void encode(const std::complex<double> *values, size_t nvals, double scale, int limbs, uint64_t *out) const;
+    // check_limbs > 0: bound checks as for an encode at that level (SEAL's
+    // encode at the top level followed by mod_switch_to keeps the top-level
+    // checks while only the first `limbs` residues survive)
+    void encode(const std::complex<double> *values, size_t nvals, double scale, int limbs, uint64_t *out,
+                int check_limbs = 0) const;
     // residue of round(value * scale) in each of the first `limbs` primes
-    void encode_scalar(double value, double scale, int limbs, uint64_t *per_limb) const;
+    void encode_scalar(double value, double scale, int limbs, uint64_t *per_limb, int check_limbs = 0) const;
     // coefficient-form residues coeffs[limbs][N] -> nvals slot values;
     // sparse_slots (0 = all) zeroes coefficients as the fork's sparse decode does
     void decode(const uint64_t *coeffs, int limbs, double scale, std::complex<double> *out, size_t nvals,

@@ -109,6 +109,53 @@ class Evaluator:
         limbs = limbs or self.top
         return Pt(scale, per_limb=self.oc.encode_scalar(value, scale, limbs))
 
+    def encode_then_drop(self, values, scale, limbs):
+        """SEAL's encode(values, scale) at the top level, then mod_switch_to(limbs)."""
+        if np.ndim(values) == 0:
+            return Pt(scale, per_limb=self.oc.encode_scalar(float(values), scale, self.top)[:limbs].copy())
+        return Pt(scale, data=np.ascontiguousarray(self.oc.encode(values, scale, self.top)[:limbs]))
+
+    # ---- fork ops (evaluator.cpp:395-590 of the bootstrapping SEAL) ----------
+    def add_const(self, ct, value):
+        return self.add_plain(ct, self.encode_then_drop(value, ct.scale, ct.limbs))
+
+    def multiply_const(self, ct, value):
+        return self.multiply_plain(ct, self.encode_then_drop(value, ct.scale, ct.limbs))
+
+    def multiply_vector_reduced_error(self, ct, values):
+        return self.multiply_plain(ct, self.encode_then_drop(np.asarray(values), ct.scale, ct.limbs))
+
+    def _adjust_down(self, hi, lo):
+        q_top = float(self.q[hi.limbs - 1])
+        scale_adjust = lo.scale * q_top / (hi.scale * hi.scale)
+        adj = self.multiply_const(hi, scale_adjust)
+        adj.scale = lo.scale * q_top
+        adj = self.rescale(adj)
+        return self.mod_switch_to(adj, lo.limbs)
+
+    def _reduced(self, a, b, op):
+        a = a.copy()
+        if a.limbs == b.limbs:
+            a.scale = b.scale
+            return op(a, b)
+        if a.limbs < b.limbs:
+            adj = self._adjust_down(b, a)
+            a.scale = adj.scale
+            return op(a, adj)
+        adj = self._adjust_down(a, b)
+        adj.scale = b.scale
+        return op(adj, b)
+
+    def add_reduced_error(self, a, b):
+        return self._reduced(a, b, self.add)
+
+    def sub_reduced_error(self, a, b):
+        return self._reduced(a, b, self.sub)
+
+    def multiply_reduced_error(self, a, b):
+        """multiply_inplace_reduced_error: level matching, multiply, relinearize."""
+        return self.relinearize(self._reduced(a, b, self.multiply))
+
     # ---- level management ------------------------------------------------------
     def mod_switch_to(self, x, limbs):
         """mod_switch_to_inplace (evaluator.cpp:1630): drop limbs, keep scale."""

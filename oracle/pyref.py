@@ -57,6 +57,9 @@ def lib():
         l.sr_decrypt.argtypes = [C.c_void_p, u64p, C.c_int, C.c_double, f64p, C.c_size_t]
         l.sr_nexus_op.argtypes = [C.c_void_p, C.c_int, u64p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
                                   C.c_double, u64p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        l.sr_fork_op.argtypes = [C.c_void_p, C.c_int, u64p, C.c_int, C.c_double, u64p, C.c_int, C.c_double,
+                                 C.c_double, f64p, f64p, C.c_size_t, u64p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_double)]
         l.sr_galois_keys_from_elts.argtypes = [C.c_void_p, C.POINTER(C.c_uint32), C.c_int]
         l.sr_mm_compress.argtypes = [C.c_void_p, f64p, C.c_double, u64p, f64p]
         l.sr_mm_power_of_x.argtypes = [C.c_void_p, u64p, C.c_int, C.c_int, u64p]
@@ -218,3 +221,23 @@ class SealRef:
         out = np.zeros((m, 2, ct.shape[1], self.n), np.uint64)
         _ck(lib().sr_mm_expand(self._h, _p(np.ascontiguousarray(ct)), ct.shape[1], scale, m, _p(out)))
         return out
+
+    FORK = {"add_const": 0, "multiply_const": 1, "add_reduced_error": 2, "sub_reduced_error": 3,
+            "multiply_reduced_error": 4, "multiply_vector_reduced_error": 5}
+
+    def fork_op(self, op, a, sa, b=None, sb=0.0, value=0.0, vec=None):
+        out = np.zeros((3, self.k - 1, self.n), np.uint64)
+        osz, ol, osc = C.c_int(), C.c_int(), C.c_double()
+        re = im = None
+        nv = 0
+        if vec is not None:
+            vec = np.asarray(vec, dtype=np.complex128)
+            re = np.ascontiguousarray(vec.real)
+            im = np.ascontiguousarray(vec.imag)
+            nv = vec.size
+        _ck(lib().sr_fork_op(self._h, self.FORK[op], _p(np.ascontiguousarray(a)), a.shape[1], sa,
+                             None if b is None else _p(np.ascontiguousarray(b)), 0 if b is None else b.shape[1], sb,
+                             value, None if re is None else _p(re), None if im is None else _p(im), nv, _p(out),
+                             C.byref(osz), C.byref(ol), C.byref(osc)))
+        flat = out.reshape(-1)[: osz.value * ol.value * self.n]
+        return np.ascontiguousarray(flat.reshape(osz.value, ol.value, self.n)), osc.value

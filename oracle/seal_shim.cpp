@@ -353,6 +353,40 @@ int sr_nexus_op(void *h, int op, const uint64_t *in, int limbs, double in_scale,
     })
 }
 
+// Fork ops of the bootstrapping SEAL (evaluator.cpp:395-590 / evaluator.h:1296-1386):
+// op 0 add_const(a, v), 1 multiply_const(a, v), 2 add_reduced_error(a, b),
+// 3 sub_reduced_error(a, b), 4 multiply_reduced_error(a, b),
+// 5 multiply_vector_reduced_error(a, complex values re/im of length nv)
+int sr_fork_op(void *h, int op, const uint64_t *a, int la, double sa, const uint64_t *b, int lb, double sb,
+               double v, const double *re, const double *im, size_t nv, uint64_t *out, int *out_size, int *out_limbs,
+               double *out_scale)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Ciphertext x, y, r;
+        load_ct(s, x, a, 2, la, sa);
+        if (b) load_ct(s, y, b, 2, lb, sb);
+        switch (op) {
+        case 0: s.ev->add_const(x, v, r); break;
+        case 1: s.ev->multiply_const(x, v, r); break;
+        case 2: s.ev->add_reduced_error(x, y, r); break;
+        case 3: s.ev->sub_reduced_error(x, y, r); break;
+        case 4: s.ev->multiply_reduced_error(x, y, *s.rk, r); break;
+        case 5: {
+            std::vector<std::complex<double>> vec(nv);
+            for (size_t i = 0; i < nv; ++i) vec[i] = {re[i], im[i]};
+            s.ev->multiply_vector_reduced_error(x, vec, r);
+            break;
+        }
+        default: throw std::invalid_argument("unknown op");
+        }
+        store_ct(s, r, out);
+        *out_size = (int)r.size();
+        *out_limbs = (int)r.coeff_modulus_size();
+        *out_scale = r.scale();
+    })
+}
+
 // Galois keys for explicit elements (the MatMul expansion uses elements, not steps)
 int sr_galois_keys_from_elts(void *h, const uint32_t *elts, int n)
 {

@@ -107,3 +107,29 @@ def test_matmul_expand(mm_env, m):
     assert len(got) == m
     for i in range(m):
         assert np.array_equal(want[i], got[i].data), i
+
+
+@pytest.mark.parametrize("la,lb", [(5, 5), (3, 6), (6, 3)])
+def test_fork_reduced_error_ops(env, la, lb):
+    """add/sub/multiply_reduced_error, add_const, multiply_const and
+    multiply_vector_reduced_error of the bootstrapping SEAL"""
+    s, ck = env
+    ev = ck.ev
+    rng = np.random.default_rng(la * 10 + lb)
+    ct_a = s.encrypt(rng.uniform(-1, 1, N // 2), SCALE)
+    ct_b = s.encrypt(rng.uniform(-1, 1, N // 2), SCALE)
+    a = L.Ct(np.ascontiguousarray(ct_a[:, :la]), SCALE * 1.0003)
+    b = L.Ct(np.ascontiguousarray(ct_b[:, :lb]), SCALE * 0.9991)
+    for op, fn in (("add_reduced_error", ev.add_reduced_error), ("sub_reduced_error", ev.sub_reduced_error),
+                   ("multiply_reduced_error", ev.multiply_reduced_error)):
+        want, wsc = s.fork_op(op, a.data, a.scale, b.data, b.scale)
+        got = fn(a, b)
+        assert got.scale == wsc and np.array_equal(got.data, want), op
+    for op, fn, v in (("add_const", ev.add_const, 0.37), ("multiply_const", ev.multiply_const, -1.7)):
+        want, wsc = s.fork_op(op, a.data, a.scale, value=v)
+        got = fn(a, v)
+        assert got.scale == wsc and np.array_equal(got.data, want), op
+    vec = rng.uniform(-1, 1, N // 2) + 1j * rng.uniform(-1, 1, N // 2)
+    want, wsc = s.fork_op("multiply_vector_reduced_error", a.data, a.scale, vec=vec)
+    got = ev.multiply_vector_reduced_error(a, vec)
+    assert got.scale == wsc and np.array_equal(got.data, want)
