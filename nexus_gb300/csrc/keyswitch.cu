@@ -103,6 +103,45 @@ __global__ void k_moddown_finish(uint64_t *__restrict__ ct, const uint64_t *__re
 
 }  // namespace
 
+// Stage 1 (ModUp + inner product) of a batched key switch.  t [B][l][N]
+// holds the targets in NTT form and is overwritten (inverse-transformed in
+// place); D is scratch of B*l*(l+1) limbs; P [B][2][l+1][N] receives the
+// inner products.
+void ks_modup_inner(Context &c, uint64_t *t, int B, int l, const uint64_t *key, uint64_t *D, uint64_t *P,
+                    cudaStream_t s)
+{
+    const size_t N = c.n, Bs = (size_t)B;
+    const int sp = c.k - 1;
+    ntt_inverse(c, t, Bs, LimbMap{l, 0, -1}, s);
+    // ModUp spread fused into the first pass of the forward NTT
+    NttLoader ld;
+    ld.kind = 1;
+    ld.src = t;
+    ld.group = l + 1;
+    ld.src_limbs = l;
+    ntt_forward_loaded(c, D, Bs * l, LimbMap{l + 1, 0, sp}, ld, s);
+    size_t tot = Bs * (l + 1) * N;
+    k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, tot); NEXUS_LAUNCHED();
+}
+
+// Stage 2: the rounding terms T [B][2][l][N] of the ModDown from the special
+// limbs of P; `last` is scratch of 2B limbs.
+void ks_moddown_terms(Context &c, const uint64_t *P, int B, int l, uint64_t *T, uint64_t *last, cudaStream_t s)
+{
+    const size_t N = c.n, Bs = (size_t)B;
+    const int sp = c.k - 1;
+    cudaMemcpy2DAsync(last, N * 8, P + (size_t)l * N, (size_t)(l + 1) * N * 8, N * 8, 2 * Bs,
+                      cudaMemcpyDeviceToDevice, s);
+    ntt_inverse(c, last, 2 * Bs, LimbMap{1, sp, -1}, s);
+    // rounding spread fused into the first pass of the forward NTT
+    NttLoader ld;
+    ld.kind = 2;
+    ld.src = last;
+    ld.group = l;
+    ld.special = sp;
+    ntt_forward_loaded(c, T, 2 * Bs, LimbMap{l, 0, -1}, ld, s);
+}
+
 void switch_key_batch(Context &c, uint64_t *ct, int batch, int l, const uint64_t *target, const uint64_t *key,
                       cudaStream_t s)
 {
@@ -119,19 +158,9 @@ void switch_key_batch(Context &c, uint64_t *ct, int batch, int l, const uint64_t
     uint64_t *last = T + B * 2 * l * N;
 
     cudaMemcpyAsync(t, target, sizeof(uint64_t) * B * l * N, cudaMemcpyDeviceToDevice, s);
-    ntt_inverse(c, t, B, LimbMap{l, 0, -1}, s);
-    size_t tot = B * l * N;
-    k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot); NEXUS_LAUNCHED();
-    ntt_forward(c, D, B * l, LimbMap{l + 1, 0, sp}, s);
-    tot = B * (l + 1) * N;
-    k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, tot); NEXUS_LAUNCHED();
-    // ModDown: the special limb of every (ciphertext, component) to coefficient form
-    cudaMemcpy2DAsync(last, N * 8, P + (size_t)l * N, (size_t)(l + 1) * N * 8, N * 8, 2 * B,
-                      cudaMemcpyDeviceToDevice, s);
-    ntt_inverse(c, last, 2 * B, LimbMap{1, sp, -1}, s);
-    launch_round_spread(c, last, T, (int)(2 * B), sp, l, s);
-    ntt_forward(c, T, 2 * B, LimbMap{l, 0, -1}, s);
-    tot = B * 2 * l * N;
+    ks_modup_inner(c, t, batch, l, key, D, P, s);
+    ks_moddown_terms(c, P, batch, l, T, last, s);
+    const size_t tot = B * 2 * l * N;
     k_moddown_finish<<<grid_for(tot), kBlock, 0, s>>>(ct, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn, tot); NEXUS_LAUNCHED();
 }
 

@@ -8,11 +8,14 @@
 //
 // GPU form, word-for-word equal to the reference:
 //  * all nodes of a level share one Galois key, so their key switches run as
-//    one batched key switch (switch_key_batch);
+//    one batched key switch (the key is read once per level, not per node);
+//  * the automorphism's permutation is folded into the gather of the key
+//    switch target and into the epilogue, which forms both children at once:
+//    the rotated ciphertext is never written;
 //  * multiply_power_of_x is a pointwise product with NTT(X^k), whose slot j
-//    is psi^(k (2 bitrev(j) + 1)) read from the forward twiddle table, fused
-//    with the additions into one kernel (no INTT/shift/NTT round trip and no
-//    host copy as in the reference's GPU build);
+//    is psi^(k (2 bitrev(j) + 1)) read from the forward twiddle table (no
+//    INTT/shift/NTT round trip and no host copy as in the reference's GPU
+//    build);
 //  * leaves are never all materialised: the tree is split into 2^d subtrees
 //    whose leaves are multiplied by their plaintexts and accumulated into the
 //    output rows straight away (modular sums are exact, so the order of the
@@ -48,27 +51,46 @@ __device__ __forceinline__ ulonglong2 monomial_slot(const ulonglong2 *__restrict
     return W[__brev(t & (n - 1)) >> (32 - logn)];
 }
 
-// one level of the expansion for `count` nodes, nodes[count][2][l][N]:
-//   left[a]  = T[a] + R[a]
-//   right[a] = T[a] * X^k1 + R[a] * X^k2   (NTT domain)
-__global__ void k_expand_combine(const uint64_t *__restrict__ T, const uint64_t *__restrict__ R, uint64_t *left,
-                                 uint64_t *right, const PrimeConst *__restrict__ pc,
-                                 const ulonglong2 *__restrict__ tw, int l, int logn, uint32_t k1, uint32_t k2,
-                                 size_t total)
+// key-switch target of the automorphism: tgt[a][j][i] = nodes[a][1][j][tab[i]]
+__global__ void k_galois_c1(const uint64_t *__restrict__ nodes, const uint32_t *__restrict__ tab, uint64_t *tgt,
+                            int l, int logn, size_t total)
 {
-    const size_t mask = ((size_t)1 << logn) - 1;
+    const size_t N = (size_t)1 << logn, mask = N - 1;
     for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
-        const int limb = (int)((x >> logn) % (size_t)l);
+        const size_t row = x >> logn;  // a*l + j
+        const size_t a = row / (size_t)l, j = row % (size_t)l;
+        tgt[x] = nodes[((a * 2 + 1) * l + j) * N + tab[x & mask]];
+    }
+}
+
+// One expansion level after the key switch's inner products P and ModDown
+// terms T: R = apply_galois(T_a) = (perm(c0) | 0) + (P - T) * p^{-1}, then
+// left = node + R and right = node * X^k1 + R * X^k2, without writing R.
+__global__ void k_expand_fused(const uint64_t *__restrict__ nodes, const uint32_t *__restrict__ tab,
+                               const uint64_t *__restrict__ P, const uint64_t *__restrict__ T,
+                               const ulonglong2 *__restrict__ inv_p, uint64_t *left, uint64_t *right,
+                               const PrimeConst *__restrict__ pc, const ulonglong2 *__restrict__ tw, int l, int logn,
+                               uint32_t k1, uint32_t k2, size_t total)
+{
+    const size_t N = (size_t)1 << logn, mask = N - 1;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = x >> logn;          // (a*2 + comp)*l + limb
+        const int limb = (int)(row % (size_t)l);
+        const size_t ac = row / (size_t)l;     // a*2 + comp
+        const int comp = (int)(ac & 1);
         const uint32_t j = (uint32_t)(x & mask);
         const uint64_t q = pc[limb].q;
+        const ulonglong2 w = inv_p[limb];
+        uint64_t r = mul_shoup(P[(ac * (l + 1) + limb) * N + j] + q - T[x], w.x, w.y, q);
+        if (comp == 0) r = csub(r + nodes[((ac * l) + limb) * N + tab[j]], q);
+        const uint64_t a = nodes[x];
+        left[x] = csub(a + r, q);
         const ulonglong2 *W = tw + ((size_t)limb << logn);
-        const uint64_t a = T[x], b = R[x];
-        left[x] = csub(a + b, q);
         bool n1, n2;
         const ulonglong2 w1 = monomial_slot(W, k1, j, logn, n1);
         const ulonglong2 w2 = monomial_slot(W, k2, j, logn, n2);
         uint64_t u = mul_shoup(a, w1.x, w1.y, q);
-        uint64_t v = mul_shoup(b, w2.x, w2.y, q);
+        uint64_t v = mul_shoup(r, w2.x, w2.y, q);
         if (n1 && u) u = q - u;
         if (n2 && v) v = q - v;
         right[x] = csub(u + v, q);
@@ -137,25 +159,32 @@ __global__ void k_mm_accumulate(const uint64_t *__restrict__ leaves, const uint6
 
 // One expansion level for `count` nodes: nodes[count][2][l][N] -> next[2*count][2][l][N]
 // (left children first, then right children, the order of expand_ciphertext).
+// The automorphism's permutation is folded into the key-switch target gather
+// and into the epilogue, which also forms both children.
 static void expand_level(Context &c, const uint64_t *nodes, int count, int l, int level, const uint64_t *key,
-                         uint64_t *next, uint64_t *rot, cudaStream_t s)
+                         uint64_t *next, cudaStream_t s)
 {
-    const size_t N = c.n, per = (size_t)2 * l * N;
+    const size_t N = c.n, per = (size_t)2 * l * N, B = (size_t)count;
     const uint32_t n = (uint32_t)N;
     const uint32_t elt = (n + (1u << level)) / (1u << level);
     const uint32_t idx_raw = 2 * n - (1u << level);
     const uint32_t idx = (uint32_t)(((uint64_t)idx_raw * elt) % (2ull * n));
-    // rot = apply_galois(nodes): permute both components, c1 -> key-switch target
-    galois_permute(c, nodes, 2 * count, l, elt, rot, s);
-    uint64_t *tgt = nullptr;
-    if (cudaMallocAsync(&tgt, (size_t)count * l * N * 8, s) != cudaSuccess) throw std::runtime_error("cudaMallocAsync");
-    cudaMemcpy2DAsync(tgt, l * N * 8, rot + (size_t)l * N, per * 8, l * N * 8, count, cudaMemcpyDeviceToDevice, s);
-    cudaMemset2DAsync(rot + (size_t)l * N, per * 8, 0, l * N * 8, count, s);
-    switch_key_batch(c, rot, count, l, tgt, key, s);
-    cudaFreeAsync(tgt, s);
-    const size_t total = (size_t)count * per;
-    k_expand_combine<<<grid_for(total), kBlock, 0, s>>>(nodes, rot, next, next + (size_t)count * per, c.d_pc,
-                                                         c.d_tw_fwd, l, c.logn, idx_raw, idx, total); NEXUS_LAUNCHED();
+    const uint32_t *tab = c.galois_table(elt);
+    // scratch: tgt[B][l] | D[B][l][l+1] | P[B][2][l+1] | T[B][2][l] | last[B][2]
+    const size_t words = B * N * ((size_t)l + (size_t)l * (l + 1) + 2 * (size_t)(l + 1) + 2 * (size_t)l + 2);
+    uint64_t *tgt = c.get_scratch(words);
+    uint64_t *D = tgt + B * l * N;
+    uint64_t *P = D + B * l * (l + 1) * N;
+    uint64_t *T = P + B * 2 * (l + 1) * N;
+    uint64_t *last = T + B * 2 * l * N;
+    size_t total = B * l * N;
+    k_galois_c1<<<grid_for(total), kBlock, 0, s>>>(nodes, tab, tgt, l, c.logn, total); NEXUS_LAUNCHED();
+    ks_modup_inner(c, tgt, count, l, key, D, P, s);
+    ks_moddown_terms(c, P, count, l, T, last, s);
+    total = B * per;
+    k_expand_fused<<<grid_for(total), kBlock, 0, s>>>(nodes, tab, P, T, c.d_inv_q + (size_t)(c.k - 1) * c.k, next,
+                                                       next + B * per, c.d_pc, c.d_tw_fwd, l, c.logn, idx_raw, idx,
+                                                       total); NEXUS_LAUNCHED();
 }
 
 // ---------------------------------------------------------------- MMEvaluator
@@ -202,14 +231,13 @@ std::vector<Ciphertext> MMEvaluator::expand_ciphertext(const Ciphertext &encrypt
     while ((1u << logm) < m) ++logm;
     const int l = encrypted.limbs();
     const size_t per = (size_t)2 * l * c.n;
-    DeviceBuffer cur, next, rot;
+    DeviceBuffer cur, next;
     cur.reserve(per, s);
     cudaMemcpyAsync(cur.get(), encrypted.data(), per * 8, cudaMemcpyDeviceToDevice, s);
     int count = 1;
     for (int i = 0; i < logm; ++i) {
         next.reserve(per * 2 * count, s);
-        rot.reserve(per * count, s);
-        expand_level(c, cur.get(), count, l, i, key_for(rots[i]), next.get(), rot.get(), s);
+        expand_level(c, cur.get(), count, l, i, key_for(rots[i]), next.get(), s);
         std::swap(cur, next);
         count *= 2;
     }
@@ -270,7 +298,7 @@ void MMEvaluator::matrix_mul(const std::vector<const Ciphertext *> &compressed, 
 
     const int logn = c.logn;
     const int d = std::min(subtree_depth, logn);
-    DeviceBuffer roots, next, rot, cur;
+    DeviceBuffer roots, next, cur;
     for (size_t ci = 0; ci < compressed.size(); ++ci) {
         // rows touched by this ciphertext
         const long long e0 = (long long)ci * N, e1 = e0 + N;
@@ -284,8 +312,7 @@ void MMEvaluator::matrix_mul(const std::vector<const Ciphertext *> &compressed, 
         int count = 1;
         for (int i = 0; i < d; ++i) {
             next.reserve(per * 2 * count, s);
-            rot.reserve(per * count, s);
-            expand_level(c, roots.get(), count, l, i, key_for(rots[i]), next.get(), rot.get(), s);
+            expand_level(c, roots.get(), count, l, i, key_for(rots[i]), next.get(), s);
             std::swap(roots, next);
             count *= 2;
         }
@@ -296,8 +323,7 @@ void MMEvaluator::matrix_mul(const std::vector<const Ciphertext *> &compressed, 
             int cnt = 1;
             for (int i = d; i < logn; ++i) {
                 next.reserve(per * 2 * cnt, s);
-                rot.reserve(per * cnt, s);
-                expand_level(c, cur.get(), cnt, l, i, key_for(rots[i]), next.get(), rot.get(), s);
+                expand_level(c, cur.get(), cnt, l, i, key_for(rots[i]), next.get(), s);
                 std::swap(cur, next);
                 cnt *= 2;
             }

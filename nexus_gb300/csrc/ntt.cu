@@ -122,9 +122,12 @@ __device__ __forceinline__ int swz(int s) { return s + (s >> 4); }
 // ---------------------------------------------------------------- forward
 
 // Pass 1: size-2^LOGS transforms down the columns.  Output stays in [0,4q).
-template <int LOGS>
+// KIND selects the input (NttLoader): 0 the data itself, 1 the ModUp spread,
+// 2 the ModDown rounding spread of a key switch.
+template <int LOGS, int KIND>
 __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
-                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
+                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm,
+                                                       NttLoader ld)
 {
     constexpr int S = 1 << LOGS, T = S / kE, C = kThreads / T;
     __shared__ uint64_t sm[S * C];
@@ -139,8 +142,30 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
     const int c = threadIdx.x % C, t = threadIdx.x / C;
 
     uint64_t x[kE];
+    if (KIND == 0) {
 #pragma unroll
-    for (int k = 0; k < kE; ++k) x[k] = p[(size_t)(t + T * k) * n2 + c];
+        for (int k = 0; k < kE; ++k) x[k] = p[(size_t)(t + T * k) * n2 + c];
+    } else {
+        const size_t srow = pl / (size_t)ld.group;
+        const uint64_t *sp = ld.src + (srow << logn) + col0;
+        const uint64_t r1 = pc[prime].r1;
+        if (KIND == 1) {
+            const uint64_t qj = pc[(int)(srow % (size_t)ld.src_limbs)].q;
+#pragma unroll
+            for (int k = 0; k < kE; ++k) {
+                const uint64_t v = sp[(size_t)(t + T * k) * n2 + c];
+                x[k] = (q < qj) ? barrett_64(v, q, r1) : v;
+            }
+        } else {
+            const uint64_t P = pc[ld.special].q, h = P >> 1;
+            const uint64_t hr = (q < P) ? barrett_64(h, q, r1) : h;
+#pragma unroll
+            for (int k = 0; k < kE; ++k) {
+                const uint64_t v = csub(sp[(size_t)(t + T * k) * n2 + c] + h, P);
+                x[k] = ((q < P) ? barrett_64(v, q, r1) : v) + (q - hr);
+            }
+        }
+    }
     fwd_regs_strided(x, W, 1, q, q2);
 #pragma unroll
     for (int k = 0; k < kE; ++k) sm[(t + T * k) * C + c] = x[k];
@@ -260,14 +285,20 @@ __global__ void __launch_bounds__(kThreads) k_inv_cols(uint64_t *__restrict__ da
 }
 
 template <int L1, int L2>
-void launch_fwd(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s)
+void launch_fwd(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s, NttLoader ld = NttLoader())
 {
     const size_t limbs = n_polys * (size_t)lm.count;
     constexpr int C = kThreads / ((1 << L1) / kE);
     constexpr int R = kThreads / ((1 << L2) / kE);
     const unsigned g1 = (unsigned)(limbs * ((1u << L2) / C));
     const unsigned g2 = (unsigned)(limbs * ((1u << L1) / R));
-    k_fwd_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm); NEXUS_LAUNCHED();
+    if (ld.kind == 1)
+        k_fwd_cols<L1, 1><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
+    else if (ld.kind == 2)
+        k_fwd_cols<L1, 2><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
+    else
+        k_fwd_cols<L1, 0><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
+    NEXUS_LAUNCHED();
     k_fwd_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm); NEXUS_LAUNCHED();
 }
 
@@ -293,7 +324,7 @@ static void timing_mark(const Context &c, cudaStream_t s)
     c.ntt_events.push_back(e);
 }
 
-void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s)
+void ntt_forward_loaded(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, NttLoader ld, cudaStream_t s)
 {
     if (n_polys == 0 || lm.count == 0) return;
     if (c.ntt_timing) {
@@ -301,14 +332,19 @@ void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cuda
         c.ntt_limbs.push_back(n_polys * lm.count);
     }
     switch (c.logn) {
-    case 12: launch_fwd<6, 6>(c, d, n_polys, lm, s); break;
-    case 13: launch_fwd<6, 7>(c, d, n_polys, lm, s); break;
-    case 14: launch_fwd<7, 7>(c, d, n_polys, lm, s); break;
-    case 15: launch_fwd<7, 8>(c, d, n_polys, lm, s); break;
-    case 16: launch_fwd<8, 8>(c, d, n_polys, lm, s); break;
+    case 12: launch_fwd<6, 6>(c, d, n_polys, lm, s, ld); break;
+    case 13: launch_fwd<6, 7>(c, d, n_polys, lm, s, ld); break;
+    case 14: launch_fwd<7, 7>(c, d, n_polys, lm, s, ld); break;
+    case 15: launch_fwd<7, 8>(c, d, n_polys, lm, s, ld); break;
+    case 16: launch_fwd<8, 8>(c, d, n_polys, lm, s, ld); break;
     default: throw std::invalid_argument("unsupported log_n");
     }
     if (c.ntt_timing) timing_mark(c, s);
+}
+
+void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s)
+{
+    ntt_forward_loaded(c, d, n_polys, lm, NttLoader(), s);
 }
 
 void ntt_inverse(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s)

@@ -21,7 +21,23 @@ struct LimbMap {
     }
 };
 
+// Where the forward NTT's first pass reads its input.  Besides the in-place
+// transform it can fuse the two element-wise steps of a key switch that feed
+// an NTT: the ModUp spread (limb p of the output is row p / group of `src`,
+// a coefficient-form residue of prime (p / group) % src_limbs, reduced into the
+// output prime) and the ModDown rounding spread (row p / group of `src` is
+// the coefficient-form special limb x; the input is ((x + h) mod P) mod q
+// + (q - h mod q) with h = P/2 and P the prime `special`).
+struct NttLoader {
+    int kind = 0;                   // 0 in place, 1 ModUp spread, 2 rounding spread
+    const uint64_t *src = nullptr;
+    int group = 1;
+    int src_limbs = 1;
+    int special = 0;
+};
+
 void ntt_forward(const Context &c, uint64_t *data, size_t n_polys, LimbMap lm, cudaStream_t s);
+void ntt_forward_loaded(const Context &c, uint64_t *data, size_t n_polys, LimbMap lm, NttLoader ld, cudaStream_t s);
 void ntt_inverse(const Context &c, uint64_t *data, size_t n_polys, LimbMap lm, cudaStream_t s);
 
 // data: [n_polys][limb_end - limb_begin][N]; limb l of each polynomial uses

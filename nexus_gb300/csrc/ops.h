@@ -54,6 +54,15 @@ void switch_key(Context &c, uint64_t *ct, int limbs, const uint64_t *target, con
 void switch_key_batch(Context &c, uint64_t *ct, int batch, int limbs, const uint64_t *target, const uint64_t *key,
                       cudaStream_t s);
 
+// stages of the batched key switch, for callers that fuse their own epilogue:
+// ModUp + inner products (t [B][l] NTT-form targets, overwritten; D scratch
+// B*l*(l+1) limbs; P [B][2][l+1] out), then the ModDown rounding terms
+// (T [B][2][l] out; last scratch 2B limbs).  The result of the key switch is
+// (P[b][k][i] - T[b][k][i]) * p^{-1} mod q_i.
+void ks_modup_inner(Context &c, uint64_t *t, int B, int l, const uint64_t *key, uint64_t *D, uint64_t *P,
+                    cudaStream_t s);
+void ks_moddown_terms(Context &c, const uint64_t *P, int B, int l, uint64_t *T, uint64_t *last, cudaStream_t s);
+
 // relinearize a size-3 ciphertext into out2 (may alias ct3)
 void relinearize(Context &c, const uint64_t *ct3, int limbs, const uint64_t *key, uint64_t *out2, cudaStream_t s);
 

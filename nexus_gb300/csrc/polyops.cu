@@ -298,9 +298,13 @@ void rescale(const Context &c_in, const uint64_t *in, int size, int limbs, uint6
     k_gather_limb<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, (ulonglong2 *)last, limbs, limbs - 1, c.logn,
                                                    pr); NEXUS_LAUNCHED();
     ntt_inverse(c, last, size, LimbMap{1, limbs - 1, -1}, s);
-    size_t tot = (size_t)size * n;
-    k_round_spread<<<grid_for(tot), kBlock, 0, s>>>(last, t, c.d_pc, limbs - 1, limbs - 1, c.logn, tot); NEXUS_LAUNCHED();
-    ntt_forward(c, t, size, LimbMap{limbs - 1, 0, -1}, s);
+    // rounding spread fused into the first pass of the forward NTT
+    NttLoader ld;
+    ld.kind = 2;
+    ld.src = last;
+    ld.group = limbs - 1;
+    ld.special = limbs - 1;
+    ntt_forward_loaded(c, t, size, LimbMap{limbs - 1, 0, -1}, ld, s);
     pr = pairs_of(c, size, limbs - 1);
     k_rescale_finish<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, (const ulonglong2 *)t, (ulonglong2 *)out,
                                                       c.d_pc, c.d_inv_q + (size_t)(limbs - 1) * c.k, limbs, c.logn,
