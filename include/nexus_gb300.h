@@ -339,6 +339,65 @@ int nexus_matrix_mul(nexus_evaluator *ev, nexus_ciphertext *const *compressed, i
                      const uint64_t *d_pts, double pt_scale, int rows, int cols, double factor, const double *bias,
                      int bias_len, nexus_ciphertext *const *res);
 
+/* ------------------------------------------------------------------------
+ * Bootstrapping (src/bootstrapping/Bootstrapper.{h,cpp}, ModularReducer.cpp)
+ * ------------------------------------------------------------------------ */
+typedef struct nexus_bootstrapper nexus_bootstrapper;
+
+/* Bootstrapper::Bootstrapper (Bootstrapper.h:52-69, Bootstrapper.cpp:3-26):
+ * the evaluator's keys must hold the relinearisation key and the Galois keys
+ * of nexus_bootstrapper_add_rot_steps. */
+int nexus_bootstrapper_create(nexus_evaluator *ev, long loge, long logn, long logNh, long L, double final_scale,
+                              long boundary_K, long sin_cos_deg, long scale_factor, long inverse_deg,
+                              nexus_bootstrapper **out);
+int nexus_bootstrapper_destroy(nexus_bootstrapper *bs);
+
+/* Bootstrapper::prepare_mod_polynomial (Bootstrapper.cpp:1973-1977): the
+ * EvalMod polynomial heap (Polynomial::generate_poly_heap,
+ * common/Polynomial.cpp:168-214) as doubles.  node_len[i] is the number of
+ * Chebyshev coefficients of heap node i (0 = absent) for the 2^(heap_m+1)-1
+ * nodes; coeffs holds them back to back.  scale_inverse_coeff as in
+ * ModularReducer.cpp:38-46. */
+int nexus_bootstrapper_prepare_mod_polynomial(nexus_bootstrapper *bs, int heap_k, int heap_m, const int *node_len,
+                                              const double *coeffs, double scale_inverse_coeff);
+
+/* Bootstrapper::addLeftRotKeys_Linear_to_vector_3 (Bootstrapper.cpp:89-184):
+ * appends the missing rotation steps to steps[0..*count) (capacity entries). */
+int nexus_bootstrapper_add_rot_steps(const nexus_bootstrapper *bs, int *steps, int *count, int capacity);
+
+/* Bootstrapper::generate_LT_coefficient_3 (Bootstrapper.cpp:1967-1971). */
+int nexus_bootstrapper_generate_lt(nexus_bootstrapper *bs);
+
+/* The LT diagonals of genfftcoeff_3 / geninvfftcoeff_3
+ * (Bootstrapper.cpp:1144-1954) for 2^logn slots, host-only: which = 0..2
+ * fftcoeff1..3, 3..5 invfftcoeff1..3.  out = NULL queries *count diagonals
+ * of *len complex values; otherwise out[count][len][2] (re, im), shorter
+ * diagonals zero-padded.  No counterpart in the reference (the diagonals are
+ * Bootstrapper members there). */
+int nexus_lt_coefficients_3(int logn, int logNh, long boundary_K, int which, double *out, int *count, int *len);
+
+/* Bootstrapper::bootstrap_3 (Bootstrapper.cpp:3489-3495): ct (one data
+ * limb) is modulus-raised in place as in the reference; rtn receives the
+ * refreshed ciphertext at scale final_scale. */
+int nexus_bootstrap(nexus_bootstrapper *bs, nexus_ciphertext *ct, nexus_ciphertext *rtn);
+
+/* The stages of bootstrap_full_3 (Bootstrapper.cpp:3224-3244), for
+ * stage-wise checking: MODRAISE a in place (modraise_inplace :2937-2991);
+ * COEFFTOSLOT a -> r1, r2 (coefftoslot_full_3 :2741-2757);
+ * MODULAR_REDUCTION a -> r1 (ModularReducer::modular_reduction
+ * ModularReducer.cpp:58-78); SLOTTOCOEFF a, b -> r1 (slottocoeff_full_3
+ * :2759-2775); SET_INITIAL_SCALE from a's scale (bootstrap_3 :3490). */
+#define NEXUS_BOOT_MODRAISE 0
+#define NEXUS_BOOT_COEFFTOSLOT 1
+#define NEXUS_BOOT_MODULAR_REDUCTION 2
+#define NEXUS_BOOT_SLOTTOCOEFF 3
+#define NEXUS_BOOT_SET_INITIAL_SCALE 4
+int nexus_bootstrapper_stage(nexus_bootstrapper *bs, int stage, nexus_ciphertext *a, const nexus_ciphertext *b,
+                             nexus_ciphertext *r1, nexus_ciphertext *r2);
+
+/* Number of encoded LT diagonals the bootstrapper keeps on the device. */
+int nexus_bootstrapper_cached_plaintexts(const nexus_bootstrapper *bs, uint64_t *count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,6 +69,18 @@ SIGNATURES = [
     ("nexus_mm_expand", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     ("nexus_matrix_mul", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_int, C.c_int,
                                    C.c_double, C.c_void_p, C.c_int, C.c_void_p]),
+    ("nexus_bootstrapper_create", C.c_int, [C.c_void_p, C.c_long, C.c_long, C.c_long, C.c_long, C.c_double,
+                                            C.c_long, C.c_long, C.c_long, C.c_long, C.POINTER(C.c_void_p)]),
+    ("nexus_bootstrapper_destroy", C.c_int, [C.c_void_p]),
+    ("nexus_bootstrapper_prepare_mod_polynomial", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                                            C.POINTER(C.c_double), C.c_double]),
+    ("nexus_bootstrapper_add_rot_steps", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]),
+    ("nexus_bootstrapper_generate_lt", C.c_int, [C.c_void_p]),
+    ("nexus_lt_coefficients_3", C.c_int, [C.c_int, C.c_int, C.c_long, C.c_int, C.c_void_p, C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int)]),
+    ("nexus_bootstrap", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("nexus_bootstrapper_stage", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("nexus_bootstrapper_cached_plaintexts", C.c_int, [C.c_void_p, u64p]),
     ("nexus_plain_op", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
 ]

@@ -1,0 +1,122 @@
+// NEXUS's CKKS bootstrapping on the engine: Bootstrapper
+// (src/bootstrapping/Bootstrapper.{h,cpp}, the three-level BSGS "_3" path)
+// and ModularReducer (src/bootstrapping/ModularReducer.{h,cpp}) with the
+// heap-based polynomial evaluation of common/Polynomial.cpp:255-485.  Same
+// member names, arguments and call order, so the ciphertext words equal the
+// reference's for the same keys, input and EvalMod polynomial heap.
+//
+// Differences from the reference, none of which changes a result word:
+//  * the EvalMod polynomial (minimax cosine + heap split) is computed once
+//    offline in high precision and passed in as the doubles the reference
+//    encodes (the reference runs its NTL Remez in prepare_mod_polynomial);
+//  * every LT diagonal, once encoded at a given level and scale, is kept on
+//    the device and reused by later bootstraps (the reference re-encodes it
+//    each time; encoding is a pure function of values, scale and level).
+#pragma once
+#include <complex>
+#include <cstdint>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "ckks.h"
+
+namespace nexus {
+
+using CVec = std::vector<std::complex<double>>;
+
+// giantstep (common/func.cpp:204-214)
+int giantstep(int m);
+// rotation (common/func.cpp:216-225)
+void rotation(int logslot, int nh, int shiftcount, const CVec &vec, CVec &rtnvec);
+// genorigcoeff + genfftcoeff_3 + geninvfftcoeff_3 for one slot count 2^logn:
+// out = {fftcoeff1, fftcoeff2, fftcoeff3, invfftcoeff1, invfftcoeff2, invfftcoeff3}
+void lt_coefficients_3(long logn, long logNh, long boundary_K, std::vector<CVec> out[6]);
+
+class ModularReducer {
+public:
+    long boundary_K;
+    double log_width;
+    long deg;
+    long num_double_formula;
+    long inverse_deg;
+    double scale_inverse_coeff = 1.0;
+
+    // Polynomial heap of the scaled cosine (generate_poly_heap): node i holds
+    // its Chebyshev coefficients; an empty node is absent.
+    long heap_k = 0, heap_m = 0;
+    std::vector<std::vector<double>> heap;
+
+    ModularReducer(Evaluator &ev, long boundary_K, double log_width, long deg, long num_double_formula,
+                   long inverse_deg);
+    void set_polynomial_heap(long k, long m, std::vector<std::vector<double>> nodes, double scale_inverse_coeff);
+
+    void double_angle_formula(Ciphertext &cipher);
+    void double_angle_formula_scaled(Ciphertext &cipher, double scale_coeff);
+    void homomorphic_poly_evaluation(Ciphertext &rtn, const Ciphertext &cipher);
+    void modular_reduction(Ciphertext &rtn, const Ciphertext &cipher);
+
+private:
+    Evaluator *ev_;
+};
+
+class Bootstrapper {
+public:
+    long loge, logn, n, logNh, Nh, L;
+    double initial_scale = 0.0, final_scale;
+    long boundary_K, sin_cos_deg, scale_factor, inverse_deg;
+
+    std::vector<long> slot_vec;
+    long slot_index = 0;
+    // per slot_vec entry: the LT diagonals of the three levels
+    std::vector<std::vector<CVec>> fftcoeff1, fftcoeff2, fftcoeff3;
+    std::vector<std::vector<CVec>> invfftcoeff1, invfftcoeff2, invfftcoeff3;
+
+    ModularReducer mod_reducer;
+
+    Bootstrapper(Evaluator &ev, long loge, long logn, long logNh, long L, double final_scale, long boundary_K,
+                 long sin_cos_deg, long scale_factor, long inverse_deg);
+
+    void set_final_scale(double s) { final_scale = s; }
+    void prepare_mod_polynomial(long heap_k, long heap_m, std::vector<std::vector<double>> nodes,
+                                double scale_inverse_coeff);
+    void addLeftRotKeys_Linear_to_vector_3(std::vector<int> &gal_steps_vector) const;
+    void generate_LT_coefficient_3();
+    void change_logn(long new_logn);
+
+    void bsgs_linear_transform(Ciphertext &rtncipher, const Ciphertext &cipher, int totlen, int basicstep,
+                               int coeff_logn, const std::vector<CVec> &fftcoeff, int tag);
+    void rotated_bsgs_linear_transform(Ciphertext &rtncipher, const Ciphertext &cipher, int totlen, int basicstep,
+                                       int coeff_logn, const std::vector<CVec> &fftcoeff, int tag);
+
+    void sfl_3(Ciphertext &rtncipher, const Ciphertext &cipher);
+    void sfl_full_3(Ciphertext &rtncipher, const Ciphertext &cipher);
+    void sflinv_3(Ciphertext &rtncipher, const Ciphertext &cipher);
+    void sflinv_full_3(Ciphertext &rtncipher, const Ciphertext &cipher);
+    void coefftoslot_3(Ciphertext &rtncipher, const Ciphertext &cipher);
+    void slottocoeff_3(Ciphertext &rtncipher, const Ciphertext &cipher);
+    void coefftoslot_full_3(Ciphertext &rtncipher1, Ciphertext &rtncipher2, const Ciphertext &cipher);
+    void slottocoeff_full_3(Ciphertext &rtncipher, const Ciphertext &cipher1, const Ciphertext &cipher2);
+    void modraise_inplace(Ciphertext &cipher);
+
+    void bootstrap_sparse_3(Ciphertext &rtncipher, Ciphertext &cipher);
+    void bootstrap_full_3(Ciphertext &rtncipher, Ciphertext &cipher);
+    void bootstrap_3(Ciphertext &rtncipher, Ciphertext &cipher);
+    void bootstrap_inplace_3(Ciphertext &cipher);
+
+    // device copies of encoded diagonals kept between bootstraps
+    size_t cached_plaintexts() const { return cache_.size(); }
+    void clear_cache() { cache_.clear(); }
+
+private:
+    // multiply_vector_reduced_error of `ct` by rotation(coeff_logn, Nh, shift, v),
+    // with the encoded diagonal taken from (or put into) the cache
+    void mul_diagonal(const Ciphertext &ct, int tag, int index, int shift, int coeff_logn, const CVec &v,
+                      uint64_t salt, Ciphertext &out);
+    Evaluator *ev_;
+    using Key = std::tuple<int, int, int, int, uint64_t, uint64_t>;
+    std::map<Key, Plaintext> cache_;
+    uint64_t salt_ = 0;  // distinguishes diagonals that depend on the scales of the call
+};
+
+}  // namespace nexus

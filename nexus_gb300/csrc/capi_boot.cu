@@ -1,0 +1,171 @@
+// C ABI of the bootstrapper (declared in include/nexus_gb300.h).
+#include <stdexcept>
+#include <string>
+
+#include "../../include/nexus_gb300.h"
+#include "bootstrap.h"
+#include "capi_types.h"
+
+using namespace nexus;
+
+struct nexus_bootstrapper {
+    nexus_evaluator *ev;
+    Bootstrapper bs;
+};
+
+namespace {
+
+int fail(const char *fn, const std::string &msg)
+{
+    set_error(std::string(fn) + ": " + msg);
+    return -1;
+}
+
+template <class F>
+int guarded(const char *fn, F &&f)
+{
+    try {
+        f();
+    } catch (const std::exception &e) {
+        return fail(fn, e.what());
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(fn, cudaGetErrorString(e));
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int nexus_bootstrapper_create(nexus_evaluator *ev, long loge, long logn, long logNh, long L,
+                                         double final_scale, long boundary_K, long sin_cos_deg, long scale_factor,
+                                         long inverse_deg, nexus_bootstrapper **out)
+{
+    static const char *fn = "nexus_bootstrapper_create";
+    if (!ev || !out) return fail(fn, "null argument");
+    *out = nullptr;
+    return guarded(fn, [&] {
+        *out = new nexus_bootstrapper{ev, Bootstrapper(ev->ev, loge, logn, logNh, L, final_scale, boundary_K,
+                                                       sin_cos_deg, scale_factor, inverse_deg)};
+    });
+}
+
+extern "C" int nexus_bootstrapper_destroy(nexus_bootstrapper *bs)
+{
+    delete bs;
+    return 0;
+}
+
+extern "C" int nexus_bootstrapper_prepare_mod_polynomial(nexus_bootstrapper *bs, int heap_k, int heap_m,
+                                                         const int *node_len, const double *coeffs,
+                                                         double scale_inverse_coeff)
+{
+    static const char *fn = "nexus_bootstrapper_prepare_mod_polynomial";
+    if (!bs || !node_len || !coeffs) return fail(fn, "null argument");
+    if (heap_m < 0 || heap_m > 16) return fail(fn, "heap_m out of range");
+    return guarded(fn, [&] {
+        const int len = (1 << (heap_m + 1)) - 1;
+        std::vector<std::vector<double>> nodes(len);
+        size_t off = 0;
+        for (int i = 0; i < len; i++) {
+            if (node_len[i] < 0) throw std::invalid_argument("negative node length");
+            nodes[i].assign(coeffs + off, coeffs + off + node_len[i]);
+            off += (size_t)node_len[i];
+        }
+        bs->bs.prepare_mod_polynomial(heap_k, heap_m, std::move(nodes), scale_inverse_coeff);
+    });
+}
+
+extern "C" int nexus_bootstrapper_add_rot_steps(const nexus_bootstrapper *bs, int *steps, int *count, int capacity)
+{
+    static const char *fn = "nexus_bootstrapper_add_rot_steps";
+    if (!bs || !steps || !count) return fail(fn, "null argument");
+    return guarded(fn, [&] {
+        std::vector<int> v(steps, steps + *count);
+        bs->bs.addLeftRotKeys_Linear_to_vector_3(v);
+        if ((int)v.size() > capacity) throw std::length_error("capacity too small");
+        for (size_t i = 0; i < v.size(); i++) steps[i] = v[i];
+        *count = (int)v.size();
+    });
+}
+
+extern "C" int nexus_bootstrapper_generate_lt(nexus_bootstrapper *bs)
+{
+    static const char *fn = "nexus_bootstrapper_generate_lt";
+    if (!bs) return fail(fn, "null argument");
+    return guarded(fn, [&] { bs->bs.generate_LT_coefficient_3(); });
+}
+
+extern "C" int nexus_lt_coefficients_3(int logn, int logNh, long boundary_K, int which, double *out, int *count,
+                                       int *len)
+{
+    static const char *fn = "nexus_lt_coefficients_3";
+    if (!count || !len) return fail(fn, "null argument");
+    if (which < 0 || which > 5) return fail(fn, "which must be 0..5");
+    if (logn < 1 || logn > logNh || logNh > 16) return fail(fn, "bad logn / logNh");
+    try {
+        std::vector<CVec> v[6];
+        lt_coefficients_3(logn, logNh, boundary_K, v);
+        const std::vector<CVec> &d = v[which];
+        *count = (int)d.size();
+        *len = 0;
+        for (const CVec &x : d)
+            if ((int)x.size() > *len) *len = (int)x.size();
+        if (!out) return 0;
+        for (size_t i = 0; i < d.size(); i++)
+            for (int j = 0; j < *len; j++) {
+                const std::complex<double> z = j < (int)d[i].size() ? d[i][j] : std::complex<double>(0, 0);
+                out[((size_t)i * *len + j) * 2] = z.real();
+                out[((size_t)i * *len + j) * 2 + 1] = z.imag();
+            }
+    } catch (const std::exception &e) {
+        return fail(fn, e.what());
+    }
+    return 0;
+}
+
+extern "C" int nexus_bootstrap(nexus_bootstrapper *bs, nexus_ciphertext *ct, nexus_ciphertext *rtn)
+{
+    static const char *fn = "nexus_bootstrap";
+    if (!bs || !ct || !rtn) return fail(fn, "null argument");
+    if (ct == rtn) return fail(fn, "rtn must be a different ciphertext");
+    return guarded(fn, [&] { bs->bs.bootstrap_3(rtn->ct, ct->ct); });
+}
+
+extern "C" int nexus_bootstrapper_stage(nexus_bootstrapper *bs, int stage, nexus_ciphertext *a,
+                                        const nexus_ciphertext *b, nexus_ciphertext *r1, nexus_ciphertext *r2)
+{
+    static const char *fn = "nexus_bootstrapper_stage";
+    if (!bs || !a) return fail(fn, "null argument");
+    return guarded(fn, [&] {
+        Bootstrapper &B = bs->bs;
+        switch (stage) {
+        case NEXUS_BOOT_MODRAISE:
+            B.modraise_inplace(a->ct);
+            break;
+        case NEXUS_BOOT_COEFFTOSLOT:
+            if (!r1 || !r2) throw std::invalid_argument("null result");
+            B.coefftoslot_full_3(r1->ct, r2->ct, a->ct);
+            break;
+        case NEXUS_BOOT_MODULAR_REDUCTION:
+            if (!r1) throw std::invalid_argument("null result");
+            B.mod_reducer.modular_reduction(r1->ct, a->ct);
+            break;
+        case NEXUS_BOOT_SLOTTOCOEFF:
+            if (!b || !r1) throw std::invalid_argument("null argument");
+            B.slottocoeff_full_3(r1->ct, a->ct, b->ct);
+            break;
+        case NEXUS_BOOT_SET_INITIAL_SCALE:
+            B.initial_scale = a->ct.scale();
+            break;
+        default:
+            throw std::invalid_argument("unknown stage");
+        }
+    });
+}
+
+extern "C" int nexus_bootstrapper_cached_plaintexts(const nexus_bootstrapper *bs, uint64_t *count)
+{
+    if (!bs || !count) return fail("nexus_bootstrapper_cached_plaintexts", "null argument");
+    *count = bs->bs.cached_plaintexts();
+    return 0;
+}

@@ -5,22 +5,9 @@
 #include <string>
 
 #include "../../include/nexus_gb300.h"
-#include "ckks.h"
-#include "nexus_ops.h"
+#include "capi_types.h"
 
 using namespace nexus;
-
-struct nexus_evaluator {
-    nexus_context *ctx;
-    Evaluator ev;
-    CKKSEvaluator ck;
-    nexus_evaluator(nexus_context *c, double scale) : ctx(c), ev(c->c), ck(ev, scale) {}
-};
-
-struct nexus_ciphertext {
-    nexus_context *ctx;
-    Ciphertext ct;
-};
 
 namespace {
 

@@ -144,3 +144,89 @@ class Evaluator:
                                      int(cols), float(factor), None if b is None else b.ctypes.data,
                                      0 if b is None else b.size, out), "nexus_matrix_mul")
         return res
+
+
+BOOT_MODRAISE, BOOT_COEFFTOSLOT, BOOT_MODULAR_REDUCTION, BOOT_SLOTTOCOEFF, BOOT_SET_INITIAL_SCALE = range(5)
+
+
+class Bootstrapper:
+    """Bootstrapper (src/bootstrapping/Bootstrapper.h:52-69) over an Evaluator
+    whose keys include the relinearisation key and the Galois keys of
+    ``rotation_steps()``."""
+
+    def __init__(self, evaluator: Evaluator, loge: int, logn: int, logNh: int, L: int, final_scale: float,
+                 boundary_K: int, sin_cos_deg: int, scale_factor: int, inverse_deg: int):
+        self.ev = evaluator
+        self.ctx = evaluator.ctx
+        self.params = dict(boundary_k=boundary_K, deg=sin_cos_deg, loge=loge, double_angle=scale_factor,
+                           inverse_deg=inverse_deg)
+        h = C.c_void_p()
+        check(lib().nexus_bootstrapper_create(evaluator._h, loge, logn, logNh, L, float(final_scale), boundary_K,
+                                              sin_cos_deg, scale_factor, inverse_deg, C.byref(h)),
+              "nexus_bootstrapper_create")
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nexus_bootstrapper_destroy(self._h)
+            self._h = None
+
+    def prepare_mod_polynomial(self, table: dict | None = None):
+        """Load the EvalMod heap (nexus_gb300.remez.load_table for this
+        Bootstrapper's parameters unless a table is given)."""
+        from .remez import load_table
+        t = table or load_table(**self.params)
+        size = (1 << (t["heap_m"] + 1)) - 1
+        lens = (C.c_int * size)(*[len(t["nodes"].get(i, [])) for i in range(size)])
+        flat = [c for i in range(size) for c in t["nodes"].get(i, [])]
+        coeffs = (C.c_double * len(flat))(*flat)
+        check(lib().nexus_bootstrapper_prepare_mod_polynomial(self._h, t["heap_k"], t["heap_m"], lens, coeffs,
+                                                              float(t["scale_inverse_coeff"])),
+              "nexus_bootstrapper_prepare_mod_polynomial")
+
+    def addLeftRotKeys_Linear_to_vector_3(self, gal_steps_vector: list) -> None:
+        cap = len(gal_steps_vector) + 256
+        arr = (C.c_int * cap)(*gal_steps_vector)
+        cnt = C.c_int(len(gal_steps_vector))
+        check(lib().nexus_bootstrapper_add_rot_steps(self._h, arr, C.byref(cnt), cap),
+              "nexus_bootstrapper_add_rot_steps")
+        gal_steps_vector[:] = list(arr[:cnt.value])
+
+    def rotation_steps(self, log_nh: int) -> list:
+        """The reference driver's key steps (src/bootstrapping.cpp:111-118):
+        0, 2^i for i < logNh, then addLeftRotKeys_Linear_to_vector_3."""
+        steps = [0] + [1 << i for i in range(log_nh)]
+        self.addLeftRotKeys_Linear_to_vector_3(steps)
+        return steps
+
+    def generate_LT_coefficient_3(self):
+        check(lib().nexus_bootstrapper_generate_lt(self._h), "nexus_bootstrapper_generate_lt")
+
+    def bootstrap_3(self, ct: Ciphertext) -> Ciphertext:
+        """Refresh ``ct`` (one data limb; modulus-raised in place as in the
+        reference) and return the new ciphertext."""
+        rtn = Ciphertext(self.ctx)
+        check(lib().nexus_bootstrap(self._h, ct.handle, rtn.handle), "nexus_bootstrap")
+        return rtn
+
+    def stage(self, stage: int, a: Ciphertext, b: Ciphertext | None = None):
+        r1, r2 = Ciphertext(self.ctx), Ciphertext(self.ctx)
+        check(lib().nexus_bootstrapper_stage(self._h, stage, a.handle, None if b is None else b.handle, r1.handle,
+                                             r2.handle), "nexus_bootstrapper_stage")
+        return r1, r2
+
+    def cached_plaintexts(self) -> int:
+        n = C.c_uint64()
+        check(lib().nexus_bootstrapper_cached_plaintexts(self._h, C.byref(n)), "nexus_bootstrapper_cached_plaintexts")
+        return n.value
+
+
+def lt_coefficients_3(logn: int, log_nh: int, boundary_k: int, which: int) -> np.ndarray:
+    """The engine's host-computed LT diagonals (complex [count][len])."""
+    cnt, ln = C.c_int(), C.c_int()
+    check(lib().nexus_lt_coefficients_3(logn, log_nh, boundary_k, which, None, C.byref(cnt), C.byref(ln)),
+          "nexus_lt_coefficients_3")
+    out = np.zeros((cnt.value, ln.value, 2))
+    check(lib().nexus_lt_coefficients_3(logn, log_nh, boundary_k, which, out.ctypes.data, C.byref(cnt),
+                                        C.byref(ln)), "nexus_lt_coefficients_3")
+    return out

@@ -1,0 +1,139 @@
+"""Bootstrapping on the GPU engine against the oracle restatement
+(oracle/bootstrap.py), word for word, stage by stage and end to end, plus the
+decrypted error of the refreshed ciphertext against the input values.
+
+Parameters follow the reference driver (src/bootstrapping.cpp:33-63) at a
+smaller ring: N = 2^13 with all 2^12 slots (the full-slot path), q0 51 bits,
+two 46-bit primes, fourteen 51-bit bootstrapping primes, a 51-bit special
+prime, sparse secret of Hamming weight 192, K = 25, cosine degree 59, two
+double-angle steps, loge = 10, scale 2^46."""
+import numpy as np
+import pytest
+
+from oracle import bootstrap as B
+from oracle import nexus_l3 as L
+from oracle import pyoracle as po
+from tests.util import to_host
+
+pytestmark = pytest.mark.gpu
+
+LOG_N = 13
+N = 1 << LOG_N
+LOG_NH = LOG_N - 1
+SCALE = 2.0 ** 46
+BITS = [51] + [46] * 2 + [51] * 14 + [51]
+PARAMS = dict(loge=10, logn=LOG_NH, logNh=LOG_NH, L=len(BITS) - 2, final_scale=SCALE, boundary_K=25,
+              sin_cos_deg=59, scale_factor=2, inverse_deg=1)
+
+
+@pytest.fixture(scope="module")
+def env(cuda):
+    import nexus_gb300 as ng
+    from nexus_gb300.operators import Bootstrapper, Evaluator
+    from nexus_gb300.remez import load_table
+    qs = ng.create_coeff_modulus(N, BITS)
+    ctx = ng.Context(LOG_N, qs)
+    sk = ctx.keygen_secret(seed=41, hamming_weight=192)
+    rk = ctx.keygen_relin(sk, seed=42)
+    steps = B.rot_key_steps_3(LOG_NH, LOG_NH)
+    gks = {ctx.galois_elt(st): ctx.keygen_galois(sk, ctx.galois_elt(st), seed=43 + i) for i, st in enumerate(steps)}
+    ev = Evaluator(ctx, SCALE, rk, gks)
+    bs = Bootstrapper(ev, **PARAMS)
+    bs.prepare_mod_polynomial()
+    bs.generate_LT_coefficient_3()
+    table = load_table()
+    oev = L.Evaluator(po.OracleContext(LOG_N, qs), to_host(rk), {e: to_host(k) for e, k in gks.items()})
+    obs = B.Bootstrapper(oev, PARAMS["loge"], LOG_NH, LOG_NH, PARAMS["L"], SCALE, 25, 59, 2, 1, table)
+    obs.generate_LT_coefficient_3()
+    return ctx, sk, bs, obs, steps
+
+
+def _input(ctx, sk, seed):
+    """Encrypt U(-1, 1) slots at the top level and keep the q0 limb only."""
+    import torch
+    from nexus_gb300.operators import Ciphertext
+    vals = np.random.default_rng(seed).uniform(-1, 1, N // 2)
+    top = len(ctx.moduli) - 1
+    pt = torch.empty((top, N), dtype=torch.int64, device="cuda")
+    ctx.encode(vals, SCALE, top, pt)
+    ct = ctx.encrypt_symmetric(sk, pt, top, seed)
+    low = to_host(ct)[:, :1, :].copy()
+    return vals, Ciphertext.from_numpy(ctx, low, SCALE), L.Ct(low, SCALE)
+
+
+def _same(eng, orc):
+    assert eng.scale == orc.scale
+    assert np.array_equal(eng.to_numpy(), orc.data)
+
+
+def _decrypt(ctx, sk, ct):
+    return ctx.decode(ctx.decrypt(sk, ct.to_device()), ct.scale).real
+
+
+def test_rotation_steps_match(env):
+    ctx, sk, bs, obs, steps = env
+    assert bs.rotation_steps(LOG_NH) == steps
+
+
+def test_stages_match_oracle(env):
+    from nexus_gb300.operators import (BOOT_COEFFTOSLOT, BOOT_MODRAISE, BOOT_MODULAR_REDUCTION,
+                                       BOOT_SET_INITIAL_SCALE, BOOT_SLOTTOCOEFF, Ciphertext)
+    ctx, sk, bs, obs, _ = env
+    _, x, ox = _input(ctx, sk, 5)
+    bs.stage(BOOT_SET_INITIAL_SCALE, x)
+    obs.initial_scale = ox.scale
+    bs.stage(BOOT_MODRAISE, x)
+    oraised = obs.modraise_inplace(ox)
+    _same(x, oraised)
+
+    q0 = float(ctx.moduli[0])
+    x = Ciphertext.from_numpy(ctx, oraised.data, q0)
+    oraised.scale = q0
+    r1, r2 = bs.stage(BOOT_COEFFTOSLOT, x)
+    o1, o2 = obs.coefftoslot_full_3(oraised)
+    _same(r1, o1)
+    _same(r2, o2)
+
+    m1, _ = bs.stage(BOOT_MODULAR_REDUCTION, r1)
+    om1 = obs.modular_reduction(o1)
+    _same(m1, om1)
+    m2, _ = bs.stage(BOOT_MODULAR_REDUCTION, r2)
+    om2 = obs.modular_reduction(o2)
+    _same(m2, om2)
+
+    out, _ = bs.stage(BOOT_SLOTTOCOEFF, m1, m2)
+    _same(out, obs.slottocoeff_full_3(om1, om2))
+
+
+def test_bootstrap_matches_oracle_and_refreshes(env):
+    ctx, sk, bs, obs, _ = env
+    vals, x, ox = _input(ctx, sk, 7)
+    before = _decrypt(ctx, sk, x)
+    out = bs.bootstrap_3(x)
+    oout = obs.bootstrap_3(ox)
+    _same(out, oout)
+    after = _decrypt(ctx, sk, out)
+    err = np.abs(after - before)
+    assert out.info()[1] >= 2
+    assert err.max() < 2.0 ** -12, err.max()
+
+
+def test_second_bootstrap_reuses_encoded_diagonals(env):
+    ctx, sk, bs, obs, _ = env
+    _, x1, _ = _input(ctx, sk, 9)
+    _, x2, _ = _input(ctx, sk, 9)
+    a = bs.bootstrap_3(x1)
+    cached = bs.cached_plaintexts()
+    assert cached > 0
+    b = bs.bootstrap_3(x2)
+    assert bs.cached_plaintexts() == cached
+    assert np.array_equal(a.to_numpy(), b.to_numpy())
+
+
+def test_bootstrap_rejects_higher_level(env):
+    from nexus_gb300._lib import NexusError
+    from nexus_gb300.operators import Ciphertext
+    ctx, sk, bs, obs, _ = env
+    data = np.zeros((2, 2, N), dtype=np.uint64)
+    with pytest.raises(NexusError, match="lowest level"):
+        bs.bootstrap_3(Ciphertext.from_numpy(ctx, data, SCALE))
