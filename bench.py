@@ -5,7 +5,14 @@
 
 Prints ONE JSON line (rank 0).  Workloads:
 
-  matmul (default) NEXUS's ct x pt MatMul at the BERT-base shape: an encrypted
+  bootstrap (default) NEXUS's full-slot CKKS bootstrap (Bootstrapper::bootstrap_3,
+        three-level BSGS CoeffToSlot / EvalMod / SlotToCoeff) at N = 2^16 with
+        all 32768 slots: primes 51 + 16 x 46 + 14 x 51 + special 51, sparse
+        secret of Hamming weight 192, K = 25, cosine degree 59, two double
+        angles, scale 2^46; one step = 16 one-limb ciphertexts of U(-1,1)
+        slots refreshed.  Keys (~49 GB) stay resident; no L2 flush needed.
+
+  matmul NEXUS's ct x pt MatMul at the BERT-base shape: an encrypted
         128 x 768 input of N(0,1), coefficient-packed into 2 ciphertexts,
         times plaintext weights 768 x 768 of N(0, 0.02) plus a bias of 768,
         at N = 2^16 with primes {60, 40, 60} (one 60-bit special prime), scale
@@ -19,8 +26,8 @@ Prints ONE JSON line (rank 0).  Workloads:
         of uniform residues = 3072 limb-NTTs per step, one engine call per
         step.  Inputs (1.5 GiB) are larger than L2, so no flush is needed.
 
-`--impl reference` times the CPU restatement of SEAL's NTT (the oracle port,
-all host threads) on a bounded sample of the same workload.  Under torchrun
+`--impl reference` times the CPU restatement (the oracle port, all host
+threads) on a bounded sample of the same workload.  Under torchrun
 (N>1) every rank runs an independent replica (the path has no exchange step),
 the timed region is bracketed by barriers and the slowest rank's time is used.
 """
@@ -463,6 +470,243 @@ def cpu_mm_sample(workers: int = 1, depth: int = 7):
                       f"extrapolated to 2 x 65535 nodes + 98304 products"}
 
 
+# ----------------------------------------------------------------------------- bootstrap workload
+
+BOOT_LOGN = 16
+BOOT_BITS = [51] + [46] * 16 + [51] * 14 + [51]
+BOOT_SCALE = 2.0 ** 46
+BOOT_CTS = 16
+BOOT_PARAMS = dict(loge=10, logn=BOOT_LOGN - 1, logNh=BOOT_LOGN - 1, L=len(BOOT_BITS) - 2, final_scale=BOOT_SCALE,
+                   boundary_K=25, sin_cos_deg=59, scale_factor=2, inverse_deg=1)
+
+
+def boot_config(n_keys=None):
+    return {"workload": f"bootstrap_full_n65536_{BOOT_CTS}ct", "N": 1 << BOOT_LOGN, "slots": 1 << (BOOT_LOGN - 1),
+            "moduli_bits": "51 + 16x46 + 14x51 + special 51", "hamming_weight": 192, "boundary_K": 25,
+            "sin_cos_deg": 59, "double_angle": 2, "inverse_deg": 1, "loge": 10, "scale": "2^46",
+            "cts_per_step": BOOT_CTS, "galois_keys": n_keys, "parallelism": "replicas",
+            "l2": "keys (~49 GB) and per-step ciphertext traffic far above L2, no flush"}
+
+
+def run_boot_gpu(args, rank, world):
+    import numpy as np
+    import torch
+
+    import nexus_gb300 as ng
+    from nexus_gb300.operators import Bootstrapper, Ciphertext, Evaluator
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = 1 << BOOT_LOGN
+    qs = ng.create_coeff_modulus(n, BOOT_BITS)
+    ctx = ng.Context(BOOT_LOGN, qs)
+    sk = ctx.keygen_secret(seed=71 + rank, hamming_weight=192)
+    rk = ctx.keygen_relin(sk, seed=72)
+    ev = Evaluator(ctx, BOOT_SCALE, rk)
+    bs = Bootstrapper(ev, **BOOT_PARAMS)
+    steps = bs.rotation_steps(BOOT_LOGN - 1)
+    for i, st in enumerate(steps):
+        e = ctx.galois_elt(st)
+        ev.add_galois_key(e, ctx.keygen_galois(sk, e, seed=1000 + i))
+    bs.prepare_mod_polynomial()
+    bs.generate_LT_coefficient_3()
+    top = len(qs) - 1
+    rng = np.random.default_rng(4096 + rank)
+    vals, inputs, host_in = [], [], []
+    for i in range(BOOT_CTS):
+        v = rng.uniform(-1, 1, n // 2)
+        pt = torch.empty((top, n), dtype=torch.int64, device=dev)
+        ctx.encode(v, BOOT_SCALE, top, pt)
+        ct = ctx.encrypt_symmetric(sk, pt, top, 500 + i)
+        low = ct[:, :1, :].contiguous()
+        vals.append(v)
+        inputs.append(low)
+        host_in.append(low.cpu().numpy().view(np.uint64).copy())
+        del pt, ct
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        return [bs.bootstrap_3(Ciphertext.from_device(ctx, x, BOOT_SCALE)) for x in inputs]
+
+    for _ in range(args.warmup):
+        res = step()
+    torch.cuda.synchronize(dev)
+    dec = ctx.decode(ctx.decrypt(sk, res[0].to_device()), res[0].scale).real
+    err = float(np.max(np.abs(dec - vals[0])))
+    out_limbs = res[0].info()[1]
+    del res
+    barrier(world)
+    l0 = ng.kernel_launches()
+    # engine launches before the timed region: the -s value of a launch-list capture
+    print(f"engine_launches_before_timed={l0}", file=sys.stderr, flush=True)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize(dev)
+        t0.record(stream)
+        for _ in range(args.steps):
+            res = step()
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = ng.kernel_launches() - l0
+    barrier(world)
+    total_ms = max_over_ranks(t0.elapsed_time(t1), world)
+    del res
+
+    ctx.ntt_timing_begin()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    res = step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ntt_ms, ntt_calls, ntt_limbs = ctx.ntt_timing_end()
+    instr_ms = e0.elapsed_time(e1)
+    del res
+
+    # end to end through the C ABI: one-limb ciphertexts from pinned host
+    # memory, bootstrap, refreshed ciphertexts back to the host
+    h_in = [torch.from_numpy(h.view(np.int64)).pin_memory() for h in host_in]
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    w0 = time.perf_counter()
+    out_bytes = 0
+    for h in h_in:
+        c = Ciphertext(ctx)
+        ng.check(ng.lib().nexus_ciphertext_load(c.handle, h.data_ptr(), 2, 1, BOOT_SCALE, 1, None), "load")
+        out_bytes += bs.bootstrap_3(c).to_numpy().nbytes
+    torch.cuda.synchronize(dev)
+    e2e_s = max_over_ranks(time.perf_counter() - w0, world)
+    in_bytes = sum(h.nbytes for h in host_in)
+
+    step_ms = total_ms / args.steps
+    value = world * args.steps * BOOT_CTS / (total_ms / 1e3)
+    peak, peak_kind = _peak_hbm()
+    ntt_avg_ms = ntt_ms / max(1, ntt_calls)
+    alg_bytes_per_call = 16.0 * n * ntt_limbs / max(1, ntt_calls)
+    achieved = alg_bytes_per_call / (ntt_avg_ms / 1e3) / 1e9
+    res = {
+        "metric": "bootstrap_throughput_n65536",
+        "value": value,
+        "unit": "bootstraps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic: slots ~ U(-1,1), seeded; engine-generated keys (sparse secret h=192)",
+        "config": boot_config(len(steps)),
+        "accuracy": {"max_abs_err_vs_input": err, "precision_bits": -float(np.log2(err)),
+                     "output_limbs": out_limbs},
+        "roofline": {
+            "kernel": "nexus NTT launches inside the bootstrap (k_fwd/k_inv cols+rows)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": alg_bytes_per_call,
+            "avg_launch_ms": ntt_avg_ms, "launches_per_step": ntt_calls, "limb_ntts_per_step": ntt_limbs,
+            "share_of_step": ntt_ms / instr_ms,
+            "traffic": _profile_traffic(f"bootstrap_full_n65536_{BOOT_CTS}ct"),
+        },
+        "e2e": {"value": world * BOOT_CTS / e2e_s, "unit": "bootstraps/s", "h2d_bytes_per_step": in_bytes,
+                "d2h_bytes_per_step": out_bytes},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+    }
+    if rank == 0 and world == 1:
+        res["cpu_baseline"] = cpu_boot_sample(workers=1)
+    return res
+
+
+def _boot_cpu_worker(seed):
+    """Time the oracle port's ring operations at N=2^16 on this core:
+    key switches at three levels (a quadratic in the limb count), and rescale,
+    tensor, plaintext product, addition, encode and the modulus raise."""
+    import numpy as np
+
+    from oracle import nexus_l3 as L
+    from oracle import pyoracle as po
+    n = 1 << BOOT_LOGN
+    qs = po.create_coeff_modulus(n, BOOT_BITS)
+    oc = po.OracleContext(BOOT_LOGN, qs)
+    rng = np.random.default_rng(seed)
+    elt = po.galois_elt_from_step(BOOT_LOGN, 1)
+    # random keys cost exactly what real ones do (nothing is decrypted here)
+    key = po.random_residues(rng, (len(qs) - 1, 2, len(qs), n), qs)
+    ev = L.Evaluator(oc, key, {elt: key})
+
+    def ct(limbs, size=2):
+        return L.Ct(po.random_residues(rng, (size, limbs, n), qs[:limbs]), BOOT_SCALE)
+
+    def timed(f):
+        t = time.perf_counter()
+        f()
+        return time.perf_counter() - t
+
+    ks = {l: timed(lambda: ev.apply_galois(ct(l), elt)) for l in (31, 24, 18)}
+    top = len(qs) - 1
+    per_limb = {
+        "rescale": timed(lambda: ev.rescale(ct(top))) / top,
+        "tensor": timed(lambda: ev.multiply(ct(top), ct(top))) / top,
+        "mul_plain": timed(lambda: ev.multiply_plain(ct(top), L.Pt(1.0, data=ct(top, 1).data[0]))) / top,
+        "add": timed(lambda: ev.add(ct(top), ct(top))) / top,
+    }
+    v = rng.uniform(-1, 1, n // 2)
+    e_top = timed(lambda: ev.encode(v, 2.0 ** 40, top))
+    e_one = timed(lambda: ev.encode(v, 2.0 ** 40, 1))
+    raise_s = timed(lambda: oc.ntt(oc.ntt(ct(1).data, 0, 1, inverse=True), 0, 1)) + per_limb["rescale"] * top
+    return ks, per_limb, (e_one, (e_top - e_one) / (top - 1)), raise_s
+
+
+def cpu_boot_sample(workers: int = 1):
+    """The oracle port on the host cores: per-operation times at N=2^16
+    (bounded sample) times the exact operation counts of one bootstrap_3
+    (oracle/opcount.py), giving the modelled time of one bootstrap per core."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+
+    import numpy as np
+
+    from nexus_gb300.remez import load_table
+    from oracle import opcount
+    from oracle import pyoracle as po
+    qs = po.create_coeff_modulus(1 << BOOT_LOGN, BOOT_BITS)
+    counts = opcount.bootstrap_op_counts(qs, BOOT_LOGN, BOOT_LOGN - 1, load_table())
+    w0 = time.perf_counter()
+    if workers <= 1:
+        outs = [_boot_cpu_worker(0)]
+    else:
+        with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            outs = list(ex.map(_boot_cpu_worker, range(workers)))
+    wall = time.perf_counter() - w0
+    totals = []
+    for ks, per_limb, (e0, e1), raise_s in outs:
+        ls = sorted(ks)
+        coef = np.polyfit(ls, [ks[l] for l in ls], 2)
+        t = 0.0
+        for (name, limbs), k in counts.items():
+            if name in ("galois", "relin"):
+                t += k * float(np.polyval(coef, limbs))
+                if name == "relin":
+                    t += k * per_limb["add"] * limbs
+            elif name in per_limb:
+                t += k * per_limb[name] * limbs
+            elif name == "encode":
+                t += k * (e0 + e1 * (limbs - 1))
+            elif name == "modraise":
+                t += k * raise_s
+        totals.append(t)
+    t_boot = statistics.mean(totals)
+    n_ks = sum(k for (nm, _), k in counts.items() if nm in ("galois", "relin"))
+    return {"value": workers / t_boot, "unit": "bootstraps/s", "cores": workers, "kind": "port",
+            "sample": f"{workers} worker(s) timing the oracle's key switch at 31/24/18 limbs and its rescale, "
+                      f"tensor, plaintext product, addition, encode and modulus raise at N=2^16 ({wall:.1f} s wall), "
+                      f"scaled by the exact operation counts of one bootstrap_3 ({n_ks} key switches, "
+                      f"modelled {t_boot:.1f} s per bootstrap per core)"}
+
+
 # ----------------------------------------------------------------------------- plumbing
 
 def barrier(world):
@@ -488,23 +732,48 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["nexus", "reference"], default="nexus")
-    ap.add_argument("--workload", choices=["matmul", "ntt"], default="matmul")
+    ap.add_argument("--workload", choices=["bootstrap", "matmul", "ntt"], default="bootstrap")
     ap.add_argument("--cpu-depth", type=int, default=7, help="expansion-subtree depth of the MatMul CPU sample")
     ap.add_argument("--mm-rows", type=int, default=128,
                     help="rows of the encrypted input (smaller values are for profiling captures only)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--boot-cts", type=int, default=16,
+                    help="ciphertexts per bootstrap step (smaller values are for profiling captures only)")
     ap.add_argument("--ntt-cts", type=int, default=64,
                     help="ciphertexts per step (smaller values are for profiling captures only)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     NTT_CTS = args.ntt_cts
-    global MM_ROWS
+    global MM_ROWS, BOOT_CTS
     MM_ROWS = args.mm_rows
+    BOOT_CTS = args.boot_cts
     if args.steps is None:
-        args.steps = 5 if args.workload == "matmul" else 20
+        args.steps = {"bootstrap": 3, "matmul": 5}.get(args.workload, 20)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+
+    if args.impl == "reference" and args.workload == "bootstrap":
+        if rank != 0:
+            return
+        workers = max(1, os.cpu_count() or 1)
+        vals = []
+        for i in range(args.warmup + args.steps):
+            r = cpu_boot_sample(workers=workers)
+            if i >= args.warmup:
+                vals.append(r)
+        value = statistics.mean(r["value"] for r in vals)
+        res = {
+            "impl": "reference", "metric": "bootstrap_throughput_n65536", "value": value, "unit": "bootstraps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": BOOT_CTS * 1e3 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (random residues; cost is data-independent)", "config": boot_config(),
+            "cpu_baseline": {"value": value, "unit": "bootstraps/s", "cores": workers, "kind": "port",
+                             "sample": "per step: " + vals[0]["sample"]},
+            "e2e": {"value": value, "unit": "bootstraps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(res), flush=True)
+        return
 
     if args.impl == "reference" and args.workload == "matmul":
         if rank != 0:
@@ -556,7 +825,8 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
-    res = run_mm_gpu(args, rank, world) if args.workload == "matmul" else run_ntt_gpu(args, rank, world)
+    run = {"bootstrap": run_boot_gpu, "matmul": run_mm_gpu, "ntt": run_ntt_gpu}[args.workload]
+    res = run(args, rank, world)
     if rank == 0:
         print(json.dumps(res), flush=True)
     if world > 1:

@@ -151,6 +151,7 @@ int nexus_relinearize(nexus_context *ctx, const uint64_t *d_ct3, int limbs, cons
  * Apply the automorphism X -> X^galois_elt and switch back to the secret key.
  * Replaces: Evaluator::apply_galois_inplace (native/src/seal/evaluator.cpp:2563-2665);
  *   rotate_vector / complex_conjugate use it with the element of a step.
+ * d_out ([2][limbs][N]) must not overlap d_ct.
  */
 int nexus_apply_galois(nexus_context *ctx, const uint64_t *d_ct, int limbs, uint32_t galois_elt,
                        const uint64_t *d_galois_key, uint64_t *d_out, void *stream);

@@ -439,8 +439,8 @@ void Bootstrapper::generate_LT_coefficient_3()
     cache_.clear();
 }
 
-void Bootstrapper::mul_diagonal(const Ciphertext &ct, int tag, int index, int shift, int coeff_logn, const CVec &v,
-                                uint64_t salt, Ciphertext &out)
+const Plaintext &Bootstrapper::diagonal(const Ciphertext &ct, int tag, int index, int shift, int coeff_logn,
+                                        const CVec &v, uint64_t salt)
 {
     const double scale = ct.scale();
     uint64_t sbits;
@@ -454,7 +454,7 @@ void Bootstrapper::mul_diagonal(const Ciphertext &ct, int tag, int index, int sh
         ev_->encode_then_drop(rot, ct.limbs(), ct.scale(), p);
         it = cache_.emplace(key, std::move(p)).first;
     }
-    ev_->multiply_plain(ct, it->second, out);
+    return it->second;
 }
 
 void Bootstrapper::bsgs_linear_transform(Ciphertext &rtncipher, const Ciphertext &cipher, int totlen, int basicstep,
@@ -475,19 +475,20 @@ void Bootstrapper::bsgs_linear_transform(Ciphertext &rtncipher, const Ciphertext
     }
     Ciphertext giant, acc, t;
     bool have_acc = false;
+    std::vector<const Ciphertext *> terms;
+    std::vector<const Plaintext *> diags;
     for (int i = gfirst; i <= glast; i++) {
-        bool have_giant = false;
+        // giant = sum_j baby_j * diag_ij: the products and their
+        // add_inplace_reduced_error chain at one level, fused
+        terms.clear();
+        diags.clear();
         const int jend = i != glast ? start + gs1 - 1 : totlen - i * gs1;
         for (int j = start; j <= jend; j++) {
             const int idx = i * gs1 + j + totlen;
-            mul_diagonal(baby[j - start], tag, idx, -i * gs1 * basicstep, coeff_logn, fftcoeff[idx], salt_, t);
-            if (!have_giant) {
-                giant = std::move(t);
-                have_giant = true;
-            } else {
-                ev.add_inplace_reduced_error(giant, t);
-            }
+            terms.push_back(&baby[j - start]);
+            diags.push_back(&diagonal(baby[j - start], tag, idx, -i * gs1 * basicstep, coeff_logn, fftcoeff[idx], salt_));
         }
+        ev.multiply_plain_accumulate(terms, diags, giant);
         if (i != 0) {
             ev.rotate_vector(giant, (nh + i * gs1 * basicstep) % nh, t);
             if (!have_acc) {
@@ -525,19 +526,18 @@ void Bootstrapper::rotated_bsgs_linear_transform(Ciphertext &rtncipher, const Ci
     }
     Ciphertext giant, acc, t;
     bool have_acc = false;
+    std::vector<const Ciphertext *> terms;
+    std::vector<const Plaintext *> diags;
     for (int i = 0; i <= glast; i++) {
-        bool have_giant = false;
+        terms.clear();
+        diags.clear();
         const int jend = i != glast ? gs2 - 1 : totlen - i * gs2;
         for (int j = 0; j <= jend; j++) {
             const int idx = i * gs2 + j;
-            mul_diagonal(baby[j], tag, idx, -i * gs2 * basicstep, coeff_logn, fftcoeff[idx], salt_, t);
-            if (!have_giant) {
-                giant = std::move(t);
-                have_giant = true;
-            } else {
-                ev.add_inplace_reduced_error(giant, t);
-            }
+            terms.push_back(&baby[j]);
+            diags.push_back(&diagonal(baby[j], tag, idx, -i * gs2 * basicstep, coeff_logn, fftcoeff[idx], salt_));
         }
+        ev.multiply_plain_accumulate(terms, diags, giant);
         if (i != 0) {
             ev.rotate_vector(giant, (nh + i * gs2 * basicstep) % nh, t);
             if (!have_acc) {
@@ -681,17 +681,34 @@ void Bootstrapper::slottocoeff_3(Ciphertext &rtncipher, const Ciphertext &cipher
     ev_->add_reduced_error(t1, t2, rtncipher);
 }
 
+// encode(vector of +-i, 1.0) at the top level, then mod_switch_to(limbs): the
+// constant plaintexts of coefftoslot_full_3 / slottocoeff_full_3, kept on the device
+const Plaintext &Bootstrapper::unit_plain(bool plus_i, int limbs)
+{
+    const Key key{plus_i ? -1 : -2, 0, 0, limbs, 0, 0};
+    auto it = cache_.find(key);
+    if (it == cache_.end()) {
+        CVec v(Nh, 0);
+        const std::complex<double> iunit(0.0, 1.0);
+        for (long i = 0; i < Nh; i++) {
+            if (plus_i)
+                v[i] += iunit;
+            else
+                v[i] -= iunit;
+        }
+        Plaintext p;
+        ev_->encode(v, ev_->top_limbs(), 1.0, p);
+        ev_->mod_switch_to_inplace(p, limbs);
+        it = cache_.emplace(key, std::move(p)).first;
+    }
+    return it->second;
+}
+
 void Bootstrapper::coefftoslot_full_3(Ciphertext &rtncipher1, Ciphertext &rtncipher2, const Ciphertext &cipher)
 {
     Ciphertext t1, t2, t3, t4;
     sflinv_full_3(t1, cipher);
-    CVec minus_i(Nh, 0);
-    const std::complex<double> iunit(0.0, 1.0);
-    for (long i = 0; i < Nh; i++) minus_i[i] -= iunit;
-    Plaintext p;
-    ev_->encode(minus_i, ev_->top_limbs(), 1.0, p);
-    ev_->mod_switch_to_inplace(p, t1.limbs());
-    ev_->multiply_plain(t1, p, t2);
+    ev_->multiply_plain(t1, unit_plain(false, t1.limbs()), t2);
     t3 = t2;
     ev_->complex_conjugate_inplace(t3);
     t4 = t1;
@@ -702,14 +719,8 @@ void Bootstrapper::coefftoslot_full_3(Ciphertext &rtncipher1, Ciphertext &rtncip
 
 void Bootstrapper::slottocoeff_full_3(Ciphertext &rtncipher, const Ciphertext &cipher1, const Ciphertext &cipher2)
 {
-    CVec plus_i(Nh, 0);
-    const std::complex<double> iunit(0.0, 1.0);
-    for (long i = 0; i < Nh; i++) plus_i[i] += iunit;
-    Plaintext p;
-    ev_->encode(plus_i, ev_->top_limbs(), 1.0, p);
-    ev_->mod_switch_to_inplace(p, cipher2.limbs());
     Ciphertext t1, t3;
-    ev_->multiply_plain(cipher2, p, t1);
+    ev_->multiply_plain(cipher2, unit_plain(true, cipher2.limbs()), t1);
     ev_->add_reduced_error(cipher1, t1, t3);
     sfl_full_3(rtncipher, t3);
 }

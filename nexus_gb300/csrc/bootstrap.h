@@ -109,10 +109,11 @@ public:
     void clear_cache() { cache_.clear(); }
 
 private:
-    // multiply_vector_reduced_error of `ct` by rotation(coeff_logn, Nh, shift, v),
-    // with the encoded diagonal taken from (or put into) the cache
-    void mul_diagonal(const Ciphertext &ct, int tag, int index, int shift, int coeff_logn, const CVec &v,
-                      uint64_t salt, Ciphertext &out);
+    // the plaintext multiply_vector_reduced_error(ct, rotation(coeff_logn, Nh,
+    // shift, v)) encodes, taken from (or put into) the cache
+    const Plaintext &diagonal(const Ciphertext &ct, int tag, int index, int shift, int coeff_logn, const CVec &v,
+                              uint64_t salt);
+    const Plaintext &unit_plain(bool plus_i, int limbs);
     Evaluator *ev_;
     using Key = std::tuple<int, int, int, int, uint64_t, uint64_t>;
     std::map<Key, Plaintext> cache_;

@@ -134,6 +134,8 @@ extern "C" int nexus_apply_galois(nexus_context *ctx, const uint64_t *ct, int li
     if (check_ct(fn, ctx, limbs)) return -1;
     if (!ct || !key || !out) return fail(fn, "null argument");
     if (!(elt & 1) || elt >= 2 * ctx->c.n) return fail(fn, "Galois element is not valid");
+    const size_t words = (size_t)2 * limbs * ctx->c.n;
+    if (out < ct + words && ct < out + words) return fail(fn, "d_out must not overlap d_ct");
     return guarded(fn, [&] { apply_galois(ctx->c, ct, limbs, elt, key, out, (cudaStream_t)stream); });
 }
 

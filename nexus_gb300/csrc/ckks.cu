@@ -1,6 +1,7 @@
 // C++ evaluator with SEAL's semantics over the engine's kernels (see ckks.h).
 // Error conditions and their messages follow SEAL's Evaluator
 // (evaluator.cpp in SEAL-4.1-bs) so NEXUS's code paths fail where SEAL's do.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -427,8 +428,56 @@ void Evaluator::multiply_plain_inplace(Ciphertext &ct, const Plaintext &pt)
 
 void Evaluator::multiply_plain(const Ciphertext &ct, const Plaintext &pt, Ciphertext &dest)
 {
-    if (&ct != &dest) dest = ct;
-    multiply_plain_inplace(dest, pt);
+    if (&ct == &dest) {
+        multiply_plain_inplace(dest, pt);
+        return;
+    }
+    // out of place: the product is written straight into dest
+    if (ct.limbs() != pt.limbs()) throw std::invalid_argument("encrypted and plain parameter mismatch");
+    const double scale = ct.scale() * pt.scale();
+    check_scale(scale, ct.limbs());
+    dest.resize(c_, ct.size(), ct.limbs(), s_);
+    if (pt.is_scalar())
+        poly_mul_scalar(c_, ct.data(), ct.size(), ct.limbs(), pt.residues().data(), dest.data(), s_);
+    else
+        poly_mul_plain(c_, ct.data(), ct.size(), ct.limbs(), pt.data(), dest.data(), s_);
+    dest.scale() = scale;
+}
+
+void Evaluator::multiply_plain_accumulate(const std::vector<const Ciphertext *> &cts,
+                                          const std::vector<const Plaintext *> &pts, Ciphertext &dest)
+{
+    const size_t m = cts.size();
+    if (m == 0 || pts.size() != m) throw std::invalid_argument("multiply_plain_accumulate: bad term count");
+    const int limbs = cts[0]->limbs();
+    double scale = 0.0;
+    std::vector<const uint64_t *> cp(m), pp(m);
+    for (size_t j = 0; j < m; ++j) {
+        const Ciphertext &ct = *cts[j];
+        const Plaintext &pt = *pts[j];
+        if (ct.size() != 2 || ct.limbs() != limbs || &ct == &dest)
+            throw std::invalid_argument("multiply_plain_accumulate: ciphertexts must be distinct, size 2, one level");
+        if (pt.is_scalar() || pt.limbs() != limbs) throw std::invalid_argument("encrypted and plain parameter mismatch");
+        scale = ct.scale() * pt.scale();
+        check_scale(scale, limbs);
+        cp[j] = ct.data();
+        pp[j] = pt.data();
+    }
+    dest.resize(c_, 2, limbs, s_);
+    size_t done = 0;
+    while (done < m) {
+        const int take = (int)std::min<size_t>(16, m - done);
+        if (done == 0) {
+            poly_mac_plain(c_, cp.data(), pp.data(), take, limbs, dest.data(), s_);
+        } else {
+            Ciphertext part;
+            part.resize(c_, 2, limbs, s_);
+            poly_mac_plain(c_, cp.data() + done, pp.data() + done, take, limbs, part.data(), s_);
+            poly_add(c_, dest.data(), part.data(), 2, limbs, dest.data(), s_);
+        }
+        done += take;
+    }
+    dest.scale() = scale;
 }
 
 // ---------------------------------------------------------------- fork ops
@@ -452,8 +501,9 @@ void Evaluator::multiply_const_inplace(Ciphertext &ct, double value)
 
 void Evaluator::multiply_const(const Ciphertext &ct, double value, Ciphertext &dest)
 {
-    if (&ct != &dest) dest = ct;
-    multiply_const_inplace(dest, value);
+    Plaintext p;
+    encode_then_drop(value, ct.limbs(), ct.scale(), p);
+    multiply_plain(ct, p, dest);
 }
 
 void Evaluator::multiply_vector_inplace_reduced_error(Ciphertext &ct, const std::vector<std::complex<double>> &values)
@@ -594,6 +644,18 @@ void Evaluator::rotate_vector_inplace(Ciphertext &ct, int steps)
 
 void Evaluator::rotate_vector(const Ciphertext &ct, int steps, Ciphertext &dest)
 {
+    if (&ct != &dest && steps != 0) {
+        // a direct key: permute and key-switch straight into dest
+        const uint32_t elt = galois_elt(steps);
+        auto it = galois_keys.find(elt);
+        if (it != galois_keys.end()) {
+            if (ct.size() != 2) throw std::invalid_argument("encrypted size must be 2");
+            dest.resize(c_, 2, ct.limbs(), s_);
+            apply_galois(c_, ct.data(), ct.limbs(), elt, it->second, dest.data(), s_);
+            dest.scale() = ct.scale();
+            return;
+        }
+    }
     if (&ct != &dest) dest = ct;
     rotate_vector_inplace(dest, steps);
 }

@@ -165,6 +165,11 @@ public:
     void sub_plain(const Ciphertext &ct, const Plaintext &pt, Ciphertext &dest);
     void multiply_plain_inplace(Ciphertext &ct, const Plaintext &pt);
     void multiply_plain(const Ciphertext &ct, const Plaintext &pt, Ciphertext &dest);
+    // sum_j multiply_plain(cts[j], pts[j]) for size-2 ciphertexts at one level,
+    // as repeated add_inplace_reduced_error of the products does at one
+    // level (the result takes the last product's scale); one fused kernel
+    void multiply_plain_accumulate(const std::vector<const Ciphertext *> &cts,
+                                   const std::vector<const Plaintext *> &pts, Ciphertext &dest);
 
     // constant / vector ops of the bootstrapping fork of SEAL (evaluator.cpp:395-418)
     void add_const_inplace(Ciphertext &ct, double value);

@@ -215,6 +215,8 @@ extern "C" int nexus_context_create(int log_n, const uint64_t *moduli, int n_mod
                 }
         CK(cudaMalloc(&c.d_inv_q, sizeof(ulonglong2) * c.inv_q.size()));
         CK(cudaMemcpy(c.d_inv_q, c.inv_q.data(), sizeof(ulonglong2) * c.inv_q.size(), cudaMemcpyHostToDevice));
+        c.small_primes = true;
+        for (uint64_t qq : c.q) c.small_primes = c.small_primes && qq < (1ull << 52);
         CK(cudaMalloc(&c.d_pc, sizeof(PrimeConst) * n_moduli));
         CK(cudaMemcpy(c.d_pc, c.pc.data(), sizeof(PrimeConst) * n_moduli, cudaMemcpyHostToDevice));
         CK(cudaMalloc(&c.d_tw_fwd, sizeof(ulonglong2) * fwd.size()));

@@ -36,6 +36,9 @@ struct Context {
 
     // Split of the two-pass NTT: n = n1 * n2 (rows x columns).
     int log_n1 = 0, log_n2 = 0;
+    // every prime below 2^52: the forward NTT may skip its per-stage
+    // conditional subtractions (values stay below 2^58 over 16 stages)
+    bool small_primes = false;
 
     // inv_q[a*k + b] = {q_a^{-1} mod q_b, Shoup quotient} (0 on the diagonal);
     // rescale divides by q_{l-1}, ModDown by the special prime q_{k-1}.

@@ -186,12 +186,13 @@ void apply_galois(Context &c, const uint64_t *ct, int l, uint32_t elt, const uin
 {
     const size_t N = c.n;
     uint64_t *tmp = nullptr;
-    if (cudaMallocAsync(&tmp, sizeof(uint64_t) * 2 * l * N, s) != cudaSuccess)
+    if (cudaMallocAsync(&tmp, sizeof(uint64_t) * l * N, s) != cudaSuccess)
         throw std::runtime_error("cudaMallocAsync");
-    galois_permute(c, ct, 2, l, elt, tmp, s);
-    cudaMemcpyAsync(out, tmp, sizeof(uint64_t) * l * N, cudaMemcpyDeviceToDevice, s);
+    // c0 permuted straight into out, c1 permuted into the key-switch target
+    galois_permute(c, ct, 1, l, elt, out, s);
+    galois_permute(c, ct + (size_t)l * N, 1, l, elt, tmp, s);
     cudaMemsetAsync(out + (size_t)l * N, 0, sizeof(uint64_t) * l * N, s);
-    switch_key(c, out, l, tmp + (size_t)l * N, key, s);
+    switch_key(c, out, l, tmp, key, s);
     cudaFreeAsync(tmp, s);
 }
 

@@ -38,6 +38,39 @@ __device__ __forceinline__ void ct_bfly(uint64_t &x, uint64_t &y, ulonglong2 w, 
     y = u + q2 - v;
 }
 
+// Lazy product for primes below 2^52: the Shoup quotient estimate from three of
+// the four 32-bit partial products of y * wq (the dropped low x low term moves
+// the estimate down by at most one), so the result is congruent to y*w and
+// lies in [0, 3q).
+__device__ __forceinline__ uint64_t mul_shoup_lazy3(uint64_t y, uint64_t w, uint64_t wq, uint64_t q)
+{
+    const uint32_t y0 = (uint32_t)y, y1 = (uint32_t)(y >> 32), b0 = (uint32_t)wq, b1 = (uint32_t)(wq >> 32);
+    const uint64_t m1 = (uint64_t)y1 * b0, m2 = (uint64_t)y0 * b1;
+    const uint64_t mid = m1 + m2;
+    const uint64_t hi = (uint64_t)y1 * b1 + (mid >> 32) + ((uint64_t)(mid < m1) << 32);
+    return y * w - hi * q;
+}
+
+// Cooley-Tukey butterfly without reductions for primes below 2^52: each stage
+// adds less than 3q to the largest value, so 16 stages from [0, 2q) stay below
+// 50q < 2^58.
+__device__ __forceinline__ void ct_bfly_small(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q, uint64_t q3)
+{
+    const uint64_t v = mul_shoup_lazy3(y, w.x, w.y, q);
+    const uint64_t u = x;
+    x = u + v;
+    y = u + q3 - v;
+}
+
+template <bool SMALL>
+__device__ __forceinline__ void fwd_bfly(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q, uint64_t q2)
+{
+    if (SMALL)
+        ct_bfly_small(x, y, w, q, q2 + q);
+    else
+        ct_bfly(x, y, w, q, q2);
+}
+
 __device__ __forceinline__ void gs_bfly(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q, uint64_t q2)
 {
     uint64_t u = x, v = y;
@@ -48,6 +81,7 @@ __device__ __forceinline__ void gs_bfly(uint64_t &x, uint64_t &y, ulonglong2 w, 
 // Forward stages whose pairs are (k, k+h) inside the thread, residues at
 // sub-transform positions s = t + T*k.  Stage with pair distance h has
 // m = E/(2h) blocks and block index k/(2h).
+template <bool SMALL>
 __device__ __forceinline__ void fwd_regs_strided(uint64_t (&x)[kE], const ulonglong2 *__restrict__ W, uint64_t B,
                                                  uint64_t q, uint64_t q2)
 {
@@ -58,13 +92,13 @@ __device__ __forceinline__ void fwd_regs_strided(uint64_t (&x)[kE], const ulongl
         for (int k = 0; k < kE; ++k) {
             if (k & h) continue;
             ulonglong2 w = __ldg(&W[B * m + k / (2 * h)]);
-            ct_bfly(x[k], x[k + h], w, q, q2);
+            fwd_bfly<SMALL>(x[k], x[k + h], w, q, q2);
         }
     }
 }
 
 // Forward stages with gaps T/2 .. 1 on residues at s = E*t + k.
-template <int T>
+template <int T, bool SMALL>
 __device__ __forceinline__ void fwd_regs_blocked(uint64_t (&x)[kE], const ulonglong2 *__restrict__ W, uint64_t B,
                                                  int t, uint64_t q, uint64_t q2)
 {
@@ -77,7 +111,7 @@ __device__ __forceinline__ void fwd_regs_blocked(uint64_t (&x)[kE], const ulongl
         for (int k = 0; k < kE; ++k) {
             if (k & g) continue;
             ulonglong2 w = __ldg(&W[base + k / (2 * g)]);
-            ct_bfly(x[k], x[k + g], w, q, q2);
+            fwd_bfly<SMALL>(x[k], x[k + g], w, q, q2);
         }
     }
 }
@@ -124,7 +158,7 @@ __device__ __forceinline__ int swz(int s) { return s + (s >> 4); }
 // Pass 1: size-2^LOGS transforms down the columns.  Output stays in [0,4q).
 // KIND selects the input (NttLoader): 0 the data itself, 1 the ModUp spread,
 // 2 the ModDown rounding spread of a key switch.
-template <int LOGS, int KIND>
+template <int LOGS, int KIND, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
                                                        const PrimeConst *__restrict__ pc, int logn, LimbMap lm,
                                                        NttLoader ld)
@@ -166,20 +200,20 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
             }
         }
     }
-    fwd_regs_strided(x, W, 1, q, q2);
+    fwd_regs_strided<SMALL>(x, W, 1, q, q2);
 #pragma unroll
     for (int k = 0; k < kE; ++k) sm[(t + T * k) * C + c] = x[k];
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < kE; ++k) x[k] = sm[(kE * t + k) * C + c];
-    fwd_regs_blocked<T>(x, W, 1, t, q, q2);
+    fwd_regs_blocked<T, SMALL>(x, W, 1, t, q, q2);
 #pragma unroll
     for (int k = 0; k < kE; ++k) p[(size_t)(kE * t + k) * n2 + c] = x[k];
 }
 
 // Pass 2: size-2^LOGS transforms along contiguous rows, then the final
-// reduction [0,4q) -> [0,q).
-template <int LOGS>
+// reduction to [0,q) (from [0,4q), or from [0,50q) on the small-prime path).
+template <int LOGS, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_fwd_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
                                                        const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
 {
@@ -200,15 +234,21 @@ __global__ void __launch_bounds__(kThreads) k_fwd_rows(uint64_t *__restrict__ da
     uint64_t x[kE];
 #pragma unroll
     for (int k = 0; k < kE; ++k) x[k] = p[t + T * k];
-    fwd_regs_strided(x, W, B, q, q2);
+    fwd_regs_strided<SMALL>(x, W, B, q, q2);
 #pragma unroll
     for (int k = 0; k < kE; ++k) srow[swz(t + T * k)] = x[k];
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < kE; ++k) x[k] = srow[swz(kE * t + k)];
-    fwd_regs_blocked<T>(x, W, B, t, q, q2);
+    fwd_regs_blocked<T, SMALL>(x, W, B, t, q, q2);
+    if (SMALL) {
+        const uint64_t r1 = pc[prime].r1;
 #pragma unroll
-    for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = csub(csub(x[k], q2), q);
+        for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = barrett_64(x[k], q, r1);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = csub(csub(x[k], q2), q);
+    }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < kE; ++k) p[t + T * k] = srow[swz(t + T * k)];
@@ -284,8 +324,8 @@ __global__ void __launch_bounds__(kThreads) k_inv_cols(uint64_t *__restrict__ da
     for (int k = 0; k < kE; ++k) p[(size_t)(t + T * k) * n2 + c] = mul_shoup(x[k], P.inv_n, P.inv_n_q, q);
 }
 
-template <int L1, int L2>
-void launch_fwd(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s, NttLoader ld = NttLoader())
+template <int L1, int L2, bool SMALL>
+void launch_fwd_t(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s, NttLoader ld)
 {
     const size_t limbs = n_polys * (size_t)lm.count;
     constexpr int C = kThreads / ((1 << L1) / kE);
@@ -293,13 +333,22 @@ void launch_fwd(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaS
     const unsigned g1 = (unsigned)(limbs * ((1u << L2) / C));
     const unsigned g2 = (unsigned)(limbs * ((1u << L1) / R));
     if (ld.kind == 1)
-        k_fwd_cols<L1, 1><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
+        k_fwd_cols<L1, 1, SMALL><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
     else if (ld.kind == 2)
-        k_fwd_cols<L1, 2><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
+        k_fwd_cols<L1, 2, SMALL><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
     else
-        k_fwd_cols<L1, 0><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
+        k_fwd_cols<L1, 0, SMALL><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
     NEXUS_LAUNCHED();
-    k_fwd_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm); NEXUS_LAUNCHED();
+    k_fwd_rows<L2, SMALL><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm); NEXUS_LAUNCHED();
+}
+
+template <int L1, int L2>
+void launch_fwd(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s, NttLoader ld = NttLoader())
+{
+    if (c.small_primes)
+        launch_fwd_t<L1, L2, true>(c, d, n_polys, lm, s, ld);
+    else
+        launch_fwd_t<L1, L2, false>(c, d, n_polys, lm, s, ld);
 }
 
 template <int L1, int L2>

@@ -20,6 +20,10 @@ void poly_negate(const Context &c, const uint64_t *a, int polys, int limbs, uint
 // out[p] = ct[p] * pt for every polynomial p of ct (pt is one [limbs][N] polynomial)
 void poly_mul_plain(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *pt, uint64_t *out,
                     cudaStream_t s);
+// out[p] = sum_j cts[j][p] * pts[j] for both polynomials p of `count` (<= 16)
+// two-polynomial ciphertexts; 128-bit exact accumulation, one reduction
+void poly_mac_plain(const Context &c, const uint64_t *const *cts, const uint64_t *const *pts, int count, int limbs,
+                    uint64_t *out, cudaStream_t s);
 // out[p] = ct[p] + pt (pt broadcast); used for add_plain
 void poly_add_plain(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *pt, int sub,
                     uint64_t *out, cudaStream_t s);

@@ -2,6 +2,7 @@
 //
 // Every result is the fully reduced residue SEAL produces for the same
 // operation (references are to the SEAL-4.1-bs tree bundled with NEXUS).
+#include <algorithm>
 #include <stdexcept>
 
 #include "context.h"
@@ -13,6 +14,7 @@ namespace nexus {
 namespace {
 
 constexpr int kBlock = 256;
+constexpr int kMacTerms = 16;
 
 inline unsigned grid_for(size_t pairs)
 {
@@ -83,6 +85,37 @@ __global__ void k_plain(const ulonglong2 *__restrict__ ct, const ulonglong2 *__r
             x.y = sub_mod(x.y, y.y, P.q);
         }
         out[pi] = x;
+    }
+}
+
+// out[p] = sum_j ct_j[p] * pt_j mod q over `count` ciphertext / plaintext
+// pairs, for both polynomials, accumulated exactly in 128 bits and reduced once
+struct MacTerms {
+    const uint64_t *ct[kMacTerms];
+    const uint64_t *pt[kMacTerms];
+};
+
+__device__ __forceinline__ void mac128p(uint64_t &lo, uint64_t &hi, uint64_t a, uint64_t b)
+{
+    asm("mad.lo.cc.u64 %0, %2, %3, %0;\n\tmadc.hi.u64 %1, %2, %3, %1;" : "+l"(lo), "+l"(hi) : "l"(a), "l"(b));
+}
+
+__global__ void k_mac_plain(MacTerms t, int count, uint64_t *__restrict__ out, const PrimeConst *__restrict__ pc,
+                            int limbs, int logn, size_t total)
+{
+    const size_t poly = (size_t)limbs << logn;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t e = x % poly;  // limb * N + coefficient
+        const int limb = (int)(e >> logn);
+        uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
+        for (int j = 0; j < count; ++j) {
+            const uint64_t w = t.pt[j][e];
+            mac128p(lo0, hi0, t.ct[j][e], w);
+            mac128p(lo1, hi1, t.ct[j][poly + e], w);
+        }
+        const PrimeConst P = pc[limb];
+        out[e] = barrett_128(lo0, hi0, P.q, P.r0, P.r1);
+        out[poly + e] = barrett_128(lo1, hi1, P.q, P.r0, P.r1);
     }
 }
 
@@ -247,6 +280,20 @@ void poly_mul_plain(const Context &c, const uint64_t *ct, int polys, int limbs, 
     size_t pr = pairs_of(c, polys, limbs);
     k_plain<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)ct, (const ulonglong2 *)pt, (ulonglong2 *)out, c.d_pc,
                                              limbs, c.logn, pr, 0); NEXUS_LAUNCHED();
+}
+
+void poly_mac_plain(const Context &c, const uint64_t *const *cts, const uint64_t *const *pts, int count, int limbs,
+                    uint64_t *out, cudaStream_t s)
+{
+    if (count < 1 || count > kMacTerms) throw std::invalid_argument("poly_mac_plain: 1..16 terms");
+    MacTerms t{};
+    for (int j = 0; j < count; ++j) {
+        t.ct[j] = cts[j];
+        t.pt[j] = pts[j];
+    }
+    const size_t total = ((size_t)limbs << c.logn);
+    const unsigned grid = (unsigned)std::min<size_t>((total + kBlock - 1) / kBlock, 152 * 8);
+    k_mac_plain<<<grid, kBlock, 0, s>>>(t, count, out, c.d_pc, limbs, c.logn, total); NEXUS_LAUNCHED();
 }
 
 void poly_add_plain(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *pt, int sub,

@@ -89,6 +89,11 @@ class Evaluator:
             lib().nexus_evaluator_destroy(self._h)
             self._h = None
 
+    def add_galois_key(self, elt: int, key) -> None:
+        self._keys.append(key)
+        check(lib().nexus_evaluator_add_galois_key(self._h, int(elt), key.data_ptr()),
+              "nexus_evaluator_add_galois_key")
+
     def gelu(self, x: Ciphertext) -> Ciphertext:
         res = Ciphertext(self.ctx)
         check(lib().nexus_gelu(self._h, x.handle, res.handle), "nexus_gelu")

@@ -14,6 +14,10 @@ pytestmark = pytest.mark.gpu
     (14, [60] + [40] * 7 + [60]),
     (15, [50, 40, 60]),
     (16, [60] * 3),
+    # every prime below 2^52: the forward NTT's reduction-free small-prime path
+    (13, [51, 46, 46, 51, 51]),
+    (16, [51] + [46] * 3 + [51] * 2),
+    (14, [52, 52, 30]),
 ])
 def test_ntt_forward_inverse_matches_oracle(cuda, log_n, bits):
     from nexus_gb300 import Context
@@ -52,11 +56,13 @@ def test_ntt_limb_subrange(cuda):
     assert np.array_equal(to_host(t), oc.ntt(x, 1, 3))
 
 
-def test_ntt_edge_values(cuda):
-    """All-zero, all q-1 and single-spike inputs."""
+@pytest.mark.parametrize("bits", [[60, 60], [51, 51]])
+def test_ntt_edge_values(cuda, bits):
+    """All-zero, all q-1 and single-spike inputs (all q-1 is the largest
+    input of the small-prime path too)."""
     from nexus_gb300 import Context
     log_n, n = 16, 1 << 16
-    qs = po.create_coeff_modulus(n, [60, 60])
+    qs = po.create_coeff_modulus(n, bits)
     ctx = Context(log_n, qs)
     oc = po.OracleContext(log_n, qs)
     q = np.array(qs, dtype=np.uint64).reshape(2, 1)
