@@ -129,6 +129,7 @@ NTT_LOGN = 16
 NTT_PRIMES = 24
 NTT_CTS = 64
 NTT_POLYS = 2
+NTT_BITS = 60
 
 
 def ntt_config():
@@ -147,7 +148,7 @@ def run_ntt_gpu(args, rank, world):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     n = 1 << NTT_LOGN
-    qs = ng.create_coeff_modulus(n, [60] * NTT_PRIMES)
+    qs = ng.create_coeff_modulus(n, [NTT_BITS] * NTT_PRIMES)
     ctx = ng.Context(NTT_LOGN, qs)
     limbs = NTT_CTS * NTT_POLYS * NTT_PRIMES
     g = torch.Generator(device=dev).manual_seed(1234 + rank)
@@ -737,6 +738,8 @@ def main():
     ap.add_argument("--mm-rows", type=int, default=128,
                     help="rows of the encrypted input (smaller values are for profiling captures only)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ntt-bits", type=int, default=60,
+                    help="prime size of the NTT workload (other values are for profiling captures only)")
     ap.add_argument("--boot-cts", type=int, default=16,
                     help="ciphertexts per bootstrap step (smaller values are for profiling captures only)")
     ap.add_argument("--ntt-cts", type=int, default=64,
@@ -744,7 +747,8 @@ def main():
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     NTT_CTS = args.ntt_cts
-    global MM_ROWS, BOOT_CTS
+    global MM_ROWS, BOOT_CTS, NTT_BITS
+    NTT_BITS = args.ntt_bits
     MM_ROWS = args.mm_rows
     BOOT_CTS = args.boot_cts
     if args.steps is None:
