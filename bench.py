@@ -526,7 +526,14 @@ def run_boot_gpu(args, rank, world):
         del pt, ct
     stream = torch.cuda.current_stream(dev)
 
+    in_cts = [Ciphertext.from_device(ctx, x, BOOT_SCALE) for x in inputs]
+
     def step():
+        # the lockstep form: every operation once over all ciphertexts (inputs are not modified)
+        return bs.bootstrap_batch(in_cts)
+
+    def plain_step():
+        # the single-ciphertext form, one bootstrap_3 per ciphertext (it raises its input in place)
         return [bs.bootstrap_3(Ciphertext.from_device(ctx, x, BOOT_SCALE)) for x in inputs]
 
     for _ in range(args.warmup):
@@ -572,13 +579,29 @@ def run_boot_gpu(args, rank, world):
     barrier(world)
     w0 = time.perf_counter()
     out_bytes = 0
+    loaded = []
     for h in h_in:
         c = Ciphertext(ctx)
         ng.check(ng.lib().nexus_ciphertext_load(c.handle, h.data_ptr(), 2, 1, BOOT_SCALE, 1, None), "load")
-        out_bytes += bs.bootstrap_3(c).to_numpy().nbytes
+        loaded.append(c)
+    for r in bs.bootstrap_batch(loaded):
+        out_bytes += r.to_numpy().nbytes
     torch.cuda.synchronize(dev)
     e2e_s = max_over_ranks(time.perf_counter() - w0, world)
     in_bytes = sum(h.nbytes for h in host_in)
+
+    # the single-ciphertext form on the same inputs, for comparison
+    plain_step()
+    torch.cuda.synchronize(dev)
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    res = plain_step()
+    p1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_ms = p0.elapsed_time(p1)
+    same = all(np.array_equal(a.to_numpy(), b.to_numpy()) for a, b in zip(res[:2], bs.bootstrap_batch(in_cts[:2])))
+    del res
 
     step_ms = total_ms / args.steps
     value = world * args.steps * BOOT_CTS / (total_ms / 1e3)
@@ -613,6 +636,9 @@ def run_boot_gpu(args, rank, world):
         },
         "e2e": {"value": world * BOOT_CTS / e2e_s, "unit": "bootstraps/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes},
+        "plain_single_ct_form": {"value": world * BOOT_CTS / (plain_ms / 1e3), "unit": "bootstraps/s",
+                                 "ms_per_bootstrap": plain_ms / BOOT_CTS,
+                                 "batched_words_equal_single": bool(same)},
         "clocks": clk.summary(),
         "gpu_launches": launches,
     }

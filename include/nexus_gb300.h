@@ -382,6 +382,14 @@ int nexus_lt_coefficients_3(int logn, int logNh, long boundary_K, int which, dou
  * refreshed ciphertext at scale final_scale. */
 int nexus_bootstrap(nexus_bootstrapper *bs, nexus_ciphertext *ct, nexus_ciphertext *rtn);
 
+/* bootstrap_3 of `count` ciphertexts in lockstep (one scale, one limb each):
+ * every operation runs once over the whole batch and every key is read once
+ * per batch.  rtn[b] receives the same words nexus_bootstrap gives for
+ * cts[b]; the inputs are left unchanged.  No counterpart in the reference
+ * (it bootstraps one ciphertext per call). */
+int nexus_bootstrap_batch(nexus_bootstrapper *bs, nexus_ciphertext *const *cts, int count,
+                          nexus_ciphertext *const *rtn);
+
 /* The stages of bootstrap_full_3 (Bootstrapper.cpp:3224-3244), for
  * stage-wise checking: MODRAISE a in place (modraise_inplace :2937-2991);
  * COEFFTOSLOT a -> r1, r2 (coefftoslot_full_3 :2741-2757);

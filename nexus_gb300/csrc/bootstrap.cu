@@ -17,6 +17,11 @@
 
 namespace nexus {
 
+namespace {
+inline int batch_of(const Ciphertext &) { return 1; }
+inline int batch_of(const CtBatch &c) { return c.batch(); }
+}  // namespace
+
 int giantstep(int m)
 {
     int minval = m, mink = 1;
@@ -46,12 +51,14 @@ void rotation(int logslot, int nh, int shiftcount, const CVec &vec, CVec &rtnvec
 
 // ------------------------------------------------------------------ EvalMod
 
-ModularReducer::ModularReducer(Evaluator &ev, long K, double lw, long d, long ndf, long ideg)
+template <class EV, class CT>
+ModularReducerT<EV, CT>::ModularReducerT(EV &ev, long K, double lw, long d, long ndf, long ideg)
     : boundary_K(K), log_width(lw), deg(d), num_double_formula(ndf), inverse_deg(ideg), ev_(&ev)
 {
 }
 
-void ModularReducer::set_polynomial_heap(long k, long m, std::vector<std::vector<double>> nodes, double sic)
+template <class EV, class CT>
+void ModularReducerT<EV, CT>::set_polynomial_heap(long k, long m, std::vector<std::vector<double>> nodes, double sic)
 {
     if (k < 2 || m < 0 || nodes.size() != (size_t)((1 << (m + 1)) - 1) || nodes[0].empty())
         throw std::invalid_argument("malformed polynomial heap");
@@ -61,7 +68,8 @@ void ModularReducer::set_polynomial_heap(long k, long m, std::vector<std::vector
     scale_inverse_coeff = sic;
 }
 
-void ModularReducer::double_angle_formula(Ciphertext &cipher)
+template <class EV, class CT>
+void ModularReducerT<EV, CT>::double_angle_formula(CT &cipher)
 {
     ev_->square_inplace(cipher);
     ev_->relinearize_inplace(cipher);
@@ -70,7 +78,8 @@ void ModularReducer::double_angle_formula(Ciphertext &cipher)
     ev_->add_const_inplace(cipher, -1.0);
 }
 
-void ModularReducer::double_angle_formula_scaled(Ciphertext &cipher, double scale_coeff)
+template <class EV, class CT>
+void ModularReducerT<EV, CT>::double_angle_formula_scaled(CT &cipher, double scale_coeff)
 {
     ev_->square_inplace(cipher);
     ev_->relinearize_inplace(cipher);
@@ -83,16 +92,17 @@ void ModularReducer::double_angle_formula_scaled(Ciphertext &cipher, double scal
 // over the heap: Chebyshev baby steps T_1..T_{k-1}, giant steps
 // T_k, T_2k, ..., leaves as sums of constant multiples, then the heap
 // combined bottom-up with the giant steps.
-void ModularReducer::homomorphic_poly_evaluation(Ciphertext &rtn, const Ciphertext &cipher)
+template <class EV, class CT>
+void ModularReducerT<EV, CT>::homomorphic_poly_evaluation(CT &rtn, const CT &cipher)
 {
-    Evaluator &ev = *ev_;
+    EV &ev = *ev_;
     const double zero = 1. / cipher.scale();
     // the reference evaluates polynomials of degree 1..3 directly on their
     // power-basis coefficients; only the heap path is used for EvalMod
     if ((long)heap[0].size() - 1 < 4 || heap_m < 1)
         throw std::invalid_argument("homomorphic_poly_evaluation: polynomial heap of degree >= 4 expected");
     const long k = heap_k, m = heap_m;
-    std::vector<Ciphertext> baby(k);
+    std::vector<CT> baby(k);
     std::vector<bool> have(k, false);
     baby[1] = cipher;
     have[1] = true;
@@ -115,7 +125,7 @@ void ModularReducer::homomorphic_poly_evaluation(Ciphertext &rtn, const Cipherte
         ev.sub_inplace_reduced_error(baby[i], baby[diff]);
         have[i] = true;
     }
-    std::vector<Ciphertext> giant(m);
+    std::vector<CT> giant(m);
     {
         const long lpow2 = 1L << ((int)std::ceil(std::log((double)k) / std::log(2.0)) - 1);
         const long res = k - lpow2;
@@ -144,9 +154,9 @@ void ModularReducer::homomorphic_poly_evaluation(Ciphertext &rtn, const Cipherte
     }
 
     const long len = (1L << (m + 1)) - 1;
-    std::vector<Ciphertext> ch(len);
+    std::vector<CT> ch(len);
     std::vector<bool> chb(len, false);
-    Ciphertext tmp;
+    CT tmp;
     for (long i = (1L << m) - 1; i < len; i++) {
         const std::vector<double> &cf = heap[i];
         if (cf.empty()) continue;
@@ -181,11 +191,12 @@ void ModularReducer::homomorphic_poly_evaluation(Ciphertext &rtn, const Cipherte
     rtn = std::move(ch[0]);
 }
 
-void ModularReducer::modular_reduction(Ciphertext &rtn, const Ciphertext &cipher)
+template <class EV, class CT>
+void ModularReducerT<EV, CT>::modular_reduction(CT &rtn, const CT &cipher)
 {
     if (heap.empty()) throw std::logic_error("prepare_mod_polynomial has not been called");
     if (inverse_deg != 1) throw std::invalid_argument("only inverse_deg == 1 (scaled double angle) is supported");
-    Ciphertext tmp2;
+    CT tmp2;
     homomorphic_poly_evaluation(tmp2, cipher);
     double curr_scale = scale_inverse_coeff;
     for (long i = 0; i < num_double_formula; i++) {
@@ -197,7 +208,8 @@ void ModularReducer::modular_reduction(Ciphertext &rtn, const Ciphertext &cipher
 
 // ------------------------------------------------------------ Bootstrapper
 
-Bootstrapper::Bootstrapper(Evaluator &ev, long loge_, long logn_, long logNh_, long L_, double fs, long K, long scd,
+template <class EV, class CT>
+BootstrapperT<EV, CT>::BootstrapperT(EV &ev, long loge_, long logn_, long logNh_, long L_, double fs, long K, long scd,
                            long sf, long ideg)
     : loge(loge_), logn(logn_), logNh(logNh_), L(L_), final_scale(fs), boundary_K(K), sin_cos_deg(scd),
       scale_factor(sf), inverse_deg(ideg), mod_reducer(ev, K, (double)loge_, scd, sf, ideg), ev_(&ev)
@@ -208,13 +220,15 @@ Bootstrapper::Bootstrapper(Evaluator &ev, long loge_, long logn_, long logNh_, l
     Nh = 1L << logNh;
 }
 
-void Bootstrapper::prepare_mod_polynomial(long heap_k, long heap_m, std::vector<std::vector<double>> nodes,
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::prepare_mod_polynomial(long heap_k, long heap_m, std::vector<std::vector<double>> nodes,
                                           double scale_inverse_coeff)
 {
     mod_reducer.set_polynomial_heap(heap_k, heap_m, std::move(nodes), scale_inverse_coeff);
 }
 
-void Bootstrapper::change_logn(long new_logn)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::change_logn(long new_logn)
 {
     logn = new_logn;
     n = 1L << logn;
@@ -227,7 +241,8 @@ void Bootstrapper::change_logn(long new_logn)
     if (slot_index == -1) throw std::invalid_argument("LT coefficients were not generated for this logn");
 }
 
-void Bootstrapper::addLeftRotKeys_Linear_to_vector_3(std::vector<int> &v) const
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::addLeftRotKeys_Linear_to_vector_3(std::vector<int> &v) const
 {
     auto push = [&](int s) {
         for (int x : v)
@@ -412,7 +427,8 @@ void lt_coefficients_3(long cl, long logNh, long boundary_K, std::vector<CVec> o
     }
 }
 
-void Bootstrapper::generate_LT_coefficient_3()
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::generate_LT_coefficient_3()
 {
     if (slot_vec.empty()) slot_vec.push_back(logn);
     const size_t U = slot_vec.size();
@@ -439,7 +455,8 @@ void Bootstrapper::generate_LT_coefficient_3()
     cache_.clear();
 }
 
-const Plaintext &Bootstrapper::diagonal(const Ciphertext &ct, int tag, int index, int shift, int coeff_logn,
+template <class EV, class CT>
+const Plaintext &BootstrapperT<EV, CT>::diagonal(const CT &ct, int tag, int index, int shift, int coeff_logn,
                                         const CVec &v, uint64_t salt)
 {
     const double scale = ct.scale();
@@ -457,25 +474,26 @@ const Plaintext &Bootstrapper::diagonal(const Ciphertext &ct, int tag, int index
     return it->second;
 }
 
-void Bootstrapper::bsgs_linear_transform(Ciphertext &rtncipher, const Ciphertext &cipher, int totlen, int basicstep,
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::bsgs_linear_transform(CT &rtncipher, const CT &cipher, int totlen, int basicstep,
                                          int coeff_logn, const std::vector<CVec> &fftcoeff, int tag)
 {
-    Evaluator &ev = *ev_;
+    EV &ev = *ev_;
     const int nh = (int)Nh;
     const int gs1 = giantstep(2 * totlen + 1);
     const int start = -totlen + gs1 * (int)std::floor((totlen + 0.0) / (gs1 + 0.0));
     const int gfirst = -(int)std::floor((totlen + 0.0) / (gs1 + 0.0));
     const int glast = (int)std::floor((2 * totlen + 0.0) / (gs1 + 0.0)) + gfirst;
-    std::vector<Ciphertext> baby(gs1);
+    std::vector<CT> baby(gs1);
     for (int i = start; i < start + gs1; i++) {
         if (i == 0)
             baby[i - start] = cipher;
         else
             ev.rotate_vector(cipher, (nh + i * basicstep) % nh, baby[i - start]);
     }
-    Ciphertext giant, acc, t;
+    CT giant, acc, t;
     bool have_acc = false;
-    std::vector<const Ciphertext *> terms;
+    std::vector<const CT *> terms;
     std::vector<const Plaintext *> diags;
     for (int i = gfirst; i <= glast; i++) {
         // giant = sum_j baby_j * diag_ij: the products and their
@@ -509,24 +527,25 @@ void Bootstrapper::bsgs_linear_transform(Ciphertext &rtncipher, const Ciphertext
     rtncipher = std::move(acc);
 }
 
-void Bootstrapper::rotated_bsgs_linear_transform(Ciphertext &rtncipher, const Ciphertext &cipher, int totlen,
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::rotated_bsgs_linear_transform(CT &rtncipher, const CT &cipher, int totlen,
                                                  int basicstep, int coeff_logn, const std::vector<CVec> &fftcoeff,
                                                  int tag)
 {
-    Evaluator &ev = *ev_;
+    EV &ev = *ev_;
     const int nh = (int)Nh;
     const int gs2 = giantstep(totlen + 1);
     const int glast = (int)std::floor((totlen + 0.0) / (gs2 + 0.0));
-    std::vector<Ciphertext> baby(gs2);
+    std::vector<CT> baby(gs2);
     for (int i = 0; i < gs2; i++) {
         if (i == 0)
             baby[i] = cipher;
         else
             ev.rotate_vector(cipher, (nh + i * basicstep) % nh, baby[i]);
     }
-    Ciphertext giant, acc, t;
+    CT giant, acc, t;
     bool have_acc = false;
-    std::vector<const Ciphertext *> terms;
+    std::vector<const CT *> terms;
     std::vector<const Plaintext *> diags;
     for (int i = 0; i <= glast; i++) {
         terms.clear();
@@ -585,13 +604,14 @@ std::vector<CVec> scale_level3(const std::vector<CVec> &c3, size_t count, size_t
 
 }  // namespace
 
-void Bootstrapper::sflinv_full_3(Ciphertext &rtncipher, const Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::sflinv_full_3(CT &rtncipher, const CT &cipher)
 {
     const int d1 = (int)std::floor(logn / 3.0);
     const int d2 = (int)std::floor((logn - d1) / 2.0);
     const int d3 = (int)logn - d1 - d2;
     const int t1 = (1 << d1) - 1, t2 = (1 << d2) - 1, t3 = (1 << d3) - 1;
-    Ciphertext tmpct, tmpct2;
+    CT tmpct, tmpct2;
     salt_ = 0;
     rotated_bsgs_linear_transform(tmpct, cipher, t1, 1 << (logn - d1), (int)logn, invfftcoeff1[slot_index], kInv1);
     ev_->rescale_to_next_inplace(tmpct);
@@ -601,13 +621,14 @@ void Bootstrapper::sflinv_full_3(Ciphertext &rtncipher, const Ciphertext &cipher
     ev_->rescale_to_next_inplace(rtncipher);
 }
 
-void Bootstrapper::sflinv_3(Ciphertext &rtncipher, const Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::sflinv_3(CT &rtncipher, const CT &cipher)
 {
     const int d1 = (int)std::floor(logn / 3.0);
     const int d2 = (int)std::floor((logn - d1) / 2.0);
     const int d3 = (int)logn - d1 - d2;
     const int t1 = (1 << d1) - 1, t2 = (1 << d2) - 1, t3 = (1 << d3) - 1;
-    Ciphertext tmpct, tmpct2;
+    CT tmpct, tmpct2;
     salt_ = 0;
     rotated_bsgs_linear_transform(tmpct, cipher, t1, 1 << (logn - d1), (int)logn, invfftcoeff1[slot_index], kInv1);
     ev_->rescale_to_next_inplace(tmpct);
@@ -617,7 +638,8 @@ void Bootstrapper::sflinv_3(Ciphertext &rtncipher, const Ciphertext &cipher)
     ev_->rescale_to_next_inplace(rtncipher);
 }
 
-void Bootstrapper::sfl_full_3(Ciphertext &rtncipher, const Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::sfl_full_3(CT &rtncipher, const CT &cipher)
 {
     const int d3 = (int)std::floor(logn / 3.0);
     const int d2 = (int)std::floor((logn - d3) / 2.0);
@@ -626,7 +648,7 @@ void Bootstrapper::sfl_full_3(Ciphertext &rtncipher, const Ciphertext &cipher)
     // the reference scales totlen2 + 1 level-3 diagonals and reads
     // totlen3 + 1 of them: defined only when the two agree
     if (t2 != t3) throw std::invalid_argument("sfl_full_3 needs logn % 3 != 2");
-    Ciphertext tmpct, tmpct2;
+    CT tmpct, tmpct2;
     salt_ = 0;
     bsgs_linear_transform(tmpct, cipher, t1, 1, (int)logn, fftcoeff1[slot_index], kFwd1);
     ev_->rescale_to_next_inplace(tmpct);
@@ -642,13 +664,14 @@ void Bootstrapper::sfl_full_3(Ciphertext &rtncipher, const Ciphertext &cipher)
     ev_->rescale_to_next_inplace(rtncipher);
 }
 
-void Bootstrapper::sfl_3(Ciphertext &rtncipher, const Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::sfl_3(CT &rtncipher, const CT &cipher)
 {
     const int d3 = (int)std::floor(logn / 3.0);
     const int d2 = (int)std::floor((logn - d3) / 2.0);
     const int d1 = (int)logn - d3 - d2;
     const int t1 = (1 << d1) - 1, t2 = (1 << d2) - 1, t3 = (1 << d3) - 1;
-    Ciphertext tmpct, tmpct2;
+    CT tmpct, tmpct2;
     salt_ = 0;
     bsgs_linear_transform(tmpct, cipher, t1, 1, (int)logn + 1, fftcoeff1[slot_index], kFwd1);
     ev_->rescale_to_next_inplace(tmpct);
@@ -664,18 +687,20 @@ void Bootstrapper::sfl_3(Ciphertext &rtncipher, const Ciphertext &cipher)
     ev_->rescale_to_next_inplace(rtncipher);
 }
 
-void Bootstrapper::coefftoslot_3(Ciphertext &rtncipher, const Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::coefftoslot_3(CT &rtncipher, const CT &cipher)
 {
-    Ciphertext t1, t2;
+    CT t1, t2;
     sflinv_3(t1, cipher);
     t2 = t1;
     ev_->complex_conjugate_inplace(t2);
     ev_->add_reduced_error(t1, t2, rtncipher);
 }
 
-void Bootstrapper::slottocoeff_3(Ciphertext &rtncipher, const Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::slottocoeff_3(CT &rtncipher, const CT &cipher)
 {
-    Ciphertext t1, t2;
+    CT t1, t2;
     sfl_3(t1, cipher);
     ev_->rotate_vector(t1, (int)n, t2);
     ev_->add_reduced_error(t1, t2, rtncipher);
@@ -683,7 +708,8 @@ void Bootstrapper::slottocoeff_3(Ciphertext &rtncipher, const Ciphertext &cipher
 
 // encode(vector of +-i, 1.0) at the top level, then mod_switch_to(limbs): the
 // constant plaintexts of coefftoslot_full_3 / slottocoeff_full_3, kept on the device
-const Plaintext &Bootstrapper::unit_plain(bool plus_i, int limbs)
+template <class EV, class CT>
+const Plaintext &BootstrapperT<EV, CT>::unit_plain(bool plus_i, int limbs)
 {
     const Key key{plus_i ? -1 : -2, 0, 0, limbs, 0, 0};
     auto it = cache_.find(key);
@@ -704,9 +730,10 @@ const Plaintext &Bootstrapper::unit_plain(bool plus_i, int limbs)
     return it->second;
 }
 
-void Bootstrapper::coefftoslot_full_3(Ciphertext &rtncipher1, Ciphertext &rtncipher2, const Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::coefftoslot_full_3(CT &rtncipher1, CT &rtncipher2, const CT &cipher)
 {
-    Ciphertext t1, t2, t3, t4;
+    CT t1, t2, t3, t4;
     sflinv_full_3(t1, cipher);
     ev_->multiply_plain(t1, unit_plain(false, t1.limbs()), t2);
     t3 = t2;
@@ -717,9 +744,10 @@ void Bootstrapper::coefftoslot_full_3(Ciphertext &rtncipher1, Ciphertext &rtncip
     ev_->add_reduced_error(t2, t3, rtncipher2);
 }
 
-void Bootstrapper::slottocoeff_full_3(Ciphertext &rtncipher, const Ciphertext &cipher1, const Ciphertext &cipher2)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::slottocoeff_full_3(CT &rtncipher, const CT &cipher1, const CT &cipher2)
 {
-    Ciphertext t1, t3;
+    CT t1, t3;
     ev_->multiply_plain(cipher2, unit_plain(true, cipher2.limbs()), t1);
     ev_->add_reduced_error(cipher1, t1, t3);
     sfl_full_3(rtncipher, t3);
@@ -753,32 +781,35 @@ __global__ void k_modraise(const uint64_t *__restrict__ src, uint64_t *__restric
 
 }  // namespace
 
-void Bootstrapper::modraise_inplace(Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::modraise_inplace(CT &cipher)
 {
     if (cipher.size() != 2) throw std::invalid_argument("Ciphertexts of size 2 are supported only!");
     if (cipher.limbs() != 1) throw std::invalid_argument("Ciphertexts in the lowest level are supported only!");
     Context &c = ev_->context();
     cudaStream_t s = ev_->stream();
     const int top = ev_->top_limbs();
-    Ciphertext src = cipher;  // [2][1][N], inverse-transformed below
-    ntt_inverse(c, src.data(), 2, 0, 1, s);
+    const int polys = 2 * batch_of(cipher);
+    CT src = cipher;  // [polys][1][N], inverse-transformed below
+    ntt_inverse(c, src.data(), polys, 0, 1, s);
     const double scale = cipher.scale();
     cipher.resize(c, 2, top, s);
     cipher.scale() = scale;
-    const size_t total = (size_t)2 * top * c.n;
+    const size_t total = (size_t)polys * top * c.n;
     const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 152 * 16);
     k_modraise<<<grid, 256, 0, s>>>(src.data(), cipher.data(), c.d_pc, top, c.logn, total);
     NEXUS_LAUNCHED();
-    ntt_forward(c, cipher.data(), 2, 0, top, s);
+    ntt_forward(c, cipher.data(), polys, 0, top, s);
 }
 
 // ------------------------------------------------------------------ drivers
 
-void Bootstrapper::bootstrap_full_3(Ciphertext &rtncipher, Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::bootstrap_full_3(CT &rtncipher, CT &cipher)
 {
     modraise_inplace(cipher);
     cipher.scale() = (double)ev_->modulus(0);
-    Ciphertext rtn1, rtn2, m1, m2;
+    CT rtn1, rtn2, m1, m2;
     coefftoslot_full_3(rtn1, rtn2, cipher);
     mod_reducer.modular_reduction(m1, rtn1);
     mod_reducer.modular_reduction(m2, rtn2);
@@ -786,17 +817,18 @@ void Bootstrapper::bootstrap_full_3(Ciphertext &rtncipher, Ciphertext &cipher)
     rtncipher.scale() = final_scale;
 }
 
-void Bootstrapper::bootstrap_sparse_3(Ciphertext &rtncipher, Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::bootstrap_sparse_3(CT &rtncipher, CT &cipher)
 {
-    Evaluator &ev = *ev_;
+    EV &ev = *ev_;
     modraise_inplace(cipher);
     cipher.scale() = (double)ev.modulus(0);
-    Ciphertext rot;
+    CT rot;
     for (long i = logn; i < logNh; ++i) {
         ev.rotate_vector(cipher, (int)(1L << i), rot);
         ev.add_inplace(cipher, rot);
     }
-    Ciphertext rtn;
+    CT rtn;
     if (logn == 0) {
         CVec cts(Nh, 0);
         for (long i = 0; i < Nh; i++) {
@@ -807,13 +839,13 @@ void Bootstrapper::bootstrap_sparse_3(Ciphertext &rtncipher, Ciphertext &cipher)
         }
         ev.multiply_vector_reduced_error(cipher, cts, rtn);
         ev.rescale_to_next_inplace(rtn);
-        Ciphertext conj = rtn;
+        CT conj = rtn;
         ev.complex_conjugate_inplace(conj);
         ev.add_inplace_reduced_error(rtn, conj);
     } else {
         coefftoslot_3(rtn, cipher);
     }
-    Ciphertext modrtn;
+    CT modrtn;
     mod_reducer.modular_reduction(modrtn, rtn);
     if (logn == 0) {
         const double mod_zero = (double)ev.modulus(0);
@@ -828,7 +860,7 @@ void Bootstrapper::bootstrap_sparse_3(Ciphertext &rtncipher, Ciphertext &cipher)
         }
         ev.multiply_vector_reduced_error(modrtn, stc, rtncipher);
         ev.rescale_to_next_inplace(rtncipher);
-        Ciphertext r;
+        CT r;
         ev.rotate_vector(rtncipher, 1, r);
         ev.add_inplace_reduced_error(rtncipher, r);
     } else {
@@ -837,7 +869,8 @@ void Bootstrapper::bootstrap_sparse_3(Ciphertext &rtncipher, Ciphertext &cipher)
     rtncipher.scale() = final_scale;
 }
 
-void Bootstrapper::bootstrap_3(Ciphertext &rtncipher, Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::bootstrap_3(CT &rtncipher, CT &cipher)
 {
     if (fftcoeff1.empty()) throw std::logic_error("generate_LT_coefficient_3 has not been called");
     initial_scale = cipher.scale();
@@ -847,11 +880,17 @@ void Bootstrapper::bootstrap_3(Ciphertext &rtncipher, Ciphertext &cipher)
         bootstrap_sparse_3(rtncipher, cipher);
 }
 
-void Bootstrapper::bootstrap_inplace_3(Ciphertext &cipher)
+template <class EV, class CT>
+void BootstrapperT<EV, CT>::bootstrap_inplace_3(CT &cipher)
 {
-    Ciphertext r;
+    CT r;
     bootstrap_3(r, cipher);
     cipher = std::move(r);
 }
+
+template class ModularReducerT<Evaluator, Ciphertext>;
+template class ModularReducerT<BatchEvaluator, CtBatch>;
+template class BootstrapperT<Evaluator, Ciphertext>;
+template class BootstrapperT<BatchEvaluator, CtBatch>;
 
 }  // namespace nexus

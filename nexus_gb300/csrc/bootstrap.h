@@ -19,6 +19,7 @@
 #include <tuple>
 #include <vector>
 
+#include "batch.h"
 #include "ckks.h"
 
 namespace nexus {
@@ -33,7 +34,10 @@ void rotation(int logslot, int nh, int shiftcount, const CVec &vec, CVec &rtnvec
 // out = {fftcoeff1, fftcoeff2, fftcoeff3, invfftcoeff1, invfftcoeff2, invfftcoeff3}
 void lt_coefficients_3(long logn, long logNh, long boundary_K, std::vector<CVec> out[6]);
 
-class ModularReducer {
+// EV / CT: Evaluator / Ciphertext (one ciphertext) or BatchEvaluator / CtBatch
+// (ciphertexts in lockstep); the code is the same call sequence for both.
+template <class EV, class CT>
+class ModularReducerT {
 public:
     long boundary_K;
     double log_width;
@@ -47,20 +51,20 @@ public:
     long heap_k = 0, heap_m = 0;
     std::vector<std::vector<double>> heap;
 
-    ModularReducer(Evaluator &ev, long boundary_K, double log_width, long deg, long num_double_formula,
-                   long inverse_deg);
+    ModularReducerT(EV &ev, long boundary_K, double log_width, long deg, long num_double_formula, long inverse_deg);
     void set_polynomial_heap(long k, long m, std::vector<std::vector<double>> nodes, double scale_inverse_coeff);
 
-    void double_angle_formula(Ciphertext &cipher);
-    void double_angle_formula_scaled(Ciphertext &cipher, double scale_coeff);
-    void homomorphic_poly_evaluation(Ciphertext &rtn, const Ciphertext &cipher);
-    void modular_reduction(Ciphertext &rtn, const Ciphertext &cipher);
+    void double_angle_formula(CT &cipher);
+    void double_angle_formula_scaled(CT &cipher, double scale_coeff);
+    void homomorphic_poly_evaluation(CT &rtn, const CT &cipher);
+    void modular_reduction(CT &rtn, const CT &cipher);
 
 private:
-    Evaluator *ev_;
+    EV *ev_;
 };
 
-class Bootstrapper {
+template <class EV, class CT>
+class BootstrapperT {
 public:
     long loge, logn, n, logNh, Nh, L;
     double initial_scale = 0.0, final_scale;
@@ -72,10 +76,28 @@ public:
     std::vector<std::vector<CVec>> fftcoeff1, fftcoeff2, fftcoeff3;
     std::vector<std::vector<CVec>> invfftcoeff1, invfftcoeff2, invfftcoeff3;
 
-    ModularReducer mod_reducer;
+    ModularReducerT<EV, CT> mod_reducer;
 
-    Bootstrapper(Evaluator &ev, long loge, long logn, long logNh, long L, double final_scale, long boundary_K,
-                 long sin_cos_deg, long scale_factor, long inverse_deg);
+    BootstrapperT(EV &ev, long loge, long logn, long logNh, long L, double final_scale, long boundary_K,
+                  long sin_cos_deg, long scale_factor, long inverse_deg);
+    // take the EvalMod heap and LT diagonals of another bootstrapper with the
+    // same parameters (the batched form reuses the single form's setup)
+    template <class EV2, class CT2>
+    void adopt_setup(const BootstrapperT<EV2, CT2> &o)
+    {
+        slot_vec = o.slot_vec;
+        slot_index = o.slot_index;
+        fftcoeff1 = o.fftcoeff1;
+        fftcoeff2 = o.fftcoeff2;
+        fftcoeff3 = o.fftcoeff3;
+        invfftcoeff1 = o.invfftcoeff1;
+        invfftcoeff2 = o.invfftcoeff2;
+        invfftcoeff3 = o.invfftcoeff3;
+        final_scale = o.final_scale;
+        mod_reducer.set_polynomial_heap(o.mod_reducer.heap_k, o.mod_reducer.heap_m, o.mod_reducer.heap,
+                                        o.mod_reducer.scale_inverse_coeff);
+        cache_.clear();
+    }
 
     void set_final_scale(double s) { final_scale = s; }
     void prepare_mod_polynomial(long heap_k, long heap_m, std::vector<std::vector<double>> nodes,
@@ -84,25 +106,25 @@ public:
     void generate_LT_coefficient_3();
     void change_logn(long new_logn);
 
-    void bsgs_linear_transform(Ciphertext &rtncipher, const Ciphertext &cipher, int totlen, int basicstep,
+    void bsgs_linear_transform(CT &rtncipher, const CT &cipher, int totlen, int basicstep,
                                int coeff_logn, const std::vector<CVec> &fftcoeff, int tag);
-    void rotated_bsgs_linear_transform(Ciphertext &rtncipher, const Ciphertext &cipher, int totlen, int basicstep,
+    void rotated_bsgs_linear_transform(CT &rtncipher, const CT &cipher, int totlen, int basicstep,
                                        int coeff_logn, const std::vector<CVec> &fftcoeff, int tag);
 
-    void sfl_3(Ciphertext &rtncipher, const Ciphertext &cipher);
-    void sfl_full_3(Ciphertext &rtncipher, const Ciphertext &cipher);
-    void sflinv_3(Ciphertext &rtncipher, const Ciphertext &cipher);
-    void sflinv_full_3(Ciphertext &rtncipher, const Ciphertext &cipher);
-    void coefftoslot_3(Ciphertext &rtncipher, const Ciphertext &cipher);
-    void slottocoeff_3(Ciphertext &rtncipher, const Ciphertext &cipher);
-    void coefftoslot_full_3(Ciphertext &rtncipher1, Ciphertext &rtncipher2, const Ciphertext &cipher);
-    void slottocoeff_full_3(Ciphertext &rtncipher, const Ciphertext &cipher1, const Ciphertext &cipher2);
-    void modraise_inplace(Ciphertext &cipher);
+    void sfl_3(CT &rtncipher, const CT &cipher);
+    void sfl_full_3(CT &rtncipher, const CT &cipher);
+    void sflinv_3(CT &rtncipher, const CT &cipher);
+    void sflinv_full_3(CT &rtncipher, const CT &cipher);
+    void coefftoslot_3(CT &rtncipher, const CT &cipher);
+    void slottocoeff_3(CT &rtncipher, const CT &cipher);
+    void coefftoslot_full_3(CT &rtncipher1, CT &rtncipher2, const CT &cipher);
+    void slottocoeff_full_3(CT &rtncipher, const CT &cipher1, const CT &cipher2);
+    void modraise_inplace(CT &cipher);
 
-    void bootstrap_sparse_3(Ciphertext &rtncipher, Ciphertext &cipher);
-    void bootstrap_full_3(Ciphertext &rtncipher, Ciphertext &cipher);
-    void bootstrap_3(Ciphertext &rtncipher, Ciphertext &cipher);
-    void bootstrap_inplace_3(Ciphertext &cipher);
+    void bootstrap_sparse_3(CT &rtncipher, CT &cipher);
+    void bootstrap_full_3(CT &rtncipher, CT &cipher);
+    void bootstrap_3(CT &rtncipher, CT &cipher);
+    void bootstrap_inplace_3(CT &cipher);
 
     // device copies of encoded diagonals kept between bootstraps
     size_t cached_plaintexts() const { return cache_.size(); }
@@ -111,13 +133,17 @@ public:
 private:
     // the plaintext multiply_vector_reduced_error(ct, rotation(coeff_logn, Nh,
     // shift, v)) encodes, taken from (or put into) the cache
-    const Plaintext &diagonal(const Ciphertext &ct, int tag, int index, int shift, int coeff_logn, const CVec &v,
+    const Plaintext &diagonal(const CT &ct, int tag, int index, int shift, int coeff_logn, const CVec &v,
                               uint64_t salt);
     const Plaintext &unit_plain(bool plus_i, int limbs);
-    Evaluator *ev_;
+    EV *ev_;
     using Key = std::tuple<int, int, int, int, uint64_t, uint64_t>;
     std::map<Key, Plaintext> cache_;
     uint64_t salt_ = 0;  // distinguishes diagonals that depend on the scales of the call
 };
+
+using ModularReducer = ModularReducerT<Evaluator, Ciphertext>;
+using Bootstrapper = BootstrapperT<Evaluator, Ciphertext>;
+using BatchBootstrapper = BootstrapperT<BatchEvaluator, CtBatch>;
 
 }  // namespace nexus

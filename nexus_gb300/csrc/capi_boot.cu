@@ -1,4 +1,5 @@
 // C ABI of the bootstrapper (declared in include/nexus_gb300.h).
+#include <memory>
 #include <stdexcept>
 #include <string>
 
@@ -11,6 +12,9 @@ using namespace nexus;
 struct nexus_bootstrapper {
     nexus_evaluator *ev;
     Bootstrapper bs;
+    // the lockstep form, built from bs's setup on the first batched call
+    std::unique_ptr<BatchEvaluator> bev;
+    std::unique_ptr<BatchBootstrapper> bbs;
 };
 
 namespace {
@@ -44,8 +48,10 @@ extern "C" int nexus_bootstrapper_create(nexus_evaluator *ev, long loge, long lo
     if (!ev || !out) return fail(fn, "null argument");
     *out = nullptr;
     return guarded(fn, [&] {
-        *out = new nexus_bootstrapper{ev, Bootstrapper(ev->ev, loge, logn, logNh, L, final_scale, boundary_K,
-                                                       sin_cos_deg, scale_factor, inverse_deg)};
+        *out = new nexus_bootstrapper{ev,
+                                      Bootstrapper(ev->ev, loge, logn, logNh, L, final_scale, boundary_K, sin_cos_deg,
+                                                   scale_factor, inverse_deg),
+                                      nullptr, nullptr};
     });
 }
 
@@ -72,6 +78,7 @@ extern "C" int nexus_bootstrapper_prepare_mod_polynomial(nexus_bootstrapper *bs,
             off += (size_t)node_len[i];
         }
         bs->bs.prepare_mod_polynomial(heap_k, heap_m, std::move(nodes), scale_inverse_coeff);
+        bs->bbs.reset();
     });
 }
 
@@ -92,7 +99,10 @@ extern "C" int nexus_bootstrapper_generate_lt(nexus_bootstrapper *bs)
 {
     static const char *fn = "nexus_bootstrapper_generate_lt";
     if (!bs) return fail(fn, "null argument");
-    return guarded(fn, [&] { bs->bs.generate_LT_coefficient_3(); });
+    return guarded(fn, [&] {
+        bs->bs.generate_LT_coefficient_3();
+        bs->bbs.reset();
+    });
 }
 
 extern "C" int nexus_lt_coefficients_3(int logn, int logNh, long boundary_K, int which, double *out, int *count,
@@ -131,6 +141,54 @@ extern "C" int nexus_bootstrap(nexus_bootstrapper *bs, nexus_ciphertext *ct, nex
     return guarded(fn, [&] { bs->bs.bootstrap_3(rtn->ct, ct->ct); });
 }
 
+extern "C" int nexus_bootstrap_batch(nexus_bootstrapper *bs, nexus_ciphertext *const *cts, int count,
+                                     nexus_ciphertext *const *rtn)
+{
+    static const char *fn = "nexus_bootstrap_batch";
+    if (!bs || !cts || !rtn || count < 1) return fail(fn, "null argument");
+    for (int b = 0; b < count; ++b) {
+        if (!cts[b] || !rtn[b]) return fail(fn, "null ciphertext");
+        for (int j = 0; j < count; ++j)
+            if (rtn[b] == cts[j]) return fail(fn, "rtn must not alias an input");
+    }
+    return guarded(fn, [&] {
+        Bootstrapper &S = bs->bs;
+        if (S.fftcoeff1.empty()) throw std::logic_error("generate_LT_coefficient_3 has not been called");
+        if (!bs->bbs) {
+            bs->bev.reset(new BatchEvaluator(bs->ev->ev));
+            bs->bbs.reset(new BatchBootstrapper(*bs->bev, S.loge, S.logn, S.logNh, S.L, S.final_scale, S.boundary_K,
+                                                S.sin_cos_deg, S.scale_factor, S.inverse_deg));
+            bs->bbs->adopt_setup(S);
+        }
+        bs->bbs->set_final_scale(S.final_scale);
+        const Ciphertext &first = cts[0]->ct;
+        for (int b = 0; b < count; ++b) {
+            const Ciphertext &c = cts[b]->ct;
+            if (c.size() != 2) throw std::invalid_argument("Ciphertexts of size 2 are supported only!");
+            if (c.limbs() != 1) throw std::invalid_argument("Ciphertexts in the lowest level are supported only!");
+            if (c.scale() != first.scale()) throw std::invalid_argument("the ciphertexts of a batch must share one scale");
+        }
+        Context &ctx = bs->ev->ctx->c;
+        cudaStream_t s = bs->ev->ev.stream();
+        CtBatch in, out;
+        in.resize(ctx, count, 2, 1, s);
+        in.scale() = first.scale();
+        for (int b = 0; b < count; ++b)
+            if (cudaMemcpyAsync(in.ct(b), cts[b]->ct.data(), in.words_per_ct() * 8, cudaMemcpyDeviceToDevice, s) !=
+                cudaSuccess)
+                throw std::runtime_error("copy failed");
+        bs->bbs->bootstrap_3(out, in);
+        for (int b = 0; b < count; ++b) {
+            Ciphertext &r = rtn[b]->ct;
+            r.resize(ctx, out.size(), out.limbs(), s);
+            r.scale() = out.scale();
+            if (cudaMemcpyAsync(r.data(), out.ct(b), out.words_per_ct() * 8, cudaMemcpyDeviceToDevice, s) !=
+                cudaSuccess)
+                throw std::runtime_error("copy failed");
+        }
+    });
+}
+
 extern "C" int nexus_bootstrapper_stage(nexus_bootstrapper *bs, int stage, nexus_ciphertext *a,
                                         const nexus_ciphertext *b, nexus_ciphertext *r1, nexus_ciphertext *r2)
 {
@@ -166,6 +224,6 @@ extern "C" int nexus_bootstrapper_stage(nexus_bootstrapper *bs, int stage, nexus
 extern "C" int nexus_bootstrapper_cached_plaintexts(const nexus_bootstrapper *bs, uint64_t *count)
 {
     if (!bs || !count) return fail("nexus_bootstrapper_cached_plaintexts", "null argument");
-    *count = bs->bs.cached_plaintexts();
+    *count = bs->bs.cached_plaintexts() + (bs->bbs ? bs->bbs->cached_plaintexts() : 0);
     return 0;
 }

@@ -195,9 +195,10 @@ public:
     uint32_t galois_elt(int step) const;
 
     int total_bits(int limbs) const;
+    // is_scale_within_bounds (evaluator.cpp:29-47)
+    void check_scale(double scale, int limbs) const;
 
 private:
-    void check_scale(double scale, int limbs) const;
     void plain_arith(Ciphertext &ct, const Plaintext &pt, bool sub);
     // the scale adjustment shared by the *_reduced_error ops: bring the higher
     // ciphertext `hi` down to lo's level at lo's scale

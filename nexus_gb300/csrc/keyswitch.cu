@@ -143,7 +143,7 @@ void ks_moddown_terms(Context &c, const uint64_t *P, int B, int l, uint64_t *T, 
 }
 
 void switch_key_batch(Context &c, uint64_t *ct, int batch, int l, const uint64_t *target, const uint64_t *key,
-                      cudaStream_t s)
+                      cudaStream_t s, size_t target_pitch)
 {
     if (l < 1 || l > c.k - 1) throw std::invalid_argument("switch_key: level out of range");
     if (batch < 1) return;
@@ -157,7 +157,11 @@ void switch_key_batch(Context &c, uint64_t *ct, int batch, int l, const uint64_t
     uint64_t *T = P + B * 2 * (l + 1) * N;
     uint64_t *last = T + B * 2 * l * N;
 
-    cudaMemcpyAsync(t, target, sizeof(uint64_t) * B * l * N, cudaMemcpyDeviceToDevice, s);
+    if (target_pitch == 0 || target_pitch == (size_t)l * N)
+        cudaMemcpyAsync(t, target, sizeof(uint64_t) * B * l * N, cudaMemcpyDeviceToDevice, s);
+    else
+        cudaMemcpy2DAsync(t, sizeof(uint64_t) * l * N, target, sizeof(uint64_t) * target_pitch,
+                          sizeof(uint64_t) * l * N, B, cudaMemcpyDeviceToDevice, s);
     ks_modup_inner(c, t, batch, l, key, D, P, s);
     ks_moddown_terms(c, P, batch, l, T, last, s);
     const size_t tot = B * 2 * l * N;

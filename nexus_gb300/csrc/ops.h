@@ -22,8 +22,9 @@ void poly_mul_plain(const Context &c, const uint64_t *ct, int polys, int limbs, 
                     cudaStream_t s);
 // out[p] = sum_j cts[j][p] * pts[j] for both polynomials p of `count` (<= 16)
 // two-polynomial ciphertexts; 128-bit exact accumulation, one reduction
+// (batch > 1: each cts[j] and out hold `batch` ciphertexts back to back)
 void poly_mac_plain(const Context &c, const uint64_t *const *cts, const uint64_t *const *pts, int count, int limbs,
-                    uint64_t *out, cudaStream_t s);
+                    uint64_t *out, cudaStream_t s, int batch = 1);
 // out[p] = ct[p] + pt (pt broadcast); used for add_plain
 void poly_add_plain(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *pt, int sub,
                     uint64_t *out, cudaStream_t s);
@@ -31,12 +32,15 @@ void poly_add_plain(const Context &c, const uint64_t *ct, int polys, int limbs, 
 void poly_mul_scalar(const Context &c, const uint64_t *ct, int polys, int limbs, const uint64_t *scalars,
                      uint64_t *out, cudaStream_t s);
 
-// out = in (+|-) per-limb scalar, one polynomial [limbs][N] (add_plain of a scalar plaintext)
+// out = in (+|-) per-limb scalar, one polynomial [limbs][N] (add_plain of a scalar plaintext);
+// batch > 1: `batch` such polynomials every stride_words words (component 0 of a batch)
 void poly_add_scalar(const Context &c, const uint64_t *in, int limbs, const uint64_t *scalars, int sub, uint64_t *out,
-                     cudaStream_t s);
+                     cudaStream_t s, int batch = 1, size_t stride_words = 0);
 
-// ckks_multiply / ckks_square tensor: out3 = (a0 b0, a0 b1 + a1 b0, a1 b1)
-void tensor(const Context &c, const uint64_t *a, const uint64_t *b, int limbs, uint64_t *out3, cudaStream_t s);
+// ckks_multiply / ckks_square tensor: out3 = (a0 b0, a0 b1 + a1 b0, a1 b1), over
+// `batch` pairs back to back
+void tensor(const Context &c, const uint64_t *a, const uint64_t *b, int limbs, uint64_t *out3, cudaStream_t s,
+            int batch = 1);
 
 // divide_and_round_q_last_ntt over every polynomial: [size][limbs] -> [size][limbs-1]
 void rescale(const Context &c, const uint64_t *in, int size, int limbs, uint64_t *out, cudaStream_t s);
@@ -54,9 +58,10 @@ void galois_permute(Context &c, const uint64_t *in, int polys, int limbs, uint32
 void switch_key(Context &c, uint64_t *ct, int limbs, const uint64_t *target, const uint64_t *key, cudaStream_t s);
 
 // the same for `batch` ciphertexts ct[batch][2][limbs] and targets[batch][limbs]
-// sharing one key (the key is read once per launch, not once per ciphertext)
+// sharing one key (the key is read once per launch, not once per ciphertext);
+// target_pitch: words between consecutive targets (0 = limbs * N)
 void switch_key_batch(Context &c, uint64_t *ct, int batch, int limbs, const uint64_t *target, const uint64_t *key,
-                      cudaStream_t s);
+                      cudaStream_t s, size_t target_pitch = 0);
 
 // stages of the batched key switch, for callers that fuse their own epilogue:
 // ModUp + inner products (t [B][l] NTT-form targets, overwritten; D scratch

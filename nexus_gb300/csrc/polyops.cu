@@ -100,22 +100,24 @@ __device__ __forceinline__ void mac128p(uint64_t &lo, uint64_t &hi, uint64_t a, 
     asm("mad.lo.cc.u64 %0, %2, %3, %0;\n\tmadc.hi.u64 %1, %2, %3, %1;" : "+l"(lo), "+l"(hi) : "l"(a), "l"(b));
 }
 
+// (ct_j and out hold `total / (limbs N)` ciphertexts back to back, [batch][2][limbs][N])
 __global__ void k_mac_plain(MacTerms t, int count, uint64_t *__restrict__ out, const PrimeConst *__restrict__ pc,
                             int limbs, int logn, size_t total)
 {
     const size_t poly = (size_t)limbs << logn;
     for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
-        const size_t e = x % poly;  // limb * N + coefficient
+        const size_t b = x / poly, e = x - b * poly;  // ciphertext, limb * N + coefficient
+        const size_t at = b * 2 * poly + e;
         const int limb = (int)(e >> logn);
         uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
         for (int j = 0; j < count; ++j) {
             const uint64_t w = t.pt[j][e];
-            mac128p(lo0, hi0, t.ct[j][e], w);
-            mac128p(lo1, hi1, t.ct[j][poly + e], w);
+            mac128p(lo0, hi0, t.ct[j][at], w);
+            mac128p(lo1, hi1, t.ct[j][at + poly], w);
         }
         const PrimeConst P = pc[limb];
-        out[e] = barrett_128(lo0, hi0, P.q, P.r0, P.r1);
-        out[poly + e] = barrett_128(lo1, hi1, P.q, P.r0, P.r1);
+        out[at] = barrett_128(lo0, hi0, P.q, P.r0, P.r1);
+        out[at + poly] = barrett_128(lo1, hi1, P.q, P.r0, P.r1);
     }
 }
 
@@ -138,15 +140,19 @@ __global__ void k_mul_scalar(const ulonglong2 *__restrict__ ct, const LimbScalar
     }
 }
 
-// out[l] = in[l] (+|-) sc[l] over one polynomial [limbs][N]
+// out[l] = in[l] (+|-) sc[l] over `batch` polynomials [limbs][N] that start
+// every `stride` pairs (component 0 of each ciphertext of a batch)
 __global__ void k_add_scalar(const ulonglong2 *__restrict__ in, const LimbScalars sc, ulonglong2 *out,
-                             const PrimeConst *__restrict__ pc, int logn, size_t pairs, int sub)
+                             const PrimeConst *__restrict__ pc, int logn, size_t poly_pairs, int sub, size_t stride,
+                             size_t total)
 {
-    FOR_PAIRS(pairs)
+    FOR_PAIRS(total)
     {
-        const int limb = (int)(pi >> (logn - 1));
+        const size_t b = pi / poly_pairs, e = pi - b * poly_pairs;
+        const size_t at = b * stride + e;
+        const int limb = (int)(e >> (logn - 1));
         const uint64_t q = pc[limb].q, w = sc.w[limb].x;
-        ulonglong2 x = in[pi];
+        ulonglong2 x = in[at];
         if (sub) {
             x.x = sub_mod(x.x, w, q);
             x.y = sub_mod(x.y, w, q);
@@ -154,20 +160,24 @@ __global__ void k_add_scalar(const ulonglong2 *__restrict__ in, const LimbScalar
             x.x = add_mod(x.x, w, q);
             x.y = add_mod(x.y, w, q);
         }
-        out[pi] = x;
+        out[at] = x;
     }
 }
 
 // ckks_multiply (evaluator.cpp:770-850): out3 = (a0 b0, a0 b1 + a1 b0, a1 b1)
-__global__ void k_tensor(const ulonglong2 *__restrict__ a, const ulonglong2 *__restrict__ b, ulonglong2 *out,
-                         const PrimeConst *__restrict__ pc, int limbs, int logn)
+// over `batch` ciphertext pairs laid out back to back ([batch][2] in, [batch][3] out)
+__global__ void k_tensor(const ulonglong2 *__restrict__ a_, const ulonglong2 *__restrict__ b_, ulonglong2 *out_,
+                         const PrimeConst *__restrict__ pc, int limbs, int logn, size_t total)
 {
     const size_t poly_pairs = ((size_t)limbs << logn) >> 1;
-    FOR_PAIRS(poly_pairs)
+    FOR_PAIRS(total)
     {
-        const int limb = (int)(pi >> (logn - 1));
+        const size_t bt = pi / poly_pairs, e = pi - bt * poly_pairs;
+        const ulonglong2 *a = a_ + bt * 2 * poly_pairs, *b = b_ + bt * 2 * poly_pairs;
+        ulonglong2 *out = out_ + bt * 3 * poly_pairs;
+        const int limb = (int)(e >> (logn - 1));
         const PrimeConst P = pc[limb];
-        const ulonglong2 x0 = a[pi], x1 = a[pi + poly_pairs], y0 = b[pi], y1 = b[pi + poly_pairs];
+        const ulonglong2 x0 = a[e], x1 = a[e + poly_pairs], y0 = b[e], y1 = b[e + poly_pairs];
         ulonglong2 o0, o1, o2;
         o0.x = mul_mod(x0.x, y0.x, P.q, P.r0, P.r1);
         o0.y = mul_mod(x0.y, y0.y, P.q, P.r0, P.r1);
@@ -175,9 +185,9 @@ __global__ void k_tensor(const ulonglong2 *__restrict__ a, const ulonglong2 *__r
         o2.y = mul_mod(x1.y, y1.y, P.q, P.r0, P.r1);
         o1.x = add_mod(mul_mod(x0.x, y1.x, P.q, P.r0, P.r1), mul_mod(x1.x, y0.x, P.q, P.r0, P.r1), P.q);
         o1.y = add_mod(mul_mod(x0.y, y1.y, P.q, P.r0, P.r1), mul_mod(x1.y, y0.y, P.q, P.r0, P.r1), P.q);
-        out[pi] = o0;
-        out[pi + poly_pairs] = o1;
-        out[pi + 2 * poly_pairs] = o2;
+        out[e] = o0;
+        out[e + poly_pairs] = o1;
+        out[e + 2 * poly_pairs] = o2;
     }
 }
 
@@ -283,7 +293,7 @@ void poly_mul_plain(const Context &c, const uint64_t *ct, int polys, int limbs, 
 }
 
 void poly_mac_plain(const Context &c, const uint64_t *const *cts, const uint64_t *const *pts, int count, int limbs,
-                    uint64_t *out, cudaStream_t s)
+                    uint64_t *out, cudaStream_t s, int batch)
 {
     if (count < 1 || count > kMacTerms) throw std::invalid_argument("poly_mac_plain: 1..16 terms");
     MacTerms t{};
@@ -291,7 +301,7 @@ void poly_mac_plain(const Context &c, const uint64_t *const *cts, const uint64_t
         t.ct[j] = cts[j];
         t.pt[j] = pts[j];
     }
-    const size_t total = ((size_t)limbs << c.logn);
+    const size_t total = ((size_t)limbs << c.logn) * (size_t)batch;
     const unsigned grid = (unsigned)std::min<size_t>((total + kBlock - 1) / kBlock, 152 * 8);
     k_mac_plain<<<grid, kBlock, 0, s>>>(t, count, out, c.d_pc, limbs, c.logn, total); NEXUS_LAUNCHED();
 }
@@ -317,21 +327,24 @@ void poly_mul_scalar(const Context &c, const uint64_t *ct, int polys, int limbs,
 }
 
 void poly_add_scalar(const Context &c, const uint64_t *in, int limbs, const uint64_t *scalars, int sub, uint64_t *out,
-                     cudaStream_t s)
+                     cudaStream_t s, int batch, size_t stride_words)
 {
     if (limbs > 64) throw std::invalid_argument("at most 64 limbs");
     LimbScalars w;
     for (int l = 0; l < limbs; ++l) w.w[l] = make_ulonglong2(scalars[l], 0);
-    size_t pr = pairs_of(c, 1, limbs);
-    k_add_scalar<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, w, (ulonglong2 *)out, c.d_pc, c.logn, pr,
-                                                  sub); NEXUS_LAUNCHED();
+    const size_t pp = pairs_of(c, 1, limbs);
+    const size_t stride = stride_words ? stride_words / 2 : pp;
+    const size_t total = pp * (size_t)batch;
+    k_add_scalar<<<grid_for(total), kBlock, 0, s>>>((const ulonglong2 *)in, w, (ulonglong2 *)out, c.d_pc, c.logn, pp,
+                                                     sub, stride, total); NEXUS_LAUNCHED();
 }
 
-void tensor(const Context &c, const uint64_t *a, const uint64_t *b, int limbs, uint64_t *out3, cudaStream_t s)
+void tensor(const Context &c, const uint64_t *a, const uint64_t *b, int limbs, uint64_t *out3, cudaStream_t s,
+            int batch)
 {
-    size_t pr = pairs_of(c, 1, limbs);
+    size_t pr = pairs_of(c, batch, limbs);
     k_tensor<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)a, (const ulonglong2 *)b, (ulonglong2 *)out3, c.d_pc,
-                                              limbs, c.logn); NEXUS_LAUNCHED();
+                                              limbs, c.logn, pr); NEXUS_LAUNCHED();
 }
 
 void rescale(const Context &c_in, const uint64_t *in, int size, int limbs, uint64_t *out, cudaStream_t s)

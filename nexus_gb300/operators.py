@@ -214,6 +214,16 @@ class Bootstrapper:
         check(lib().nexus_bootstrap(self._h, ct.handle, rtn.handle), "nexus_bootstrap")
         return rtn
 
+    def bootstrap_batch(self, cts: list) -> list:
+        """bootstrap_3 of every ciphertext, run in lockstep (one launch per
+        operation for the whole batch, each key read once); the inputs are
+        left unchanged."""
+        res = [Ciphertext(self.ctx) for _ in cts]
+        a = (C.c_void_p * len(cts))(*[c.handle.value for c in cts])
+        r = (C.c_void_p * len(res))(*[x.handle.value for x in res])
+        check(lib().nexus_bootstrap_batch(self._h, a, len(cts), r), "nexus_bootstrap_batch")
+        return res
+
     def stage(self, stage: int, a: Ciphertext, b: Ciphertext | None = None):
         r1, r2 = Ciphertext(self.ctx), Ciphertext(self.ctx)
         check(lib().nexus_bootstrapper_stage(self._h, stage, a.handle, None if b is None else b.handle, r1.handle,

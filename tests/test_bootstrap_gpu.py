@@ -130,6 +130,29 @@ def test_second_bootstrap_reuses_encoded_diagonals(env):
     assert np.array_equal(a.to_numpy(), b.to_numpy())
 
 
+def test_batched_bootstrap_equals_single(env):
+    """The lockstep form gives every ciphertext the single form's words."""
+    ctx, sk, bs, obs, _ = env
+    ins = [_input(ctx, sk, 20 + i) for i in range(3)]
+    batch = bs.bootstrap_batch([x for _, x, _ in ins])
+    for (_, x, _), got in zip(ins, batch):
+        want = bs.bootstrap_3(x)
+        assert got.scale == want.scale
+        assert np.array_equal(got.to_numpy(), want.to_numpy())
+    one = bs.bootstrap_batch([_input(ctx, sk, 20)[1]])[0]
+    assert np.array_equal(one.to_numpy(), batch[0].to_numpy())
+
+
+def test_batched_bootstrap_rejects_mixed_scales(env):
+    from nexus_gb300._lib import NexusError
+    from nexus_gb300.operators import Ciphertext
+    ctx, sk, bs, obs, _ = env
+    _, x, ox = _input(ctx, sk, 30)
+    y = Ciphertext.from_numpy(ctx, ox.data, SCALE * 2)
+    with pytest.raises(NexusError, match="share one scale"):
+        bs.bootstrap_batch([x, y])
+
+
 def test_bootstrap_rejects_higher_level(env):
     from nexus_gb300._lib import NexusError
     from nexus_gb300.operators import Ciphertext
