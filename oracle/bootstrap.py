@@ -180,6 +180,41 @@ def gen_invfft_coeff_3_full(logn: int, inv, boundary_k: int):
     return c1, c2, c3
 
 
+def gen_fft_coeff_3_sparse(logn: int, orig):
+    """genfftcoeff_3, sparse branch (Bootstrapper.cpp:1284-1428): diagonals of
+    length 2n, the second half a copy (levels 1, 2) or i times the first
+    half (level 3)."""
+    n = 1 << logn
+    d1, d2, d3 = split3_fwd(logn)
+    t1, t2, t3 = (1 << d1) - 1, (1 << d2) - 1, (1 << d3) - 1
+    c1 = _merge_level(orig, 0, d1, 1, n, False, 2 * t1 + 1, lambda pos: pos + t1)
+    c2 = _merge_level(orig, d1, d2, 1 << d1, n, False, 2 * t2 + 1, lambda pos: pos + t2)
+    c3 = _merge_level(orig, d1 + d2, d3, 1 << (d1 + d2), n, False, 2 * t3 + 1, lambda pos: pos + t3)
+    c1 = [(np.concatenate([r, r]), np.concatenate([i, i])) for r, i in c1]
+    c2 = [(np.concatenate([r, r]), np.concatenate([i, i])) for r, i in c2]
+    # complex(0, 1) * z = (0*a - 1*b, 0*b + 1*a)
+    c3 = [(np.concatenate([r, 0.0 * r - 1.0 * i]), np.concatenate([i, 0.0 * i + 1.0 * r])) for r, i in c3]
+    return c1, c2, c3
+
+
+def gen_invfft_coeff_3_sparse(logn: int, log_nh: int, inv, boundary_k: int):
+    """geninvfftcoeff_3, sparse branch (Bootstrapper.cpp:1690-1818)."""
+    n = 1 << logn
+    d1, d2, d3 = split3_inv(logn)
+    t1, t2, t3 = (1 << d1) - 1, (1 << d2) - 1, (1 << d3) - 1
+    c1 = _merge_level(inv, 0, d1, 1 << (logn - d1), n, True, t1 + 1, lambda pos: (pos + t1 + 1) % (t1 + 1))
+    c2 = _merge_level(inv, d1, d2, 1 << (logn - d1 - d2), n, True, 2 * t2 + 1, lambda pos: pos + t2)
+    c3 = _merge_level(inv, d1 + d2, d3, 1, n, True, 2 * t3 + 1, lambda pos: pos + t3)
+    s = 1.0 / (boundary_k * (1 << (log_nh - logn)))
+    c1 = [(r * s, i * s) for r, i in c1]
+    out3 = []
+    for r, i in c3:
+        r, i = r * 0.5, i * 0.5
+        # complex(0, -1) * z = (0*a - (-1)*b, 0*b + (-1)*a)
+        out3.append((np.concatenate([r, 0.0 * r - (-1.0) * i]), np.concatenate([i, 0.0 * i + (-1.0) * r])))
+    return c1, c2, out3
+
+
 def rot_key_steps_3(logn: int, log_nh: int) -> list[int]:
     """Rotation steps of the driver (src/bootstrapping.cpp:111-118: 0 and 2^i)
     followed by addLeftRotKeys_Linear_to_vector_3 (Bootstrapper.cpp:89-184)."""
@@ -264,11 +299,13 @@ class Bootstrapper:
 
     # -- setup ---------------------------------------------------------------
     def generate_LT_coefficient_3(self):
-        if self.logn != self.log_nh:
-            raise NotImplementedError("sparse-slot LT coefficients are not restated")
         orig, inv = gen_orig_coeff(self.logn)
-        self.fftcoeff = gen_fft_coeff_3_full(self.logn, orig)
-        self.invfftcoeff = gen_invfft_coeff_3_full(self.logn, inv, self.boundary_k)
+        if self.logn == self.log_nh:
+            self.fftcoeff = gen_fft_coeff_3_full(self.logn, orig)
+            self.invfftcoeff = gen_invfft_coeff_3_full(self.logn, inv, self.boundary_k)
+        else:
+            self.fftcoeff = gen_fft_coeff_3_sparse(self.logn, orig)
+            self.invfftcoeff = gen_invfft_coeff_3_sparse(self.logn, self.log_nh, inv, self.boundary_k)
 
     def rotation_steps(self):
         return rot_key_steps_3(self.logn, self.log_nh)
@@ -350,6 +387,43 @@ class Bootstrapper:
             f[i] = ((re * curr_mod) * mod_zero * self.final_scale / s,
                     (im * curr_mod) * mod_zero * self.final_scale / s)
         return self.ev.rescale(self.rotated_bsgs_linear_transform(x, t3, 1 << (d1 + d2), logn, f))
+
+    def sflinv_3(self, ct):
+        """Bootstrapper.cpp:2578-2602."""
+        logn = self.logn
+        d1, d2, d3 = split3_inv(logn)
+        t1, t2, t3 = (1 << d1) - 1, (1 << d2) - 1, (1 << d3) - 1
+        c1, c2, c3 = self.invfftcoeff
+        x = self.ev.rescale(self.rotated_bsgs_linear_transform(ct, t1, 1 << (logn - d1), logn, c1))
+        x = self.ev.rescale(self.bsgs_linear_transform(x, t2, 1 << (logn - d1 - d2), logn, c2))
+        return self.ev.rescale(self.bsgs_linear_transform(x, t3, 1, logn + 1, c3))
+
+    def sfl_3(self, ct):
+        """Bootstrapper.cpp:2419-2456."""
+        logn = self.logn
+        d1, d2, d3 = split3_fwd(logn)
+        t1, t2, t3 = (1 << d1) - 1, (1 << d2) - 1, (1 << d3) - 1
+        c1, c2, c3 = self.fftcoeff
+        x = self.ev.rescale(self.bsgs_linear_transform(ct, t1, 1, logn + 1, c1))
+        x = self.ev.rescale(self.bsgs_linear_transform(x, t2, 1 << d1, logn + 1, c2))
+        mod_zero = float(self.ev.q[0])
+        curr_mod = float(self.ev.q[x.limbs - 1])
+        f = []
+        for re, im in c3:
+            s = x.scale * x.scale * self.initial_scale
+            f.append(((re * curr_mod) * mod_zero * self.final_scale / s,
+                      (im * curr_mod) * mod_zero * self.final_scale / s))
+        return self.ev.rescale(self.bsgs_linear_transform(x, t3, 1 << (d1 + d2), logn + 1, f))
+
+    def coefftoslot_3(self, ct):
+        """Bootstrapper.cpp:2720-2725."""
+        t1 = self.sflinv_3(ct)
+        return self.ev.add_reduced_error(t1, self.ev.conjugate(t1))
+
+    def slottocoeff_3(self, ct):
+        """Bootstrapper.cpp:2727-2732."""
+        t1 = self.sfl_3(ct)
+        return self.ev.add_reduced_error(t1, self.ev.rotate(t1, self.n))
 
     def coefftoslot_full_3(self, ct):
         """Bootstrapper.cpp:2741-2757: (real part, imaginary part) ciphertexts."""
@@ -481,9 +555,36 @@ class Bootstrapper:
         out.scale = self.final_scale
         return out
 
+    def bootstrap_sparse_3(self, ct):
+        """Bootstrapper.cpp:3142-3222."""
+        ev, nh = self.ev, self.nh
+        x = self.modraise_inplace(ct)
+        x.scale = float(ev.q[0])
+        for i in range(self.logn, self.log_nh):
+            x = ev.add(x, ev.rotate(x, 1 << i))
+        if self.logn == 0:
+            k = 2.0 * self.boundary_k * (1 << self.log_nh)
+            v = np.array([1.0 / k if i % 2 == 0 else -1j / k for i in range(nh)])
+            rtn = ev.rescale(ev.multiply_vector_reduced_error(x, v))
+            rtn = ev.add_reduced_error(rtn, ev.conjugate(rtn))
+        else:
+            rtn = self.coefftoslot_3(x)
+        mod = self.modular_reduction(rtn)
+        if self.logn == 0:
+            mod_zero = float(ev.q[0])
+            curr_mod = float(ev.q[mod.limbs - 1])
+            adj = curr_mod * mod_zero * self.final_scale / (mod.scale * mod.scale * self.initial_scale)
+            v = np.array([adj if i % 2 == 0 else 1j * adj for i in range(nh)])
+            out = ev.rescale(ev.multiply_vector_reduced_error(mod, v))
+            out = ev.add_reduced_error(out, ev.rotate(out, 1))
+        else:
+            out = self.slottocoeff_3(mod)
+        out.scale = self.final_scale
+        return out
+
     def bootstrap_3(self, ct):
         """Bootstrapper.cpp:3489-3495."""
         self.initial_scale = ct.scale
         if self.logn == self.log_nh:
             return self.bootstrap_full_3(ct)
-        raise NotImplementedError("sparse-slot bootstrap is not restated")
+        return self.bootstrap_sparse_3(ct)

@@ -160,3 +160,48 @@ def test_bootstrap_rejects_higher_level(env):
     data = np.zeros((2, 2, N), dtype=np.uint64)
     with pytest.raises(NexusError, match="lowest level"):
         bs.bootstrap_3(Ciphertext.from_numpy(ctx, data, SCALE))
+
+
+@pytest.fixture(scope="module")
+def sparse_env(cuda):
+    """The sparse-slot path (bootstrap_sparse_3): 2^11 distinct slots repeating
+    across the 2^12 slots, as the reference driver (src/bootstrapping.cpp) runs it."""
+    import nexus_gb300 as ng
+    from nexus_gb300.operators import Bootstrapper, Evaluator
+    from nexus_gb300.remez import load_table
+    logn = LOG_NH - 1
+    qs = ng.create_coeff_modulus(N, BITS)
+    ctx = ng.Context(LOG_N, qs)
+    sk = ctx.keygen_secret(seed=51, hamming_weight=192)
+    rk = ctx.keygen_relin(sk, seed=52)
+    steps = B.rot_key_steps_3(logn, LOG_NH)
+    gks = {ctx.galois_elt(st): ctx.keygen_galois(sk, ctx.galois_elt(st), seed=53 + i) for i, st in enumerate(steps)}
+    ev = Evaluator(ctx, SCALE, rk, gks)
+    params = dict(PARAMS, logn=logn)
+    bs = Bootstrapper(ev, **params)
+    bs.prepare_mod_polynomial()
+    bs.generate_LT_coefficient_3()
+    oev = L.Evaluator(po.OracleContext(LOG_N, qs), to_host(rk), {e: to_host(k) for e, k in gks.items()})
+    obs = B.Bootstrapper(oev, 10, logn, LOG_NH, PARAMS["L"], SCALE, 25, 59, 2, 1, load_table())
+    obs.generate_LT_coefficient_3()
+    return ctx, sk, bs, obs, steps, logn
+
+
+def test_sparse_bootstrap_matches_oracle(sparse_env):
+    import torch
+    from nexus_gb300.operators import Ciphertext
+    ctx, sk, bs, obs, steps, logn = sparse_env
+    assert bs.rotation_steps(LOG_NH) == steps
+    sparse = np.random.default_rng(61).uniform(-1, 1, 1 << logn)
+    vals = np.resize(sparse, N // 2)
+    top = len(ctx.moduli) - 1
+    pt = torch.empty((top, N), dtype=torch.int64, device="cuda")
+    ctx.encode(vals, SCALE, top, pt)
+    low = to_host(ctx.encrypt_symmetric(sk, pt, top, 62))[:, :1, :].copy()
+    x = Ciphertext.from_numpy(ctx, low, SCALE)
+    batch = bs.bootstrap_batch([x])[0]
+    out = bs.bootstrap_3(x)
+    _same(out, obs.bootstrap_3(L.Ct(low, SCALE)))
+    assert np.array_equal(batch.to_numpy(), out.to_numpy())
+    err = np.abs(_decrypt(ctx, sk, out) - vals)
+    assert err.max() < 2.0 ** -12, err.max()

@@ -34,13 +34,16 @@ def test_rotation_steps():
     assert all(0 <= x < 4096 for x in s)
 
 
-@pytest.mark.parametrize("logn", [12, 13])
-def test_engine_diagonals_equal_oracle(logn):
+@pytest.mark.parametrize("logn,log_nh", [(12, 12), (13, 13), (11, 12), (9, 12)])
+def test_engine_diagonals_equal_oracle(logn, log_nh):
     from nexus_gb300.operators import lt_coefficients_3
     orig, inv = B.gen_orig_coeff(logn)
-    mine = list(B.gen_fft_coeff_3_full(logn, orig)) + list(B.gen_invfft_coeff_3_full(logn, inv, K))
+    if logn == log_nh:
+        mine = list(B.gen_fft_coeff_3_full(logn, orig)) + list(B.gen_invfft_coeff_3_full(logn, inv, K))
+    else:
+        mine = list(B.gen_fft_coeff_3_sparse(logn, orig)) + list(B.gen_invfft_coeff_3_sparse(logn, log_nh, inv, K))
     for which, diags in enumerate(mine):
-        eng = lt_coefficients_3(logn, logn, K, which)
+        eng = lt_coefficients_3(logn, log_nh, K, which)
         assert eng.shape[0] == len(diags)
         for i, (re, im) in enumerate(diags):
             assert np.array_equal(eng[i, :len(re), 0].view(np.uint64), re.view(np.uint64)), (which, i)
@@ -120,7 +123,10 @@ def test_evalmod_table():
     assert np.abs(y - (xs - np.round(xs))).max() < 1e-8
 
 
-def test_oracle_bootstrap_decrypts_to_input():
+@pytest.mark.parametrize("logn", [12, 11])
+def test_oracle_bootstrap_decrypts_to_input(logn):
+    """Full-slot (logn = logNh) and sparse-slot (logn < logNh, slots repeating
+    with period 2^logn as in src/bootstrapping.cpp:139-141) bootstraps."""
     from oracle import nexus_l3 as L
     from oracle import pyoracle as po
     from oracle import pyref as pr
@@ -130,13 +136,14 @@ def test_oracle_bootstrap_decrypts_to_input():
     log_n = 13
     n = 1 << log_n
     qs = po.create_coeff_modulus(n, [51] + [46] * 2 + [51] * 14 + [51])
-    steps = B.rot_key_steps_3(log_n - 1, log_n - 1)
+    steps = B.rot_key_steps_3(logn, log_n - 1)
     s = pr.SealRef(log_n, qs, seed=7, hamming_weight=192, steps=steps)
     ev = L.Evaluator(po.OracleContext(log_n, qs), s.relin_key(),
                      {s.galois_elt(st): s.galois_key(s.galois_elt(st)) for st in steps})
-    bs = B.Bootstrapper(ev, 10, log_n - 1, log_n - 1, len(qs) - 2, 2.0 ** 46, K, 59, 2, 1, load_table())
+    bs = B.Bootstrapper(ev, 10, logn, log_n - 1, len(qs) - 2, 2.0 ** 46, K, 59, 2, 1, load_table())
     bs.generate_LT_coefficient_3()
-    vals = np.random.default_rng(1).uniform(-1, 1, n // 2)
+    sparse = np.random.default_rng(1).uniform(-1, 1, 1 << logn)
+    vals = np.resize(sparse, n // 2)
     ct = ev.mod_switch_to(L.Ct(s.encrypt(vals, 2.0 ** 46), 2.0 ** 46), 1)
     out = bs.bootstrap_3(ct)
     assert out.scale == 2.0 ** 46
