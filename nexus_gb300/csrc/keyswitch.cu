@@ -55,14 +55,16 @@ __device__ __forceinline__ void mac128(uint64_t &lo, uint64_t &hi, uint64_t a, u
 }
 
 // P[b][k][i'][n] = sum_j D[b][j][i'][n] * key[j][k][kidx(i')][n] mod q(i')
+// Rows run i'-major over the batch (row = i' * B + b), so the ciphertexts of a
+// batch read the key rows of one prime (2l limbs) back to back, from L2.
 __global__ void k_ks_inner(const uint64_t *__restrict__ D, const uint64_t *__restrict__ key, uint64_t *__restrict__ P,
-                           const PrimeConst *__restrict__ pc, int l, int K, int logn, size_t total)
+                           const PrimeConst *__restrict__ pc, int l, int K, int logn, int B, size_t total)
 {
     const size_t N = (size_t)1 << logn;
     for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
-        const size_t row = x >> logn;            // b*(l+1) + i
-        const size_t b = row / (size_t)(l + 1);
-        const int i = (int)(row % (size_t)(l + 1));
+        const size_t row = x >> logn;            // i * B + b
+        const size_t b = row % (size_t)B;
+        const int i = (int)(row / (size_t)B);
         const size_t n = x & (N - 1);
         const int kidx = (i == l) ? K - 1 : i;
         const PrimeConst P0 = pc[kidx];
@@ -121,7 +123,7 @@ void ks_modup_inner(Context &c, uint64_t *t, int B, int l, const uint64_t *key, 
     ld.src_limbs = l;
     ntt_forward_loaded(c, D, Bs * l, LimbMap{l + 1, 0, sp}, ld, s);
     size_t tot = Bs * (l + 1) * N;
-    k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, tot); NEXUS_LAUNCHED();
+    k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, tot); NEXUS_LAUNCHED();
 }
 
 // Stage 2: the rounding terms T [B][2][l][N] of the ModDown from the special
@@ -285,7 +287,7 @@ extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l,
         k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot); NEXUS_LAUNCHED();
         ntt_forward(c, D, l, LimbMap{l + 1, 0, sp}, s);
         tot = (size_t)(l + 1) * N;
-        k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, tot); NEXUS_LAUNCHED();
+        k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, 1, tot); NEXUS_LAUNCHED();
         cudaMemcpyAsync(last, P + (size_t)l * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(last + N, P + (size_t)(2 * l + 1) * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
         ntt_inverse(c, last, 2, LimbMap{1, sp, -1}, s);

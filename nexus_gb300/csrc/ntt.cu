@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
 // Pass 2: size-2^LOGS transforms along contiguous rows, then the final
 // reduction to [0,q) (from [0,4q), or from [0,50q) on the small-prime path).
 template <int LOGS, bool SMALL>
-__global__ void __launch_bounds__(kThreads) k_fwd_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
+__global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
                                                        const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
 {
     constexpr int S = 1 << LOGS, T = S / kE, R = kThreads / T, SP = S + S / 16;
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_rows(uint64_t *__restrict__ da
 
 // Inverse pass A: rows first (undoing pass 2).  Output in [0,2q).
 template <int LOGS>
-__global__ void __launch_bounds__(kThreads) k_inv_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
+__global__ void __launch_bounds__(kThreads, 3) k_inv_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
                                                        const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
 {
     constexpr int S = 1 << LOGS, T = S / kE, R = kThreads / T, SP = S + S / 16;
