@@ -12,6 +12,10 @@ Prints ONE JSON line (rank 0).  Workloads:
         angles, scale 2^46; one step = 16 one-limb ciphertexts of U(-1,1)
         slots refreshed.  Keys (~49 GB) stay resident; no L2 flush needed.
 
+  gelu  NEXUS's GELU (src/gelu.cpp) at N = 2^14 on the reference chain
+        58 + 18 x 40 + 58 (the literal 60 + 7 x 40 + 60 has too few levels), scale
+        2^40, 8192 slots; one step = 16 ciphertexts (U(-8,8) and U(-5,5)).
+
   matmul NEXUS's ct x pt MatMul at the BERT-base shape: an encrypted
         128 x 768 input of N(0,1), coefficient-packed into 2 ciphertexts,
         times plaintext weights 768 x 768 of N(0, 0.02) plus a bias of 768,
@@ -734,6 +738,171 @@ def cpu_boot_sample(workers: int = 1):
                       f"modelled {t_boot:.1f} s per bootstrap per core)"}
 
 
+# ----------------------------------------------------------------------------- GELU workload
+
+GELU_LOGN = 14
+GELU_BITS = [58] + [40] * 18 + [58]   # the reference chain (src/main.cpp:28); 60+7x40+60 runs out of levels
+GELU_SCALE = 2.0 ** 40
+GELU_CTS = 16
+
+
+def gelu_config():
+    return {"workload": f"gelu_n16384_{GELU_CTS}ct", "N": 1 << GELU_LOGN, "slots": 1 << (GELU_LOGN - 1),
+            "moduli_bits": "58 + 18x40 + 58", "scale": "2^40", "inputs": "U(-8,8) slots (U(-5,5) accuracy also)",
+            "cts_per_step": GELU_CTS, "parallelism": "replicas",
+            "note": "the literal chain 60+7x40+60 is infeasible (GELU needs 18 rescales)",
+            "l2": "relin key 2.9 GB and ciphertexts re-read per op; no flush"}
+
+
+def run_gelu_gpu(args, rank, world):
+    import math
+
+    import numpy as np
+    import torch
+
+    import nexus_gb300 as ng
+    from nexus_gb300.operators import Ciphertext, Evaluator
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = 1 << GELU_LOGN
+    qs = ng.create_coeff_modulus(n, GELU_BITS)
+    ctx = ng.Context(GELU_LOGN, qs)
+    sk = ctx.keygen_secret(seed=81 + rank)
+    rk = ctx.keygen_relin(sk, seed=82)
+    ev = Evaluator(ctx, GELU_SCALE, rk)
+    top = len(qs) - 1
+    rng = np.random.default_rng(777 + rank)
+    vals, cts, host = [], [], []
+    for i in range(GELU_CTS):
+        v = rng.uniform(-8, 8, n // 2) if i % 2 == 0 else rng.uniform(-5, 5, n // 2)
+        pt = torch.empty((top, n), dtype=torch.int64, device=dev)
+        ctx.encode(v, GELU_SCALE, top, pt)
+        ct = ctx.encrypt_symmetric(sk, pt, top, 900 + i)
+        vals.append(v)
+        cts.append(Ciphertext.from_device(ctx, ct, GELU_SCALE))
+        host.append(ct.cpu().numpy().view(np.uint64).copy())
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        return [ev.gelu(c) for c in cts]
+
+    for _ in range(args.warmup):
+        res = step()
+    torch.cuda.synchronize(dev)
+
+    def gelu_ref(x):
+        return 0.5 * x * (1 + np.tanh(math.sqrt(2 / math.pi) * (x + 0.044715 * x ** 3)))
+
+    errs = {}
+    for i, tag in ((0, "U(-8,8)"), (1, "U(-5,5)")):
+        dec = ctx.decode(ctx.decrypt(sk, res[i].to_device()), res[i].scale).real
+        errs[tag] = float(np.max(np.abs(dec - gelu_ref(vals[i]))))
+    del res
+    barrier(world)
+    l0 = ng.kernel_launches()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize(dev)
+        t0.record(stream)
+        for _ in range(args.steps):
+            res = step()
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = ng.kernel_launches() - l0
+    barrier(world)
+    total_ms = max_over_ranks(t0.elapsed_time(t1), world)
+    del res
+
+    ctx.ntt_timing_begin()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    res = step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ntt_ms, ntt_calls, ntt_limbs = ctx.ntt_timing_end()
+    instr_ms = e0.elapsed_time(e1)
+    del res
+
+    h_in = [torch.from_numpy(h.view(np.int64)).pin_memory() for h in host]
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    w0 = time.perf_counter()
+    out_bytes = 0
+    for h in h_in:
+        c = Ciphertext(ctx)
+        ng.check(ng.lib().nexus_ciphertext_load(c.handle, h.data_ptr(), 2, top, GELU_SCALE, 1, None), "load")
+        out_bytes += ev.gelu(c).to_numpy().nbytes
+    torch.cuda.synchronize(dev)
+    e2e_s = max_over_ranks(time.perf_counter() - w0, world)
+    in_bytes = sum(h.nbytes for h in host)
+
+    value = world * args.steps * GELU_CTS / (total_ms / 1e3)
+    peak, peak_kind = _peak_hbm()
+    ntt_avg_ms = ntt_ms / max(1, ntt_calls)
+    alg_bytes_per_call = 16.0 * n * ntt_limbs / max(1, ntt_calls)
+    achieved = alg_bytes_per_call / (ntt_avg_ms / 1e3) / 1e9
+    res = {
+        "metric": "gelu_throughput_n16384", "value": value, "unit": "GELU/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic: slots ~ U(-8,8) and U(-5,5) (alternating ciphertexts), seeded; engine-generated keys",
+        "config": gelu_config(),
+        "accuracy": {"max_abs_err_vs_fp64_gelu": errs},
+        "roofline": {
+            "kernel": "nexus NTT launches inside GELU (k_fwd/k_inv cols+rows)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg_bytes_per_call,
+            "avg_launch_ms": ntt_avg_ms, "launches_per_step": ntt_calls, "share_of_step": ntt_ms / instr_ms,
+            "traffic": None,
+        },
+        "e2e": {"value": world * GELU_CTS / e2e_s, "unit": "GELU/s", "h2d_bytes_per_step": in_bytes,
+                "d2h_bytes_per_step": out_bytes},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+    }
+    if rank == 0 and world == 1:
+        res["cpu_baseline"] = cpu_gelu_sample(workers=1)
+    return res
+
+
+def _gelu_cpu_worker(seed):
+    """One NEXUS GELU with the oracle port at N=2^14 on this core; returns seconds."""
+    import numpy as np
+
+    from oracle import nexus_l3 as L
+    from oracle import pyoracle as po
+    n = 1 << GELU_LOGN
+    qs = po.create_coeff_modulus(n, GELU_BITS)
+    rng = np.random.default_rng(seed)
+    rk = po.random_residues(rng, (len(qs) - 1, 2, len(qs), n), qs)  # cost is data-independent
+    ev = L.Evaluator(po.OracleContext(GELU_LOGN, qs), rk)
+    ck = L.CKKSEvaluator(ev, GELU_SCALE)
+    x = L.Ct(po.random_residues(rng, (2, len(qs) - 1, n), qs[:-1]), GELU_SCALE)
+    t = time.perf_counter()
+    L.gelu(ck, x)
+    return time.perf_counter() - t
+
+
+def cpu_gelu_sample(workers: int = 1):
+    """The oracle port's GELU at N=2^14 on `workers` host cores, one GELU per core."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    w0 = time.perf_counter()
+    if workers <= 1:
+        ts = [_gelu_cpu_worker(0)]
+    else:
+        with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            ts = list(ex.map(_gelu_cpu_worker, range(workers)))
+    wall = time.perf_counter() - w0
+    t = statistics.mean(ts)
+    return {"value": workers / t, "unit": "GELU/s", "cores": workers, "kind": "port",
+            "sample": f"{workers} worker(s) x one full GELU (N=2^14, 58+18x40+58) with the oracle port, "
+                      f"{t:.1f} s each ({wall:.1f} s wall)"}
+
+
 # ----------------------------------------------------------------------------- plumbing
 
 def barrier(world):
@@ -759,7 +928,7 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["nexus", "reference"], default="nexus")
-    ap.add_argument("--workload", choices=["bootstrap", "matmul", "ntt"], default="bootstrap")
+    ap.add_argument("--workload", choices=["bootstrap", "matmul", "ntt", "gelu"], default="bootstrap")
     ap.add_argument("--cpu-depth", type=int, default=7, help="expansion-subtree depth of the MatMul CPU sample")
     ap.add_argument("--mm-rows", type=int, default=128,
                     help="rows of the encrypted input (smaller values are for profiling captures only)")
@@ -778,10 +947,32 @@ def main():
     MM_ROWS = args.mm_rows
     BOOT_CTS = args.boot_cts
     if args.steps is None:
-        args.steps = {"bootstrap": 3, "matmul": 5}.get(args.workload, 20)
+        args.steps = {"bootstrap": 3, "matmul": 5, "gelu": 5}.get(args.workload, 20)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+
+    if args.impl == "reference" and args.workload == "gelu":
+        if rank != 0:
+            return
+        workers = max(1, os.cpu_count() or 1)
+        vals = []
+        for i in range(1 + args.steps):
+            r = cpu_gelu_sample(workers=workers)
+            if i >= 1:
+                vals.append(r)
+        value = statistics.mean(r["value"] for r in vals)
+        res = {
+            "impl": "reference", "metric": "gelu_throughput_n16384", "value": value, "unit": "GELU/s",
+            "n_gpus": world, "steps": args.steps, "warmup": 1, "ms_per_step": GELU_CTS * 1e3 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (random residues; cost is data-independent)", "config": gelu_config(),
+            "cpu_baseline": {"value": value, "unit": "GELU/s", "cores": workers, "kind": "port",
+                             "sample": "per step: " + vals[0]["sample"]},
+            "e2e": {"value": value, "unit": "GELU/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(res), flush=True)
+        return
 
     if args.impl == "reference" and args.workload == "bootstrap":
         if rank != 0:
@@ -855,7 +1046,7 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
-    run = {"bootstrap": run_boot_gpu, "matmul": run_mm_gpu, "ntt": run_ntt_gpu}[args.workload]
+    run = {"bootstrap": run_boot_gpu, "matmul": run_mm_gpu, "ntt": run_ntt_gpu, "gelu": run_gelu_gpu}[args.workload]
     res = run(args, rank, world)
     if rank == 0:
         print(json.dumps(res), flush=True)
