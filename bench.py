@@ -780,12 +780,14 @@ def run_gelu_gpu(args, rank, world):
         ctx.encode(v, GELU_SCALE, top, pt)
         ct = ctx.encrypt_symmetric(sk, pt, top, 900 + i)
         vals.append(v)
-        cts.append(Ciphertext.from_device(ctx, ct, GELU_SCALE))
+        cts.append(ct)
         host.append(ct.cpu().numpy().view(np.uint64).copy())
     stream = torch.cuda.current_stream(dev)
 
     def step():
-        return [ev.gelu(c) for c in cts]
+        # GeLUEvaluator::gelu mod-switches its input in place (src/gelu.cpp), so
+        # every step starts from fresh device copies of the inputs
+        return [ev.gelu(Ciphertext.from_device(ctx, c, GELU_SCALE)) for c in cts]
 
     for _ in range(args.warmup):
         res = step()
