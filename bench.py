@@ -784,9 +784,15 @@ def run_gelu_gpu(args, rank, world):
         host.append(ct.cpu().numpy().view(np.uint64).copy())
     stream = torch.cuda.current_stream(dev)
 
+    in_cts = [Ciphertext.from_device(ctx, c, GELU_SCALE) for c in cts]
+
     def step():
+        # the lockstep form (inputs are left unchanged)
+        return ev.gelu_batch(in_cts)
+
+    def plain_step():
         # GeLUEvaluator::gelu mod-switches its input in place (src/gelu.cpp), so
-        # every step starts from fresh device copies of the inputs
+        # each call gets a fresh device copy
         return [ev.gelu(Ciphertext.from_device(ctx, c, GELU_SCALE)) for c in cts]
 
     for _ in range(args.warmup):
@@ -833,13 +839,28 @@ def run_gelu_gpu(args, rank, world):
     barrier(world)
     w0 = time.perf_counter()
     out_bytes = 0
+    loaded = []
     for h in h_in:
         c = Ciphertext(ctx)
         ng.check(ng.lib().nexus_ciphertext_load(c.handle, h.data_ptr(), 2, top, GELU_SCALE, 1, None), "load")
-        out_bytes += ev.gelu(c).to_numpy().nbytes
+        loaded.append(c)
+    for r in ev.gelu_batch(loaded):
+        out_bytes += r.to_numpy().nbytes
     torch.cuda.synchronize(dev)
     e2e_s = max_over_ranks(time.perf_counter() - w0, world)
     in_bytes = sum(h.nbytes for h in host)
+
+    plain_step()
+    torch.cuda.synchronize(dev)
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    res = plain_step()
+    p1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_ms = p0.elapsed_time(p1)
+    same = all(np.array_equal(a.to_numpy(), b.to_numpy()) for a, b in zip(res[:2], ev.gelu_batch(in_cts[:2])))
+    del res
 
     value = world * args.steps * GELU_CTS / (total_ms / 1e3)
     peak, peak_kind = _peak_hbm()
@@ -862,6 +883,8 @@ def run_gelu_gpu(args, rank, world):
         },
         "e2e": {"value": world * GELU_CTS / e2e_s, "unit": "GELU/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes},
+        "plain_single_ct_form": {"value": world * GELU_CTS / (plain_ms / 1e3), "unit": "GELU/s",
+                                 "batched_words_equal_single": bool(same)},
         "clocks": clk.summary(),
         "gpu_launches": launches,
     }

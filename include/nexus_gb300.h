@@ -319,6 +319,20 @@ int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext *x, int a1
 int nexus_encode_coefficients(nexus_context *ctx, const double *values, size_t n, double scale, int limbs,
                               uint64_t *d_out, void *stream);
 
+/* The operators above on `count` ciphertexts in lockstep (one size, level
+ * and scale): every step runs once over the whole batch, every key is read
+ * once per batch, and res[b] receives the words the single form gives for
+ * cts[b].  The inputs are left unchanged (the single forms of gelu, softmax
+ * and layer_norm mod-switch or update their input in place, as NEXUS's do).
+ * No counterpart in the reference. */
+int nexus_gelu_batch(nexus_evaluator *ev, nexus_ciphertext *const *cts, int count, nexus_ciphertext *const *res);
+int nexus_softmax_batch(nexus_evaluator *ev, nexus_ciphertext *const *cts, int count, int len,
+                        nexus_ciphertext *const *res);
+int nexus_layer_norm_batch(nexus_evaluator *ev, nexus_ciphertext *const *cts, int count, int len,
+                           nexus_ciphertext *const *res);
+int nexus_ckks_op_batch(nexus_evaluator *ev, int op, nexus_ciphertext *const *cts, int count, int a1, int a2,
+                        double f, nexus_ciphertext *const *res);
+
 /* MMEvaluator::multiply_power_of_x (src/matrix_mul.cpp:131-172): res = x * X^index. */
 int nexus_mm_power_of_x(nexus_evaluator *ev, nexus_ciphertext *x, int index, nexus_ciphertext *res);
 

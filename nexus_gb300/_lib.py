@@ -65,6 +65,11 @@ SIGNATURES = [
     ("nexus_ckks_op", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_void_p]),
     ("nexus_encode_coefficients", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_size_t, C.c_double, C.c_int, C.c_void_p, C.c_void_p]),
+    ("nexus_gelu_batch", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("nexus_softmax_batch", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    ("nexus_layer_norm_batch", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    ("nexus_ckks_op_batch", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                      C.c_void_p]),
     ("nexus_mm_power_of_x", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("nexus_mm_expand", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     ("nexus_matrix_mul", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_int, C.c_int,

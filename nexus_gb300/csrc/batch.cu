@@ -162,17 +162,40 @@ void BatchEvaluator::sub(const CtBatch &a, const CtBatch &b, CtBatch &dest)
     sub_inplace(dest, bb);
 }
 
-void BatchEvaluator::add_plain_inplace(CtBatch &ct, const Plaintext &pt)
+void BatchEvaluator::plain_arith(CtBatch &ct, const Plaintext &pt, bool sub)
 {
     if (ct.limbs() != pt.limbs()) throw std::invalid_argument("encrypted and plain parameter mismatch");
     if (!are_close(ct.scale(), pt.scale())) throw std::invalid_argument("scale mismatch");
     if (pt.is_scalar()) {
-        poly_add_scalar(c_, ct.data(), ct.limbs(), pt.residues().data(), 0, ct.data(), stream(), ct.batch(),
+        poly_add_scalar(c_, ct.data(), ct.limbs(), pt.residues().data(), sub ? 1 : 0, ct.data(), stream(), ct.batch(),
                         ct.words_per_ct());
     } else {
         for (int b = 0; b < ct.batch(); ++b)
-            poly_add_plain(c_, ct.ct(b), 1, ct.limbs(), pt.data(), 0, ct.ct(b), stream());
+            poly_add_plain(c_, ct.ct(b), 1, ct.limbs(), pt.data(), sub ? 1 : 0, ct.ct(b), stream());
     }
+}
+
+void BatchEvaluator::add_plain(const CtBatch &ct, const Plaintext &pt, CtBatch &dest)
+{
+    if (&ct != &dest) dest = ct;
+    add_plain_inplace(dest, pt);
+}
+
+void BatchEvaluator::sub_plain(const CtBatch &ct, const Plaintext &pt, CtBatch &dest)
+{
+    if (&ct != &dest) dest = ct;
+    sub_plain_inplace(dest, pt);
+}
+
+void BatchEvaluator::negate_inplace(CtBatch &ct)
+{
+    poly_negate(c_, ct.data(), ct.size() * ct.batch(), ct.limbs(), ct.data(), stream());
+}
+
+void BatchEvaluator::negate(const CtBatch &ct, CtBatch &dest)
+{
+    if (&ct != &dest) dest = ct;
+    negate_inplace(dest);
 }
 
 void BatchEvaluator::multiply_plain_inplace(CtBatch &ct, const Plaintext &pt)

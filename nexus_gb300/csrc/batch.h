@@ -65,10 +65,17 @@ public:
     {
         ev_.encode_then_drop(v, limbs, scale, out);
     }
+    void encode(const std::vector<double> &v, int limbs, double scale, Plaintext &out)
+    {
+        ev_.encode(v, limbs, scale, out);
+    }
+    void encode(double value, int limbs, double scale, Plaintext &out) { ev_.encode(value, limbs, scale, out); }
+    void encode(double value, double scale, Plaintext &out) { ev_.encode(value, scale, out); }
     void mod_switch_to_inplace(Plaintext &pt, int limbs) { ev_.mod_switch_to_inplace(pt, limbs); }
 
     // level management
     void mod_switch_to_inplace(CtBatch &ct, int limbs);
+    void mod_switch_to_next_inplace(CtBatch &ct) { mod_switch_to_inplace(ct, ct.limbs() - 1); }
     void rescale_to_next_inplace(CtBatch &ct);
 
     // arithmetic
@@ -82,7 +89,12 @@ public:
     void sub_inplace(CtBatch &a, const CtBatch &b);
     void sub(const CtBatch &a, const CtBatch &b, CtBatch &dest);
     void double_inplace(CtBatch &ct) { add_inplace(ct, ct); }
-    void add_plain_inplace(CtBatch &ct, const Plaintext &pt);
+    void negate_inplace(CtBatch &ct);
+    void negate(const CtBatch &ct, CtBatch &dest);
+    void add_plain_inplace(CtBatch &ct, const Plaintext &pt) { plain_arith(ct, pt, false); }
+    void sub_plain_inplace(CtBatch &ct, const Plaintext &pt) { plain_arith(ct, pt, true); }
+    void add_plain(const CtBatch &ct, const Plaintext &pt, CtBatch &dest);
+    void sub_plain(const CtBatch &ct, const Plaintext &pt, CtBatch &dest);
     void multiply_plain_inplace(CtBatch &ct, const Plaintext &pt);
     void multiply_plain(const CtBatch &ct, const Plaintext &pt, CtBatch &dest);
     void multiply_plain_accumulate(const std::vector<const CtBatch *> &cts, const std::vector<const Plaintext *> &pts,
@@ -108,6 +120,7 @@ public:
     void complex_conjugate_inplace(CtBatch &ct) { apply_galois_inplace(ct, ev_.galois_elt(0)); }
 
 private:
+    void plain_arith(CtBatch &ct, const Plaintext &pt, bool sub);
     void apply_galois(const CtBatch &ct, uint32_t elt, const uint64_t *key, CtBatch &out);
     CtBatch adjust_down(const CtBatch &hi, const CtBatch &lo);
     Evaluator &ev_;

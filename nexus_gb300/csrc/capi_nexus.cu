@@ -5,6 +5,7 @@
 #include <string>
 
 #include "../../include/nexus_gb300.h"
+#include "batch.h"
 #include "capi_types.h"
 
 using namespace nexus;
@@ -161,6 +162,129 @@ extern "C" int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext
         case NEXUS_OP_INVERT_SQRT: res->ct = ev->ck.invert_sqrt(x->ct, a1, a2); break;
         default: throw std::invalid_argument("unknown op");
         }
+    });
+}
+
+// ------------------------------------------------------------ lockstep forms
+
+namespace {
+
+using BatchCKKS = CKKSEvaluatorT<BatchEvaluator, CtBatch>;
+
+// gather `count` ciphertexts of one size, level and scale into a batch
+CtBatch gather(nexus_evaluator *ev, nexus_ciphertext *const *cts, int count)
+{
+    const Ciphertext &first = cts[0]->ct;
+    if (first.empty()) throw std::invalid_argument("empty ciphertext");
+    for (int b = 1; b < count; ++b) {
+        const Ciphertext &c = cts[b]->ct;
+        if (c.size() != first.size() || c.limbs() != first.limbs())
+            throw std::invalid_argument("the ciphertexts of a batch must share one size and level");
+        if (c.scale() != first.scale()) throw std::invalid_argument("the ciphertexts of a batch must share one scale");
+    }
+    Context &ctx = ev->ctx->c;
+    cudaStream_t s = ev->ev.stream();
+    CtBatch in;
+    in.resize(ctx, count, first.size(), first.limbs(), s);
+    in.scale() = first.scale();
+    for (int b = 0; b < count; ++b)
+        if (cudaMemcpyAsync(in.ct(b), cts[b]->ct.data(), in.words_per_ct() * 8, cudaMemcpyDeviceToDevice, s) !=
+            cudaSuccess)
+            throw std::runtime_error("copy failed");
+    return in;
+}
+
+void scatter(nexus_evaluator *ev, const CtBatch &out, nexus_ciphertext *const *res)
+{
+    Context &ctx = ev->ctx->c;
+    cudaStream_t s = ev->ev.stream();
+    for (int b = 0; b < out.batch(); ++b) {
+        Ciphertext &r = res[b]->ct;
+        r.resize(ctx, out.size(), out.limbs(), s);
+        r.scale() = out.scale();
+        if (cudaMemcpyAsync(r.data(), out.ct(b), out.words_per_ct() * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            throw std::runtime_error("copy failed");
+    }
+}
+
+int check_batch(const char *fn, nexus_evaluator *ev, nexus_ciphertext *const *cts, int count,
+                nexus_ciphertext *const *res)
+{
+    if (!ev || !cts || !res || count < 1) return fail(fn, "null argument");
+    for (int b = 0; b < count; ++b) {
+        if (!cts[b] || !res[b]) return fail(fn, "null ciphertext");
+        for (int j = 0; j < count; ++j)
+            if (res[b] == cts[j]) return fail(fn, "results must not alias inputs");
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int nexus_gelu_batch(nexus_evaluator *ev, nexus_ciphertext *const *cts, int count,
+                                nexus_ciphertext *const *res)
+{
+    static const char *fn = "nexus_gelu_batch";
+    if (check_batch(fn, ev, cts, count, res)) return -1;
+    return guarded(fn, [&] {
+        BatchEvaluator bev(ev->ev);
+        BatchCKKS ck(bev, ev->ck.scale);
+        GeLUEvaluatorT<BatchEvaluator, CtBatch> g(ck);
+        CtBatch x = gather(ev, cts, count), out;
+        g.gelu(x, out);
+        scatter(ev, out, res);
+    });
+}
+
+extern "C" int nexus_softmax_batch(nexus_evaluator *ev, nexus_ciphertext *const *cts, int count, int len,
+                                   nexus_ciphertext *const *res)
+{
+    static const char *fn = "nexus_softmax_batch";
+    if (check_batch(fn, ev, cts, count, res)) return -1;
+    if (len < 1 || (len & (len - 1))) return fail(fn, "len must be a power of two");
+    return guarded(fn, [&] {
+        BatchEvaluator bev(ev->ev);
+        BatchCKKS ck(bev, ev->ck.scale);
+        SoftmaxEvaluatorT<BatchEvaluator, CtBatch> sm(ck);
+        CtBatch x = gather(ev, cts, count), out;
+        sm.softmax(x, out, len);
+        scatter(ev, out, res);
+    });
+}
+
+extern "C" int nexus_layer_norm_batch(nexus_evaluator *ev, nexus_ciphertext *const *cts, int count, int len,
+                                      nexus_ciphertext *const *res)
+{
+    static const char *fn = "nexus_layer_norm_batch";
+    if (check_batch(fn, ev, cts, count, res)) return -1;
+    if (len < 1 || (len & (len - 1))) return fail(fn, "len must be a power of two");
+    return guarded(fn, [&] {
+        BatchEvaluator bev(ev->ev);
+        BatchCKKS ck(bev, ev->ck.scale);
+        LNEvaluatorT<BatchEvaluator, CtBatch> ln(ck);
+        CtBatch x = gather(ev, cts, count), out;
+        ln.layer_norm(x, out, len);
+        scatter(ev, out, res);
+    });
+}
+
+extern "C" int nexus_ckks_op_batch(nexus_evaluator *ev, int op, nexus_ciphertext *const *cts, int count, int a1,
+                                   int a2, double f, nexus_ciphertext *const *res)
+{
+    static const char *fn = "nexus_ckks_op_batch";
+    if (check_batch(fn, ev, cts, count, res)) return -1;
+    return guarded(fn, [&] {
+        BatchEvaluator bev(ev->ev);
+        BatchCKKS ck(bev, ev->ck.scale);
+        CtBatch x = gather(ev, cts, count), out;
+        switch (op) {
+        case NEXUS_OP_SGN_EVAL: out = ck.sgn_eval(x, a1, a2, f); break;
+        case NEXUS_OP_EXP: out = ck.exp(x); break;
+        case NEXUS_OP_INVERSE: out = ck.inverse(x, a1); break;
+        case NEXUS_OP_INVERT_SQRT: out = ck.invert_sqrt(x, a1, a2); break;
+        default: throw std::invalid_argument("unknown op");
+        }
+        scatter(ev, out, res);
     });
 }
 

@@ -7,14 +7,16 @@
 
 namespace nexus {
 
-CKKSEvaluator::CKKSEvaluator(Evaluator &ev, double scale_) : evaluator(&ev), scale(scale_)
+template <class EV, class CT>
+CKKSEvaluatorT<EV, CT>::CKKSEvaluatorT(EV &ev, double scale_) : evaluator(&ev), scale(scale_)
 {
     slot_count = ev.slot_count();
     degree = slot_count * 2;
 }
 
 // get_modulus (src/ckks_evaluator.cpp:511-515): q[limbs - k] of x's level
-uint64_t CKKSEvaluator::get_modulus(const Ciphertext &x, int k) const
+template <class EV, class CT>
+uint64_t CKKSEvaluatorT<EV, CT>::get_modulus(const CT &x, int k) const
 {
     const int idx = x.limbs() - k;
     if (idx < 0) throw std::invalid_argument("level too low for the degree-9 evaluation");
@@ -23,7 +25,8 @@ uint64_t CKKSEvaluator::get_modulus(const Ciphertext &x, int k) const
 
 // sgn_eval (src/ckks_evaluator.cpp:181-212): g-polynomials then f-polynomials,
 // the last of each scaled by sgn_factor
-Ciphertext CKKSEvaluator::sgn_eval(Ciphertext x, int d_g, int d_f, double sgn_factor)
+template <class EV, class CT>
+CT CKKSEvaluatorT<EV, CT>::sgn_eval(CT x, int d_g, int d_f, double sgn_factor)
 {
     std::vector<double> f4 = F4_COEFFS, g4 = G4_COEFFS, f4_last(10), g4_last(10);
     for (int i = 0; i <= 9; ++i) {
@@ -32,7 +35,7 @@ Ciphertext CKKSEvaluator::sgn_eval(Ciphertext x, int d_g, int d_f, double sgn_fa
         g4[i] /= g4_scale;
         g4_last[i] = g4[i] * sgn_factor;
     }
-    Ciphertext dest = x;
+    CT dest = x;
     for (int i = 0; i < d_g; ++i) eval_odd_deg9_poly(i == d_g - 1 ? g4_last : g4, dest, dest);
     for (int i = 0; i < d_f; ++i) eval_odd_deg9_poly(i == d_f - 1 ? f4_last : f4, dest, dest);
     return dest;
@@ -41,14 +44,15 @@ Ciphertext CKKSEvaluator::sgn_eval(Ciphertext x, int d_g, int d_f, double sgn_fa
 // eval_odd_deg9_poly (src/ckks_evaluator.cpp:214-364): P = T1 + T2 + T3 with
 // T1 = (a3 + a5 x^2) x^3, T2 = (a7 x + a9 x^3) x^6, T3 = a1 x, each
 // coefficient encoded at the scale that makes the three terms meet.
-void CKKSEvaluator::eval_odd_deg9_poly(const std::vector<double> &a, Ciphertext &x_in, Ciphertext &dest)
+template <class EV, class CT>
+void CKKSEvaluatorT<EV, CT>::eval_odd_deg9_poly(const std::vector<double> &a, CT &x_in, CT &dest)
 {
-    Evaluator &ev = *evaluator;
-    Ciphertext x = x_in;
+    EV &ev = *evaluator;
+    CT x = x_in;
     const double D = x.scale();
     const uint64_t p = get_modulus(x, 2), q = get_modulus(x, 3), r = get_modulus(x, 4);
 
-    Ciphertext x2, x3, x6;
+    CT x2, x3, x6;
     ev.square(x, x2);
     ev.relinearize_inplace(x2);
     ev.rescale_to_next_inplace(x2);
@@ -61,7 +65,7 @@ void CKKSEvaluator::eval_odd_deg9_poly(const std::vector<double> &a, Ciphertext 
     ev.rescale_to_next_inplace(x6);
 
     Plaintext a1, a3, a5, a7, a9;
-    Ciphertext T1;
+    CT T1;
     const double a5_scale = D / x2.scale() * (double)p / x3.scale() * (double)q;
     ev.encode(a[5], x2.limbs(), a5_scale, a5);
     ev.multiply_plain(x2, a5, T1);
@@ -72,7 +76,7 @@ void CKKSEvaluator::eval_odd_deg9_poly(const std::vector<double> &a, Ciphertext 
     ev.relinearize_inplace(T1);
     ev.rescale_to_next_inplace(T1);
 
-    Ciphertext T2, a7x;
+    CT T2, a7x;
     const double a9_scale = D / x3.scale() * (double)r / x6.scale() * (double)q;
     ev.encode(a[9], x3.limbs(), a9_scale, a9);
     ev.multiply_plain(x3, a9, T2);
@@ -89,7 +93,7 @@ void CKKSEvaluator::eval_odd_deg9_poly(const std::vector<double> &a, Ciphertext 
     ev.relinearize_inplace(T2);
     ev.rescale_to_next_inplace(T2);
 
-    Ciphertext T3;
+    CT T3;
     ev.encode(a[1], x.limbs(), (double)p, a1);
     ev.multiply_plain(x, a1, T3);
     ev.rescale_to_next_inplace(T3);
@@ -104,14 +108,15 @@ void CKKSEvaluator::eval_odd_deg9_poly(const std::vector<double> &a, Ciphertext 
 }
 
 // newtonIter (src/ckks_evaluator.cpp:366-422): res <- 1.5 res - 0.5 x res^3
-Ciphertext CKKSEvaluator::newtonIter(Ciphertext x, Ciphertext res, int iter)
+template <class EV, class CT>
+CT CKKSEvaluatorT<EV, CT>::newtonIter(CT x, CT res, int iter)
 {
-    Evaluator &ev = *evaluator;
+    EV &ev = *evaluator;
     for (int i = 0; i < iter; ++i) {
         Plaintext three_half, neg_half;
         ev.encode(1.5, scale, three_half);
         ev.encode(-0.5, scale, neg_half);
-        Ciphertext res_sq, res_x;
+        CT res_sq, res_x;
         ev.square(res, res_sq);
         ev.relinearize_inplace(res_sq);
         ev.rescale_to_next_inplace(res_sq);
@@ -141,10 +146,11 @@ Ciphertext CKKSEvaluator::newtonIter(Ciphertext x, Ciphertext res, int iter)
 }
 
 // goldSchmidtIter (src/ckks_evaluator.cpp:424-478)
-std::pair<Ciphertext, Ciphertext> CKKSEvaluator::goldSchmidtIter(Ciphertext v, Ciphertext y, int d)
+template <class EV, class CT>
+std::pair<CT, CT> CKKSEvaluatorT<EV, CT>::goldSchmidtIter(CT v, CT y, int d)
 {
-    Evaluator &ev = *evaluator;
-    Ciphertext x, h, r, temp;
+    EV &ev = *evaluator;
+    CT x, h, r, temp;
     Plaintext constant;
     ev.encode(0.5, scale, constant);
     ev.mod_switch_to_inplace(v, y.limbs());
@@ -188,18 +194,20 @@ std::pair<Ciphertext, Ciphertext> CKKSEvaluator::goldSchmidtIter(Ciphertext v, C
 }
 
 // invert_sqrt (src/ckks_evaluator.cpp:480-485): line guess, Newton, Goldschmidt
-Ciphertext CKKSEvaluator::invert_sqrt(Ciphertext x, int d_newt, int d_gold)
+template <class EV, class CT>
+CT CKKSEvaluatorT<EV, CT>::invert_sqrt(CT x, int d_newt, int d_gold)
 {
-    Ciphertext res = initGuess(x);
-    Ciphertext y = newtonIter(x, res, d_newt);
+    CT res = initGuess(x);
+    CT y = newtonIter(x, res, d_newt);
     return goldSchmidtIter(x, y, d_gold).second;
 }
 
 // inverse (src/ckks_evaluator.cpp:487-509): prod_i (1 + (1-x)^(2^i))
-Ciphertext CKKSEvaluator::inverse(Ciphertext x, int iter)
+template <class EV, class CT>
+CT CKKSEvaluatorT<EV, CT>::inverse(CT x, int iter)
 {
-    Evaluator &ev = *evaluator;
-    Ciphertext y, tmp, res;
+    EV &ev = *evaluator;
+    CT y, tmp, res;
     Plaintext one;
     ev.encode(1.0, x.limbs(), x.scale(), one);
     ev.sub_plain(x, one, y);
@@ -221,7 +229,8 @@ Ciphertext CKKSEvaluator::inverse(Ciphertext x, int iter)
 }
 
 // initGuess / evalLine (src/ckks_evaluator.cpp:517-532)
-Ciphertext CKKSEvaluator::initGuess(Ciphertext x)
+template <class EV, class CT>
+CT CKKSEvaluatorT<EV, CT>::initGuess(CT x)
 {
     Plaintext A, B;
     evaluator->encode(-1.29054537e-04, scale, A);
@@ -229,9 +238,10 @@ Ciphertext CKKSEvaluator::initGuess(Ciphertext x)
     return evalLine(x, A, B);
 }
 
-Ciphertext CKKSEvaluator::evalLine(Ciphertext x, Plaintext m, Plaintext c)
+template <class EV, class CT>
+CT CKKSEvaluatorT<EV, CT>::evalLine(CT x, Plaintext m, Plaintext c)
 {
-    Evaluator &ev = *evaluator;
+    EV &ev = *evaluator;
     ev.mod_switch_to_inplace(m, x.limbs());
     ev.multiply_plain_inplace(x, m);
     ev.rescale_to_next_inplace(x);
@@ -242,9 +252,10 @@ Ciphertext CKKSEvaluator::evalLine(Ciphertext x, Plaintext m, Plaintext c)
 }
 
 // exp (src/ckks_evaluator.cpp:534-548): (1 + x/128)^128
-Ciphertext CKKSEvaluator::exp(Ciphertext x)
+template <class EV, class CT>
+CT CKKSEvaluatorT<EV, CT>::exp(CT x)
 {
-    Evaluator &ev = *evaluator;
+    EV &ev = *evaluator;
     Plaintext one, inverse_128;
     ev.encode(0.0078125, x.limbs(), x.scale(), inverse_128);
     ev.multiply_plain_inplace(x, inverse_128);
@@ -260,11 +271,12 @@ Ciphertext CKKSEvaluator::exp(Ciphertext x)
 }
 
 // GeLUEvaluator::gelu (src/gelu.cpp:5-111); like the original, x is mod-switched in place
-void GeLUEvaluator::gelu(Ciphertext &x, Ciphertext &res)
+template <class EV, class CT>
+void GeLUEvaluatorT<EV, CT>::gelu(CT &x, CT &res)
 {
-    Evaluator &ev = *ckks->evaluator;
+    EV &ev = *ckks->evaluator;
     const size_t sc = ckks->slot_count;
-    Ciphertext b0, b1;
+    CT b0, b1;
     Plaintext p0, p1, delta;
     ev.encode(ckks->init_vec_with_value(sc, -3.5), x.limbs(), x.scale(), p0);
     ev.encode(ckks->init_vec_with_value(sc, 3.5), x.limbs(), x.scale(), p1);
@@ -280,11 +292,11 @@ void GeLUEvaluator::gelu(Ciphertext &x, Ciphertext &res)
 
     Plaintext zero_point_five;
     ev.encode(ckks->init_vec_with_value(sc, 0.5), b1.limbs(), b1.scale(), zero_point_five);
-    Ciphertext a1, a2;
+    CT a1, a2;
     ev.sub(b0, b1, a1);
     ev.add_plain(b1, zero_point_five, a2);
 
-    Ciphertext x_2, x_4, x_6, x_8, x_10, x_12;
+    CT x_2, x_4, x_6, x_8, x_10, x_12;
     ev.square(x, x_2);
     ev.relinearize_inplace(x_2);
     ev.rescale_to_next_inplace(x_2);
@@ -310,7 +322,7 @@ void GeLUEvaluator::gelu(Ciphertext &x, Ciphertext &res)
                         3.49617829e-05, -7.26059653e-07};
     std::vector<Plaintext> coeff_A(8);
     for (size_t i = 0; i < 8; ++i) ev.encode(A[i], ckks->scale, coeff_A[i]);
-    std::vector<Ciphertext> cts(8);
+    std::vector<CT> cts(8);
     cts[1] = x;
     cts[2] = x_2;
     cts[3] = x_4;
@@ -324,7 +336,7 @@ void GeLUEvaluator::gelu(Ciphertext &x, Ciphertext &res)
         ev.rescale_to_next_inplace(cts[i]);
         cts[i].scale() = ckks->scale;
     }
-    Ciphertext Ax = cts[7];
+    CT Ax = cts[7];
     for (size_t i = 1; i < 7; ++i) {
         ev.mod_switch_to_inplace(cts[i], Ax.limbs());
         ev.add_inplace(Ax, cts[i]);
@@ -332,7 +344,7 @@ void GeLUEvaluator::gelu(Ciphertext &x, Ciphertext &res)
     ev.mod_switch_to_inplace(coeff_A[0], Ax.limbs());
     ev.add_plain_inplace(Ax, coeff_A[0]);
 
-    Ciphertext s1, s2;
+    CT s1, s2;
     ev.mod_switch_to_inplace(Ax, a1.limbs());
     ev.multiply(Ax, a1, s1);
     ev.relinearize_inplace(s1);
@@ -348,10 +360,11 @@ void GeLUEvaluator::gelu(Ciphertext &x, Ciphertext &res)
 }
 
 // SoftmaxEvaluator::softmax (src/softmax.cpp:6-42); x is updated in place as in the original
-void SoftmaxEvaluator::softmax(Ciphertext &x, Ciphertext &res, int len)
+template <class EV, class CT>
+void SoftmaxEvaluatorT<EV, CT>::softmax(CT &x, CT &res, int len)
 {
-    Evaluator &ev = *ckks->evaluator;
-    Ciphertext tmp, exp_x;
+    EV &ev = *ckks->evaluator;
+    CT tmp, exp_x;
     const int log_step = (int)std::log2(len);
     ev.rotate_vector(x, -len, tmp);
     ev.add_inplace(x, tmp);
@@ -377,10 +390,11 @@ void SoftmaxEvaluator::softmax(Ciphertext &x, Ciphertext &res, int len)
 }
 
 // LNEvaluator::layer_norm (src/layer_norm.cpp:6-33); x is updated in place as in the original
-void LNEvaluator::layer_norm(Ciphertext &x, Ciphertext &res, int len)
+template <class EV, class CT>
+void LNEvaluatorT<EV, CT>::layer_norm(CT &x, CT &res, int len)
 {
-    Evaluator &ev = *ckks->evaluator;
-    Ciphertext tmp, x2;
+    EV &ev = *ckks->evaluator;
+    CT tmp, x2;
     const int log_step = (int)std::log2(len);
     ev.rotate_vector(x, -len, tmp);
     ev.add_inplace(x, tmp);
@@ -403,5 +417,14 @@ void LNEvaluator::layer_norm(Ciphertext &x, Ciphertext &res, int len)
     ev.relinearize_inplace(res);
     ev.rescale_to_next_inplace(res);
 }
+
+template class CKKSEvaluatorT<Evaluator, Ciphertext>;
+template class CKKSEvaluatorT<BatchEvaluator, CtBatch>;
+template class GeLUEvaluatorT<Evaluator, Ciphertext>;
+template class GeLUEvaluatorT<BatchEvaluator, CtBatch>;
+template class SoftmaxEvaluatorT<Evaluator, Ciphertext>;
+template class SoftmaxEvaluatorT<BatchEvaluator, CtBatch>;
+template class LNEvaluatorT<Evaluator, Ciphertext>;
+template class LNEvaluatorT<BatchEvaluator, CtBatch>;
 
 }  // namespace nexus

@@ -7,11 +7,16 @@
 #include <utility>
 #include <vector>
 
+#include "batch.h"
 #include "ckks.h"
 
 namespace nexus {
 
-class CKKSEvaluator {
+// EV / CT: Evaluator / Ciphertext, or BatchEvaluator / CtBatch to run the
+// same operator on several ciphertexts in lockstep (one launch per step for
+// the whole batch); the call sequence is NEXUS's in both cases.
+template <class EV, class CT>
+class CKKSEvaluatorT {
 public:
     // constants of src/ckks_evaluator.h:14-27
     std::vector<double> F4_COEFFS = {0, 315, 0, -420, 0, 378, 0, -180, 0, 35};
@@ -19,55 +24,63 @@ public:
     std::vector<double> G4_COEFFS = {0, 5850, 0, -34974, 0, 97015, 0, -113492, 0, 46623};
     int g4_scale = (1 << 10);
 
-    Evaluator *evaluator;
+    EV *evaluator;
     double scale;
     size_t slot_count;
     size_t degree;
 
-    CKKSEvaluator(Evaluator &ev, double scale);
+    CKKSEvaluatorT(EV &ev, double scale);
 
     std::vector<double> init_vec_with_value(size_t n, double value) const { return std::vector<double>(n, value); }
-    uint64_t get_modulus(const Ciphertext &x, int k) const;
-    void eval_odd_deg9_poly(const std::vector<double> &a, Ciphertext &x, Ciphertext &dest);
+    uint64_t get_modulus(const CT &x, int k) const;
+    void eval_odd_deg9_poly(const std::vector<double> &a, CT &x, CT &dest);
 
-    Ciphertext sgn_eval(Ciphertext x, int d_g, int d_f, double sgn_factor = 0.5);
-    Ciphertext invert_sqrt(Ciphertext x, int d_newt = 5, int d_gold = 2);
-    Ciphertext exp(Ciphertext x);
-    Ciphertext inverse(Ciphertext x, int iter = 4);
+    CT sgn_eval(CT x, int d_g, int d_f, double sgn_factor = 0.5);
+    CT invert_sqrt(CT x, int d_newt = 5, int d_gold = 2);
+    CT exp(CT x);
+    CT inverse(CT x, int iter = 4);
 
-    Ciphertext newtonIter(Ciphertext x, Ciphertext res, int iter = 4);
-    std::pair<Ciphertext, Ciphertext> goldSchmidtIter(Ciphertext v, Ciphertext y, int d = 1);
-    Ciphertext initGuess(Ciphertext x);
-    Ciphertext evalLine(Ciphertext x, Plaintext m, Plaintext c);
+    CT newtonIter(CT x, CT res, int iter = 4);
+    std::pair<CT, CT> goldSchmidtIter(CT v, CT y, int d = 1);
+    CT initGuess(CT x);
+    CT evalLine(CT x, Plaintext m, Plaintext c);
 };
 
-class GeLUEvaluator {
+template <class EV, class CT>
+class GeLUEvaluatorT {
 public:
-    explicit GeLUEvaluator(CKKSEvaluator &ckks) : ckks(&ckks) {}
-    void gelu(Ciphertext &x, Ciphertext &res);
+    explicit GeLUEvaluatorT(CKKSEvaluatorT<EV, CT> &ckks) : ckks(&ckks) {}
+    void gelu(CT &x, CT &res);
 
 private:
-    CKKSEvaluator *ckks;
+    CKKSEvaluatorT<EV, CT> *ckks;
 };
+
+template <class EV, class CT>
+class SoftmaxEvaluatorT {
+public:
+    explicit SoftmaxEvaluatorT(CKKSEvaluatorT<EV, CT> &ckks) : ckks(&ckks) {}
+    void softmax(CT &x, CT &res, int len);
+
+private:
+    CKKSEvaluatorT<EV, CT> *ckks;
+};
+
+template <class EV, class CT>
+class LNEvaluatorT {
+public:
+    explicit LNEvaluatorT(CKKSEvaluatorT<EV, CT> &ckks) : ckks(&ckks) {}
+    void layer_norm(CT &x, CT &res, int len);
+
+private:
+    CKKSEvaluatorT<EV, CT> *ckks;
+};
+
+using CKKSEvaluator = CKKSEvaluatorT<Evaluator, Ciphertext>;
+using GeLUEvaluator = GeLUEvaluatorT<Evaluator, Ciphertext>;
 using GELUEvaluator = GeLUEvaluator;  // name of the CUDA build (cuda/src/gelu.cuh)
-
-class SoftmaxEvaluator {
-public:
-    explicit SoftmaxEvaluator(CKKSEvaluator &ckks) : ckks(&ckks) {}
-    void softmax(Ciphertext &x, Ciphertext &res, int len);
-
-private:
-    CKKSEvaluator *ckks;
-};
-
-class LNEvaluator {
-public:
-    explicit LNEvaluator(CKKSEvaluator &ckks) : ckks(&ckks) {}
-    void layer_norm(Ciphertext &x, Ciphertext &res, int len);
-
-private:
-    CKKSEvaluator *ckks;
-};
+using SoftmaxEvaluator = SoftmaxEvaluatorT<Evaluator, Ciphertext>;
+using LNEvaluator = LNEvaluatorT<Evaluator, Ciphertext>;
 
 // MMEvaluator (src/matrix_mul.{h,cpp}): ct x pt MatMul through the ciphertext
 // expansion tree; see matmul.cu for the GPU form.

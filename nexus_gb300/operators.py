@@ -126,6 +126,31 @@ class Evaluator:
     def invert_sqrt(self, x, d_newt=5, d_gold=2):
         return self._op(OP_INVERT_SQRT, x, d_newt, d_gold)
 
+    # ---- lockstep forms: one launch per step for the whole list ------------------
+    def _batch(self, fn, name, cts, *args):
+        res = [Ciphertext(self.ctx) for _ in cts]
+        a = (C.c_void_p * len(cts))(*[c.handle.value for c in cts])
+        r = (C.c_void_p * len(res))(*[x.handle.value for x in res])
+        check(fn(self._h, a, len(cts), *args, r), name)
+        return res
+
+    def gelu_batch(self, cts):
+        return self._batch(lib().nexus_gelu_batch, "nexus_gelu_batch", cts)
+
+    def softmax_batch(self, cts, length: int):
+        return self._batch(lib().nexus_softmax_batch, "nexus_softmax_batch", cts, int(length))
+
+    def layer_norm_batch(self, cts, length: int):
+        return self._batch(lib().nexus_layer_norm_batch, "nexus_layer_norm_batch", cts, int(length))
+
+    def ckks_op_batch(self, op: int, cts, a1=0, a2=0, f=0.0):
+        res = [Ciphertext(self.ctx) for _ in cts]
+        a = (C.c_void_p * len(cts))(*[c.handle.value for c in cts])
+        r = (C.c_void_p * len(res))(*[x.handle.value for x in res])
+        check(lib().nexus_ckks_op_batch(self._h, int(op), a, len(cts), int(a1), int(a2), float(f), r),
+              "nexus_ckks_op_batch")
+        return res
+
     # ---- MatMul (src/matrix_mul.cpp) ------------------------------------------
     def mm_power_of_x(self, x: Ciphertext, index: int) -> Ciphertext:
         res = Ciphertext(self.ctx)

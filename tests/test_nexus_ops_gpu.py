@@ -113,3 +113,31 @@ def test_errors_match_seal_conditions(env):
     x = Ciphertext.from_device(ctx, ct, SCALE)
     with pytest.raises(NexusError, match="scale out of bounds|end of modulus|level too low"):
         ev.gelu(x)
+
+
+def test_lockstep_operators_equal_single(env):
+    """gelu / softmax / layer_norm / sgn / exp / inverse / invert_sqrt on three
+    ciphertexts in lockstep give each ciphertext the single form's words."""
+    from nexus_gb300.operators import OP_EXP, OP_INVERSE, OP_INVERT_SQRT, OP_SGN_EVAL
+    ctx, sk, ev, ock = env
+    rng = np.random.default_rng(40)
+
+    def fresh(lo, hi):
+        vals = [rng.uniform(lo, hi, N // 2) for _ in range(3)]
+        return lambda: [_encrypt(ctx, sk, v, 100 + i)[0] for i, v in enumerate(vals)]
+
+    cases = [
+        (fresh(-5, 5), lambda xs: ev.gelu_batch(xs), lambda x: ev.gelu(x)),
+        (fresh(-5, 0), lambda xs: ev.softmax_batch(xs, 128), lambda x: ev.softmax(x, 128)),
+        (fresh(-1, 1), lambda xs: ev.layer_norm_batch(xs, 128), lambda x: ev.layer_norm(x, 128)),
+        (fresh(-1, 1), lambda xs: ev.ckks_op_batch(OP_SGN_EVAL, xs, 2, 2, 0.5), lambda x: ev.sgn_eval(x, 2, 2, 0.5)),
+        (fresh(-1, 0), lambda xs: ev.ckks_op_batch(OP_EXP, xs), lambda x: ev.exp(x)),
+        (fresh(0.5, 1.5), lambda xs: ev.ckks_op_batch(OP_INVERSE, xs, 4), lambda x: ev.inverse(x, 4)),
+        (fresh(1, 100), lambda xs: ev.ckks_op_batch(OP_INVERT_SQRT, xs, 5, 2), lambda x: ev.invert_sqrt(x, 5, 2)),
+    ]
+    for make, batched, single in cases:
+        got = batched(make())
+        for g, x in zip(got, make()):
+            want = single(x)
+            assert g.scale == want.scale
+            assert np.array_equal(g.to_numpy(), want.to_numpy())
