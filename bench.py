@@ -937,11 +937,13 @@ def barrier(world):
 
 
 def max_over_ranks(v: float, world: int) -> float:
+    """The slowest rank's time: the only value the replicas exchange."""
     if world == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
