@@ -54,9 +54,21 @@ __device__ __forceinline__ void mac128(uint64_t &lo, uint64_t &hi, uint64_t a, u
     asm("mad.lo.cc.u64 %0, %2, %3, %0;\n\tmadc.hi.u64 %1, %2, %3, %1;" : "+l"(lo), "+l"(hi) : "l"(a), "l"(b));
 }
 
+// v = hh * 2^52 + mid * 2^26 + ll as a 128-bit value, reduced mod q
+__device__ __forceinline__ uint64_t reduce_split(uint64_t hh, uint64_t mid, uint64_t ll, const PrimeConst &P)
+{
+    const uint64_t a = hh << 52, b = mid << 26;
+    const uint64_t lo = a + b;
+    uint64_t hi = (hh >> 12) + (mid >> 38) + (lo < a);
+    const uint64_t lo2 = lo + ll;
+    hi += lo2 < lo;
+    return barrett_128(lo2, hi, P.q, P.r0, P.r1);
+}
+
 // P[b][k][i'][n] = sum_j D[b][j][i'][n] * key[j][k][kidx(i')][n] mod q(i')
 // Rows run i'-major over the batch (row = i' * B + b), so the ciphertexts of a
 // batch read the key rows of one prime (2l limbs) back to back, from L2.
+template <bool SPLIT>
 __global__ void k_ks_inner(const uint64_t *__restrict__ D, const uint64_t *__restrict__ key, uint64_t *__restrict__ P,
                            const PrimeConst *__restrict__ pc, int l, int K, int logn, int B, size_t total)
 {
@@ -74,14 +86,36 @@ __global__ void k_ks_inner(const uint64_t *__restrict__ D, const uint64_t *__res
         const size_t dstride = (size_t)(l + 1) << logn;
         const size_t kstride = (size_t)2 * K << logn;
         const size_t kcomp = (size_t)K << logn;
-        for (int j = 0; j < l; ++j) {
-            const uint64_t dv = d[j * dstride];
-            mac128(lo0, hi0, dv, k0[j * kstride]);
-            mac128(lo1, hi1, dv, k0[j * kstride + kcomp]);
-        }
         uint64_t *pb = P + ((b * 2 * (l + 1)) << logn);
-        pb[((size_t)i << logn) + n] = barrett_128(lo0, hi0, P0.q, P0.r0, P0.r1);
-        pb[((size_t)(l + 1 + i) << logn) + n] = barrett_128(lo1, hi1, P0.q, P0.r0, P0.r1);
+        if (SPLIT) {
+            // every residue below 2^52: each product as four 26 x 26-bit
+            // partial products summed exactly in three 64-bit accumulators
+            // (< 2 * 31 * 2^52 each), one recombination and reduction at the end
+            uint64_t h0 = 0, m0 = 0, w0 = 0, h1 = 0, m1 = 0, w1 = 0;
+            for (int j = 0; j < l; ++j) {
+                const uint64_t dv = d[j * dstride];
+                const uint64_t ka = k0[j * kstride], kb = k0[j * kstride + kcomp];
+                const uint32_t dh = (uint32_t)(dv >> 26), dl = (uint32_t)dv & 0x3ffffffu;
+                const uint32_t ah = (uint32_t)(ka >> 26), al = (uint32_t)ka & 0x3ffffffu;
+                const uint32_t bh = (uint32_t)(kb >> 26), bl = (uint32_t)kb & 0x3ffffffu;
+                h0 += (uint64_t)dh * ah;
+                m0 += (uint64_t)dh * al + (uint64_t)dl * ah;
+                w0 += (uint64_t)dl * al;
+                h1 += (uint64_t)dh * bh;
+                m1 += (uint64_t)dh * bl + (uint64_t)dl * bh;
+                w1 += (uint64_t)dl * bl;
+            }
+            pb[((size_t)i << logn) + n] = reduce_split(h0, m0, w0, P0);
+            pb[((size_t)(l + 1 + i) << logn) + n] = reduce_split(h1, m1, w1, P0);
+        } else {
+            for (int j = 0; j < l; ++j) {
+                const uint64_t dv = d[j * dstride];
+                mac128(lo0, hi0, dv, k0[j * kstride]);
+                mac128(lo1, hi1, dv, k0[j * kstride + kcomp]);
+            }
+            pb[((size_t)i << logn) + n] = barrett_128(lo0, hi0, P0.q, P0.r0, P0.r1);
+            pb[((size_t)(l + 1 + i) << logn) + n] = barrett_128(lo1, hi1, P0.q, P0.r0, P0.r1);
+        }
     }
 }
 
@@ -123,7 +157,11 @@ void ks_modup_inner(Context &c, uint64_t *t, int B, int l, const uint64_t *key, 
     ld.src_limbs = l;
     ntt_forward_loaded(c, D, Bs * l, LimbMap{l + 1, 0, sp}, ld, s);
     size_t tot = Bs * (l + 1) * N;
-    k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, tot); NEXUS_LAUNCHED();
+    if (c.small_primes && l <= 31)
+        k_ks_inner<true><<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, tot);
+    else
+        k_ks_inner<false><<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, tot);
+    NEXUS_LAUNCHED();
 }
 
 // Stage 2: the rounding terms T [B][2][l][N] of the ModDown from the special
@@ -287,7 +325,7 @@ extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l,
         k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot); NEXUS_LAUNCHED();
         ntt_forward(c, D, l, LimbMap{l + 1, 0, sp}, s);
         tot = (size_t)(l + 1) * N;
-        k_ks_inner<<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, 1, tot); NEXUS_LAUNCHED();
+        k_ks_inner<false><<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, 1, tot); NEXUS_LAUNCHED();
         cudaMemcpyAsync(last, P + (size_t)l * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(last + N, P + (size_t)(2 * l + 1) * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
         ntt_inverse(c, last, 2, LimbMap{1, sp, -1}, s);
