@@ -421,6 +421,24 @@ int nexus_bootstrapper_stage(nexus_bootstrapper *bs, int stage, nexus_ciphertext
 /* Number of encoded LT diagonals the bootstrapper keeps on the device. */
 int nexus_bootstrapper_cached_plaintexts(const nexus_bootstrapper *bs, uint64_t *count);
 
+/* ------------------------------------------------------------------------
+ * SEAL byte format of a CKKS ciphertext (host-side, compr_mode_type::none)
+ * ------------------------------------------------------------------------ */
+
+/* Ciphertext::save (native/src/seal/ciphertext.cpp:190-248 with the
+ * SEALHeader of serialization.h:60-93): words [size][limbs][2^log_n] as SEAL
+ * stores them, the caller's parms_id (4 words, the SEALContext's id of the
+ * ciphertext's level).  out = NULL only reports the byte count in *written. */
+int nexus_seal_ciphertext_save(const uint64_t *words, int size, int limbs, int log_n, double scale,
+                               const uint64_t *parms_id, int is_ntt_form, uint8_t *out, size_t capacity,
+                               size_t *written);
+
+/* Ciphertext::load (ciphertext.cpp:249-330), structural checks only (the
+ * caller validates parms_id against its context): words = NULL only reports
+ * the shape. */
+int nexus_seal_ciphertext_load(const uint8_t *bytes, size_t len, uint64_t *words, size_t capacity_words, int *size,
+                               int *limbs, int *log_n, double *scale, uint64_t *parms_id, int *is_ntt_form);
+
 #ifdef __cplusplus
 }
 #endif

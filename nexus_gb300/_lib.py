@@ -87,6 +87,11 @@ SIGNATURES = [
     ("nexus_bootstrap_batch", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("nexus_bootstrapper_stage", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nexus_bootstrapper_cached_plaintexts", C.c_int, [C.c_void_p, u64p]),
+    ("nexus_seal_ciphertext_save", C.c_int, [u64p, C.c_int, C.c_int, C.c_int, C.c_double, u64p, C.c_int,
+                                             C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    ("nexus_seal_ciphertext_load", C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(C.c_int),
+                                             C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double), u64p,
+                                             C.POINTER(C.c_int)]),
     ("nexus_plain_op", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
 ]

@@ -61,12 +61,57 @@ class Ciphertext:
         check(lib().nexus_ciphertext_store(self._h, out.ctypes.data, 1, None), "nexus_ciphertext_store")
         return out
 
+    def save_seal(self, parms_id) -> bytes:
+        """SEAL's Ciphertext::save bytes (compr_mode none) for this ciphertext."""
+        return seal_save(self.to_numpy(), self.scale, parms_id)
+
+    @classmethod
+    def load_seal(cls, ctx: Context, data: bytes):
+        """(ciphertext, parms_id) from SEAL's Ciphertext::save bytes."""
+        words, scale, pid, ntt = seal_load(data)
+        if not ntt:
+            raise ValueError("the engine keeps ciphertexts in NTT form")
+        return cls.from_numpy(ctx, words, scale), pid
+
     def to_device(self):
         import torch
         size, limbs, _, _ = self.info()
         t = torch.empty((size, limbs, self.ctx.n), dtype=torch.int64, device="cuda")
         check(lib().nexus_ciphertext_store(self._h, t.data_ptr(), 0, None), "nexus_ciphertext_store")
         return t
+
+
+def seal_save(words: np.ndarray, scale: float, parms_id, is_ntt_form: bool = True) -> bytes:
+    """Ciphertext::save (compr_mode none) of host words [size][limbs][N]."""
+    w = np.ascontiguousarray(words, dtype=np.uint64)
+    size, limbs, n = w.shape
+    pid = np.ascontiguousarray(parms_id, dtype=np.uint64)
+    nbytes = C.c_size_t()
+    log_n = n.bit_length() - 1
+    u64 = C.POINTER(C.c_uint64)
+    check(lib().nexus_seal_ciphertext_save(w.ctypes.data_as(u64), size, limbs, log_n, float(scale),
+                                           pid.ctypes.data_as(u64), int(is_ntt_form), None, 0, C.byref(nbytes)),
+          "nexus_seal_ciphertext_save")
+    out = np.zeros(nbytes.value, dtype=np.uint8)
+    check(lib().nexus_seal_ciphertext_save(w.ctypes.data_as(u64), size, limbs, log_n, float(scale),
+                                           pid.ctypes.data_as(u64), int(is_ntt_form), out.ctypes.data,
+                                           out.size, C.byref(nbytes)), "nexus_seal_ciphertext_save")
+    return out.tobytes()
+
+
+def seal_load(data: bytes):
+    """Ciphertext::load: (words [size][limbs][N], scale, parms_id, is_ntt_form)."""
+    buf = np.frombuffer(data, dtype=np.uint8)
+    size, limbs, log_n, ntt = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    scale = C.c_double()
+    pid = np.zeros(4, dtype=np.uint64)
+    u64 = C.POINTER(C.c_uint64)
+    args = (C.byref(size), C.byref(limbs), C.byref(log_n), C.byref(scale), pid.ctypes.data_as(u64), C.byref(ntt))
+    check(lib().nexus_seal_ciphertext_load(buf.ctypes.data, buf.size, None, 0, *args), "nexus_seal_ciphertext_load")
+    words = np.zeros((size.value, limbs.value, 1 << log_n.value), dtype=np.uint64)
+    check(lib().nexus_seal_ciphertext_load(buf.ctypes.data, buf.size, words.ctypes.data, words.size, *args),
+          "nexus_seal_ciphertext_load")
+    return words, scale.value, pid, bool(ntt.value)
 
 
 class Evaluator:

@@ -64,6 +64,11 @@ def lib():
         l.sr_mm_compress.argtypes = [C.c_void_p, f64p, C.c_double, u64p, f64p]
         l.sr_mm_power_of_x.argtypes = [C.c_void_p, u64p, C.c_int, C.c_int, u64p]
         l.sr_mm_expand.argtypes = [C.c_void_p, u64p, C.c_int, C.c_double, C.c_uint32, u64p]
+        l.sr_parms_id.argtypes = [C.c_void_p, C.c_int, u64p]
+        l.sr_ct_save.argtypes = [C.c_void_p, u64p, C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_size_t,
+                                 C.POINTER(C.c_size_t)]
+        l.sr_ct_load.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, u64p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_double)]
         _lib = l
     return _lib
 
@@ -189,6 +194,28 @@ class SealRef:
         out = np.zeros(nvals)
         _ck(lib().sr_decrypt(self._h, _p(np.ascontiguousarray(ct)), ct.shape[1], scale, _p(out), nvals))
         return out
+
+    def parms_id(self, limbs):
+        out = np.zeros(4, np.uint64)
+        _ck(lib().sr_parms_id(self._h, limbs, _p(out)))
+        return out
+
+    def save(self, ct, scale) -> bytes:
+        ct = np.ascontiguousarray(ct, dtype=np.uint64)
+        n = C.c_size_t()
+        _ck(lib().sr_ct_save(self._h, _p(ct), ct.shape[0], ct.shape[1], scale, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.uint8)
+        _ck(lib().sr_ct_save(self._h, _p(ct), ct.shape[0], ct.shape[1], scale, out.ctypes.data, out.size,
+                             C.byref(n)))
+        return out.tobytes()
+
+    def load(self, data: bytes):
+        buf = np.frombuffer(data, dtype=np.uint8)
+        size, limbs, scale = C.c_int(), C.c_int(), C.c_double()
+        big = np.zeros(16 * self.k * self.n, np.uint64)
+        _ck(lib().sr_ct_load(self._h, buf.ctypes.data, buf.size, _p(big), C.byref(size), C.byref(limbs),
+                             C.byref(scale)))
+        return big[:size.value * limbs.value * self.n].reshape(size.value, limbs.value, self.n), scale.value
 
     OPS = {"gelu": 0, "softmax": 1, "layer_norm": 2, "sgn_eval": 3, "exp": 4, "inverse": 5, "invert_sqrt": 6}
 

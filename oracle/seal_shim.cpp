@@ -9,6 +9,7 @@
 #include <array>
 #include <complex>
 #include <cstring>
+#include <sstream>
 #include <memory>
 #include <string>
 #include <vector>
@@ -439,6 +440,48 @@ int sr_mm_expand(void *h, const uint64_t *in, int limbs, double scale, uint32_t 
         auto leaves = mm.expand_ciphertext(x, m, *s.gk, ck.rots);
         size_t per = 2 * (size_t)limbs * s.n;
         for (size_t i = 0; i < leaves.size(); ++i) std::memcpy(out + i * per, leaves[i].data(), per * 8);
+    })
+}
+
+// Ciphertext::save / load with compr_mode_type::none, and a level's parms_id
+int sr_parms_id(void *h, int limbs, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        auto pid = pid_for_limbs(s, limbs);
+        for (int i = 0; i < 4; ++i) out[i] = pid[i];
+    })
+}
+
+int sr_ct_save(void *h, const uint64_t *in, int size, int limbs, double scale, uint8_t *out, size_t cap,
+               size_t *written)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Ciphertext ct;
+        load_ct(s, ct, in, size, limbs, scale);
+        std::stringstream ss;
+        ct.save(ss, compr_mode_type::none);
+        const std::string b = ss.str();
+        *written = b.size();
+        if (out) {
+            if (cap < b.size()) throw std::invalid_argument("buffer too small");
+            std::memcpy(out, b.data(), b.size());
+        }
+    })
+}
+
+int sr_ct_load(void *h, const uint8_t *in, size_t len, uint64_t *out, int *size, int *limbs, double *scale)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Ciphertext ct;
+        std::stringstream ss(std::string(reinterpret_cast<const char *>(in), len));
+        ct.load(*s.ctx, ss);
+        *size = (int)ct.size();
+        *limbs = (int)ct.coeff_modulus_size();
+        *scale = ct.scale();
+        if (out) store_ct(s, ct, out);
     })
 }
 
