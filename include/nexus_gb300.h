@@ -418,6 +418,12 @@ int nexus_bootstrap_batch(nexus_bootstrapper *bs, nexus_ciphertext *const *cts, 
 int nexus_bootstrapper_stage(nexus_bootstrapper *bs, int stage, nexus_ciphertext *a, const nexus_ciphertext *b,
                              nexus_ciphertext *r1, nexus_ciphertext *r2);
 
+/* ArgmaxEvaluator::argmax (src/argmax.cpp:9-81) with the bootstrapper's
+ * evaluator and keys: slots 0..len-1 of x -> the one-hot indicator of the
+ * maximum (sgn(x - max) + 1), bootstrapping after every round.  x is updated
+ * in place as in the reference; len a power of two. */
+int nexus_argmax(nexus_bootstrapper *bs, nexus_ciphertext *x, int len, nexus_ciphertext *res);
+
 /* Number of encoded LT diagonals the bootstrapper keeps on the device. */
 int nexus_bootstrapper_cached_plaintexts(const nexus_bootstrapper *bs, uint64_t *count);
 

@@ -84,6 +84,7 @@ SIGNATURES = [
     ("nexus_lt_coefficients_3", C.c_int, [C.c_int, C.c_int, C.c_long, C.c_int, C.c_void_p, C.POINTER(C.c_int),
                                           C.POINTER(C.c_int)]),
     ("nexus_bootstrap", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("nexus_argmax", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("nexus_bootstrap_batch", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("nexus_bootstrapper_stage", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nexus_bootstrapper_cached_plaintexts", C.c_int, [C.c_void_p, u64p]),

@@ -4,6 +4,7 @@
 #include <string>
 
 #include "../../include/nexus_gb300.h"
+#include "argmax.h"
 #include "bootstrap.h"
 #include "capi_types.h"
 
@@ -186,6 +187,19 @@ extern "C" int nexus_bootstrap_batch(nexus_bootstrapper *bs, nexus_ciphertext *c
                 cudaSuccess)
                 throw std::runtime_error("copy failed");
         }
+    });
+}
+
+extern "C" int nexus_argmax(nexus_bootstrapper *bs, nexus_ciphertext *x, int len, nexus_ciphertext *res)
+{
+    static const char *fn = "nexus_argmax";
+    if (!bs || !x || !res) return fail(fn, "null argument");
+    if (len < 1 || (len & (len - 1))) return fail(fn, "len must be a power of two");
+    if (x == res) return fail(fn, "res must be a different ciphertext");
+    return guarded(fn, [&] {
+        if (bs->bs.fftcoeff1.empty()) throw std::logic_error("generate_LT_coefficient_3 has not been called");
+        ArgmaxEvaluator am(bs->ev->ck, bs->bs);
+        am.argmax(x->ct, res->ct, len);
     });
 }
 

@@ -294,6 +294,13 @@ class Bootstrapper:
         check(lib().nexus_bootstrap_batch(self._h, a, len(cts), r), "nexus_bootstrap_batch")
         return res
 
+    def argmax(self, x: Ciphertext, length: int) -> Ciphertext:
+        """ArgmaxEvaluator::argmax (src/argmax.cpp) over slots 0..length-1 of x
+        (x is updated in place as in the reference)."""
+        res = Ciphertext(self.ctx)
+        check(lib().nexus_argmax(self._h, x.handle, int(length), res.handle), "nexus_argmax")
+        return res
+
     def stage(self, stage: int, a: Ciphertext, b: Ciphertext | None = None):
         r1, r2 = Ciphertext(self.ctx), Ciphertext(self.ctx)
         check(lib().nexus_bootstrapper_stage(self._h, stage, a.handle, None if b is None else b.handle, r1.handle,

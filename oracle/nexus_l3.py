@@ -517,6 +517,35 @@ def layer_norm(ck: CKKSEvaluator, x: Ct, length: int) -> Ct:
     return ev.rescale(ev.relinearize(ev.multiply(res, x)))
 
 
+def argmax(ck: CKKSEvaluator, bs, x: Ct, length: int) -> Ct:
+    """ArgmaxEvaluator::argmax (src/argmax.cpp:9-81); bs is an
+    oracle.bootstrap.Bootstrapper over the same evaluator."""
+    ev = ck.ev
+    log_step = int(math.log2(length))
+    x = ev.add(x, ev.rotate(x, -length))
+    a = x
+    for i in range(log_step):
+        b = ev.rotate(a, 1 << i)
+        a_plus_b = ev.add(a, b)
+        a_minus_b = ev.sub(a, b)
+        sign = ck.sgn_eval(a_minus_b, 2, 2)
+        a_minus_b = ev.mod_switch_to(a_minus_b, sign.limbs)
+        a_minus_b_sgn = ev.rescale(ev.relinearize(ev.multiply(a_minus_b, sign)))
+        half = ev.encode_scalar(0.5, a_plus_b.scale, a_plus_b.limbs)
+        a_plus_b = ev.rescale(ev.multiply_plain(a_plus_b, half))
+        a_plus_b.scale = a_minus_b_sgn.scale
+        a_plus_b = ev.mod_switch_to(a_plus_b, a_minus_b_sgn.limbs)
+        a = ev.add(a_plus_b, a_minus_b_sgn)
+        # ArgmaxEvaluator::bootstrap (:83-106)
+        a = ev.mod_switch_to(a, 1)
+        bs.final_scale = a.scale
+        a = bs.bootstrap_3(a)
+    x.scale = a.scale
+    x = ev.mod_switch_to(x, a.limbs)
+    res = ck.sgn_eval(ev.sub(x, a), 2, 2, 1.0)
+    return ev.add_plain(res, ev.encode_scalar(1.0, res.scale, res.limbs))
+
+
 def negacyclic_shift(coeffs: np.ndarray, index: int, q_per_limb) -> np.ndarray:
     """negacyclic_shift_poly_coeffmod (util/polyarithsmallmod.cpp:319-370) on
     coefficient-form residues [..., limbs, N]: multiply by X^index mod X^N+1."""

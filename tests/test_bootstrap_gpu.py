@@ -205,3 +205,41 @@ def test_sparse_bootstrap_matches_oracle(sparse_env):
     assert np.array_equal(batch.to_numpy(), out.to_numpy())
     err = np.abs(_decrypt(ctx, sk, out) - vals)
     assert err.max() < 2.0 ** -12, err.max()
+
+
+def test_argmax_matches_oracle(cuda):
+    """ArgmaxEvaluator (src/argmax.cpp) with a bootstrap per round, on the
+    reference's argmax parameters scaled to N=2^12 (sparse slots 2^(logN-2),
+    q0 51 bits, 17 x 46-bit, 14 x 51-bit, special 58 bits)."""
+    import torch
+    import nexus_gb300 as ng
+    from nexus_gb300.operators import Bootstrapper, Ciphertext, Evaluator
+    from nexus_gb300.remez import load_table
+    log_n, length = 12, 4
+    n, log_nh = 1 << log_n, log_n - 1
+    logn = log_n - 2
+    qs = ng.create_coeff_modulus(n, [51] + [46] * 17 + [51] * 14 + [58])
+    ctx = ng.Context(log_n, qs)
+    sk = ctx.keygen_secret(seed=71, hamming_weight=192)
+    rk = ctx.keygen_relin(sk, seed=72)
+    steps = B.rot_key_steps_3(logn, log_nh) + [-length]
+    gks = {ctx.galois_elt(st): ctx.keygen_galois(sk, ctx.galois_elt(st), seed=73 + i) for i, st in enumerate(steps)}
+    ev = Evaluator(ctx, SCALE, rk, gks)
+    bs = Bootstrapper(ev, 10, logn, log_nh, len(qs) - 2, SCALE, 25, 59, 2, 1)
+    bs.prepare_mod_polynomial()
+    bs.generate_LT_coefficient_3()
+    sparse = np.zeros(1 << logn)
+    sparse[:length] = [0.1, 0.7, -0.3, 0.2]
+    vals = np.resize(sparse, n // 2)
+    top = len(qs) - 1
+    pt = torch.empty((top, n), dtype=torch.int64, device="cuda")
+    ctx.encode(vals, SCALE, top, pt)
+    words = to_host(ctx.encrypt_symmetric(sk, pt, top, 74))
+    out = bs.argmax(Ciphertext.from_numpy(ctx, words, SCALE), length)
+    oev = L.Evaluator(po.OracleContext(log_n, qs), to_host(rk), {e: to_host(k) for e, k in gks.items()})
+    obs = B.Bootstrapper(oev, 10, logn, log_nh, len(qs) - 2, SCALE, 25, 59, 2, 1, load_table())
+    obs.generate_LT_coefficient_3()
+    want = L.argmax(L.CKKSEvaluator(oev, SCALE), obs, L.Ct(words, SCALE), length)
+    _same(out, want)
+    dec = _decrypt(ctx, sk, out)[:length]
+    assert np.argmax(dec) == 1 and dec[1] > 1.5 and np.all(np.abs(np.delete(dec, 1)) < 0.5)
