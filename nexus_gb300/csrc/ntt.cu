@@ -102,6 +102,7 @@ template <int T, bool SMALL>
 __device__ __forceinline__ void fwd_regs_blocked(uint64_t (&x)[kE], const ulonglong2 *__restrict__ W, uint64_t B,
                                                  int t, uint64_t q, uint64_t q2)
 {
+    static_assert(T <= kE, "the blocked stages pair residues inside one thread: at most kE * kE points per pass");
     constexpr int S = kE * T;
 #pragma unroll
     for (int g = T / 2; g >= 1; g >>= 1) {
@@ -121,6 +122,7 @@ template <int T>
 __device__ __forceinline__ void inv_regs_blocked(uint64_t (&x)[kE], const ulonglong2 *__restrict__ W, uint64_t B,
                                                  int t, uint64_t q, uint64_t q2)
 {
+    static_assert(T <= kE, "the blocked stages pair residues inside one thread: at most kE * kE points per pass");
     constexpr int S = kE * T;
 #pragma unroll
     for (int g = 1; g <= T / 2; g <<= 1) {
