@@ -62,18 +62,31 @@ def _peak_hbm():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def _profile_traffic(name: str):
-    """Per-launch DRAM bytes recorded from ncu in profiles/<name>.txt."""
+def _profile_value(name: str, key: str):
+    """A figure recorded from ncu in profiles/<name>.txt (a "key: value" line)."""
     p = ROOT / "profiles" / f"{name}.txt"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch:"):
+        if line.startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def _profile_traffic(name: str):
+    """Per-launch DRAM bytes recorded from ncu in profiles/<name>.txt."""
+    return _profile_value(name, "traffic_bytes_per_launch")
+
+
+def _ntt_traffic(limbs_per_launch: float, n: int = 1 << 16):
+    """DRAM bytes of one NTT launch of `limbs_per_launch` limb-NTTs of degree n,
+    scaled from the ncu capture of the N=2^16 NTT (DRAM traffic grows with the
+    limbs and with n)."""
+    per_limb = _profile_value("ntt_forward_n65536_51bit_8ct", "traffic_bytes_per_limb")
+    return None if per_limb is None else per_limb * limbs_per_launch * n / (1 << 16)
 
 
 class ClockSampler:
@@ -409,7 +422,8 @@ def run_mm_gpu(args, rank, world):
             "algorithmic_bytes_per_launch": alg_bytes_per_call,
             "avg_launch_ms": ntt_avg_ms, "launches_per_step": ntt_calls, "limb_ntts_per_step": ntt_limbs,
             "share_of_step": ntt_ms / instr_ms,
-            "traffic": _profile_traffic("matmul_bert_128x768x768_n65536"),
+            "traffic": _ntt_traffic(ntt_limbs / max(1, ntt_calls)),
+            "traffic_source": "ncu DRAM bytes per limb-NTT of the N=2^16 capture x limbs per launch",
         },
         "e2e": {"value": world * e2e_steps / e2e_s, "unit": "matmul/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes},
@@ -636,7 +650,8 @@ def run_boot_gpu(args, rank, world):
             "algorithmic_bytes_per_launch": alg_bytes_per_call,
             "avg_launch_ms": ntt_avg_ms, "launches_per_step": ntt_calls, "limb_ntts_per_step": ntt_limbs,
             "share_of_step": ntt_ms / instr_ms,
-            "traffic": _profile_traffic(f"bootstrap_full_n65536_{BOOT_CTS}ct"),
+            "traffic": _ntt_traffic(ntt_limbs / max(1, ntt_calls)),
+            "traffic_source": "ncu DRAM bytes per limb-NTT of the 51-bit NTT capture x limbs per launch",
         },
         "e2e": {"value": world * BOOT_CTS / e2e_s, "unit": "bootstraps/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes},
@@ -879,7 +894,8 @@ def run_gelu_gpu(args, rank, world):
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg_bytes_per_call,
             "avg_launch_ms": ntt_avg_ms, "launches_per_step": ntt_calls, "share_of_step": ntt_ms / instr_ms,
-            "traffic": None,
+            "traffic": _ntt_traffic(ntt_limbs / max(1, ntt_calls), n),
+            "traffic_source": "ncu DRAM bytes per limb-NTT of the N=2^16 capture, scaled by N and limbs per launch",
         },
         "e2e": {"value": world * GELU_CTS / e2e_s, "unit": "GELU/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes},
