@@ -60,8 +60,13 @@ ModularReducerT<EV, CT>::ModularReducerT(EV &ev, long K, double lw, long d, long
 template <class EV, class CT>
 void ModularReducerT<EV, CT>::set_polynomial_heap(long k, long m, std::vector<std::vector<double>> nodes, double sic)
 {
-    if (k < 2 || m < 0 || nodes.size() != (size_t)((1 << (m + 1)) - 1) || nodes[0].empty())
+    if (k < 2 || m < 1 || nodes.size() != (size_t)((1 << (m + 1)) - 1) || nodes[0].empty())
         throw std::invalid_argument("malformed polynomial heap");
+    // the evaluation reads coefficients 0 and 1 of every leaf and at most
+    // k + 1 of them (T_k is the first giant step)
+    for (size_t i = (size_t)(1 << m) - 1; i < nodes.size(); i++)
+        if (!nodes[i].empty() && (nodes[i].size() < 2 || nodes[i].size() > (size_t)k + 1))
+            throw std::invalid_argument("malformed polynomial heap");
     heap_k = k;
     heap_m = m;
     heap = std::move(nodes);

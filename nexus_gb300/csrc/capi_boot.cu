@@ -87,6 +87,7 @@ extern "C" int nexus_bootstrapper_add_rot_steps(const nexus_bootstrapper *bs, in
 {
     static const char *fn = "nexus_bootstrapper_add_rot_steps";
     if (!bs || !steps || !count) return fail(fn, "null argument");
+    if (*count < 0 || *count > capacity) return fail(fn, "count out of range");
     return guarded(fn, [&] {
         std::vector<int> v(steps, steps + *count);
         bs->bs.addLeftRotKeys_Linear_to_vector_3(v);
@@ -113,6 +114,7 @@ extern "C" int nexus_lt_coefficients_3(int logn, int logNh, long boundary_K, int
     if (!count || !len) return fail(fn, "null argument");
     if (which < 0 || which > 5) return fail(fn, "which must be 0..5");
     if (logn < 1 || logn > logNh || logNh > 16) return fail(fn, "bad logn / logNh");
+    if (boundary_K < 1) return fail(fn, "boundary_K must be positive");
     try {
         std::vector<CVec> v[6];
         lt_coefficients_3(logn, logNh, boundary_K, v);
@@ -139,6 +141,7 @@ extern "C" int nexus_bootstrap(nexus_bootstrapper *bs, nexus_ciphertext *ct, nex
     static const char *fn = "nexus_bootstrap";
     if (!bs || !ct || !rtn) return fail(fn, "null argument");
     if (ct == rtn) return fail(fn, "rtn must be a different ciphertext");
+    if (const char *e = input_problem(bs->ev->ctx, ct)) return fail(fn, e);
     return guarded(fn, [&] { bs->bs.bootstrap_3(rtn->ct, ct->ct); });
 }
 
@@ -149,6 +152,7 @@ extern "C" int nexus_bootstrap_batch(nexus_bootstrapper *bs, nexus_ciphertext *c
     if (!bs || !cts || !rtn || count < 1) return fail(fn, "null argument");
     for (int b = 0; b < count; ++b) {
         if (!cts[b] || !rtn[b]) return fail(fn, "null ciphertext");
+        if (const char *e = input_problem(bs->ev->ctx, cts[b])) return fail(fn, e);
         for (int j = 0; j < count; ++j)
             if (rtn[b] == cts[j]) return fail(fn, "rtn must not alias an input");
     }
@@ -196,6 +200,7 @@ extern "C" int nexus_argmax(nexus_bootstrapper *bs, nexus_ciphertext *x, int len
     if (!bs || !x || !res) return fail(fn, "null argument");
     if (len < 1 || (len & (len - 1))) return fail(fn, "len must be a power of two");
     if (x == res) return fail(fn, "res must be a different ciphertext");
+    if (const char *e = input_problem(bs->ev->ctx, x)) return fail(fn, e);
     return guarded(fn, [&] {
         if (bs->bs.fftcoeff1.empty()) throw std::logic_error("generate_LT_coefficient_3 has not been called");
         ArgmaxEvaluator am(bs->ev->ck, bs->bs);
@@ -208,6 +213,10 @@ extern "C" int nexus_bootstrapper_stage(nexus_bootstrapper *bs, int stage, nexus
 {
     static const char *fn = "nexus_bootstrapper_stage";
     if (!bs || !a) return fail(fn, "null argument");
+    if (const char *e = input_problem(bs->ev->ctx, a)) return fail(fn, e);
+    if (b) {
+        if (const char *e = input_problem(bs->ev->ctx, b)) return fail(fn, e);
+    }
     return guarded(fn, [&] {
         Bootstrapper &B = bs->bs;
         switch (stage) {

@@ -121,6 +121,7 @@ extern "C" int nexus_gelu(nexus_evaluator *ev, nexus_ciphertext *x, nexus_cipher
 {
     static const char *fn = "nexus_gelu";
     if (!ev || !x || !res) return fail(fn, "null argument");
+    if (const char *e = input_problem(ev->ctx, x)) return fail(fn, e);
     return guarded(fn, [&] {
         GeLUEvaluator g(ev->ck);
         g.gelu(x->ct, res->ct);
@@ -131,6 +132,7 @@ extern "C" int nexus_softmax(nexus_evaluator *ev, nexus_ciphertext *x, int len, 
 {
     static const char *fn = "nexus_softmax";
     if (!ev || !x || !res) return fail(fn, "null argument");
+    if (const char *e = input_problem(ev->ctx, x)) return fail(fn, e);
     if (len < 1 || (len & (len - 1))) return fail(fn, "len must be a power of two");
     return guarded(fn, [&] {
         SoftmaxEvaluator sm(ev->ck);
@@ -142,6 +144,7 @@ extern "C" int nexus_layer_norm(nexus_evaluator *ev, nexus_ciphertext *x, int le
 {
     static const char *fn = "nexus_layer_norm";
     if (!ev || !x || !res) return fail(fn, "null argument");
+    if (const char *e = input_problem(ev->ctx, x)) return fail(fn, e);
     if (len < 1 || (len & (len - 1))) return fail(fn, "len must be a power of two");
     return guarded(fn, [&] {
         LNEvaluator ln(ev->ck);
@@ -154,6 +157,7 @@ extern "C" int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext
 {
     static const char *fn = "nexus_ckks_op";
     if (!ev || !x || !res) return fail(fn, "null argument");
+    if (const char *e = input_problem(ev->ctx, x)) return fail(fn, e);
     return guarded(fn, [&] {
         switch (op) {
         case NEXUS_OP_SGN_EVAL: res->ct = ev->ck.sgn_eval(x->ct, a1, a2, f); break;
@@ -213,6 +217,7 @@ int check_batch(const char *fn, nexus_evaluator *ev, nexus_ciphertext *const *ct
     if (!ev || !cts || !res || count < 1) return fail(fn, "null argument");
     for (int b = 0; b < count; ++b) {
         if (!cts[b] || !res[b]) return fail(fn, "null ciphertext");
+        if (const char *e = input_problem(ev->ctx, cts[b])) return fail(fn, e);
         for (int j = 0; j < count; ++j)
             if (res[b] == cts[j]) return fail(fn, "results must not alias inputs");
     }
@@ -292,6 +297,7 @@ extern "C" int nexus_mm_power_of_x(nexus_evaluator *ev, nexus_ciphertext *x, int
 {
     static const char *fn = "nexus_mm_power_of_x";
     if (!ev || !x || !res) return fail(fn, "null argument");
+    if (const char *e = input_problem(ev->ctx, x)) return fail(fn, e);
     return guarded(fn, [&] {
         MMEvaluator mm(ev->ck);
         mm.multiply_power_of_x(x->ct, res->ct, index);
@@ -302,6 +308,7 @@ extern "C" int nexus_mm_expand(nexus_evaluator *ev, const nexus_ciphertext *x, u
 {
     static const char *fn = "nexus_mm_expand";
     if (!ev || !x || !d_out) return fail(fn, "null argument");
+    if (const char *e = input_problem(ev->ctx, x)) return fail(fn, e);
     if (m < 1 || (m & (m - 1)) || m > ev->ctx->c.n) return fail(fn, "m must be a power of two <= N");
     return guarded(fn, [&] {
         MMEvaluator mm(ev->ck);
@@ -318,8 +325,10 @@ extern "C" int nexus_matrix_mul(nexus_evaluator *ev, nexus_ciphertext *const *co
 {
     static const char *fn = "nexus_matrix_mul";
     if (!ev || !compressed || !d_pts || !res || n_compressed < 1) return fail(fn, "null argument");
-    for (int i = 0; i < n_compressed; ++i)
+    for (int i = 0; i < n_compressed; ++i) {
         if (!compressed[i]) return fail(fn, "null compressed ciphertext");
+        if (const char *e = input_problem(ev->ctx, compressed[i])) return fail(fn, e);
+    }
     for (int r = 0; r < rows; ++r)
         if (!res[r]) return fail(fn, "null result handle");
     return guarded(fn, [&] {

@@ -16,3 +16,11 @@ struct nexus_ciphertext {
     nexus_context *ctx;
     nexus::Ciphertext ct;
 };
+
+// an input ciphertext must hold data and belong to the evaluator's context
+inline const char *input_problem(const nexus_context *ctx, const nexus_ciphertext *c)
+{
+    if (c->ctx != ctx) return "ciphertext belongs to another context";
+    if (c->ct.empty()) return "ciphertext is empty";
+    return nullptr;
+}

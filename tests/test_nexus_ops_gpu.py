@@ -141,3 +141,20 @@ def test_lockstep_operators_equal_single(env):
             want = single(x)
             assert g.scale == want.scale
             assert np.array_equal(g.to_numpy(), want.to_numpy())
+
+
+def test_inputs_are_validated(env):
+    """An empty ciphertext or one of another context is an error, not a kernel
+    launch on missing or mis-sized data."""
+    import nexus_gb300 as ng
+    from nexus_gb300 import NexusError
+    from nexus_gb300.operators import Ciphertext
+    ctx, sk, ev, ock = env
+    with pytest.raises(NexusError, match="empty"):
+        ev.gelu(Ciphertext(ctx))
+    other = ng.Context(LOG_N, ng.create_coeff_modulus(N, [50, 40, 50]))
+    foreign = Ciphertext.from_numpy(other, np.zeros((2, 2, N), dtype=np.uint64), SCALE)
+    with pytest.raises(NexusError, match="another context"):
+        ev.exp(foreign)
+    with pytest.raises(NexusError, match="another context"):
+        ev.gelu_batch([foreign])
