@@ -158,3 +158,23 @@ def test_inputs_are_validated(env):
         ev.exp(foreign)
     with pytest.raises(NexusError, match="another context"):
         ev.gelu_batch([foreign])
+
+
+def test_gelu_on_the_short_chain_fails_like_seal(cuda):
+    """GELU needs 18 rescales; on 60 + 7 x 40 + 60 SEAL stops with "scale out
+    of bounds" (NEXUS on SEAL, N=2^14), and so does the engine."""
+    import torch
+    import nexus_gb300 as ng
+    from nexus_gb300 import NexusError
+    from nexus_gb300.operators import Ciphertext, Evaluator
+    n = 1 << 14
+    qs = ng.create_coeff_modulus(n, [60] + [40] * 7 + [60])
+    ctx = ng.Context(14, qs)
+    sk = ctx.keygen_secret(seed=5)
+    ev = Evaluator(ctx, SCALE, ctx.keygen_relin(sk, seed=6))
+    top = len(qs) - 1
+    pt = torch.empty((top, n), dtype=torch.int64, device="cuda")
+    ctx.encode(np.random.default_rng(0).uniform(-5, 5, n // 2), SCALE, top, pt)
+    x = Ciphertext.from_device(ctx, ctx.encrypt_symmetric(sk, pt, top, 7), SCALE)
+    with pytest.raises(NexusError, match="scale out of bounds|end of modulus switching chain|level too low"):
+        ev.gelu(x)
