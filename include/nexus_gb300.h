@@ -111,12 +111,26 @@ int nexus_rescale(nexus_context *ctx, const uint64_t *d_in, int size, int limbs,
 /*
  * Key switching: d_ct [2][limbs][N] += switch(d_target [limbs][N]) under the
  * key-switching key d_key [n_moduli-1][2][n_moduli][N] (SEAL's KSwitchKeys
- * layout: one PublicKey per data prime at the key level).
+ * layout: one PublicKey per data prime at the key level).  Every key passed to
+ * the key-switching calls (switch, relinearize, Galois) must start on a
+ * 16-byte boundary, as any cudaMalloc'd buffer does; others are rejected.
  * Replaces: Evaluator::switch_key_inplace (native/src/seal/evaluator.cpp:2724-3022);
  *   Phantom keyswitch_inplace (cuda/thirdparty/phantom-fhe/src/eval_key_switch.cu:93).
  */
 int nexus_switch_key(nexus_context *ctx, uint64_t *d_ct, int limbs, const uint64_t *d_target, const uint64_t *d_key,
                      void *stream);
+
+/*
+ * Key switching of `batch` ciphertexts at one level under one key:
+ * d_ct [batch][2][limbs][N], d_target [batch][limbs][N] (must not overlap
+ * d_ct).  Ciphertext b receives the words nexus_switch_key gives for
+ * (d_ct[b], d_target[b]); every kernel runs once over the whole batch and the
+ * key is read once per batch.
+ * No counterpart in the reference: SEAL's switch_key_inplace
+ *   (native/src/seal/evaluator.cpp:2724-3022) takes one ciphertext per call.
+ */
+int nexus_switch_key_batch(nexus_context *ctx, uint64_t *d_ct, int batch, int limbs, const uint64_t *d_target,
+                           const uint64_t *d_key, void *stream);
 
 /*
  * Key switching that allocates nothing: the same operation and output words

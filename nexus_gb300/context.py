@@ -80,6 +80,11 @@ class Context:
         check(lib().nexus_switch_key(self._h, ct.data_ptr(), ct.shape[1], target.data_ptr(), key.data_ptr(),
                                      _stream_ptr(stream)), "nexus_switch_key")
 
+    def switch_key_batch(self, cts, targets, key, stream=None):
+        """cts [B][2][limbs][N], targets [B][limbs][N]: every ciphertext in one pass."""
+        check(lib().nexus_switch_key_batch(self._h, cts.data_ptr(), cts.shape[0], cts.shape[2], targets.data_ptr(),
+                                           key.data_ptr(), _stream_ptr(stream)), "nexus_switch_key_batch")
+
     def relinearize(self, ct3, key, out2, stream=None):
         check(lib().nexus_relinearize(self._h, ct3.data_ptr(), ct3.shape[1], key.data_ptr(), out2.data_ptr(),
                                       _stream_ptr(stream)), "nexus_relinearize")

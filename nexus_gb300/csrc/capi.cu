@@ -118,6 +118,19 @@ extern "C" int nexus_switch_key(nexus_context *ctx, uint64_t *ct, int limbs, con
     return guarded(fn, [&] { switch_key(ctx->c, ct, limbs, target, key, (cudaStream_t)stream); });
 }
 
+extern "C" int nexus_switch_key_batch(nexus_context *ctx, uint64_t *ct, int batch, int limbs, const uint64_t *target,
+                                      const uint64_t *key, void *stream)
+{
+    static const char *fn = "nexus_switch_key_batch";
+    if (check_ct(fn, ctx, limbs)) return -1;
+    if (batch < 0) return fail(fn, "batch must be >= 0");
+    if (batch == 0) return 0;
+    if (!ct || !target || !key) return fail(fn, "null argument");
+    const size_t ct_words = (size_t)batch * 2 * limbs * ctx->c.n, t_words = (size_t)batch * limbs * ctx->c.n;
+    if (ct < target + t_words && target < ct + ct_words) return fail(fn, "d_target must not overlap d_ct");
+    return guarded(fn, [&] { switch_key_batch(ctx->c, ct, batch, limbs, target, key, (cudaStream_t)stream); });
+}
+
 extern "C" int nexus_relinearize(nexus_context *ctx, const uint64_t *ct3, int limbs, const uint64_t *key,
                                  uint64_t *out2, void *stream)
 {

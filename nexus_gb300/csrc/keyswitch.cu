@@ -10,6 +10,7 @@
 //      reduction: P[k][i] = sum_j D[j][i] * key[j][k][i] mod q_i.
 //   4. ModDown with rounding: ct[k][i] += (P[k][i] - NTT_i(((INTT_p(P[k][p]) + p/2)
 //      mod p) - p/2)) * p^{-1} mod q_i.
+#include <cstdint>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -67,55 +68,69 @@ __device__ __forceinline__ uint64_t reduce_split(uint64_t hh, uint64_t mid, uint
 
 // P[b][k][i'][n] = sum_j D[b][j][i'][n] * key[j][k][kidx(i')][n] mod q(i')
 // Rows run i'-major over the batch (row = i' * B + b), so the ciphertexts of a
-// batch read the key rows of one prime (2l limbs) back to back, from L2.
+// batch read the key rows of one prime (2l limbs) back to back, from L2.  Each
+// thread owns two neighbouring coefficients (16-byte loads) and the digit loop
+// is unrolled so that several rows' loads are in flight at once: the kernel is
+// bound by the latency of its D and key reads.
 template <bool SPLIT>
 __global__ void k_ks_inner(const uint64_t *__restrict__ D, const uint64_t *__restrict__ key, uint64_t *__restrict__ P,
                            const PrimeConst *__restrict__ pc, int l, int K, int logn, int B, size_t total)
 {
     const size_t N = (size_t)1 << logn;
     for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
-        const size_t row = x >> logn;            // i * B + b
+        const size_t row = x >> (logn - 1);      // i * B + b
         const size_t b = row % (size_t)B;
         const int i = (int)(row / (size_t)B);
-        const size_t n = x & (N - 1);
+        const size_t n = (x & ((N >> 1) - 1)) << 1;
         const int kidx = (i == l) ? K - 1 : i;
         const PrimeConst P0 = pc[kidx];
-        uint64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
-        const uint64_t *d = D + ((b * l * (l + 1) + i) << logn) + n;
-        const uint64_t *k0 = key + ((size_t)kidx << logn) + n;
-        const size_t dstride = (size_t)(l + 1) << logn;
-        const size_t kstride = (size_t)2 * K << logn;
-        const size_t kcomp = (size_t)K << logn;
-        uint64_t *pb = P + ((b * 2 * (l + 1)) << logn);
+        const ulonglong2 *d = reinterpret_cast<const ulonglong2 *>(D + ((b * l * (l + 1) + i) << logn) + n);
+        const ulonglong2 *k0 = reinterpret_cast<const ulonglong2 *>(key + ((size_t)kidx << logn) + n);
+        const size_t dstride = ((size_t)(l + 1) << logn) >> 1;   // in ulonglong2
+        const size_t kstride = ((size_t)2 * K << logn) >> 1;
+        const size_t kcomp = ((size_t)K << logn) >> 1;
+        uint64_t *pb = P + ((b * 2 * (l + 1)) << logn) + n;
+        ulonglong2 r0, r1;
         if (SPLIT) {
             // every residue below 2^52: each product as four 26 x 26-bit
             // partial products summed exactly in three 64-bit accumulators
             // (< 2 * 31 * 2^52 each), one recombination and reduction at the end
-            uint64_t h0 = 0, m0 = 0, w0 = 0, h1 = 0, m1 = 0, w1 = 0;
+            uint64_t h[4] = {0, 0, 0, 0}, m[4] = {0, 0, 0, 0}, w[4] = {0, 0, 0, 0};
+#pragma unroll 4
             for (int j = 0; j < l; ++j) {
-                const uint64_t dv = d[j * dstride];
-                const uint64_t ka = k0[j * kstride], kb = k0[j * kstride + kcomp];
-                const uint32_t dh = (uint32_t)(dv >> 26), dl = (uint32_t)dv & 0x3ffffffu;
-                const uint32_t ah = (uint32_t)(ka >> 26), al = (uint32_t)ka & 0x3ffffffu;
-                const uint32_t bh = (uint32_t)(kb >> 26), bl = (uint32_t)kb & 0x3ffffffu;
-                h0 += (uint64_t)dh * ah;
-                m0 += (uint64_t)dh * al + (uint64_t)dl * ah;
-                w0 += (uint64_t)dl * al;
-                h1 += (uint64_t)dh * bh;
-                m1 += (uint64_t)dh * bl + (uint64_t)dl * bh;
-                w1 += (uint64_t)dl * bl;
+                const ulonglong2 dv = d[j * dstride];
+                const ulonglong2 ka = k0[j * kstride], kb = k0[j * kstride + kcomp];
+                const uint64_t dd[2] = {dv.x, dv.y}, aa[4] = {ka.x, ka.y, kb.x, kb.y};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const uint64_t dx = dd[e & 1];
+                    const uint32_t dh = (uint32_t)(dx >> 26), dl = (uint32_t)dx & 0x3ffffffu;
+                    const uint32_t ah = (uint32_t)(aa[e] >> 26), al = (uint32_t)aa[e] & 0x3ffffffu;
+                    h[e] += (uint64_t)dh * ah;
+                    m[e] += (uint64_t)dh * al + (uint64_t)dl * ah;
+                    w[e] += (uint64_t)dl * al;
+                }
             }
-            pb[((size_t)i << logn) + n] = reduce_split(h0, m0, w0, P0);
-            pb[((size_t)(l + 1 + i) << logn) + n] = reduce_split(h1, m1, w1, P0);
+            r0 = make_ulonglong2(reduce_split(h[0], m[0], w[0], P0), reduce_split(h[1], m[1], w[1], P0));
+            r1 = make_ulonglong2(reduce_split(h[2], m[2], w[2], P0), reduce_split(h[3], m[3], w[3], P0));
         } else {
+            uint64_t lo[4] = {0, 0, 0, 0}, hi[4] = {0, 0, 0, 0};
+#pragma unroll 4
             for (int j = 0; j < l; ++j) {
-                const uint64_t dv = d[j * dstride];
-                mac128(lo0, hi0, dv, k0[j * kstride]);
-                mac128(lo1, hi1, dv, k0[j * kstride + kcomp]);
+                const ulonglong2 dv = d[j * dstride];
+                const ulonglong2 ka = k0[j * kstride], kb = k0[j * kstride + kcomp];
+                mac128(lo[0], hi[0], dv.x, ka.x);
+                mac128(lo[1], hi[1], dv.y, ka.y);
+                mac128(lo[2], hi[2], dv.x, kb.x);
+                mac128(lo[3], hi[3], dv.y, kb.y);
             }
-            pb[((size_t)i << logn) + n] = barrett_128(lo0, hi0, P0.q, P0.r0, P0.r1);
-            pb[((size_t)(l + 1 + i) << logn) + n] = barrett_128(lo1, hi1, P0.q, P0.r0, P0.r1);
+            r0 = make_ulonglong2(barrett_128(lo[0], hi[0], P0.q, P0.r0, P0.r1),
+                                 barrett_128(lo[1], hi[1], P0.q, P0.r0, P0.r1));
+            r1 = make_ulonglong2(barrett_128(lo[2], hi[2], P0.q, P0.r0, P0.r1),
+                                 barrett_128(lo[3], hi[3], P0.q, P0.r0, P0.r1));
         }
+        *reinterpret_cast<ulonglong2 *>(pb + ((size_t)i << logn)) = r0;
+        *reinterpret_cast<ulonglong2 *>(pb + ((size_t)(l + 1 + i) << logn)) = r1;
     }
 }
 
@@ -156,7 +171,7 @@ void ks_modup_inner(Context &c, uint64_t *t, int B, int l, const uint64_t *key, 
     ld.group = l + 1;
     ld.src_limbs = l;
     ntt_forward_loaded(c, D, Bs * l, LimbMap{l + 1, 0, sp}, ld, s);
-    size_t tot = Bs * (l + 1) * N;
+    size_t tot = Bs * (l + 1) * N / 2;
     if (c.small_primes && l <= 31)
         k_ks_inner<true><<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, tot);
     else
@@ -187,6 +202,7 @@ void switch_key_batch(Context &c, uint64_t *ct, int batch, int l, const uint64_t
 {
     if (l < 1 || l > c.k - 1) throw std::invalid_argument("switch_key: level out of range");
     if (batch < 1) return;
+    if (reinterpret_cast<uintptr_t>(key) & 15) throw std::invalid_argument("switch_key: the key must be 16-byte aligned");
     const size_t N = c.n, B = (size_t)batch;
     const int sp = c.k - 1;
     // scratch per ciphertext: t[l] | D[l][l+1] | P[2][l+1] | T[2][l] | last[2]
@@ -306,6 +322,10 @@ extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l,
                   "device buffer holds " + std::to_string(kNoAllocWords));
         return -1;
     }
+    if (reinterpret_cast<uintptr_t>(key) & 15) {
+        set_error(std::string(fn) + ": the key must be 16-byte aligned");
+        return -1;
+    }
     try {
         int dev = -1;
         if (cudaGetDevice(&dev) != cudaSuccess || dev != c.device)
@@ -324,7 +344,7 @@ extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l,
         size_t tot = (size_t)l * N;
         k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot); NEXUS_LAUNCHED();
         ntt_forward(c, D, l, LimbMap{l + 1, 0, sp}, s);
-        tot = (size_t)(l + 1) * N;
+        tot = (size_t)(l + 1) * N / 2;
         k_ks_inner<false><<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, 1, tot); NEXUS_LAUNCHED();
         cudaMemcpyAsync(last, P + (size_t)l * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(last + N, P + (size_t)(2 * l + 1) * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);

@@ -185,12 +185,16 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
         const size_t srow = pl / (size_t)ld.group;
         const uint64_t *sp = ld.src + (srow << logn) + col0;
         const uint64_t r1 = pc[prime].r1;
+        // On the small-prime path the spread values enter unreduced: they are
+        // below 2^53, the reduction-free stages add less than 3q each (below
+        // 2^58 after all 16) and the final Barrett step of the rows pass
+        // returns the canonical residue, so the output words are the same.
         if (KIND == 1) {
             const uint64_t qj = pc[(int)(srow % (size_t)ld.src_limbs)].q;
 #pragma unroll
             for (int k = 0; k < kE; ++k) {
                 const uint64_t v = sp[(size_t)(t + T * k) * n2 + c];
-                x[k] = (q < qj) ? barrett_64(v, q, r1) : v;
+                x[k] = (!SMALL && q < qj) ? barrett_64(v, q, r1) : v;
             }
         } else {
             const uint64_t P = pc[ld.special].q, h = P >> 1;
@@ -198,7 +202,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
 #pragma unroll
             for (int k = 0; k < kE; ++k) {
                 const uint64_t v = csub(sp[(size_t)(t + T * k) * n2 + c] + h, P);
-                x[k] = ((q < P) ? barrett_64(v, q, r1) : v) + (q - hr);
+                x[k] = ((!SMALL && q < P) ? barrett_64(v, q, r1) : v) + (q - hr);
             }
         }
     }

@@ -104,6 +104,37 @@ def test_switch_key_random(big, limbs):
     assert np.array_equal(to_host(d), want)
 
 
+@pytest.fixture(scope="module")
+def small(cuda):
+    """Every prime below 2^52: the reduction-free NTT and split inner product."""
+    from nexus_gb300 import Context
+    qs = po.create_coeff_modulus(N, [51, 46, 46, 46, 51, 51, 51, 51])
+    return Context(LOG_N, qs), po.OracleContext(LOG_N, qs), qs
+
+
+@pytest.mark.parametrize("chain", ["big", "small"])
+@pytest.mark.parametrize("limbs", [7, 2])
+def test_switch_key_batch(request, chain, limbs):
+    """nexus_switch_key_batch gives every ciphertext the single-call words."""
+    import torch
+    ctx, oc, qs = request.getfixturevalue(chain)
+    rng = np.random.default_rng(100 + limbs)
+    cts = [_rand_ct(rng, 2, limbs, qs) for _ in range(3)]
+    tgts = [_rand_ct(rng, 1, limbs, qs)[0] for _ in range(3)]
+    key = _rand_key(rng, qs)
+    d = to_dev(np.stack(cts))
+    t = to_dev(np.stack(tgts))
+    ctx.switch_key_batch(d, t, to_dev(key))
+    got = to_host(d)
+    for b in range(3):
+        assert np.array_equal(got[b], oc.switch_key(cts[b], tgts[b], key)), b
+    assert np.array_equal(to_host(t), np.stack(tgts)), "targets must be left unchanged"
+    with pytest.raises(RuntimeError):
+        ctx.switch_key_batch(d, d[:, 0], to_dev(key))
+    empty = torch.empty((0, 2, limbs, N), dtype=torch.int64, device="cuda")
+    ctx.switch_key_batch(empty, torch.empty((0, limbs, N), dtype=torch.int64, device="cuda"), to_dev(key))
+
+
 @pytest.mark.parametrize("limbs", [7, 3, 2])
 def test_rescale_random(big, limbs):
     import torch
