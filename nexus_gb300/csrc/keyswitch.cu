@@ -4,8 +4,8 @@
 //
 //   1. INTT of the target's l limbs (coefficient form, each in [0, q_j)).
 //   2. ModUp: digit j is reduced into every prime of {q_0..q_{l-1}, p} and
-//      transformed: D[j][i] = NTT_i(t_j mod q_i).  (For i == j this equals the
-//      target limb SEAL reuses.)
+//      transformed: D[j][i] = NTT_i(t_j mod q_i).  For i == j this is the
+//      target limb itself, which SEAL reuses; it is copied, not transformed.
 //   3. Inner product with the key, 128-bit accumulation, one Barrett
 //      reduction: P[k][i] = sum_j D[j][i] * key[j][k][i] mod q_i.
 //   4. ModDown with rounding: ct[k][i] += (P[k][i] - NTT_i(((INTT_p(P[k][p]) + p/2)
@@ -47,6 +47,19 @@ __global__ void k_modup_spread(const uint64_t *__restrict__ t, uint64_t *__restr
             const PrimeConst P = pc[i == l ? sp : i];
             o[(size_t)i << logn] = (P.q < qj) ? barrett_64(v, P.q, P.r1) : v;
         }
+    }
+}
+
+// D[b][j][j] = t[b][j] for the rows of t (B*l rows, row = b*l + j): digit j's
+// own limb of the ModUp is the NTT-form target limb, as in SEAL
+__global__ void k_modup_diag(const ulonglong2 *__restrict__ t, ulonglong2 *__restrict__ D, int l, int logn,
+                             size_t total)
+{
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = x >> (logn - 1);
+        const size_t n2 = x & (((size_t)1 << (logn - 1)) - 1);
+        const size_t j = row % (size_t)l;
+        D[((row * (size_t)(l + 1) + j) << (logn - 1)) + n2] = t[x];
     }
 }
 
@@ -163,14 +176,20 @@ void ks_modup_inner(Context &c, uint64_t *t, int B, int l, const uint64_t *key, 
 {
     const size_t N = c.n, Bs = (size_t)B;
     const int sp = c.k - 1;
+    // digit j's limb j is the target limb itself (SEAL reuses it for CKKS):
+    // copy it across and leave it out of the forward transform
+    const size_t pairs = Bs * l * N / 2;
+    k_modup_diag<<<grid_for(pairs), kBlock, 0, s>>>(reinterpret_cast<const ulonglong2 *>(t),
+                                                    reinterpret_cast<ulonglong2 *>(D), l, c.logn, pairs);
+    NEXUS_LAUNCHED();
     ntt_inverse(c, t, Bs, LimbMap{l, 0, -1}, s);
     // ModUp spread fused into the first pass of the forward NTT
     NttLoader ld;
     ld.kind = 1;
     ld.src = t;
-    ld.group = l + 1;
+    ld.group = l;
     ld.src_limbs = l;
-    ntt_forward_loaded(c, D, Bs * l, LimbMap{l + 1, 0, sp}, ld, s);
+    ntt_forward_loaded(c, D, Bs * l, LimbMap{l, 0, sp, 1}, ld, s);
     size_t tot = Bs * (l + 1) * N / 2;
     if (c.small_primes && l <= 31)
         k_ks_inner<true><<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, tot);

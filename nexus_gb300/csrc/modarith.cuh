@@ -59,6 +59,17 @@ __device__ __forceinline__ uint64_t barrett_64(uint64_t x, uint64_t q, uint64_t 
     return csub(x - t * q, q);
 }
 
+// barrett_64 for q > 2^32, where r1 = floor(2^64/q) fits in 32 bits: the
+// same quotient floor(x * r1 / 2^64), formed exactly from two 32 x 32-bit
+// products (x * r1 = x1 * r1 * 2^32 + x0 * r1), so the same result.
+__device__ __forceinline__ uint64_t barrett_64_r32(uint64_t x, uint64_t q, uint32_t r1)
+{
+    const uint32_t x0 = (uint32_t)x, x1 = (uint32_t)(x >> 32);
+    const uint64_t lo = (uint64_t)x0 * r1;
+    const uint32_t t = (uint32_t)(((uint64_t)x1 * r1 + (lo >> 32)) >> 32);
+    return csub(x - (uint64_t)t * q, q);
+}
+
 #endif  // __CUDACC__
 
 // Per-prime constants stored on the device.

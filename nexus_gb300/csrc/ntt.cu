@@ -169,12 +169,14 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
     __shared__ uint64_t sm[S * C];
     const int n2 = 1 << (logn - LOGS);
     const int tiles = n2 / C;
-    const size_t pl = blockIdx.x / tiles;
-    const int col0 = (blockIdx.x % tiles) * C;
-    const int prime = lm.prime((int)(pl % (size_t)lm.count));
+    const uint32_t pl = blockIdx.x / (uint32_t)tiles;
+    const int col0 = (int)(blockIdx.x - pl * (uint32_t)tiles) * C;
+    size_t lrow;
+    int prime;
+    lm.locate(pl, lrow, prime);
     const uint64_t q = pc[prime].q, q2 = q << 1;
     const ulonglong2 *W = tw + ((size_t)prime << logn);
-    uint64_t *p = data + (pl << logn) + col0;
+    uint64_t *p = data + (lrow << logn) + col0;
     const int c = threadIdx.x % C, t = threadIdx.x / C;
 
     uint64_t x[kE];
@@ -182,15 +184,15 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
 #pragma unroll
         for (int k = 0; k < kE; ++k) x[k] = p[(size_t)(t + T * k) * n2 + c];
     } else {
-        const size_t srow = pl / (size_t)ld.group;
-        const uint64_t *sp = ld.src + (srow << logn) + col0;
+        const uint32_t srow = pl / (uint32_t)ld.group;
+        const uint64_t *sp = ld.src + ((size_t)srow << logn) + col0;
         const uint64_t r1 = pc[prime].r1;
         // On the small-prime path the spread values enter unreduced: they are
         // below 2^53, the reduction-free stages add less than 3q each (below
         // 2^58 after all 16) and the final Barrett step of the rows pass
         // returns the canonical residue, so the output words are the same.
         if (KIND == 1) {
-            const uint64_t qj = pc[(int)(srow % (size_t)ld.src_limbs)].q;
+            const uint64_t qj = pc[(int)(srow % (uint32_t)ld.src_limbs)].q;
 #pragma unroll
             for (int k = 0; k < kE; ++k) {
                 const uint64_t v = sp[(size_t)(t + T * k) * n2 + c];
@@ -228,12 +230,14 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
     const int log_n1 = logn - LOGS;
     const int rr = threadIdx.x / T, t = threadIdx.x % T;
     const size_t grow = (size_t)blockIdx.x * R + rr;
-    const size_t pl = grow >> log_n1;
+    const uint32_t pl = (uint32_t)(grow >> log_n1);
     const uint64_t r = grow & ((1u << log_n1) - 1);
-    const int prime = lm.prime((int)(pl % (size_t)lm.count));
+    size_t lrow;
+    int prime;
+    lm.locate(pl, lrow, prime);
     const uint64_t q = pc[prime].q, q2 = q << 1;
     const ulonglong2 *W = tw + ((size_t)prime << logn);
-    uint64_t *p = data + grow * S;
+    uint64_t *p = data + (lrow << logn) + r * S;
     uint64_t *srow = sm + rr * SP;
     const uint64_t B = (1ull << log_n1) + r;
 
@@ -249,8 +253,13 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
     fwd_regs_blocked<T, SMALL>(x, W, B, t, q, q2);
     if (SMALL) {
         const uint64_t r1 = pc[prime].r1;
+        if (r1 >> 32) {
 #pragma unroll
-        for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = barrett_64(x[k], q, r1);
+            for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = barrett_64(x[k], q, r1);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = barrett_64_r32(x[k], q, (uint32_t)r1);
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = csub(csub(x[k], q2), q);
@@ -272,12 +281,14 @@ __global__ void __launch_bounds__(kThreads, 3) k_inv_rows(uint64_t *__restrict__
     const int log_n1 = logn - LOGS;
     const int rr = threadIdx.x / T, t = threadIdx.x % T;
     const size_t grow = (size_t)blockIdx.x * R + rr;
-    const size_t pl = grow >> log_n1;
+    const uint32_t pl = (uint32_t)(grow >> log_n1);
     const uint64_t r = grow & ((1u << log_n1) - 1);
-    const int prime = lm.prime((int)(pl % (size_t)lm.count));
+    size_t lrow;
+    int prime;
+    lm.locate(pl, lrow, prime);
     const uint64_t q = pc[prime].q, q2 = q << 1;
     const ulonglong2 *W = tw + ((size_t)prime << logn);
-    uint64_t *p = data + grow * S;
+    uint64_t *p = data + (lrow << logn) + r * S;
     uint64_t *srow = sm + rr * SP;
     const uint64_t B = (1ull << log_n1) + r;
 
@@ -307,13 +318,15 @@ __global__ void __launch_bounds__(kThreads) k_inv_cols(uint64_t *__restrict__ da
     __shared__ uint64_t sm[S * C];
     const int n2 = 1 << (logn - LOGS);
     const int tiles = n2 / C;
-    const size_t pl = blockIdx.x / tiles;
-    const int col0 = (blockIdx.x % tiles) * C;
-    const int prime = lm.prime((int)(pl % (size_t)lm.count));
+    const uint32_t pl = blockIdx.x / (uint32_t)tiles;
+    const int col0 = (int)(blockIdx.x - pl * (uint32_t)tiles) * C;
+    size_t lrow;
+    int prime;
+    lm.locate(pl, lrow, prime);
     const PrimeConst P = pc[prime];
     const uint64_t q = P.q, q2 = q << 1;
     const ulonglong2 *W = tw + ((size_t)prime << logn);
-    uint64_t *p = data + (pl << logn) + col0;
+    uint64_t *p = data + (lrow << logn) + col0;
     const int c = threadIdx.x % C, t = threadIdx.x / C;
 
     uint64_t x[kE];
@@ -379,9 +392,18 @@ static void timing_mark(const Context &c, cudaStream_t s)
     c.ntt_events.push_back(e);
 }
 
+// every launch indexes its limbs and CTAs with 32-bit integers
+static void check_launch_size(const Context &c, size_t n_polys, const LimbMap &lm)
+{
+    const size_t blocks_per_limb = c.n / ((size_t)kThreads * kE);   // CTAs per limb of either pass
+    if (n_polys * (size_t)lm.count * (blocks_per_limb ? blocks_per_limb : 1) >= (size_t)1 << 31)
+        throw std::invalid_argument("NTT: too many limbs in one call");
+}
+
 void ntt_forward_loaded(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, NttLoader ld, cudaStream_t s)
 {
     if (n_polys == 0 || lm.count == 0) return;
+    check_launch_size(c, n_polys, lm);
     if (c.ntt_timing) {
         timing_mark(c, s);
         c.ntt_limbs.push_back(n_polys * lm.count);
@@ -405,6 +427,7 @@ void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cuda
 void ntt_inverse(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s)
 {
     if (n_polys == 0 || lm.count == 0) return;
+    check_launch_size(c, n_polys, lm);
     if (c.ntt_timing) {
         timing_mark(c, s);
         c.ntt_limbs.push_back(n_polys * lm.count);

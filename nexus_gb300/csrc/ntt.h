@@ -11,13 +11,35 @@ namespace nexus {
 // Which prime each limb of a polynomial uses: limb l < count-1 (or every
 // limb when special_last < 0) uses prime begin + l; with special_last >= 0 the
 // last limb uses prime special_last (the ModUp layout q_0..q_{l-1}, p).
+//
+// skip_diag: the polynomials are the digits of a ModUp, stored with count + 1
+// limbs each ([B][count digits][count + 1][N], the last limb on special_last)
+// and digit j's limb j is left out of the transform (it is the NTT-form
+// target limb itself).  The transform then covers count limbs per digit:
+// launch limb m of digit j is stored limb m + (m >= j).
 struct LimbMap {
     int count;
     int begin;
     int special_last;
+    int skip_diag = 0;
     __host__ __device__ int prime(int l) const
     {
         return (special_last >= 0 && l == count - 1) ? special_last : begin + l;
+    }
+    // Memory row (limb index from the start of the buffer) and prime of
+    // launch limb pl; launches hold fewer than 2^32 limbs.
+    __host__ __device__ void locate(uint32_t pl, size_t &row, int &p) const
+    {
+        const uint32_t cnt = (uint32_t)count;
+        const uint32_t poly = pl / cnt, m = pl - poly * cnt;
+        if (!skip_diag) {
+            row = pl;
+            p = prime((int)m);
+            return;
+        }
+        const uint32_t j = poly % cnt, i = m + (m >= j ? 1u : 0u);
+        row = (size_t)poly * (cnt + 1) + i;
+        p = (i == cnt) ? special_last : begin + (int)i;
     }
 };
 
