@@ -80,36 +80,41 @@ __device__ __forceinline__ uint64_t reduce_split(uint64_t hh, uint64_t mid, uint
 }
 
 // P[b][k][i'][n] = sum_j D[b][j][i'][n] * key[j][k][kidx(i')][n] mod q(i')
-// Rows run i'-major over the batch (row = i' * B + b), so the ciphertexts of a
-// batch read the key rows of one prime (2l limbs) back to back, from L2.  Each
-// thread owns two neighbouring coefficients (16-byte loads) and the digit loop
-// is unrolled so that several rows' loads are in flight at once: the kernel is
-// bound by the latency of its D and key reads.
+// One CTA covers 512 coefficients (two per thread, 16-byte loads) of one
+// (b, i') pair; CTAs run i'-major, then by coefficient chunk, with the batch
+// index fastest, so the B CTAs that read one chunk of the key rows run back
+// to back and all but the first find it in L2.  The kernel is bound by its D
+// reads; the register cap keeps four CTAs (32 warps) per SM in flight on the
+// small-prime path, three with 128-bit accumulators.
+constexpr int kInnerCoeffs = 2 * kBlock;
+
 template <bool SPLIT>
-__global__ void k_ks_inner(const uint64_t *__restrict__ D, const uint64_t *__restrict__ key, uint64_t *__restrict__ P,
-                           const PrimeConst *__restrict__ pc, int l, int K, int logn, int B, size_t total)
+__global__ void __launch_bounds__(kBlock, SPLIT ? 4 : 3)
+    k_ks_inner(const uint64_t *__restrict__ D, const uint64_t *__restrict__ key, uint64_t *__restrict__ P,
+               const PrimeConst *__restrict__ pc, int l, int K, int logn, int B, unsigned nblocks)
 {
-    const size_t N = (size_t)1 << logn;
-    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
-        const size_t row = x >> (logn - 1);      // i * B + b
-        const size_t b = row % (size_t)B;
-        const int i = (int)(row / (size_t)B);
-        const size_t n = (x & ((N >> 1) - 1)) << 1;
+    const int log_chunks = logn - 9;
+    for (unsigned blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
+        const unsigned b = blk % (unsigned)B, rest = blk / (unsigned)B;
+        const unsigned chunk = rest & ((1u << log_chunks) - 1);
+        const int i = (int)(rest >> log_chunks);
+        const size_t n = ((size_t)chunk * kInnerCoeffs) + 2 * threadIdx.x;
         const int kidx = (i == l) ? K - 1 : i;
         const PrimeConst P0 = pc[kidx];
-        const ulonglong2 *d = reinterpret_cast<const ulonglong2 *>(D + ((b * l * (l + 1) + i) << logn) + n);
+        const ulonglong2 *d =
+            reinterpret_cast<const ulonglong2 *>(D + (((size_t)b * l * (l + 1) + i) << logn) + n);
         const ulonglong2 *k0 = reinterpret_cast<const ulonglong2 *>(key + ((size_t)kidx << logn) + n);
         const size_t dstride = ((size_t)(l + 1) << logn) >> 1;   // in ulonglong2
         const size_t kstride = ((size_t)2 * K << logn) >> 1;
         const size_t kcomp = ((size_t)K << logn) >> 1;
-        uint64_t *pb = P + ((b * 2 * (l + 1)) << logn) + n;
+        uint64_t *pb = P + (((size_t)b * 2 * (l + 1)) << logn) + n;
         ulonglong2 r0, r1;
         if (SPLIT) {
             // every residue below 2^52: each product as four 26 x 26-bit
             // partial products summed exactly in three 64-bit accumulators
             // (< 2 * 31 * 2^52 each), one recombination and reduction at the end
             uint64_t h[4] = {0, 0, 0, 0}, m[4] = {0, 0, 0, 0}, w[4] = {0, 0, 0, 0};
-#pragma unroll 4
+#pragma unroll 2
             for (int j = 0; j < l; ++j) {
                 const ulonglong2 dv = d[j * dstride];
                 const ulonglong2 ka = k0[j * kstride], kb = k0[j * kstride + kcomp];
@@ -128,7 +133,7 @@ __global__ void k_ks_inner(const uint64_t *__restrict__ D, const uint64_t *__res
             r1 = make_ulonglong2(reduce_split(h[2], m[2], w[2], P0), reduce_split(h[3], m[3], w[3], P0));
         } else {
             uint64_t lo[4] = {0, 0, 0, 0}, hi[4] = {0, 0, 0, 0};
-#pragma unroll 4
+#pragma unroll 2
             for (int j = 0; j < l; ++j) {
                 const ulonglong2 dv = d[j * dstride];
                 const ulonglong2 ka = k0[j * kstride], kb = k0[j * kstride + kcomp];
@@ -145,6 +150,20 @@ __global__ void k_ks_inner(const uint64_t *__restrict__ D, const uint64_t *__res
         *reinterpret_cast<ulonglong2 *>(pb + ((size_t)i << logn)) = r0;
         *reinterpret_cast<ulonglong2 *>(pb + ((size_t)(l + 1 + i) << logn)) = r1;
     }
+}
+
+// launch of k_ks_inner over B ciphertexts at l limbs
+void launch_ks_inner(const Context &c, const uint64_t *D, const uint64_t *key, uint64_t *P, int l, int B,
+                     cudaStream_t s)
+{
+    static_assert(kInnerCoeffs == 512, "k_ks_inner maps 512 coefficients to a CTA");
+    if (c.logn < 9) throw std::invalid_argument("key switching needs N >= 512");
+    const unsigned nb = (unsigned)((size_t)B * (l + 1) << (c.logn - 9));
+    if (c.small_primes && l <= 31)
+        k_ks_inner<true><<<nb, kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, nb);
+    else
+        k_ks_inner<false><<<nb, kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, nb);
+    NEXUS_LAUNCHED();
 }
 
 // ct[kb][i] += (P[kb][i] - T[kb][i]) * p^{-1} mod q_i with kb = 2*b + k over the
@@ -190,12 +209,7 @@ void ks_modup_inner(Context &c, uint64_t *t, int B, int l, const uint64_t *key, 
     ld.group = l;
     ld.src_limbs = l;
     ntt_forward_loaded(c, D, Bs * l, LimbMap{l, 0, sp, 1}, ld, s);
-    size_t tot = Bs * (l + 1) * N / 2;
-    if (c.small_primes && l <= 31)
-        k_ks_inner<true><<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, tot);
-    else
-        k_ks_inner<false><<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, tot);
-    NEXUS_LAUNCHED();
+    launch_ks_inner(c, D, key, P, l, B, s);
 }
 
 // Stage 2: the rounding terms T [B][2][l][N] of the ModDown from the special
@@ -363,8 +377,7 @@ extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l,
         size_t tot = (size_t)l * N;
         k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot); NEXUS_LAUNCHED();
         ntt_forward(c, D, l, LimbMap{l + 1, 0, sp}, s);
-        tot = (size_t)(l + 1) * N / 2;
-        k_ks_inner<false><<<grid_for(tot), kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, 1, tot); NEXUS_LAUNCHED();
+        launch_ks_inner(c, D, key, P, l, 1, s);
         cudaMemcpyAsync(last, P + (size_t)l * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(last + N, P + (size_t)(2 * l + 1) * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
         ntt_inverse(c, last, 2, LimbMap{1, sp, -1}, s);
