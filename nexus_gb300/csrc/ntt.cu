@@ -226,6 +226,9 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
                                                        const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
 {
     constexpr int S = 1 << LOGS, T = S / kE, R = kThreads / T, SP = S + S / 16;
+    // the T threads of a row sit in one warp and share only their row's
+    // slice of shared memory, so warp barriers order the exchanges
+    static_assert(32 % T == 0, "a row's threads must lie inside one warp");
     __shared__ uint64_t sm[R * SP];
     const int log_n1 = logn - LOGS;
     const int rr = threadIdx.x / T, t = threadIdx.x % T;
@@ -247,7 +250,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
     fwd_regs_strided<SMALL>(x, W, B, q, q2);
 #pragma unroll
     for (int k = 0; k < kE; ++k) srow[swz(t + T * k)] = x[k];
-    __syncthreads();
+    __syncwarp();
 #pragma unroll
     for (int k = 0; k < kE; ++k) x[k] = srow[swz(kE * t + k)];
     fwd_regs_blocked<T, SMALL>(x, W, B, t, q, q2);
@@ -264,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
 #pragma unroll
         for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = csub(csub(x[k], q2), q);
     }
-    __syncthreads();
+    __syncwarp();
 #pragma unroll
     for (int k = 0; k < kE; ++k) p[t + T * k] = srow[swz(t + T * k)];
 }
@@ -277,6 +280,9 @@ __global__ void __launch_bounds__(kThreads, 3) k_inv_rows(uint64_t *__restrict__
                                                        const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
 {
     constexpr int S = 1 << LOGS, T = S / kE, R = kThreads / T, SP = S + S / 16;
+    // the T threads of a row sit in one warp and share only their row's
+    // slice of shared memory, so warp barriers order the exchanges
+    static_assert(32 % T == 0, "a row's threads must lie inside one warp");
     __shared__ uint64_t sm[R * SP];
     const int log_n1 = logn - LOGS;
     const int rr = threadIdx.x / T, t = threadIdx.x % T;
@@ -295,13 +301,13 @@ __global__ void __launch_bounds__(kThreads, 3) k_inv_rows(uint64_t *__restrict__
     uint64_t x[kE];
 #pragma unroll
     for (int k = 0; k < kE; ++k) srow[swz(t + T * k)] = p[t + T * k];
-    __syncthreads();
+    __syncwarp();
 #pragma unroll
     for (int k = 0; k < kE; ++k) x[k] = srow[swz(kE * t + k)];
     inv_regs_blocked<T>(x, W, B, t, q, q2);
 #pragma unroll
     for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = x[k];
-    __syncthreads();
+    __syncwarp();
 #pragma unroll
     for (int k = 0; k < kE; ++k) x[k] = srow[swz(t + T * k)];
     inv_regs_strided(x, W, B, q, q2);
