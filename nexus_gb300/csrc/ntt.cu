@@ -38,35 +38,35 @@ __device__ __forceinline__ void ct_bfly(uint64_t &x, uint64_t &y, ulonglong2 w, 
     y = u + q2 - v;
 }
 
-// Lazy product for primes below 2^52: the Shoup quotient estimate from three of
-// the four 32-bit partial products of y * wq (the dropped low x low term moves
-// the estimate down by at most one), so the result is congruent to y*w and
-// lies in [0, 3q).
-__device__ __forceinline__ uint64_t mul_shoup_lazy3(uint64_t y, uint64_t w, uint64_t wq, uint64_t q)
+// Lazy product for primes below 2^52: the Shoup quotient estimate
+// floor(y * wq / 2^64) from the high halves of the three upper 32-bit partial
+// products of y * wq.  Each dropped low half (and the dropped low x low
+// product) is below one unit of the estimate, so it is at most two below the
+// exact Shoup quotient, which is itself at most one below floor(y*w/q): the
+// result is congruent to y*w and lies in [0, 4q).
+__device__ __forceinline__ uint64_t mul_shoup_lazy4(uint64_t y, uint64_t w, uint64_t wq, uint64_t q)
 {
     const uint32_t y0 = (uint32_t)y, y1 = (uint32_t)(y >> 32), b0 = (uint32_t)wq, b1 = (uint32_t)(wq >> 32);
-    const uint64_t m1 = (uint64_t)y1 * b0, m2 = (uint64_t)y0 * b1;
-    const uint64_t mid = m1 + m2;
-    const uint64_t hi = (uint64_t)y1 * b1 + (mid >> 32) + ((uint64_t)(mid < m1) << 32);
+    const uint64_t hi = (uint64_t)y1 * b1 + __umulhi(y1, b0) + __umulhi(y0, b1);
     return y * w - hi * q;
 }
 
 // Cooley-Tukey butterfly without reductions for primes below 2^52: each stage
-// adds less than 3q to the largest value, so 16 stages from [0, 2q) stay below
-// 50q < 2^58.
-__device__ __forceinline__ void ct_bfly_small(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q, uint64_t q3)
+// adds less than 4q to the largest value, so 16 stages from below 2^53 stay
+// below 2^53 + 64q < 2^59.
+__device__ __forceinline__ void ct_bfly_small(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q, uint64_t q4)
 {
-    const uint64_t v = mul_shoup_lazy3(y, w.x, w.y, q);
+    const uint64_t v = mul_shoup_lazy4(y, w.x, w.y, q);
     const uint64_t u = x;
     x = u + v;
-    y = u + q3 - v;
+    y = u + q4 - v;
 }
 
 template <bool SMALL>
 __device__ __forceinline__ void fwd_bfly(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q, uint64_t q2)
 {
     if (SMALL)
-        ct_bfly_small(x, y, w, q, q2 + q);
+        ct_bfly_small(x, y, w, q, q2 << 1);
     else
         ct_bfly(x, y, w, q, q2);
 }
@@ -188,8 +188,8 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
         const uint64_t *sp = ld.src + ((size_t)srow << logn) + col0;
         const uint64_t r1 = pc[prime].r1;
         // On the small-prime path the spread values enter unreduced: they are
-        // below 2^53, the reduction-free stages add less than 3q each (below
-        // 2^58 after all 16) and the final Barrett step of the rows pass
+        // below 2^53, the reduction-free stages add less than 4q each (below
+        // 2^59 after all 16) and the final Barrett step of the rows pass
         // returns the canonical residue, so the output words are the same.
         if (KIND == 1) {
             const uint64_t qj = pc[(int)(srow % (uint32_t)ld.src_limbs)].q;
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
 }
 
 // Pass 2: size-2^LOGS transforms along contiguous rows, then the final
-// reduction to [0,q) (from [0,4q), or from [0,50q) on the small-prime path).
+// reduction to [0,q) (from [0,4q), or from below 2^59 on the small-prime path).
 template <int LOGS, bool SMALL>
 __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
                                                        const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
