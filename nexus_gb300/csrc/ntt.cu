@@ -30,6 +30,52 @@ namespace {
 constexpr int kE = 16;          // residues per thread
 constexpr int kThreads = 256;   // threads per CTA
 
+// Every CTA of either pass covers kThreads * kE residues (32 KB): 256 lines of
+// 128 bytes.  Before its own work each CTA asks L2 for the tile of the CTA one
+// residency wave ahead (the CTA that will take its slot), one line per thread,
+// so that CTA's loads find their data in L2 instead of waiting on HBM.  A
+// prefetch is only a hint: nothing waits for it.
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+__device__ __forceinline__ unsigned sm_count()
+{
+    unsigned n;
+    asm("mov.u32 %0, %%nsmid;" : "=r"(n));
+    return n;
+}
+
+// the tile of CTA fb in a columns pass: S rows of C residues, row stride n2
+template <int S, int C>
+__device__ __forceinline__ void prefetch_cols_tile(const uint64_t *data, unsigned fb, int logn, int n2, int tiles,
+                                                   const LimbMap &lm)
+{
+    const uint32_t pl = fb / (uint32_t)tiles;
+    const int col0 = (int)(fb - pl * (uint32_t)tiles) * C;
+    size_t lrow;
+    int prime;
+    lm.locate(pl, lrow, prime);
+    constexpr int kLinesPerRow = C / 16;
+    const int row = threadIdx.x / kLinesPerRow, sub = threadIdx.x % kLinesPerRow;
+    prefetch_l2(data + (lrow << logn) + col0 + (size_t)row * n2 + sub * 16);
+}
+
+// the tile of CTA fb in a rows pass: R contiguous rows of S residues
+template <int S, int R>
+__device__ __forceinline__ void prefetch_rows_tile(const uint64_t *data, unsigned fb, int logn, int log_n1,
+                                                   const LimbMap &lm)
+{
+    const size_t grow = (size_t)fb * R;
+    const uint32_t pl = (uint32_t)(grow >> log_n1);
+    const uint64_t r = grow & ((1u << log_n1) - 1);
+    size_t lrow;
+    int prime;
+    lm.locate(pl, lrow, prime);
+    prefetch_l2(data + (lrow << logn) + r * S + (size_t)threadIdx.x * 16);
+}
+
 __device__ __forceinline__ void ct_bfly(uint64_t &x, uint64_t &y, ulonglong2 w, uint64_t q, uint64_t q2)
 {
     uint64_t u = csub(x, q2);
@@ -181,6 +227,9 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
 
     uint64_t x[kE];
     if (KIND == 0) {
+        static_assert(S * C == kThreads * kE, "a columns tile is kThreads * kE residues");
+        const unsigned fb = blockIdx.x + 3 * sm_count();
+        if (fb < gridDim.x) prefetch_cols_tile<S, C>(data, fb, logn, n2, tiles, lm);
 #pragma unroll
         for (int k = 0; k < kE; ++k) x[k] = p[(size_t)(t + T * k) * n2 + c];
     } else {
@@ -243,6 +292,10 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
     uint64_t *p = data + (lrow << logn) + r * S;
     uint64_t *srow = sm + rr * SP;
     const uint64_t B = (1ull << log_n1) + r;
+    {
+        const unsigned fb = blockIdx.x + 3 * sm_count();
+        if (fb < gridDim.x) prefetch_rows_tile<S, R>(data, fb, logn, log_n1, lm);
+    }
 
     uint64_t x[kE];
 #pragma unroll
@@ -297,6 +350,10 @@ __global__ void __launch_bounds__(kThreads, 3) k_inv_rows(uint64_t *__restrict__
     uint64_t *p = data + (lrow << logn) + r * S;
     uint64_t *srow = sm + rr * SP;
     const uint64_t B = (1ull << log_n1) + r;
+    {
+        const unsigned fb = blockIdx.x + 3 * sm_count();
+        if (fb < gridDim.x) prefetch_rows_tile<S, R>(data, fb, logn, log_n1, lm);
+    }
 
     uint64_t x[kE];
 #pragma unroll
@@ -334,6 +391,11 @@ __global__ void __launch_bounds__(kThreads) k_inv_cols(uint64_t *__restrict__ da
     const ulonglong2 *W = tw + ((size_t)prime << logn);
     uint64_t *p = data + (lrow << logn) + col0;
     const int c = threadIdx.x % C, t = threadIdx.x / C;
+
+    {
+        const unsigned fb = blockIdx.x + 3 * sm_count();
+        if (fb < gridDim.x) prefetch_cols_tile<S, C>(data, fb, logn, n2, tiles, lm);
+    }
 
     uint64_t x[kE];
 #pragma unroll
