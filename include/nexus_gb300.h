@@ -432,6 +432,17 @@ int nexus_bootstrap_batch(nexus_bootstrapper *bs, nexus_ciphertext *const *cts, 
 int nexus_bootstrapper_stage(nexus_bootstrapper *bs, int stage, nexus_ciphertext *a, const nexus_ciphertext *b,
                              nexus_ciphertext *r1, nexus_ciphertext *r2);
 
+/* The same stages run in lockstep over `count` ciphertexts of one size, level
+ * and scale: a[k] (and b[k] for SLOTTOCOEFF) in, r1[k] / r2[k] out, each
+ * receiving the words nexus_bootstrapper_stage gives for a[k] alone; MODRAISE
+ * updates every a[k] in place and SET_INITIAL_SCALE takes the shared scale.
+ * The lockstep form keeps its own initial scale (set it with this call before
+ * a lockstep SLOTTOCOEFF).  No counterpart in the reference (it has no
+ * lockstep form). */
+int nexus_bootstrapper_stage_batch(nexus_bootstrapper *bs, int stage, nexus_ciphertext *const *a,
+                                   const nexus_ciphertext *const *b, int count, nexus_ciphertext *const *r1,
+                                   nexus_ciphertext *const *r2);
+
 /* ArgmaxEvaluator::argmax (src/argmax.cpp:9-81) with the bootstrapper's
  * evaluator and keys: slots 0..len-1 of x -> the one-hot indicator of the
  * maximum (sgn(x - max) + 1), bootstrapping after every round.  x is updated

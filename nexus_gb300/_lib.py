@@ -89,6 +89,8 @@ SIGNATURES = [
     ("nexus_argmax", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("nexus_bootstrap_batch", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("nexus_bootstrapper_stage", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("nexus_bootstrapper_stage_batch", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                                 C.c_void_p]),
     ("nexus_bootstrapper_cached_plaintexts", C.c_int, [C.c_void_p, u64p]),
     ("nexus_seal_ciphertext_save", C.c_int, [u64p, C.c_int, C.c_int, C.c_int, C.c_double, u64p, C.c_int,
                                              C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),

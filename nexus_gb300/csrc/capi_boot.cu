@@ -39,6 +39,21 @@ int guarded(const char *fn, F &&f)
     return 0;
 }
 
+// the lockstep form of bs, built from its setup on first use
+BatchBootstrapper &lockstep_form(nexus_bootstrapper *bs)
+{
+    Bootstrapper &S = bs->bs;
+    if (S.fftcoeff1.empty()) throw std::logic_error("generate_LT_coefficient_3 has not been called");
+    if (!bs->bbs) {
+        bs->bev.reset(new BatchEvaluator(bs->ev->ev));
+        bs->bbs.reset(new BatchBootstrapper(*bs->bev, S.loge, S.logn, S.logNh, S.L, S.final_scale, S.boundary_K,
+                                            S.sin_cos_deg, S.scale_factor, S.inverse_deg));
+        bs->bbs->adopt_setup(S);
+    }
+    bs->bbs->set_final_scale(S.final_scale);
+    return *bs->bbs;
+}
+
 }  // namespace
 
 extern "C" int nexus_bootstrapper_create(nexus_evaluator *ev, long loge, long logn, long logNh, long L,
@@ -157,15 +172,7 @@ extern "C" int nexus_bootstrap_batch(nexus_bootstrapper *bs, nexus_ciphertext *c
             if (rtn[b] == cts[j]) return fail(fn, "rtn must not alias an input");
     }
     return guarded(fn, [&] {
-        Bootstrapper &S = bs->bs;
-        if (S.fftcoeff1.empty()) throw std::logic_error("generate_LT_coefficient_3 has not been called");
-        if (!bs->bbs) {
-            bs->bev.reset(new BatchEvaluator(bs->ev->ev));
-            bs->bbs.reset(new BatchBootstrapper(*bs->bev, S.loge, S.logn, S.logNh, S.L, S.final_scale, S.boundary_K,
-                                                S.sin_cos_deg, S.scale_factor, S.inverse_deg));
-            bs->bbs->adopt_setup(S);
-        }
-        bs->bbs->set_final_scale(S.final_scale);
+        BatchBootstrapper &BB = lockstep_form(bs);
         const Ciphertext &first = cts[0]->ct;
         for (int b = 0; b < count; ++b) {
             const Ciphertext &c = cts[b]->ct;
@@ -182,7 +189,7 @@ extern "C" int nexus_bootstrap_batch(nexus_bootstrapper *bs, nexus_ciphertext *c
             if (cudaMemcpyAsync(in.ct(b), cts[b]->ct.data(), in.words_per_ct() * 8, cudaMemcpyDeviceToDevice, s) !=
                 cudaSuccess)
                 throw std::runtime_error("copy failed");
-        bs->bbs->bootstrap_3(out, in);
+        BB.bootstrap_3(out, in);
         for (int b = 0; b < count; ++b) {
             Ciphertext &r = rtn[b]->ct;
             r.resize(ctx, out.size(), out.limbs(), s);
@@ -237,6 +244,67 @@ extern "C" int nexus_bootstrapper_stage(nexus_bootstrapper *bs, int stage, nexus
             break;
         case NEXUS_BOOT_SET_INITIAL_SCALE:
             B.initial_scale = a->ct.scale();
+            break;
+        default:
+            throw std::invalid_argument("unknown stage");
+        }
+    });
+}
+
+extern "C" int nexus_bootstrapper_stage_batch(nexus_bootstrapper *bs, int stage, nexus_ciphertext *const *a,
+                                              const nexus_ciphertext *const *b, int count, nexus_ciphertext *const *r1,
+                                              nexus_ciphertext *const *r2)
+{
+    static const char *fn = "nexus_bootstrapper_stage_batch";
+    if (!bs || !a || count < 1) return fail(fn, "null argument");
+    for (int k = 0; k < count; ++k) {
+        if (!a[k]) return fail(fn, "null ciphertext");
+        if (const char *e = input_problem(bs->ev->ctx, a[k])) return fail(fn, e);
+        if (b) {
+            if (!b[k]) return fail(fn, "null ciphertext");
+            if (const char *e = input_problem(bs->ev->ctx, b[k])) return fail(fn, e);
+        }
+        for (int j = 0; j < count; ++j) {
+            if ((r1 && r1[k] && (r1[k] == a[j] || (b && r1[k] == b[j]))) ||
+                (r2 && r2[k] && (r2[k] == a[j] || (b && r2[k] == b[j]))))
+                return fail(fn, "results must not alias inputs");
+        }
+    }
+    auto all = [&](nexus_ciphertext *const *r) {
+        if (!r) return false;
+        for (int k = 0; k < count; ++k)
+            if (!r[k]) return false;
+        return true;
+    };
+    return guarded(fn, [&] {
+        BatchBootstrapper &BB = lockstep_form(bs);
+        nexus_evaluator *ev = bs->ev;
+        CtBatch x = gather_batch(ev, a, count), o1, o2;
+        switch (stage) {
+        case NEXUS_BOOT_MODRAISE:
+            BB.modraise_inplace(x);
+            scatter_batch(ev, x, a);
+            break;
+        case NEXUS_BOOT_COEFFTOSLOT:
+            if (!all(r1) || !all(r2)) throw std::invalid_argument("null result");
+            BB.coefftoslot_full_3(o1, o2, x);
+            scatter_batch(ev, o1, r1);
+            scatter_batch(ev, o2, r2);
+            break;
+        case NEXUS_BOOT_MODULAR_REDUCTION:
+            if (!all(r1)) throw std::invalid_argument("null result");
+            BB.mod_reducer.modular_reduction(o1, x);
+            scatter_batch(ev, o1, r1);
+            break;
+        case NEXUS_BOOT_SLOTTOCOEFF: {
+            if (!b || !all(r1)) throw std::invalid_argument("null argument");
+            CtBatch y = gather_batch(ev, b, count);
+            BB.slottocoeff_full_3(o1, x, y);
+            scatter_batch(ev, o1, r1);
+            break;
+        }
+        case NEXUS_BOOT_SET_INITIAL_SCALE:
+            BB.initial_scale = x.scale();
             break;
         default:
             throw std::invalid_argument("unknown stage");

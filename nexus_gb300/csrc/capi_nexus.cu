@@ -175,42 +175,6 @@ namespace {
 
 using BatchCKKS = CKKSEvaluatorT<BatchEvaluator, CtBatch>;
 
-// gather `count` ciphertexts of one size, level and scale into a batch
-CtBatch gather(nexus_evaluator *ev, nexus_ciphertext *const *cts, int count)
-{
-    const Ciphertext &first = cts[0]->ct;
-    if (first.empty()) throw std::invalid_argument("empty ciphertext");
-    for (int b = 1; b < count; ++b) {
-        const Ciphertext &c = cts[b]->ct;
-        if (c.size() != first.size() || c.limbs() != first.limbs())
-            throw std::invalid_argument("the ciphertexts of a batch must share one size and level");
-        if (c.scale() != first.scale()) throw std::invalid_argument("the ciphertexts of a batch must share one scale");
-    }
-    Context &ctx = ev->ctx->c;
-    cudaStream_t s = ev->ev.stream();
-    CtBatch in;
-    in.resize(ctx, count, first.size(), first.limbs(), s);
-    in.scale() = first.scale();
-    for (int b = 0; b < count; ++b)
-        if (cudaMemcpyAsync(in.ct(b), cts[b]->ct.data(), in.words_per_ct() * 8, cudaMemcpyDeviceToDevice, s) !=
-            cudaSuccess)
-            throw std::runtime_error("copy failed");
-    return in;
-}
-
-void scatter(nexus_evaluator *ev, const CtBatch &out, nexus_ciphertext *const *res)
-{
-    Context &ctx = ev->ctx->c;
-    cudaStream_t s = ev->ev.stream();
-    for (int b = 0; b < out.batch(); ++b) {
-        Ciphertext &r = res[b]->ct;
-        r.resize(ctx, out.size(), out.limbs(), s);
-        r.scale() = out.scale();
-        if (cudaMemcpyAsync(r.data(), out.ct(b), out.words_per_ct() * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
-            throw std::runtime_error("copy failed");
-    }
-}
-
 int check_batch(const char *fn, nexus_evaluator *ev, nexus_ciphertext *const *cts, int count,
                 nexus_ciphertext *const *res)
 {
@@ -235,9 +199,9 @@ extern "C" int nexus_gelu_batch(nexus_evaluator *ev, nexus_ciphertext *const *ct
         BatchEvaluator bev(ev->ev);
         BatchCKKS ck(bev, ev->ck.scale);
         GeLUEvaluatorT<BatchEvaluator, CtBatch> g(ck);
-        CtBatch x = gather(ev, cts, count), out;
+        CtBatch x = gather_batch(ev, cts, count), out;
         g.gelu(x, out);
-        scatter(ev, out, res);
+        scatter_batch(ev, out, res);
     });
 }
 
@@ -251,9 +215,9 @@ extern "C" int nexus_softmax_batch(nexus_evaluator *ev, nexus_ciphertext *const 
         BatchEvaluator bev(ev->ev);
         BatchCKKS ck(bev, ev->ck.scale);
         SoftmaxEvaluatorT<BatchEvaluator, CtBatch> sm(ck);
-        CtBatch x = gather(ev, cts, count), out;
+        CtBatch x = gather_batch(ev, cts, count), out;
         sm.softmax(x, out, len);
-        scatter(ev, out, res);
+        scatter_batch(ev, out, res);
     });
 }
 
@@ -267,9 +231,9 @@ extern "C" int nexus_layer_norm_batch(nexus_evaluator *ev, nexus_ciphertext *con
         BatchEvaluator bev(ev->ev);
         BatchCKKS ck(bev, ev->ck.scale);
         LNEvaluatorT<BatchEvaluator, CtBatch> ln(ck);
-        CtBatch x = gather(ev, cts, count), out;
+        CtBatch x = gather_batch(ev, cts, count), out;
         ln.layer_norm(x, out, len);
-        scatter(ev, out, res);
+        scatter_batch(ev, out, res);
     });
 }
 
@@ -281,7 +245,7 @@ extern "C" int nexus_ckks_op_batch(nexus_evaluator *ev, int op, nexus_ciphertext
     return guarded(fn, [&] {
         BatchEvaluator bev(ev->ev);
         BatchCKKS ck(bev, ev->ck.scale);
-        CtBatch x = gather(ev, cts, count), out;
+        CtBatch x = gather_batch(ev, cts, count), out;
         switch (op) {
         case NEXUS_OP_SGN_EVAL: out = ck.sgn_eval(x, a1, a2, f); break;
         case NEXUS_OP_EXP: out = ck.exp(x); break;
@@ -289,7 +253,7 @@ extern "C" int nexus_ckks_op_batch(nexus_evaluator *ev, int op, nexus_ciphertext
         case NEXUS_OP_INVERT_SQRT: out = ck.invert_sqrt(x, a1, a2); break;
         default: throw std::invalid_argument("unknown op");
         }
-        scatter(ev, out, res);
+        scatter_batch(ev, out, res);
     });
 }
 

@@ -307,6 +307,19 @@ class Bootstrapper:
                                              r2.handle), "nexus_bootstrapper_stage")
         return r1, r2
 
+    def stage_batch(self, stage: int, a: list, b: list | None = None):
+        """``stage`` run in lockstep over the ciphertexts ``a`` (and ``b``);
+        returns the lists (r1, r2)."""
+        cnt = len(a)
+        r1 = [Ciphertext(self.ctx) for _ in a]
+        r2 = [Ciphertext(self.ctx) for _ in a]
+
+        def arr(xs):
+            return (C.c_void_p * cnt)(*[x.handle.value for x in xs])
+        check(lib().nexus_bootstrapper_stage_batch(self._h, stage, arr(a), None if b is None else arr(b), cnt,
+                                                   arr(r1), arr(r2)), "nexus_bootstrapper_stage_batch")
+        return r1, r2
+
     def cached_plaintexts(self) -> int:
         n = C.c_uint64()
         check(lib().nexus_bootstrapper_cached_plaintexts(self._h, C.byref(n)), "nexus_bootstrapper_cached_plaintexts")

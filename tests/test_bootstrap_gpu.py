@@ -105,6 +105,35 @@ def test_stages_match_oracle(env):
     _same(out, obs.slottocoeff_full_3(om1, om2))
 
 
+def test_lockstep_stages_equal_single_stages(env):
+    """nexus_bootstrapper_stage_batch gives each ciphertext the single-stage words."""
+    from nexus_gb300.operators import (BOOT_COEFFTOSLOT, BOOT_MODRAISE, BOOT_MODULAR_REDUCTION,
+                                       BOOT_SET_INITIAL_SCALE, BOOT_SLOTTOCOEFF, Ciphertext)
+    ctx, sk, bs, _, _ = env
+    xs = [_input(ctx, sk, 20 + i)[1] for i in range(2)]
+    ys = [Ciphertext.from_numpy(ctx, x.to_numpy(), x.scale) for x in xs]
+    bs.stage_batch(BOOT_SET_INITIAL_SCALE, xs)
+    bs.stage_batch(BOOT_MODRAISE, xs)
+    q0 = float(ctx.moduli[0])
+    raised = [Ciphertext.from_numpy(ctx, x.to_numpy(), q0) for x in xs]
+    c1, c2 = bs.stage_batch(BOOT_COEFFTOSLOT, raised)
+    m1, _ = bs.stage_batch(BOOT_MODULAR_REDUCTION, c1)
+    m2, _ = bs.stage_batch(BOOT_MODULAR_REDUCTION, c2)
+    out, _ = bs.stage_batch(BOOT_SLOTTOCOEFF, m1, m2)
+    for k, y in enumerate(ys):
+        bs.stage(BOOT_SET_INITIAL_SCALE, y)
+        bs.stage(BOOT_MODRAISE, y)
+        assert np.array_equal(y.to_numpy(), xs[k].to_numpy())
+        y = Ciphertext.from_numpy(ctx, y.to_numpy(), q0)
+        s1, s2 = bs.stage(BOOT_COEFFTOSLOT, y)
+        assert np.array_equal(s1.to_numpy(), c1[k].to_numpy()) and np.array_equal(s2.to_numpy(), c2[k].to_numpy())
+        e1, _ = bs.stage(BOOT_MODULAR_REDUCTION, s1)
+        e2, _ = bs.stage(BOOT_MODULAR_REDUCTION, s2)
+        assert np.array_equal(e1.to_numpy(), m1[k].to_numpy()) and e1.scale == m1[k].scale
+        o, _ = bs.stage(BOOT_SLOTTOCOEFF, e1, e2)
+        assert np.array_equal(o.to_numpy(), out[k].to_numpy()) and o.scale == out[k].scale
+
+
 def test_bootstrap_matches_oracle_and_refreshes(env):
     ctx, sk, bs, obs, _ = env
     vals, x, ox = _input(ctx, sk, 7)
