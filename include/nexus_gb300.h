@@ -321,6 +321,20 @@ enum { NEXUS_OP_SGN_EVAL = 0, NEXUS_OP_EXP = 1, NEXUS_OP_INVERSE = 2, NEXUS_OP_I
 int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext *x, int a1, int a2, double f,
                   nexus_ciphertext *res);
 
+/*
+ * Rotate one ciphertext by several slot steps: res[i] receives the words
+ * Evaluator::rotate_vector(x, steps[i]) gives (NAF decomposition included,
+ * evaluator.cpp:2667-2722).  The steps that have their own Galois key share
+ * one ModUp of x's c1 (hoisted rotations) whenever that is exact -- always,
+ * except when a coefficient of INTT(c1) is zero, where each step is switched
+ * on its own.  Hoisting keeps, per Galois element, a copy of the key with
+ * permuted rows (as large as the key) and a per-level correction.
+ * No counterpart in the reference: SEAL rotates one step per call, and the
+ * reference's BSGS transforms call rotate_vector once per baby step.
+ */
+int nexus_rotate_vector_many(nexus_evaluator *ev, const nexus_ciphertext *x, const int *steps, int count,
+                             nexus_ciphertext *const *res);
+
 /* ------------------------------------------------------------------ */
 /* MatMul (src/matrix_mul.cpp in the NEXUS tree)                        */
 /* ------------------------------------------------------------------ */

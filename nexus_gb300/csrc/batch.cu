@@ -417,6 +417,37 @@ void BatchEvaluator::rotate_vector_inplace(CtBatch &ct, int steps)
         if ((size_t)std::abs(st) != (c_.n >> 1)) rotate_vector_inplace(ct, st);
 }
 
+void BatchEvaluator::rotate_vector_many(const CtBatch &ct, const std::vector<int> &steps, std::vector<CtBatch> &outs)
+{
+    outs.resize(steps.size());
+    for (const CtBatch &o : outs)
+        if (&o == &ct) throw std::invalid_argument("rotate_vector_many: ct must not be one of the outputs");
+    const int l = ct.limbs(), B = ct.batch();
+    std::vector<bool> done(steps.size(), false);
+    std::vector<size_t> direct;
+    for (size_t i = 0; i < steps.size(); ++i)
+        if (steps[i] != 0 && ev_.galois_keys.count(ev_.galois_elt(steps[i]))) direct.push_back(i);
+    if (ct.size() == 2 && Evaluator::hoist_pays((int)direct.size(), l)) {
+        const size_t N = c_.n, pitch = ct.words_per_ct();
+        DeviceBuffer t, D;
+        t.reserve((size_t)B * l * N, stream());
+        D.reserve((size_t)B * l * (l + 1) * N, stream());
+        if (hoist_decompose(c_, ct.data() + (size_t)l * N, pitch, B, l, t.get(), D.get(), ev_.hoist_flag(),
+                            stream())) {
+            for (size_t i : direct) {
+                const uint32_t elt = ev_.galois_elt(steps[i]);
+                const uint64_t *pk = ev_.hoist_key(elt), *corr = ev_.hoist_corr(elt, l);
+                outs[i].resize(c_, B, 2, l, stream());
+                outs[i].scale() = ct.scale();
+                hoist_rotate(c_, D.get(), B, l, elt, pk, corr, ct.data(), pitch, outs[i].data(), stream());
+                done[i] = true;
+            }
+        }
+    }
+    for (size_t i = 0; i < steps.size(); ++i)
+        if (!done[i]) rotate_vector(ct, steps[i], outs[i]);
+}
+
 void BatchEvaluator::rotate_vector(const CtBatch &ct, int steps, CtBatch &dest)
 {
     if (&ct != &dest && steps != 0) {

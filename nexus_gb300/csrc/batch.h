@@ -118,6 +118,9 @@ public:
     void rotate_vector_inplace(CtBatch &ct, int steps);
     void rotate_vector(const CtBatch &ct, int steps, CtBatch &dest);
     void complex_conjugate_inplace(CtBatch &ct) { apply_galois_inplace(ct, ev_.galois_elt(0)); }
+    // outs[i] = rotate_vector(ct, steps[i]); the steps with their own key share
+    // one ModUp of the batch's c1 polynomials when that is exact
+    void rotate_vector_many(const CtBatch &ct, const std::vector<int> &steps, std::vector<CtBatch> &outs);
 
 private:
     void plain_arith(CtBatch &ct, const Plaintext &pt, bool sub);

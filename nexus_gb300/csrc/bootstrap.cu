@@ -489,12 +489,22 @@ void BootstrapperT<EV, CT>::bsgs_linear_transform(CT &rtncipher, const CT &ciphe
     const int start = -totlen + gs1 * (int)std::floor((totlen + 0.0) / (gs1 + 0.0));
     const int gfirst = -(int)std::floor((totlen + 0.0) / (gs1 + 0.0));
     const int glast = (int)std::floor((2 * totlen + 0.0) / (gs1 + 0.0)) + gfirst;
+    // the baby steps rotate one ciphertext: they share its decomposition
     std::vector<CT> baby(gs1);
-    for (int i = start; i < start + gs1; i++) {
-        if (i == 0)
-            baby[i - start] = cipher;
-        else
-            ev.rotate_vector(cipher, (nh + i * basicstep) % nh, baby[i - start]);
+    {
+        std::vector<int> steps;
+        std::vector<int> slot;
+        for (int i = start; i < start + gs1; i++) {
+            if (i == 0) {
+                baby[i - start] = cipher;
+            } else {
+                steps.push_back((nh + i * basicstep) % nh);
+                slot.push_back(i - start);
+            }
+        }
+        std::vector<CT> rotated;
+        ev.rotate_vector_many(cipher, steps, rotated);
+        for (size_t r = 0; r < slot.size(); r++) baby[slot[r]] = std::move(rotated[r]);
     }
     CT giant, acc, t;
     bool have_acc = false;
@@ -541,12 +551,15 @@ void BootstrapperT<EV, CT>::rotated_bsgs_linear_transform(CT &rtncipher, const C
     const int nh = (int)Nh;
     const int gs2 = giantstep(totlen + 1);
     const int glast = (int)std::floor((totlen + 0.0) / (gs2 + 0.0));
+    // the baby steps rotate one ciphertext: they share its decomposition
     std::vector<CT> baby(gs2);
-    for (int i = 0; i < gs2; i++) {
-        if (i == 0)
-            baby[i] = cipher;
-        else
-            ev.rotate_vector(cipher, (nh + i * basicstep) % nh, baby[i]);
+    {
+        std::vector<int> steps;
+        for (int i = 1; i < gs2; i++) steps.push_back((nh + i * basicstep) % nh);
+        std::vector<CT> rotated;
+        ev.rotate_vector_many(cipher, steps, rotated);
+        baby[0] = cipher;
+        for (int i = 1; i < gs2; i++) baby[i] = std::move(rotated[i - 1]);
     }
     CT giant, acc, t;
     bool have_acc = false;

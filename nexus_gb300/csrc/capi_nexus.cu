@@ -58,7 +58,7 @@ extern "C" int nexus_evaluator_add_galois_key(nexus_evaluator *ev, uint32_t galo
     static const char *fn = "nexus_evaluator_add_galois_key";
     if (!ev || !d_key) return fail(fn, "null argument");
     if (!(galois_elt & 1) || galois_elt >= 2 * ev->ctx->c.n) return fail(fn, "Galois element is not valid");
-    ev->ev.galois_keys[galois_elt] = d_key;
+    ev->ev.set_galois_key(galois_elt, d_key);
     return 0;
 }
 
@@ -166,6 +166,25 @@ extern "C" int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext
         case NEXUS_OP_INVERT_SQRT: res->ct = ev->ck.invert_sqrt(x->ct, a1, a2); break;
         default: throw std::invalid_argument("unknown op");
         }
+    });
+}
+
+extern "C" int nexus_rotate_vector_many(nexus_evaluator *ev, const nexus_ciphertext *x, const int *steps, int count,
+                                        nexus_ciphertext *const *res)
+{
+    static const char *fn = "nexus_rotate_vector_many";
+    if (!ev || !x || !res || (count > 0 && !steps) || count < 0) return fail(fn, "null argument");
+    if (const char *e = input_problem(ev->ctx, x)) return fail(fn, e);
+    for (int i = 0; i < count; ++i) {
+        if (!res[i]) return fail(fn, "null result");
+        if (res[i] == x) return fail(fn, "results must not alias the input");
+        for (int j = 0; j < i; ++j)
+            if (res[j] == res[i]) return fail(fn, "results must be distinct");
+    }
+    return guarded(fn, [&] {
+        std::vector<Ciphertext> outs;
+        ev->ev.rotate_vector_many(x->ct, std::vector<int>(steps, steps + count), outs);
+        for (int i = 0; i < count; ++i) res[i]->ct = std::move(outs[i]);
     });
 }
 

@@ -662,4 +662,82 @@ void Evaluator::rotate_vector(const Ciphertext &ct, int steps, Ciphertext &dest)
 
 void Evaluator::complex_conjugate_inplace(Ciphertext &ct) { apply_galois_inplace(ct, galois_elt(0)); }
 
+// ------------------------------------------------------- hoisted rotations
+
+void Evaluator::set_galois_key(uint32_t elt, const uint64_t *key)
+{
+    galois_keys[elt] = key;
+    hoist_keys_.erase(elt);
+    for (auto it = hoist_corrs_.begin(); it != hoist_corrs_.end();)
+        it = (it->first.first == elt) ? hoist_corrs_.erase(it) : std::next(it);
+}
+
+const uint64_t *Evaluator::hoist_key(uint32_t elt)
+{
+    auto it = hoist_keys_.find(elt);
+    if (it != hoist_keys_.end()) return it->second.get();
+    auto k = galois_keys.find(elt);
+    if (k == galois_keys.end()) throw std::invalid_argument("Galois key not present");
+    DeviceBuffer &b = hoist_keys_[elt];
+    b.reserve((size_t)(c_.k - 1) * 2 * c_.k * c_.n, s_);
+    hoist_permute_key(c_, k->second, elt, b.get(), s_);
+    return b.get();
+}
+
+const uint64_t *Evaluator::hoist_corr(uint32_t elt, int limbs)
+{
+    auto it = hoist_corrs_.find({elt, limbs});
+    if (it != hoist_corrs_.end()) return it->second.get();
+    auto k = galois_keys.find(elt);
+    if (k == galois_keys.end()) throw std::invalid_argument("Galois key not present");
+    auto m = hoist_masks_.find(elt);
+    if (m == hoist_masks_.end()) {
+        DeviceBuffer &mb = hoist_masks_[elt];
+        mb.reserve((size_t)c_.k * c_.n, s_);
+        hoist_galois_mask_ntt(c_, elt, mb.get(), s_);
+        m = hoist_masks_.find(elt);
+    }
+    DeviceBuffer &b = hoist_corrs_[{elt, limbs}];
+    b.reserve((size_t)2 * (limbs + 1) * c_.n, s_);
+    hoist_correction(c_, k->second, m->second.get(), limbs, b.get(), s_);
+    return b.get();
+}
+
+int *Evaluator::hoist_flag()
+{
+    hoist_flag_.reserve(1, s_);
+    return reinterpret_cast<int *>(hoist_flag_.get());
+}
+
+void Evaluator::rotate_vector_many(const Ciphertext &ct, const std::vector<int> &steps, std::vector<Ciphertext> &outs)
+{
+    outs.resize(steps.size());
+    for (const Ciphertext &o : outs)
+        if (&o == &ct) throw std::invalid_argument("rotate_vector_many: ct must not be one of the outputs");
+    const int l = ct.limbs();
+    std::vector<bool> done(steps.size(), false);
+    std::vector<size_t> direct;
+    for (size_t i = 0; i < steps.size(); ++i)
+        if (steps[i] != 0 && galois_keys.count(galois_elt(steps[i]))) direct.push_back(i);
+    if (ct.size() == 2 && hoist_pays((int)direct.size(), l)) {
+        const size_t N = c_.n;
+        DeviceBuffer t, D;
+        t.reserve((size_t)l * N, s_);
+        D.reserve((size_t)l * (l + 1) * N, s_);
+        if (hoist_decompose(c_, ct.data() + (size_t)l * N, 2 * (size_t)l * N, 1, l, t.get(), D.get(), hoist_flag(),
+                            s_)) {
+            for (size_t i : direct) {
+                const uint32_t elt = galois_elt(steps[i]);
+                const uint64_t *pk = hoist_key(elt), *corr = hoist_corr(elt, l);
+                outs[i].resize(c_, 2, l, s_);
+                outs[i].scale() = ct.scale();
+                hoist_rotate(c_, D.get(), 1, l, elt, pk, corr, ct.data(), 0, outs[i].data(), s_);
+                done[i] = true;
+            }
+        }
+    }
+    for (size_t i = 0; i < steps.size(); ++i)
+        if (!done[i]) rotate_vector(ct, steps[i], outs[i]);
+}
+
 }  // namespace nexus

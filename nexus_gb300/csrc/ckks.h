@@ -10,6 +10,7 @@
 #include <complex>
 #include <cstdint>
 #include <map>
+#include <utility>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -130,6 +131,9 @@ public:
     // keys (device pointers owned by the caller, SEAL layout [K-1][2][K][N])
     const uint64_t *relin_key = nullptr;
     std::map<uint32_t, const uint64_t *> galois_keys;
+    // set (or replace) the key of a Galois element; drops the element's
+    // hoisting data, which is derived from the key
+    void set_galois_key(uint32_t elt, const uint64_t *key);
 
     // CKKSEncoder
     void encode(const std::vector<double> &values, int limbs, double scale, Plaintext &out);
@@ -193,6 +197,20 @@ public:
     void rotate_vector(const Ciphertext &ct, int steps, Ciphertext &dest);
     void complex_conjugate_inplace(Ciphertext &ct);
     uint32_t galois_elt(int step) const;
+    // outs[i] = rotate_vector(ct, steps[i]) for every i, word for word; the
+    // steps that have their own Galois key share one ModUp of c1 (hoisted
+    // rotations, ops.h) when that is exact.  ct must not be one of outs.
+    void rotate_vector_many(const Ciphertext &ct, const std::vector<int> &steps, std::vector<Ciphertext> &outs);
+
+    // Hoisting data of a Galois element, built on first use and kept until
+    // its key is replaced: the key with its rows permuted (the size of the
+    // key) and, per level, a [2][limbs+1][N] correction.
+    const uint64_t *hoist_key(uint32_t elt);
+    const uint64_t *hoist_corr(uint32_t elt, int limbs);
+    int *hoist_flag();
+    // hoisting pays when at least two rotations share the decomposition and
+    // the level is high enough for the ModUp to dominate the key switch
+    static bool hoist_pays(int direct_steps, int limbs) { return direct_steps >= 2 && limbs >= 8; }
 
     int total_bits(int limbs) const;
     // is_scale_within_bounds (evaluator.cpp:29-47)
@@ -207,6 +225,9 @@ private:
     cudaStream_t s_;
     Encoder *enc_ = nullptr;
     std::vector<int> bits_;
+    std::map<uint32_t, DeviceBuffer> hoist_keys_, hoist_masks_;
+    std::map<std::pair<uint32_t, int>, DeviceBuffer> hoist_corrs_;
+    DeviceBuffer hoist_flag_;
 };
 
 bool are_close(double a, double b);

@@ -292,6 +292,200 @@ void apply_galois(Context &c, const uint64_t *ct, int l, uint32_t elt, const uin
 }  // namespace nexus
 
 // ---------------------------------------------------------------------------
+// Hoisted rotations: several Galois elements applied to one batch of
+// ciphertexts share one ModUp of c1.
+//
+// For the automorphism sigma_g the key-switch target of a rotation is
+// pi_g(c1) (pi_g the NTT-domain permutation), whose coefficient form is the
+// signed permutation of t_j = INTT_j(c1_j): a coefficient that lands on a
+// negated position becomes q_j - a.  Reduced into another prime q_i that is
+// (q_j mod q_i) - (a mod q_i), so when no coefficient of t is zero
+//
+//   ModUp(pi_g(c1))[j][i] = pi_g(D[j][i]) + (q_j mod q_i) * M_g[i],
+//
+// with D the ModUp of c1 itself and M_g[i] the NTT of the 0/1 polynomial of
+// negated positions.  The key inner product of a rotation is then
+//
+//   P[k][i][n] = Ptil[k][i][pi_g(n)] + Corr_g[k][i][n],
+//   Ptil = sum_j D[j][i] * Kperm[j][k][i],   Kperm[..][pi_g(n)] = K_g[..][n],
+//   Corr_g[k][i] = M_g[i] * sum_j (q_j mod q_i) * K_g[j][k][i]   (mod q_i),
+//
+// the same residues as the inner product of the rotated target, so the
+// ModDown and the output words are the ones apply_galois gives.  A zero
+// coefficient in t (probability about B*l*N/q for random data, certain for a
+// trivial c1) breaks the identity; hoist_decompose reports it and the caller
+// rotates one element at a time instead.
+
+namespace nexus {
+
+namespace {
+
+__global__ void k_any_zero(const uint64_t *__restrict__ t, size_t total, int *flag)
+{
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x)
+        if (t[x] == 0) *flag = 1;
+}
+
+// out[p][pos] = 1 where the automorphism X -> X^elt negates the coefficient
+// it moves to pos, else 0; the same 0/1 polynomial in each of the `limbs` rows
+__global__ void k_galois_mask(uint64_t *__restrict__ out, uint32_t elt, int logn, int limbs)
+{
+    const size_t N = (size_t)1 << logn;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < N; x += (size_t)gridDim.x * blockDim.x) {
+        const uint64_t raw = (x * (uint64_t)elt) & (2 * N - 1);
+        if (raw >= N)
+            for (int p = 0; p < limbs; ++p) out[p * N + (raw - N)] = 1;
+    }
+}
+
+// out[row][tab[n]] = in[row][n] for every N-word row
+__global__ void k_scatter_rows(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
+                               const uint32_t *__restrict__ tab, int logn, size_t total)
+{
+    const size_t mask = ((size_t)1 << logn) - 1;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x)
+        out[(x & ~mask) + tab[x & mask]] = in[x];
+}
+
+// Corr[k][i][n] = M[kidx(i)][n] * sum_{j<l} (q_j mod q_kidx) * key[j][k][kidx(i)][n] mod q_kidx
+__global__ void k_hoist_corr(const uint64_t *__restrict__ key, const uint64_t *__restrict__ M,
+                             const PrimeConst *__restrict__ pc, int l, int K, int logn, uint64_t *__restrict__ out)
+{
+    const size_t N = (size_t)1 << logn, total = (size_t)2 * (l + 1) * N;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = x >> logn, n = x & (N - 1);
+        const int k = (int)(row / (size_t)(l + 1)), i = (int)(row % (size_t)(l + 1));
+        const int kidx = (i == l) ? K - 1 : i;
+        const PrimeConst P = pc[kidx];
+        uint64_t lo = 0, hi = 0;
+        for (int j = 0; j < l; ++j) {
+            const uint64_t qj = pc[j].q;
+            const uint64_t c = (qj >= P.q) ? barrett_64(qj, P.q, P.r1) : qj;
+            mac128(lo, hi, c, key[(((size_t)j * 2 + k) * K + kidx) * N + n]);
+        }
+        const uint64_t s = barrett_128(lo, hi, P.q, P.r0, P.r1);
+        out[x] = mul_mod(s, M[(size_t)kidx * N + n], P.q, P.r0, P.r1);
+    }
+}
+
+// P[b][k][i][n] = Ptil[b][k][i][tab[n]] + Corr[k][i][n] mod q_kidx(i)
+__global__ void k_hoist_fix(const uint64_t *__restrict__ Pt, const uint64_t *__restrict__ corr,
+                            const uint32_t *__restrict__ tab, const PrimeConst *__restrict__ pc, int l, int K,
+                            int logn, size_t total, uint64_t *__restrict__ P)
+{
+    const size_t N = (size_t)1 << logn;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = x >> logn, n = x & (N - 1);
+        const size_t krow = row % (size_t)(2 * (l + 1));          // k * (l+1) + i
+        const int i = (int)(krow % (size_t)(l + 1));
+        const uint64_t q = pc[(i == l) ? K - 1 : i].q;
+        P[x] = csub(Pt[(row << logn) + tab[n]] + corr[(krow << logn) + n], q);
+    }
+}
+
+// out[b][0] = pi(in[b][0]) for the c0 polynomial (l limbs) of each ciphertext;
+// in has `pitch` words between ciphertexts, out 2 * l * N
+__global__ void k_permute_c0(const uint64_t *__restrict__ in, size_t pitch, uint64_t *__restrict__ out,
+                             const uint32_t *__restrict__ tab, int logn, size_t poly, size_t total)
+{
+    const size_t mask = ((size_t)1 << logn) - 1;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t b = x / poly, r = x - b * poly;
+        out[b * 2 * poly + r] = in[b * pitch + (r & ~mask) + tab[r & mask]];
+    }
+}
+
+}  // namespace
+
+bool hoist_decompose(Context &c, const uint64_t *c1, size_t c1_pitch, int B, int l, uint64_t *t, uint64_t *D,
+                     int *d_flag, cudaStream_t s)
+{
+    const size_t N = c.n, Bs = (size_t)B;
+    const int sp = c.k - 1;
+    if (c1_pitch == 0 || c1_pitch == (size_t)l * N)
+        cudaMemcpyAsync(t, c1, sizeof(uint64_t) * Bs * l * N, cudaMemcpyDeviceToDevice, s);
+    else
+        cudaMemcpy2DAsync(t, sizeof(uint64_t) * l * N, c1, sizeof(uint64_t) * c1_pitch, sizeof(uint64_t) * l * N, Bs,
+                          cudaMemcpyDeviceToDevice, s);
+    const size_t pairs = Bs * l * N / 2;
+    k_modup_diag<<<grid_for(pairs), kBlock, 0, s>>>(reinterpret_cast<const ulonglong2 *>(t),
+                                                    reinterpret_cast<ulonglong2 *>(D), l, c.logn, pairs);
+    NEXUS_LAUNCHED();
+    ntt_inverse(c, t, Bs, LimbMap{l, 0, -1}, s);
+    cudaMemsetAsync(d_flag, 0, sizeof(int), s);
+    const size_t words = Bs * l * N;
+    k_any_zero<<<grid_for(words), kBlock, 0, s>>>(t, words, d_flag);
+    NEXUS_LAUNCHED();
+    int h_flag = 0;
+    if (cudaMemcpyAsync(&h_flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        throw std::runtime_error("hoist_decompose: reading the zero flag failed");
+    if (h_flag) return false;
+    NttLoader ld;
+    ld.kind = 1;
+    ld.src = t;
+    ld.group = l;
+    ld.src_limbs = l;
+    ntt_forward_loaded(c, D, Bs * l, LimbMap{l, 0, sp, 1}, ld, s);
+    return true;
+}
+
+void hoist_galois_mask_ntt(Context &c, uint32_t elt, uint64_t *M, cudaStream_t s)
+{
+    const size_t N = c.n;
+    cudaMemsetAsync(M, 0, sizeof(uint64_t) * c.k * N, s);
+    k_galois_mask<<<grid_for(N), kBlock, 0, s>>>(M, elt, c.logn, c.k);
+    NEXUS_LAUNCHED();
+    ntt_forward(c, M, 1, LimbMap{c.k, 0, -1}, s);
+}
+
+void hoist_permute_key(Context &c, const uint64_t *key, uint32_t elt, uint64_t *out, cudaStream_t s)
+{
+    const size_t total = (size_t)(c.k - 1) * 2 * c.k * c.n;
+    k_scatter_rows<<<grid_for(total), kBlock, 0, s>>>(key, out, c.galois_table(elt), c.logn, total);
+    NEXUS_LAUNCHED();
+}
+
+void hoist_correction(Context &c, const uint64_t *key, const uint64_t *M, int l, uint64_t *out, cudaStream_t s)
+{
+    const size_t total = (size_t)2 * (l + 1) * c.n;
+    k_hoist_corr<<<grid_for(total), kBlock, 0, s>>>(key, M, c.d_pc, l, c.k, c.logn, out);
+    NEXUS_LAUNCHED();
+}
+
+void hoist_rotate(Context &c, const uint64_t *D, int B, int l, uint32_t elt, const uint64_t *perm_key,
+                  const uint64_t *corr, const uint64_t *ct, size_t ct_pitch, uint64_t *out, cudaStream_t s)
+{
+    if (reinterpret_cast<uintptr_t>(perm_key) & 15) throw std::invalid_argument("hoist_rotate: unaligned key");
+    const size_t N = c.n, Bs = (size_t)B;
+    const int sp = c.k - 1;
+    const size_t poly = (size_t)l * N;
+    if (ct_pitch == 0) ct_pitch = 2 * poly;
+    // scratch per ciphertext: Ptil[2][l+1] | P[2][l+1] | T[2][l] | last[2]
+    const size_t words = Bs * N * (4 * (size_t)(l + 1) + 2 * (size_t)l + 2);
+    uint64_t *Pt = c.get_scratch(words);
+    uint64_t *P = Pt + Bs * 2 * (l + 1) * N;
+    uint64_t *T = P + Bs * 2 * (l + 1) * N;
+    uint64_t *last = T + Bs * 2 * l * N;
+    launch_ks_inner(c, D, perm_key, Pt, l, B, s);
+    const uint32_t *tab = c.galois_table(elt);
+    const size_t tot = Bs * 2 * (l + 1) * N;
+    k_hoist_fix<<<grid_for(tot), kBlock, 0, s>>>(Pt, corr, tab, c.d_pc, l, c.k, c.logn, tot, P);
+    NEXUS_LAUNCHED();
+    // out[b] = (pi_g(c0), 0), then the ModDown adds the switched pair
+    k_permute_c0<<<grid_for(Bs * poly), kBlock, 0, s>>>(ct, ct_pitch, out, tab, c.logn, poly, Bs * poly);
+    NEXUS_LAUNCHED();
+    cudaMemset2DAsync(out + poly, 2 * poly * 8, 0, poly * 8, Bs, s);
+    ks_moddown_terms(c, P, B, l, T, last, s);
+    const size_t tot2 = Bs * 2 * l * N;
+    k_moddown_finish<<<grid_for(tot2), kBlock, 0, s>>>(out, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn,
+                                                        tot2);
+    NEXUS_LAUNCHED();
+}
+
+}  // namespace nexus
+
+// ---------------------------------------------------------------------------
 // Key switching that allocates nothing.
 //
 // nexus_switch_key takes its temporaries from the context's scratch arena,

@@ -72,6 +72,25 @@ void ks_modup_inner(Context &c, uint64_t *t, int B, int l, const uint64_t *key, 
                     cudaStream_t s);
 void ks_moddown_terms(Context &c, const uint64_t *P, int B, int l, uint64_t *T, uint64_t *last, cudaStream_t s);
 
+// Hoisted rotations (keyswitch.cu): one ModUp of the c1 polynomials of B
+// ciphertexts at l limbs (c1 at c1 + b * c1_pitch) shared by several Galois
+// elements.  hoist_decompose fills D [B][l][l+1][N] (t is scratch of B*l
+// limbs, d_flag one device int) and returns false, with D unset, when a
+// coefficient of INTT(c1) is zero: the shared decomposition is then not
+// exact and the caller must rotate element by element.  Per element:
+// perm_key (hoist_permute_key, the key with every row scattered by the
+// element's NTT permutation) and corr [2][l+1][N] (hoist_correction from the
+// key and M = hoist_galois_mask_ntt [K][N]) are reusable across calls;
+// hoist_rotate writes out [B][2][l][N] with the words apply_galois gives for
+// each ciphertext (ct at ct + b * ct_pitch, 0 = 2 * l * N).
+bool hoist_decompose(Context &c, const uint64_t *c1, size_t c1_pitch, int B, int l, uint64_t *t, uint64_t *D,
+                     int *d_flag, cudaStream_t s);
+void hoist_galois_mask_ntt(Context &c, uint32_t elt, uint64_t *M, cudaStream_t s);
+void hoist_permute_key(Context &c, const uint64_t *key, uint32_t elt, uint64_t *out, cudaStream_t s);
+void hoist_correction(Context &c, const uint64_t *key, const uint64_t *M, int l, uint64_t *out, cudaStream_t s);
+void hoist_rotate(Context &c, const uint64_t *D, int B, int l, uint32_t elt, const uint64_t *perm_key,
+                  const uint64_t *corr, const uint64_t *ct, size_t ct_pitch, uint64_t *out, cudaStream_t s);
+
 // relinearize a size-3 ciphertext into out2 (may alias ct3)
 void relinearize(Context &c, const uint64_t *ct3, int limbs, const uint64_t *key, uint64_t *out2, cudaStream_t s);
 

@@ -139,6 +139,16 @@ class Evaluator:
         check(lib().nexus_evaluator_add_galois_key(self._h, int(elt), key.data_ptr()),
               "nexus_evaluator_add_galois_key")
 
+    def rotate_vector_many(self, x: Ciphertext, steps) -> list:
+        """rotate_vector(x, s) for every s in steps (one shared decomposition
+        of x where that is exact)."""
+        steps = [int(v) for v in steps]
+        res = [Ciphertext(self.ctx) for _ in steps]
+        arr = (C.c_int * len(steps))(*steps)
+        out = (C.c_void_p * len(res))(*[r.handle.value for r in res])
+        check(lib().nexus_rotate_vector_many(self._h, x.handle, arr, len(steps), out), "nexus_rotate_vector_many")
+        return res
+
     def gelu(self, x: Ciphertext) -> Ciphertext:
         res = Ciphertext(self.ctx)
         check(lib().nexus_gelu(self._h, x.handle, res.handle), "nexus_gelu")
