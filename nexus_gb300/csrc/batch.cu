@@ -289,11 +289,25 @@ CtBatch BatchEvaluator::adjust_down(const CtBatch &hi, const CtBatch &lo)
     const double q_top = (double)c_.q[hi.limbs() - 1];
     const double scale_adjust = lo.scale() * q_top / (hi.scale() * hi.scale());
     CtBatch adj;
-    multiply_const(hi, scale_adjust, adj);
-    adj.scale() = lo.scale() * q_top;
-    rescale_to_next_inplace(adj);
+    multiply_const_rescale(hi, scale_adjust, adj, lo.scale() * q_top);
     mod_switch_to_inplace(adj, lo.limbs());
     return adj;
+}
+
+void BatchEvaluator::multiply_const_rescale(const CtBatch &ct, double value, CtBatch &dest, double set_scale)
+{
+    Plaintext p;
+    ev_.encode_then_drop(value, ct.limbs(), ct.scale(), p);
+    const double prod = ct.scale() * p.scale();
+    ev_.check_scale(prod, ct.limbs());
+    if (ct.limbs() < 2) throw std::invalid_argument("end of modulus switching chain reached");
+    const double scale = (set_scale > 0.0 ? set_scale : prod) / (double)c_.q[ct.limbs() - 1];
+    ev_.check_scale(scale, ct.limbs() - 1);
+    CtBatch out;
+    out.resize(c_, ct.batch(), ct.size(), ct.limbs() - 1, stream());
+    rescale_scaled(c_, ct.data(), ct.size() * ct.batch(), ct.limbs(), p.residues().data(), out.data(), stream());
+    out.scale() = scale;
+    dest = std::move(out);
 }
 
 void BatchEvaluator::add_inplace_reduced_error(CtBatch &a, const CtBatch &b)

@@ -166,13 +166,11 @@ void ModularReducerT<EV, CT>::homomorphic_poly_evaluation(CT &rtn, const CT &cip
         const std::vector<double> &cf = heap[i];
         if (cf.empty()) continue;
         chb[i] = true;
-        ev.multiply_const(baby[1], cf[1], ch[i]);
-        ev.rescale_to_next_inplace(ch[i]);
+        ev.multiply_const_rescale(baby[1], cf[1], ch[i]);
         if (!(std::fabs(cf[1]) <= zero)) ev.add_const_inplace(ch[i], cf[0]);
         for (size_t j = 2; j < cf.size(); j++) {
             if (std::fabs(cf[j]) <= zero) continue;
-            ev.multiply_const((long)j < k ? baby[j] : giant[0], cf[j], tmp);
-            ev.rescale_to_next_inplace(tmp);
+            ev.multiply_const_rescale((long)j < k ? baby[j] : giant[0], cf[j], tmp);
             ev.add_inplace_reduced_error(ch[i], tmp);
         }
     }

@@ -529,11 +529,25 @@ Ciphertext Evaluator::adjust_down(const Ciphertext &hi, const Ciphertext &lo)
     const double q_top = (double)c_.q[hi.limbs() - 1];
     const double scale_adjust = lo.scale() * q_top / (hi.scale() * hi.scale());
     Ciphertext adj;
-    multiply_const(hi, scale_adjust, adj);
-    adj.scale() = lo.scale() * q_top;
-    rescale_to_next_inplace(adj);
+    multiply_const_rescale(hi, scale_adjust, adj, lo.scale() * q_top);
     mod_switch_to_inplace(adj, lo.limbs());
     return adj;
+}
+
+void Evaluator::multiply_const_rescale(const Ciphertext &ct, double value, Ciphertext &dest, double set_scale)
+{
+    Plaintext p;
+    encode_then_drop(value, ct.limbs(), ct.scale(), p);
+    const double prod = ct.scale() * p.scale();
+    check_scale(prod, ct.limbs());
+    if (ct.limbs() < 2) throw std::invalid_argument("end of modulus switching chain reached");
+    const double scale = (set_scale > 0.0 ? set_scale : prod) / (double)c_.q[ct.limbs() - 1];
+    check_scale(scale, ct.limbs() - 1);
+    Ciphertext out;
+    out.resize(c_, ct.size(), ct.limbs() - 1, s_);
+    rescale_scaled(c_, ct.data(), ct.size(), ct.limbs(), p.residues().data(), out.data(), s_);
+    out.scale() = scale;
+    dest = std::move(out);
 }
 
 void Evaluator::add_inplace_reduced_error(Ciphertext &a, const Ciphertext &b)

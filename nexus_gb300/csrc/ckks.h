@@ -179,6 +179,10 @@ public:
     void add_const_inplace(Ciphertext &ct, double value);
     void multiply_const_inplace(Ciphertext &ct, double value);
     void multiply_const(const Ciphertext &ct, double value, Ciphertext &dest);
+    // multiply_const then rescale_to_next_inplace, same words and checks, with
+    // the constant applied inside the rescale; set_scale > 0 replaces the
+    // product's scale before the rescale (as the reduced-error level matching does)
+    void multiply_const_rescale(const Ciphertext &ct, double value, Ciphertext &dest, double set_scale = 0.0);
     void multiply_vector_inplace_reduced_error(Ciphertext &ct, const std::vector<std::complex<double>> &values);
     void multiply_vector_reduced_error(const Ciphertext &ct, const std::vector<std::complex<double>> &values,
                                        Ciphertext &dest);

@@ -54,6 +54,11 @@ void launch_round_spread(const Context &c, const uint64_t *last, uint64_t *out, 
 void galois_permute(Context &c, const uint64_t *in, int polys, int limbs, uint32_t elt, uint64_t *out,
                     cudaStream_t s);
 
+// rescale of in * c for a per-limb scalar c (host residues, c[l] < q_l):
+// the words of poly_mul_scalar followed by rescale, in one pass fewer
+void rescale_scaled(const Context &c, const uint64_t *in, int size, int limbs, const uint64_t *scalars,
+                    uint64_t *out, cudaStream_t s);
+
 // switch_key_inplace: ct[2][limbs] += key-switch(target[limbs])
 void switch_key(Context &c, uint64_t *ct, int limbs, const uint64_t *target, const uint64_t *key, cudaStream_t s);
 

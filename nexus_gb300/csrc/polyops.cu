@@ -248,6 +248,47 @@ __global__ void k_rescale_finish(const ulonglong2 *__restrict__ in, const ulongl
     }
 }
 
+// k_gather_limb / k_rescale_finish of in * c (c a per-limb scalar, Shoup
+// pairs in sc): the product is formed where each is read instead of by a
+// separate pass, with the same residues
+__global__ void k_gather_limb_scaled(const ulonglong2 *__restrict__ in, ulonglong2 *__restrict__ out, const LimbScalars sc,
+                                     const PrimeConst *__restrict__ pc, int limbs, int which, int logn, size_t pairs)
+{
+    const size_t half = (size_t)1 << (logn - 1);
+    const uint64_t q = pc[which].q;
+    const ulonglong2 w = sc.w[which];
+    FOR_PAIRS(pairs)
+    {
+        const size_t p = pi / half, i = pi % half;
+        ulonglong2 x = in[(p * limbs + which) * half + i];
+        x.x = mul_shoup(x.x, w.x, w.y, q);
+        x.y = mul_shoup(x.y, w.x, w.y, q);
+        out[pi] = x;
+    }
+}
+
+__global__ void k_rescale_finish_scaled(const ulonglong2 *__restrict__ in, const ulonglong2 *__restrict__ t,
+                                        ulonglong2 *out, const LimbScalars sc, const PrimeConst *__restrict__ pc,
+                                        const ulonglong2 *__restrict__ inv_row, int limbs, int logn, size_t pairs)
+{
+    const size_t half = (size_t)1 << (logn - 1);
+    const int ol = limbs - 1;
+    FOR_PAIRS(pairs)
+    {
+        const size_t row = pi / half, i = pi % half;
+        const size_t p = row / ol;
+        const int l = (int)(row % ol);
+        const uint64_t q = pc[l].q;
+        const ulonglong2 w = inv_row[l], c = sc.w[l];
+        const ulonglong2 x = in[(p * limbs + l) * half + i], y = t[pi];
+        const uint64_t x0 = mul_shoup(x.x, c.x, c.y, q), x1 = mul_shoup(x.y, c.x, c.y, q);
+        ulonglong2 r;
+        r.x = mul_shoup(x0 + q - y.x, w.x, w.y, q);
+        r.y = mul_shoup(x1 + q - y.y, w.x, w.y, q);
+        out[pi] = r;
+    }
+}
+
 __global__ void k_permute(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
                           const uint32_t *__restrict__ tab, int logn, size_t total)
 {
@@ -369,6 +410,34 @@ void rescale(const Context &c_in, const uint64_t *in, int size, int limbs, uint6
     k_rescale_finish<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, (const ulonglong2 *)t, (ulonglong2 *)out,
                                                       c.d_pc, c.d_inv_q + (size_t)(limbs - 1) * c.k, limbs, c.logn,
                                                       pr); NEXUS_LAUNCHED();
+}
+
+void rescale_scaled(const Context &c_in, const uint64_t *in, int size, int limbs, const uint64_t *scalars,
+                    uint64_t *out, cudaStream_t s)
+{
+    if (limbs < 2) throw std::invalid_argument("rescale needs at least two limbs");
+    if (limbs > 64) throw std::invalid_argument("at most 64 limbs");
+    Context &c = const_cast<Context &>(c_in);
+    LimbScalars w;
+    for (int l = 0; l < limbs; ++l) w.w[l] = make_ulonglong2(scalars[l], host_shoup(scalars[l], c.q[l]));
+    const size_t n = c.n;
+    uint64_t *last = c.get_scratch((size_t)size * n * limbs);
+    uint64_t *t = last + (size_t)size * n;
+    size_t pr = ((size_t)size * n) >> 1;
+    k_gather_limb_scaled<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, (ulonglong2 *)last, w, c.d_pc, limbs,
+                                                          limbs - 1, c.logn, pr); NEXUS_LAUNCHED();
+    ntt_inverse(c, last, size, LimbMap{1, limbs - 1, -1}, s);
+    NttLoader ld;
+    ld.kind = 2;
+    ld.src = last;
+    ld.group = limbs - 1;
+    ld.special = limbs - 1;
+    ntt_forward_loaded(c, t, size, LimbMap{limbs - 1, 0, -1}, ld, s);
+    pr = pairs_of(c, size, limbs - 1);
+    k_rescale_finish_scaled<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, (const ulonglong2 *)t,
+                                                             (ulonglong2 *)out, w, c.d_pc,
+                                                             c.d_inv_q + (size_t)(limbs - 1) * c.k, limbs, c.logn,
+                                                             pr); NEXUS_LAUNCHED();
 }
 
 void launch_round_spread(const Context &c, const uint64_t *last, uint64_t *out, int polys, int last_prime,
