@@ -207,7 +207,7 @@ __device__ __forceinline__ int swz(int s) { return s + (s >> 4); }
 // KIND selects the input (NttLoader): 0 the data itself, 1 the ModUp spread,
 // 2 the ModDown rounding spread of a key switch.
 template <int LOGS, int KIND, bool SMALL>
-__global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
+__global__ void __launch_bounds__(kThreads, 3) k_fwd_cols(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
                                                        const PrimeConst *__restrict__ pc, int logn, LimbMap lm,
                                                        NttLoader ld)
 {
@@ -227,9 +227,6 @@ __global__ void __launch_bounds__(kThreads) k_fwd_cols(uint64_t *__restrict__ da
 
     uint64_t x[kE];
     if (KIND == 0) {
-        static_assert(S * C == kThreads * kE, "a columns tile is kThreads * kE residues");
-        const unsigned fb = blockIdx.x + 3 * sm_count();
-        if (fb < gridDim.x) prefetch_cols_tile<S, C>(data, fb, logn, n2, tiles, lm);
 #pragma unroll
         for (int k = 0; k < kE; ++k) x[k] = p[(size_t)(t + T * k) * n2 + c];
     } else {
@@ -374,7 +371,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_inv_rows(uint64_t *__restrict__
 
 // Inverse pass B: columns (undoing pass 1), then n^{-1} and reduction to [0,q).
 template <int LOGS>
-__global__ void __launch_bounds__(kThreads) k_inv_cols(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
+__global__ void __launch_bounds__(kThreads, 3) k_inv_cols(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
                                                        const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
 {
     constexpr int S = 1 << LOGS, T = S / kE, C = kThreads / T;
