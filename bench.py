@@ -81,6 +81,16 @@ def _profile_traffic(name: str):
     return _profile_value(name, "traffic_bytes_per_launch")
 
 
+def _int_pipe(profile: str, what: str):
+    """The integer-multiply (fmaheavy) pipe's measured busy fraction for the
+    NTT passes, from the committed ncu summary: the bound that binds them."""
+    frac = _profile_value(profile, "fmaheavy_active_frac")
+    if frac is None:
+        return None
+    return {"fmaheavy_active_frac": frac, "source": f"ncu sm__pipe_fmaheavy_cycles_active of {what}, "
+            f"profiles/{profile}.txt"}
+
+
 def _ntt_traffic(limbs_per_launch: float, n: int = 1 << 16):
     """DRAM bytes of one NTT launch of `limbs_per_launch` limb-NTTs of degree n,
     scaled from the ncu capture of the N=2^16 NTT (DRAM traffic grows with the
@@ -243,6 +253,7 @@ def run_ntt_gpu(args, rank, world):
             "peak_source": peak_kind,
             "algorithmic_bytes_per_launch": alg_bytes,
             "traffic": _profile_traffic("ntt_forward_n65536_l24_64ct"),
+            "int_multiply_pipe": _int_pipe("ntt_forward_n65536_l24_64ct", "the 60-bit NTT passes"),
         },
         "e2e": {"value": limbs * e2e_steps * world / (e2e_ms / 1e3), "unit": "limb-NTT/s",
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
@@ -652,6 +663,7 @@ def run_boot_gpu(args, rank, world):
             "share_of_step": ntt_ms / instr_ms,
             "traffic": _ntt_traffic(ntt_limbs / max(1, ntt_calls)),
             "traffic_source": "ncu DRAM bytes per limb-NTT of the 51-bit NTT capture x limbs per launch",
+            "int_multiply_pipe": _int_pipe("keyswitch_n65536_l31_4ct", "the key switch's ModUp NTT passes"),
         },
         "e2e": {"value": world * BOOT_CTS / e2e_s, "unit": "bootstraps/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes},
