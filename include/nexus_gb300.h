@@ -335,6 +335,15 @@ int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext *x, int a1
 int nexus_rotate_vector_many(nexus_evaluator *ev, const nexus_ciphertext *x, const int *steps, int count,
                              nexus_ciphertext *const *res);
 
+/*
+ * Hoisted rotations on (enable != 0, the default) or off for this evaluator
+ * and every bootstrapper built on it.  Off, every rotation is switched on its
+ * own and no permuted key copies are made; the output words are the same
+ * either way.  When the copies cannot be allocated the evaluator also falls
+ * back to one key switch per step.  No counterpart in the reference.
+ */
+int nexus_evaluator_set_hoisting(nexus_evaluator *ev, int enable);
+
 /* ------------------------------------------------------------------ */
 /* MatMul (src/matrix_mul.cpp in the NEXUS tree)                        */
 /* ------------------------------------------------------------------ */

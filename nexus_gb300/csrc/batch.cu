@@ -441,7 +441,9 @@ void BatchEvaluator::rotate_vector_many(const CtBatch &ct, const std::vector<int
     std::vector<size_t> direct;
     for (size_t i = 0; i < steps.size(); ++i)
         if (steps[i] != 0 && ev_.galois_keys.count(ev_.galois_elt(steps[i]))) direct.push_back(i);
-    if (ct.size() == 2 && Evaluator::hoist_pays((int)direct.size(), l)) {
+    std::vector<uint32_t> elts;
+    for (size_t i : direct) elts.push_back(ev_.galois_elt(steps[i]));
+    if (ev_.hoisting && ct.size() == 2 && Evaluator::hoist_pays((int)direct.size(), l) && ev_.hoist_prepare(elts, l)) {
         const size_t N = c_.n, pitch = ct.words_per_ct();
         DeviceBuffer t, D;
         t.reserve((size_t)B * l * N, stream());

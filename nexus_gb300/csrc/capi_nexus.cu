@@ -169,6 +169,13 @@ extern "C" int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext
     });
 }
 
+extern "C" int nexus_evaluator_set_hoisting(nexus_evaluator *ev, int enable)
+{
+    if (!ev) return fail("nexus_evaluator_set_hoisting", "null argument");
+    ev->ev.hoisting = enable != 0;
+    return 0;
+}
+
 extern "C" int nexus_rotate_vector_many(nexus_evaluator *ev, const nexus_ciphertext *x, const int *steps, int count,
                                         nexus_ciphertext *const *res)
 {

@@ -692,10 +692,10 @@ const uint64_t *Evaluator::hoist_key(uint32_t elt)
     if (it != hoist_keys_.end()) return it->second.get();
     auto k = galois_keys.find(elt);
     if (k == galois_keys.end()) throw std::invalid_argument("Galois key not present");
-    DeviceBuffer &b = hoist_keys_[elt];
+    DeviceBuffer b;
     b.reserve((size_t)(c_.k - 1) * 2 * c_.k * c_.n, s_);
     hoist_permute_key(c_, k->second, elt, b.get(), s_);
-    return b.get();
+    return (hoist_keys_[elt] = std::move(b)).get();
 }
 
 const uint64_t *Evaluator::hoist_corr(uint32_t elt, int limbs)
@@ -706,15 +706,30 @@ const uint64_t *Evaluator::hoist_corr(uint32_t elt, int limbs)
     if (k == galois_keys.end()) throw std::invalid_argument("Galois key not present");
     auto m = hoist_masks_.find(elt);
     if (m == hoist_masks_.end()) {
-        DeviceBuffer &mb = hoist_masks_[elt];
+        DeviceBuffer mb;
         mb.reserve((size_t)c_.k * c_.n, s_);
         hoist_galois_mask_ntt(c_, elt, mb.get(), s_);
-        m = hoist_masks_.find(elt);
+        m = hoist_masks_.emplace(elt, std::move(mb)).first;
     }
-    DeviceBuffer &b = hoist_corrs_[{elt, limbs}];
+    DeviceBuffer b;
     b.reserve((size_t)2 * (limbs + 1) * c_.n, s_);
     hoist_correction(c_, k->second, m->second.get(), limbs, b.get(), s_);
-    return b.get();
+    return (hoist_corrs_[{elt, limbs}] = std::move(b)).get();
+}
+
+bool Evaluator::hoist_prepare(const std::vector<uint32_t> &elts, int limbs)
+{
+    try {
+        hoist_flag();
+        for (uint32_t e : elts) {
+            hoist_key(e);
+            hoist_corr(e, limbs);
+        }
+    } catch (const std::runtime_error &) {
+        cudaGetLastError();   // an out-of-memory allocation is not sticky
+        return false;
+    }
+    return true;
 }
 
 int *Evaluator::hoist_flag()
@@ -733,7 +748,9 @@ void Evaluator::rotate_vector_many(const Ciphertext &ct, const std::vector<int> 
     std::vector<size_t> direct;
     for (size_t i = 0; i < steps.size(); ++i)
         if (steps[i] != 0 && galois_keys.count(galois_elt(steps[i]))) direct.push_back(i);
-    if (ct.size() == 2 && hoist_pays((int)direct.size(), l)) {
+    std::vector<uint32_t> elts;
+    for (size_t i : direct) elts.push_back(galois_elt(steps[i]));
+    if (hoisting && ct.size() == 2 && hoist_pays((int)direct.size(), l) && hoist_prepare(elts, l)) {
         const size_t N = c_.n;
         DeviceBuffer t, D;
         t.reserve((size_t)l * N, s_);

@@ -215,6 +215,12 @@ public:
     // hoisting pays when at least two rotations share the decomposition and
     // the level is high enough for the ModUp to dominate the key switch
     static bool hoist_pays(int direct_steps, int limbs) { return direct_steps >= 2 && limbs >= 8; }
+    // hoisting on (default) or off; off, or when its data cannot be
+    // allocated, every step is switched on its own (the same words)
+    bool hoisting = true;
+    // the permuted keys and corrections for these rotations, or false when
+    // they cannot be allocated (the allocation error is cleared)
+    bool hoist_prepare(const std::vector<uint32_t> &elts, int limbs);
 
     int total_bits(int limbs) const;
     // is_scale_within_bounds (evaluator.cpp:29-47)

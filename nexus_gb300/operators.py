@@ -139,6 +139,11 @@ class Evaluator:
         check(lib().nexus_evaluator_add_galois_key(self._h, int(elt), key.data_ptr()),
               "nexus_evaluator_add_galois_key")
 
+    def set_hoisting(self, enable: bool) -> None:
+        """Share one decomposition between rotations of one ciphertext (default
+        on; off saves the permuted key copies; the words are the same)."""
+        check(lib().nexus_evaluator_set_hoisting(self._h, 1 if enable else 0), "nexus_evaluator_set_hoisting")
+
     def rotate_vector_many(self, x: Ciphertext, steps) -> list:
         """rotate_vector(x, s) for every s in steps (one shared decomposition
         of x where that is exact)."""

@@ -84,3 +84,17 @@ def test_trivial_c1_falls_back(env):
     data = po.random_residues(np.random.default_rng(5), (2, limbs, N), qs[:limbs])
     data[1] = 0
     _check(ctx, ev, keys, data, STEPS)
+
+
+def test_hoisting_off_gives_the_same_words(env):
+    ctx, ev, keys, qs = env
+    from nexus_gb300.operators import Ciphertext
+    data = po.random_residues(np.random.default_rng(6), (2, 11, N), qs[:11])
+    x = Ciphertext.from_numpy(ctx, data, SCALE)
+    on = [o.to_numpy() for o in ev.rotate_vector_many(x, STEPS)]
+    ev.set_hoisting(False)
+    try:
+        off = [o.to_numpy() for o in ev.rotate_vector_many(x, STEPS)]
+    finally:
+        ev.set_hoisting(True)
+    assert all(np.array_equal(a, b) for a, b in zip(on, off))
