@@ -294,6 +294,27 @@ CtBatch BatchEvaluator::adjust_down(const CtBatch &hi, const CtBatch &lo)
     return adj;
 }
 
+void BatchEvaluator::multiply_const_rescale_add(const CtBatch &x, double value, CtBatch &acc)
+{
+    // the rescaled product lands on acc's level: add_inplace_reduced_error's
+    // equal-level case (acc takes the product's scale, then acc += product),
+    // done by the rescale's finishing kernel
+    if (&x != &acc && x.limbs() >= 2 && acc.limbs() == x.limbs() - 1 && acc.size() == x.size() && acc.batch() == x.batch()) {
+        Plaintext p;
+        ev_.encode_then_drop(value, x.limbs(), x.scale(), p);
+        const double prod = x.scale() * p.scale();
+        ev_.check_scale(prod, x.limbs());
+        const double scale = prod / (double)c_.q[x.limbs() - 1];
+        ev_.check_scale(scale, x.limbs() - 1);
+        rescale_scaled(c_, x.data(), x.size() * x.batch(), x.limbs(), p.residues().data(), acc.data(), stream(), true);
+        acc.scale() = scale;
+        return;
+    }
+    CtBatch tmp;
+    multiply_const_rescale(x, value, tmp);
+    add_inplace_reduced_error(acc, tmp);
+}
+
 void BatchEvaluator::multiply_const_rescale(const CtBatch &ct, double value, CtBatch &dest, double set_scale)
 {
     Plaintext p;

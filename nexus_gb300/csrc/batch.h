@@ -105,6 +105,7 @@ public:
     void multiply_const_inplace(CtBatch &ct, double value);
     void multiply_const(const CtBatch &ct, double value, CtBatch &dest);
     void multiply_const_rescale(const CtBatch &ct, double value, CtBatch &dest, double set_scale = 0.0);
+    void multiply_const_rescale_add(const CtBatch &x, double value, CtBatch &acc);
     void multiply_vector_reduced_error(const CtBatch &ct, const std::vector<std::complex<double>> &values,
                                        CtBatch &dest);
     void add_inplace_reduced_error(CtBatch &a, const CtBatch &b);

@@ -161,7 +161,6 @@ void ModularReducerT<EV, CT>::homomorphic_poly_evaluation(CT &rtn, const CT &cip
     const long len = (1L << (m + 1)) - 1;
     std::vector<CT> ch(len);
     std::vector<bool> chb(len, false);
-    CT tmp;
     for (long i = (1L << m) - 1; i < len; i++) {
         const std::vector<double> &cf = heap[i];
         if (cf.empty()) continue;
@@ -170,8 +169,7 @@ void ModularReducerT<EV, CT>::homomorphic_poly_evaluation(CT &rtn, const CT &cip
         if (!(std::fabs(cf[1]) <= zero)) ev.add_const_inplace(ch[i], cf[0]);
         for (size_t j = 2; j < cf.size(); j++) {
             if (std::fabs(cf[j]) <= zero) continue;
-            ev.multiply_const_rescale((long)j < k ? baby[j] : giant[0], cf[j], tmp);
-            ev.add_inplace_reduced_error(ch[i], tmp);
+            ev.multiply_const_rescale_add((long)j < k ? baby[j] : giant[0], cf[j], ch[i]);
         }
     }
     long depth = m, gindex = 0;

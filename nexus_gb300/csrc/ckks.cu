@@ -534,6 +534,27 @@ Ciphertext Evaluator::adjust_down(const Ciphertext &hi, const Ciphertext &lo)
     return adj;
 }
 
+void Evaluator::multiply_const_rescale_add(const Ciphertext &x, double value, Ciphertext &acc)
+{
+    // the rescaled product lands on acc's level: add_inplace_reduced_error's
+    // equal-level case (acc takes the product's scale, then acc += product),
+    // done by the rescale's finishing kernel
+    if (&x != &acc && x.limbs() >= 2 && acc.limbs() == x.limbs() - 1 && acc.size() == x.size()) {
+        Plaintext p;
+        encode_then_drop(value, x.limbs(), x.scale(), p);
+        const double prod = x.scale() * p.scale();
+        check_scale(prod, x.limbs());
+        const double scale = prod / (double)c_.q[x.limbs() - 1];
+        check_scale(scale, x.limbs() - 1);
+        rescale_scaled(c_, x.data(), x.size(), x.limbs(), p.residues().data(), acc.data(), s_, true);
+        acc.scale() = scale;
+        return;
+    }
+    Ciphertext tmp;
+    multiply_const_rescale(x, value, tmp);
+    add_inplace_reduced_error(acc, tmp);
+}
+
 void Evaluator::multiply_const_rescale(const Ciphertext &ct, double value, Ciphertext &dest, double set_scale)
 {
     Plaintext p;

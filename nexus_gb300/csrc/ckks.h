@@ -183,6 +183,8 @@ public:
     // the constant applied inside the rescale; set_scale > 0 replaces the
     // product's scale before the rescale (as the reduced-error level matching does)
     void multiply_const_rescale(const Ciphertext &ct, double value, Ciphertext &dest, double set_scale = 0.0);
+    // multiply_const_rescale(x, value, tmp) then add_inplace_reduced_error(acc, tmp)
+    void multiply_const_rescale_add(const Ciphertext &x, double value, Ciphertext &acc);
     void multiply_vector_inplace_reduced_error(Ciphertext &ct, const std::vector<std::complex<double>> &values);
     void multiply_vector_reduced_error(const Ciphertext &ct, const std::vector<std::complex<double>> &values,
                                        Ciphertext &dest);

@@ -55,9 +55,10 @@ void galois_permute(Context &c, const uint64_t *in, int polys, int limbs, uint32
                     cudaStream_t s);
 
 // rescale of in * c for a per-limb scalar c (host residues, c[l] < q_l):
-// the words of poly_mul_scalar followed by rescale, in one pass fewer
+// the words of poly_mul_scalar followed by rescale, in one pass fewer;
+// accumulate: out += that (mod q) instead of out = it
 void rescale_scaled(const Context &c, const uint64_t *in, int size, int limbs, const uint64_t *scalars,
-                    uint64_t *out, cudaStream_t s);
+                    uint64_t *out, cudaStream_t s, bool accumulate = false);
 
 // switch_key_inplace: ct[2][limbs] += key-switch(target[limbs])
 void switch_key(Context &c, uint64_t *ct, int limbs, const uint64_t *target, const uint64_t *key, cudaStream_t s);

@@ -267,6 +267,8 @@ __global__ void k_gather_limb_scaled(const ulonglong2 *__restrict__ in, ulonglon
     }
 }
 
+// ACC: out += the rescaled value (mod q) instead of out = it
+template <bool ACC>
 __global__ void k_rescale_finish_scaled(const ulonglong2 *__restrict__ in, const ulonglong2 *__restrict__ t,
                                         ulonglong2 *out, const LimbScalars sc, const PrimeConst *__restrict__ pc,
                                         const ulonglong2 *__restrict__ inv_row, int limbs, int logn, size_t pairs)
@@ -285,6 +287,11 @@ __global__ void k_rescale_finish_scaled(const ulonglong2 *__restrict__ in, const
         ulonglong2 r;
         r.x = mul_shoup(x0 + q - y.x, w.x, w.y, q);
         r.y = mul_shoup(x1 + q - y.y, w.x, w.y, q);
+        if (ACC) {
+            const ulonglong2 a = out[pi];
+            r.x = csub(r.x + a.x, q);
+            r.y = csub(r.y + a.y, q);
+        }
         out[pi] = r;
     }
 }
@@ -413,7 +420,7 @@ void rescale(const Context &c_in, const uint64_t *in, int size, int limbs, uint6
 }
 
 void rescale_scaled(const Context &c_in, const uint64_t *in, int size, int limbs, const uint64_t *scalars,
-                    uint64_t *out, cudaStream_t s)
+                    uint64_t *out, cudaStream_t s, bool accumulate)
 {
     if (limbs < 2) throw std::invalid_argument("rescale needs at least two limbs");
     if (limbs > 64) throw std::invalid_argument("at most 64 limbs");
@@ -434,10 +441,15 @@ void rescale_scaled(const Context &c_in, const uint64_t *in, int size, int limbs
     ld.special = limbs - 1;
     ntt_forward_loaded(c, t, size, LimbMap{limbs - 1, 0, -1}, ld, s);
     pr = pairs_of(c, size, limbs - 1);
-    k_rescale_finish_scaled<<<grid_for(pr), kBlock, 0, s>>>((const ulonglong2 *)in, (const ulonglong2 *)t,
-                                                             (ulonglong2 *)out, w, c.d_pc,
-                                                             c.d_inv_q + (size_t)(limbs - 1) * c.k, limbs, c.logn,
-                                                             pr); NEXUS_LAUNCHED();
+    if (accumulate)
+        k_rescale_finish_scaled<true><<<grid_for(pr), kBlock, 0, s>>>(
+            (const ulonglong2 *)in, (const ulonglong2 *)t, (ulonglong2 *)out, w, c.d_pc,
+            c.d_inv_q + (size_t)(limbs - 1) * c.k, limbs, c.logn, pr);
+    else
+        k_rescale_finish_scaled<false><<<grid_for(pr), kBlock, 0, s>>>(
+            (const ulonglong2 *)in, (const ulonglong2 *)t, (ulonglong2 *)out, w, c.d_pc,
+            c.d_inv_q + (size_t)(limbs - 1) * c.k, limbs, c.logn, pr);
+    NEXUS_LAUNCHED();
 }
 
 void launch_round_spread(const Context &c, const uint64_t *last, uint64_t *out, int polys, int last_prime,
