@@ -472,6 +472,12 @@ int nexus_bootstrapper_stage_batch(nexus_bootstrapper *bs, int stage, nexus_ciph
  * in place as in the reference; len a power of two. */
 int nexus_argmax(nexus_bootstrapper *bs, nexus_ciphertext *x, int len, nexus_ciphertext *res);
 
+/* nexus_argmax over `count` ciphertexts of one level and scale in lockstep:
+ * res[k] receives the words nexus_argmax gives for x[k], and x[k] is updated
+ * as nexus_argmax updates its input.  No counterpart in the reference. */
+int nexus_argmax_batch(nexus_bootstrapper *bs, nexus_ciphertext *const *x, int count, int len,
+                       nexus_ciphertext *const *res);
+
 /* Number of encoded LT diagonals the bootstrapper keeps on the device. */
 int nexus_bootstrapper_cached_plaintexts(const nexus_bootstrapper *bs, uint64_t *count);
 

@@ -215,6 +215,30 @@ extern "C" int nexus_argmax(nexus_bootstrapper *bs, nexus_ciphertext *x, int len
     });
 }
 
+extern "C" int nexus_argmax_batch(nexus_bootstrapper *bs, nexus_ciphertext *const *x, int count, int len,
+                                  nexus_ciphertext *const *res)
+{
+    static const char *fn = "nexus_argmax_batch";
+    if (!bs || !x || !res || count < 1) return fail(fn, "null argument");
+    if (len < 1 || (len & (len - 1))) return fail(fn, "len must be a power of two");
+    for (int k = 0; k < count; ++k) {
+        if (!x[k] || !res[k]) return fail(fn, "null ciphertext");
+        if (const char *e = input_problem(bs->ev->ctx, x[k])) return fail(fn, e);
+        for (int j = 0; j < count; ++j)
+            if (res[k] == x[j] || (j != k && (res[k] == res[j] || x[k] == x[j])))
+                return fail(fn, "results and inputs must be distinct ciphertexts");
+    }
+    return guarded(fn, [&] {
+        BatchBootstrapper &BB = lockstep_form(bs);
+        CKKSEvaluatorT<BatchEvaluator, CtBatch> ck(*bs->bev, bs->ev->ck.scale);
+        ArgmaxEvaluatorT<BatchEvaluator, CtBatch> am(ck, BB);
+        CtBatch xb = gather_batch(bs->ev, x, count), out;
+        am.argmax(xb, out, len);
+        scatter_batch(bs->ev, xb, x);   // the inputs are updated as the single form updates its input
+        scatter_batch(bs->ev, out, res);
+    });
+}
+
 extern "C" int nexus_bootstrapper_stage(nexus_bootstrapper *bs, int stage, nexus_ciphertext *a,
                                         const nexus_ciphertext *b, nexus_ciphertext *r1, nexus_ciphertext *r2)
 {

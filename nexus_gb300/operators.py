@@ -316,6 +316,15 @@ class Bootstrapper:
         check(lib().nexus_argmax(self._h, x.handle, int(length), res.handle), "nexus_argmax")
         return res
 
+    def argmax_batch(self, xs: list, length: int) -> list:
+        """argmax of every ciphertext in lockstep (each x updated in place as
+        the single form does)."""
+        res = [Ciphertext(self.ctx) for _ in xs]
+        a = (C.c_void_p * len(xs))(*[c.handle.value for c in xs])
+        r = (C.c_void_p * len(res))(*[c.handle.value for c in res])
+        check(lib().nexus_argmax_batch(self._h, a, len(xs), int(length), r), "nexus_argmax_batch")
+        return res
+
     def stage(self, stage: int, a: Ciphertext, b: Ciphertext | None = None):
         r1, r2 = Ciphertext(self.ctx), Ciphertext(self.ctx)
         check(lib().nexus_bootstrapper_stage(self._h, stage, a.handle, None if b is None else b.handle, r1.handle,

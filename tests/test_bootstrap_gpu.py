@@ -272,3 +272,10 @@ def test_argmax_matches_oracle(cuda):
     _same(out, want)
     dec = _decrypt(ctx, sk, out)[:length]
     assert np.argmax(dec) == 1 and dec[1] > 1.5 and np.all(np.abs(np.delete(dec, 1)) < 0.5)
+    # the lockstep form over two ciphertexts gives each the single form's words
+    other = to_host(ctx.encrypt_symmetric(sk, pt, top, 75))
+    xs = [Ciphertext.from_numpy(ctx, words, SCALE), Ciphertext.from_numpy(ctx, other, SCALE)]
+    outs = bs.argmax_batch(xs, length)
+    _same(outs[0], want)
+    single = bs.argmax(Ciphertext.from_numpy(ctx, other, SCALE), length)
+    assert np.array_equal(outs[1].to_numpy(), single.to_numpy()) and outs[1].scale == single.scale
