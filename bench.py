@@ -355,6 +355,7 @@ def run_mm_gpu(args, rank, world):
     del res
     barrier(world)
     l0 = ng.kernel_launches()
+    print(f"engine_launches_before_timed={l0}", file=sys.stderr, flush=True)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clk:
@@ -836,6 +837,7 @@ def run_gelu_gpu(args, rank, world):
     del res
     barrier(world)
     l0 = ng.kernel_launches()
+    print(f"engine_launches_before_timed={l0}", file=sys.stderr, flush=True)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clk:
