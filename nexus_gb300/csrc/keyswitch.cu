@@ -114,9 +114,10 @@ __global__ void __launch_bounds__(kBlock, SPLIT ? 4 : 3)
             // partial products summed exactly in three 64-bit accumulators
             // (< 2 * 31 * 2^52 each), one recombination and reduction at the end
             uint64_t h[4] = {0, 0, 0, 0}, m[4] = {0, 0, 0, 0}, w[4] = {0, 0, 0, 0};
-#pragma unroll 2
+            // D is read once: streaming loads keep the key rows in L2
+#pragma unroll 4
             for (int j = 0; j < l; ++j) {
-                const ulonglong2 dv = d[j * dstride];
+                const ulonglong2 dv = __ldcs(d + j * dstride);
                 const ulonglong2 ka = k0[j * kstride], kb = k0[j * kstride + kcomp];
                 const uint64_t dd[2] = {dv.x, dv.y}, aa[4] = {ka.x, ka.y, kb.x, kb.y};
 #pragma unroll
@@ -212,14 +213,12 @@ void ks_modup_inner(Context &c, uint64_t *t, int B, int l, const uint64_t *key, 
     launch_ks_inner(c, D, key, P, l, B, s);
 }
 
-// Stage 2: the rounding terms T [B][2][l][N] of the ModDown from the special
-// limbs of P; `last` is scratch of 2B limbs.
-void ks_moddown_terms(Context &c, const uint64_t *P, int B, int l, uint64_t *T, uint64_t *last, cudaStream_t s)
+// The ModDown rounding terms T [B][2][l][N] from the special limbs already
+// gathered into `last` [B][2][N] (inverse-transformed in place).
+static void ks_moddown_terms_from_last(Context &c, int B, int l, uint64_t *T, uint64_t *last, cudaStream_t s)
 {
-    const size_t N = c.n, Bs = (size_t)B;
+    const size_t Bs = (size_t)B;
     const int sp = c.k - 1;
-    cudaMemcpy2DAsync(last, N * 8, P + (size_t)l * N, (size_t)(l + 1) * N * 8, N * 8, 2 * Bs,
-                      cudaMemcpyDeviceToDevice, s);
     ntt_inverse(c, last, 2 * Bs, LimbMap{1, sp, -1}, s);
     // rounding spread fused into the first pass of the forward NTT
     NttLoader ld;
@@ -228,6 +227,16 @@ void ks_moddown_terms(Context &c, const uint64_t *P, int B, int l, uint64_t *T, 
     ld.group = l;
     ld.special = sp;
     ntt_forward_loaded(c, T, 2 * Bs, LimbMap{l, 0, -1}, ld, s);
+}
+
+// Stage 2: the rounding terms T [B][2][l][N] of the ModDown from the special
+// limbs of P; `last` is scratch of 2B limbs.
+void ks_moddown_terms(Context &c, const uint64_t *P, int B, int l, uint64_t *T, uint64_t *last, cudaStream_t s)
+{
+    const size_t N = c.n, Bs = (size_t)B;
+    cudaMemcpy2DAsync(last, N * 8, P + (size_t)l * N, (size_t)(l + 1) * N * 8, N * 8, 2 * Bs,
+                      cudaMemcpyDeviceToDevice, s);
+    ks_moddown_terms_from_last(c, B, l, T, last, s);
 }
 
 void switch_key_batch(Context &c, uint64_t *ct, int batch, int l, const uint64_t *target, const uint64_t *key,
@@ -368,30 +377,45 @@ __global__ void k_hoist_corr(const uint64_t *__restrict__ key, const uint64_t *_
     }
 }
 
-// P[b][k][i][n] = Ptil[b][k][i][tab[n]] + Corr[k][i][n] mod q_kidx(i)
-__global__ void k_hoist_fix(const uint64_t *__restrict__ Pt, const uint64_t *__restrict__ corr,
-                            const uint32_t *__restrict__ tab, const PrimeConst *__restrict__ pc, int l, int K,
-                            int logn, size_t total, uint64_t *__restrict__ P)
+// last[b][k][n] = Ptil[b][k][l][tab[n]] + Corr[k][l][n] mod p: the special
+// limbs of the rotation's inner product, which the ModDown's INTT needs first
+__global__ void k_hoist_special(const uint64_t *__restrict__ Pt, const uint64_t *__restrict__ corr,
+                                const uint32_t *__restrict__ tab, const PrimeConst *__restrict__ pc, int l, int K,
+                                int logn, size_t total, uint64_t *__restrict__ last)
 {
     const size_t N = (size_t)1 << logn;
+    const uint64_t p = pc[K - 1].q;
     for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
-        const size_t row = x >> logn, n = x & (N - 1);
-        const size_t krow = row % (size_t)(2 * (l + 1));          // k * (l+1) + i
-        const int i = (int)(krow % (size_t)(l + 1));
-        const uint64_t q = pc[(i == l) ? K - 1 : i].q;
-        P[x] = csub(Pt[(row << logn) + tab[n]] + corr[(krow << logn) + n], q);
+        const size_t row = x >> logn, n = x & (N - 1);     // b * 2 + k
+        const size_t k = row & 1;
+        const size_t prow = row * (size_t)(l + 1) + (size_t)l;
+        last[x] = csub(Pt[(prow << logn) + tab[n]] + corr[((k * (size_t)(l + 1) + (size_t)l) << logn) + n], p);
     }
 }
 
-// out[b][0] = pi(in[b][0]) for the c0 polynomial (l limbs) of each ciphertext;
-// in has `pitch` words between ciphertexts, out 2 * l * N
-__global__ void k_permute_c0(const uint64_t *__restrict__ in, size_t pitch, uint64_t *__restrict__ out,
-                             const uint32_t *__restrict__ tab, int logn, size_t poly, size_t total)
+// The rotation's ModDown finish with the hoisted inner product read in
+// place: out[b][k][i][n] = (k == 0 ? c0[b][i][tab[n]] : 0)
+//   + (Ptil[b][k][i][tab[n]] + Corr[k][i][n] - T[b][k][i][n]) * p^{-1} mod q_i
+__global__ void k_hoist_finish(const uint64_t *__restrict__ Pt, const uint64_t *__restrict__ corr,
+                               const uint64_t *__restrict__ T, const uint64_t *__restrict__ ct, size_t ct_pitch,
+                               const uint32_t *__restrict__ tab, const PrimeConst *__restrict__ pc,
+                               const ulonglong2 *__restrict__ inv_p, int l, int logn, size_t total,
+                               uint64_t *__restrict__ out)
 {
-    const size_t mask = ((size_t)1 << logn) - 1;
+    const size_t N = (size_t)1 << logn;
     for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
-        const size_t b = x / poly, r = x - b * poly;
-        out[b * 2 * poly + r] = in[b * pitch + (r & ~mask) + tab[r & mask]];
+        const size_t row = x >> logn, n = x & (N - 1);     // (b * 2 + k) * l + i
+        const size_t bk = row / (size_t)l;
+        const int i = (int)(row - bk * (size_t)l);
+        const size_t b = bk >> 1, k = bk & 1;
+        const uint64_t q = pc[i].q;
+        const ulonglong2 w = inv_p[i];
+        const size_t tn = tab[n];
+        const uint64_t pv = csub(Pt[((bk * (size_t)(l + 1) + (size_t)i) << logn) + tn] +
+                                     corr[((k * (size_t)(l + 1) + (size_t)i) << logn) + n], q);
+        uint64_t v = mul_shoup(pv + q - T[x], w.x, w.y, q);
+        if (k == 0) v = csub(v + ct[b * ct_pitch + ((size_t)i << logn) + tn], q);
+        out[x] = v;
     }
 }
 
@@ -461,25 +485,20 @@ void hoist_rotate(Context &c, const uint64_t *D, int B, int l, uint32_t elt, con
     const int sp = c.k - 1;
     const size_t poly = (size_t)l * N;
     if (ct_pitch == 0) ct_pitch = 2 * poly;
-    // scratch per ciphertext: Ptil[2][l+1] | P[2][l+1] | T[2][l] | last[2]
-    const size_t words = Bs * N * (4 * (size_t)(l + 1) + 2 * (size_t)l + 2);
+    // scratch per ciphertext: Ptil[2][l+1] | T[2][l] | last[2]
+    const size_t words = Bs * N * (2 * (size_t)(l + 1) + 2 * (size_t)l + 2);
     uint64_t *Pt = c.get_scratch(words);
-    uint64_t *P = Pt + Bs * 2 * (l + 1) * N;
-    uint64_t *T = P + Bs * 2 * (l + 1) * N;
+    uint64_t *T = Pt + Bs * 2 * (l + 1) * N;
     uint64_t *last = T + Bs * 2 * l * N;
     launch_ks_inner(c, D, perm_key, Pt, l, B, s);
     const uint32_t *tab = c.galois_table(elt);
-    const size_t tot = Bs * 2 * (l + 1) * N;
-    k_hoist_fix<<<grid_for(tot), kBlock, 0, s>>>(Pt, corr, tab, c.d_pc, l, c.k, c.logn, tot, P);
+    const size_t tot_sp = Bs * 2 * N;
+    k_hoist_special<<<grid_for(tot_sp), kBlock, 0, s>>>(Pt, corr, tab, c.d_pc, l, c.k, c.logn, tot_sp, last);
     NEXUS_LAUNCHED();
-    // out[b] = (pi_g(c0), 0), then the ModDown adds the switched pair
-    k_permute_c0<<<grid_for(Bs * poly), kBlock, 0, s>>>(ct, ct_pitch, out, tab, c.logn, poly, Bs * poly);
-    NEXUS_LAUNCHED();
-    cudaMemset2DAsync(out + poly, 2 * poly * 8, 0, poly * 8, Bs, s);
-    ks_moddown_terms(c, P, B, l, T, last, s);
-    const size_t tot2 = Bs * 2 * l * N;
-    k_moddown_finish<<<grid_for(tot2), kBlock, 0, s>>>(out, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn,
-                                                        tot2);
+    ks_moddown_terms_from_last(c, B, l, T, last, s);
+    const size_t tot = Bs * 2 * poly;
+    k_hoist_finish<<<grid_for(tot), kBlock, 0, s>>>(Pt, corr, T, ct, ct_pitch, tab, c.d_pc,
+                                                     c.d_inv_q + (size_t)sp * c.k, l, c.logn, tot, out);
     NEXUS_LAUNCHED();
 }
 
