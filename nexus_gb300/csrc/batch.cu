@@ -409,23 +409,14 @@ void BatchEvaluator::multiply_reduced_error(const CtBatch &a, const CtBatch &b, 
 
 // ------------------------------------------------------------------ rotations
 
-// out = apply_galois of every ciphertext: both components permuted, c0 into
-// out, c1 into the key-switch targets, then one batched key switch
+// out = apply_galois of every ciphertext, one batched key switch
 void BatchEvaluator::apply_galois(const CtBatch &ct, uint32_t elt, const uint64_t *key, CtBatch &out)
 {
-    const int l = ct.limbs(), B = ct.batch();
-    const size_t poly = (size_t)l * c_.n;
-    uint64_t *perm = nullptr;
-    ck(cudaMallocAsync(&perm, sizeof(uint64_t) * 2 * poly * B, stream()), "cudaMallocAsync");
-    galois_permute(c_, ct.data(), 2 * B, l, elt, perm, stream());
-    out.resize(c_, B, 2, l, stream());
-    out.scale() = ct.scale();
-    ck(cudaMemcpy2DAsync(out.data(), 2 * poly * 8, perm, 2 * poly * 8, poly * 8, B, cudaMemcpyDeviceToDevice,
-                         stream()),
-       "galois copy");
-    ck(cudaMemset2DAsync(out.data() + poly, 2 * poly * 8, 0, poly * 8, B, stream()), "galois zero");
-    switch_key_batch(c_, out.data(), B, l, perm + poly, key, stream(), 2 * poly);
-    cudaFreeAsync(perm, stream());
+    CtBatch res;
+    res.resize(c_, ct.batch(), 2, ct.limbs(), stream());
+    res.scale() = ct.scale();
+    apply_galois_batch(c_, ct.data(), ct.batch(), ct.limbs(), elt, key, res.data(), stream());
+    out = std::move(res);
 }
 
 void BatchEvaluator::apply_galois_inplace(CtBatch &ct, uint32_t elt)

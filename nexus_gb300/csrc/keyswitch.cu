@@ -185,6 +185,38 @@ __global__ void k_moddown_finish(uint64_t *__restrict__ ct, const uint64_t *__re
     }
 }
 
+// the key-switch targets of a Galois automorphism: t[b][j][n] = ct[b][1][j][tab[n]]
+__global__ void k_galois_target(const uint64_t *__restrict__ ct, const uint32_t *__restrict__ tab,
+                                uint64_t *__restrict__ t, int l, int logn, size_t total)
+{
+    const size_t N = (size_t)1 << logn, poly = (size_t)l << logn;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t b = x / poly, r = x - b * poly;
+        t[x] = ct[(2 * b + 1) * poly + (r & ~(N - 1)) + tab[r & (N - 1)]];
+    }
+}
+
+// the automorphism's result: out[b][k][i][n] = (k == 0 ? ct[b][0][i][tab[n]] : 0)
+//   + (P[b][k][i][n] - T[b][k][i][n]) * p^{-1} mod q_i
+__global__ void k_galois_finish(const uint64_t *__restrict__ ct, const uint32_t *__restrict__ tab,
+                                const uint64_t *__restrict__ P, const uint64_t *__restrict__ T,
+                                const PrimeConst *__restrict__ pc, const ulonglong2 *__restrict__ inv_p, int l,
+                                int logn, size_t total, uint64_t *__restrict__ out)
+{
+    const size_t N = (size_t)1 << logn;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = x >> logn, n = x & (N - 1);     // (b * 2 + k) * l + i
+        const size_t bk = row / (size_t)l;
+        const int i = (int)(row - bk * (size_t)l);
+        const uint64_t q = pc[i].q;
+        const ulonglong2 w = inv_p[i];
+        const uint64_t pv = P[((bk * (size_t)(l + 1) + (size_t)i) << logn) + n];
+        uint64_t v = mul_shoup(pv + q - T[x], w.x, w.y, q);
+        if ((bk & 1) == 0) v = csub(v + ct[((bk * (size_t)l + (size_t)i) << logn) + tab[n]], q);
+        out[x] = v;
+    }
+}
+
 }  // namespace
 
 // Stage 1 (ModUp + inner product) of a batched key switch.  t [B][l][N]
@@ -283,19 +315,37 @@ void relinearize(Context &c, const uint64_t *ct3, int l, const uint64_t *key, ui
     cudaFreeAsync(c2, s);
 }
 
+void apply_galois_batch(Context &c, const uint64_t *ct, int B, int l, uint32_t elt, const uint64_t *key,
+                        uint64_t *out, cudaStream_t s)
+{
+    if (l < 1 || l > c.k - 1) throw std::invalid_argument("apply_galois: level out of range");
+    if (B < 1) return;
+    if (reinterpret_cast<uintptr_t>(key) & 15) throw std::invalid_argument("apply_galois: the key must be 16-byte aligned");
+    const size_t N = c.n, Bs = (size_t)B;
+    const int sp = c.k - 1;
+    // scratch per ciphertext: t[l] | D[l][l+1] | P[2][l+1] | T[2][l] | last[2]
+    const size_t words = Bs * N * ((size_t)l + (size_t)l * (l + 1) + 2 * (size_t)(l + 1) + 2 * (size_t)l + 2);
+    uint64_t *t = c.get_scratch(words);
+    uint64_t *D = t + Bs * l * N;
+    uint64_t *P = D + Bs * l * (l + 1) * N;
+    uint64_t *T = P + Bs * 2 * (l + 1) * N;
+    uint64_t *last = T + Bs * 2 * l * N;
+    const uint32_t *tab = c.galois_table(elt);
+    size_t tot = Bs * l * N;
+    k_galois_target<<<grid_for(tot), kBlock, 0, s>>>(ct, tab, t, l, c.logn, tot);
+    NEXUS_LAUNCHED();
+    ks_modup_inner(c, t, B, l, key, D, P, s);
+    ks_moddown_terms(c, P, B, l, T, last, s);
+    tot = Bs * 2 * l * N;
+    k_galois_finish<<<grid_for(tot), kBlock, 0, s>>>(ct, tab, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn,
+                                                      tot, out);
+    NEXUS_LAUNCHED();
+}
+
 void apply_galois(Context &c, const uint64_t *ct, int l, uint32_t elt, const uint64_t *key, uint64_t *out,
                   cudaStream_t s)
 {
-    const size_t N = c.n;
-    uint64_t *tmp = nullptr;
-    if (cudaMallocAsync(&tmp, sizeof(uint64_t) * l * N, s) != cudaSuccess)
-        throw std::runtime_error("cudaMallocAsync");
-    // c0 permuted straight into out, c1 permuted into the key-switch target
-    galois_permute(c, ct, 1, l, elt, out, s);
-    galois_permute(c, ct + (size_t)l * N, 1, l, elt, tmp, s);
-    cudaMemsetAsync(out + (size_t)l * N, 0, sizeof(uint64_t) * l * N, s);
-    switch_key(c, out, l, tmp, key, s);
-    cudaFreeAsync(tmp, s);
+    apply_galois_batch(c, ct, 1, l, elt, key, out, s);
 }
 
 }  // namespace nexus

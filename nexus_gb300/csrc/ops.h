@@ -101,8 +101,14 @@ void hoist_rotate(Context &c, const uint64_t *D, int B, int l, uint32_t elt, con
 void relinearize(Context &c, const uint64_t *ct3, int limbs, const uint64_t *key, uint64_t *out2, cudaStream_t s);
 
 // apply_galois_inplace: permute both polynomials, key-switch the second
+// (out must not overlap ct)
 void apply_galois(Context &c, const uint64_t *ct, int limbs, uint32_t elt, const uint64_t *key, uint64_t *out,
                   cudaStream_t s);
+// the same for B ciphertexts ct/out [B][2][limbs][N] under one key: c1 is
+// permuted straight into the key-switch targets and the ModDown's finishing
+// kernel adds the permuted c0
+void apply_galois_batch(Context &c, const uint64_t *ct, int B, int limbs, uint32_t elt, const uint64_t *key,
+                        uint64_t *out, cudaStream_t s);
 
 // key generation / symmetric encryption / decryption (sampling.cu)
 void keygen_secret(Context &c, uint64_t seed, int hamming_weight, uint64_t *sk, cudaStream_t s);
