@@ -121,15 +121,10 @@ void BatchEvaluator::relinearize_inplace(CtBatch &ct)
     if (ct.size() == 2) return;
     if (!ev_.relin_key) throw std::invalid_argument("relin_keys is not valid for encryption parameters");
     const int l = ct.limbs();
-    const size_t poly = (size_t)l * c_.n;
     CtBatch out;
     out.resize(c_, ct.batch(), 2, l, stream());
     out.scale() = ct.scale();
-    ck(cudaMemcpy2DAsync(out.data(), 2 * poly * 8, ct.data(), 3 * poly * 8, 2 * poly * 8, ct.batch(),
-                         cudaMemcpyDeviceToDevice, stream()),
-       "relinearize copy");
-    // c2 of every ciphertext (pitch 3 polynomials) is the key-switch target
-    switch_key_batch(c_, out.data(), ct.batch(), l, ct.data() + 2 * poly, ev_.relin_key, stream(), 3 * poly);
+    relinearize_batch(c_, ct.data(), ct.batch(), l, ev_.relin_key, out.data(), stream());
     ct = std::move(out);
 }
 

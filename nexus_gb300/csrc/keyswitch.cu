@@ -217,6 +217,27 @@ __global__ void k_galois_finish(const uint64_t *__restrict__ ct, const uint32_t 
     }
 }
 
+// relinearisation's result: out[b][k][i][n] = ct3[b][k][i][n]
+//   + (P[b][k][i][n] - T[b][k][i][n]) * p^{-1} mod q_i
+__global__ void k_relin_finish(const uint64_t *__restrict__ ct3, const uint64_t *__restrict__ P,
+                               const uint64_t *__restrict__ T, const PrimeConst *__restrict__ pc,
+                               const ulonglong2 *__restrict__ inv_p, int l, int logn, size_t total,
+                               uint64_t *__restrict__ out)
+{
+    const size_t N = (size_t)1 << logn;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = x >> logn, n = x & (N - 1);     // (b * 2 + k) * l + i
+        const size_t bk = row / (size_t)l;
+        const int i = (int)(row - bk * (size_t)l);
+        const size_t b = bk >> 1, k = bk & 1;
+        const uint64_t q = pc[i].q;
+        const ulonglong2 w = inv_p[i];
+        const uint64_t pv = P[((bk * (size_t)(l + 1) + (size_t)i) << logn) + n];
+        const uint64_t v = mul_shoup(pv + q - T[x], w.x, w.y, q);
+        out[x] = csub(v + ct3[(((b * 3 + k) * (size_t)l + (size_t)i) << logn) + n], q);
+    }
+}
+
 }  // namespace
 
 // Stage 1 (ModUp + inner product) of a batched key switch.  t [B][l][N]
@@ -303,16 +324,46 @@ void switch_key(Context &c, uint64_t *ct, int l, const uint64_t *target, const u
     switch_key_batch(c, ct, 1, l, target, key, s);
 }
 
+void relinearize_batch(Context &c, const uint64_t *ct3, int B, int l, const uint64_t *key, uint64_t *out2,
+                       cudaStream_t s)
+{
+    if (l < 1 || l > c.k - 1) throw std::invalid_argument("relinearize: level out of range");
+    if (B < 1) return;
+    if (reinterpret_cast<uintptr_t>(key) & 15) throw std::invalid_argument("relinearize: the key must be 16-byte aligned");
+    const size_t N = c.n, Bs = (size_t)B, poly = (size_t)l * N;
+    const int sp = c.k - 1;
+    // scratch per ciphertext: t[l] | D[l][l+1] | P[2][l+1] | T[2][l] | last[2]
+    const size_t words = Bs * N * ((size_t)l + (size_t)l * (l + 1) + 2 * (size_t)(l + 1) + 2 * (size_t)l + 2);
+    uint64_t *t = c.get_scratch(words);
+    uint64_t *D = t + Bs * l * N;
+    uint64_t *P = D + Bs * l * (l + 1) * N;
+    uint64_t *T = P + Bs * 2 * (l + 1) * N;
+    uint64_t *last = T + Bs * 2 * l * N;
+    // c2 of every ciphertext is the key-switch target
+    cudaMemcpy2DAsync(t, sizeof(uint64_t) * poly, ct3 + 2 * poly, sizeof(uint64_t) * 3 * poly, sizeof(uint64_t) * poly,
+                      Bs, cudaMemcpyDeviceToDevice, s);
+    ks_modup_inner(c, t, B, l, key, D, P, s);
+    ks_moddown_terms(c, P, B, l, T, last, s);
+    const size_t tot = Bs * 2 * poly;
+    k_relin_finish<<<grid_for(tot), kBlock, 0, s>>>(ct3, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn, tot,
+                                                     out2);
+    NEXUS_LAUNCHED();
+}
+
 void relinearize(Context &c, const uint64_t *ct3, int l, const uint64_t *key, uint64_t *out2, cudaStream_t s)
 {
-    const size_t N = c.n;
-    // the c2 input must survive until the key switch has read it
-    uint64_t *c2 = nullptr;
-    if (cudaMallocAsync(&c2, sizeof(uint64_t) * l * N, s) != cudaSuccess) throw std::runtime_error("cudaMallocAsync");
-    cudaMemcpyAsync(c2, ct3 + (size_t)2 * l * N, sizeof(uint64_t) * l * N, cudaMemcpyDeviceToDevice, s);
-    if (out2 != ct3) cudaMemcpyAsync(out2, ct3, sizeof(uint64_t) * 2 * l * N, cudaMemcpyDeviceToDevice, s);
-    switch_key(c, out2, l, c2, key, s);
-    cudaFreeAsync(c2, s);
+    const size_t words = (size_t)2 * l * c.n;
+    if (out2 + words <= ct3 || ct3 + 3 * (size_t)l * c.n <= out2) {
+        relinearize_batch(c, ct3, 1, l, key, out2, s);
+        return;
+    }
+    // in place (out2 overlaps ct3): the finishing kernel reads ct3, so it
+    // writes a temporary that is copied back
+    uint64_t *tmp = nullptr;
+    if (cudaMallocAsync(&tmp, sizeof(uint64_t) * words, s) != cudaSuccess) throw std::runtime_error("cudaMallocAsync");
+    relinearize_batch(c, ct3, 1, l, key, tmp, s);
+    cudaMemcpyAsync(out2, tmp, sizeof(uint64_t) * words, cudaMemcpyDeviceToDevice, s);
+    cudaFreeAsync(tmp, s);
 }
 
 void apply_galois_batch(Context &c, const uint64_t *ct, int B, int l, uint32_t elt, const uint64_t *key,

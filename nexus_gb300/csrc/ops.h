@@ -97,6 +97,11 @@ void hoist_correction(Context &c, const uint64_t *key, const uint64_t *M, int l,
 void hoist_rotate(Context &c, const uint64_t *D, int B, int l, uint32_t elt, const uint64_t *perm_key,
                   const uint64_t *corr, const uint64_t *ct, size_t ct_pitch, uint64_t *out, cudaStream_t s);
 
+// relinearize B size-3 ciphertexts ct3 [B][3][l][N] into out2 [B][2][l][N]
+// (no overlap); the ModDown's finishing kernel adds c0 and c1 from ct3
+void relinearize_batch(Context &c, const uint64_t *ct3, int B, int limbs, const uint64_t *key, uint64_t *out2,
+                       cudaStream_t s);
+
 // relinearize a size-3 ciphertext into out2 (may alias ct3)
 void relinearize(Context &c, const uint64_t *ct3, int limbs, const uint64_t *key, uint64_t *out2, cudaStream_t s);
 
