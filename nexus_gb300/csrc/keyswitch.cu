@@ -81,11 +81,13 @@ __device__ __forceinline__ uint64_t reduce_split(uint64_t hh, uint64_t mid, uint
 
 // P[b][k][i'][n] = sum_j D[b][j][i'][n] * key[j][k][kidx(i')][n] mod q(i')
 // One CTA covers 512 coefficients (two per thread, 16-byte loads) of one
-// (b, i') pair; CTAs run i'-major, then by coefficient chunk, with the batch
-// index fastest, so the B CTAs that read one chunk of the key rows run back
-// to back and all but the first find it in L2.  The kernel is bound by its D
-// reads; the register cap keeps four CTAs (32 warps) per SM in flight on the
-// small-prime path, three with 128-bit accumulators.
+// (b, i') pair; CTAs run prime-major, then by ciphertext, with the coefficient
+// chunk fastest: neighbouring CTAs read neighbouring 4 KB pieces of the same
+// D rows (few pages in flight), and a prime's key rows (2l limbs) are read
+// by the B ciphertexts one after another while they are still in L2.  The
+// kernel is bound by its D stream; the register cap keeps four CTAs (32
+// warps) per SM in flight on the small-prime path, three with 128-bit
+// accumulators.
 constexpr int kInnerCoeffs = 2 * kBlock;
 
 template <bool SPLIT>
@@ -95,9 +97,9 @@ __global__ void __launch_bounds__(kBlock, SPLIT ? 4 : 3)
 {
     const int log_chunks = logn - 9;
     for (unsigned blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
-        const unsigned b = blk % (unsigned)B, rest = blk / (unsigned)B;
-        const unsigned chunk = rest & ((1u << log_chunks) - 1);
-        const int i = (int)(rest >> log_chunks);
+        const unsigned chunk = blk & ((1u << log_chunks) - 1), rest = blk >> log_chunks;
+        const unsigned b = rest % (unsigned)B;
+        const int i = (int)(rest / (unsigned)B);
         const size_t n = ((size_t)chunk * kInnerCoeffs) + 2 * threadIdx.x;
         const int kidx = (i == l) ? K - 1 : i;
         const PrimeConst P0 = pc[kidx];
@@ -115,7 +117,7 @@ __global__ void __launch_bounds__(kBlock, SPLIT ? 4 : 3)
             // (< 2 * 31 * 2^52 each), one recombination and reduction at the end
             uint64_t h[4] = {0, 0, 0, 0}, m[4] = {0, 0, 0, 0}, w[4] = {0, 0, 0, 0};
             // D is read once: streaming loads keep the key rows in L2
-#pragma unroll 4
+#pragma unroll 2
             for (int j = 0; j < l; ++j) {
                 const ulonglong2 dv = __ldcs(d + j * dstride);
                 const ulonglong2 ka = k0[j * kstride], kb = k0[j * kstride + kcomp];
