@@ -42,3 +42,29 @@ def test_context_rejects_bad_arguments_without_gpu():
     assert b"log_n" in lib.nexus_last_error()
     assert lib.nexus_ntt_forward(None, None, 1, 0, 1, None) != 0
     assert b"null" in lib.nexus_last_error()
+
+
+def test_lockstep_and_hoisting_entry_points_reject_null_arguments_without_gpu():
+    # every check below runs before any device work
+    from nexus_gb300 import _lib
+    lib = _lib.lib()
+    one = (ctypes.c_void_p * 1)(None)
+    steps = (ctypes.c_int * 1)(1)
+    cases = [
+        ("nexus_switch_key_batch", lambda: lib.nexus_switch_key_batch(None, None, 1, 1, None, None, None), b"null"),
+        ("nexus_rotate_vector_many", lambda: lib.nexus_rotate_vector_many(None, None, steps, 1, one), b"null"),
+        ("nexus_evaluator_set_hoisting", lambda: lib.nexus_evaluator_set_hoisting(None, 1), b"null"),
+        ("nexus_argmax_batch", lambda: lib.nexus_argmax_batch(None, one, 1, 4, one), b"null"),
+        ("nexus_bootstrapper_stage_batch", lambda: lib.nexus_bootstrapper_stage_batch(None, 0, one, None, 1, one, one),
+         b"null"),
+    ]
+    for name, call, word in cases:
+        assert call() != 0, name
+        msg = lib.nexus_last_error()
+        assert msg.startswith(name.encode()) and word in msg, (name, msg)
+
+
+def test_probe_rejects_a_level_outside_the_chain_without_gpu():
+    from nexus_gb300 import probe
+    with pytest.raises(SystemExit):
+        probe.main(["keyswitch", "--limbs", "40", "--once"])
