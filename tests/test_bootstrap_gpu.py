@@ -134,6 +134,30 @@ def test_lockstep_stages_equal_single_stages(env):
         assert np.array_equal(o.to_numpy(), out[k].to_numpy()) and o.scale == out[k].scale
 
 
+def test_lockstep_hoisting_falls_back_on_a_trivial_ciphertext(env):
+    """A batch in which one ciphertext has c1 = 0 cannot share one exact
+    decomposition; the lockstep CoeffToSlot must still give every ciphertext
+    the single-form words."""
+    from nexus_gb300.operators import BOOT_COEFFTOSLOT, BOOT_MODRAISE, BOOT_SET_INITIAL_SCALE, Ciphertext
+    ctx, sk, bs, _, _ = env
+    q0 = float(ctx.moduli[0])
+    a = _input(ctx, sk, 31)[1]
+    trivial = a.to_numpy().copy()
+    trivial[1] = 0
+    raised = []
+    for words in (a.to_numpy(), trivial):
+        x = Ciphertext.from_numpy(ctx, words, SCALE)
+        bs.stage(BOOT_SET_INITIAL_SCALE, x)
+        bs.stage(BOOT_MODRAISE, x)
+        raised.append(x.to_numpy())
+    xs = [Ciphertext.from_numpy(ctx, w, q0) for w in raised]
+    bs.stage_batch(BOOT_SET_INITIAL_SCALE, [a])
+    c1, c2 = bs.stage_batch(BOOT_COEFFTOSLOT, xs)
+    for k, w in enumerate(raised):
+        s1, s2 = bs.stage(BOOT_COEFFTOSLOT, Ciphertext.from_numpy(ctx, w, q0))
+        assert np.array_equal(s1.to_numpy(), c1[k].to_numpy()) and np.array_equal(s2.to_numpy(), c2[k].to_numpy())
+
+
 def test_bootstrap_matches_oracle_and_refreshes(env):
     ctx, sk, bs, obs, _ = env
     vals, x, ox = _input(ctx, sk, 7)
