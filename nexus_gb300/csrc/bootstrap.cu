@@ -818,6 +818,46 @@ void BootstrapperT<EV, CT>::modraise_inplace(CT &cipher)
 
 // ------------------------------------------------------------------ drivers
 
+// EvalMod of the two halves of a full-slot bootstrap, one after the other
+template <class EV, class CT>
+static void evalmod_halves(ModularReducerT<EV, CT> &mr, EV &, CT &m1, CT &m2, const CT &r1, const CT &r2)
+{
+    mr.modular_reduction(m1, r1);
+    mr.modular_reduction(m2, r2);
+}
+
+// In lockstep the two halves take the same operation sequence (same level
+// and scale), so they run as one batch of twice the size: every ciphertext
+// gets the words it gets on its own, with half the launches and key reads
+// per ciphertext.
+static void evalmod_halves(ModularReducerT<BatchEvaluator, CtBatch> &mr, BatchEvaluator &ev, CtBatch &m1,
+                           CtBatch &m2, const CtBatch &r1, const CtBatch &r2)
+{
+    if (r1.batch() != r2.batch() || r1.size() != r2.size() || r1.limbs() != r2.limbs() || r1.scale() != r2.scale()) {
+        mr.modular_reduction(m1, r1);
+        mr.modular_reduction(m2, r2);
+        return;
+    }
+    Context &c = ev.context();
+    cudaStream_t s = ev.stream();
+    const size_t half = (size_t)r1.batch() * r1.words_per_ct() * 8;
+    CtBatch both, m;
+    both.resize(c, 2 * r1.batch(), r1.size(), r1.limbs(), s);
+    both.scale() = r1.scale();
+    if (cudaMemcpyAsync(both.data(), r1.data(), half, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(both.ct(r1.batch()), r2.data(), half, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        throw std::runtime_error("EvalMod: batch copy failed");
+    mr.modular_reduction(m, both);
+    const size_t out_half = (size_t)r1.batch() * m.words_per_ct() * 8;
+    for (CtBatch *dst : {&m1, &m2}) {
+        dst->resize(c, r1.batch(), m.size(), m.limbs(), s);
+        dst->scale() = m.scale();
+    }
+    if (cudaMemcpyAsync(m1.data(), m.data(), out_half, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(m2.data(), m.ct(r1.batch()), out_half, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        throw std::runtime_error("EvalMod: batch copy failed");
+}
+
 template <class EV, class CT>
 void BootstrapperT<EV, CT>::bootstrap_full_3(CT &rtncipher, CT &cipher)
 {
@@ -825,8 +865,7 @@ void BootstrapperT<EV, CT>::bootstrap_full_3(CT &rtncipher, CT &cipher)
     cipher.scale() = (double)ev_->modulus(0);
     CT rtn1, rtn2, m1, m2;
     coefftoslot_full_3(rtn1, rtn2, cipher);
-    mod_reducer.modular_reduction(m1, rtn1);
-    mod_reducer.modular_reduction(m2, rtn2);
+    evalmod_halves(mod_reducer, *ev_, m1, m2, rtn1, rtn2);
     slottocoeff_full_3(rtncipher, m1, m2);
     rtncipher.scale() = final_scale;
 }
