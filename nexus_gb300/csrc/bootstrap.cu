@@ -858,6 +858,40 @@ static void evalmod_halves(ModularReducerT<BatchEvaluator, CtBatch> &mr, BatchEv
         throw std::runtime_error("EvalMod: batch copy failed");
 }
 
+// The single-ciphertext bootstrap's two halves likewise run as a lockstep
+// batch of two: the same words as two modular_reduction calls.
+static void evalmod_halves(ModularReducerT<Evaluator, Ciphertext> &mr, Evaluator &ev, Ciphertext &m1,
+                           Ciphertext &m2, const Ciphertext &r1, const Ciphertext &r2)
+{
+    if (r1.size() != r2.size() || r1.limbs() != r2.limbs() || r1.scale() != r2.scale()) {
+        mr.modular_reduction(m1, r1);
+        mr.modular_reduction(m2, r2);
+        return;
+    }
+    Context &c = ev.context();
+    cudaStream_t s = ev.stream();
+    BatchEvaluator bev(ev);
+    ModularReducerT<BatchEvaluator, CtBatch> bmr(bev, mr.boundary_K, mr.log_width, mr.deg, mr.num_double_formula,
+                                                 mr.inverse_deg);
+    bmr.set_polynomial_heap(mr.heap_k, mr.heap_m, mr.heap, mr.scale_inverse_coeff);
+    const size_t words = (size_t)r1.size() * r1.limbs() * c.n;
+    CtBatch both, m;
+    both.resize(c, 2, r1.size(), r1.limbs(), s);
+    both.scale() = r1.scale();
+    if (cudaMemcpyAsync(both.ct(0), r1.data(), words * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(both.ct(1), r2.data(), words * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        throw std::runtime_error("EvalMod: batch copy failed");
+    bmr.modular_reduction(m, both);
+    const size_t out_words = m.words_per_ct();
+    for (Ciphertext *dst : {&m1, &m2}) {
+        dst->resize(c, m.size(), m.limbs(), s);
+        dst->scale() = m.scale();
+    }
+    if (cudaMemcpyAsync(m1.data(), m.ct(0), out_words * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(m2.data(), m.ct(1), out_words * 8, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        throw std::runtime_error("EvalMod: batch copy failed");
+}
+
 template <class EV, class CT>
 void BootstrapperT<EV, CT>::bootstrap_full_3(CT &rtncipher, CT &cipher)
 {
