@@ -228,6 +228,71 @@ int nexus_decrypt(nexus_context *ctx, const uint64_t *d_sk, const uint64_t *d_ct
                   uint64_t *d_pt, void *stream);
 
 /* ------------------------------------------------------------------ */
+/* Keys and encryption with SEAL's own randomness                       */
+/* ------------------------------------------------------------------ */
+/*
+ * The same words SEAL-4.1-bs produces: every `seed` is 8 words (64 bytes),
+ * the seed that one UniformRandomGeneratorFactory::create() call hands to a
+ * Blake2xbPRNG (randomgen.h:440-448, 504-567).  A factory made with a default
+ * seed (Blake2xbPRNGFactory(seed)) gives that seed to every call; the default
+ * factory draws a fresh one per call.  Key-switching keys make one call per
+ * data prime, so they take n_moduli-1 seeds back to back, in digit order.
+ * The byte streams and samplers run on the host, the NTTs and the modular
+ * arithmetic on the GPU; these calls return after the device work is done.
+ */
+
+/* Bytes [offset, offset + n) of the Blake2xbPRNG stream of `seed` (host only).
+ * Replaces: UniformRandomGenerator::generate (native/src/seal/randomgen.cpp:174-190)
+ *   over Blake2xbPRNG::refill_buffer (:197-207). */
+int nexus_seal_prng_bytes(const uint64_t *seed, uint64_t offset, size_t n, uint8_t *out);
+
+/* One SEAL sampler on a fresh stream advanced by `offset` bytes, written as
+ * residues out [k][2^log_n] (host only): kind 0 sample_poly_ternary, 1
+ * sample_poly_sparse_ternary (hamming_weight nonzeros), 2 sample_poly_cbd,
+ * 3 sample_poly_uniform.
+ * Replaces: native/src/seal/util/rlwe.cpp:21-37, 39-69, 99-135, 137-165. */
+int nexus_seal_sample_poly(const uint64_t *seed, uint64_t offset, int kind, int log_n, const uint64_t *moduli, int k,
+                           int hamming_weight, uint64_t *out);
+
+/* Secret key d_sk [n_moduli][N] (NTT form); hamming_weight > 0 gives the
+ * NEXUS fork's sparse secret.
+ * Replaces: KeyGenerator::generate_sk (native/src/seal/keygenerator.cpp:56-93). */
+int nexus_seal_keygen_secret(nexus_context *ctx, const uint64_t *seed, int hamming_weight, uint64_t *d_sk,
+                             void *stream);
+
+/* Public key d_pk [2][n_moduli][N].
+ * Replaces: KeyGenerator::generate_pk (native/src/seal/keygenerator.cpp:95-122)
+ *   -> encrypt_zero_symmetric (util/rlwe.cpp:311-441). */
+int nexus_seal_keygen_public(nexus_context *ctx, const uint64_t *seed, const uint64_t *d_sk, uint64_t *d_pk,
+                             void *stream);
+
+/* Relinearization key for s^2, d_key [n_moduli-1][2][n_moduli][N]; seeds
+ * [n_moduli-1][8].
+ * Replaces: KeyGenerator::create_relin_keys (native/src/seal/keygenerator.cpp:124-162)
+ *   -> generate_one_kswitch_key (:303-336). */
+int nexus_seal_keygen_relin(nexus_context *ctx, const uint64_t *seeds, const uint64_t *d_sk, uint64_t *d_key,
+                            void *stream);
+
+/* Galois key for X -> X^galois_elt, same layout and seeds.
+ * Replaces: KeyGenerator::create_galois_keys (native/src/seal/keygenerator.cpp:164-223). */
+int nexus_seal_keygen_galois(nexus_context *ctx, const uint64_t *seeds, const uint64_t *d_sk, uint32_t galois_elt,
+                             uint64_t *d_key, void *stream);
+
+/* Public-key encryption of the NTT-form plaintext d_pt [limbs][N] (NULL:
+ * zero) into d_ct [2][limbs][N]: an encryption of zero one level up, divided
+ * and rounded by that level's last prime.
+ * Replaces: Encryptor::encrypt -> encrypt_zero_internal (native/src/seal/encryptor.cpp:88-174,
+ *   176-237) -> encrypt_zero_asymmetric (util/rlwe.cpp:224-309). */
+int nexus_seal_encrypt(nexus_context *ctx, const uint64_t *seed, const uint64_t *d_pk, const uint64_t *d_pt,
+                       int limbs, uint64_t *d_ct, void *stream);
+
+/* Secret-key encryption of d_pt (NULL: zero) into d_ct [2][limbs][N].
+ * Replaces: Encryptor::encrypt_symmetric -> encrypt_zero_symmetric
+ *   (native/src/seal/encryptor.cpp:176-237, util/rlwe.cpp:311-441). */
+int nexus_seal_encrypt_symmetric(nexus_context *ctx, const uint64_t *seed, const uint64_t *d_sk,
+                                 const uint64_t *d_pt, int limbs, uint64_t *d_ct, void *stream);
+
+/* ------------------------------------------------------------------ */
 /* CKKS encoding                                                        */
 /* ------------------------------------------------------------------ */
 

@@ -45,6 +45,15 @@ SIGNATURES = [
     ("nexus_encrypt_symmetric", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c_void_p, C.c_void_p]),
     ("nexus_decrypt", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    ("nexus_seal_prng_bytes", C.c_int, [u64p, C.c_uint64, C.c_size_t, C.c_void_p]),
+    ("nexus_seal_sample_poly", C.c_int, [u64p, C.c_uint64, C.c_int, C.c_int, u64p, C.c_int, C.c_int, u64p]),
+    ("nexus_seal_keygen_secret", C.c_int, [C.c_void_p, u64p, C.c_int, C.c_void_p, C.c_void_p]),
+    ("nexus_seal_keygen_public", C.c_int, [C.c_void_p, u64p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("nexus_seal_keygen_relin", C.c_int, [C.c_void_p, u64p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("nexus_seal_keygen_galois", C.c_int, [C.c_void_p, u64p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("nexus_seal_encrypt", C.c_int, [C.c_void_p, u64p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    ("nexus_seal_encrypt_symmetric", C.c_int,
+     [C.c_void_p, u64p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     ("nexus_encode", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_double, C.c_int, C.c_void_p,
                                C.c_void_p]),
     ("nexus_encode_scalar", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, u64p]),

@@ -22,6 +22,41 @@ def create_coeff_modulus(poly_degree: int, bit_sizes) -> list[int]:
     return [int(x) for x in out]
 
 
+def _u64p(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_uint64))
+
+
+def seal_seed(seed) -> np.ndarray:
+    """SEAL's prng_seed_type: 8 words; an int sets word 0 and leaves the rest zero."""
+    if isinstance(seed, (int, np.integer)):
+        w = np.zeros(8, dtype=np.uint64)
+        w[0] = int(seed)
+        return w
+    w = np.ascontiguousarray(seed, dtype=np.uint64)
+    if w.shape != (8,):
+        raise ValueError("a SEAL seed is 8 64-bit words")
+    return w
+
+
+def seal_prng_bytes(seed, offset: int, n: int) -> bytes:
+    """Bytes [offset, offset + n) of SEAL's Blake2xbPRNG stream for `seed` (host only)."""
+    out = (C.c_uint8 * max(1, n))()
+    check(lib().nexus_seal_prng_bytes(_u64p(seal_seed(seed)), int(offset), int(n), out), "nexus_seal_prng_bytes")
+    return bytes(out)[:n]
+
+
+SEAL_TERNARY, SEAL_SPARSE_TERNARY, SEAL_CBD, SEAL_UNIFORM = 0, 1, 2, 3
+
+
+def seal_sample_poly(seed, kind: int, log_n: int, moduli, hamming_weight: int = 0, offset: int = 0) -> np.ndarray:
+    """One of SEAL's samplers (util/rlwe.cpp) on a fresh stream: residues [k][2^log_n] (host only)."""
+    q = np.ascontiguousarray([int(x) for x in moduli], dtype=np.uint64)
+    out = np.zeros((q.size, 1 << log_n), dtype=np.uint64)
+    check(lib().nexus_seal_sample_poly(_u64p(seal_seed(seed)), int(offset), int(kind), int(log_n), _u64p(q), q.size,
+                                       int(hamming_weight), _u64p(out)), "nexus_seal_sample_poly")
+    return out
+
+
 class Context:
     """RNS context: data primes followed by the special prime."""
 
@@ -179,6 +214,61 @@ class Context:
         check(lib().nexus_decrypt(self._h, sk.data_ptr(), ct.data_ptr(), size, limbs, pt.data_ptr(),
                                   _stream_ptr(stream)), "nexus_decrypt")
         return pt
+
+    # ---- the same with SEAL's own randomness -----------------------------------
+    # seed: an int (word 0 of SEAL's 8-word prng_seed_type, the rest zero) or 8
+    # words; seeds of a key-switching key: one seed for all digits (what a
+    # Blake2xbPRNGFactory with a default seed gives) or one per digit
+    def _digit_seeds(self, seeds):
+        k = len(self.moduli)
+        a = np.asarray(seeds, dtype=np.uint64) if not isinstance(seeds, (int, np.integer)) else None
+        if a is None or a.shape == (8,):
+            one = seal_seed(seeds)
+            return np.ascontiguousarray(np.tile(one, (k - 1, 1)))
+        a = np.ascontiguousarray(a.reshape(-1, 8))
+        if a.shape[0] != k - 1:
+            raise ValueError(f"a key-switching key takes {k - 1} seeds, got {a.shape[0]}")
+        return a
+
+    def seal_keygen_secret(self, seed, hamming_weight: int = 0, stream=None):
+        sk = self._empty(len(self.moduli), self.n)
+        check(lib().nexus_seal_keygen_secret(self._h, _u64p(seal_seed(seed)), int(hamming_weight), sk.data_ptr(),
+                                             _stream_ptr(stream)), "nexus_seal_keygen_secret")
+        return sk
+
+    def seal_keygen_public(self, sk, seed, stream=None):
+        pk = self._empty(2, len(self.moduli), self.n)
+        check(lib().nexus_seal_keygen_public(self._h, _u64p(seal_seed(seed)), sk.data_ptr(), pk.data_ptr(),
+                                             _stream_ptr(stream)), "nexus_seal_keygen_public")
+        return pk
+
+    def seal_keygen_relin(self, sk, seeds, stream=None):
+        k = len(self.moduli)
+        key = self._empty(k - 1, 2, k, self.n)
+        check(lib().nexus_seal_keygen_relin(self._h, _u64p(self._digit_seeds(seeds)), sk.data_ptr(), key.data_ptr(),
+                                            _stream_ptr(stream)), "nexus_seal_keygen_relin")
+        return key
+
+    def seal_keygen_galois(self, sk, elt: int, seeds, stream=None):
+        k = len(self.moduli)
+        key = self._empty(k - 1, 2, k, self.n)
+        check(lib().nexus_seal_keygen_galois(self._h, _u64p(self._digit_seeds(seeds)), sk.data_ptr(), int(elt),
+                                             key.data_ptr(), _stream_ptr(stream)), "nexus_seal_keygen_galois")
+        return key
+
+    def seal_encrypt(self, pk, pt, limbs: int, seed, stream=None):
+        ct = self._empty(2, limbs, self.n)
+        check(lib().nexus_seal_encrypt(self._h, _u64p(seal_seed(seed)), pk.data_ptr(),
+                                       None if pt is None else pt.data_ptr(), limbs, ct.data_ptr(),
+                                       _stream_ptr(stream)), "nexus_seal_encrypt")
+        return ct
+
+    def seal_encrypt_symmetric(self, sk, pt, limbs: int, seed, stream=None):
+        ct = self._empty(2, limbs, self.n)
+        check(lib().nexus_seal_encrypt_symmetric(self._h, _u64p(seal_seed(seed)), sk.data_ptr(),
+                                                 None if pt is None else pt.data_ptr(), limbs, ct.data_ptr(),
+                                                 _stream_ptr(stream)), "nexus_seal_encrypt_symmetric")
+        return ct
 
     def encode_coefficients(self, values, scale: float, limbs: int, out, stream=None):
         v = np.ascontiguousarray(values, dtype=np.float64)

@@ -125,4 +125,18 @@ void encrypt_symmetric(Context &c, const uint64_t *sk, const uint64_t *m, int li
                        cudaStream_t s);
 void decrypt(Context &c, const uint64_t *sk, const uint64_t *ct, int size, int limbs, uint64_t *m, cudaStream_t s);
 
+// the same with SEAL's randomness (sampling.cu, seal_prng.cpp): each seed is
+// 8 words, the seed of one Blake2xbPRNG; kswitch keys take K-1 seeds (one per
+// digit, in order).  These return after the device work is done.
+void seal_keygen_secret(Context &c, const uint64_t seed[8], int hamming_weight, uint64_t *sk, cudaStream_t s);
+void seal_encrypt_zero_symmetric(Context &c, const uint64_t seed[8], const uint64_t *sk, const uint64_t *m,
+                                 int limbs, uint64_t *ct, cudaStream_t s);
+void seal_keygen_kswitch(Context &c, const uint64_t *seeds, const uint64_t *sk, const uint64_t *new_key,
+                         uint64_t *key, cudaStream_t s);
+void seal_keygen_relin(Context &c, const uint64_t *seeds, const uint64_t *sk, uint64_t *key, cudaStream_t s);
+void seal_keygen_galois(Context &c, const uint64_t *seeds, const uint64_t *sk, uint32_t elt, uint64_t *key,
+                        cudaStream_t s);
+void seal_encrypt_asymmetric(Context &c, const uint64_t seed[8], const uint64_t *pk, const uint64_t *m, int limbs,
+                             uint64_t *ct, cudaStream_t s);
+
 }  // namespace nexus

@@ -7,10 +7,11 @@
 // every data prime j, a symmetric encryption of zero at the key level whose
 // component 0, limb j, also carries (p mod q_j) * new_key_j.
 //
-// Randomness comes from a counter-based hash of (seed, stream, index).  It is
-// reproducible and statistically sound but NOT a cryptographic generator:
-// keys made here are for tests and benchmarks.  Deployed keys are generated
-// by the client (SEAL) and imported in SEAL's layout.
+// Two sources of randomness.  keygen_* / encrypt_symmetric draw from a
+// counter-based hash of (seed, stream, index): reproducible and
+// statistically sound but NOT a cryptographic generator, for tests and
+// benchmarks.  seal_* draw from SEAL's own Blake2xbPRNG streams and samplers
+// (seal_prng.cpp) and give SEAL's words for the same seeds.
 #include <algorithm>
 #include <random>
 #include <stdexcept>
@@ -19,6 +20,7 @@
 #include "context.h"
 #include "ntt.h"
 #include "ops.h"
+#include "seal_prng.h"
 
 namespace nexus {
 
@@ -144,6 +146,51 @@ __global__ void k_square(uint64_t *out, const uint64_t *__restrict__ in, const P
     }
 }
 
+// raw uniform words [rows][N] to residues mod the prime of each row (in place allowed)
+__global__ void k_reduce_rows(const uint64_t *raw, uint64_t *out, const PrimeConst *__restrict__ pc, int logn,
+                              size_t total)
+{
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const PrimeConst P = pc[x >> logn];
+        out[x] = barrett_128(raw[x], 0, P.q, P.r0, P.r1);
+    }
+}
+
+// c0 = -(s a + e) (+ m) over `limbs` limbs, and on limb `digit` also
+// + nk * factor: encrypt_zero_symmetric's c0 (util/rlwe.cpp:387-422), the
+// plaintext added by Encryptor::encrypt_internal (encryptor.cpp:232-236) and
+// the key term of generate_one_kswitch_key (keygenerator.cpp:324-329)
+__global__ void k_seal_c0(uint64_t *c0, const uint64_t *__restrict__ a, const uint64_t *__restrict__ e,
+                          const uint64_t *__restrict__ s, const uint64_t *__restrict__ m,
+                          const uint64_t *__restrict__ nk, int digit, uint64_t factor,
+                          const PrimeConst *__restrict__ pc, int limbs, int logn)
+{
+    const size_t total = (size_t)limbs << logn;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
+        const int l = (int)(x >> logn);
+        const PrimeConst P = pc[l];
+        uint64_t v = csub(mul_mod(s[x], a[x], P.q, P.r0, P.r1) + e[x], P.q);
+        v = v ? P.q - v : 0;
+        if (m) v = csub(v + m[x], P.q);
+        if (l == digit) v = csub(v + mul_mod(nk[x], factor, P.q, P.r0, P.r1), P.q);
+        c0[x] = v;
+    }
+}
+
+// c[j] = u pk[j] + e[j], j = 0, 1, over `limbs` limbs (encrypt_zero_asymmetric,
+// util/rlwe.cpp:224-309); pk components are pk_pitch words apart
+__global__ void k_seal_asym(uint64_t *c, const uint64_t *__restrict__ u, const uint64_t *__restrict__ e,
+                            const uint64_t *__restrict__ pk, size_t pk_pitch, const PrimeConst *__restrict__ pc,
+                            int limbs, int logn)
+{
+    const size_t per = (size_t)limbs << logn;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < 2 * per; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t j = x / per, y = x - j * per;
+        const PrimeConst P = pc[y >> logn];
+        c[x] = csub(mul_mod(u[y], pk[j * pk_pitch + y], P.q, P.r0, P.r1) + e[x], P.q);
+    }
+}
+
 }  // namespace
 
 // Ternary secret (uniform in {-1,0,1}, or exactly `hamming_weight` nonzeros
@@ -233,6 +280,180 @@ void decrypt(Context &c, const uint64_t *sk, const uint64_t *ct, int size, int l
 {
     size_t tot = (size_t)limbs * c.n;
     k_decrypt<<<grid_for(tot), kBlock, 0, s>>>(m, ct, size, sk, c.d_pc, limbs, c.logn); NEXUS_LAUNCHED();
+}
+
+// ---------------------------------------------------------------------------
+// Key generation and encryption with SEAL's own randomness: every seed is the
+// 64-byte seed that one UniformRandomGeneratorFactory::create() call gives a
+// Blake2xbPRNG (a factory built with a default seed gives that seed to every
+// call).  The streams and samplers run on the host (seal_prng.cpp), the NTTs
+// and the modular arithmetic here.
+
+namespace {
+
+struct DeviceTemp {
+    void *p = nullptr;
+    cudaStream_t s;
+    DeviceTemp(size_t bytes, cudaStream_t st) : s(st)
+    {
+        if (cudaMallocAsync(&p, bytes, s) != cudaSuccess) throw std::runtime_error("cudaMallocAsync failed");
+    }
+    ~DeviceTemp() { cudaFreeAsync(p, s); }
+    template <class T> T *as(size_t byte_offset = 0) { return reinterpret_cast<T *>((char *)p + byte_offset); }
+};
+
+// small signed values (int8 on the host) as residues [limbs][N] on the device
+void upload_small(Context &c, const std::vector<int8_t> &v, int8_t *d_tmp, uint64_t *out, int limbs, cudaStream_t s)
+{
+    cudaMemcpyAsync(d_tmp, v.data(), v.size(), cudaMemcpyHostToDevice, s);
+    k_small_to_rns<<<grid_for(c.n), kBlock, 0, s>>>(d_tmp, out, c.d_pc, limbs, c.logn); NEXUS_LAUNCHED();
+}
+
+// encrypt_zero_symmetric(secret_key, level of `limbs` primes, is_ntt_form,
+// no saved seed) (util/rlwe.cpp:311-441) into ct [2][limbs][N], with the
+// plaintext m and the key-switching term folded into c0.  `e` [limbs][N] and
+// `e8` [N] are device scratch; with reuse_noise the noise already in `e`
+// and the c1 already in ct (same seed as the call before) are kept.
+void seal_zero_symmetric(Context &c, const uint64_t seed[8], const uint64_t *sk, const uint64_t *m, int limbs,
+                         const uint64_t *nk, int digit, uint64_t factor, uint64_t *ct, uint64_t *e, int8_t *e8,
+                         bool reuse_noise, cudaStream_t s)
+{
+    const size_t N = c.n, words = (size_t)limbs * N;
+    uint64_t *c1 = ct + words;
+    if (!reuse_noise) {
+        sealrng::Stream boot(seed);
+        uint64_t pub[sealrng::kSeedWords];
+        boot.bytes(reinterpret_cast<uint8_t *>(pub), sizeof(pub));
+        sealrng::Stream cs(pub);
+        std::vector<uint64_t> raw(words);
+        sealrng::sample_uniform_raw(cs, N, c.q.data(), limbs, raw.data());
+        std::vector<int8_t> noise(N);
+        sealrng::sample_cbd(boot, N, noise.data());
+        cudaMemcpyAsync(c1, raw.data(), words * sizeof(uint64_t), cudaMemcpyHostToDevice, s);
+        k_reduce_rows<<<grid_for(words), kBlock, 0, s>>>(c1, c1, c.d_pc, c.logn, words); NEXUS_LAUNCHED();
+        upload_small(c, noise, e8, e, limbs, s);
+        ntt_forward(c, e, 1, 0, limbs, s);
+    }
+    k_seal_c0<<<grid_for(words), kBlock, 0, s>>>(ct, c1, e, sk, m, nk, digit, factor, c.d_pc, limbs, c.logn);
+    NEXUS_LAUNCHED();
+}
+
+void check_level(const Context &c, int limbs)
+{
+    if (limbs < 1 || limbs > c.k) throw std::invalid_argument("parms_id is not valid for encryption parameters");
+}
+
+}  // namespace
+
+void seal_keygen_secret(Context &c, const uint64_t seed[8], int hamming_weight, uint64_t *sk, cudaStream_t s)
+{
+    const size_t N = c.n, words = (size_t)c.k * N;
+    if (hamming_weight < 0 || (size_t)hamming_weight > N) throw std::invalid_argument("invalid hamming weight");
+    sealrng::Stream st(seed);
+    if (hamming_weight > 0) {
+        std::vector<uint64_t> v(words);
+        sealrng::sample_sparse_ternary(st, N, c.q.data(), c.k, (size_t)hamming_weight, v.data());
+        // A draw at position N leaves q_{r-1} - 1 at coefficient 0 of row r.
+        // SEAL's forward NTT takes inputs below 4 q_r to the canonical
+        // transform of their residue; from 4 q_r up its output words are out
+        // of range and SEAL rejects the key (is_valid_for) when it is used.
+        for (int r = 1; r < c.k; ++r) {
+            uint64_t &x = v[(size_t)r * N];
+            if (x >= c.q[r]) {
+                if (x / 4 >= c.q[r]) throw std::invalid_argument("secret key is not valid for encryption parameters");
+                x %= c.q[r];
+            }
+        }
+        cudaMemcpyAsync(sk, v.data(), words * sizeof(uint64_t), cudaMemcpyHostToDevice, s);
+    } else {
+        std::vector<int8_t> v(N);
+        sealrng::sample_ternary(st, N, v.data());
+        DeviceTemp t(N, s);
+        upload_small(c, v, t.as<int8_t>(), sk, c.k, s);
+    }
+    ntt_forward(c, sk, 1, 0, c.k, s);
+    cudaStreamSynchronize(s);
+}
+
+void seal_encrypt_zero_symmetric(Context &c, const uint64_t seed[8], const uint64_t *sk, const uint64_t *m,
+                                 int limbs, uint64_t *ct, cudaStream_t s)
+{
+    check_level(c, limbs);
+    const size_t words = (size_t)limbs * c.n;
+    DeviceTemp t(words * sizeof(uint64_t) + c.n, s);
+    seal_zero_symmetric(c, seed, sk, m, limbs, nullptr, -1, 0, ct, t.as<uint64_t>(),
+                        t.as<int8_t>(words * sizeof(uint64_t)), false, s);
+    cudaStreamSynchronize(s);
+}
+
+void seal_keygen_kswitch(Context &c, const uint64_t *seeds, const uint64_t *sk, const uint64_t *new_key,
+                         uint64_t *key, cudaStream_t s)
+{
+    const size_t N = c.n, K = (size_t)c.k, words = K * N;
+    DeviceTemp t(words * sizeof(uint64_t) + N, s);
+    uint64_t *e = t.as<uint64_t>();
+    int8_t *e8 = t.as<int8_t>(words * sizeof(uint64_t));
+    const uint64_t p = c.q[K - 1];
+    for (size_t j = 0; j + 1 < K; ++j) {
+        const uint64_t *sd = seeds + j * sealrng::kSeedWords;
+        uint64_t *kj = key + j * 2 * words;
+        const bool same = j > 0 && std::equal(sd, sd + sealrng::kSeedWords, sd - sealrng::kSeedWords);
+        if (same)   // same seed: the same c1 and noise as the digit before
+            cudaMemcpyAsync(kj + words, kj - words, words * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
+        seal_zero_symmetric(c, sd, sk, nullptr, (int)K, new_key, (int)j, p % c.q[j], kj, e, e8, same, s);
+    }
+    cudaStreamSynchronize(s);
+}
+
+void seal_keygen_relin(Context &c, const uint64_t *seeds, const uint64_t *sk, uint64_t *key, cudaStream_t s)
+{
+    const size_t words = (size_t)c.k * c.n;
+    DeviceTemp sq(words * sizeof(uint64_t), s);
+    k_square<<<grid_for(words), kBlock, 0, s>>>(sq.as<uint64_t>(), sk, c.d_pc, c.logn, words); NEXUS_LAUNCHED();
+    seal_keygen_kswitch(c, seeds, sk, sq.as<uint64_t>(), key, s);
+}
+
+void seal_keygen_galois(Context &c, const uint64_t *seeds, const uint64_t *sk, uint32_t elt, uint64_t *key,
+                        cudaStream_t s)
+{
+    const size_t words = (size_t)c.k * c.n;
+    DeviceTemp rot(words * sizeof(uint64_t), s);
+    galois_permute(c, sk, 1, c.k, elt, rot.as<uint64_t>(), s);
+    seal_keygen_kswitch(c, seeds, sk, rot.as<uint64_t>(), key, s);
+}
+
+// Encryptor::encrypt with the public key (encryptor.cpp:88-174, 176-237): an
+// asymmetric encryption of zero one level up (the key level for the first
+// data level), divided and rounded by that level's last prime, plus m.
+void seal_encrypt_asymmetric(Context &c, const uint64_t seed[8], const uint64_t *pk, const uint64_t *m, int limbs,
+                             uint64_t *ct, cudaStream_t s)
+{
+    check_level(c, limbs);
+    const size_t N = c.n;
+    const int up = limbs < c.k ? limbs + 1 : limbs;
+    const size_t words = (size_t)up * N;
+    sealrng::Stream st(seed);
+    std::vector<int8_t> u(N), e0(N), e1(N);
+    sealrng::sample_ternary(st, N, u.data());
+    sealrng::sample_cbd(st, N, e0.data());
+    sealrng::sample_cbd(st, N, e1.data());
+    // u [up][N] | e [2][up][N] | c [2][up][N] | int8 staging [3][N]
+    DeviceTemp t(5 * words * sizeof(uint64_t) + 3 * N, s);
+    uint64_t *du = t.as<uint64_t>(), *de = du + words, *dc = de + 2 * words;
+    int8_t *d8 = t.as<int8_t>(5 * words * sizeof(uint64_t));
+    upload_small(c, u, d8, du, up, s);
+    upload_small(c, e0, d8 + N, de, up, s);
+    upload_small(c, e1, d8 + 2 * N, de + words, up, s);
+    ntt_forward(c, du, 1, 0, up, s);
+    ntt_forward(c, de, 2, 0, up, s);
+    k_seal_asym<<<grid_for(2 * words), kBlock, 0, s>>>(dc, du, de, pk, (size_t)c.k * N, c.d_pc, up, c.logn);
+    NEXUS_LAUNCHED();
+    if (up > limbs)
+        rescale(c, dc, 2, up, ct, s);
+    else
+        cudaMemcpyAsync(ct, dc, 2 * words * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
+    if (m) poly_add(c, ct, m, 1, limbs, ct, s);
+    cudaStreamSynchronize(s);
 }
 
 }  // namespace nexus

@@ -69,6 +69,11 @@ def lib():
                                  C.POINTER(C.c_size_t)]
         l.sr_ct_load.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, u64p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                  C.POINTER(C.c_double)]
+        l.sr_create_seeded.restype = C.c_void_p
+        l.sr_create_seeded.argtypes = [C.c_int, u64p, C.c_int, u64p, C.c_int]
+        l.sr_export_public.argtypes = [C.c_void_p, u64p]
+        l.sr_encrypt_ntt.argtypes = [C.c_void_p, u64p, C.c_int, C.c_double, C.c_int, u64p]
+        l.sr_prng_bytes.argtypes = [u64p, C.c_uint64, C.c_size_t, C.c_void_p]
         _lib = l
     return _lib
 
@@ -89,6 +94,14 @@ def ntt(log_n: int, q: int, a: np.ndarray, inverse=False) -> np.ndarray:
     return a
 
 
+def prng_bytes(seed, offset: int, n: int) -> bytes:
+    """Bytes [offset, offset + n) of SEAL's Blake2xbPRNG stream for an 8-word seed."""
+    sd = np.ascontiguousarray(seed, dtype=np.uint64)
+    out = (C.c_uint8 * max(1, n))()
+    _ck(lib().sr_prng_bytes(_p(sd), offset, n, out))
+    return bytes(out)[:n]
+
+
 class SealRef:
     """SEAL CKKS context with seeded keys over explicit primes."""
 
@@ -97,7 +110,12 @@ class SealRef:
         self.moduli = [int(q) for q in moduli]
         self.k = len(self.moduli)
         arr = np.array(self.moduli, dtype=np.uint64)
-        self._h = lib().sr_create(log_n, _p(arr), self.k, seed, hamming_weight)
+        if isinstance(seed, (int, np.integer)):
+            self._h = lib().sr_create(log_n, _p(arr), self.k, seed, hamming_weight)
+        else:   # the full 8-word seed of the Blake2xbPRNGFactory
+            sd = np.ascontiguousarray(seed, dtype=np.uint64)
+            assert sd.shape == (8,)
+            self._h = lib().sr_create_seeded(log_n, _p(arr), self.k, _p(sd), hamming_weight)
         if not self._h:
             raise RuntimeError(lib().sr_last_error().decode())
         st = (C.c_int * max(1, len(steps)))(*steps)
@@ -111,6 +129,18 @@ class SealRef:
     def secret_key(self):
         out = np.zeros((self.k, self.n), np.uint64)
         _ck(lib().sr_export_secret(self._h, _p(out)))
+        return out
+
+    def public_key(self):
+        out = np.zeros((2, self.k, self.n), np.uint64)
+        _ck(lib().sr_export_public(self._h, _p(out)))
+        return out
+
+    def encrypt_ntt(self, pt, scale=2.0 ** 40, symmetric=False):
+        """Encryptor::encrypt (public key) or encrypt_symmetric of an NTT-form plaintext [limbs][N]."""
+        pt = np.ascontiguousarray(pt, dtype=np.uint64)
+        out = np.zeros((2,) + pt.shape, np.uint64)
+        _ck(lib().sr_encrypt_ntt(self._h, _p(pt), pt.shape[0], scale, 1 if symmetric else 0, _p(out)))
         return out
 
     def relin_key(self):

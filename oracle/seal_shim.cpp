@@ -485,4 +485,75 @@ int sr_ct_load(void *h, const uint8_t *in, size_t len, uint64_t *out, int *size,
     })
 }
 
+// ---- seeded randomness (key generation and encryption) ----------------
+
+// sr_create with the full 8-word seed of the Blake2xbPRNGFactory
+void *sr_create_seeded(int logn, const uint64_t *moduli, int k, const uint64_t *seed, int hamming_weight)
+{
+    auto *s = static_cast<Shim *>(sr_create(logn, moduli, k, 0, hamming_weight));
+    if (!s) return nullptr;
+    try {
+        EncryptionParameters parms = s->ctx->key_context_data()->parms();
+        prng_seed_type sd{};
+        for (size_t i = 0; i < sd.size(); ++i) sd[i] = seed[i];
+        parms.set_random_generator(std::make_shared<Blake2xbPRNGFactory>(sd));
+        s->ctx.reset(new SEALContext(parms, true, sec_level_type::none));
+        s->enc.reset(new CKKSEncoder(*s->ctx));
+        s->ev.reset(new Evaluator(*s->ctx, *s->enc));
+        return s;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        delete s;
+        return nullptr;
+    }
+}
+
+// public key [2][K][N]
+int sr_export_public(void *h, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD(std::memcpy(out, s.pk->data().data(), sizeof(uint64_t) * 2 * s.k * s.n))
+}
+
+// Encryptor::encrypt (symmetric = 0, public key) or encrypt_symmetric of the
+// NTT-form plaintext pt [limbs][N] at `scale` into out [2][limbs][N]
+int sr_encrypt_ntt(void *h, const uint64_t *pt, int limbs, double scale, int symmetric, uint64_t *out)
+{
+    auto &s = *static_cast<Shim *>(h);
+    GUARD({
+        Plaintext p;
+        p.parms_id() = parms_id_zero;
+        p.resize(limbs * s.n);
+        std::memcpy(p.data(), pt, sizeof(uint64_t) * limbs * s.n);
+        p.parms_id() = pid_for_limbs(s, limbs);
+        p.scale() = scale;
+        Ciphertext c;
+        if (symmetric) {
+            Encryptor e(*s.ctx, *s.sk);
+            e.encrypt_symmetric(p, c);
+        } else {
+            Encryptor e(*s.ctx, *s.pk);
+            e.encrypt(p, c);
+        }
+        store_ct(s, c, out);
+    })
+}
+
+// bytes [offset, offset + n) of the Blake2xbPRNG stream of an 8-word seed
+int sr_prng_bytes(const uint64_t *seed, uint64_t offset, size_t n, uint8_t *out)
+{
+    GUARD({
+        prng_seed_type sd{};
+        for (size_t i = 0; i < sd.size(); ++i) sd[i] = seed[i];
+        Blake2xbPRNG g(sd);
+        std::vector<seal_byte> skip(4096);
+        while (offset) {
+            size_t t = (size_t)std::min<uint64_t>(offset, skip.size());
+            g.generate(t, skip.data());
+            offset -= t;
+        }
+        g.generate(n, reinterpret_cast<seal_byte *>(out));
+    })
+}
+
 }  // extern "C"
