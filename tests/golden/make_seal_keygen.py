@@ -36,10 +36,10 @@ CONFIGS = [
                                                                     for i in range(1, 9)],
          hamming_weight=0, steps=[1, -3], pt_seed=77, enc_limbs=[3, 1], relin=True),
     # sparse secret whose position-N draw leaves a residue below 4q (reduced)
-    dict(name="n1024_sparse_reduced", log_n=10, bits=[30, 29, 40], seed=[6] + [0] * 7, hamming_weight=192,
+    dict(name="n4096_sparse_reduced", log_n=12, bits=[30, 29, 40], seed=[75] + [0] * 7, hamming_weight=192,
          steps=[], pt_seed=78, enc_limbs=[2], relin=True),
     # the same draw with a residue above 4q: SEAL rejects the key
-    dict(name="n1024_sparse_invalid", log_n=10, bits=[40, 30, 40], seed=[6] + [0] * 7, hamming_weight=192,
+    dict(name="n4096_sparse_invalid", log_n=12, bits=[40, 30, 40], seed=[75] + [0] * 7, hamming_weight=192,
          steps=[], pt_seed=0, enc_limbs=[], relin=False),
     # the bootstrap chain at N=2^16 with NEXUS's h=192 sparse secret
     dict(name="n65536_boot_sparse", log_n=16, bits=BOOT_BITS, seed=[2024] + [0] * 7, hamming_weight=192,

@@ -97,7 +97,7 @@ def _oracle_outputs(c):
     return out
 
 
-@pytest.mark.parametrize("name", ["n4096_dense", "n1024_sparse_reduced"])
+@pytest.mark.parametrize("name", ["n4096_dense", "n4096_sparse_reduced"])
 def test_oracle_keygen_and_encryption_match_seal_digests(name):
     c = CONFIGS[name]
     got = {k: digest(v) for k, v in _oracle_outputs(c).items()}
@@ -105,7 +105,7 @@ def test_oracle_keygen_and_encryption_match_seal_digests(name):
 
 
 def test_oracle_rejects_the_key_seal_rejects():
-    c = CONFIGS["n1024_sparse_invalid"]
+    c = CONFIGS["n4096_sparse_invalid"]
     assert c["error"] == "secret key is not valid for encryption parameters"
     kg = sr.SealKeygen(po.OracleContext(c["log_n"], [int(q) for q in c["moduli"]]))
     with pytest.raises(ValueError, match=c["error"]):
