@@ -68,16 +68,6 @@ __device__ __forceinline__ void mac128(uint64_t &lo, uint64_t &hi, uint64_t a, u
     asm("mad.lo.cc.u64 %0, %2, %3, %0;\n\tmadc.hi.u64 %1, %2, %3, %1;" : "+l"(lo), "+l"(hi) : "l"(a), "l"(b));
 }
 
-// v = hh * 2^52 + mid * 2^26 + ll as a 128-bit value, reduced mod q
-__device__ __forceinline__ uint64_t reduce_split(uint64_t hh, uint64_t mid, uint64_t ll, const PrimeConst &P)
-{
-    const uint64_t a = hh << 52, b = mid << 26;
-    const uint64_t lo = a + b;
-    uint64_t hi = (hh >> 12) + (mid >> 38) + (lo < a);
-    const uint64_t lo2 = lo + ll;
-    hi += lo2 < lo;
-    return barrett_128(lo2, hi, P.q, P.r0, P.r1);
-}
 
 // P[b][k][i'][n] = sum_j D[b][j][i'][n] * key[j][k][kidx(i')][n] mod q(i')
 // One CTA covers 512 coefficients (two per thread, 16-byte loads) of one
@@ -112,10 +102,11 @@ __global__ void __launch_bounds__(kBlock, SPLIT ? 4 : 3)
         uint64_t *pb = P + (((size_t)b * 2 * (l + 1)) << logn) + n;
         ulonglong2 r0, r1;
         if (SPLIT) {
-            // every residue below 2^52: each product as four 26 x 26-bit
-            // partial products summed exactly in three 64-bit accumulators
-            // (< 2 * 31 * 2^52 each), one recombination and reduction at the end
-            uint64_t h[4] = {0, 0, 0, 0}, m[4] = {0, 0, 0, 0}, w[4] = {0, 0, 0, 0};
+            // every residue below 2^52: each product from three 32 x 32 -> 64
+            // products of its 26-bit halves (mac_split), summed exactly in
+            // three 64-bit accumulators, one reduction at the end; the
+            // inner product is bound by these wide multiplies
+            uint64_t h[4] = {0, 0, 0, 0}, x[4] = {0, 0, 0, 0}, w[4] = {0, 0, 0, 0};
             // D is read once: streaming loads keep the key rows in L2
 #pragma unroll 2
             for (int j = 0; j < l; ++j) {
@@ -123,17 +114,10 @@ __global__ void __launch_bounds__(kBlock, SPLIT ? 4 : 3)
                 const ulonglong2 ka = k0[j * kstride], kb = k0[j * kstride + kcomp];
                 const uint64_t dd[2] = {dv.x, dv.y}, aa[4] = {ka.x, ka.y, kb.x, kb.y};
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const uint64_t dx = dd[e & 1];
-                    const uint32_t dh = (uint32_t)(dx >> 26), dl = (uint32_t)dx & 0x3ffffffu;
-                    const uint32_t ah = (uint32_t)(aa[e] >> 26), al = (uint32_t)aa[e] & 0x3ffffffu;
-                    h[e] += (uint64_t)dh * ah;
-                    m[e] += (uint64_t)dh * al + (uint64_t)dl * ah;
-                    w[e] += (uint64_t)dl * al;
-                }
+                for (int e = 0; e < 4; ++e) mac_split(h[e], x[e], w[e], dd[e & 1], aa[e]);
             }
-            r0 = make_ulonglong2(reduce_split(h[0], m[0], w[0], P0), reduce_split(h[1], m[1], w[1], P0));
-            r1 = make_ulonglong2(reduce_split(h[2], m[2], w[2], P0), reduce_split(h[3], m[3], w[3], P0));
+            r0 = make_ulonglong2(reduce_karatsuba(h[0], x[0], w[0], P0), reduce_karatsuba(h[1], x[1], w[1], P0));
+            r1 = make_ulonglong2(reduce_karatsuba(h[2], x[2], w[2], P0), reduce_karatsuba(h[3], x[3], w[3], P0));
         } else {
             uint64_t lo[4] = {0, 0, 0, 0}, hi[4] = {0, 0, 0, 0};
 #pragma unroll 2

@@ -79,4 +79,38 @@ struct PrimeConst {
     uint64_t inv_n, inv_n_q; // n^{-1} mod q and its Shoup quotient
 };
 
+#ifdef __CUDACC__
+
+// Exact sums of products a * b with a, b < 2^52 from 32 x 32 -> 64 products
+// of their 26-bit halves (Karatsuba): h += ah*bh, w += al*bl and
+// x += (ah+al)*(bh+bl), each term below 2^54, so up to 32 terms stay below
+// 2^59.  The middle term sum(ah*bl + al*bh) = x - h - w (below 2^58).
+__device__ __forceinline__ void mac_split(uint64_t &h, uint64_t &x, uint64_t &w, uint64_t a, uint64_t b)
+{
+    const uint32_t ah = (uint32_t)(a >> 26), al = (uint32_t)a & 0x3ffffffu;
+    const uint32_t bh = (uint32_t)(b >> 26), bl = (uint32_t)b & 0x3ffffffu;
+    h += (uint64_t)ah * bh;
+    w += (uint64_t)al * bl;
+    x += (uint64_t)(ah + al) * (bh + bl);
+}
+
+// hh * 2^52 + mid * 2^26 + ll as a 128-bit value, reduced mod q
+__device__ __forceinline__ uint64_t reduce_split(uint64_t hh, uint64_t mid, uint64_t ll, const PrimeConst &P)
+{
+    const uint64_t a = hh << 52, b = mid << 26;
+    const uint64_t lo = a + b;
+    uint64_t hi = (hh >> 12) + (mid >> 38) + (lo < a);
+    const uint64_t lo2 = lo + ll;
+    hi += lo2 < lo;
+    return barrett_128(lo2, hi, P.q, P.r0, P.r1);
+}
+
+// the sum accumulated by mac_split, reduced mod q
+__device__ __forceinline__ uint64_t reduce_karatsuba(uint64_t h, uint64_t x, uint64_t w, const PrimeConst &P)
+{
+    return reduce_split(h, x - h - w, w, P);
+}
+
+#endif  // __CUDACC__
+
 }  // namespace nexus
