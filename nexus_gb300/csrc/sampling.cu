@@ -286,7 +286,8 @@ void decrypt(Context &c, const uint64_t *sk, const uint64_t *ct, int size, int l
 // Key generation and encryption with SEAL's own randomness: every seed is the
 // 64-byte seed that one UniformRandomGeneratorFactory::create() call gives a
 // Blake2xbPRNG (a factory built with a default seed gives that seed to every
-// call).  The streams and samplers run on the host (seal_prng.cpp), the NTTs
+// call).  The uniform samples' streams run on the GPU (seal_prng_gpu.cu), the
+// short ones (secret, noise, ternary u) on the host (seal_prng.cpp), the NTTs
 // and the modular arithmetic here.
 
 namespace {
@@ -324,12 +325,9 @@ void seal_zero_symmetric(Context &c, const uint64_t seed[8], const uint64_t *sk,
         sealrng::Stream boot(seed);
         uint64_t pub[sealrng::kSeedWords];
         boot.bytes(reinterpret_cast<uint8_t *>(pub), sizeof(pub));
-        sealrng::Stream cs(pub);
-        std::vector<uint64_t> raw(words);
-        sealrng::sample_uniform_raw(cs, N, c.q.data(), limbs, raw.data());
+        sealrng::sample_uniform_raw_device(pub, c.logn, c.q.data(), limbs, c1, s);
         std::vector<int8_t> noise(N);
         sealrng::sample_cbd(boot, N, noise.data());
-        cudaMemcpyAsync(c1, raw.data(), words * sizeof(uint64_t), cudaMemcpyHostToDevice, s);
         k_reduce_rows<<<grid_for(words), kBlock, 0, s>>>(c1, c1, c.d_pc, c.logn, words); NEXUS_LAUNCHED();
         upload_small(c, noise, e8, e, limbs, s);
         ntt_forward(c, e, 1, 0, limbs, s);

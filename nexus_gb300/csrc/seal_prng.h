@@ -15,6 +15,7 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <cuda_runtime.h>
 
 namespace nexus {
 namespace sealrng {
@@ -66,6 +67,12 @@ void sample_sparse_ternary(Stream &s, size_t n, const uint64_t *q, int k, size_t
 void sample_uniform_raw(Stream &s, size_t n, const uint64_t *q, int k, uint64_t *raw);
 // the bound of sample_poly_uniform: 2^64 - 1 - ((2^64 - 1) mod q) - 1
 uint64_t uniform_bound(uint64_t q);
+
+// sample_uniform_raw of a fresh stream of `seed` into d_raw [k][2^logn] on
+// the device (seal_prng_gpu.cu): the bulk refills on the GPU, the redraws
+// from the stream after the bulk on the host.  Returns after the device work.
+void sample_uniform_raw_device(const uint64_t seed[kSeedWords], int logn, const uint64_t *q, int k, uint64_t *d_raw,
+                               cudaStream_t s);
 
 }  // namespace sealrng
 }  // namespace nexus
