@@ -75,9 +75,9 @@ __device__ __forceinline__ void mac128(uint64_t &lo, uint64_t &hi, uint64_t a, u
 // chunk fastest: neighbouring CTAs read neighbouring 4 KB pieces of the same
 // D rows (few pages in flight), and a prime's key rows (2l limbs) are read
 // by the B ciphertexts one after another while they are still in L2.  The
-// kernel is bound by its D stream; the register cap keeps four CTAs (32
-// warps) per SM in flight on the small-prime path, three with 128-bit
-// accumulators.
+// kernel is bound by its D stream and its 32 x 32 -> 64 multiplies together
+// (three per product on the small-prime path); the register cap keeps four
+// CTAs (32 warps) per SM in flight there, three with 128-bit accumulators.
 constexpr int kInnerCoeffs = 2 * kBlock;
 
 template <bool SPLIT>
