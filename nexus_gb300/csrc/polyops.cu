@@ -164,6 +164,25 @@ __global__ void k_add_scalar(const ulonglong2 *__restrict__ in, const LimbScalar
     }
 }
 
+// (x0 y0, x0 y1 + x1 y0, x1 y1) mod q from three 128-bit products: the cross
+// term is (x0 + x1)(y0 + y1) - x0 y0 - x1 y1, exact in 128 bits (below 2^123
+// for q < 2^61), then one reduction each
+__device__ __forceinline__ void tensor3(uint64_t x0, uint64_t x1, uint64_t y0, uint64_t y1, const PrimeConst &P,
+                                        uint64_t &o0, uint64_t &o1, uint64_t &o2)
+{
+    const uint64_t l00 = x0 * y0, h00 = __umul64hi(x0, y0);
+    const uint64_t l11 = x1 * y1, h11 = __umul64hi(x1, y1);
+    const uint64_t sx = x0 + x1, sy = y0 + y1;
+    const uint64_t ls = sx * sy, hs = __umul64hi(sx, sy);
+    const uint64_t m1 = ls - l00;
+    uint64_t mh = hs - h00 - (ls < l00);
+    const uint64_t m2 = m1 - l11;
+    mh = mh - h11 - (m1 < l11);
+    o0 = barrett_128(l00, h00, P.q, P.r0, P.r1);
+    o1 = barrett_128(m2, mh, P.q, P.r0, P.r1);
+    o2 = barrett_128(l11, h11, P.q, P.r0, P.r1);
+}
+
 // ckks_multiply (evaluator.cpp:770-850): out3 = (a0 b0, a0 b1 + a1 b0, a1 b1)
 // over `batch` ciphertext pairs laid out back to back ([batch][2] in, [batch][3] out)
 __global__ void k_tensor(const ulonglong2 *__restrict__ a_, const ulonglong2 *__restrict__ b_, ulonglong2 *out_,
@@ -178,13 +197,11 @@ __global__ void k_tensor(const ulonglong2 *__restrict__ a_, const ulonglong2 *__
         const int limb = (int)(e >> (logn - 1));
         const PrimeConst P = pc[limb];
         const ulonglong2 x0 = a[e], x1 = a[e + poly_pairs], y0 = b[e], y1 = b[e + poly_pairs];
-        ulonglong2 o0, o1, o2;
-        o0.x = mul_mod(x0.x, y0.x, P.q, P.r0, P.r1);
-        o0.y = mul_mod(x0.y, y0.y, P.q, P.r0, P.r1);
-        o2.x = mul_mod(x1.x, y1.x, P.q, P.r0, P.r1);
-        o2.y = mul_mod(x1.y, y1.y, P.q, P.r0, P.r1);
-        o1.x = add_mod(mul_mod(x0.x, y1.x, P.q, P.r0, P.r1), mul_mod(x1.x, y0.x, P.q, P.r0, P.r1), P.q);
-        o1.y = add_mod(mul_mod(x0.y, y1.y, P.q, P.r0, P.r1), mul_mod(x1.y, y0.y, P.q, P.r0, P.r1), P.q);
+        uint64_t r[6];
+        tensor3(x0.x, x1.x, y0.x, y1.x, P, r[0], r[1], r[2]);
+        tensor3(x0.y, x1.y, y0.y, y1.y, P, r[3], r[4], r[5]);
+        const ulonglong2 o0 = make_ulonglong2(r[0], r[3]), o1 = make_ulonglong2(r[1], r[4]),
+                         o2 = make_ulonglong2(r[2], r[5]);
         out[e] = o0;
         out[e + poly_pairs] = o1;
         out[e + 2 * poly_pairs] = o2;
