@@ -15,7 +15,7 @@ from oracle import pyoracle as po
 from oracle import seal_random as sr
 
 KAT = json.loads((Path(__file__).parent / "golden" / "seal_keygen_kat.json").read_text())
-CONFIGS = {c["name"]: c for c in KAT["configs"]}
+CASES = {c["name"]: c for c in KAT["configs"]}
 
 
 def digest(a) -> str:
@@ -99,13 +99,13 @@ def _oracle_outputs(c):
 
 @pytest.mark.parametrize("name", ["n4096_dense", "n4096_sparse_reduced"])
 def test_oracle_keygen_and_encryption_match_seal_digests(name):
-    c = CONFIGS[name]
+    c = CASES[name]
     got = {k: digest(v) for k, v in _oracle_outputs(c).items()}
     assert got == c["sha256"]
 
 
 def test_oracle_rejects_the_key_seal_rejects():
-    c = CONFIGS["n4096_sparse_invalid"]
+    c = CASES["n4096_sparse_invalid"]
     assert c["error"] == "secret key is not valid for encryption parameters"
     kg = sr.SealKeygen(po.OracleContext(c["log_n"], [int(q) for q in c["moduli"]]))
     with pytest.raises(ValueError, match=c["error"]):

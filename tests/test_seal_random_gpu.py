@@ -15,7 +15,7 @@ from oracle import seal_random as sr
 pytestmark = pytest.mark.gpu
 
 KAT = json.loads((Path(__file__).parent / "golden" / "seal_keygen_kat.json").read_text())
-CONFIGS = {c["name"]: c for c in KAT["configs"]}
+CASES = {c["name"]: c for c in KAT["configs"]}
 
 
 def _digest(t) -> str:
@@ -36,11 +36,11 @@ def _pt(ctx, seed, log_n, moduli):
     return torch.from_numpy(a.view(np.int64)).cuda()
 
 
-@pytest.mark.parametrize("name", list(CONFIGS))
+@pytest.mark.parametrize("name", list(CASES))
 def test_engine_matches_seal_digests(name):
     import torch
     import nexus_gb300 as ng
-    c = CONFIGS[name]
+    c = CASES[name]
     qs = [int(q) for q in c["moduli"]]
     ctx = ng.Context(c["log_n"], qs)
     seed = np.array(c["seed"], dtype=np.uint64)
