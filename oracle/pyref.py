@@ -71,6 +71,8 @@ def lib():
                                  C.POINTER(C.c_double)]
         l.sr_create_seeded.restype = C.c_void_p
         l.sr_create_seeded.argtypes = [C.c_int, u64p, C.c_int, u64p, C.c_int]
+        l.sr_create_seed_list.restype = C.c_void_p
+        l.sr_create_seed_list.argtypes = [C.c_int, u64p, C.c_int, u64p, C.c_int, C.c_int]
         l.sr_export_public.argtypes = [C.c_void_p, u64p]
         l.sr_encrypt_ntt.argtypes = [C.c_void_p, u64p, C.c_int, C.c_double, C.c_int, u64p]
         l.sr_prng_bytes.argtypes = [u64p, C.c_uint64, C.c_size_t, C.c_void_p]
@@ -112,6 +114,9 @@ class SealRef:
         arr = np.array(self.moduli, dtype=np.uint64)
         if isinstance(seed, (int, np.integer)):
             self._h = lib().sr_create(log_n, _p(arr), self.k, seed, hamming_weight)
+        elif np.ndim(seed) == 2:   # one 8-word seed per create() call, in call order
+            sd = np.ascontiguousarray(seed, dtype=np.uint64)
+            self._h = lib().sr_create_seed_list(log_n, _p(arr), self.k, _p(sd), sd.shape[0], hamming_weight)
         else:   # the full 8-word seed of the Blake2xbPRNGFactory
             sd = np.ascontiguousarray(seed, dtype=np.uint64)
             assert sd.shape == (8,)

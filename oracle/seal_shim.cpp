@@ -487,6 +487,52 @@ int sr_ct_load(void *h, const uint8_t *in, size_t len, uint64_t *out, int *size,
 
 // ---- seeded randomness (key generation and encryption) ----------------
 
+namespace {
+// A factory that hands create() calls the seeds of a list in order, so every
+// Blake2xbPRNG SEAL makes (one per sampled key, digit and encryption) gets
+// its own known seed.  Test infrastructure only.
+class SeedListFactory : public UniformRandomGeneratorFactory {
+public:
+    explicit SeedListFactory(std::vector<prng_seed_type> seeds)
+        : UniformRandomGeneratorFactory(prng_seed_type{}), seeds_(std::move(seeds))
+    {}
+
+protected:
+    auto create_impl(prng_seed_type) -> std::shared_ptr<UniformRandomGenerator> override
+    {
+        if (next_ >= seeds_.size()) throw std::logic_error("seed list exhausted");
+        return std::make_shared<Blake2xbPRNG>(seeds_[next_++]);
+    }
+
+private:
+    std::vector<prng_seed_type> seeds_;
+    size_t next_ = 0;
+};
+}  // namespace
+
+// sr_create whose PRNG factory gives create() call i the seed seeds[i] (8 words each)
+void *sr_create_seed_list(int logn, const uint64_t *moduli, int k, const uint64_t *seeds, int nseeds,
+                          int hamming_weight)
+{
+    auto *s = static_cast<Shim *>(sr_create(logn, moduli, k, 0, hamming_weight));
+    if (!s) return nullptr;
+    try {
+        EncryptionParameters parms = s->ctx->key_context_data()->parms();
+        std::vector<prng_seed_type> list((size_t)nseeds);
+        for (int i = 0; i < nseeds; ++i)
+            for (size_t w = 0; w < list[i].size(); ++w) list[i][w] = seeds[(size_t)i * 8 + w];
+        parms.set_random_generator(std::make_shared<SeedListFactory>(std::move(list)));
+        s->ctx.reset(new SEALContext(parms, true, sec_level_type::none));
+        s->enc.reset(new CKKSEncoder(*s->ctx));
+        s->ev.reset(new Evaluator(*s->ctx, *s->enc));
+        return s;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        delete s;
+        return nullptr;
+    }
+}
+
 // sr_create with the full 8-word seed of the Blake2xbPRNGFactory
 void *sr_create_seeded(int logn, const uint64_t *moduli, int k, const uint64_t *seed, int hamming_weight)
 {

@@ -135,6 +135,33 @@ def test_oracle_matches_live_seal():
             assert np.array_equal(kg.encrypt_symmetric(seed, sk, pt, limbs), ref.encrypt_ntt(pt, symmetric=True))
 
 
+def test_oracle_matches_live_seal_with_a_seed_per_call():
+    # a factory handing every create() its own seed: SEAL draws the secret
+    # key, the public key, each relinearisation digit, each Galois digit and
+    # each encryption from separate streams, in that order
+    from oracle import pyref
+    if not pyref.available():
+        pytest.skip("SEAL reference build unavailable")
+    log_n, n = 11, 1 << 11
+    qs = po.create_coeff_modulus(n, [45, 36, 36, 45])
+    k = len(qs)
+    calls = 2 + 2 * (k - 1) + 2
+    seeds = (np.arange(calls * 8, dtype=np.uint64).reshape(calls, 8) + np.uint64(1)) * np.uint64(0x9E3779B97F4A7C15)
+    for hw in (0, 64):
+        ref = pyref.SealRef(log_n, qs, seed=seeds, hamming_weight=hw, steps=[3])
+        kg = sr.SealKeygen(po.OracleContext(log_n, qs))
+        sk = kg.secret_key(seeds[0], hw)
+        assert np.array_equal(sk, ref.secret_key())
+        pk = kg.public_key(seeds[1], sk)
+        assert np.array_equal(pk, ref.public_key())
+        assert np.array_equal(kg.relin_key(list(seeds[2:k + 1]), sk), ref.relin_key())
+        e = ref.galois_elt(3)
+        assert np.array_equal(kg.galois_key(list(seeds[k + 1:2 * k]), sk, e), ref.galois_key(e))
+        pt = sr.sample_uniform(sr.Stream(5), n, qs[:2])
+        assert np.array_equal(kg.encrypt(seeds[2 * k], pk, pt, 2), ref.encrypt_ntt(pt))
+        assert np.array_equal(kg.encrypt_symmetric(seeds[2 * k + 1], sk, pt, 2), ref.encrypt_ntt(pt, symmetric=True))
+
+
 def test_seal_entry_points_reject_bad_arguments_without_gpu():
     from nexus_gb300 import _lib
     lib = _lib.lib()
