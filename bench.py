@@ -766,6 +766,193 @@ def cpu_boot_sample(workers: int = 1):
                       f"modelled {t_boot:.1f} s per bootstrap per core)"}
 
 
+# ----------------------------------------------------------------------------- BERT layer workload
+
+BERT_LOGN = 16
+BERT_BITS = [51] + [46] * 19 + [51] * 14 + [51]   # 19 levels between bootstraps (NEXUS's GELU needs 18)
+BERT_SCALE = 2.0 ** 46
+BERT_SEED = 600
+
+
+def bert_config():
+    return {"workload": "bert_base_layer_n65536", "N": 1 << BERT_LOGN, "hidden": 768, "heads": 12, "ffn": 3072,
+            "requests": [128, 32, 64], "lanes": "[128] | [32 + 64]", "token_slots_per_block": 256,
+            "moduli_bits": "51 + 19x46 + 14x51 + special 51", "hamming_weight": 192, "scale": "2^46",
+            "weights": "N(0, 0.02)", "tokens": "N(0, 1)", "parallelism": "replicas",
+            "l2": "keys (~110 GB), encoded weights (~60 GB) and activations far above L2, no flush"}
+
+
+def _seal_seed(tag: int):
+    import numpy as np
+    return np.array([(0x9E3779B97F4A7C15 * (tag + i + 1)) % 2 ** 64 for i in range(8)], dtype=np.uint64)
+
+
+def run_bert_gpu(args, rank, world):
+    import numpy as np
+    import torch
+
+    import nexus_gb300 as ng
+    from nexus_gb300 import bert as NB
+    from nexus_gb300.operators import Bootstrapper, Ciphertext, Evaluator
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = 1 << BERT_LOGN
+    qs = ng.create_coeff_modulus(n, BERT_BITS)
+    ctx = ng.Context(BERT_LOGN, qs)
+    seed = _seal_seed(BERT_SEED + rank)
+    sk = ctx.seal_keygen_secret(seed, 192)
+    ev = Evaluator(ctx, BERT_SCALE, ctx.seal_keygen_relin(sk, seed))
+    log_nh = BERT_LOGN - 1
+    bs = Bootstrapper(ev, 10, log_nh, log_nh, len(qs) - 2, BERT_SCALE, 25, 59, 2, 1)
+    shape = NB.BertShape()
+    w = NB.random_weights(shape, np.random.default_rng(11 + rank))
+    rng = np.random.default_rng(12 + rank)
+    tokens = [[rng.normal(0, 1, (L, shape.hidden)) for (_, L) in lane] for lane in shape.lanes]
+    steps = bs.rotation_steps(log_nh)
+    bs.prepare_mod_polynomial()
+    bs.generate_LT_coefficient_3()
+    layer = NB.BertLayer(bs, shape, w)
+    all_steps = steps + [s for s in layer.rotation_steps() if s not in steps]
+    for s in all_steps:
+        e = ctx.galois_elt(s)
+        ev.add_galois_key(e, ctx.seal_keygen_galois(sk, e, seed))
+    top = len(qs) - 1
+    x, host_x = [], []
+    for lane in range(len(shape.lanes)):
+        for v in NB.pack_lane(shape, n // 2, lane, tokens[lane]):
+            pt = torch.empty((top, n), dtype=torch.int64, device=dev)
+            ctx.encode(v, BERT_SCALE, top, pt)
+            ct = ctx.seal_encrypt_symmetric(sk, pt, top, seed)
+            x.append(Ciphertext.from_device(ctx, ct, BERT_SCALE))
+            host_x.append(ct.cpu().numpy().view(np.uint64).copy())
+            del pt, ct
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        return layer.forward(x, lockstep=True)
+
+    t_setup = time.perf_counter()
+    res = step()            # the first call encodes the weights' diagonals (kept on the device)
+    torch.cuda.synchronize(dev)
+    setup_s = time.perf_counter() - t_setup
+    for _ in range(max(0, args.warmup - 1)):
+        res = step()
+    torch.cuda.synchronize(dev)
+
+    # decrypted output against the FP64 layer (NEXUS's approximations, and exact)
+    errs, errs_exact, means = [], [], []
+    for lane in range(layer.n_lanes):
+        cts = res[lane * layer.n_hid:(lane + 1) * layer.n_hid]
+        dec = np.stack([ctx.decode(ctx.decrypt(sk, c.to_device()), c.scale).real for c in cts])
+        ys = NB.unpack_lane(shape, n // 2, lane, dec)
+        ref = NB.layer_reference(shape, w, tokens[lane])
+        ref_exact = NB.layer_reference(shape, w, tokens[lane], exact=True)
+        for y, r, re in zip(ys, ref, ref_exact):
+            errs.append(float(np.max(np.abs(y - r))))
+            means.append(float(np.mean(np.abs(y - r))))
+            errs_exact.append(float(np.max(np.abs(y - re))))
+    del res
+    barrier(world)
+    l0 = ng.kernel_launches()
+    print(f"engine_launches_before_timed={l0}", file=sys.stderr, flush=True)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize(dev)
+        t0.record(stream)
+        for _ in range(args.steps):
+            res = step()
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = ng.kernel_launches() - l0
+    barrier(world)
+    total_ms = max_over_ranks(t0.elapsed_time(t1), world)
+    del res
+
+    ctx.ntt_timing_begin()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    res = step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ntt_ms, ntt_calls, ntt_limbs = ctx.ntt_timing_end()
+    instr_ms = e0.elapsed_time(e1)
+    lock_words = [r.to_numpy() for r in res[:layer.n_hid]]
+    del res
+
+    # end to end: the encrypted inputs from pinned host memory, the layer, the
+    # outputs back to the host
+    h_in = [torch.from_numpy(h.view(np.int64)).pin_memory() for h in host_x]
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    w0 = time.perf_counter()
+    loaded = []
+    for h in h_in:
+        c = Ciphertext(ctx)
+        ng.check(ng.lib().nexus_ciphertext_load(c.handle, h.data_ptr(), h.shape[0], h.shape[1], BERT_SCALE, 1,
+                                                None), "load")
+        loaded.append(c)
+    out_bytes = sum(r.to_numpy().nbytes for r in layer.forward(loaded, lockstep=True))
+    torch.cuda.synchronize(dev)
+    e2e_s = max_over_ranks(time.perf_counter() - w0, world)
+    in_bytes = sum(h.nbytes for h in host_x)
+
+    # the plain form: each lane on its own, one ciphertext per operation
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    res = layer.forward(x, lockstep=False)
+    p1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_ms = p0.elapsed_time(p1)
+    same = all(np.array_equal(a.to_numpy(), b) for a, b in zip(res[:layer.n_hid], lock_words))
+    del res
+
+    step_ms = total_ms / args.steps
+    peak, peak_kind = _peak_hbm()
+    ntt_avg_ms = ntt_ms / max(1, ntt_calls)
+    alg_bytes_per_call = 16.0 * n * ntt_limbs / max(1, ntt_calls)
+    achieved = alg_bytes_per_call / (ntt_avg_ms / 1e3) / 1e9
+    return {
+        "metric": "bert_base_layer_latency_n65536",
+        "value": step_ms / 1e3,
+        "unit": "s per layer (224 tokens: requests of 128, 32, 64)",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_ms,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic: weights ~ N(0,0.02), tokens ~ N(0,1), seeded; keys and encryptions from a SEAL seed",
+        "config": bert_config(),
+        "throughput": {"value": world * 224 / (step_ms / 1e3), "unit": "tokens/s"},
+        "accuracy": {"max_abs_err_vs_fp64_same_approx": max(errs), "mean_abs_err_vs_fp64_same_approx":
+                     float(np.mean(means)), "max_abs_err_vs_fp64_exact": max(errs_exact),
+                     "bits_vs_same_approx": -float(np.log2(max(errs)))},
+        "roofline": {
+            "kernel": "nexus NTT launches inside the layer (k_fwd/k_inv cols+rows)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg_bytes_per_call,
+            "avg_launch_ms": ntt_avg_ms, "launches_per_step": ntt_calls, "limb_ntts_per_step": ntt_limbs,
+            "share_of_step": ntt_ms / instr_ms,
+            "traffic": _ntt_traffic(ntt_limbs / max(1, ntt_calls)),
+            "traffic_source": "ncu DRAM bytes per limb-NTT of the 51-bit NTT capture x limbs per launch",
+        },
+        "e2e": {"value": e2e_s, "unit": "s per layer", "h2d_bytes_per_step": in_bytes,
+                "d2h_bytes_per_step": out_bytes},
+        "plain_single_ct_form": {"value": plain_ms / 1e3, "unit": "s per layer",
+                                 "lockstep_speedup": plain_ms / step_ms, "words_equal_lockstep": bool(same)},
+        "setup": {"first_call_s": setup_s, "galois_keys": len(all_steps),
+                  "cached_plaintexts": layer.cached_plaintexts()},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+    }
+
+
 # ----------------------------------------------------------------------------- GELU workload
 
 GELU_LOGN = 14
@@ -985,7 +1172,7 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["nexus", "reference"], default="nexus")
-    ap.add_argument("--workload", choices=["bootstrap", "matmul", "ntt", "gelu"], default="bootstrap")
+    ap.add_argument("--workload", choices=["bootstrap", "matmul", "ntt", "gelu", "bert"], default="bootstrap")
     ap.add_argument("--cpu-depth", type=int, default=7, help="expansion-subtree depth of the MatMul CPU sample")
     ap.add_argument("--mm-rows", type=int, default=128,
                     help="rows of the encrypted input (smaller values are for profiling captures only)")
@@ -1004,7 +1191,7 @@ def main():
     MM_ROWS = args.mm_rows
     BOOT_CTS = args.boot_cts
     if args.steps is None:
-        args.steps = {"bootstrap": 3, "matmul": 5, "gelu": 5}.get(args.workload, 20)
+        args.steps = {"bootstrap": 3, "matmul": 5, "gelu": 5, "bert": 2}.get(args.workload, 20)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -1103,7 +1290,8 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
-    run = {"bootstrap": run_boot_gpu, "matmul": run_mm_gpu, "ntt": run_ntt_gpu, "gelu": run_gelu_gpu}[args.workload]
+    run = {"bootstrap": run_boot_gpu, "matmul": run_mm_gpu, "ntt": run_ntt_gpu, "gelu": run_gelu_gpu,
+           "bert": run_bert_gpu}[args.workload]
     res = run(args, rank, world)
     if rank == 0:
         print(json.dumps(res), flush=True)

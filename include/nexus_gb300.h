@@ -547,6 +547,63 @@ int nexus_argmax_batch(nexus_bootstrapper *bs, nexus_ciphertext *const *x, int c
 int nexus_bootstrapper_cached_plaintexts(const nexus_bootstrapper *bs, uint64_t *count);
 
 /* ------------------------------------------------------------------------
+ * Encrypted BERT encoder layer
+ * ------------------------------------------------------------------------ */
+/*
+ * One BERT encoder layer over the bootstrapper's evaluator, keys and chain:
+ * Q/K/V projections, multi-head attention (QK^T / sqrt(head_dim), softmax,
+ * .V), output projection, residual + LayerNorm, W1 -> GELU -> W2, residual +
+ * LayerNorm, bootstrapping (bootstrap_3) between the blocks.  The
+ * nonlinearities are NEXUS's CKKSEvaluator::exp / ::inverse (the call
+ * sequence of SoftmaxEvaluator::softmax, src/softmax.cpp:6-42),
+ * ::invert_sqrt (LNEvaluator::layer_norm, src/layer_norm.cpp:6-33) and
+ * GeLUEvaluator::gelu (src/gelu.cpp:5-111).  No counterpart in the
+ * reference: its drivers (src/main.cpp:25-27) run one operator at a time and
+ * it has no ciphertext x ciphertext product for attention.
+ *
+ * Packing: slot j*T + t of a ciphertext is feature block j, token slot t;
+ * each of n_lanes lanes packs lane_requests[l] requests, request r as
+ * requests[2r] = first token slot o and requests[2r+1] = tokens L, its
+ * tokens at slots o + i and o + L + i (i < L).  Hidden activations use
+ * ceil(hidden / (N/2/T)) ciphertexts, feature f in ciphertext f / (N/2/T),
+ * block f % (N/2/T).  weights holds wq, wk, wv, wo [hidden][hidden], w1
+ * [hidden][ffn], w2 [ffn][hidden] (row-major [in][out]) then bq, bk, bv, bo,
+ * b1, b2.  Values are divided by boot_shrink before each bootstrap (and the
+ * scale with them) so the refreshed message stays small.  The bootstrapper
+ * must have its EvalMod polynomial and LT coefficients; its evaluator needs
+ * the relinearization key, the bootstrapping keys and the Galois keys of
+ * nexus_bert_layer_rotation_steps.
+ */
+typedef struct nexus_bert_layer nexus_bert_layer;
+int nexus_bert_layer_create(nexus_bootstrapper *bs, int hidden, int heads, int head_dim, int ffn, int T,
+                            int n_lanes, const int *lane_requests, const int *requests, double boot_shrink,
+                            const double *weights, nexus_bert_layer **out);
+int nexus_bert_layer_destroy(nexus_bert_layer *layer);
+/* ciphertexts per lane of the hidden, head-layout and FFN activations, and
+ * the plaintexts (encoded diagonals, biases, masks) kept on the device */
+int nexus_bert_layer_info(const nexus_bert_layer *layer, int *n_lanes, int *n_hidden_cts, int *n_head_cts,
+                          int *n_ffn_cts, uint64_t *cached_plaintexts);
+/* the slot rotations the layer performs (steps = NULL only counts them) */
+int nexus_bert_layer_rotation_steps(const nexus_bert_layer *layer, int *steps, int *count, int capacity);
+/* out[l * n_hidden_cts + c] = the layer applied to x[l * n_hidden_cts + c]
+ * (lane-major; x at 3 or more limbs, both token copies filled); lockstep = 0
+ * runs each lane on its own, one ciphertext at a time (the plain form),
+ * lockstep = 1 runs every lane together and bootstraps and evaluates the
+ * nonlinearities over all ciphertexts of a step at once, with the same words. */
+int nexus_bert_layer_forward(nexus_bert_layer *layer, int lockstep, nexus_ciphertext *const *x,
+                             nexus_ciphertext *const *out);
+/* One stage of the layer on lane-major ciphertexts, for stage-wise checking:
+ * PROJECT linear map `which` (0 Q, 1 K, 2 V, 3 output, 4 W1, 5 W2) plus its
+ * bias; ATTENTION q, k, v (head layout, in that order) -> the attention
+ * output; LAYER_NORM and BOOTSTRAP return their inputs transformed. */
+#define NEXUS_BERT_PROJECT 0
+#define NEXUS_BERT_ATTENTION 1
+#define NEXUS_BERT_LAYER_NORM 2
+#define NEXUS_BERT_BOOTSTRAP 3
+int nexus_bert_layer_stage(nexus_bert_layer *layer, int lockstep, int stage, int which, nexus_ciphertext *const *in,
+                           int count_in, nexus_ciphertext *const *out, int count_out);
+
+/* ------------------------------------------------------------------------
  * SEAL byte format of a CKKS ciphertext (host-side, compr_mode_type::none)
  * ------------------------------------------------------------------------ */
 

@@ -1,0 +1,770 @@
+// Encrypted BERT encoder layer (see bert.h for the packing and the method).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <thread>
+#include <type_traits>
+
+#include "bert.h"
+#include "ops.h"
+
+namespace nexus {
+
+namespace {
+
+int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+int pow2_ceil(int v)
+{
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+uint64_t bits_of(double d)
+{
+    uint64_t b;
+    std::memcpy(&b, &d, 8);
+    return b;
+}
+
+// apply f to every ciphertext of `cts`: one by one for the single form, as
+// lockstep batches of at most `chunk` ciphertexts for the batched form
+template <class F>
+void each(Evaluator &, std::vector<Ciphertext *> &cts, int, F &&f)
+{
+    for (auto *c : cts) f(*c);
+}
+
+template <class F>
+void each(BatchEvaluator &ev, std::vector<CtBatch *> &cts, int chunk, F &&f)
+{
+    if (cts.empty()) return;
+    Context &c = ev.context();
+    cudaStream_t s = ev.stream();
+    size_t i = 0;
+    while (i < cts.size()) {
+        size_t j = i, elems = 0;
+        while (j < cts.size() && (elems == 0 || (int)(elems + cts[j]->batch()) <= chunk)) elems += cts[j++]->batch();
+        const CtBatch &first = *cts[i];
+        CtBatch all;
+        all.resize(c, (int)elems, first.size(), first.limbs(), s);
+        all.scale() = first.scale();
+        size_t off = 0;
+        for (size_t k = i; k < j; ++k) {
+            const CtBatch &x = *cts[k];
+            if (x.size() != first.size() || x.limbs() != first.limbs() || x.scale() != first.scale())
+                throw std::invalid_argument("lockstep group: ciphertexts differ in size, level or scale");
+            cudaMemcpyAsync(all.ct((int)off), x.data(), (size_t)x.batch() * x.words_per_ct() * 8,
+                            cudaMemcpyDeviceToDevice, s);
+            off += x.batch();
+        }
+        f(all);
+        off = 0;
+        for (size_t k = i; k < j; ++k) {
+            CtBatch &x = *cts[k];
+            const int b = x.batch();
+            x.resize(c, b, all.size(), all.limbs(), s);
+            x.scale() = all.scale();
+            cudaMemcpyAsync(x.data(), all.ct((int)off), (size_t)b * all.words_per_ct() * 8, cudaMemcpyDeviceToDevice,
+                            s);
+            off += b;
+        }
+        i = j;
+    }
+}
+
+// per-element plaintext product / sum: lane b of the batch uses pts[b]
+void mul_plain_each(Evaluator &ev, Ciphertext &ct, const std::vector<const Plaintext *> &pts)
+{
+    ev.multiply_plain_inplace(ct, *pts[0]);
+}
+
+void mul_plain_each(BatchEvaluator &ev, CtBatch &ct, const std::vector<const Plaintext *> &pts)
+{
+    Context &c = ev.context();
+    const double scale = ct.scale() * pts[0]->scale();
+    for (int b = 0; b < ct.batch(); ++b) {
+        const Plaintext &p = *pts[b];
+        if (p.limbs() != ct.limbs() || p.is_scalar() || p.scale() != pts[0]->scale())
+            throw std::invalid_argument("per-lane plaintexts differ in level or scale");
+        poly_mul_plain(c, ct.ct(b), ct.size(), ct.limbs(), p.data(), ct.ct(b), ev.stream());
+    }
+    ev.base().check_scale(scale, ct.limbs());
+    ct.scale() = scale;
+}
+
+void add_plain_each(Evaluator &ev, Ciphertext &ct, const std::vector<const Plaintext *> &pts)
+{
+    ev.add_plain_inplace(ct, *pts[0]);
+}
+
+void add_plain_each(BatchEvaluator &ev, CtBatch &ct, const std::vector<const Plaintext *> &pts)
+{
+    Context &c = ev.context();
+    for (int b = 0; b < ct.batch(); ++b) {
+        const Plaintext &p = *pts[b];
+        if (p.limbs() != ct.limbs() || p.is_scalar() || !are_close(ct.scale(), p.scale()))
+            throw std::invalid_argument("per-lane plaintexts differ in level or scale");
+        poly_add_plain(c, ct.ct(b), 1, ct.limbs(), p.data(), 0, ct.ct(b), ev.stream());
+    }
+}
+
+int batch_of(const Ciphertext &) { return 1; }
+int batch_of(const CtBatch &c) { return c.batch(); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ shape
+
+void BertShape::derive(size_t slots)
+{
+    S = (int)slots;
+    if (T < 2 || (T & (T - 1)) || T > S) throw std::invalid_argument("T must be a power of two <= the slot count");
+    NB = S / T;
+    if (hidden < 1 || heads < 1 || head_dim < 1 || ffn < 1 || hidden != heads * head_dim)
+        throw std::invalid_argument("hidden must equal heads * head_dim");
+    H2 = pow2_ceil(heads);
+    if (H2 > NB) throw std::invalid_argument("more heads than blocks per ciphertext");
+    KB = NB / H2;
+    n_head = ceil_div(head_dim, KB);
+    n_hid = ceil_div(hidden, NB);
+    n_ffn = ceil_div(ffn, NB);
+    if (lanes.empty()) throw std::invalid_argument("no lanes");
+    Lmax = 0;
+    for (auto &lane : lanes) {
+        if (lane.empty()) throw std::invalid_argument("empty lane");
+        std::vector<std::pair<int, int>> r = lane;
+        std::sort(r.begin(), r.end());
+        int end = 0;
+        for (auto &q : r) {
+            if (q.second < 1 || q.first < end || q.first + 2 * q.second > T)
+                throw std::invalid_argument("requests of a lane overlap or leave the token block");
+            end = q.first + 2 * q.second;
+            Lmax = std::max(Lmax, q.second);
+        }
+    }
+    G = (int)std::ceil(std::sqrt((double)Lmax));
+    Glt = (int)std::ceil(std::sqrt((double)NB));
+    if (!(boot_shrink >= 1.0)) throw std::invalid_argument("boot_shrink must be >= 1");
+}
+
+std::vector<int> BertShape::rotation_steps() const
+{
+    std::vector<int> v;
+    auto push = [&](int s) {
+        s = ((s % S) + S) % S;
+        if (s && std::find(v.begin(), v.end(), s) == v.end()) v.push_back(s);
+    };
+    for (int b = 1; b < Glt; ++b) push(b * T);
+    for (int g = 1; g * Glt < NB; ++g) push(g * Glt * T);
+    for (int b = 1; b < G; ++b) push(b);
+    for (int g = 1; g * G < Lmax; ++g) {
+        push(g * G);
+        push(-g * G);
+    }
+    for (int m = 1; m < KB; m <<= 1) push(H2 * T * m);
+    for (int m = 1; m < NB; m <<= 1) push(T * m);
+    return v;
+}
+
+// ------------------------------------------------------------------ layer
+
+template <class EV, class CT>
+BertLayerT<EV, CT>::BertLayerT(EV &ev, BootstrapperT<EV, CT> &bs, const BertShape &shape, const BertWeights &w,
+                               std::vector<int> lanes, std::shared_ptr<BertPlaintexts> plain)
+    : ev_(&ev), bs_(&bs), ck_(ev, bs.final_scale), sh_(shape), w_(w), lanes_(std::move(lanes)),
+      delta_(bs.final_scale), pt_(plain ? std::move(plain) : std::make_shared<BertPlaintexts>())
+{
+    sh_.derive(ev.slot_count());
+    const size_t d = sh_.hidden, f = sh_.ffn;
+    auto need = [](const std::vector<double> &v, size_t n, const char *what) {
+        if (v.size() != n) throw std::invalid_argument(std::string("weight ") + what + " has the wrong size");
+    };
+    need(w_.wq, d * d, "wq");
+    need(w_.wk, d * d, "wk");
+    need(w_.wv, d * d, "wv");
+    need(w_.wo, d * d, "wo");
+    need(w_.w1, d * f, "w1");
+    need(w_.w2, f * d, "w2");
+    need(w_.bq, d, "bq");
+    need(w_.bk, d, "bk");
+    need(w_.bv, d, "bv");
+    need(w_.bo, d, "bo");
+    need(w_.b1, f, "b1");
+    need(w_.b2, d, "b2");
+    for (int l : lanes_)
+        if (l < 0 || l >= (int)sh_.lanes.size()) throw std::invalid_argument("lane index out of range");
+}
+
+template <class EV, class CT>
+int BertLayerT<EV, CT>::in_features(int which) const
+{
+    return which == LT_2 ? sh_.ffn : sh_.hidden;
+}
+
+template <class EV, class CT>
+int BertLayerT<EV, CT>::out_features(int which) const
+{
+    return which == LT_1 ? sh_.ffn : sh_.hidden;
+}
+
+template <class EV, class CT>
+int BertLayerT<EV, CT>::in_count(int which) const
+{
+    if (which == LT_O) return sh_.n_head;
+    return which == LT_2 ? sh_.n_ffn : sh_.n_hid;
+}
+
+template <class EV, class CT>
+int BertLayerT<EV, CT>::out_count(int which) const
+{
+    if (which <= LT_V) return sh_.n_head;
+    return which == LT_1 ? sh_.n_ffn : sh_.n_hid;
+}
+
+template <class EV, class CT>
+const std::vector<double> &BertLayerT<EV, CT>::weights(int which) const
+{
+    switch (which) {
+    case LT_Q: return w_.wq;
+    case LT_K: return w_.wk;
+    case LT_V: return w_.wv;
+    case LT_O: return w_.wo;
+    case LT_1: return w_.w1;
+    default: return w_.w2;
+    }
+}
+
+template <class EV, class CT>
+const std::vector<double> &BertLayerT<EV, CT>::bias(int which) const
+{
+    switch (which) {
+    case LT_Q: return w_.bq;
+    case LT_K: return w_.bk;
+    case LT_V: return w_.bv;
+    case LT_O: return w_.bo;
+    case LT_1: return w_.b1;
+    default: return w_.b2;
+    }
+}
+
+// head layout: feature h*dh + k -> ct k / KB, block (k % KB) * H2 + h
+template <class EV, class CT>
+int BertLayerT<EV, CT>::in_feature(int which, int ct, int block) const
+{
+    if (which == LT_O) {
+        const int h = block % sh_.H2, k = ct * sh_.KB + block / sh_.H2;
+        if (h >= sh_.heads || k >= sh_.head_dim) return -1;
+        return h * sh_.head_dim + k;
+    }
+    const int f = ct * sh_.NB + block;
+    return f < in_features(which) ? f : -1;
+}
+
+template <class EV, class CT>
+int BertLayerT<EV, CT>::out_feature(int which, int ct, int block) const
+{
+    if (which <= LT_V) {
+        const int h = block % sh_.H2, k = ct * sh_.KB + block / sh_.H2;
+        if (h >= sh_.heads || k >= sh_.head_dim) return -1;
+        return h * sh_.head_dim + k;
+    }
+    const int f = ct * sh_.NB + block;
+    return f < out_features(which) ? f : -1;
+}
+
+template <class EV, class CT>
+bool BertLayerT<EV, CT>::diag_nonzero(int which, int a, int b, int d) const
+{
+    for (int j = 0; j < sh_.NB; ++j)
+        if (out_feature(which, b, j) >= 0 && in_feature(which, a, (j + d) % sh_.NB) >= 0) return true;
+    return false;
+}
+
+// diagonal d of the (a -> b) block of map `which`, scaled by 1/boot_shrink,
+// rotated right by pre_rotate_blocks blocks: slot s holds the entry of block
+// (s / T - pre_rotate_blocks) mod NB
+template <class EV, class CT>
+std::vector<double> BertLayerT<EV, CT>::diag_vector(int which, int a, int b, int d, int pre_rotate_blocks) const
+{
+    const auto &W = weights(which);
+    const int nout = out_features(which), NB = sh_.NB, T = sh_.T;
+    std::vector<double> v((size_t)sh_.S, 0.0);
+    for (int j = 0; j < NB; ++j) {
+        const int fo = out_feature(which, b, j), fi = in_feature(which, a, (j + d) % NB);
+        if (fo < 0 || fi < 0) continue;
+        const double x = W[(size_t)fi * nout + fo] / sh_.boot_shrink;
+        const int dst = (j + pre_rotate_blocks) % NB;
+        std::fill(v.begin() + (size_t)dst * T, v.begin() + (size_t)(dst + 1) * T, x);
+    }
+    return v;
+}
+
+// encode every nonzero diagonal of map `which` at (limbs, scale) that is not
+// cached yet: host FFTs on all cores, one NTT launch per plaintext
+template <class EV, class CT>
+void BertLayerT<EV, CT>::encode_diagonals(int which, int limbs, double scale)
+{
+    std::vector<BertPlaintexts::DKey> keys;
+    const uint64_t sb = bits_of(scale);
+    for (int a = 0; a < in_count(which); ++a)
+        for (int b = 0; b < out_count(which); ++b)
+            for (int d = 0; d < sh_.NB; ++d) {
+                const BertPlaintexts::DKey key{which, a, b, d, limbs, sb};
+                if (!pt_->diag.count(key) && diag_nonzero(which, a, b, d)) keys.push_back(key);
+            }
+    Evaluator &base = [&]() -> Evaluator & {
+        if constexpr (std::is_same<EV, Evaluator>::value) return *ev_;
+        else return ev_->base();
+    }();
+    // host FFTs on every core, in chunks that bound the host staging memory;
+    // a chunk enters the cache only once all of it is encoded
+    const size_t chunk = 256;
+    for (size_t lo = 0; lo < keys.size(); lo += chunk) {
+        const size_t hi = std::min(keys.size(), lo + chunk);
+        std::vector<std::vector<std::complex<double>>> vecs(hi - lo);
+        std::vector<Plaintext> plains(hi - lo);
+        std::vector<const std::vector<std::complex<double>> *> vp;
+        std::vector<Plaintext *> outs;
+        for (size_t i = lo; i < hi; ++i) {
+            const int a = std::get<1>(keys[i]), b = std::get<2>(keys[i]), d = std::get<3>(keys[i]);
+            const std::vector<double> v = diag_vector(which, a, b, d, (d / sh_.Glt) * sh_.Glt);
+            vecs[i - lo].assign(v.begin(), v.end());
+            vp.push_back(&vecs[i - lo]);
+            outs.push_back(&plains[i - lo]);
+        }
+        base.encode_many(vp, limbs, scale, outs);
+        for (size_t i = lo; i < hi; ++i) pt_->diag.emplace(keys[i], std::move(plains[i - lo]));
+    }
+}
+
+template <class EV, class CT>
+const Plaintext &BertLayerT<EV, CT>::diag(int which, int a, int b, int d, int limbs, double scale)
+{
+    const BertPlaintexts::DKey key{which, a, b, d, limbs, bits_of(scale)};
+    auto it = pt_->diag.find(key);
+    if (it == pt_->diag.end()) {
+        encode_diagonals(which, limbs, scale);
+        it = pt_->diag.find(key);
+        if (it == pt_->diag.end()) throw std::logic_error("diagonal missing after encoding");
+    }
+    return it->second;
+}
+
+// bias of map `which` for output ciphertext ct: b[f] on every token slot of f's block
+template <class EV, class CT>
+const Plaintext &BertLayerT<EV, CT>::bias_plain(int which, int ct, int limbs, double scale)
+{
+    const auto key = std::make_tuple(which, ct, limbs, bits_of(scale));
+    auto it = pt_->bias.find(key);
+    if (it != pt_->bias.end()) return it->second;
+    const auto &bv = bias(which);
+    std::vector<std::complex<double>> v((size_t)sh_.S, 0.0);
+    for (int j = 0; j < sh_.NB; ++j) {
+        const int f = out_feature(which, ct, j);
+        if (f < 0) continue;
+        for (int t = 0; t < sh_.T; ++t) v[(size_t)j * sh_.T + t] = bv[f];
+    }
+    Plaintext p;
+    ev_->encode(v, limbs, scale, p);
+    return pt_->bias.emplace(key, std::move(p)).first->second;
+}
+
+// softmax masks for offset delta, per lane element: kind 0 multiplies by
+// 1/sqrt(d_h) on the valid slots (a head that exists, a first-copy token of a
+// request longer than delta) and by 0 elsewhere (encoded at the scale of the
+// prime the rescale drops, so the rescale restores the scale); kind 1 adds
+// -128 on the other slots (encoded at `scale`)
+template <class EV, class CT>
+void BertLayerT<EV, CT>::masks(int delta, int kind, int limbs, double scale, std::vector<const Plaintext *> &out)
+{
+    out.clear();
+    const double sc = kind == 0 ? (double)ev_->modulus(limbs - 1) : scale;
+    for (int lane : lanes_) {
+        // a mask depends on delta only through the requests longer than it
+        int sig = 0;
+        const auto &reqs = sh_.lanes[lane];
+        for (size_t r = 0; r < reqs.size(); ++r)
+            if (delta < reqs[r].second) sig |= 1 << r;
+        const auto key = std::make_tuple(lane, sig, limbs, bits_of(sc), kind);
+        auto it = pt_->mask.find(key);
+        if (it == pt_->mask.end()) {
+            std::vector<std::complex<double>> v((size_t)sh_.S, 0.0);
+            const double inv_sqrt = 1.0 / std::sqrt((double)sh_.head_dim);
+            for (int j = 0; j < sh_.NB; ++j) {
+                const bool head_ok = (j % sh_.H2) < sh_.heads;
+                for (int t = 0; t < sh_.T; ++t) {
+                    bool ok = false;
+                    if (head_ok)
+                        for (size_t r = 0; r < reqs.size(); ++r)
+                            if ((sig >> r & 1) && t >= reqs[r].first && t < reqs[r].first + reqs[r].second) ok = true;
+                    v[(size_t)j * sh_.T + t] = kind == 0 ? (ok ? inv_sqrt : 0.0) : (ok ? 0.0 : -128.0);
+                }
+            }
+            Plaintext p;
+            ev_->encode(v, limbs, sc, p);
+            it = pt_->mask.emplace(key, std::move(p)).first;
+        }
+        out.push_back(&it->second);
+    }
+}
+
+// ct *= value with the constant encoded so that, after the rescale, the
+// scale is target_scale (set exactly)
+template <class EV, class CT>
+void BertLayerT<EV, CT>::exact_scale_const(CT &ct, double value, double target_scale)
+{
+    const int l = ct.limbs();
+    const double q = (double)ev_->modulus(l - 1);
+    Plaintext p;
+    ev_->encode(value, l, q * target_scale / ct.scale(), p);
+    ev_->multiply_plain_inplace(ct, p);
+    ev_->rescale_to_next_inplace(ct);
+    ct.scale() = target_scale;
+}
+
+// y = map(x) + bias, x at >= 2 limbs: y at x.limbs - 1 at scale delta / boot_shrink
+template <class EV, class CT>
+void BertLayerT<EV, CT>::project(const std::vector<CT> &x, int which, std::vector<CT> &y)
+{
+    EV &ev = *ev_;
+    const int n_in = in_count(which), n_out = out_count(which);
+    if ((int)x.size() != n_in) throw std::invalid_argument("project: wrong number of input ciphertexts");
+    const int l = x[0].limbs();
+    if (l < 2) throw std::invalid_argument("project: the input needs a level to spend");
+    const double in_scale = x[0].scale();
+    for (auto &c : x)
+        if (c.limbs() != l || c.scale() != in_scale) throw std::invalid_argument("project: inputs differ");
+    // diagonals at a scale that brings the product back to delta after the rescale
+    const double dscale = (double)ev.modulus(l - 1) * delta_ / in_scale;
+    encode_diagonals(which, l, dscale);
+    const int Glt = sh_.Glt, T = sh_.T, NB = sh_.NB;
+    std::vector<std::vector<CT>> baby(n_in);
+    std::vector<int> steps;
+    for (int b = 1; b < Glt; ++b) steps.push_back(b * T);
+    for (int a = 0; a < n_in; ++a) {
+        std::vector<CT> rot;
+        ev.rotate_vector_many(x[a], steps, rot);
+        baby[a].resize(Glt);
+        baby[a][0] = x[a];
+        for (int b = 1; b < Glt; ++b) baby[a][b] = std::move(rot[b - 1]);
+    }
+    y.assign(n_out, CT());
+    std::vector<const CT *> terms;
+    std::vector<const Plaintext *> pts;
+    for (int b = 0; b < n_out; ++b) {
+        CT acc, giant, t;
+        bool have = false;
+        for (int g = 0; g * Glt < NB; ++g) {
+            terms.clear();
+            pts.clear();
+            for (int a = 0; a < n_in; ++a)
+                for (int bb = 0; bb < Glt && g * Glt + bb < NB; ++bb) {
+                    const int d = g * Glt + bb;
+                    if (!diag_nonzero(which, a, b, d)) continue;
+                    terms.push_back(&baby[a][bb]);
+                    pts.push_back(&diag(which, a, b, d, l, dscale));
+                }
+            if (terms.empty()) continue;
+            ev.multiply_plain_accumulate(terms, pts, giant);
+            if (g) {
+                ev.rotate_vector(giant, g * Glt * T, t);
+            } else {
+                t = std::move(giant);
+            }
+            if (!have) {
+                acc = std::move(t);
+                have = true;
+            } else {
+                ev.add_inplace(acc, t);
+            }
+        }
+        if (!have) throw std::logic_error("project: an output ciphertext has no diagonal");
+        ev.rescale_to_next_inplace(acc);
+        acc.scale() = delta_ / sh_.boot_shrink;
+        ev.add_plain_inplace(acc, bias_plain(which, b, acc.limbs(), acc.scale()));
+        y[b] = std::move(acc);
+    }
+}
+
+template <class EV, class CT>
+void BertLayerT<EV, CT>::bootstrap_all(std::vector<CT> &cts)
+{
+    std::vector<CT *> p;
+    for (auto &c : cts) {
+        ev_->mod_switch_to_inplace(c, 1);
+        p.push_back(&c);
+    }
+    each(*ev_, p, 16, [&](CT &c) {
+        CT r;
+        bs_->bootstrap_3(r, c);
+        c = std::move(r);
+    });
+}
+
+template <class EV, class CT>
+void BertLayerT<EV, CT>::attention(std::vector<CT> &q, std::vector<CT> &k, std::vector<CT> &v, std::vector<CT> &o)
+{
+    EV &ev = *ev_;
+    const int nh = sh_.n_head, G = sh_.G, L = sh_.Lmax, S = sh_.S;
+    // levels, counted back from the output projection (2 limbs): PV 1,
+    // P = E * I 1, exp 8 (constant + 7 squarings), mask 1, Q.K 1
+    const int e_limbs = 4, qk_limbs = e_limbs + 10, v_limbs = e_limbs - 1;
+    for (auto &c : q) ev.mod_switch_to_inplace(c, qk_limbs);
+    for (auto &c : k) ev.mod_switch_to_inplace(c, qk_limbs);
+    for (auto &c : v) ev.mod_switch_to_inplace(c, v_limbs);
+    const int n_g = ceil_div(L, G);
+    // hoisted rotations would keep a permuted copy of every key used here
+    // (one key's size each); the attention's rotations are switched one by
+    // one instead, which leaves that memory to the encoded weights
+    Evaluator &base = [&]() -> Evaluator & {
+        if constexpr (std::is_same<EV, Evaluator>::value) return ev;
+        else return ev.base();
+    }();
+    struct Restore {
+        Evaluator &e;
+        bool on;
+        ~Restore() { e.hoisting = on; }
+    } restore{base, base.hoisting};
+    base.hoisting = false;
+
+    // baby steps of K and V, giant pre-rotations of Q
+    std::vector<int> baby_steps;
+    for (int b = 1; b < G; ++b) baby_steps.push_back(b);
+    std::vector<std::vector<CT>> kb(nh), vb(nh), qg(nh);
+    for (int c = 0; c < nh; ++c) {
+        std::vector<CT> r;
+        ev.rotate_vector_many(k[c], baby_steps, r);
+        kb[c].resize(G);
+        kb[c][0] = k[c];
+        for (int b = 1; b < G; ++b) kb[c][b] = std::move(r[b - 1]);
+        ev.rotate_vector_many(v[c], baby_steps, r);
+        vb[c].resize(G);
+        vb[c][0] = v[c];
+        for (int b = 1; b < G; ++b) vb[c][b] = std::move(r[b - 1]);
+        std::vector<int> gsteps;
+        for (int g = 1; g < n_g; ++g) gsteps.push_back(S - g * G);
+        ev.rotate_vector_many(q[c], gsteps, r);
+        qg[c].resize(n_g);
+        qg[c][0] = q[c];
+        for (int g = 1; g < n_g; ++g) qg[c][g] = std::move(r[g - 1]);
+    }
+
+    // scores S_delta, masked and passed through exp
+    std::vector<CT> e(L);
+    std::vector<const Plaintext *> mp;
+    for (int d = 0; d < L; ++d) {
+        const int g = d / G, b = d % G;
+        CT acc, t;
+        for (int c = 0; c < nh; ++c) {
+            ev.multiply(qg[c][g], kb[c][b], t);
+            if (c == 0) acc = std::move(t);
+            else ev.add_inplace(acc, t);
+        }
+        ev.relinearize_inplace(acc);
+        ev.rescale_to_next_inplace(acc);
+        for (int m = 1; m < sh_.KB; m <<= 1) {
+            ev.rotate_vector(acc, sh_.H2 * sh_.T * m, t);
+            ev.add_inplace(acc, t);
+        }
+        if (g) {
+            ev.rotate_vector(acc, g * G, t);
+            acc = std::move(t);
+        }
+        masks(d, 0, acc.limbs(), acc.scale(), mp);
+        mul_plain_each(ev, acc, mp);
+        ev.rescale_to_next_inplace(acc);
+        masks(d, 1, acc.limbs(), acc.scale(), mp);
+        add_plain_each(ev, acc, mp);
+        e[d] = std::move(acc);
+    }
+    {
+        std::vector<CT *> p;
+        for (auto &x : e) p.push_back(&x);
+        each(ev, p, 64, [&](CT &x) { x = ck_.exp(x); });
+    }
+
+    // row sums over delta, the inverse after a bootstrap (softmax.cpp:24-35)
+    CT sum = e[0];
+    for (int d = 1; d < L; ++d) ev.add_inplace(sum, e[d]);
+    {
+        Plaintext delta;
+        ev.encode(0.01 / sh_.boot_shrink, sum.limbs(), sum.scale(), delta);
+        ev.multiply_plain_inplace(sum, delta);
+        ev.rescale_to_next_inplace(sum);
+        sum.scale() /= sh_.boot_shrink;
+    }
+    std::vector<CT> one{std::move(sum)};
+    bootstrap_all(one);
+    CT inv = ck_.inverse(one[0]);
+    {
+        Plaintext delta;
+        ev.encode(0.01, inv.limbs(), inv.scale(), delta);
+        ev.multiply_plain_inplace(inv, delta);
+        ev.rescale_to_next_inplace(inv);
+    }
+    ev.mod_switch_to_inplace(inv, e[0].limbs());
+    // P_delta = exp(S_delta) * inverse(sum) (softmax.cpp:37-40)
+    for (int d = 0; d < L; ++d) {
+        ev.multiply_inplace(e[d], inv);
+        ev.relinearize_inplace(e[d]);
+        ev.rescale_to_next_inplace(e[d]);
+    }
+
+    // O_c = sum_g rot(sum_b rot(P_{G g + b}, -G g) * rot(V_c, b), G g)
+    o.assign(nh, CT());
+    std::vector<std::vector<CT>> pg(n_g);
+    for (int g = 0; g < n_g; ++g) {
+        pg[g].resize(G);
+        for (int b = 0; b < G && g * G + b < L; ++b) {
+            if (g) ev.rotate_vector(e[g * G + b], S - g * G, pg[g][b]);
+            else pg[g][b] = e[b];
+        }
+    }
+    for (int c = 0; c < nh; ++c) {
+        CT acc, t, u;
+        bool have = false;
+        for (int g = 0; g < n_g; ++g) {
+            CT part;
+            bool hp = false;
+            for (int b = 0; b < G && g * G + b < L; ++b) {
+                ev.multiply(pg[g][b], vb[c][b], t);
+                if (!hp) {
+                    part = std::move(t);
+                    hp = true;
+                } else {
+                    ev.add_inplace(part, t);
+                }
+            }
+            ev.relinearize_inplace(part);
+            ev.rescale_to_next_inplace(part);
+            if (g) {
+                ev.rotate_vector(part, g * G, u);
+                part = std::move(u);
+            }
+            if (!have) {
+                acc = std::move(part);
+                have = true;
+            } else {
+                ev.add_inplace(acc, part);
+            }
+        }
+        o[c] = std::move(acc);
+    }
+}
+
+// LayerNorm of NEXUS (layer_norm.cpp:6-33): the sum of squares over the
+// features is a sum over ciphertexts and a fold over the NB blocks
+template <class EV, class CT>
+void BertLayerT<EV, CT>::layer_norm(std::vector<CT> &x)
+{
+    EV &ev = *ev_;
+    CT sum, t;
+    for (size_t c = 0; c < x.size(); ++c) {
+        ev.square(x[c], t);
+        ev.relinearize_inplace(t);
+        ev.rescale_to_next_inplace(t);
+        if (c == 0) sum = std::move(t);
+        else ev.add_inplace(sum, t);
+    }
+    for (int m = 1; m < sh_.NB; m <<= 1) {
+        ev.rotate_vector(sum, sh_.T * m, t);
+        ev.add_inplace(sum, t);
+    }
+    Plaintext delta;
+    ev.encode(1.0 / sh_.hidden, sum.limbs(), sum.scale(), delta);
+    ev.multiply_plain_inplace(sum, delta);
+    ev.rescale_to_next_inplace(sum);
+    CT r = ck_.invert_sqrt(sum, 4, 2);
+    for (auto &c : x) {
+        ev.mod_switch_to_inplace(c, r.limbs());
+        ev.multiply_inplace(c, r);
+        ev.relinearize_inplace(c);
+        ev.rescale_to_next_inplace(c);
+    }
+}
+
+template <class EV, class CT>
+void BertLayerT<EV, CT>::shrink_for_bootstrap(std::vector<CT> &cts)
+{
+    for (auto &c : cts) {
+        exact_scale_const(c, 1.0 / sh_.boot_shrink, delta_);
+        c.scale() = delta_ / sh_.boot_shrink;
+    }
+}
+
+template <class EV, class CT>
+void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &out)
+{
+    EV &ev = *ev_;
+    if ((int)x_in.size() != sh_.n_hid) throw std::invalid_argument("forward: wrong number of input ciphertexts");
+    for (auto &c : x_in)
+        if (batch_of(c) != (int)lanes_.size()) throw std::invalid_argument("forward: batch does not match the lanes");
+    if (x_in[0].limbs() < 3) throw std::invalid_argument("forward: the input needs at least 3 limbs");
+    // the residual branch: x / boot_shrink at one limb
+    std::vector<CT> x_res = x_in;
+    shrink_for_bootstrap(x_res);
+    for (auto &c : x_res) ev.mod_switch_to_inplace(c, 1);
+    // Q, K, V at one limb, refreshed
+    std::vector<CT> x2 = x_in;
+    for (auto &c : x2) ev.mod_switch_to_inplace(c, 2);
+    std::vector<CT> q, k, v;
+    project(x2, LT_Q, q);
+    project(x2, LT_K, k);
+    project(x2, LT_V, v);
+    {
+        std::vector<CT> all;
+        for (auto *t : {&q, &k, &v})
+            for (auto &c : *t) all.push_back(std::move(c));
+        bootstrap_all(all);
+        const int nh = sh_.n_head;
+        for (int i = 0; i < nh; ++i) {
+            q[i] = std::move(all[i]);
+            k[i] = std::move(all[nh + i]);
+            v[i] = std::move(all[2 * nh + i]);
+        }
+    }
+    std::vector<CT> o, a;
+    attention(q, k, v, o);
+    project(o, LT_O, a);
+    // residual + LayerNorm
+    for (int c = 0; c < sh_.n_hid; ++c) {
+        a[c].scale() = x_res[c].scale();
+        ev.add_inplace(a[c], x_res[c]);
+    }
+    bootstrap_all(a);
+    layer_norm(a);
+    // FFN
+    std::vector<CT> y_res = a;
+    shrink_for_bootstrap(y_res);
+    for (auto &c : y_res) ev.mod_switch_to_inplace(c, 1);
+    for (auto &c : a) ev.mod_switch_to_inplace(c, 2);
+    std::vector<CT> h, f;
+    project(a, LT_1, h);
+    bootstrap_all(h);
+    {
+        GeLUEvaluatorT<EV, CT> gelu(ck_);
+        std::vector<CT *> p;
+        for (auto &c : h) p.push_back(&c);
+        each(ev, p, 64, [&](CT &c) {
+            CT r;
+            gelu.gelu(c, r);
+            c = std::move(r);
+        });
+    }
+    project(h, LT_2, f);
+    for (int c = 0; c < sh_.n_hid; ++c) {
+        f[c].scale() = y_res[c].scale();
+        ev.add_inplace(f[c], y_res[c]);
+    }
+    bootstrap_all(f);
+    layer_norm(f);
+    out = std::move(f);
+}
+
+template class BertLayerT<Evaluator, Ciphertext>;
+template class BertLayerT<BatchEvaluator, CtBatch>;
+
+}  // namespace nexus

@@ -1,0 +1,146 @@
+// An encrypted BERT encoder layer composed from NEXUS's operators.
+//
+// The NEXUS tree has no layer driver (its src/main.cpp runs one operator at a
+// time) and no ciphertext x ciphertext product for attention; this file
+// defines both.  One layer: Q/K/V projections, attention (QK^T / sqrt(d_h),
+// softmax, .V), output projection, residual + LayerNorm, FFN (W1, GELU, W2),
+// residual + LayerNorm, with bootstraps (Bootstrapper::bootstrap_3) between
+// the blocks.  The nonlinearities are NEXUS's: CKKSEvaluator::exp and
+// ::inverse inside the softmax (src/softmax.cpp:6-42 call sequence, with the
+// row sum taken over diagonals, below), CKKSEvaluator::invert_sqrt inside the
+// LayerNorm (src/layer_norm.cpp:6-33, the feature sum taken over blocks), and
+// GeLUEvaluator::gelu (src/gelu.cpp:5-111).
+//
+// Packing.  A ciphertext's S = N/2 slots form NB = S/T blocks of T token
+// slots; block j of a ciphertext holds one feature for every token slot.  A
+// lane is a set of requests sharing the token slots: request r occupies
+// [o_r, o_r + 2 L_r), its tokens at o_r + i and again at o_r + L_r + i (the
+// copy lets a rotation by delta < L_r read token (i + delta) mod L_r).
+//  * std layout (hidden and FFN activations): feature f in ciphertext f / NB,
+//    block f % NB;
+//  * head layout (Q, K, V and the attention output): feature h*d_h + k in
+//    ciphertext k / KB, block (k % KB) * H2 + h, with H2 the heads rounded up
+//    to a power of two and KB = NB / H2, so the sum over k of a head is a sum
+//    of ciphertexts plus log2(KB) rotations.
+// Every ciphertext op but the attention rotations acts on each token slot on
+// its own, so requests never mix.
+//
+// Linear layers are block-diagonal linear transforms: y_b = sum_a sum_d
+// diag(a,b,d) * rot(x_a, d T), baby-step giant-step over the block offset d
+// (the baby steps of one input share one ModUp); diag(a,b,d) holds
+// W[f_in(a, j + d)][f_out(b, j)] on every token slot of block j.
+//
+// Attention, per lane, in the diagonal domain: S_delta[i] = Q[i] . K[i + delta]
+// (delta < L_max), computed baby-step giant-step over delta
+// (S_{G g + b} = rot(fold(sum_c rot(Q_c, -G g) * rot(K_c, b)), G g)), the
+// softmax row sum over j becomes the sum over delta, and
+// O_c = sum_g rot(sum_b rot(P_{G g + b}, -G g) * rot(V_c, b), G g).
+// Pairs with delta >= L_r are masked to -128 before NEXUS's exp, which
+// (1 + x/128)^128 maps to 0.
+//
+// Every value about to be bootstrapped is first scaled down by boot_shrink
+// (folded into the preceding linear map or constant product) and its scale
+// divided by the same factor, so the refreshed ciphertext holds the value
+// itself while the bootstrap's sine approximation sees a small message.
+#pragma once
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <tuple>
+#include <utility>
+#include <vector>
+
+#include "batch.h"
+#include "bootstrap.h"
+#include "ckks.h"
+#include "nexus_ops.h"
+
+namespace nexus {
+
+struct BertShape {
+    int hidden = 768, heads = 12, head_dim = 64, ffn = 3072;
+    int T = 256;  // token slots per feature block
+    // per lane, each request as (first token slot, tokens)
+    std::vector<std::vector<std::pair<int, int>>> lanes;
+    double boot_shrink = 8.0;
+
+    // derived by derive()
+    int S = 0, NB = 0, H2 = 0, KB = 0, n_head = 0, n_hid = 0, n_ffn = 0, Lmax = 0, G = 0, Glt = 0;
+    void derive(size_t slots);
+    // every rotation step the layer uses (the bootstrapper's are separate)
+    std::vector<int> rotation_steps() const;
+};
+
+// row-major [in][out] matrices and biases
+struct BertWeights {
+    std::vector<double> wq, wk, wv, wo, w1, w2;
+    std::vector<double> bq, bk, bv, bo, b1, b2;
+};
+
+// encoded diagonals, biases and softmax masks, shared by the single-lane and
+// lockstep forms of one layer (the words depend only on level and scale)
+struct BertPlaintexts {
+    using DKey = std::tuple<int, int, int, int, int, uint64_t>;
+    std::map<DKey, Plaintext> diag;
+    std::map<std::tuple<int, int, int, uint64_t, int>, Plaintext> mask;
+    std::map<std::tuple<int, int, int, uint64_t>, Plaintext> bias;
+    size_t count() const { return diag.size() + mask.size() + bias.size(); }
+};
+
+// one layer over ciphertexts that each hold one lane (Evaluator, Ciphertext)
+// or every lane in lockstep (BatchEvaluator, CtBatch); `lanes` lists the lane
+// of each batch element
+template <class EV, class CT>
+class BertLayerT {
+public:
+    BertLayerT(EV &ev, BootstrapperT<EV, CT> &bs, const BertShape &shape, const BertWeights &w,
+               std::vector<int> lanes, std::shared_ptr<BertPlaintexts> plain = nullptr);
+    // x: n_hid ciphertexts in the std layout (tokens and their copies) at 2
+    // or more limbs and at the bootstrapper's final scale; out: n_hid
+    // ciphertexts (first copies valid)
+    void forward(const std::vector<CT> &x, std::vector<CT> &out);
+
+    // the stages of forward(), public for tests and profiling
+    void project(const std::vector<CT> &x, int which, std::vector<CT> &y);       // linear map + bias
+    void attention(std::vector<CT> &q, std::vector<CT> &k, std::vector<CT> &v, std::vector<CT> &o);
+    void layer_norm(std::vector<CT> &x);
+    void bootstrap_all(std::vector<CT> &cts);
+
+    enum { LT_Q = 0, LT_K, LT_V, LT_O, LT_1, LT_2, LT_COUNT };
+    double delta() const { return delta_; }
+    size_t cached_plaintexts() const { return pt_->count(); }
+    const BertShape &shape() const { return sh_; }
+
+private:
+    int in_count(int which) const;
+    int out_count(int which) const;
+    int in_features(int which) const;
+    int out_features(int which) const;
+    const std::vector<double> &weights(int which) const;
+    const std::vector<double> &bias(int which) const;
+    // feature index at (ciphertext, block) of the input / output, or -1
+    int in_feature(int which, int ct, int block) const;
+    int out_feature(int which, int ct, int block) const;
+    bool diag_nonzero(int which, int a, int b, int d) const;
+    std::vector<double> diag_vector(int which, int a, int b, int d, int pre_rotate_blocks) const;
+    const Plaintext &diag(int which, int a, int b, int d, int limbs, double scale);
+    void encode_diagonals(int which, int limbs, double scale);
+    const Plaintext &bias_plain(int which, int ct, int limbs, double scale);
+    void masks(int delta, int kind, int limbs, double scale, std::vector<const Plaintext *> &out);
+    void shrink_for_bootstrap(std::vector<CT> &cts);
+    void exact_scale_const(CT &ct, double value, double target_scale);
+
+    EV *ev_;
+    BootstrapperT<EV, CT> *bs_;
+    CKKSEvaluatorT<EV, CT> ck_;
+    BertShape sh_;
+    BertWeights w_;
+    std::vector<int> lanes_;
+    double delta_;
+    std::shared_ptr<BertPlaintexts> pt_;
+};
+
+using BertLayer = BertLayerT<Evaluator, Ciphertext>;
+using BatchBertLayer = BertLayerT<BatchEvaluator, CtBatch>;
+
+}  // namespace nexus

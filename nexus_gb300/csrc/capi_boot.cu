@@ -5,6 +5,7 @@
 
 #include "../../include/nexus_gb300.h"
 #include "argmax.h"
+#include "bert.h"
 #include "bootstrap.h"
 #include "capi_types.h"
 
@@ -341,4 +342,237 @@ extern "C" int nexus_bootstrapper_cached_plaintexts(const nexus_bootstrapper *bs
     if (!bs || !count) return fail("nexus_bootstrapper_cached_plaintexts", "null argument");
     *count = bs->bs.cached_plaintexts() + (bs->bbs ? bs->bbs->cached_plaintexts() : 0);
     return 0;
+}
+
+// ------------------------------------------------------------------ BERT layer
+
+struct nexus_bert_layer {
+    nexus_bootstrapper *bs;
+    BertShape shape;
+    BertWeights w;
+    std::shared_ptr<BertPlaintexts> plain;
+    std::vector<std::unique_ptr<BertLayer>> single;  // one per lane
+    std::unique_ptr<BatchBertLayer> lockstep;        // every lane, built on first use
+};
+
+extern "C" int nexus_bert_layer_create(nexus_bootstrapper *bs, int hidden, int heads, int head_dim, int ffn, int T,
+                                       int n_lanes, const int *lane_requests, const int *requests,
+                                       double boot_shrink, const double *weights, nexus_bert_layer **out)
+{
+    static const char *fn = "nexus_bert_layer_create";
+    if (!bs || !lane_requests || !requests || !weights || !out) return fail(fn, "null argument");
+    if (n_lanes < 1) return fail(fn, "at least one lane is required");
+    *out = nullptr;
+    return guarded(fn, [&] {
+        if (bs->bs.fftcoeff1.empty()) throw std::logic_error("generate_LT_coefficient_3 has not been called");
+        std::unique_ptr<nexus_bert_layer> L(new nexus_bert_layer());
+        L->bs = bs;
+        BertShape &sh = L->shape;
+        sh.hidden = hidden;
+        sh.heads = heads;
+        sh.head_dim = head_dim;
+        sh.ffn = ffn;
+        sh.T = T;
+        sh.boot_shrink = boot_shrink;
+        size_t r = 0;
+        for (int l = 0; l < n_lanes; ++l) {
+            if (lane_requests[l] < 1) throw std::invalid_argument("a lane needs at least one request");
+            std::vector<std::pair<int, int>> lane;
+            for (int j = 0; j < lane_requests[l]; ++j, ++r) lane.emplace_back(requests[2 * r], requests[2 * r + 1]);
+            sh.lanes.push_back(lane);
+        }
+        sh.derive(bs->ev->ev.slot_count());
+        const size_t d = hidden, f = ffn;
+        const double *p = weights;
+        auto take = [&](std::vector<double> &v, size_t n) {
+            v.assign(p, p + n);
+            p += n;
+        };
+        BertWeights &w = L->w;
+        take(w.wq, d * d);
+        take(w.wk, d * d);
+        take(w.wv, d * d);
+        take(w.wo, d * d);
+        take(w.w1, d * f);
+        take(w.w2, f * d);
+        take(w.bq, d);
+        take(w.bk, d);
+        take(w.bv, d);
+        take(w.bo, d);
+        take(w.b1, f);
+        take(w.b2, d);
+        L->plain = std::make_shared<BertPlaintexts>();
+        for (int l = 0; l < n_lanes; ++l)
+            L->single.emplace_back(new BertLayer(bs->ev->ev, bs->bs, sh, w, {l}, L->plain));
+        *out = L.release();
+    });
+}
+
+extern "C" int nexus_bert_layer_destroy(nexus_bert_layer *layer)
+{
+    delete layer;
+    return 0;
+}
+
+extern "C" int nexus_bert_layer_info(const nexus_bert_layer *layer, int *n_lanes, int *n_hidden_cts, int *n_head_cts,
+                                     int *n_ffn_cts, uint64_t *cached_plaintexts)
+{
+    if (!layer) return fail("nexus_bert_layer_info", "null argument");
+    if (n_lanes) *n_lanes = (int)layer->shape.lanes.size();
+    if (n_hidden_cts) *n_hidden_cts = layer->shape.n_hid;
+    if (n_head_cts) *n_head_cts = layer->shape.n_head;
+    if (n_ffn_cts) *n_ffn_cts = layer->shape.n_ffn;
+    if (cached_plaintexts) *cached_plaintexts = layer->plain ? layer->plain->count() : 0;
+    return 0;
+}
+
+extern "C" int nexus_bert_layer_rotation_steps(const nexus_bert_layer *layer, int *steps, int *count, int capacity)
+{
+    static const char *fn = "nexus_bert_layer_rotation_steps";
+    if (!layer || !count) return fail(fn, "null argument");
+    return guarded(fn, [&] {
+        const std::vector<int> v = layer->shape.rotation_steps();
+        if (steps) {
+            if ((int)v.size() > capacity) throw std::length_error("capacity too small");
+            for (size_t i = 0; i < v.size(); ++i) steps[i] = v[i];
+        }
+        *count = (int)v.size();
+    });
+}
+
+namespace {
+
+BatchBertLayer &bert_lockstep(nexus_bert_layer *L)
+{
+    if (!L->lockstep) {
+        BatchBootstrapper &BB = lockstep_form(L->bs);
+        std::vector<int> lanes;
+        for (size_t l = 0; l < L->shape.lanes.size(); ++l) lanes.push_back((int)l);
+        L->lockstep.reset(new BatchBertLayer(*L->bs->bev, BB, L->shape, L->w, lanes, L->plain));
+    }
+    return *L->lockstep;
+}
+
+// run `body` on the lanes' ciphertexts: in[count_in] per lane (lane-major
+// handles) -> out[count_out] per lane
+template <class F1, class F2>
+void bert_run(nexus_bert_layer *L, int lockstep, nexus_ciphertext *const *in, int count_in,
+              nexus_ciphertext *const *out, int count_out, F1 &&single_body, F2 &&batch_body)
+{
+    const int lanes = (int)L->shape.lanes.size();
+    nexus_evaluator *ev = L->bs->ev;
+    for (int i = 0; i < lanes * count_in; ++i) {
+        if (!in[i]) throw std::invalid_argument("null ciphertext");
+        if (const char *e = input_problem(ev->ctx, in[i])) throw std::invalid_argument(e);
+    }
+    for (int i = 0; i < lanes * count_out; ++i)
+        if (!out[i]) throw std::invalid_argument("null result");
+    if (!lockstep) {
+        for (int l = 0; l < lanes; ++l) {
+            std::vector<Ciphertext> x(count_in), y;
+            for (int c = 0; c < count_in; ++c) x[c] = in[l * count_in + c]->ct;
+            single_body(*L->single[l], x, y);
+            if ((int)y.size() != count_out) throw std::logic_error("unexpected output count");
+            for (int c = 0; c < count_out; ++c) out[l * count_out + c]->ct = std::move(y[c]);
+        }
+        return;
+    }
+    BatchBertLayer &B = bert_lockstep(L);
+    std::vector<CtBatch> x(count_in), y;
+    std::vector<const nexus_ciphertext *> col(lanes);
+    for (int c = 0; c < count_in; ++c) {
+        for (int l = 0; l < lanes; ++l) col[l] = in[l * count_in + c];
+        x[c] = gather_batch(ev, col.data(), lanes);
+    }
+    batch_body(B, x, y);
+    if ((int)y.size() != count_out) throw std::logic_error("unexpected output count");
+    std::vector<nexus_ciphertext *> dst(lanes);
+    for (int c = 0; c < count_out; ++c) {
+        for (int l = 0; l < lanes; ++l) dst[l] = out[l * count_out + c];
+        scatter_batch(ev, y[c], dst.data());
+    }
+}
+
+}  // namespace
+
+extern "C" int nexus_bert_layer_forward(nexus_bert_layer *layer, int lockstep, nexus_ciphertext *const *x,
+                                        nexus_ciphertext *const *out)
+{
+    static const char *fn = "nexus_bert_layer_forward";
+    if (!layer || !x || !out) return fail(fn, "null argument");
+    return guarded(fn, [&] {
+        const int n = layer->shape.n_hid;
+        bert_run(
+            layer, lockstep, x, n, out, n,
+            [](BertLayer &L, std::vector<Ciphertext> &a, std::vector<Ciphertext> &b) { L.forward(a, b); },
+            [](BatchBertLayer &L, std::vector<CtBatch> &a, std::vector<CtBatch> &b) { L.forward(a, b); });
+    });
+}
+
+extern "C" int nexus_bert_layer_stage(nexus_bert_layer *layer, int lockstep, int stage, int which,
+                                      nexus_ciphertext *const *in, int count_in, nexus_ciphertext *const *out,
+                                      int count_out)
+{
+    static const char *fn = "nexus_bert_layer_stage";
+    if (!layer || !in || !out) return fail(fn, "null argument");
+    return guarded(fn, [&] {
+        const BertShape &sh = layer->shape;
+        switch (stage) {
+        case NEXUS_BERT_PROJECT: {
+            if (which < 0 || which > 5) throw std::invalid_argument("unknown linear map");
+            const int n_in = which == 3 ? sh.n_head : which == 5 ? sh.n_ffn : sh.n_hid;
+            const int n_out = which <= 2 ? sh.n_head : which == 4 ? sh.n_ffn : sh.n_hid;
+            if (count_in != n_in || count_out != n_out) throw std::invalid_argument("wrong ciphertext count");
+            bert_run(
+                layer, lockstep, in, n_in, out, n_out,
+                [&](BertLayer &L, std::vector<Ciphertext> &a, std::vector<Ciphertext> &b) { L.project(a, which, b); },
+                [&](BatchBertLayer &L, std::vector<CtBatch> &a, std::vector<CtBatch> &b) { L.project(a, which, b); });
+            break;
+        }
+        case NEXUS_BERT_ATTENTION: {
+            const int nh = sh.n_head;
+            if (count_in != 3 * nh || count_out != nh) throw std::invalid_argument("wrong ciphertext count");
+            auto split = [nh](auto &a, auto &q, auto &k, auto &v) {
+                for (int i = 0; i < nh; ++i) {
+                    q.push_back(std::move(a[i]));
+                    k.push_back(std::move(a[nh + i]));
+                    v.push_back(std::move(a[2 * nh + i]));
+                }
+            };
+            bert_run(
+                layer, lockstep, in, 3 * nh, out, nh,
+                [&](BertLayer &L, std::vector<Ciphertext> &a, std::vector<Ciphertext> &b) {
+                    std::vector<Ciphertext> q, k, v;
+                    split(a, q, k, v);
+                    L.attention(q, k, v, b);
+                },
+                [&](BatchBertLayer &L, std::vector<CtBatch> &a, std::vector<CtBatch> &b) {
+                    std::vector<CtBatch> q, k, v;
+                    split(a, q, k, v);
+                    L.attention(q, k, v, b);
+                });
+            break;
+        }
+        case NEXUS_BERT_LAYER_NORM:
+        case NEXUS_BERT_BOOTSTRAP: {
+            if (count_in != count_out || count_in < 1) throw std::invalid_argument("wrong ciphertext count");
+            const bool ln = stage == NEXUS_BERT_LAYER_NORM;
+            bert_run(
+                layer, lockstep, in, count_in, out, count_out,
+                [&](BertLayer &L, std::vector<Ciphertext> &a, std::vector<Ciphertext> &b) {
+                    if (ln) L.layer_norm(a);
+                    else L.bootstrap_all(a);
+                    b = std::move(a);
+                },
+                [&](BatchBertLayer &L, std::vector<CtBatch> &a, std::vector<CtBatch> &b) {
+                    if (ln) L.layer_norm(a);
+                    else L.bootstrap_all(a);
+                    b = std::move(a);
+                });
+            break;
+        }
+        default:
+            throw std::invalid_argument("unknown stage");
+        }
+    });
 }

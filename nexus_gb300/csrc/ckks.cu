@@ -5,6 +5,8 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <string>
+#include <thread>
 
 #include "ckks.h"
 #include "encoder.h"
@@ -221,6 +223,39 @@ void Evaluator::encode(const std::vector<std::complex<double>> &values, int limb
     ck(cudaMemcpyAsync(out.mutable_data(), host.data(), host.size() * 8, cudaMemcpyHostToDevice, s_), "upload");
     ck(cudaStreamSynchronize(s_), "encode");
     ntt_forward(c_, out.mutable_data(), 1, 0, limbs, s_);
+}
+
+void Evaluator::encode_many(const std::vector<const std::vector<std::complex<double>> *> &values, int limbs,
+                            double scale, const std::vector<Plaintext *> &outs, unsigned threads)
+{
+    if (limbs < 1 || limbs > top_limbs()) throw std::invalid_argument("parms_id is not valid for encryption parameters");
+    if (values.size() != outs.size()) throw std::invalid_argument("encode_many: one output per value vector");
+    const size_t m = values.size(), words = (size_t)limbs * c_.n;
+    if (m == 0) return;
+    if (threads == 0) threads = std::max(1u, std::thread::hardware_concurrency());
+    threads = (unsigned)std::min<size_t>(threads, m);
+    std::vector<uint64_t> host(m * words);
+    std::vector<std::string> errors(threads);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < threads; ++t)
+        th.emplace_back([&, t] {
+            try {
+                for (size_t i = t; i < m; i += threads)
+                    enc_->encode(values[i]->data(), values[i]->size(), scale, limbs, host.data() + i * words);
+            } catch (const std::exception &e) {
+                errors[t] = e.what();
+            }
+        });
+    for (auto &t : th) t.join();
+    for (auto &e : errors)
+        if (!e.empty()) throw std::invalid_argument(e);
+    for (size_t i = 0; i < m; ++i) {
+        outs[i]->set_vector(c_, limbs, scale, s_);
+        ck(cudaMemcpyAsync(outs[i]->mutable_data(), host.data() + i * words, words * 8, cudaMemcpyHostToDevice, s_),
+           "upload");
+    }
+    ck(cudaStreamSynchronize(s_), "encode");  // host buffer lifetime
+    for (size_t i = 0; i < m; ++i) ntt_forward(c_, outs[i]->mutable_data(), 1, 0, limbs, s_);
 }
 
 void Evaluator::encode_then_drop(const std::vector<std::complex<double>> &values, int limbs, double scale,

@@ -140,6 +140,10 @@ public:
     void encode(double value, int limbs, double scale, Plaintext &out);  // scalar path
     void encode(double value, double scale, Plaintext &out) { encode(value, top_limbs(), scale, out); }
     void encode(const std::vector<std::complex<double>> &values, int limbs, double scale, Plaintext &out);
+    // outs[i] = encode(*values[i], limbs, scale): the host FFTs run on up to
+    // `threads` threads (0: every core), then one upload and NTT per plaintext
+    void encode_many(const std::vector<const std::vector<std::complex<double>> *> &values, int limbs, double scale,
+                     const std::vector<Plaintext *> &outs, unsigned threads = 0);
     // SEAL's encode(..., scale) at the top level followed by mod_switch_to(limbs)
     void encode_then_drop(const std::vector<std::complex<double>> &values, int limbs, double scale, Plaintext &out);
     void encode_then_drop(double value, int limbs, double scale, Plaintext &out);

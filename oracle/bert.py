@@ -1,0 +1,318 @@
+"""The encrypted BERT encoder layer restated on the oracle -- TEST
+INFRASTRUCTURE (the checker of nexus_gb300/csrc/bert.cu; never shipped or
+timed as the product).
+
+The layer has no counterpart in the NEXUS tree (its drivers run one operator
+at a time, src/main.cpp:25-27, and it has no ciphertext x ciphertext product);
+this is the operation sequence the engine defines, written once more over the
+oracle's SEAL restatement (nexus_l3.Evaluator) so that every word can be
+compared.  Its pieces are NEXUS's own: CKKSEvaluator::exp and ::inverse in the
+softmax sequence of src/softmax.cpp:6-42, ::invert_sqrt in the LayerNorm
+sequence of src/layer_norm.cpp:6-33, GeLUEvaluator::gelu (src/gelu.cpp:5-111)
+and Bootstrapper::bootstrap_3 (oracle/bootstrap.py).
+
+Packing (the engine's): slot j*T + t of a ciphertext is feature block j at
+token slot t; a lane packs requests (o_r, L_r) with tokens at o_r + i and
+o_r + L_r + i.  std layout: feature f in ciphertext f // NB, block f % NB;
+head layout: feature h*dh + k in ciphertext k // KB, block (k % KB)*H2 + h.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import nexus_l3 as L
+
+LT_Q, LT_K, LT_V, LT_O, LT_1, LT_2 = range(6)
+
+
+def _pow2_ceil(v):
+    p = 1
+    while p < v:
+        p <<= 1
+    return p
+
+
+class Shape:
+    def __init__(self, slots, hidden, heads, head_dim, ffn, T, lanes, boot_shrink):
+        self.S, self.hidden, self.heads, self.head_dim, self.ffn, self.T = slots, hidden, heads, head_dim, ffn, T
+        self.lanes = [list(l) for l in lanes]
+        self.boot_shrink = float(boot_shrink)
+        self.NB = slots // T
+        self.H2 = _pow2_ceil(heads)
+        self.KB = self.NB // self.H2
+        self.n_head = -(-head_dim // self.KB)
+        self.n_hid = -(-hidden // self.NB)
+        self.n_ffn = -(-ffn // self.NB)
+        self.Lmax = max(Lr for lane in lanes for (_, Lr) in lane)
+        self.G = int(math.ceil(math.sqrt(self.Lmax)))
+        self.Glt = int(math.ceil(math.sqrt(self.NB)))
+
+    def rotation_steps(self):
+        v = []
+
+        def push(s):
+            s %= self.S
+            if s and s not in v:
+                v.append(s)
+        for b in range(1, self.Glt):
+            push(b * self.T)
+        g = 1
+        while g * self.Glt < self.NB:
+            push(g * self.Glt * self.T)
+            g += 1
+        for b in range(1, self.G):
+            push(b)
+        g = 1
+        while g * self.G < self.Lmax:
+            push(g * self.G)
+            push(-g * self.G)
+            g += 1
+        m = 1
+        while m < self.KB:
+            push(self.H2 * self.T * m)
+            m <<= 1
+        m = 1
+        while m < self.NB:
+            push(self.T * m)
+            m <<= 1
+        return v
+
+
+class BertLayer:
+    """The engine's BertLayerT for one lane, on the oracle."""
+
+    def __init__(self, ev: L.Evaluator, bs, shape: Shape, w: dict, lane: int):
+        self.ev, self.bs, self.sh, self.w, self.lane = ev, bs, shape, w, lane
+        self.delta = float(bs.final_scale)
+        self.ck = L.CKKSEvaluator(ev, self.delta)
+
+    # -- linear maps -----------------------------------------------------------
+    def _in_count(self, which):
+        sh = self.sh
+        return sh.n_head if which == LT_O else (sh.n_ffn if which == LT_2 else sh.n_hid)
+
+    def _out_count(self, which):
+        sh = self.sh
+        return sh.n_head if which <= LT_V else (sh.n_ffn if which == LT_1 else sh.n_hid)
+
+    def _head_feature(self, ct, block):
+        sh = self.sh
+        h, k = block % sh.H2, ct * sh.KB + block // sh.H2
+        return -1 if h >= sh.heads or k >= sh.head_dim else h * sh.head_dim + k
+
+    def _in_feature(self, which, ct, block):
+        if which == LT_O:
+            return self._head_feature(ct, block)
+        f = ct * self.sh.NB + block
+        return f if f < (self.sh.ffn if which == LT_2 else self.sh.hidden) else -1
+
+    def _out_feature(self, which, ct, block):
+        if which <= LT_V:
+            return self._head_feature(ct, block)
+        f = ct * self.sh.NB + block
+        return f if f < (self.sh.ffn if which == LT_1 else self.sh.hidden) else -1
+
+    def _weights(self, which):
+        return self.w[("wq", "wk", "wv", "wo", "w1", "w2")[which]]
+
+    def _bias(self, which):
+        return self.w[("bq", "bk", "bv", "bo", "b1", "b2")[which]]
+
+    def _diag(self, which, a, b, d):
+        """diagonal d of block (a -> b), divided by boot_shrink, or None when zero"""
+        sh = self.sh
+        W = self._weights(which)
+        vals = np.zeros(sh.NB)
+        nz = False
+        for j in range(sh.NB):
+            fo, fi = self._out_feature(which, b, j), self._in_feature(which, a, (j + d) % sh.NB)
+            if fo >= 0 and fi >= 0:
+                vals[j] = W[fi, fo] / sh.boot_shrink
+                nz = True
+        if not nz:
+            return None
+        g = d // sh.Glt
+        vals = np.roll(vals, g * sh.Glt)       # pre-rotated by the giant step
+        return np.repeat(vals, sh.T)
+
+    def project(self, x, which):
+        ev, sh = self.ev, self.sh
+        l = x[0].limbs
+        in_scale = x[0].scale
+        dscale = float(ev.q[l - 1]) * self.delta / in_scale
+        baby = [[xa] + [ev.rotate(xa, b * sh.T) for b in range(1, sh.Glt)] for xa in x]
+        y = []
+        for b in range(self._out_count(which)):
+            acc = None
+            g = 0
+            while g * sh.Glt < sh.NB:
+                giant = None
+                for a in range(len(x)):
+                    for bb in range(sh.Glt):
+                        d = g * sh.Glt + bb
+                        if d >= sh.NB:
+                            break
+                        v = self._diag(which, a, b, d)
+                        if v is None:
+                            continue
+                        t = ev.multiply_plain(baby[a][bb], ev.encode(v, dscale, l))
+                        giant = t if giant is None else ev.add(giant, t)
+                if giant is not None:
+                    t = ev.rotate(giant, g * sh.Glt * sh.T) if g else giant
+                    acc = t if acc is None else ev.add(acc, t)
+                g += 1
+            acc = ev.rescale(acc)
+            acc.scale = self.delta / sh.boot_shrink
+            bias = np.zeros(sh.S)
+            bv = self._bias(which)
+            for j in range(sh.NB):
+                f = self._out_feature(which, b, j)
+                if f >= 0:
+                    bias[j * sh.T:(j + 1) * sh.T] = bv[f]
+            acc = ev.add_plain(acc, ev.encode(bias, acc.scale, acc.limbs))
+            y.append(acc)
+        return y
+
+    # -- helpers ------------------------------------------------------------------
+    def exact_scale_const(self, ct, value, target):
+        ev = self.ev
+        q = float(ev.q[ct.limbs - 1])
+        p = ev.encode_scalar(value, q * target / ct.scale, ct.limbs)
+        ct = ev.rescale(ev.multiply_plain(ct, p))
+        ct.scale = target
+        return ct
+
+    def shrink_for_bootstrap(self, cts):
+        out = []
+        for c in cts:
+            c = self.exact_scale_const(c, 1.0 / self.sh.boot_shrink, self.delta)
+            c.scale = self.delta / self.sh.boot_shrink
+            out.append(c)
+        return out
+
+    def bootstrap_all(self, cts):
+        return [self.bs.bootstrap_3(self.ev.mod_switch_to(c, 1)) for c in cts]
+
+    def _mask(self, delta, kind, limbs, scale):
+        sh = self.sh
+        reqs = sh.lanes[self.lane]
+        v = np.zeros(sh.S)
+        inv_sqrt = 1.0 / math.sqrt(sh.head_dim)
+        for j in range(sh.NB):
+            head_ok = (j % sh.H2) < sh.heads
+            for t in range(sh.T):
+                ok = head_ok and any(delta < Lr and o <= t < o + Lr for (o, Lr) in reqs)
+                v[j * sh.T + t] = (inv_sqrt if ok else 0.0) if kind == 0 else (0.0 if ok else -128.0)
+        sc = float(self.ev.q[limbs - 1]) if kind == 0 else scale
+        return self.ev.encode(v, sc, limbs)
+
+    # -- blocks -----------------------------------------------------------------
+    def attention(self, q, k, v):
+        ev, sh, ck = self.ev, self.sh, self.ck
+        nh, G, Lm, S = sh.n_head, sh.G, sh.Lmax, sh.S
+        e_limbs = 4
+        q = [ev.mod_switch_to(c, e_limbs + 10) for c in q]
+        k = [ev.mod_switch_to(c, e_limbs + 10) for c in k]
+        v = [ev.mod_switch_to(c, e_limbs - 1) for c in v]
+        n_g = -(-Lm // G)
+        kb = [[c] + [ev.rotate(c, b) for b in range(1, G)] for c in k]
+        vb = [[c] + [ev.rotate(c, b) for b in range(1, G)] for c in v]
+        qg = [[c] + [ev.rotate(c, S - g * G) for g in range(1, n_g)] for c in q]
+        e = []
+        for d in range(Lm):
+            g, b = divmod(d, G)
+            acc = None
+            for c in range(nh):
+                t = ev.multiply(qg[c][g], kb[c][b])
+                acc = t if acc is None else ev.add(acc, t)
+            acc = ev.rescale(ev.relinearize(acc))
+            m = 1
+            while m < sh.KB:
+                acc = ev.add(acc, ev.rotate(acc, sh.H2 * sh.T * m))
+                m <<= 1
+            if g:
+                acc = ev.rotate(acc, g * G)
+            acc = ev.rescale(ev.multiply_plain(acc, self._mask(d, 0, acc.limbs, acc.scale)))
+            acc = ev.add_plain(acc, self._mask(d, 1, acc.limbs, acc.scale))
+            e.append(ck.exp(acc))
+        total = e[0]
+        for d in range(1, Lm):
+            total = ev.add(total, e[d])
+        total = ev.rescale(ev.multiply_plain(total, ev.encode_scalar(0.01 / sh.boot_shrink, total.scale,
+                                                                     total.limbs)))
+        total.scale /= sh.boot_shrink
+        inv = ck.inverse(self.bootstrap_all([total])[0])
+        inv = ev.rescale(ev.multiply_plain(inv, ev.encode_scalar(0.01, inv.scale, inv.limbs)))
+        inv = ev.mod_switch_to(inv, e[0].limbs)
+        p = [ev.rescale(ev.relinearize(ev.multiply(ed, inv))) for ed in e]
+        pg = [[(ev.rotate(p[g * G + b], S - g * G) if g else p[b]) for b in range(G) if g * G + b < Lm]
+              for g in range(n_g)]
+        o = []
+        for c in range(nh):
+            acc = None
+            for g in range(n_g):
+                part = None
+                for b in range(len(pg[g])):
+                    t = ev.multiply(pg[g][b], vb[c][b])
+                    part = t if part is None else ev.add(part, t)
+                part = ev.rescale(ev.relinearize(part))
+                if g:
+                    part = ev.rotate(part, g * G)
+                acc = part if acc is None else ev.add(acc, part)
+            o.append(acc)
+        return o
+
+    def layer_norm(self, x):
+        ev, sh = self.ev, self.sh
+        total = None
+        for c in x:
+            t = ev.rescale(ev.relinearize(ev.square(c)))
+            total = t if total is None else ev.add(total, t)
+        m = 1
+        while m < sh.NB:
+            total = ev.add(total, ev.rotate(total, sh.T * m))
+            m <<= 1
+        total = ev.rescale(ev.multiply_plain(total, ev.encode_scalar(1.0 / sh.hidden, total.scale, total.limbs)))
+        r = self.ck.invert_sqrt(total, 4, 2)
+        return [ev.rescale(ev.relinearize(ev.multiply(ev.mod_switch_to(c, r.limbs), r))) for c in x]
+
+    def forward(self, x, trace=None):
+        """x: n_hid ciphertexts of this lane; returns the layer's output.
+        trace, a dict, receives every stage's ciphertexts."""
+        ev, sh = self.ev, self.sh
+        rec = (lambda k, v: trace.__setitem__(k, v)) if trace is not None else (lambda k, v: None)
+        x_res = [ev.mod_switch_to(c, 1) for c in self.shrink_for_bootstrap(x)]
+        x2 = [ev.mod_switch_to(c, 2) for c in x]
+        q, k, v = self.project(x2, LT_Q), self.project(x2, LT_K), self.project(x2, LT_V)
+        rec("qkv", q + k + v)
+        qkv = self.bootstrap_all(q + k + v)
+        nh = sh.n_head
+        q, k, v = qkv[:nh], qkv[nh:2 * nh], qkv[2 * nh:]
+        rec("qkv_boot", qkv)
+        o = self.attention(q, k, v)
+        rec("attention", o)
+        a = self.project(o, LT_O)
+        for c in range(sh.n_hid):
+            a[c].scale = x_res[c].scale
+            a[c] = ev.add(a[c], x_res[c])
+        a = self.bootstrap_all(a)
+        rec("residual1_boot", a)
+        a = self.layer_norm(a)
+        rec("ln1", a)
+        y_res = [ev.mod_switch_to(c, 1) for c in self.shrink_for_bootstrap(a)]
+        a2 = [ev.mod_switch_to(c, 2) for c in a]
+        h = self.bootstrap_all(self.project(a2, LT_1))
+        rec("ffn1_boot", h)
+        h = [L.gelu(self.ck, c) for c in h]
+        rec("gelu", h)
+        f = self.project(h, LT_2)
+        for c in range(sh.n_hid):
+            f[c].scale = y_res[c].scale
+            f[c] = ev.add(f[c], y_res[c])
+        f = self.bootstrap_all(f)
+        rec("residual2_boot", f)
+        out = self.layer_norm(f)
+        rec("output", out)
+        return out
