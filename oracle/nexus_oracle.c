@@ -348,6 +348,68 @@ static void intt_full(uint64_t *a, const or_ctx *c, int j)
     }
 }
 
+/* ---- worker threads ----
+ * or_set_threads(t) makes the key switch and the rescale below spread their
+ * independent per-prime loops over t threads (1: the calling thread only).
+ * Every output word is computed by the same arithmetic whatever the count. */
+
+static int g_threads = 1;
+
+void or_set_threads(int t) { g_threads = t < 1 ? 1 : (t > 256 ? 256 : t); }
+int or_get_threads(void) { return g_threads; }
+
+typedef void (*pf_fn)(void *arg, int idx, int tid);
+
+typedef struct {
+    pf_fn fn;
+    void *arg;
+    int count, next;
+    pthread_mutex_t mu;
+} pf_job;
+
+typedef struct {
+    pf_job *job;
+    int tid;
+} pf_worker_arg;
+
+static void *pf_worker(void *p)
+{
+    pf_worker_arg *w = (pf_worker_arg *)p;
+    pf_job *j = w->job;
+    for (;;) {
+        pthread_mutex_lock(&j->mu);
+        int i = j->next++;
+        pthread_mutex_unlock(&j->mu);
+        if (i >= j->count) break;
+        j->fn(j->arg, i, w->tid);
+    }
+    return NULL;
+}
+
+/* fn(arg, i, tid) for i in [0, count); tid < parallel_width(count) */
+static int parallel_width(int count) { return count < g_threads ? (count < 1 ? 1 : count) : g_threads; }
+
+static void parallel_for(int count, pf_fn fn, void *arg)
+{
+    int nt = parallel_width(count);
+    if (nt <= 1) {
+        for (int i = 0; i < count; i++) fn(arg, i, 0);
+        return;
+    }
+    pf_job job;
+    job.fn = fn; job.arg = arg; job.count = count; job.next = 0;
+    pthread_mutex_init(&job.mu, NULL);
+    pthread_t th[256];
+    pf_worker_arg wa[256];
+    for (int t = 0; t < nt; t++) {
+        wa[t].job = &job;
+        wa[t].tid = t;
+        pthread_create(&th[t], NULL, pf_worker, &wa[t]);
+    }
+    for (int t = 0; t < nt; t++) pthread_join(th[t], NULL);
+    pthread_mutex_destroy(&job.mu);
+}
+
 /* ---- threaded batch driver over [poly][limb][N] ---- */
 
 typedef struct {
@@ -403,48 +465,76 @@ void or_ntt_lazy_limb(const or_ctx *c, uint64_t *a, int j) { ntt_lazy(a, c, j); 
 /* rescale                                                              */
 /* ------------------------------------------------------------------ */
 
-/* RNSTool::divide_and_round_q_last_ntt_inplace (util/rns.cpp:830-905) for one
- * polynomial of `limbs` limbs in NTT form over primes [0, limbs).  Limbs
- * [0, limbs-1) receive the result; the last limb is clobbered. */
-static void rescale_poly(const or_ctx *c, uint64_t *poly, int limbs, uint64_t *tmp)
+typedef struct {
+    const or_ctx *c;
+    uint64_t *polys;   /* [size][limbs][N] working copy */
+    int limbs;
+    uint64_t *tmp;     /* [threads][N] */
+} rs_job;
+
+/* the dropped limb of every polynomial: INTT and +q_last/2 (add_poly_scalar_coeffmod) */
+static void rs_last_task(void *arg, int s, int tid)
 {
+    (void)tid;
+    rs_job *j = (rs_job *)arg;
+    const or_ctx *c = j->c;
     size_t n = c->n;
-    int last = limbs - 1;
-    uint64_t *li = poly + (size_t)last * n;
+    int last = j->limbs - 1;
+    uint64_t *li = j->polys + ((size_t)s * j->limbs + last) * n;
     uint64_t ql = c->q[last];
     intt_full(li, c, last);
     uint64_t half = ql >> 1;
-    for (size_t t = 0; t < n; t++) li[t] = (li[t] + half) % ql; /* add_poly_scalar_coeffmod */
-    for (int i = 0; i < last; i++) {
-        uint64_t qi = c->q[i];
-        for (size_t t = 0; t < n; t++) tmp[t] = (qi < ql) ? li[t] % qi : li[t];
-        uint64_t neg_half_mod = qi - (half % qi);
-        for (size_t t = 0; t < n; t++) tmp[t] += neg_half_mod;
-        uint64_t qi_lazy = qi << 2;
-        ntt_lazy(tmp, c, i);
-        uint64_t *ci = poly + (size_t)i * n;
-        uint64_t inv = invmod(ql % qi, qi);
-        for (size_t t = 0; t < n; t++) {
-            uint64_t x = ci[t] + qi_lazy - tmp[t];
-            ci[t] = mulmod(x, inv, qi);
-        }
+    for (size_t t = 0; t < n; t++) li[t] = (li[t] + half) % ql;
+}
+
+/* limb i of polynomial s: (c_i - NTT(last mod q_i - half)) * q_last^-1 */
+static void rs_limb_task(void *arg, int idx, int tid)
+{
+    rs_job *j = (rs_job *)arg;
+    const or_ctx *c = j->c;
+    size_t n = c->n;
+    int last = j->limbs - 1;
+    int s = idx / last, i = idx % last;
+    uint64_t *poly = j->polys + (size_t)s * j->limbs * n;
+    const uint64_t *li = poly + (size_t)last * n;
+    uint64_t ql = c->q[last], half = ql >> 1;
+    uint64_t *tmp = j->tmp + (size_t)tid * n;
+    uint64_t qi = c->q[i];
+    for (size_t t = 0; t < n; t++) tmp[t] = (qi < ql) ? li[t] % qi : li[t];
+    uint64_t neg_half_mod = qi - (half % qi);
+    for (size_t t = 0; t < n; t++) tmp[t] += neg_half_mod;
+    uint64_t qi_lazy = qi << 2;
+    ntt_lazy(tmp, c, i);
+    uint64_t *ci = poly + (size_t)i * n;
+    uint64_t inv = invmod(ql % qi, qi);
+    for (size_t t = 0; t < n; t++) {
+        uint64_t x = ci[t] + qi_lazy - tmp[t];
+        ci[t] = mulmod(x, inv, qi);
     }
 }
 
 /* Evaluator::rescale_to_next (evaluator.cpp:1402-1480, 1682) on a ciphertext
- * [size][limbs][N]; writes [size][limbs-1][N] into out (may alias in). */
+ * [size][limbs][N]; writes [size][limbs-1][N] into out (may alias in).  Each
+ * polynomial follows RNSTool::divide_and_round_q_last_ntt_inplace
+ * (util/rns.cpp:830-905): INTT of the last limb, +q_last/2, then for every
+ * other limb reduce, subtract the rounding offset, NTT-lazy, subtract and
+ * multiply by q_last^-1 mod q_i. */
 void or_rescale_ntt(const or_ctx *c, const uint64_t *in, int size, int limbs, uint64_t *out)
 {
     size_t n = c->n;
-    uint64_t *poly = (uint64_t *)malloc(sizeof(uint64_t) * n * limbs);
-    uint64_t *tmp = (uint64_t *)malloc(sizeof(uint64_t) * n);
-    for (int s = 0; s < size; s++) {
-        memcpy(poly, in + (size_t)s * limbs * n, sizeof(uint64_t) * n * limbs);
-        rescale_poly(c, poly, limbs, tmp);
-        memmove(out + (size_t)s * (limbs - 1) * n, poly, sizeof(uint64_t) * n * (limbs - 1));
-    }
-    free(poly);
-    free(tmp);
+    rs_job j;
+    j.c = c;
+    j.limbs = limbs;
+    j.polys = (uint64_t *)malloc(sizeof(uint64_t) * n * limbs * size);
+    memcpy(j.polys, in, sizeof(uint64_t) * n * limbs * size);
+    int tasks = size * (limbs - 1);
+    j.tmp = (uint64_t *)malloc(sizeof(uint64_t) * n * parallel_width(tasks));
+    parallel_for(size, rs_last_task, &j);
+    parallel_for(tasks, rs_limb_task, &j);
+    for (int s = 0; s < size; s++)
+        memmove(out + (size_t)s * (limbs - 1) * n, j.polys + (size_t)s * limbs * n, sizeof(uint64_t) * n * (limbs - 1));
+    free(j.polys);
+    free(j.tmp);
 }
 
 /* mod_switch_drop_to_next (evaluator.cpp:1483-1546): drop the last limb */
@@ -459,6 +549,105 @@ void or_drop_last_limb(const or_ctx *c, const uint64_t *in, int size, int limbs,
 /* key switching                                                        */
 /* ------------------------------------------------------------------ */
 
+typedef struct {
+    const or_ctx *c;
+    uint64_t *ct;
+    int ell, K, sp, rns;
+    const uint64_t *target, *key;
+    uint64_t *tt;     /* [ell][N] target in coefficient form */
+    uint64_t *prod;   /* [2][rns][N] inner products */
+    uint64_t *tntt;   /* [threads][N] */
+    u128 *acc;        /* [threads][2][N] */
+} ks_job;
+
+static void ks_intt_task(void *arg, int j, int tid)
+{
+    (void)tid;
+    ks_job *k = (ks_job *)arg;
+    intt_full(k->tt + (size_t)j * k->c->n, k->c, j);
+}
+
+/* output prime I (the special prime when I == ell): every digit J reduced
+ * into q_I and transformed (the target's own limb when I == J), times the
+ * key's J-th digit, accumulated in 128 bits, one Barrett reduction */
+static void ks_modup_task(void *arg, int I, int tid)
+{
+    ks_job *k = (ks_job *)arg;
+    const or_ctx *c = k->c;
+    size_t n = c->n;
+    int ell = k->ell, K = k->K;
+    int ki = (I == ell) ? k->sp : I;
+    uint64_t qk = c->q[ki];
+    uint64_t *tntt = k->tntt + (size_t)tid * n;
+    u128 *acc = k->acc + (size_t)tid * 2 * n;
+    memset(acc, 0, sizeof(u128) * 2 * n);
+    for (int J = 0; J < ell; J++) {
+        const uint64_t *op;
+        if (I == J) {
+            op = k->target + (size_t)J * n;
+        } else {
+            const uint64_t *src = k->tt + (size_t)J * n;
+            if (c->q[J] <= qk) memcpy(tntt, src, sizeof(uint64_t) * n);
+            else for (size_t t = 0; t < n; t++) tntt[t] = src[t] % qk;
+            ntt_lazy(tntt, c, ki);
+            op = tntt;
+        }
+        for (int comp = 0; comp < 2; comp++) {
+            const uint64_t *kp = k->key + (((size_t)J * 2 + comp) * K + ki) * n;
+            u128 *a = acc + (size_t)comp * n;
+            for (size_t t = 0; t < n; t++) a[t] += (u128)op[t] * kp[t];
+        }
+    }
+    /* ell < 256 always, so the final Barrett reduction applies
+     * (the lazy counter never wraps) */
+    for (int comp = 0; comp < 2; comp++) {
+        uint64_t *dst = k->prod + ((size_t)comp * k->rns + I) * n;
+        u128 *a2 = acc + (size_t)comp * n;
+        for (size_t t = 0; t < n; t++) dst[t] = (uint64_t)(a2[t] % qk);
+    }
+}
+
+/* special-prime limb of component comp: INTT and +q_k/2 */
+static void ks_special_task(void *arg, int comp, int tid)
+{
+    (void)tid;
+    ks_job *k = (ks_job *)arg;
+    const or_ctx *c = k->c;
+    size_t n = c->n;
+    uint64_t qk = c->q[k->sp], qk_half = qk >> 1;
+    uint64_t *tl = k->prod + ((size_t)comp * k->rns + k->ell) * n;
+    intt_lazy(tl, c, k->sp);
+    for (size_t t = 0; t < n; t++) tl[t] = (tl[t] + qk_half) % qk;
+}
+
+/* ModDown of component comp into data prime i, added into the ciphertext */
+static void ks_moddown_task(void *arg, int idx, int tid)
+{
+    ks_job *k = (ks_job *)arg;
+    const or_ctx *c = k->c;
+    size_t n = c->n;
+    int ell = k->ell;
+    int comp = idx / ell, i = idx % ell;
+    uint64_t qk = c->q[k->sp], qk_half = qk >> 1;
+    const uint64_t *tl = k->prod + ((size_t)comp * k->rns + ell) * n;
+    uint64_t *tntt = k->tntt + (size_t)tid * n;
+    uint64_t qi = c->q[i];
+    for (size_t t = 0; t < n; t++) tntt[t] = (qk > qi) ? tl[t] % qi : tl[t];
+    uint64_t fix = qi - (qk_half % qi);
+    for (size_t t = 0; t < n; t++) tntt[t] += fix;
+    ntt_lazy(tntt, c, i);
+    uint64_t qi_lazy = qi << 2;
+    uint64_t *pi = k->prod + ((size_t)comp * k->rns + i) * n;
+    uint64_t inv = invmod(qk % qi, qi);
+    uint64_t *ci = k->ct + ((size_t)comp * ell + i) * n;
+    for (size_t t = 0; t < n; t++) {
+        uint64_t x = pi[t] + qi_lazy - tntt[t];
+        x = mulmod(x, inv, qi);
+        uint64_t y = ci[t] + x;
+        ci[t] = y >= qi ? y - qi : y;
+    }
+}
+
 /* Evaluator::switch_key_inplace (evaluator.cpp:2724-3022), CKKS branch.
  *   ct     : [2][ell][N] ciphertext in NTT form, updated in place
  *   target : [ell][N] polynomial (NTT form) to switch
@@ -468,68 +657,21 @@ void or_drop_last_limb(const or_ctx *c, const uint64_t *in, int size, int limbs,
 void or_switch_key(const or_ctx *c, uint64_t *ct, int ell, const uint64_t *target, const uint64_t *key)
 {
     size_t n = c->n;
-    int K = c->k, sp = K - 1;
-    int rns = ell + 1;
-    uint64_t *tt = (uint64_t *)malloc(sizeof(uint64_t) * n * ell);
-    memcpy(tt, target, sizeof(uint64_t) * n * ell);
-    for (int j = 0; j < ell; j++) intt_full(tt + (size_t)j * n, c, j);
-    uint64_t *prod = (uint64_t *)calloc((size_t)2 * rns * n, sizeof(uint64_t)); /* [2][rns][N] */
-    uint64_t *tntt = (uint64_t *)malloc(sizeof(uint64_t) * n);
-    u128 *acc = (u128 *)malloc(sizeof(u128) * 2 * n);
-    for (int I = 0; I < rns; I++) {
-        int ki = (I == ell) ? sp : I;
-        uint64_t qk = c->q[ki];
-        memset(acc, 0, sizeof(u128) * 2 * n);
-        for (int J = 0; J < ell; J++) {
-            const uint64_t *op;
-            if (I == J) {
-                op = target + (size_t)J * n;
-            } else {
-                const uint64_t *src = tt + (size_t)J * n;
-                if (c->q[J] <= qk) memcpy(tntt, src, sizeof(uint64_t) * n);
-                else for (size_t t = 0; t < n; t++) tntt[t] = src[t] % qk;
-                ntt_lazy(tntt, c, ki);
-                op = tntt;
-            }
-            for (int comp = 0; comp < 2; comp++) {
-                const uint64_t *kp = key + (((size_t)J * 2 + comp) * K + ki) * n;
-                u128 *a = acc + (size_t)comp * n;
-                for (size_t t = 0; t < n; t++) a[t] += (u128)op[t] * kp[t];
-            }
-        }
-        /* ell < 256 always, so the final Barrett reduction applies
-         * (the lazy counter never wraps) */
-        for (int comp = 0; comp < 2; comp++) {
-            uint64_t *dst = prod + ((size_t)comp * rns + I) * n;
-            u128 *a = acc + (size_t)comp * n;
-            for (size_t t = 0; t < n; t++) dst[t] = (uint64_t)(a[t] % qk);
-        }
-    }
+    ks_job k;
+    k.c = c; k.ct = ct; k.ell = ell; k.K = c->k; k.sp = c->k - 1; k.rns = ell + 1;
+    k.target = target; k.key = key;
+    int width = parallel_width(2 * ell > k.rns ? 2 * ell : k.rns);
+    k.tt = (uint64_t *)malloc(sizeof(uint64_t) * n * ell);
+    memcpy(k.tt, target, sizeof(uint64_t) * n * ell);
+    k.prod = (uint64_t *)calloc((size_t)2 * k.rns * n, sizeof(uint64_t));
+    k.tntt = (uint64_t *)malloc(sizeof(uint64_t) * n * width);
+    k.acc = (u128 *)malloc(sizeof(u128) * 2 * n * width);
+    parallel_for(ell, ks_intt_task, &k);
+    parallel_for(k.rns, ks_modup_task, &k);
     /* modulus switching with scaling (ModDown), CKKS branch */
-    uint64_t qk = c->q[sp], qk_half = qk >> 1;
-    for (int comp = 0; comp < 2; comp++) {
-        uint64_t *tl = prod + ((size_t)comp * rns + ell) * n;
-        intt_lazy(tl, c, sp);
-        for (size_t t = 0; t < n; t++) tl[t] = (tl[t] + qk_half) % qk;
-        for (int i = 0; i < ell; i++) {
-            uint64_t qi = c->q[i];
-            for (size_t t = 0; t < n; t++) tntt[t] = (qk > qi) ? tl[t] % qi : tl[t];
-            uint64_t fix = qi - (qk_half % qi);
-            for (size_t t = 0; t < n; t++) tntt[t] += fix;
-            ntt_lazy(tntt, c, i);
-            uint64_t qi_lazy = qi << 2;
-            uint64_t *pi = prod + ((size_t)comp * rns + i) * n;
-            uint64_t inv = invmod(qk % qi, qi);
-            uint64_t *ci = ct + ((size_t)comp * ell + i) * n;
-            for (size_t t = 0; t < n; t++) {
-                uint64_t x = pi[t] + qi_lazy - tntt[t];
-                x = mulmod(x, inv, qi);
-                uint64_t y = ci[t] + x;
-                ci[t] = y >= qi ? y - qi : y;
-            }
-        }
-    }
-    free(tt); free(prod); free(tntt); free(acc);
+    parallel_for(2, ks_special_task, &k);
+    parallel_for(2 * ell, ks_moddown_task, &k);
+    free(k.tt); free(k.prod); free(k.tntt); free(k.acc);
 }
 
 /* relinearize_internal (evaluator.cpp:1345-1400) for a size-3 ciphertext:

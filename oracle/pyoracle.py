@@ -70,8 +70,20 @@ def lib():
         l.or_add_scalar.argtypes = [C.c_void_p, u64p, C.c_int, u64p, C.c_int, u64p]
         l.or_is_prime.restype = C.c_int
         l.or_is_prime.argtypes = [C.c_uint64]
+        l.or_set_threads.argtypes = [C.c_int]
+        l.or_get_threads.restype = C.c_int
         _lib = l
     return _lib
+
+
+def set_threads(t: int) -> None:
+    """Threads the oracle's key switch and rescale spread over (1: the caller only).
+    The words do not depend on it."""
+    lib().or_set_threads(int(t))
+
+
+def get_threads() -> int:
+    return int(lib().or_get_threads())
 
 
 def _p(a: np.ndarray):
