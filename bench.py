@@ -501,6 +501,28 @@ def cpu_mm_sample(workers: int = 1, depth: int = 7):
                       f"extrapolated to 2 x 65535 nodes + 98304 products"}
 
 
+def _seal_seed(tag: int):
+    """The 8-word seed the digest scripts under tests/golden give case `tag`."""
+    import numpy as np
+    return np.array([(0x9E3779B97F4A7C15 * (tag + i + 1)) % 2 ** 64 for i in range(8)], dtype=np.uint64)
+
+
+def _digest_check(case: str, words) -> dict | None:
+    """Compare the SHA-256 of an output's words with the oracle's digest for
+    the same seeds (tests/golden/bench_digests.json)."""
+    import hashlib
+
+    import numpy as np
+    p = ROOT / "tests" / "golden" / "bench_digests.json"
+    try:
+        want = json.loads(p.read_text())["cases"][case]["sha256"]["output"]
+    except Exception:
+        return None
+    got = hashlib.sha256(np.ascontiguousarray(words, dtype="<u8").tobytes()).hexdigest()
+    return {"checked": f"output words of ciphertext 0 against the oracle's digest ({case})",
+            "words_equal_oracle": got == want}
+
+
 # ----------------------------------------------------------------------------- bootstrap workload
 
 BOOT_LOGN = 16
@@ -531,14 +553,17 @@ def run_boot_gpu(args, rank, world):
     n = 1 << BOOT_LOGN
     qs = ng.create_coeff_modulus(n, BOOT_BITS)
     ctx = ng.Context(BOOT_LOGN, qs)
-    sk = ctx.keygen_secret(seed=71 + rank, hamming_weight=192)
-    rk = ctx.keygen_relin(sk, seed=72)
+    # keys and encryptions from SEAL's seeded randomness: ciphertext 0 of the
+    # step is the input whose oracle digests tests/golden/bench_digests.json holds
+    seed = _seal_seed(400 + rank)
+    sk = ctx.seal_keygen_secret(seed, 192)
+    rk = ctx.seal_keygen_relin(sk, seed)
     ev = Evaluator(ctx, BOOT_SCALE, rk)
     bs = Bootstrapper(ev, **BOOT_PARAMS)
     steps = bs.rotation_steps(BOOT_LOGN - 1)
-    for i, st in enumerate(steps):
+    for st in steps:
         e = ctx.galois_elt(st)
-        ev.add_galois_key(e, ctx.keygen_galois(sk, e, seed=1000 + i))
+        ev.add_galois_key(e, ctx.seal_keygen_galois(sk, e, seed))
     bs.prepare_mod_polynomial()
     bs.generate_LT_coefficient_3()
     top = len(qs) - 1
@@ -548,7 +573,9 @@ def run_boot_gpu(args, rank, world):
         v = rng.uniform(-1, 1, n // 2)
         pt = torch.empty((top, n), dtype=torch.int64, device=dev)
         ctx.encode(v, BOOT_SCALE, top, pt)
-        ct = ctx.encrypt_symmetric(sk, pt, top, 500 + i)
+        s_i = seed.copy()
+        s_i[7] ^= np.uint64(i)
+        ct = ctx.seal_encrypt_symmetric(sk, pt, top, s_i)
         low = ct[:, :1, :].contiguous()
         vals.append(v)
         inputs.append(low)
@@ -572,6 +599,7 @@ def run_boot_gpu(args, rank, world):
     dec = ctx.decode(ctx.decrypt(sk, res[0].to_device()), res[0].scale).real
     err = float(np.max(np.abs(dec - vals[0])))
     out_limbs = res[0].info()[1]
+    parity = _digest_check("bootstrap_n65536", res[0].to_numpy()) if rank == 0 else None
     del res
     barrier(world)
     l0 = ng.kernel_launches()
@@ -651,8 +679,9 @@ def run_boot_gpu(args, rank, world):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "u64",
-        "data": "synthetic: slots ~ U(-1,1), seeded; engine-generated keys (sparse secret h=192)",
+        "data": "synthetic: slots ~ U(-1,1), seeded; keys and encryptions from a SEAL seed (sparse secret h=192)",
         "config": boot_config(len(steps)),
+        "parity": parity,
         "accuracy": {"max_abs_err_vs_input": err, "precision_bits": -float(np.log2(err)),
                      "output_limbs": out_limbs},
         "roofline": {
@@ -675,95 +704,70 @@ def run_boot_gpu(args, rank, world):
         "gpu_launches": launches,
     }
     if rank == 0 and world == 1:
-        res["cpu_baseline"] = cpu_boot_sample(workers=1)
+        res["cpu_baseline"] = cpu_boot_sample(os.cpu_count() or 1)
     return res
 
 
-def _boot_cpu_worker(seed):
-    """Time the oracle port's ring operations at N=2^16 on this core:
-    key switches at three levels (a quadratic in the limb count), and rescale,
-    tensor, plaintext product, addition, encode and the modulus raise."""
-    import numpy as np
+class CpuBootstrap:
+    """The oracle port's full-slot bootstrap_3 at N=2^16 on the host cores: the
+    key switches, rescales and NTTs spread over `threads` threads (the rest of
+    the port runs on one).  Every Galois element maps to one key of uniform
+    random residues: a key switch reads its whole key whatever the values, and
+    the refreshed ciphertext is not decrypted, so the time is a bootstrap's."""
 
-    from oracle import nexus_l3 as L
-    from oracle import pyoracle as po
-    n = 1 << BOOT_LOGN
-    qs = po.create_coeff_modulus(n, BOOT_BITS)
-    oc = po.OracleContext(BOOT_LOGN, qs)
-    rng = np.random.default_rng(seed)
-    elt = po.galois_elt_from_step(BOOT_LOGN, 1)
-    # random keys cost exactly what real ones do (nothing is decrypted here)
-    key = po.random_residues(rng, (len(qs) - 1, 2, len(qs), n), qs)
-    ev = L.Evaluator(oc, key, {elt: key})
+    def __init__(self, threads: int):
+        import numpy as np
 
-    def ct(limbs, size=2):
-        return L.Ct(po.random_residues(rng, (size, limbs, n), qs[:limbs]), BOOT_SCALE)
+        from nexus_gb300.remez import load_table
+        from oracle import bootstrap as B
+        from oracle import nexus_l3 as L
+        from oracle import pyoracle as po
+        self.threads = threads
+        po.set_threads(threads)
+        n = 1 << BOOT_LOGN
+        qs = po.create_coeff_modulus(n, BOOT_BITS)
+        rng = np.random.default_rng(0)
+        key = po.random_residues(rng, (len(qs) - 1, 2, len(qs), n), qs)
+        steps = B.rot_key_steps_3(BOOT_LOGN - 1, BOOT_LOGN - 1)
+        ev = L.Evaluator(po.OracleContext(BOOT_LOGN, qs), key,
+                         {po.galois_elt_from_step(BOOT_LOGN, s): key for s in steps})
+        self.bs = B.Bootstrapper(ev, BOOT_PARAMS["loge"], BOOT_LOGN - 1, BOOT_LOGN - 1, BOOT_PARAMS["L"], BOOT_SCALE,
+                                 25, 59, 2, 1, load_table())
+        self.bs.generate_LT_coefficient_3()
+        self.input = L.Ct(po.random_residues(rng, (2, 1, n), qs[:1]), BOOT_SCALE)
 
-    def timed(f):
+    def warm(self) -> float:
+        """The modulus raise and the first CoeffToSlot transform level (seconds)."""
         t = time.perf_counter()
-        f()
+        self.bs.initial_scale = self.input.scale
+        x = self.bs.modraise_inplace(self.input.copy())
+        x.scale = float(self.bs.ev.q[0])
+        self.bs.coefftoslot_full_3(x)
         return time.perf_counter() - t
 
-    ks = {l: timed(lambda: ev.apply_galois(ct(l), elt)) for l in (31, 24, 18)}
-    top = len(qs) - 1
-    per_limb = {
-        "rescale": timed(lambda: ev.rescale(ct(top))) / top,
-        "tensor": timed(lambda: ev.multiply(ct(top), ct(top))) / top,
-        "mul_plain": timed(lambda: ev.multiply_plain(ct(top), L.Pt(1.0, data=ct(top, 1).data[0]))) / top,
-        "add": timed(lambda: ev.add(ct(top), ct(top))) / top,
-    }
-    v = rng.uniform(-1, 1, n // 2)
-    e_top = timed(lambda: ev.encode(v, 2.0 ** 40, top))
-    e_one = timed(lambda: ev.encode(v, 2.0 ** 40, 1))
-    raise_s = timed(lambda: oc.ntt(oc.ntt(ct(1).data, 0, 1, inverse=True), 0, 1)) + per_limb["rescale"] * top
-    return ks, per_limb, (e_one, (e_top - e_one) / (top - 1)), raise_s
+    def bootstrap(self) -> float:
+        t = time.perf_counter()
+        self.bs.bootstrap_3(self.input.copy())
+        return time.perf_counter() - t
 
 
-def cpu_boot_sample(workers: int = 1):
-    """The oracle port on the host cores: per-operation times at N=2^16
-    (bounded sample) times the exact operation counts of one bootstrap_3
-    (oracle/opcount.py), giving the modelled time of one bootstrap per core."""
-    import concurrent.futures as cf
-    import multiprocessing as mp
+def _calibration_note() -> str:
+    p = ROOT / "oracle" / "seal_calibration.json"
+    try:
+        d = json.loads(p.read_text())["ops"]
+        return ("; port/SEAL time ratio on one core (oracle/seal_calibration.json): " +
+                ", ".join(f"{k} {v['port_over_seal']:.2f}" for k, v in d.items()))
+    except Exception:
+        return ""
 
-    import numpy as np
 
-    from nexus_gb300.remez import load_table
-    from oracle import opcount
-    from oracle import pyoracle as po
-    qs = po.create_coeff_modulus(1 << BOOT_LOGN, BOOT_BITS)
-    counts = opcount.bootstrap_op_counts(qs, BOOT_LOGN, BOOT_LOGN - 1, load_table())
-    w0 = time.perf_counter()
-    if workers <= 1:
-        outs = [_boot_cpu_worker(0)]
-    else:
-        with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
-            outs = list(ex.map(_boot_cpu_worker, range(workers)))
-    wall = time.perf_counter() - w0
-    totals = []
-    for ks, per_limb, (e0, e1), raise_s in outs:
-        ls = sorted(ks)
-        coef = np.polyfit(ls, [ks[l] for l in ls], 2)
-        t = 0.0
-        for (name, limbs), k in counts.items():
-            if name in ("galois", "relin"):
-                t += k * float(np.polyval(coef, limbs))
-                if name == "relin":
-                    t += k * per_limb["add"] * limbs
-            elif name in per_limb:
-                t += k * per_limb[name] * limbs
-            elif name == "encode":
-                t += k * (e0 + e1 * (limbs - 1))
-            elif name == "modraise":
-                t += k * raise_s
-        totals.append(t)
-    t_boot = statistics.mean(totals)
-    n_ks = sum(k for (nm, _), k in counts.items() if nm in ("galois", "relin"))
-    return {"value": workers / t_boot, "unit": "bootstraps/s", "cores": workers, "kind": "port",
-            "sample": f"{workers} worker(s) timing the oracle's key switch at 31/24/18 limbs and its rescale, "
-                      f"tensor, plaintext product, addition, encode and modulus raise at N=2^16 ({wall:.1f} s wall), "
-                      f"scaled by the exact operation counts of one bootstrap_3 ({n_ks} key switches, "
-                      f"modelled {t_boot:.1f} s per bootstrap per core)"}
+def cpu_boot_sample(threads: int):
+    """One full bootstrap of the oracle port, timed on `threads` host threads."""
+    cb = CpuBootstrap(threads)
+    t = cb.bootstrap()
+    return {"value": 1.0 / t, "unit": "bootstraps/s", "cores": threads, "kind": "port",
+            "sample": f"one full-slot bootstrap_3 at N=2^16 (51 + 16x46 + 14x51 + 51, K=25, deg 59) with the "
+                      f"oracle port, timed: {t:.1f} s on {threads} thread(s)" + _calibration_note()}
 
 
 # ----------------------------------------------------------------------------- BERT layer workload
@@ -780,11 +784,6 @@ def bert_config():
             "moduli_bits": "51 + 19x46 + 14x51 + special 51", "hamming_weight": 192, "scale": "2^46",
             "weights": "N(0, 0.02)", "tokens": "N(0, 1)", "parallelism": "replicas",
             "l2": "keys (~110 GB), encoded weights (~60 GB) and activations far above L2, no flush"}
-
-
-def _seal_seed(tag: int):
-    import numpy as np
-    return np.array([(0x9E3779B97F4A7C15 * (tag + i + 1)) % 2 ** 64 for i in range(8)], dtype=np.uint64)
 
 
 def run_bert_gpu(args, rank, world):
@@ -1221,20 +1220,28 @@ def main():
     if args.impl == "reference" and args.workload == "bootstrap":
         if rank != 0:
             return
-        workers = max(1, os.cpu_count() or 1)
-        vals = []
-        for i in range(args.warmup + args.steps):
-            r = cpu_boot_sample(workers=workers)
-            if i >= args.warmup:
-                vals.append(r)
-        value = statistics.mean(r["value"] for r in vals)
+        threads = max(1, os.cpu_count() or 1)
+        cb = CpuBootstrap(threads)
+        warm = [cb.warm() for _ in range(args.warmup)]
+        # full bootstraps: at least one, then as many of the requested steps
+        # as fit in about three minutes
+        times = [cb.bootstrap()]
+        budget = 180.0
+        while len(times) < args.steps and sum(times) + statistics.mean(times) <= budget:
+            times.append(cb.bootstrap())
+        value = len(times) / sum(times)
         res = {
             "impl": "reference", "metric": "bootstrap_throughput_n65536", "value": value, "unit": "bootstraps/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": BOOT_CTS * 1e3 / value,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-            "data": "synthetic (random residues; cost is data-independent)", "config": boot_config(),
-            "cpu_baseline": {"value": value, "unit": "bootstraps/s", "cores": workers, "kind": "port",
-                             "sample": "per step: " + vals[0]["sample"]},
+            "n_gpus": world, "steps": len(times), "steps_requested": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64", "data": "synthetic (uniform random residues; the cost does not depend on them)",
+            "config": dict(boot_config(47), cts_per_step=1),
+            "cpu_baseline": {"value": value, "unit": "bootstraps/s", "cores": threads, "kind": "port",
+                             "sample": f"per step one full-slot bootstrap_3 at N=2^16 with the oracle port on "
+                                       f"{threads} threads, timed ({', '.join(f'{t:.1f}' for t in times)} s); "
+                                       f"{len(times)} of the {args.steps} requested steps fit the ~3 minute "
+                                       f"budget; warm-up: modulus raise + CoeffToSlot "
+                                       f"({', '.join(f'{t:.1f}' for t in warm)} s)" + _calibration_note()},
             "e2e": {"value": value, "unit": "bootstraps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(res), flush=True)
