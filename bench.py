@@ -99,6 +99,32 @@ def _ntt_traffic(limbs_per_launch: float, n: int = 1 << 16):
     return None if per_limb is None else per_limb * limbs_per_launch * n / (1 << 16)
 
 
+def _butterfly_roof(ng, q: int, limb_ntts: int, ntt_ms: float, log_n: int):
+    """The NTT launches against their compute ceiling: butterflies per second
+    achieved (limb-NTTs x N/2 x log2 N over the measured NTT time) against the
+    rate of the NTT's own butterflies on register data (nexus_butterfly_rate),
+    forward and inverse in equal shares (harmonic mean)."""
+    small = q < (1 << 52)
+    fwd = ng.butterfly_rate(1 if small else 0, q)
+    inv = ng.butterfly_rate(2, q)
+    peak = 2.0 / (1.0 / fwd + 1.0 / inv)
+    achieved = limb_ntts * (1 << (log_n - 1)) * log_n / (ntt_ms / 1e3)
+    return {"unit": "butterflies/s", "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "peak_forward": fwd, "peak_inverse": inv,
+            "peak_source": "measured here: nexus_butterfly_rate, the NTT's butterfly functions on register data "
+                           f"({'small-prime ' if small else ''}forward and inverse)"}
+
+
+def _ntt_compute_bound(ng, q: int, limb_ntts: int, ms: float, n: int):
+    """Forward-only NTT workload against the forward butterfly's rate."""
+    log_n = n.bit_length() - 1
+    small = q < (1 << 52)
+    peak = ng.butterfly_rate(1 if small else 0, q)
+    achieved = limb_ntts * (n // 2) * log_n / (ms / 1e3)
+    return {"unit": "butterflies/s", "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "peak_source": "measured here: nexus_butterfly_rate, the NTT's forward butterfly on register data"}
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling while the timed region runs."""
 
@@ -254,6 +280,7 @@ def run_ntt_gpu(args, rank, world):
             "algorithmic_bytes_per_launch": alg_bytes,
             "traffic": _profile_traffic("ntt_forward_n65536_l24_64ct"),
             "int_multiply_pipe": _int_pipe("ntt_forward_n65536_l24_64ct", "the 60-bit NTT passes"),
+            "compute_bound": _ntt_compute_bound(ng, qs[0], limbs, per_launch_ms, n),
         },
         "e2e": {"value": limbs * e2e_steps * world / (e2e_ms / 1e3), "unit": "limb-NTT/s",
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
@@ -694,6 +721,7 @@ def run_boot_gpu(args, rank, world):
             "traffic": _ntt_traffic(ntt_limbs / max(1, ntt_calls)),
             "traffic_source": "ncu DRAM bytes per limb-NTT of the 51-bit NTT capture x limbs per launch",
             "int_multiply_pipe": _int_pipe("keyswitch_n65536_l31_4ct", "the key switch's ModUp NTT passes"),
+            "compute_bound": _butterfly_roof(ng, qs[1], ntt_limbs, ntt_ms, BOOT_LOGN),
         },
         "e2e": {"value": world * BOOT_CTS / e2e_s, "unit": "bootstraps/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes},
@@ -715,7 +743,7 @@ class CpuBootstrap:
     random residues: a key switch reads its whole key whatever the values, and
     the refreshed ciphertext is not decrypted, so the time is a bootstrap's."""
 
-    def __init__(self, threads: int):
+    def __init__(self, threads: int, bits=None):
         import numpy as np
 
         from nexus_gb300.remez import load_table
@@ -725,13 +753,13 @@ class CpuBootstrap:
         self.threads = threads
         po.set_threads(threads)
         n = 1 << BOOT_LOGN
-        qs = po.create_coeff_modulus(n, BOOT_BITS)
+        qs = po.create_coeff_modulus(n, bits or BOOT_BITS)
         rng = np.random.default_rng(0)
         key = po.random_residues(rng, (len(qs) - 1, 2, len(qs), n), qs)
         steps = B.rot_key_steps_3(BOOT_LOGN - 1, BOOT_LOGN - 1)
         ev = L.Evaluator(po.OracleContext(BOOT_LOGN, qs), key,
                          {po.galois_elt_from_step(BOOT_LOGN, s): key for s in steps})
-        self.bs = B.Bootstrapper(ev, BOOT_PARAMS["loge"], BOOT_LOGN - 1, BOOT_LOGN - 1, BOOT_PARAMS["L"], BOOT_SCALE,
+        self.bs = B.Bootstrapper(ev, BOOT_PARAMS["loge"], BOOT_LOGN - 1, BOOT_LOGN - 1, len(qs) - 2, BOOT_SCALE,
                                  25, 59, 2, 1, load_table())
         self.bs.generate_LT_coefficient_3()
         self.input = L.Ct(po.random_residues(rng, (2, 1, n), qs[:1]), BOOT_SCALE)
@@ -782,7 +810,7 @@ def bert_config():
     return {"workload": "bert_base_layer_n65536", "N": 1 << BERT_LOGN, "hidden": 768, "heads": 12, "ffn": 3072,
             "requests": [128, 32, 64], "lanes": "[128] | [32 + 64]", "token_slots_per_block": 256,
             "moduli_bits": "51 + 19x46 + 14x51 + special 51", "hamming_weight": 192, "scale": "2^46",
-            "weights": "N(0, 0.02)", "tokens": "N(0, 1)", "parallelism": "replicas",
+            "boot_shrink": 2, "weights": "N(0, 0.02)", "tokens": "N(0, 1)", "parallelism": "replicas",
             "l2": "keys (~110 GB), encoded weights (~60 GB) and activations far above L2, no flush"}
 
 
@@ -940,6 +968,7 @@ def run_bert_gpu(args, rank, world):
             "share_of_step": ntt_ms / instr_ms,
             "traffic": _ntt_traffic(ntt_limbs / max(1, ntt_calls)),
             "traffic_source": "ncu DRAM bytes per limb-NTT of the 51-bit NTT capture x limbs per launch",
+            "compute_bound": _butterfly_roof(ng, qs[1], ntt_limbs, ntt_ms, BERT_LOGN),
         },
         "e2e": {"value": e2e_s, "unit": "s per layer", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes},
@@ -949,7 +978,25 @@ def run_bert_gpu(args, rank, world):
                   "cached_plaintexts": layer.cached_plaintexts()},
         "clocks": clk.summary(),
         "gpu_launches": launches,
+        "cpu_baseline": cpu_bert_sample(os.cpu_count() or 1) if rank == 0 and world == 1 else None,
     }
+
+
+BERT_BOOTSTRAPS = 122   # per layer: Q/K/V 48, softmax sums 2, residuals 12 + 12, FFN hidden 48
+
+
+def cpu_bert_sample(threads: int):
+    """A lower bound of the layer on the oracle port: one full bootstrap on the
+    layer's chain, timed, times the layer's 122 bootstraps (projections,
+    attention, GELU and LayerNorm left out)."""
+    cb = CpuBootstrap(threads, BERT_BITS)
+    t = cb.bootstrap()
+    total = BERT_BOOTSTRAPS * t
+    return {"value": total, "unit": "s per layer", "cores": threads, "kind": "port",
+            "sample": f"one full-slot bootstrap_3 on the layer chain (51 + 19x46 + 14x51 + 51) with the oracle port "
+                      f"timed at {t:.1f} s on {threads} threads, times the layer's {BERT_BOOTSTRAPS} bootstraps: a "
+                      f"lower bound (the linear maps, attention, GELU and LayerNorm are not counted)"
+                      + _calibration_note()}
 
 
 # ----------------------------------------------------------------------------- GELU workload
@@ -1144,6 +1191,143 @@ def cpu_gelu_sample(workers: int = 1):
                       f"{t:.1f} s each ({wall:.1f} s wall)"}
 
 
+# ----------------------------------------------------------------------------- micro-benchmarks
+
+def run_keyswitch_gpu(args, rank, world):
+    """nexus_switch_key_batch at N=2^16 on the bootstrap chain: --ks-batch
+    ciphertexts at --ks-limbs limbs under one random key.  --steps 1 with
+    --warmup 0 is the single call a kernel profiler captures."""
+    import torch
+
+    import nexus_gb300 as ng
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = 1 << BOOT_LOGN
+    qs = ng.create_coeff_modulus(n, BOOT_BITS)
+    limbs, batch = args.ks_limbs, args.ks_batch
+    ctx = ng.Context(BOOT_LOGN, qs)
+    k = len(qs)
+    g = torch.Generator(device=dev).manual_seed(1)
+    qd = torch.tensor(qs, dtype=torch.int64, device=dev)
+
+    def rnd(lead, rows, primes):
+        x = torch.randint(0, 2 ** 62, tuple(lead) + (rows, n), device=dev, dtype=torch.int64, generator=g)
+        return x % primes.view(rows, 1)
+
+    key = rnd((k - 1, 2), k, qd)
+    cts, tg = rnd((batch, 2), limbs, qd[:limbs]), rnd((batch,), limbs, qd[:limbs])
+    for _ in range(args.warmup):
+        ctx.switch_key_batch(cts, tg, key)
+    torch.cuda.synchronize(dev)
+    l0 = ng.kernel_launches()
+    print(f"engine_launches_before_timed={l0}", file=sys.stderr, flush=True)
+    stream = torch.cuda.current_stream(dev)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        ctx.switch_key_batch(cts, tg, key)
+    t1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = t0.elapsed_time(t1) / max(1, args.steps)
+    return {"metric": "keyswitch_latency_n65536", "value": ms, "unit": "ms per batched call",
+            "ms_per_ciphertext": ms / batch, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": False, "dtype": "u64", "data": "uniform random residues and key",
+            "config": {"workload": f"keyswitch_n65536_l{limbs}_{batch}ct", "limbs": limbs, "batch": batch},
+            "gpu_launches": ng.kernel_launches() - l0}
+
+
+def run_stages_gpu(args, rank, world):
+    """The full-slot bootstrap at N=2^16 split into its stages (modulus raise,
+    CoeffToSlot, EvalMod on each half, SlotToCoeff), in the single-ciphertext
+    and lockstep (--boot-cts ciphertexts) forms: milliseconds per bootstrap per
+    stage (host clock around synchronised stage calls)."""
+    import numpy as np
+    import torch
+
+    import nexus_gb300 as ng
+    from nexus_gb300.operators import (BOOT_COEFFTOSLOT, BOOT_MODRAISE, BOOT_MODULAR_REDUCTION,
+                                       BOOT_SET_INITIAL_SCALE, BOOT_SLOTTOCOEFF, Bootstrapper, Ciphertext, Evaluator)
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = 1 << BOOT_LOGN
+    qs = ng.create_coeff_modulus(n, BOOT_BITS)
+    ctx = ng.Context(BOOT_LOGN, qs)
+    seed = _seal_seed(400 + rank)
+    sk = ctx.seal_keygen_secret(seed, 192)
+    ev = Evaluator(ctx, BOOT_SCALE, ctx.seal_keygen_relin(sk, seed))
+    bs = Bootstrapper(ev, **BOOT_PARAMS)
+    for st in bs.rotation_steps(BOOT_LOGN - 1):
+        e = ctx.galois_elt(st)
+        ev.add_galois_key(e, ctx.seal_keygen_galois(sk, e, seed))
+    bs.prepare_mod_polynomial()
+    bs.generate_LT_coefficient_3()
+    top = len(qs) - 1
+    rng = np.random.default_rng(1)
+    pt = torch.empty((top, n), dtype=torch.int64, device=dev)
+    ins = []
+    for i in range(BOOT_CTS):
+        ctx.encode(rng.uniform(-1, 1, n // 2), BOOT_SCALE, top, pt)
+        s_i = seed.copy()
+        s_i[7] ^= np.uint64(i)
+        ins.append(ctx.seal_encrypt_symmetric(sk, pt, top, s_i)[:, :1, :].contiguous())
+    q0 = float(qs[0])
+
+    def timed(f):
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        r = f()
+        torch.cuda.synchronize(dev)
+        return r, (time.perf_counter() - t) * 1e3
+
+    def single(x0):
+        x = Ciphertext.from_device(ctx, x0.clone(), BOOT_SCALE)
+        bs.stage(BOOT_SET_INITIAL_SCALE, x)
+        t = {}
+        _, t["modraise"] = timed(lambda: bs.stage(BOOT_MODRAISE, x))
+        x = Ciphertext.from_device(ctx, x.to_device(), q0)
+        (r1, r2), t["coefftoslot"] = timed(lambda: bs.stage(BOOT_COEFFTOSLOT, x))
+        (m1, _), t["evalmod_1"] = timed(lambda: bs.stage(BOOT_MODULAR_REDUCTION, r1))
+        (m2, _), t["evalmod_2"] = timed(lambda: bs.stage(BOOT_MODULAR_REDUCTION, r2))
+        _, t["slottocoeff"] = timed(lambda: bs.stage(BOOT_SLOTTOCOEFF, m1, m2))
+        return t
+
+    def lockstep():
+        xs = [Ciphertext.from_device(ctx, x.clone(), BOOT_SCALE) for x in ins]
+        bs.stage_batch(BOOT_SET_INITIAL_SCALE, xs)
+        t, c = {}, {}
+        _, t["modraise"] = timed(lambda: bs.stage_batch(BOOT_MODRAISE, xs))
+        xs = [Ciphertext.from_device(ctx, x.to_device(), q0) for x in xs]
+        skip = ng.kernel_launches()
+        (r1, r2), t["coefftoslot"] = timed(lambda: bs.stage_batch(BOOT_COEFFTOSLOT, xs))
+        c["coefftoslot"] = ng.kernel_launches() - skip
+        b = ng.kernel_launches()
+        (m1, _), t["evalmod_1"] = timed(lambda: bs.stage_batch(BOOT_MODULAR_REDUCTION, r1))
+        c["evalmod_1"] = ng.kernel_launches() - b
+        b = ng.kernel_launches()
+        (m2, _), t["evalmod_2"] = timed(lambda: bs.stage_batch(BOOT_MODULAR_REDUCTION, r2))
+        c["evalmod_2"] = ng.kernel_launches() - b
+        b = ng.kernel_launches()
+        _, t["slottocoeff"] = timed(lambda: bs.stage_batch(BOOT_SLOTTOCOEFF, m1, m2))
+        c["slottocoeff"] = ng.kernel_launches() - b
+        return t, c, skip
+
+    single(ins[0])          # the first use builds the plaintext and hoisting caches
+    lockstep()
+    ts = [single(ins[0]) for _ in range(max(1, args.steps))]
+    tl = [lockstep() for _ in range(max(1, args.steps))]
+    print(f"skip={tl[-1][2]} " + " ".join(f"{k}={v}" for k, v in tl[-1][1].items()), file=sys.stderr)
+    avg = lambda rows, k: statistics.mean(r[k] for r in rows)
+    keys = ["modraise", "coefftoslot", "evalmod_1", "evalmod_2", "slottocoeff"]
+    single_ms = {k: avg(ts, k) for k in keys}
+    lock_ms = {k: statistics.mean(r[0][k] for r in tl) / BOOT_CTS for k in keys}
+    return {"metric": "bootstrap_stage_latency_n65536", "value": sum(lock_ms.values()),
+            "unit": "ms per bootstrap (lockstep, sum of stages)", "n_gpus": world, "steps": args.steps,
+            "higher_is_better": False, "dtype": "u64", "data": "U(-1,1) slots, keys from a SEAL seed",
+            "config": {"workload": f"bootstrap_stages_n65536_{BOOT_CTS}ct"},
+            "single_ms_per_bootstrap": single_ms, "lockstep_ms_per_bootstrap": lock_ms,
+            "lockstep_launches_per_stage": tl[-1][1]}
+
+
 # ----------------------------------------------------------------------------- plumbing
 
 def barrier(world):
@@ -1171,7 +1355,10 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["nexus", "reference"], default="nexus")
-    ap.add_argument("--workload", choices=["bootstrap", "matmul", "ntt", "gelu", "bert"], default="bootstrap")
+    ap.add_argument("--workload", choices=["bootstrap", "matmul", "ntt", "gelu", "bert", "keyswitch", "stages"],
+                    default="bootstrap")
+    ap.add_argument("--ks-limbs", type=int, default=31, help="limbs of the keyswitch workload")
+    ap.add_argument("--ks-batch", type=int, default=4, help="ciphertexts per call of the keyswitch workload")
     ap.add_argument("--cpu-depth", type=int, default=7, help="expansion-subtree depth of the MatMul CPU sample")
     ap.add_argument("--mm-rows", type=int, default=128,
                     help="rows of the encrypted input (smaller values are for profiling captures only)")
@@ -1183,14 +1370,18 @@ def main():
     ap.add_argument("--ntt-cts", type=int, default=64,
                     help="ciphertexts per step (smaller values are for profiling captures only)")
     args = ap.parse_args()
-    args.warmup = max(3, args.warmup)
+    if args.workload not in ("keyswitch", "stages"):
+        args.warmup = max(3, args.warmup)   # the micro-benchmarks allow one cold call for a profiler
+    if args.workload == "keyswitch" and not 1 <= args.ks_limbs <= len(BOOT_BITS) - 1:
+        raise SystemExit(f"--ks-limbs must be in [1, {len(BOOT_BITS) - 1}]")
     NTT_CTS = args.ntt_cts
     global MM_ROWS, BOOT_CTS, NTT_BITS
     NTT_BITS = args.ntt_bits
     MM_ROWS = args.mm_rows
     BOOT_CTS = args.boot_cts
     if args.steps is None:
-        args.steps = {"bootstrap": 3, "matmul": 5, "gelu": 5, "bert": 2}.get(args.workload, 20)
+        args.steps = {"bootstrap": 3, "matmul": 5, "gelu": 5, "bert": 2, "keyswitch": 5, "stages": 2}.get(
+            args.workload, 20)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -1269,6 +1460,26 @@ def main():
         print(json.dumps(res), flush=True)
         return
 
+    if args.impl == "reference" and args.workload == "bert":
+        if rank != 0:
+            return
+        threads = max(1, os.cpu_count() or 1)
+        r = cpu_bert_sample(threads)
+        res = {"impl": "reference", "metric": "bert_base_layer_latency_n65536", "value": r["value"],
+               "unit": r["unit"], "n_gpus": world, "steps": 1, "steps_requested": args.steps, "warmup": 0,
+               "ms_per_step": r["value"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+               "dtype": "u64", "data": "synthetic (uniform random residues; the cost does not depend on them)",
+               "config": bert_config(), "cpu_baseline": r,
+               "e2e": {"value": r["value"], "unit": r["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(res), flush=True)
+        return
+
+    if args.impl == "reference" and args.workload in ("keyswitch", "stages"):
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "micro-benchmark of the engine only; the CPU "
+                              "reference is timed by the bootstrap, gelu, matmul, ntt and bert workloads"}))
+        return
+
     if args.impl == "reference":
         if rank != 0:
             return
@@ -1298,7 +1509,7 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
     run = {"bootstrap": run_boot_gpu, "matmul": run_mm_gpu, "ntt": run_ntt_gpu, "gelu": run_gelu_gpu,
-           "bert": run_bert_gpu}[args.workload]
+           "bert": run_bert_gpu, "keyswitch": run_keyswitch_gpu, "stages": run_stages_gpu}[args.workload]
     res = run(args, rank, world)
     if rank == 0:
         print(json.dumps(res), flush=True)

@@ -85,6 +85,18 @@ int nexus_ntt_inverse(nexus_context *ctx, uint64_t *d_data, size_t n_polys, int 
 int nexus_ntt_timing_begin(nexus_context *ctx);
 int nexus_ntt_timing_end(nexus_context *ctx, double *total_ms, uint64_t *calls, uint64_t *limbs);
 
+/*
+ * The NTT's compute ceiling on this GPU: butterflies per second of its own
+ * butterfly (mode 0 the forward Harvey butterfly, 1 the forward butterfly for
+ * primes below 2^52, 2 the inverse Gentleman-Sande butterfly), each thread
+ * running `rounds` rounds of four radix-2 stages over 16 register residues,
+ * blocks_per_sm CTAs of 256 threads per SM, no memory traffic in the loop;
+ * *ms receives one launch's duration.  Synchronous.  A measurement aid with
+ * no counterpart in the reference.
+ */
+int nexus_butterfly_rate(int mode, uint64_t q, int rounds, int blocks_per_sm, double *butterflies_per_s,
+                         double *ms);
+
 /* ------------------------------------------------------------------ */
 /* CKKS ciphertext arithmetic (NTT form, limbs = data primes 0..limbs-1) */
 /* ------------------------------------------------------------------ */
@@ -140,12 +152,15 @@ int nexus_switch_key_batch(nexus_context *ctx, uint64_t *d_ct, int batch, int li
  * allowed where they call).  Temporaries live in a fixed device array of
  * 2^21 uint64 words (16 MiB) inside the library, which every GPU that loads
  * the library holds until the process exits; requests needing more than
- * N*(limbs^2 + 6*limbs + 4) > 2^21 words are rejected with an error.  The
- * first call on a device looks up the array's address (cudaGetSymbolAddress)
- * with the context's device current; make that first call before any stream
- * capture.  All calls share the array, so calls whose work overlaps on the
- * GPU (different streams, no ordering) race; every word is written before it
- * is read, so no clearing is needed between calls.
+ * N*(limbs^2 + 6*limbs + 4) > 2^21 words are rejected with an error.  Every
+ * call looks up the array's address (cudaGetSymbolAddress, a host query) with
+ * the context's device current.  The first call on a device also loads the
+ * library's kernel modules (CUDA loads modules lazily), which allocates device
+ * memory once: make that first call, or one nexus_switch_key on the same
+ * device, before any stream capture or before the other runtime takes over
+ * the device's memory.  All calls share the array, so calls whose work
+ * overlaps on the GPU (different streams, no ordering) race; every word is
+ * written before it is read, so no clearing is needed between calls.
  * No counterpart in the reference: SEAL and Phantom allocate their key-switch
  * temporaries from a memory pool on every call.
  */

@@ -111,6 +111,18 @@ SIGNATURES = [
                                              C.POINTER(C.c_int)]),
     ("nexus_plain_op", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    ("nexus_butterfly_rate", C.c_int,
+     [C.c_int, C.c_uint64, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("nexus_bert_layer_create", C.c_int,
+     [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+      C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_void_p)]),
+    ("nexus_bert_layer_destroy", C.c_int, [C.c_void_p]),
+    ("nexus_bert_layer_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int), u64p]),
+    ("nexus_bert_layer_rotation_steps", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]),
+    ("nexus_bert_layer_forward", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    ("nexus_bert_layer_stage", C.c_int,
+     [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
 ]
 
 

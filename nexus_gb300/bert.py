@@ -33,7 +33,7 @@ class BertShape:
     T: int = 256
     # per lane, requests as (first token slot, tokens)
     lanes: list = field(default_factory=lambda: [[(0, 128)], [(0, 32), (64, 64)]])
-    boot_shrink: float = 8.0
+    boot_shrink: float = 2.0
 
     def blocks(self, slots: int) -> int:
         return slots // self.T

@@ -287,3 +287,14 @@ class Context:
 
 def kernel_launches() -> int:
     return int(lib().nexus_kernel_launches())
+
+
+def butterfly_rate(mode: int, q: int, rounds: int = 512, blocks_per_sm: int = 3) -> float:
+    """Butterflies per second of the NTT's own butterfly on this GPU (mode 0
+    forward, 1 forward for primes below 2^52, 2 inverse): the compute ceiling
+    of the transform (nexus_butterfly_rate)."""
+    out = C.c_double()
+    ms = C.c_double()
+    check(lib().nexus_butterfly_rate(int(mode), C.c_uint64(int(q)), int(rounds), int(blocks_per_sm), C.byref(out),
+                                     C.byref(ms)), "nexus_butterfly_rate")
+    return out.value

@@ -41,7 +41,10 @@
 // Every value about to be bootstrapped is first scaled down by boot_shrink
 // (folded into the preceding linear map or constant product) and its scale
 // divided by the same factor, so the refreshed ciphertext holds the value
-// itself while the bootstrap's sine approximation sees a small message.
+// itself while the bootstrap's EvalMod sees a smaller message: values that
+// are constant over many slots (the softmax row sums, for one) concentrate in
+// few coefficients and leave EvalMod's intervals otherwise.  The bootstrap's
+// own error grows with the factor (about 2e-4 times it at N = 2^16), hence 2.
 #pragma once
 #include <cstdint>
 #include <map>
@@ -62,7 +65,7 @@ struct BertShape {
     int T = 256;  // token slots per feature block
     // per lane, each request as (first token slot, tokens)
     std::vector<std::vector<std::pair<int, int>>> lanes;
-    double boot_shrink = 8.0;
+    double boot_shrink = 2.0;
 
     // derived by derive()
     int S = 0, NB = 0, H2 = 0, KB = 0, n_head = 0, n_hid = 0, n_ffn = 0, Lmax = 0, G = 0, Glt = 0;

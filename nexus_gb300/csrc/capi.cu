@@ -402,3 +402,16 @@ extern "C" int nexus_ntt_timing_end(nexus_context *ctx, double *total_ms, uint64
     if (limbs) *limbs = nl;
     return 0;
 }
+
+extern "C" int nexus_butterfly_rate(int mode, uint64_t q, int rounds, int blocks_per_sm, double *butterflies_per_s,
+                                    double *ms)
+{
+    static const char *fn = "nexus_butterfly_rate";
+    if (!butterflies_per_s) return fail(fn, "null argument");
+    try {
+        *butterflies_per_s = nexus::butterfly_rate(mode, q, rounds, blocks_per_sm, ms);
+    } catch (const std::exception &e) {
+        return fail(fn, e.what());
+    }
+    return 0;
+}

@@ -11,7 +11,6 @@
 //   4. ModDown with rounding: ct[k][i] += (P[k][i] - NTT_i(((INTT_p(P[k][p]) + p/2)
 //      mod p) - p/2)) * p^{-1} mod q_i.
 #include <cstdint>
-#include <mutex>
 #include <stdexcept>
 #include <string>
 
@@ -612,25 +611,16 @@ namespace {
 constexpr size_t kNoAllocWords = size_t(1) << 21;
 static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocWords];
 
-std::mutex g_noalloc_mu;
-uint64_t *g_noalloc_addr[64] = {};
-
-// Device address of g_noalloc_scratch on the current device, looked up once
-// per device (with that device current) and cached.
+// Device address of g_noalloc_scratch in the current context.  It is looked
+// up on every call (a host-side query, no allocation): an address cached once
+// per device would go stale if the module were reloaded, for instance after
+// cudaDeviceReset.
 uint64_t *noalloc_scratch_on_current_device()
 {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) throw std::runtime_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= 64) throw std::runtime_error("device index out of range");
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) throw std::runtime_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_noalloc_addr[dev] = static_cast<uint64_t *>(p);
-    }
-    return g_noalloc_addr[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) throw std::runtime_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    return static_cast<uint64_t *>(p);
 }
 
 }  // namespace
@@ -664,8 +654,11 @@ extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l,
         if (cudaGetDevice(&dev) != cudaSuccess || dev != c.device)
             throw std::runtime_error("the context's device must be current");
         uint64_t *t = noalloc_scratch_on_current_device();
-        // same layout and kernel sequence as switch_key(); every scratch word
-        // is written before it is read, so nothing needs clearing
+        // SEAL's key switch step by step (INTT of the target, ModUp spread, a
+        // forward NTT of every limb of every digit, inner product, ModDown),
+        // the unfused sequence whose words switch_key() reproduces with its
+        // fused kernels; every scratch word is written before it is read, so
+        // nothing needs clearing
         cudaStream_t s = (cudaStream_t)stream;
         const int sp = c.k - 1;
         uint64_t *D = t + (size_t)l * N;

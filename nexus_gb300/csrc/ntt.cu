@@ -19,6 +19,7 @@
 // Shoup butterflies (values in [0,4q) forward, [0,2q) inverse).
 #include <cstdio>
 #include <stdexcept>
+#include <vector>
 
 #include "context.h"
 #include "ntt.h"
@@ -516,6 +517,111 @@ void ntt_forward(const Context &c, uint64_t *d, size_t n_polys, int limb_begin, 
 void ntt_inverse(const Context &c, uint64_t *d, size_t n_polys, int limb_begin, int limb_end, cudaStream_t s)
 {
     ntt_inverse(c, d, n_polys, LimbMap{limb_end - limb_begin, limb_begin, -1}, s);
+}
+
+// ------------------------------------------------------------------ butterfly rate
+
+namespace {
+
+// The compute ceiling of the butterflies above: every thread runs `rounds`
+// rounds of the four radix-2 stages over its 16 register residues (32
+// butterflies a round) with per-stage twiddles in registers, no memory
+// traffic in the loop.  mode 0: ct_bfly, 1: ct_bfly_small, 2: gs_bfly.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_bfly_rate(const ulonglong2 *__restrict__ W, const uint64_t *__restrict__ in,
+                                                        uint64_t *out, uint64_t q, int rounds)
+{
+    const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+    uint64_t x[kE];
+#pragma unroll
+    for (int k = 0; k < kE; ++k) x[k] = in[(t * kE + k) & 1023];
+    ulonglong2 w[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) w[s] = W[(threadIdx.x + 37 * s) & 255];
+    const uint64_t q2 = q << 1;
+    for (int r = 0; r < rounds; ++r) {
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const int h = 8 >> s;
+#pragma unroll
+            for (int k = 0; k < kE; ++k)
+                if ((k & h) == 0) {
+                    if (MODE == 0) ct_bfly(x[k], x[k + h], w[s], q, q2);
+                    else if (MODE == 1) ct_bfly_small(x[k], x[k + h], w[s], q, q2 << 1);
+                    else gs_bfly(x[k], x[k + h], w[s], q, q2);
+                }
+        }
+    }
+    uint64_t acc = 0;
+#pragma unroll
+    for (int k = 0; k < kE; ++k) acc ^= x[k];
+    out[t] = acc;
+}
+
+}  // namespace
+
+double butterfly_rate(int mode, uint64_t q, int rounds, int blocks_per_sm, double *ms_out)
+{
+    if (mode < 0 || mode > 2) throw std::invalid_argument("mode must be 0, 1 or 2");
+    if (q < 3 || q >= (1ull << 61) || rounds < 1 || blocks_per_sm < 1) throw std::invalid_argument("bad arguments");
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+        throw std::runtime_error("device query failed");
+    const unsigned blocks = (unsigned)(sms * blocks_per_sm);
+    std::vector<ulonglong2> hw(256);
+    std::vector<uint64_t> hin(1024);
+    uint64_t st = 0x9E3779B97F4A7C15ull;
+    auto next = [&]() {
+        st ^= st << 13;
+        st ^= st >> 7;
+        st ^= st << 17;
+        return st;
+    };
+    for (auto &w : hw) {
+        const uint64_t v = next() % q;
+        w.x = v;
+        w.y = (uint64_t)(((unsigned __int128)v << 64) / q);
+    }
+    for (auto &v : hin) v = next() % q;
+    ulonglong2 *dW = nullptr;
+    uint64_t *din = nullptr, *dout = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto release = [&]() {
+        cudaFree(dW);
+        cudaFree(din);
+        cudaFree(dout);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    if (cudaMalloc(&dW, 256 * sizeof(ulonglong2)) != cudaSuccess || cudaMalloc(&din, 1024 * 8) != cudaSuccess ||
+        cudaMalloc(&dout, (size_t)blocks * kThreads * 8) != cudaSuccess) {
+        release();
+        throw std::runtime_error("allocation failed");
+    }
+    cudaMemcpy(dW, hw.data(), 256 * sizeof(ulonglong2), cudaMemcpyHostToDevice);
+    cudaMemcpy(din, hin.data(), 1024 * 8, cudaMemcpyHostToDevice);
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    auto launch = [&]() {
+        if (mode == 0) k_bfly_rate<0><<<blocks, kThreads>>>(dW, din, dout, q, rounds);
+        else if (mode == 1) k_bfly_rate<1><<<blocks, kThreads>>>(dW, din, dout, q, rounds);
+        else k_bfly_rate<2><<<blocks, kThreads>>>(dW, din, dout, q, rounds);
+        NEXUS_LAUNCHED();
+    };
+    launch();  // warm-up
+    cudaEventRecord(e0);
+    const int reps = 5;
+    for (int i = 0; i < reps; ++i) launch();
+    cudaEventRecord(e1);
+    cudaError_t err = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    release();
+    if (err != cudaSuccess) throw std::runtime_error(cudaGetErrorString(err));
+    const double per = ms / reps;
+    if (ms_out) *ms_out = per;
+    return (double)blocks * kThreads * rounds * 32.0 / (per * 1e-3);
 }
 
 }  // namespace nexus

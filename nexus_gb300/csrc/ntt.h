@@ -67,4 +67,10 @@ void ntt_inverse(const Context &c, uint64_t *data, size_t n_polys, LimbMap lm, c
 void ntt_forward(const Context &c, uint64_t *data, size_t n_polys, int limb_begin, int limb_end, cudaStream_t s);
 void ntt_inverse(const Context &c, uint64_t *data, size_t n_polys, int limb_begin, int limb_end, cudaStream_t s);
 
+// Butterflies per second of the NTT's own butterfly (mode 0: forward, 1:
+// forward for primes below 2^52, 2: inverse) on register data over the whole
+// GPU: the compute ceiling of the transform.  Synchronous; *ms receives the
+// duration of one launch.
+double butterfly_rate(int mode, uint64_t q, int rounds, int blocks_per_sm, double *ms);
+
 }  // namespace nexus

@@ -2,7 +2,7 @@
 words at every stage of the encrypted BERT encoder layer (oracle/bert.py) at
 a reduced size: N = 2^13, 32 token slots per feature block, hidden 64 =
 2 heads x 32, FFN 128, two lanes with requests of 16 | 4 + 8 tokens, on
-the bootstrap chain 51 + 19x46 + 14x51 + special 51 with the sparse secret
+the chain 51 + 19x46 + 14x51 + special 51 with the sparse secret
 (h = 192).  Keys and encryptions come from the real SEAL-4.1-bs with one
 seeded Blake2xbPRNG factory, so the engine can make them again on the GPU
 from the seed (tests/test_bert_gpu.py).
@@ -38,7 +38,7 @@ OUT = Path(__file__).parent / "bert_digests.json"
 CASE = dict(log_n=13, bits=[51] + [46] * 19 + [51] * 14 + [51], seed=seed8(500), hamming_weight=192,
             scale_log2=46, loge=10, boundary_K=25, sin_cos_deg=59, scale_factor=2, inverse_deg=1,
             hidden=64, heads=2, head_dim=32, ffn=128, T=32, lanes=[[[0, 16]], [[0, 4], [8, 8]]],
-            boot_shrink=8.0, weight_seed=7, token_seed=8)
+            boot_shrink=2.0, weight_seed=7, token_seed=8)
 
 
 def digest(a) -> str:

@@ -64,7 +64,9 @@ def test_lockstep_and_hoisting_entry_points_reject_null_arguments_without_gpu():
         assert msg.startswith(name.encode()) and word in msg, (name, msg)
 
 
-def test_probe_rejects_a_level_outside_the_chain_without_gpu():
-    from nexus_gb300 import probe
-    with pytest.raises(SystemExit):
-        probe.main(["keyswitch", "--limbs", "40", "--once"])
+def test_keyswitch_workload_rejects_a_level_outside_the_chain_without_gpu():
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--workload", "keyswitch", "--ks-limbs", "40"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0 and "--ks-limbs" in r.stderr

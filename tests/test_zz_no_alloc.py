@@ -33,11 +33,13 @@ def _case(rng, qs, n, limbs):
     return ct, tgt, key
 
 
-def test_noalloc_matches_switch_key_twice(cuda):
+@pytest.mark.parametrize("bits", [[60, 40, 40, 40, 40, 50, 60],    # the 64-bit product paths
+                                  [50, 40, 40, 40, 40, 46, 50]])   # every prime < 2^52: the split paths
+def test_noalloc_matches_switch_key_twice(cuda, bits):
     import torch
     from nexus_gb300 import Context, check
     log_n, n = 13, 1 << 13
-    qs = po.create_coeff_modulus(n, [60, 40, 40, 40, 40, 50, 60])
+    qs = po.create_coeff_modulus(n, bits)
     ctx = Context(log_n, qs)
     rng = np.random.default_rng(2025)
     f = _noalloc()
