@@ -908,6 +908,13 @@ def run_bert_gpu(args, rank, world):
     instr_ms = e0.elapsed_time(e1)
     lock_words = [r.to_numpy() for r in res[:layer.n_hid]]
     del res
+    # per-block device time of one lockstep forward
+    layer.set_timing(True)
+    res = step()
+    torch.cuda.synchronize(dev)
+    blocks_lock = layer.stage_times(lockstep=True)
+    layer.set_timing(False)
+    del res
 
     # end to end: the encrypted inputs from pinned host memory, the layer, the
     # outputs back to the host
@@ -929,11 +936,15 @@ def run_bert_gpu(args, rank, world):
     # the plain form: each lane on its own, one ciphertext per operation
     p0 = torch.cuda.Event(enable_timing=True)
     p1 = torch.cuda.Event(enable_timing=True)
+    layer.set_timing(True)
     p0.record(stream)
     res = layer.forward(x, lockstep=False)
     p1.record(stream)
     torch.cuda.synchronize(dev)
     plain_ms = p0.elapsed_time(p1)
+    blocks_plain = [layer.stage_times(lockstep=False, lane=l) for l in range(layer.n_lanes)]
+    layer.set_timing(False)
+    blocks_plain = {k: sum(b[k] for b in blocks_plain) for k in blocks_plain[0]}
     same = all(np.array_equal(a.to_numpy(), b) for a, b in zip(res[:layer.n_hid], lock_words))
     del res
 
@@ -974,6 +985,7 @@ def run_bert_gpu(args, rank, world):
                 "d2h_bytes_per_step": out_bytes},
         "plain_single_ct_form": {"value": plain_ms / 1e3, "unit": "s per layer",
                                  "lockstep_speedup": plain_ms / step_ms, "words_equal_lockstep": bool(same)},
+        "blocks_ms": {"lockstep": blocks_lock, "plain": blocks_plain},
         "setup": {"first_call_s": setup_s, "galois_keys": len(all_steps),
                   "cached_plaintexts": layer.cached_plaintexts()},
         "clocks": clk.summary(),

@@ -617,6 +617,13 @@ int nexus_bert_layer_forward(nexus_bert_layer *layer, int lockstep, nexus_cipher
 #define NEXUS_BERT_BOOTSTRAP 3
 int nexus_bert_layer_stage(nexus_bert_layer *layer, int lockstep, int stage, int which, nexus_ciphertext *const *in,
                            int count_in, nexus_ciphertext *const *out, int count_out);
+/* With timing on, forward records a CUDA event after each of its blocks;
+ * stage_times returns the device time of each block of the last forward
+ * (lockstep form, or lane `lane` of the single form) in ms[], their names in
+ * `names` separated by newlines; ms = NULL only counts them. */
+int nexus_bert_layer_set_timing(nexus_bert_layer *layer, int enable);
+int nexus_bert_layer_stage_times(nexus_bert_layer *layer, int lockstep, int lane, double *ms, char *names,
+                                 size_t names_capacity, int *count, int capacity);
 
 /* ------------------------------------------------------------------------
  * SEAL byte format of a CKKS ciphertext (host-side, compr_mode_type::none)

@@ -239,6 +239,20 @@ class BertLayer:
         check(lib().nexus_bert_layer_info(self._h, None, None, None, None, C.byref(cached)), "nexus_bert_layer_info")
         return cached.value
 
+    def set_timing(self, enable: bool) -> None:
+        check(lib().nexus_bert_layer_set_timing(self._h, 1 if enable else 0), "nexus_bert_layer_set_timing")
+
+    def stage_times(self, lockstep: bool = True, lane: int = 0) -> dict:
+        """Device ms of each block of the last forward with timing on."""
+        n = C.c_int()
+        check(lib().nexus_bert_layer_stage_times(self._h, int(lockstep), lane, None, None, 0, C.byref(n), 0),
+              "nexus_bert_layer_stage_times")
+        ms = (C.c_double * max(1, n.value))()
+        names = C.create_string_buffer(4096)
+        check(lib().nexus_bert_layer_stage_times(self._h, int(lockstep), lane, ms, names, 4096, C.byref(n), n.value),
+              "nexus_bert_layer_stage_times")
+        return dict(zip(names.value.decode().split("\n"), ms[:n.value]))
+
     def _handles(self, cts):
         return (C.c_void_p * len(cts))(*[c.handle.value for c in cts])
 

@@ -703,6 +703,7 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
     for (auto &c : x_in)
         if (batch_of(c) != (int)lanes_.size()) throw std::invalid_argument("forward: batch does not match the lanes");
     if (x_in[0].limbs() < 3) throw std::invalid_argument("forward: the input needs at least 3 limbs");
+    begin_marks();
     // the residual branch: x / boot_shrink at one limb
     std::vector<CT> x_res = x_in;
     shrink_for_bootstrap(x_res);
@@ -714,6 +715,7 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
     project(x2, LT_Q, q);
     project(x2, LT_K, k);
     project(x2, LT_V, v);
+    mark("qkv projections");
     {
         std::vector<CT> all;
         for (auto *t : {&q, &k, &v})
@@ -726,16 +728,21 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
             v[i] = std::move(all[2 * nh + i]);
         }
     }
+    mark("qkv bootstraps");
     std::vector<CT> o, a;
     attention(q, k, v, o);
+    mark("attention");
     project(o, LT_O, a);
     // residual + LayerNorm
     for (int c = 0; c < sh_.n_hid; ++c) {
         a[c].scale() = x_res[c].scale();
         ev.add_inplace(a[c], x_res[c]);
     }
+    mark("output projection + residual");
     bootstrap_all(a);
+    mark("residual bootstraps 1");
     layer_norm(a);
+    mark("layer norm 1");
     // FFN
     std::vector<CT> y_res = a;
     shrink_for_bootstrap(y_res);
@@ -743,7 +750,9 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
     for (auto &c : a) ev.mod_switch_to_inplace(c, 2);
     std::vector<CT> h, f;
     project(a, LT_1, h);
+    mark("ffn1 projection");
     bootstrap_all(h);
+    mark("ffn hidden bootstraps");
     {
         GeLUEvaluatorT<EV, CT> gelu(ck_);
         std::vector<CT *> p;
@@ -754,14 +763,56 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
             c = std::move(r);
         });
     }
+    mark("gelu");
     project(h, LT_2, f);
     for (int c = 0; c < sh_.n_hid; ++c) {
         f[c].scale() = y_res[c].scale();
         ev.add_inplace(f[c], y_res[c]);
     }
+    mark("ffn2 projection + residual");
     bootstrap_all(f);
+    mark("residual bootstraps 2");
     layer_norm(f);
+    mark("layer norm 2");
     out = std::move(f);
+}
+
+template <class EV, class CT>
+void BertLayerT<EV, CT>::begin_marks()
+{
+    for (auto &m : marks_) cudaEventDestroy(m.second);
+    marks_.clear();
+    if (timing) mark("start");
+}
+
+template <class EV, class CT>
+void BertLayerT<EV, CT>::mark(const char *name)
+{
+    if (!timing) return;
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) throw std::runtime_error("cudaEventCreate failed");
+    cudaEventRecord(e, ev_->stream());
+    marks_.emplace_back(name, e);
+}
+
+template <class EV, class CT>
+std::vector<std::pair<std::string, double>> BertLayerT<EV, CT>::stage_times()
+{
+    std::vector<std::pair<std::string, double>> r;
+    for (size_t i = 1; i < marks_.size(); ++i) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(marks_[i].second) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, marks_[i - 1].second, marks_[i].second) != cudaSuccess)
+            throw std::runtime_error("event timing failed");
+        r.emplace_back(marks_[i].first, ms);
+    }
+    return r;
+}
+
+template <class EV, class CT>
+BertLayerT<EV, CT>::~BertLayerT()
+{
+    for (auto &m : marks_) cudaEventDestroy(m.second);
 }
 
 template class BertLayerT<Evaluator, Ciphertext>;

@@ -49,6 +49,7 @@
 #include <cstdint>
 #include <map>
 #include <memory>
+#include <string>
 #include <tuple>
 #include <utility>
 #include <vector>
@@ -109,6 +110,15 @@ public:
     void layer_norm(std::vector<CT> &x);
     void bootstrap_all(std::vector<CT> &cts);
 
+    ~BertLayerT();
+    BertLayerT(const BertLayerT &) = delete;
+    BertLayerT &operator=(const BertLayerT &) = delete;
+
+    // when set, forward() records a CUDA event after each of its blocks;
+    // stage_times() then gives each block's device time (ms) in order
+    bool timing = false;
+    std::vector<std::pair<std::string, double>> stage_times();
+
     enum { LT_Q = 0, LT_K, LT_V, LT_O, LT_1, LT_2, LT_COUNT };
     double delta() const { return delta_; }
     size_t cached_plaintexts() const { return pt_->count(); }
@@ -131,6 +141,8 @@ private:
     const Plaintext &bias_plain(int which, int ct, int limbs, double scale);
     void masks(int delta, int kind, int limbs, double scale, std::vector<const Plaintext *> &out);
     void shrink_for_bootstrap(std::vector<CT> &cts);
+    void begin_marks();
+    void mark(const char *name);
     void exact_scale_const(CT &ct, double value, double target_scale);
 
     EV *ev_;
@@ -141,6 +153,7 @@ private:
     std::vector<int> lanes_;
     double delta_;
     std::shared_ptr<BertPlaintexts> pt_;
+    std::vector<std::pair<std::string, cudaEvent_t>> marks_;
 };
 
 using BertLayer = BertLayerT<Evaluator, Ciphertext>;

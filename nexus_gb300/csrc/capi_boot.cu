@@ -1,4 +1,5 @@
 // C ABI of the bootstrapper (declared in include/nexus_gb300.h).
+#include <cstring>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -353,6 +354,7 @@ struct nexus_bert_layer {
     std::shared_ptr<BertPlaintexts> plain;
     std::vector<std::unique_ptr<BertLayer>> single;  // one per lane
     std::unique_ptr<BatchBertLayer> lockstep;        // every lane, built on first use
+    bool timing = false;
 };
 
 extern "C" int nexus_bert_layer_create(nexus_bootstrapper *bs, int hidden, int heads, int head_dim, int ffn, int T,
@@ -449,6 +451,7 @@ BatchBertLayer &bert_lockstep(nexus_bert_layer *L)
         std::vector<int> lanes;
         for (size_t l = 0; l < L->shape.lanes.size(); ++l) lanes.push_back((int)l);
         L->lockstep.reset(new BatchBertLayer(*L->bs->bev, BB, L->shape, L->w, lanes, L->plain));
+        L->lockstep->timing = L->timing;
     }
     return *L->lockstep;
 }
@@ -574,5 +577,44 @@ extern "C" int nexus_bert_layer_stage(nexus_bert_layer *layer, int lockstep, int
         default:
             throw std::invalid_argument("unknown stage");
         }
+    });
+}
+
+extern "C" int nexus_bert_layer_set_timing(nexus_bert_layer *layer, int enable)
+{
+    if (!layer) return fail("nexus_bert_layer_set_timing", "null argument");
+    for (auto &l : layer->single) l->timing = enable != 0;
+    if (layer->lockstep) layer->lockstep->timing = enable != 0;
+    layer->timing = enable != 0;
+    return 0;
+}
+
+extern "C" int nexus_bert_layer_stage_times(nexus_bert_layer *layer, int lockstep, int lane, double *ms, char *names,
+                                            size_t names_capacity, int *count, int capacity)
+{
+    static const char *fn = "nexus_bert_layer_stage_times";
+    if (!layer || !count) return fail(fn, "null argument");
+    return guarded(fn, [&] {
+        std::vector<std::pair<std::string, double>> t;
+        if (lockstep) {
+            if (!layer->lockstep) throw std::logic_error("the lockstep form has not run");
+            t = layer->lockstep->stage_times();
+        } else {
+            if (lane < 0 || lane >= (int)layer->single.size()) throw std::invalid_argument("lane out of range");
+            t = layer->single[lane]->stage_times();
+        }
+        if (ms) {
+            if ((int)t.size() > capacity) throw std::length_error("capacity too small");
+            std::string joined;
+            for (size_t i = 0; i < t.size(); ++i) {
+                ms[i] = t[i].second;
+                joined += t[i].first + "\n";
+            }
+            if (names) {
+                if (joined.size() + 1 > names_capacity) throw std::length_error("names capacity too small");
+                std::memcpy(names, joined.c_str(), joined.size() + 1);
+            }
+        }
+        *count = (int)t.size();
     });
 }
