@@ -1,0 +1,80 @@
+"""Host-side pieces of the encrypted BERT layer (no GPU): the client packing
+round trip, the FP64 reference's NEXUS approximations against the exact
+functions on their domains, the oracle's packing restatement against the
+engine package's, and argument rejection of the layer's C ABI."""
+import ctypes
+
+import numpy as np
+
+from nexus_gb300 import bert as NB
+
+
+def _small_shape():
+    return NB.BertShape(hidden=64, heads=2, head_dim=32, ffn=128, T=32, lanes=[[(0, 16)], [(0, 4), (8, 8)]])
+
+
+def test_pack_unpack_round_trip():
+    sh = _small_shape()
+    slots = 4096
+    rng = np.random.default_rng(0)
+    for lane, reqs in enumerate(sh.lanes):
+        toks = [rng.normal(size=(L, sh.hidden)) for (_, L) in reqs]
+        vecs = NB.pack_lane(sh, slots, lane, toks)
+        assert vecs.shape == (sh.n_hid(slots), slots)
+        back = NB.unpack_lane(sh, slots, lane, vecs)
+        for a, b in zip(toks, back):
+            assert np.array_equal(a, b)
+        # the second token copy holds the same values
+        for (o, L), x in zip(reqs, toks):
+            for f in (0, sh.hidden - 1):
+                c, j = divmod(f, slots // sh.T)
+                assert np.array_equal(vecs[c, j * sh.T + o + L:j * sh.T + o + 2 * L], x[:, f])
+
+
+def test_nexus_approximations_on_their_domains():
+    x = np.linspace(-2.0, 0.0, 50)
+    assert np.max(np.abs(NB.nexus_exp(x) - np.exp(x))) < 2e-2
+    y = np.linspace(0.2, 1.8, 50)
+    assert np.max(np.abs(NB.nexus_inverse(y) - 1.0 / y) / (1.0 / y)) < 0.2
+    z = np.linspace(5.0, 500.0, 50)
+    assert np.max(np.abs(NB.nexus_invert_sqrt(z) - 1.0 / np.sqrt(z)) * np.sqrt(z)) < 1e-2
+    g = np.linspace(-4.0, 4.0, 81)
+    exact = 0.5 * g * (1.0 + np.tanh(np.sqrt(2.0 / np.pi) * (g + 0.044715 * g ** 3)))
+    assert np.max(np.abs(NB.nexus_gelu(g) - exact)) < 2e-2
+
+
+def test_layer_reference_shapes_and_exact_softmax_rows():
+    sh = _small_shape()
+    w = NB.random_weights(sh, np.random.default_rng(1))
+    toks = [np.random.default_rng(2).normal(size=(6, sh.hidden))]
+    approx = NB.layer_reference(sh, w, toks)
+    exact = NB.layer_reference(sh, w, toks, exact=True)
+    assert approx[0].shape == exact[0].shape == (6, sh.hidden)
+    assert np.all(np.isfinite(approx[0]))
+    # the exact layer's outputs are LayerNorm'd: unit mean square per token
+    assert np.allclose(np.mean(exact[0] ** 2, axis=1), 1.0)
+
+
+def test_oracle_restates_the_rotation_steps():
+    from oracle import bert as OB
+    sh = _small_shape()
+    osh = OB.Shape(4096, sh.hidden, sh.heads, sh.head_dim, sh.ffn, sh.T, sh.lanes, sh.boot_shrink)
+    steps = osh.rotation_steps()
+    assert len(steps) == len(set(steps)) and all(0 < s < 4096 for s in steps)
+    # baby steps of the block transforms, the attention's token shifts, the folds
+    assert sh.T in steps and 1 in steps and (osh.H2 * sh.T) in steps
+
+
+def test_layer_abi_rejects_null_arguments_without_gpu():
+    from nexus_gb300 import _lib
+    lib = _lib.lib()
+    out = ctypes.c_void_p()
+    one = (ctypes.c_int * 1)(1)
+    req = (ctypes.c_int * 2)(0, 4)
+    assert lib.nexus_bert_layer_create(None, 64, 2, 32, 128, 32, 1, one, req, ctypes.c_double(2.0), None,
+                                       ctypes.byref(out)) != 0
+    assert lib.nexus_last_error().startswith(b"nexus_bert_layer_create") and b"null" in lib.nexus_last_error()
+    assert lib.nexus_bert_layer_forward(None, 1, None, None) != 0
+    assert lib.nexus_bert_layer_stage(None, 1, 0, 0, None, 0, None, 0) != 0
+    n = ctypes.c_int()
+    assert lib.nexus_bert_layer_rotation_steps(None, None, ctypes.byref(n), 0) != 0
