@@ -593,6 +593,8 @@ def run_boot_gpu(args, rank, world):
         ev.add_galois_key(e, ctx.seal_keygen_galois(sk, e, seed))
     bs.prepare_mod_polynomial()
     bs.generate_LT_coefficient_3()
+    # launch parameters chosen by the autotuner at the bootstrap's top key-switch shape
+    tuning = ctx.autotune(len(qs) - 1, BOOT_CTS)
     top = len(qs) - 1
     rng = np.random.default_rng(4096 + rank)
     vals, inputs, host_in = [], [], []
@@ -707,7 +709,7 @@ def run_boot_gpu(args, rank, world):
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic: slots ~ U(-1,1), seeded; keys and encryptions from a SEAL seed (sparse secret h=192)",
-        "config": boot_config(len(steps)),
+        "config": dict(boot_config(len(steps)), tuning=tuning),
         "parity": parity,
         "accuracy": {"max_abs_err_vs_input": err, "precision_bits": -float(np.log2(err)),
                      "output_limbs": out_limbs},
@@ -840,6 +842,7 @@ def run_bert_gpu(args, rank, world):
     bs.prepare_mod_polynomial()
     bs.generate_LT_coefficient_3()
     layer = NB.BertLayer(bs, shape, w)
+    tuning = ctx.autotune(20, 16)
     all_steps = steps + [s for s in layer.rotation_steps() if s not in steps]
     for s in all_steps:
         e = ctx.galois_elt(s)
@@ -966,7 +969,7 @@ def run_bert_gpu(args, rank, world):
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic: weights ~ N(0,0.02), tokens ~ N(0,1), seeded; keys and encryptions from a SEAL seed",
-        "config": bert_config(),
+        "config": dict(bert_config(), tuning=tuning),
         "throughput": {"value": world * 224 / (step_ms / 1e3), "unit": "tokens/s"},
         "accuracy": {"max_abs_err_vs_fp64_same_approx": max(errs), "mean_abs_err_vs_fp64_same_approx":
                      float(np.mean(means)), "max_abs_err_vs_fp64_exact": max(errs_exact),

@@ -97,6 +97,24 @@ int nexus_ntt_timing_end(nexus_context *ctx, double *total_ms, uint64_t *calls, 
 int nexus_butterfly_rate(int mode, uint64_t q, int rounds, int blocks_per_sm, double *butterflies_per_s,
                          double *ms);
 
+/*
+ * Autotuner of the context's launch parameters: the L2 prefetch distance of
+ * the NTT passes (in residency waves of 3 CTAs per SM, 0 = none; candidates
+ * 0-4) and the grid of the key inner product (CTAs per SM of its grid-stride
+ * loop, 0 = one CTA per 512 coefficients; candidates 0, 4, 8, 16).  It times
+ * a batched key switch of `batch` ciphertexts at `limbs` limbs on uniform
+ * random residues for every pair (one warm-up, then `reps` calls), keeps the
+ * fastest in the context and returns it with its milliseconds per call.
+ * Synchronous; allocates a key and the ciphertexts for the trial and frees
+ * them.  The parameters never change a result word.  set/get read or write
+ * them directly.  No counterpart in the reference (Phantom's launch
+ * constants are fixed, cuda/thirdparty/phantom-fhe/include/common.h:22-32).
+ */
+int nexus_autotune(nexus_context *ctx, int limbs, int batch, int reps, int *ntt_prefetch_waves,
+                   int *ks_inner_ctas_per_sm, double *best_ms);
+int nexus_set_tuning(nexus_context *ctx, int ntt_prefetch_waves, int ks_inner_ctas_per_sm);
+int nexus_get_tuning(const nexus_context *ctx, int *ntt_prefetch_waves, int *ks_inner_ctas_per_sm);
+
 /* ------------------------------------------------------------------ */
 /* CKKS ciphertext arithmetic (NTT form, limbs = data primes 0..limbs-1) */
 /* ------------------------------------------------------------------ */

@@ -111,6 +111,10 @@ SIGNATURES = [
                                              C.POINTER(C.c_int)]),
     ("nexus_plain_op", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    ("nexus_autotune", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_double)]),
+    ("nexus_set_tuning", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    ("nexus_get_tuning", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("nexus_butterfly_rate", C.c_int,
      [C.c_int, C.c_uint64, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("nexus_bert_layer_create", C.c_int,

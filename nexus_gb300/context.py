@@ -128,6 +128,22 @@ class Context:
         check(lib().nexus_apply_galois(self._h, ct.data_ptr(), ct.shape[1], int(elt), key.data_ptr(),
                                        out.data_ptr(), _stream_ptr(stream)), "nexus_apply_galois")
 
+    def autotune(self, limbs: int, batch: int, reps: int = 3) -> dict:
+        """Choose the launch parameters by timing a batched key switch at this
+        shape (nexus_autotune); returns the choice and its ms per call."""
+        w, g, ms = C.c_int(), C.c_int(), C.c_double()
+        check(lib().nexus_autotune(self._h, int(limbs), int(batch), int(reps), C.byref(w), C.byref(g), C.byref(ms)),
+              "nexus_autotune")
+        return {"ntt_prefetch_waves": w.value, "ks_inner_ctas_per_sm": g.value, "ms_per_call": ms.value}
+
+    def set_tuning(self, ntt_prefetch_waves: int, ks_inner_ctas_per_sm: int) -> None:
+        check(lib().nexus_set_tuning(self._h, int(ntt_prefetch_waves), int(ks_inner_ctas_per_sm)), "nexus_set_tuning")
+
+    def tuning(self) -> dict:
+        w, g = C.c_int(), C.c_int()
+        check(lib().nexus_get_tuning(self._h, C.byref(w), C.byref(g)), "nexus_get_tuning")
+        return {"ntt_prefetch_waves": w.value, "ks_inner_ctas_per_sm": g.value}
+
     def galois_elt(self, step: int) -> int:
         e = C.c_uint32()
         check(lib().nexus_galois_elt_from_step(self.log_n, int(step), C.byref(e)), "galois_elt")

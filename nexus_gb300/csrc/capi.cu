@@ -403,6 +403,41 @@ extern "C" int nexus_ntt_timing_end(nexus_context *ctx, double *total_ms, uint64
     return 0;
 }
 
+extern "C" int nexus_autotune(nexus_context *ctx, int limbs, int batch, int reps, int *ntt_prefetch_waves,
+                              int *ks_inner_ctas_per_sm, double *best_ms)
+{
+    static const char *fn = "nexus_autotune";
+    if (!ctx) return fail(fn, "null context");
+    try {
+        const double ms = nexus::autotune_keyswitch(ctx->c, limbs, batch, nullptr, reps < 1 ? 3 : reps);
+        if (best_ms) *best_ms = ms;
+    } catch (const std::exception &e) {
+        return fail(fn, e.what());
+    }
+    if (ntt_prefetch_waves) *ntt_prefetch_waves = ctx->c.tune.ntt_prefetch_waves;
+    if (ks_inner_ctas_per_sm) *ks_inner_ctas_per_sm = ctx->c.tune.ks_inner_ctas_per_sm;
+    return 0;
+}
+
+extern "C" int nexus_set_tuning(nexus_context *ctx, int ntt_prefetch_waves, int ks_inner_ctas_per_sm)
+{
+    static const char *fn = "nexus_set_tuning";
+    if (!ctx) return fail(fn, "null context");
+    if (ntt_prefetch_waves < 0 || ntt_prefetch_waves > 64 || ks_inner_ctas_per_sm < 0 || ks_inner_ctas_per_sm > 64)
+        return fail(fn, "tuning value out of range");
+    ctx->c.tune.ntt_prefetch_waves = ntt_prefetch_waves;
+    ctx->c.tune.ks_inner_ctas_per_sm = ks_inner_ctas_per_sm;
+    return 0;
+}
+
+extern "C" int nexus_get_tuning(const nexus_context *ctx, int *ntt_prefetch_waves, int *ks_inner_ctas_per_sm)
+{
+    if (!ctx) return fail("nexus_get_tuning", "null context");
+    if (ntt_prefetch_waves) *ntt_prefetch_waves = ctx->c.tune.ntt_prefetch_waves;
+    if (ks_inner_ctas_per_sm) *ks_inner_ctas_per_sm = ctx->c.tune.ks_inner_ctas_per_sm;
+    return 0;
+}
+
 extern "C" int nexus_butterfly_rate(int mode, uint64_t q, int rounds, int blocks_per_sm, double *butterflies_per_s,
                                     double *ms)
 {

@@ -165,6 +165,7 @@ extern "C" int nexus_context_create(int log_n, const uint64_t *moduli, int n_mod
         c.n = 1ull << log_n;
         c.k = n_moduli;
         CK(cudaGetDevice(&c.device));
+        CK(cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, c.device));
         // keep memory freed by stream-ordered deallocation in the pool: the
         // evaluator allocates and frees ciphertexts on every operation
         cudaMemPool_t pool;

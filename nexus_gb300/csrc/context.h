@@ -56,6 +56,18 @@ struct Context {
     uint64_t *get_scratch(size_t words);
     const uint32_t *galois_table(uint32_t elt);
 
+    // Launch parameters the autotuner (autotune.cu) chooses per context; they
+    // change how work maps to CTAs, never a result word.
+    struct Tuning {
+        // NTT passes: each CTA asks L2 for the tile of the CTA this many
+        // residency waves (3 CTAs per SM) ahead; 0 turns the prefetch off
+        int ntt_prefetch_waves = 3;
+        // key inner product: CTAs per SM of its grid-stride loop; 0 launches
+        // one CTA per 512-coefficient chunk
+        int ks_inner_ctas_per_sm = 0;
+    } tune;
+    int sm_count = 0;                // multiprocessors of `device`
+
     // Optional CUDA-event timing of every NTT launch (nexus_ntt_timing_*):
     // each forward/inverse call records an event pair on its stream.
     mutable bool ntt_timing = false;

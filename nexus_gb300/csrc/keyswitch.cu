@@ -11,6 +11,7 @@
 //   4. ModDown with rounding: ct[k][i] += (P[k][i] - NTT_i(((INTT_p(P[k][p]) + p/2)
 //      mod p) - p/2)) * p^{-1} mod q_i.
 #include <cstdint>
+#include <algorithm>
 #include <stdexcept>
 #include <string>
 
@@ -145,10 +146,13 @@ void launch_ks_inner(const Context &c, const uint64_t *D, const uint64_t *key, u
     static_assert(kInnerCoeffs == 512, "k_ks_inner maps 512 coefficients to a CTA");
     if (c.logn < 9) throw std::invalid_argument("key switching needs N >= 512");
     const unsigned nb = (unsigned)((size_t)B * (l + 1) << (c.logn - 9));
+    unsigned grid = nb;
+    if (c.tune.ks_inner_ctas_per_sm > 0 && c.sm_count > 0)
+        grid = std::min(nb, (unsigned)(c.tune.ks_inner_ctas_per_sm * c.sm_count));
     if (c.small_primes && l <= 31)
-        k_ks_inner<true><<<nb, kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, nb);
+        k_ks_inner<true><<<grid, kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, nb);
     else
-        k_ks_inner<false><<<nb, kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, nb);
+        k_ks_inner<false><<<grid, kBlock, 0, s>>>(D, key, P, c.d_pc, l, c.k, c.logn, B, nb);
     NEXUS_LAUNCHED();
 }
 

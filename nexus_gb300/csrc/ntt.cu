@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_cols(uint64_t *__restrict__
 // reduction to [0,q) (from [0,4q), or from below 2^59 on the small-prime path).
 template <int LOGS, bool SMALL>
 __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
-                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
+                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm, int pf)
 {
     constexpr int S = 1 << LOGS, T = S / kE, R = kThreads / T, SP = S + S / 16;
     // the T threads of a row sit in one warp and share only their row's
@@ -290,8 +290,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
     uint64_t *p = data + (lrow << logn) + r * S;
     uint64_t *srow = sm + rr * SP;
     const uint64_t B = (1ull << log_n1) + r;
-    {
-        const unsigned fb = blockIdx.x + 3 * sm_count();
+    if (pf) {
+        const unsigned fb = blockIdx.x + (unsigned)pf * 3 * sm_count();
         if (fb < gridDim.x) prefetch_rows_tile<S, R>(data, fb, logn, log_n1, lm);
     }
 
@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
 // Inverse pass A: rows first (undoing pass 2).  Output in [0,2q).
 template <int LOGS>
 __global__ void __launch_bounds__(kThreads, 3) k_inv_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
-                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
+                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm, int pf)
 {
     constexpr int S = 1 << LOGS, T = S / kE, R = kThreads / T, SP = S + S / 16;
     // the T threads of a row sit in one warp and share only their row's
@@ -348,8 +348,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_inv_rows(uint64_t *__restrict__
     uint64_t *p = data + (lrow << logn) + r * S;
     uint64_t *srow = sm + rr * SP;
     const uint64_t B = (1ull << log_n1) + r;
-    {
-        const unsigned fb = blockIdx.x + 3 * sm_count();
+    if (pf) {
+        const unsigned fb = blockIdx.x + (unsigned)pf * 3 * sm_count();
         if (fb < gridDim.x) prefetch_rows_tile<S, R>(data, fb, logn, log_n1, lm);
     }
 
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_inv_rows(uint64_t *__restrict__
 // Inverse pass B: columns (undoing pass 1), then n^{-1} and reduction to [0,q).
 template <int LOGS>
 __global__ void __launch_bounds__(kThreads, 3) k_inv_cols(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
-                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm)
+                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm, int pf)
 {
     constexpr int S = 1 << LOGS, T = S / kE, C = kThreads / T;
     __shared__ uint64_t sm[S * C];
@@ -390,8 +390,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_inv_cols(uint64_t *__restrict__
     uint64_t *p = data + (lrow << logn) + col0;
     const int c = threadIdx.x % C, t = threadIdx.x / C;
 
-    {
-        const unsigned fb = blockIdx.x + 3 * sm_count();
+    if (pf) {
+        const unsigned fb = blockIdx.x + (unsigned)pf * 3 * sm_count();
         if (fb < gridDim.x) prefetch_cols_tile<S, C>(data, fb, logn, n2, tiles, lm);
     }
 
@@ -424,7 +424,8 @@ void launch_fwd_t(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cud
     else
         k_fwd_cols<L1, 0, SMALL><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
     NEXUS_LAUNCHED();
-    k_fwd_rows<L2, SMALL><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm); NEXUS_LAUNCHED();
+    k_fwd_rows<L2, SMALL><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, c.tune.ntt_prefetch_waves);
+    NEXUS_LAUNCHED();
 }
 
 template <int L1, int L2>
@@ -444,8 +445,10 @@ void launch_inv(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaS
     constexpr int R = kThreads / ((1 << L2) / kE);
     const unsigned g1 = (unsigned)(limbs * ((1u << L2) / C));
     const unsigned g2 = (unsigned)(limbs * ((1u << L1) / R));
-    k_inv_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lm); NEXUS_LAUNCHED();
-    k_inv_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lm); NEXUS_LAUNCHED();
+    k_inv_rows<L2><<<g2, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lm, c.tune.ntt_prefetch_waves);
+    NEXUS_LAUNCHED();
+    k_inv_cols<L1><<<g1, kThreads, 0, s>>>(d, c.d_tw_inv, c.d_pc, c.logn, lm, c.tune.ntt_prefetch_waves);
+    NEXUS_LAUNCHED();
 }
 
 }  // namespace

@@ -69,6 +69,11 @@ void switch_key(Context &c, uint64_t *ct, int limbs, const uint64_t *target, con
 void switch_key_batch(Context &c, uint64_t *ct, int batch, int limbs, const uint64_t *target, const uint64_t *key,
                       cudaStream_t s, size_t target_pitch = 0);
 
+// Times a batched key switch of `batch` ciphertexts at `limbs` limbs on
+// random data for every candidate Context::Tuning, keeps the fastest in c.tune
+// and returns its milliseconds per call (autotune.cu).
+double autotune_keyswitch(Context &c, int limbs, int batch, cudaStream_t s, int reps = 3);
+
 // stages of the batched key switch, for callers that fuse their own epilogue:
 // ModUp + inner products (t [B][l] NTT-form targets, overwritten; D scratch
 // B*l*(l+1) limbs; P [B][2][l+1] out), then the ModDown rounding terms

@@ -57,6 +57,8 @@ def test_lockstep_and_hoisting_entry_points_reject_null_arguments_without_gpu():
         ("nexus_argmax_batch", lambda: lib.nexus_argmax_batch(None, one, 1, 4, one), b"null"),
         ("nexus_bootstrapper_stage_batch", lambda: lib.nexus_bootstrapper_stage_batch(None, 0, one, None, 1, one, one),
          b"null"),
+        ("nexus_autotune", lambda: lib.nexus_autotune(None, 1, 1, 1, None, None, None), b"null"),
+        ("nexus_set_tuning", lambda: lib.nexus_set_tuning(None, 0, 0), b"null"),
     ]
     for name, call, word in cases:
         assert call() != 0, name
