@@ -343,9 +343,13 @@ def run_mm_gpu(args, rank, world):
     n = 1 << MM_LOGN
     qs = ng.create_coeff_modulus(n, [60, 40, 60])
     ctx = ng.Context(MM_LOGN, qs)
-    sk = ctx.keygen_secret(seed=11 + rank)
+    # keys and encryptions from SEAL seeds: the oracle's digests of rows 0, 85
+    # and 127 in bench_digests.json are for these inputs
+    seed = _seal_seed(300 + rank)
+    sk = ctx.seal_keygen_secret(seed, 0)
+    pk = ctx.seal_keygen_public(sk, seed)
     rots = [(n + 2 ** i) // 2 ** i for i in range(MM_LOGN)]
-    gks = {e: ctx.keygen_galois(sk, e, seed=100 + i) for i, e in enumerate(rots)}
+    gks = {e: ctx.seal_keygen_galois(sk, e, seed) for e in rots}
     ev = Evaluator(ctx, MM_PT_SCALE, None, gks)
     rng = np.random.default_rng(2024 + rank)
     X = rng.normal(0, 1, (MM_ROWS, MM_COLS))
@@ -357,7 +361,8 @@ def run_mm_gpu(args, rank, world):
     flat = X.reshape(-1)
     packs, host_packs = [], []
     for i in range((flat.size + n - 1) // n):
-        ct = ctx.encrypt_symmetric(sk, None, 2, 50 + i)
+        # enc_compress_ciphertext: a public-key encryption of zero plus the packing
+        ct = ctx.seal_encrypt(pk, None, 2, seed)
         pt = torch.empty((2, n), dtype=torch.int64, device=dev)
         ctx.encode_coefficients(flat[i * n:(i + 1) * n], MM_PACK_SCALE, 2, pt)
         c0 = ct[0:1].clone()
@@ -379,6 +384,12 @@ def run_mm_gpu(args, rank, world):
     for r in check_rows:
         dec = ctx.decode(ctx.decrypt(sk, res[r].to_device()), res[r].scale).real[:MM_OUT]
         err = max(err, float(np.max(np.abs(dec - Y[r]))))
+    parity = None
+    if rank == 0 and MM_ROWS == 128:
+        checks = [_digest_check("matmul_n65536", res[r].to_numpy(), ("rows", str(r), "output")) for r in (0, 85, 127)]
+        if all(c is not None for c in checks):
+            parity = {"checked": "output words of rows 0, 85 and 127 against the oracle's digests",
+                      "words_equal_oracle": all(c["words_equal_oracle"] for c in checks)}
     del res
     barrier(world)
     l0 = ng.kernel_launches()
@@ -451,8 +462,9 @@ def run_mm_gpu(args, rank, world):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "u64",
-        "data": "synthetic: X ~ N(0,1), W ~ N(0,0.02), b ~ N(0,0.02), seeded; engine-generated keys",
+        "data": "synthetic: X ~ N(0,1), W ~ N(0,0.02), b ~ N(0,0.02), seeded; keys and encryptions from a SEAL seed",
         "config": mm_config(),
+        "parity": parity,
         "accuracy": {"max_abs_err_vs_fp64": err, "rows_checked": check_rows},
         "roofline": {
             "kernel": "nexus NTT launches inside the MatMul (k_fwd/k_inv cols+rows)",
@@ -534,15 +546,17 @@ def _seal_seed(tag: int):
     return np.array([(0x9E3779B97F4A7C15 * (tag + i + 1)) % 2 ** 64 for i in range(8)], dtype=np.uint64)
 
 
-def _digest_check(case: str, words) -> dict | None:
+def _digest_check(case: str, words, path=("output",)) -> dict | None:
     """Compare the SHA-256 of an output's words with the oracle's digest for
-    the same seeds (tests/golden/bench_digests.json)."""
+    the same seeds (tests/golden/bench_digests.json, entry `path` of the case)."""
     import hashlib
 
     import numpy as np
     p = ROOT / "tests" / "golden" / "bench_digests.json"
     try:
-        want = json.loads(p.read_text())["cases"][case]["sha256"]["output"]
+        want = json.loads(p.read_text())["cases"][case]["sha256"]
+        for k in path:
+            want = want[k]
     except Exception:
         return None
     got = hashlib.sha256(np.ascontiguousarray(words, dtype="<u8").tobytes()).hexdigest()
@@ -1044,17 +1058,27 @@ def run_gelu_gpu(args, rank, world):
     n = 1 << GELU_LOGN
     qs = ng.create_coeff_modulus(n, GELU_BITS)
     ctx = ng.Context(GELU_LOGN, qs)
-    sk = ctx.keygen_secret(seed=81 + rank)
-    rk = ctx.keygen_relin(sk, seed=82)
+    # keys and encryptions from SEAL seeds; ciphertexts 0 (U(-5,5)) and 1
+    # (U(-8,8)) are the inputs whose oracle digests bench_digests.json holds
+    seed = _seal_seed(200 + rank)
+    sk = ctx.seal_keygen_secret(seed, 0)
+    rk = ctx.seal_keygen_relin(sk, seed)
     ev = Evaluator(ctx, GELU_SCALE, rk)
     top = len(qs) - 1
-    rng = np.random.default_rng(777 + rank)
+    rng = np.random.default_rng(779 + rank)
     vals, cts, host = [], [], []
     for i in range(GELU_CTS):
-        v = rng.uniform(-8, 8, n // 2) if i % 2 == 0 else rng.uniform(-5, 5, n // 2)
+        if i < 2:
+            lo = 5.0 if i == 0 else 8.0
+            v = np.random.default_rng(777 + i + rank).uniform(-lo, lo, n // 2)
+        else:
+            v = rng.uniform(-8, 8, n // 2) if i % 2 else rng.uniform(-5, 5, n // 2)
         pt = torch.empty((top, n), dtype=torch.int64, device=dev)
         ctx.encode(v, GELU_SCALE, top, pt)
-        ct = ctx.encrypt_symmetric(sk, pt, top, 900 + i)
+        s_i = seed.copy()
+        if i >= 2:
+            s_i[7] ^= np.uint64(i)
+        ct = ctx.seal_encrypt_symmetric(sk, pt, top, s_i)
         vals.append(v)
         cts.append(ct)
         host.append(ct.cpu().numpy().view(np.uint64).copy())
@@ -1079,9 +1103,16 @@ def run_gelu_gpu(args, rank, world):
         return 0.5 * x * (1 + np.tanh(math.sqrt(2 / math.pi) * (x + 0.044715 * x ** 3)))
 
     errs = {}
-    for i, tag in ((0, "U(-8,8)"), (1, "U(-5,5)")):
+    for i, tag in ((0, "U(-5,5)"), (1, "U(-8,8)")):
         dec = ctx.decode(ctx.decrypt(sk, res[i].to_device()), res[i].scale).real
         errs[tag] = float(np.max(np.abs(dec - gelu_ref(vals[i]))))
+    parity = None
+    if rank == 0:
+        c0 = _digest_check("gelu_n16384", res[0].to_numpy(), ("u-5_5", "output"))
+        c1 = _digest_check("gelu_n16384", res[1].to_numpy(), ("u-8_8", "output"))
+        if c0 is not None and c1 is not None:
+            parity = {"checked": "output words of ciphertexts 0 (U(-5,5)) and 1 (U(-8,8)) against the oracle's digests",
+                      "words_equal_oracle": c0["words_equal_oracle"] and c1["words_equal_oracle"]}
     del res
     barrier(world)
     l0 = ng.kernel_launches()
@@ -1148,8 +1179,10 @@ def run_gelu_gpu(args, rank, world):
         "metric": "gelu_throughput_n16384", "value": value, "unit": "GELU/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-        "data": "synthetic: slots ~ U(-8,8) and U(-5,5) (alternating ciphertexts), seeded; engine-generated keys",
+        "data": "synthetic: slots ~ U(-5,5) and U(-8,8) (alternating ciphertexts), seeded; keys and encryptions "
+                "from a SEAL seed",
         "config": gelu_config(),
+        "parity": parity,
         "accuracy": {"max_abs_err_vs_fp64_gelu": errs},
         "roofline": {
             "kernel": "nexus NTT launches inside GELU (k_fwd/k_inv cols+rows)",
