@@ -423,15 +423,28 @@ int nexus_ckks_op(nexus_evaluator *ev, int op, const nexus_ciphertext *x, int a1
  * Rotate one ciphertext by several slot steps: res[i] receives the words
  * Evaluator::rotate_vector(x, steps[i]) gives (NAF decomposition included,
  * evaluator.cpp:2667-2722).  The steps that have their own Galois key share
- * one ModUp of x's c1 (hoisted rotations) whenever that is exact -- always,
- * except when a coefficient of INTT(c1) is zero, where each step is switched
- * on its own.  Hoisting keeps, per Galois element, a copy of the key with
+ * one ModUp of x's c1 (hoisted rotations); when a coefficient of INTT(c1) is
+ * zero, where sharing is not exact, the steps are switched on their own by a
+ * fallback launch that the device itself enables.  Hoisting keeps, per Galois element, a copy of the key with
  * permuted rows (as large as the key) and a per-level correction.
  * No counterpart in the reference: SEAL rotates one step per call, and the
  * reference's BSGS transforms call rotate_vector once per baby step.
  */
 int nexus_rotate_vector_many(nexus_evaluator *ev, const nexus_ciphertext *x, const int *steps, int count,
                              nexus_ciphertext *const *res);
+
+/*
+ * The lockstep form of nexus_rotate_vector_many: count ciphertexts of one
+ * size, level and scale, each rotated by every step; res[s * count + b]
+ * receives rotate_vector(cts[b], steps[s]), word for word the single form.
+ * The decomposition is shared by the steps and done once for the batch; a
+ * ciphertext whose INTT(c1) has a zero coefficient is recomputed by the
+ * ordinary key switch inside the same stream (no host wait).  The BSGS
+ * transforms of the lockstep bootstrap and of the encrypted layer run
+ * through this path.
+ */
+int nexus_rotate_vector_many_batch(nexus_evaluator *ev, nexus_ciphertext *const *cts, int count, const int *steps,
+                                   int n_steps, nexus_ciphertext *const *res);
 
 /*
  * Hoisted rotations on (enable != 0, the default) or off for this evaluator

@@ -455,17 +455,19 @@ void BatchEvaluator::rotate_vector_many(const CtBatch &ct, const std::vector<int
         DeviceBuffer t, D;
         t.reserve((size_t)B * l * N, stream());
         D.reserve((size_t)B * l * (l + 1) * N, stream());
-        if (hoist_decompose(c_, ct.data() + (size_t)l * N, pitch, B, l, t.get(), D.get(), ev_.hoist_flag(),
-                            stream())) {
-            for (size_t i : direct) {
-                const uint32_t elt = ev_.galois_elt(steps[i]);
-                const uint64_t *pk = ev_.hoist_key(elt), *corr = ev_.hoist_corr(elt, l);
-                outs[i].resize(c_, B, 2, l, stream());
-                outs[i].scale() = ct.scale();
-                hoist_rotate(c_, D.get(), B, l, elt, pk, corr, ct.data(), pitch, outs[i].data(), stream());
-                done[i] = true;
-            }
+        int *flags = ev_.hoist_flags(B);
+        hoist_decompose(c_, ct.data() + (size_t)l * N, pitch, B, l, t.get(), D.get(), flags, stream());
+        std::vector<HoistRotation> rots;
+        for (size_t i : direct) {
+            const uint32_t elt = ev_.galois_elt(steps[i]);
+            const uint64_t *pk = ev_.hoist_key(elt), *corr = ev_.hoist_corr(elt, l);
+            outs[i].resize(c_, B, 2, l, stream());
+            outs[i].scale() = ct.scale();
+            hoist_rotate(c_, D.get(), B, l, elt, pk, corr, ct.data(), pitch, outs[i].data(), stream());
+            rots.push_back({elt, ev_.galois_keys.at(elt), outs[i].data()});
+            done[i] = true;
         }
+        hoist_fix(c_, t.get(), ct.data(), pitch, flags, B, l, rots, stream());
     }
     for (size_t i = 0; i < steps.size(); ++i)
         if (!done[i]) rotate_vector(ct, steps[i], outs[i]);

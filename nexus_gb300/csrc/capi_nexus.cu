@@ -216,6 +216,32 @@ int check_batch(const char *fn, nexus_evaluator *ev, nexus_ciphertext *const *ct
 
 }  // namespace
 
+extern "C" int nexus_rotate_vector_many_batch(nexus_evaluator *ev, nexus_ciphertext *const *cts, int count,
+                                              const int *steps, int n_steps, nexus_ciphertext *const *res)
+{
+    static const char *fn = "nexus_rotate_vector_many_batch";
+    if (!ev || !cts || !res || count < 1 || n_steps < 0 || (n_steps > 0 && !steps)) return fail(fn, "null argument");
+    const size_t total = (size_t)count * n_steps;
+    for (int b = 0; b < count; ++b) {
+        if (!cts[b]) return fail(fn, "null ciphertext");
+        if (const char *e = input_problem(ev->ctx, cts[b])) return fail(fn, e);
+    }
+    for (size_t i = 0; i < total; ++i) {
+        if (!res[i]) return fail(fn, "null result");
+        for (int b = 0; b < count; ++b)
+            if (res[i] == cts[b]) return fail(fn, "results must not alias inputs");
+        for (size_t j = 0; j < i; ++j)
+            if (res[j] == res[i]) return fail(fn, "results must be distinct");
+    }
+    return guarded(fn, [&] {
+        BatchEvaluator bev(ev->ev);
+        CtBatch x = gather_batch(ev, cts, count);
+        std::vector<CtBatch> outs;
+        bev.rotate_vector_many(x, std::vector<int>(steps, steps + n_steps), outs);
+        for (int i = 0; i < n_steps; ++i) scatter_batch(ev, outs[i], res + (size_t)i * count);
+    });
+}
+
 extern "C" int nexus_gelu_batch(nexus_evaluator *ev, nexus_ciphertext *const *cts, int count,
                                 nexus_ciphertext *const *res)
 {

@@ -776,7 +776,7 @@ const uint64_t *Evaluator::hoist_corr(uint32_t elt, int limbs)
 bool Evaluator::hoist_prepare(const std::vector<uint32_t> &elts, int limbs)
 {
     try {
-        hoist_flag();
+        hoist_flags(1);
         for (uint32_t e : elts) {
             hoist_key(e);
             hoist_corr(e, limbs);
@@ -788,9 +788,9 @@ bool Evaluator::hoist_prepare(const std::vector<uint32_t> &elts, int limbs)
     return true;
 }
 
-int *Evaluator::hoist_flag()
+int *Evaluator::hoist_flags(int count)
 {
-    hoist_flag_.reserve(1, s_);
+    hoist_flag_.reserve(((size_t)count + 1) / 2, s_);
     return reinterpret_cast<int *>(hoist_flag_.get());
 }
 
@@ -811,17 +811,19 @@ void Evaluator::rotate_vector_many(const Ciphertext &ct, const std::vector<int> 
         DeviceBuffer t, D;
         t.reserve((size_t)l * N, s_);
         D.reserve((size_t)l * (l + 1) * N, s_);
-        if (hoist_decompose(c_, ct.data() + (size_t)l * N, 2 * (size_t)l * N, 1, l, t.get(), D.get(), hoist_flag(),
-                            s_)) {
-            for (size_t i : direct) {
-                const uint32_t elt = galois_elt(steps[i]);
-                const uint64_t *pk = hoist_key(elt), *corr = hoist_corr(elt, l);
-                outs[i].resize(c_, 2, l, s_);
-                outs[i].scale() = ct.scale();
-                hoist_rotate(c_, D.get(), 1, l, elt, pk, corr, ct.data(), 0, outs[i].data(), s_);
-                done[i] = true;
-            }
+        int *flags = hoist_flags(1);
+        hoist_decompose(c_, ct.data() + (size_t)l * N, 2 * (size_t)l * N, 1, l, t.get(), D.get(), flags, s_);
+        std::vector<HoistRotation> rots;
+        for (size_t i : direct) {
+            const uint32_t elt = galois_elt(steps[i]);
+            const uint64_t *pk = hoist_key(elt), *corr = hoist_corr(elt, l);
+            outs[i].resize(c_, 2, l, s_);
+            outs[i].scale() = ct.scale();
+            hoist_rotate(c_, D.get(), 1, l, elt, pk, corr, ct.data(), 0, outs[i].data(), s_);
+            rots.push_back({elt, galois_keys.at(elt), outs[i].data()});
+            done[i] = true;
         }
+        hoist_fix(c_, t.get(), ct.data(), 0, flags, 1, l, rots, s_);
     }
     for (size_t i = 0; i < steps.size(); ++i)
         if (!done[i]) rotate_vector(ct, steps[i], outs[i]);

@@ -217,7 +217,8 @@ public:
     // key) and, per level, a [2][limbs+1][N] correction.
     const uint64_t *hoist_key(uint32_t elt);
     const uint64_t *hoist_corr(uint32_t elt, int limbs);
-    int *hoist_flag();
+    // count device ints for hoist_decompose's per-ciphertext zero flags
+    int *hoist_flags(int count);
     // hoisting pays when at least two rotations share the decomposition and
     // the level is high enough for the ModUp to dominate the key switch
     static bool hoist_pays(int direct_steps, int limbs) { return direct_steps >= 2 && limbs >= 8; }

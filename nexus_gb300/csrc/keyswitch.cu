@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <stdexcept>
 #include <string>
+#include <vector>
+#include <cooperative_groups.h>
 
 #include "context.h"
 #include "ntt.h"
@@ -411,18 +413,23 @@ void apply_galois(Context &c, const uint64_t *ct, int l, uint32_t elt, const uin
 //
 // the same residues as the inner product of the rotated target, so the
 // ModDown and the output words are the ones apply_galois gives.  A zero
-// coefficient in t (probability about B*l*N/q for random data, certain for a
-// trivial c1) breaks the identity; hoist_decompose reports it and the caller
-// rotates one element at a time instead.
+// coefficient in t (probability about l*N/q per ciphertext for random data,
+// certain for a trivial c1) breaks the identity: a negated zero is 0, not
+// q_j.  hoist_decompose marks each ciphertext that has one in a device flag,
+// and hoist_fix, one cooperative launch after the group's hoisted rotations,
+// recomputes every rotation of the marked ciphertexts by the ordinary key
+// switch; when nothing is marked its CTAs return at once.  Nothing waits on
+// the host.
 
 namespace nexus {
 
 namespace {
 
-__global__ void k_any_zero(const uint64_t *__restrict__ t, size_t total, int *flag)
+// flag[b] = 1 when member b's rows of t (`per` words each) hold a zero
+__global__ void k_any_zero(const uint64_t *__restrict__ t, size_t total, size_t per, int *flag)
 {
     for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x)
-        if (t[x] == 0) *flag = 1;
+        if (t[x] == 0) flag[x / per] = 1;
 }
 
 // out[p][pos] = 1 where the automorphism X -> X^elt negates the coefficient
@@ -511,8 +518,8 @@ __global__ void k_hoist_finish(const uint64_t *__restrict__ Pt, const uint64_t *
 
 }  // namespace
 
-bool hoist_decompose(Context &c, const uint64_t *c1, size_t c1_pitch, int B, int l, uint64_t *t, uint64_t *D,
-                     int *d_flag, cudaStream_t s)
+void hoist_decompose(Context &c, const uint64_t *c1, size_t c1_pitch, int B, int l, uint64_t *t, uint64_t *D,
+                     int *d_flags, cudaStream_t s)
 {
     const size_t N = c.n, Bs = (size_t)B;
     const int sp = c.k - 1;
@@ -526,22 +533,16 @@ bool hoist_decompose(Context &c, const uint64_t *c1, size_t c1_pitch, int B, int
                                                     reinterpret_cast<ulonglong2 *>(D), l, c.logn, pairs);
     NEXUS_LAUNCHED();
     ntt_inverse(c, t, Bs, LimbMap{l, 0, -1}, s);
-    cudaMemsetAsync(d_flag, 0, sizeof(int), s);
+    cudaMemsetAsync(d_flags, 0, sizeof(int) * Bs, s);
     const size_t words = Bs * l * N;
-    k_any_zero<<<grid_for(words), kBlock, 0, s>>>(t, words, d_flag);
+    k_any_zero<<<grid_for(words), kBlock, 0, s>>>(t, words, (size_t)l * N, d_flags);
     NEXUS_LAUNCHED();
-    int h_flag = 0;
-    if (cudaMemcpyAsync(&h_flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-        throw std::runtime_error("hoist_decompose: reading the zero flag failed");
-    if (h_flag) return false;
     NttLoader ld;
     ld.kind = 1;
     ld.src = t;
     ld.group = l;
     ld.src_limbs = l;
     ntt_forward_loaded(c, D, Bs * l, LimbMap{l, 0, sp, 1}, ld, s);
-    return true;
 }
 
 void hoist_galois_mask_ntt(Context &c, uint32_t elt, uint64_t *M, cudaStream_t s)
@@ -590,6 +591,231 @@ void hoist_rotate(Context &c, const uint64_t *D, int B, int l, uint32_t elt, con
     k_hoist_finish<<<grid_for(tot), kBlock, 0, s>>>(Pt, corr, T, ct, ct_pitch, tab, c.d_pc,
                                                      c.d_inv_q + (size_t)sp * c.k, l, c.logn, tot, out);
     NEXUS_LAUNCHED();
+}
+
+// ---------------------------------------------------------------------------
+// The exact fallback of a hoisted group, for the ciphertexts whose INTT(c1)
+// has a zero coefficient.  One cooperative launch covers up to kFixMaxRot
+// rotations of the group; its CTAs read the flags written by
+// hoist_decompose and return when none is set.  Otherwise, for each marked
+// ciphertext and each element, the grid runs the key switch of
+// switch_key_inplace on the rotated target with grid-wide barriers between
+// the steps: digit j of the target is the signed permutation of t_j (a
+// negated zero stays 0), reduced into the l+1 primes, transformed by a
+// radix-2 negacyclic NTT, multiplied into P with the unpermuted key; then
+// the ModDown with rounding, and the permuted c0 added to the first
+// polynomial.  Slow, rare, and word for word apply_galois.
+
+namespace {
+
+namespace cg = cooperative_groups;
+
+constexpr int kFixMaxRot = 48;
+
+struct HoistFixArgs {
+    const uint64_t *t;        // [B][l][N], INTT of the c1 polynomials
+    const uint64_t *ct;       // c0 of ciphertext b at ct + b * pitch
+    size_t pitch;
+    const int *flags;         // [B]
+    const PrimeConst *pc;
+    const ulonglong2 *tw_fwd, *tw_inv;
+    const ulonglong2 *inv_p;  // p^{-1} mod q_i with its Shoup quotient
+    uint64_t *U, *P, *V;      // scratch [l+1][N], [2][l+1][N], [N]
+    int B, l, K, logn, R;
+    uint32_t elt[kFixMaxRot];
+    const uint64_t *key[kFixMaxRot];   // [K-1][2][K][N], as generated
+    const uint32_t *tab[kFixMaxRot];   // NTT-domain permutation of elt
+    uint64_t *out[kFixMaxRot];         // [B][2][l][N]
+};
+
+// prime of row r: fixed when >= 0, else the ModUp order q_0..q_{l-1}, p
+__device__ __forceinline__ int fix_prime(int r, int fixed, int l, int K)
+{
+    return fixed >= 0 ? fixed : (r == l ? K - 1 : r);
+}
+
+// forward negacyclic NTT of `rows` rows of a, radix 2, one stage between
+// grid barriers; input and output in [0, q)
+__device__ void fix_ntt_forward(cg::grid_group &g, const HoistFixArgs &a, uint64_t *d, int rows, int fixed)
+{
+    const size_t N = (size_t)1 << a.logn, half = N >> 1;
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    for (int lm = 0; lm < a.logn; ++lm) {
+        const size_t m = (size_t)1 << lm, t = half >> lm;
+        for (size_t x = tid; x < (size_t)rows * half; x += stride) {
+            const int r = (int)(x >> (a.logn - 1));
+            const size_t b = x & (half - 1), i = b >> (a.logn - 1 - lm);
+            const size_t idx = 2 * i * t + (b & (t - 1));
+            const int p = fix_prime(r, fixed, a.l, a.K);
+            const uint64_t q = a.pc[p].q;
+            const ulonglong2 w = a.tw_fwd[(size_t)p * N + m + i];
+            uint64_t *row = d + ((size_t)r << a.logn);
+            const uint64_t X = row[idx], Y = mul_shoup(row[idx + t], w.x, w.y, q);
+            row[idx] = csub(X + Y, q);
+            row[idx + t] = csub(X + q - Y, q);
+        }
+        g.sync();
+    }
+}
+
+// inverse of fix_ntt_forward (Gentleman-Sande stages, then n^{-1})
+__device__ void fix_ntt_inverse(cg::grid_group &g, const HoistFixArgs &a, uint64_t *d, int rows, int fixed)
+{
+    const size_t N = (size_t)1 << a.logn, half = N >> 1;
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    for (int lm = a.logn - 1; lm >= 0; --lm) {
+        const size_t m = (size_t)1 << lm, t = half >> lm;
+        for (size_t x = tid; x < (size_t)rows * half; x += stride) {
+            const int r = (int)(x >> (a.logn - 1));
+            const size_t b = x & (half - 1), i = b >> (a.logn - 1 - lm);
+            const size_t idx = 2 * i * t + (b & (t - 1));
+            const int p = fix_prime(r, fixed, a.l, a.K);
+            const uint64_t q = a.pc[p].q;
+            const ulonglong2 w = a.tw_inv[(size_t)p * N + m + i];
+            uint64_t *row = d + ((size_t)r << a.logn);
+            const uint64_t X = row[idx], Y = row[idx + t];
+            row[idx] = csub(X + Y, q);
+            row[idx + t] = mul_shoup(X + q - Y, w.x, w.y, q);
+        }
+        g.sync();
+    }
+    for (size_t x = tid; x < ((size_t)rows << a.logn); x += stride) {
+        const PrimeConst P = a.pc[fix_prime((int)(x >> a.logn), fixed, a.l, a.K)];
+        d[x] = mul_shoup(d[x], P.inv_n, P.inv_n_q, P.q);
+    }
+    g.sync();
+}
+
+__global__ void __launch_bounds__(kBlock) k_hoist_fix(const HoistFixArgs a)
+{
+    bool any = false;
+    for (int b = 0; b < a.B; ++b) any |= a.flags[b] != 0;
+    if (!any) return;   // the same answer in every CTA: the flags were written by an earlier launch
+    cg::grid_group g = cg::this_grid();
+    const int l = a.l, K = a.K, logn = a.logn;
+    const size_t N = (size_t)1 << logn;
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    const PrimeConst Psp = a.pc[K - 1];
+    for (int b = 0; b < a.B; ++b) {
+        if (!a.flags[b]) continue;
+        const uint64_t *tb = a.t + (size_t)b * l * N;
+        const uint64_t *c0 = a.ct + (size_t)b * a.pitch;
+        for (int r = 0; r < a.R; ++r) {
+            const uint64_t elt = a.elt[r];
+            const uint64_t *key = a.key[r];
+            for (size_t x = tid; x < (size_t)2 * (l + 1) * N; x += stride) a.P[x] = 0;
+            g.sync();
+            for (int j = 0; j < l; ++j) {
+                // digit j of the rotated target: coefficient n of t_j moves to
+                // n * elt mod 2N, negated (mod q_j) past N; reduced into every prime
+                const uint64_t qj = a.pc[j].q;
+                for (size_t n = tid; n < N; n += stride) {
+                    const uint64_t raw = (n * elt) & (2 * N - 1), v0 = tb[(size_t)j * N + n];
+                    const size_t dst = raw < N ? raw : raw - N;
+                    const uint64_t v = raw < N ? v0 : (v0 ? qj - v0 : 0);
+                    for (int i = 0; i <= l; ++i) {
+                        const PrimeConst Q = a.pc[fix_prime(i, -1, l, K)];
+                        a.U[((size_t)i << logn) + dst] = Q.q < qj ? barrett_64(v, Q.q, Q.r1) : v;
+                    }
+                }
+                g.sync();
+                fix_ntt_forward(g, a, a.U, l + 1, -1);
+                for (size_t x = tid; x < ((size_t)(l + 1) << logn); x += stride) {
+                    const int i = (int)(x >> logn);
+                    const int kidx = fix_prime(i, -1, l, K);
+                    const size_t n = x & (N - 1);
+                    const PrimeConst Q = a.pc[kidx];
+                    const uint64_t u = a.U[x];
+#pragma unroll
+                    for (int k = 0; k < 2; ++k) {
+                        const uint64_t kv = key[((((size_t)j * 2 + k) * K + kidx) << logn) + n];
+                        uint64_t &acc = a.P[(((size_t)k * (l + 1) + i) << logn) + n];
+                        acc = csub(acc + mul_mod(u, kv, Q.q, Q.r0, Q.r1), Q.q);
+                    }
+                }
+                g.sync();
+            }
+            const uint32_t *tab = a.tab[r];
+            uint64_t *out = a.out[r] + (size_t)b * 2 * l * N;
+            for (int k = 0; k < 2; ++k) {
+                const uint64_t *Pk = a.P + (((size_t)k * (l + 1)) << logn);
+                for (size_t n = tid; n < N; n += stride) a.V[n] = Pk[((size_t)l << logn) + n];
+                g.sync();
+                fix_ntt_inverse(g, a, a.V, 1, K - 1);
+                // rounding: ((x + p/2) mod p) mod q_i - (p/2 mod q_i)
+                const uint64_t h = Psp.q >> 1;
+                for (size_t x = tid; x < ((size_t)l << logn); x += stride) {
+                    const PrimeConst Q = a.pc[(int)(x >> logn)];
+                    const uint64_t u = csub(a.V[x & (N - 1)] + h, Psp.q);
+                    const uint64_t ui = Q.q < Psp.q ? barrett_64(u, Q.q, Q.r1) : u;
+                    const uint64_t hi = Q.q < Psp.q ? barrett_64(h, Q.q, Q.r1) : h;
+                    a.U[x] = csub(ui + Q.q - hi, Q.q);
+                }
+                g.sync();
+                fix_ntt_forward(g, a, a.U, l, -1);
+                for (size_t x = tid; x < ((size_t)l << logn); x += stride) {
+                    const int i = (int)(x >> logn);
+                    const size_t n = x & (N - 1);
+                    const uint64_t q = a.pc[i].q;
+                    const ulonglong2 w = a.inv_p[i];
+                    uint64_t v = mul_shoup(Pk[((size_t)i << logn) + n] + q - a.U[x], w.x, w.y, q);
+                    if (k == 0) v = csub(v + c0[((size_t)i << logn) + tab[n]], q);
+                    out[((size_t)k * l << logn) + x] = v;
+                }
+                g.sync();
+            }
+        }
+    }
+}
+
+}  // namespace
+
+void hoist_fix(Context &c, const uint64_t *t, const uint64_t *ct, size_t ct_pitch, const int *d_flags, int B, int l,
+               const std::vector<HoistRotation> &rots, cudaStream_t s)
+{
+    const size_t N = c.n;
+    if (ct_pitch == 0) ct_pitch = 2 * (size_t)l * N;
+    // co-resident CTAs per SM (a cooperative launch must not exceed them)
+    static const int blocks_per_sm = [] {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_hoist_fix, kBlock, 0) != cudaSuccess || nb < 1)
+            throw std::runtime_error("hoist_fix: occupancy query failed");
+        return nb;
+    }();
+    // scratch U | P | V; hoist_rotate's arena (B*N*(4l+4) words) already holds it
+    uint64_t *U = c.get_scratch(N * (3 * (size_t)(l + 1) + 1));
+    HoistFixArgs a{};
+    a.t = t;
+    a.ct = ct;
+    a.pitch = ct_pitch;
+    a.flags = d_flags;
+    a.pc = c.d_pc;
+    a.tw_fwd = c.d_tw_fwd;
+    a.tw_inv = c.d_tw_inv;
+    a.inv_p = c.d_inv_q + (size_t)(c.k - 1) * c.k;
+    a.U = U;
+    a.P = U + (size_t)(l + 1) * N;
+    a.V = a.P + 2 * (size_t)(l + 1) * N;
+    a.B = B;
+    a.l = l;
+    a.K = c.k;
+    a.logn = c.logn;
+    const unsigned grid = (unsigned)(blocks_per_sm * c.sm_count);
+    for (size_t first = 0; first < rots.size(); first += kFixMaxRot) {
+        a.R = (int)std::min(rots.size() - first, (size_t)kFixMaxRot);
+        for (int r = 0; r < a.R; ++r) {
+            const HoistRotation &h = rots[first + r];
+            a.elt[r] = h.elt;
+            a.key[r] = h.key;
+            a.tab[r] = c.galois_table(h.elt);
+            a.out[r] = h.out;
+        }
+        void *args[] = {&a};
+        if (cudaLaunchCooperativeKernel((const void *)k_hoist_fix, dim3(grid), dim3(kBlock), args, 0, s) !=
+            cudaSuccess)
+            throw std::runtime_error("hoist_fix: cooperative launch failed");
+        NEXUS_LAUNCHED();
+    }
 }
 
 }  // namespace nexus

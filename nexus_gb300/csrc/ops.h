@@ -5,6 +5,7 @@
 // on `s`; multi-kernel operations share the context's scratch arena.
 #pragma once
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "context.h"
@@ -85,17 +86,26 @@ void ks_moddown_terms(Context &c, const uint64_t *P, int B, int l, uint64_t *T, 
 
 // Hoisted rotations (keyswitch.cu): one ModUp of the c1 polynomials of B
 // ciphertexts at l limbs (c1 at c1 + b * c1_pitch) shared by several Galois
-// elements.  hoist_decompose fills D [B][l][l+1][N] (t is scratch of B*l
-// limbs, d_flag one device int) and returns false, with D unset, when a
-// coefficient of INTT(c1) is zero: the shared decomposition is then not
-// exact and the caller must rotate element by element.  Per element:
-// perm_key (hoist_permute_key, the key with every row scattered by the
-// element's NTT permutation) and corr [2][l+1][N] (hoist_correction from the
-// key and M = hoist_galois_mask_ntt [K][N]) are reusable across calls;
-// hoist_rotate writes out [B][2][l][N] with the words apply_galois gives for
-// each ciphertext (ct at ct + b * ct_pitch, 0 = 2 * l * N).
-bool hoist_decompose(Context &c, const uint64_t *c1, size_t c1_pitch, int B, int l, uint64_t *t, uint64_t *D,
-                     int *d_flag, cudaStream_t s);
+// elements.  hoist_decompose fills D [B][l][l+1][N] and t [B][l][N] (the
+// INTT of c1) and sets d_flags[b] (B device ints) when a coefficient of
+// ciphertext b's INTT(c1) is zero, where the shared decomposition is not
+// exact.  Per element: perm_key (hoist_permute_key, the key with every row
+// scattered by the element's NTT permutation) and corr [2][l+1][N]
+// (hoist_correction from the key and M = hoist_galois_mask_ntt [K][N]) are
+// reusable across calls; hoist_rotate writes out [B][2][l][N] (ct at
+// ct + b * ct_pitch, 0 = 2 * l * N), and once every element of the group is
+// written, hoist_fix rewrites the flagged ciphertexts' outputs by the
+// ordinary key switch (one cooperative launch; nothing when no flag is set).
+// Together they give the words apply_galois gives, with no host wait.
+struct HoistRotation {
+    uint32_t elt;
+    const uint64_t *key;   // the element's Galois key as generated
+    uint64_t *out;         // [B][2][l][N], written by hoist_rotate
+};
+void hoist_decompose(Context &c, const uint64_t *c1, size_t c1_pitch, int B, int l, uint64_t *t, uint64_t *D,
+                     int *d_flags, cudaStream_t s);
+void hoist_fix(Context &c, const uint64_t *t, const uint64_t *ct, size_t ct_pitch, const int *d_flags, int B, int l,
+               const std::vector<HoistRotation> &rots, cudaStream_t s);
 void hoist_galois_mask_ntt(Context &c, uint32_t elt, uint64_t *M, cudaStream_t s);
 void hoist_permute_key(Context &c, const uint64_t *key, uint32_t elt, uint64_t *out, cudaStream_t s);
 void hoist_correction(Context &c, const uint64_t *key, const uint64_t *M, int l, uint64_t *out, cudaStream_t s);

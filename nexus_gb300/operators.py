@@ -154,6 +154,19 @@ class Evaluator:
         check(lib().nexus_rotate_vector_many(self._h, x.handle, arr, len(steps), out), "nexus_rotate_vector_many")
         return res
 
+    def rotate_vector_many_batch(self, cts, steps) -> list:
+        """[[rotate_vector(c, s) for c in cts] for s in steps], in lockstep
+        (one shared decomposition for the batch)."""
+        steps = [int(v) for v in steps]
+        res = [[Ciphertext(self.ctx) for _ in cts] for _ in steps]
+        a = (C.c_void_p * len(cts))(*[c.handle.value for c in cts])
+        arr = (C.c_int * max(1, len(steps)))(*steps)
+        flat = [r for row in res for r in row]
+        out = (C.c_void_p * max(1, len(flat)))(*[r.handle.value for r in flat])
+        check(lib().nexus_rotate_vector_many_batch(self._h, a, len(cts), arr, len(steps), out),
+              "nexus_rotate_vector_many_batch")
+        return res
+
     def gelu(self, x: Ciphertext) -> Ciphertext:
         res = Ciphertext(self.ctx)
         check(lib().nexus_gelu(self._h, x.handle, res.handle), "nexus_gelu")

@@ -53,6 +53,8 @@ def test_lockstep_and_hoisting_entry_points_reject_null_arguments_without_gpu():
     cases = [
         ("nexus_switch_key_batch", lambda: lib.nexus_switch_key_batch(None, None, 1, 1, None, None, None), b"null"),
         ("nexus_rotate_vector_many", lambda: lib.nexus_rotate_vector_many(None, None, steps, 1, one), b"null"),
+        ("nexus_rotate_vector_many_batch",
+         lambda: lib.nexus_rotate_vector_many_batch(None, one, 1, steps, 1, one), b"null"),
         ("nexus_evaluator_set_hoisting", lambda: lib.nexus_evaluator_set_hoisting(None, 1), b"null"),
         ("nexus_argmax_batch", lambda: lib.nexus_argmax_batch(None, one, 1, 4, one), b"null"),
         ("nexus_bootstrapper_stage_batch", lambda: lib.nexus_bootstrapper_stage_batch(None, 0, one, None, 1, one, one),

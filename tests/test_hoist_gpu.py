@@ -1,10 +1,11 @@
 """Rotations of one ciphertext by several steps sharing one decomposition.
 
-nexus_rotate_vector_many must give, for every step, exactly the words of the
-ordinary Galois key switch (nexus_apply_galois): on random ciphertexts (the
-shared-ModUp path), on a ciphertext whose c1 has zero coefficients in
-coefficient form and on a trivial one (both must fall back to one key switch
-per step), below the level where sharing pays, and for step 0.
+nexus_rotate_vector_many and its lockstep form must give, for every step,
+exactly the words of the ordinary Galois key switch (nexus_apply_galois): on
+random ciphertexts (the shared-ModUp path), on a ciphertext whose c1 has a
+zero coefficient in coefficient form and on a trivial one (both are
+recomputed by the device-enabled fallback launch, in a batch only for the
+member concerned), below the level where sharing pays, and for step 0.
 """
 import numpy as np
 import pytest
@@ -98,3 +99,49 @@ def test_hoisting_off_gives_the_same_words(env):
     finally:
         ev.set_hoisting(True)
     assert all(np.array_equal(a, b) for a, b in zip(on, off))
+
+
+def _zero_at(ctx, qs, data, limb, pos):
+    """data with coefficient `pos` of INTT(c1)'s limb `limb` set to zero."""
+    oc = po.OracleContext(LOG_N, qs)
+    limbs = data.shape[1]
+    coeff = oc.ntt(data[1], 0, limbs, inverse=True)
+    coeff[limb, pos] = 0
+    out = data.copy()
+    out[1] = oc.ntt(coeff, 0, limbs)
+    return out
+
+
+def test_lockstep_member_with_a_zero_is_recomputed(env):
+    """In a lockstep batch only the member with a zero takes the fallback;
+    every member's words equal its own apply_galois."""
+    import torch
+    from nexus_gb300.operators import Ciphertext
+    ctx, ev, keys, qs = env
+    limbs = 11
+    rng = np.random.default_rng(7)
+    datas = [po.random_residues(rng, (2, limbs, N), qs[:limbs]) for _ in range(3)]
+    datas[1] = _zero_at(ctx, qs, datas[1], 5, 4000)
+    datas[2][1] = 0
+    xs = [Ciphertext.from_numpy(ctx, d, SCALE) for d in datas]
+    res = ev.rotate_vector_many_batch(xs, STEPS)
+    for s, row in zip(STEPS, res):
+        elt = ctx.galois_elt(s)
+        for d, o in zip(datas, row):
+            want = torch.empty_like(to_dev(d))
+            ctx.apply_galois(to_dev(d), elt, keys[elt], want)
+            assert o.scale == SCALE
+            assert np.array_equal(o.to_numpy(), to_host(want)), s
+
+
+def test_lockstep_matches_single_form(env):
+    from nexus_gb300.operators import Ciphertext
+    ctx, ev, keys, qs = env
+    rng = np.random.default_rng(8)
+    datas = [po.random_residues(rng, (2, 9, N), qs[:9]) for _ in range(2)]
+    xs = [Ciphertext.from_numpy(ctx, d, SCALE) for d in datas]
+    res = ev.rotate_vector_many_batch(xs, STEPS + [0])
+    for b, x in enumerate(xs):
+        single = ev.rotate_vector_many(x, STEPS + [0])
+        for row, o in zip(res, single):
+            assert np.array_equal(row[b].to_numpy(), o.to_numpy())
