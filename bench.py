@@ -192,6 +192,14 @@ def ntt_config():
             "l2": "inputs 1.5 GiB > L2, no flush"}
 
 
+def _apply_ntt_form(ctx, args) -> int:
+    """--ntt-form 0/1 overrides the context's forward-NTT form (after any
+    autotuning); returns the form in use."""
+    if args.ntt_form != "auto":
+        ctx.set_ntt_form(int(args.ntt_form))
+    return ctx.ntt_form()
+
+
 def run_ntt_gpu(args, rank, world):
     import numpy as np
     import torch
@@ -203,6 +211,7 @@ def run_ntt_gpu(args, rank, world):
     n = 1 << NTT_LOGN
     qs = ng.create_coeff_modulus(n, [NTT_BITS] * NTT_PRIMES)
     ctx = ng.Context(NTT_LOGN, qs)
+    _apply_ntt_form(ctx, args)
     limbs = NTT_CTS * NTT_POLYS * NTT_PRIMES
     g = torch.Generator(device=dev).manual_seed(1234 + rank)
     qd = torch.tensor(qs, dtype=torch.int64, device=dev).view(1, NTT_PRIMES, 1)
@@ -222,6 +231,7 @@ def run_ntt_gpu(args, rank, world):
     t1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clk:
         torch.cuda.synchronize(dev)
+        launches0 = ng.kernel_launches()
         t0.record(stream)
         for i in range(args.steps):
             evs[i][0].record(stream)
@@ -229,6 +239,7 @@ def run_ntt_gpu(args, rank, world):
             evs[i][1].record(stream)
         t1.record(stream)
         torch.cuda.synchronize(dev)
+        launches = ng.kernel_launches() - launches0
     barrier(world)
     total_ms = t0.elapsed_time(t1)
     total_ms = max_over_ranks(total_ms, world)
@@ -273,8 +284,10 @@ def run_ntt_gpu(args, rank, world):
         "dtype": "u64",
         "data": "synthetic uniform residues (seeded)",
         "config": ntt_config(),
+        "ntt_form": ctx.ntt_form(),
         "roofline": {
-            "kernel": "nexus_ntt_forward (k_fwd_cols + k_fwd_rows)",
+            "kernel": ("nexus_ntt_forward (k_fwd_cluster, one pass)" if ctx.ntt_form() == 1
+                       else "nexus_ntt_forward (k_fwd_cols + k_fwd_rows)"),
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": peak_kind,
             "algorithmic_bytes_per_launch": alg_bytes,
@@ -285,7 +298,7 @@ def run_ntt_gpu(args, rank, world):
         "e2e": {"value": limbs * e2e_steps * world / (e2e_ms / 1e3), "unit": "limb-NTT/s",
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "clocks": clk.summary(),
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches,
     }
     if rank == 0 and world == 1:
         res["cpu_baseline"] = cpu_ntt_sample(budget_s=args.cpu_seconds)
@@ -343,6 +356,7 @@ def run_mm_gpu(args, rank, world):
     n = 1 << MM_LOGN
     qs = ng.create_coeff_modulus(n, [60, 40, 60])
     ctx = ng.Context(MM_LOGN, qs)
+    _apply_ntt_form(ctx, args)
     # keys and encryptions from SEAL seeds: the oracle's digests of rows 0, 85
     # and 127 in bench_digests.json are for these inputs
     seed = _seal_seed(300 + rank)
@@ -609,6 +623,7 @@ def run_boot_gpu(args, rank, world):
     bs.generate_LT_coefficient_3()
     # launch parameters chosen by the autotuner at the bootstrap's top key-switch shape
     tuning = ctx.autotune(len(qs) - 1, BOOT_CTS)
+    tuning["ntt_form"] = _apply_ntt_form(ctx, args)
     top = len(qs) - 1
     rng = np.random.default_rng(4096 + rank)
     vals, inputs, host_in = [], [], []
@@ -857,6 +872,7 @@ def run_bert_gpu(args, rank, world):
     bs.generate_LT_coefficient_3()
     layer = NB.BertLayer(bs, shape, w)
     tuning = ctx.autotune(20, 16)
+    tuning["ntt_form"] = _apply_ntt_form(ctx, args)
     all_steps = steps + [s for s in layer.rotation_steps() if s not in steps]
     for s in all_steps:
         e = ctx.galois_elt(s)
@@ -1058,6 +1074,9 @@ def run_gelu_gpu(args, rank, world):
     n = 1 << GELU_LOGN
     qs = ng.create_coeff_modulus(n, GELU_BITS)
     ctx = ng.Context(GELU_LOGN, qs)
+    # launch parameters chosen by the autotuner at the GELU's top key-switch shape
+    tuning = ctx.autotune(len(qs) - 1, GELU_CTS)
+    tuning["ntt_form"] = _apply_ntt_form(ctx, args)
     # keys and encryptions from SEAL seeds; ciphertexts 0 (U(-5,5)) and 1
     # (U(-8,8)) are the inputs whose oracle digests bench_digests.json holds
     seed = _seal_seed(200 + rank)
@@ -1181,7 +1200,7 @@ def run_gelu_gpu(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic: slots ~ U(-5,5) and U(-8,8) (alternating ciphertexts), seeded; keys and encryptions "
                 "from a SEAL seed",
-        "config": gelu_config(),
+        "config": dict(gelu_config(), tuning=tuning),
         "parity": parity,
         "accuracy": {"max_abs_err_vs_fp64_gelu": errs},
         "roofline": {
@@ -1254,6 +1273,7 @@ def run_keyswitch_gpu(args, rank, world):
     qs = ng.create_coeff_modulus(n, BOOT_BITS)
     limbs, batch = args.ks_limbs, args.ks_batch
     ctx = ng.Context(BOOT_LOGN, qs)
+    _apply_ntt_form(ctx, args)
     k = len(qs)
     g = torch.Generator(device=dev).manual_seed(1)
     qd = torch.tensor(qs, dtype=torch.int64, device=dev)
@@ -1280,7 +1300,8 @@ def run_keyswitch_gpu(args, rank, world):
     return {"metric": "keyswitch_latency_n65536", "value": ms, "unit": "ms per batched call",
             "ms_per_ciphertext": ms / batch, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": False, "dtype": "u64", "data": "uniform random residues and key",
-            "config": {"workload": f"keyswitch_n65536_l{limbs}_{batch}ct", "limbs": limbs, "batch": batch},
+            "config": {"workload": f"keyswitch_n65536_l{limbs}_{batch}ct", "limbs": limbs, "batch": batch,
+                       "ntt_form": ctx.ntt_form()},
             "gpu_launches": ng.kernel_launches() - l0}
 
 
@@ -1405,6 +1426,9 @@ def main():
     ap.add_argument("--impl", choices=["nexus", "reference"], default="nexus")
     ap.add_argument("--workload", choices=["bootstrap", "matmul", "ntt", "gelu", "bert", "keyswitch", "stages"],
                     default="bootstrap")
+    ap.add_argument("--ntt-form", choices=["auto", "0", "1"], default="auto",
+                    help="forward NTT form: 0 two passes, 1 one pass of thread-block clusters, auto the "
+                         "autotuner's choice (the two-pass default where no autotuner runs)")
     ap.add_argument("--ks-limbs", type=int, default=31, help="limbs of the keyswitch workload")
     ap.add_argument("--ks-batch", type=int, default=4, help="ciphertexts per call of the keyswitch workload")
     ap.add_argument("--cpu-depth", type=int, default=7, help="expansion-subtree depth of the MatMul CPU sample")

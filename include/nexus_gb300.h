@@ -115,6 +115,17 @@ int nexus_autotune(nexus_context *ctx, int limbs, int batch, int reps, int *ntt_
 int nexus_set_tuning(nexus_context *ctx, int ntt_prefetch_waves, int ks_inner_ctas_per_sm);
 int nexus_get_tuning(const nexus_context *ctx, int *ntt_prefetch_waves, int *ks_inner_ctas_per_sm);
 
+/*
+ * Form of the forward NTT (every forward transform of the context, the key
+ * switch's ModUp and ModDown included): 0 = two launches, a columns pass and
+ * a rows pass, each reading and writing the limb in HBM (default); 1 = one
+ * launch of thread-block clusters of N/4096 CTAs that keep a limb in their
+ * distributed shared memory between the passes, so the limb crosses HBM
+ * once each way.  Same words either way.
+ */
+int nexus_set_ntt_form(nexus_context *ctx, int form);
+int nexus_get_ntt_form(const nexus_context *ctx, int *form);
+
 /* ------------------------------------------------------------------ */
 /* CKKS ciphertext arithmetic (NTT form, limbs = data primes 0..limbs-1) */
 /* ------------------------------------------------------------------ */

@@ -117,6 +117,8 @@ SIGNATURES = [
                                  C.POINTER(C.c_double)]),
     ("nexus_set_tuning", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("nexus_get_tuning", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("nexus_set_ntt_form", C.c_int, [C.c_void_p, C.c_int]),
+    ("nexus_get_ntt_form", C.c_int, [C.c_void_p, C.c_void_p]),
     ("nexus_butterfly_rate", C.c_int,
      [C.c_int, C.c_uint64, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("nexus_bert_layer_create", C.c_int,

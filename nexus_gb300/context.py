@@ -134,7 +134,8 @@ class Context:
         w, g, ms = C.c_int(), C.c_int(), C.c_double()
         check(lib().nexus_autotune(self._h, int(limbs), int(batch), int(reps), C.byref(w), C.byref(g), C.byref(ms)),
               "nexus_autotune")
-        return {"ntt_prefetch_waves": w.value, "ks_inner_ctas_per_sm": g.value, "ms_per_call": ms.value}
+        return {"ntt_prefetch_waves": w.value, "ks_inner_ctas_per_sm": g.value, "ntt_form": self.ntt_form(),
+                "ms_per_call": ms.value}
 
     def set_tuning(self, ntt_prefetch_waves: int, ks_inner_ctas_per_sm: int) -> None:
         check(lib().nexus_set_tuning(self._h, int(ntt_prefetch_waves), int(ks_inner_ctas_per_sm)), "nexus_set_tuning")
@@ -142,7 +143,17 @@ class Context:
     def tuning(self) -> dict:
         w, g = C.c_int(), C.c_int()
         check(lib().nexus_get_tuning(self._h, C.byref(w), C.byref(g)), "nexus_get_tuning")
-        return {"ntt_prefetch_waves": w.value, "ks_inner_ctas_per_sm": g.value}
+        return {"ntt_prefetch_waves": w.value, "ks_inner_ctas_per_sm": g.value, "ntt_form": self.ntt_form()}
+
+    def set_ntt_form(self, form: int) -> None:
+        """0: forward NTT in two launches (default); 1: one launch of
+        thread-block clusters holding each limb in distributed shared memory."""
+        check(lib().nexus_set_ntt_form(self._h, int(form)), "nexus_set_ntt_form")
+
+    def ntt_form(self) -> int:
+        f = C.c_int()
+        check(lib().nexus_get_ntt_form(self._h, C.byref(f)), "nexus_get_ntt_form")
+        return f.value
 
     def galois_elt(self, step: int) -> int:
         e = C.c_uint32()

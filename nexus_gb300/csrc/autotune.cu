@@ -1,11 +1,12 @@
-// Autotuner of the launch parameters (Context::Tuning): the L2 prefetch
-// distance of the NTT passes and the grid of the key inner product.
+// Autotuner of the launch parameters (Context::Tuning): the form of the
+// forward NTT (two passes, or one pass of thread-block clusters), the L2
+// prefetch distance of the NTT passes and the grid of the key inner product.
 //
 // Both only change how work maps to CTAs and when tiles reach L2, never a
 // result word.  The tuner times a batched key switch -- a ModUp NTT over
 // l(l+1) limbs per ciphertext, the inner product, the ModDown NTTs, the
 // shape that dominates the bootstrap and the layer -- on uniform random
-// residues for every candidate pair, with CUDA events after one warm-up,
+// residues for every candidate, with CUDA events after one warm-up,
 // and keeps the fastest in the context.
 #include <cstdio>
 #include <stdexcept>
@@ -73,24 +74,41 @@ double autotune_keyswitch(Context &c, int l, int B, cudaStream_t s, int reps)
     double best_ms = 1e300;
     const int waves[] = {0, 1, 2, 3, 4};
     const int ctas[] = {0, 4, 8, 16};
+    // milliseconds per call of the current tuning, after one warm-up call
+    auto trial = [&]() {
+        switch_key_batch(c, ct, B, l, tg, key, s);
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < reps; ++r) switch_key_batch(c, ct, B, l, tg, key, s);
+        cudaEventRecord(e1, s);
+        if (cudaEventSynchronize(e1) != cudaSuccess) throw std::runtime_error("autotune: timing failed");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return (double)ms / reps;
+    };
     try {
-        for (int w : waves)
-            for (int g : ctas) {
-                c.tune.ntt_prefetch_waves = w;
-                c.tune.ks_inner_ctas_per_sm = g;
-                switch_key_batch(c, ct, B, l, tg, key, s);   // warm-up
-                cudaEventRecord(e0, s);
-                for (int r = 0; r < reps; ++r) switch_key_batch(c, ct, B, l, tg, key, s);
-                cudaEventRecord(e1, s);
-                if (cudaEventSynchronize(e1) != cudaSuccess) throw std::runtime_error("autotune: timing failed");
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                const double per = (double)ms / reps;
-                if (per < best_ms) {
-                    best_ms = per;
-                    best = c.tune;
+        for (int form = 0; form < 2; ++form) {
+            c.tune.ntt_cluster = form;
+            if (form == 1) {
+                // the cluster form needs clusters of N/4096 CTAs; where the
+                // device refuses them the two-pass form is kept
+                try {
+                    switch_key_batch(c, ct, B, l, tg, key, s);
+                } catch (const std::runtime_error &) {
+                    cudaGetLastError();
+                    break;
                 }
             }
+            for (int w : waves)
+                for (int g : ctas) {
+                    c.tune.ntt_prefetch_waves = w;
+                    c.tune.ks_inner_ctas_per_sm = g;
+                    const double per = trial();
+                    if (per < best_ms) {
+                        best_ms = per;
+                        best = c.tune;
+                    }
+                }
+        }
     } catch (...) {
         c.tune = saved;
         release();

@@ -438,6 +438,22 @@ extern "C" int nexus_get_tuning(const nexus_context *ctx, int *ntt_prefetch_wave
     return 0;
 }
 
+extern "C" int nexus_set_ntt_form(nexus_context *ctx, int form)
+{
+    static const char *fn = "nexus_set_ntt_form";
+    if (!ctx) return fail(fn, "null context");
+    if (form != 0 && form != 1) return fail(fn, "form must be 0 (two passes) or 1 (one cluster pass)");
+    ctx->c.tune.ntt_cluster = form;
+    return 0;
+}
+
+extern "C" int nexus_get_ntt_form(const nexus_context *ctx, int *form)
+{
+    if (!ctx || !form) return fail("nexus_get_ntt_form", "null argument");
+    *form = ctx->c.tune.ntt_cluster;
+    return 0;
+}
+
 extern "C" int nexus_butterfly_rate(int mode, uint64_t q, int rounds, int blocks_per_sm, double *butterflies_per_s,
                                     double *ms)
 {

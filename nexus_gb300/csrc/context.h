@@ -65,6 +65,10 @@ struct Context {
         // key inner product: CTAs per SM of its grid-stride loop; 0 launches
         // one CTA per 512-coefficient chunk
         int ks_inner_ctas_per_sm = 0;
+        // forward NTT: 0 two launches (columns pass, rows pass), 1 one launch
+        // of thread-block clusters that keep each limb in distributed shared
+        // memory between the passes
+        int ntt_cluster = 0;
     } tune;
     int sm_count = 0;                // multiprocessors of `device`
 

@@ -19,7 +19,9 @@
 // Shoup butterflies (values in [0,4q) forward, [0,2q) inverse).
 #include <cstdio>
 #include <stdexcept>
+#include <string>
 #include <vector>
+#include <cooperative_groups.h>
 
 #include "context.h"
 #include "ntt.h"
@@ -323,6 +325,158 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
     for (int k = 0; k < kE; ++k) p[t + T * k] = srow[swz(t + T * k)];
 }
 
+// ------------------------------------------------- forward, one pass per cluster
+//
+// The same two passes in one launch: a cluster of CS = N / 4096 CTAs holds
+// one limb in its shared memory.  CTA rank cr first runs the columns pass on
+// column tile cr (the tile of k_fwd_cols, loaders included) and keeps the
+// result in its own shared memory; after a cluster barrier it reads its R
+// rows from the CS tiles through distributed shared memory (the row's
+// column col lives in CTA col / C at column col % C) into registers, runs
+// the rows pass's first stages there, waits until every peer has read its
+// own tile, reuses that tile for the rows pass's exchange and writes the
+// rows to global memory.  A limb crosses HBM
+// once each way instead of twice.  Each CTA needs only its 32 KB tile, so
+// the cluster scheduler is limited by registers (3 CTAs per SM), not by
+// shared memory.
+template <int L1, int L2>
+struct ClusterShape {
+    static constexpr int T1 = (1 << L1) / kE, C = kThreads / T1;          // columns pass
+    static constexpr int S2 = 1 << L2, T2 = S2 / kE, R = kThreads / T2;   // rows pass
+    static constexpr int CS = (1 << (L1 + L2)) / (kThreads * kE);        // CTAs per limb
+    static constexpr size_t smem_words = (size_t)kThreads * kE;          // one tile
+    static_assert((1 << L2) / C == CS && (1 << L1) / R == CS, "tiles must cover the limb once");
+    static_assert((size_t)R * S2 == smem_words && (size_t)(1 << L1) * C == smem_words, "the exchanges share one tile");
+};
+
+// a cluster-wide barrier with release/acquire ordering of shared memory
+__device__ __forceinline__ void cluster_barrier()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// the 64-bit word at shared-memory offset `addr` of CTA `rank` of this cluster
+__device__ __forceinline__ uint64_t ld_cluster(uint32_t addr, uint32_t rank)
+{
+    uint32_t remote;
+    uint64_t v;
+    asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(addr), "r"(rank));
+    asm volatile("ld.shared::cluster.u64 %0, [%1];" : "=l"(v) : "r"(remote));
+    return v;
+}
+
+// The rows exchange without padding: word s of a row sits at
+// s ^ ((s >> 4) & 15), which keeps both access patterns free of bank
+// conflicts.  For s = t + T*k (t < T <= 16) that is s ^ ((T*k) >> 4), a
+// constant per register k; for s = kE*t + k it is kE*t + (k ^ t).
+template <int T>
+__device__ __forceinline__ int swx_strided(int t, int k) { return (t + T * k) ^ ((T * k) >> 4); }
+__device__ __forceinline__ int swx_blocked(int t, int k) { return kE * t + (k ^ t); }
+
+template <int L1, int L2, int KIND, bool SMALL>
+__global__ void __launch_bounds__(kThreads, 3)
+    k_fwd_cluster(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw, const PrimeConst *__restrict__ pc,
+                  int logn, LimbMap lm, NttLoader ld)
+{
+    using Sh = ClusterShape<L1, L2>;
+    constexpr int T1 = Sh::T1, C = Sh::C, S2 = Sh::S2, T2 = Sh::T2;
+    // the T2 threads of a row sit in one warp (warp barriers order the row exchange)
+    static_assert(32 % T2 == 0, "a row's threads must lie inside one warp");
+    extern __shared__ uint64_t tile[];   // [2^L1][C] after pass 1, then [R][S2] for the rows exchange
+    const unsigned cr = blockIdx.x % (unsigned)Sh::CS;   // rank in the cluster (clusters run along x)
+    const uint32_t pl = blockIdx.x / (unsigned)Sh::CS;
+    size_t lrow;
+    int prime;
+    lm.locate(pl, lrow, prime);
+    const uint64_t q = pc[prime].q, q2 = q << 1;
+    const ulonglong2 *W = tw + ((size_t)prime << logn);
+    const int n2 = S2;
+
+    // pass 1: columns cr * C .. cr * C + C - 1
+    {
+        const int col0 = (int)cr * C;
+        const uint64_t *p = data + (lrow << logn) + col0;
+        const int c = threadIdx.x % C, t = threadIdx.x / C;
+        uint64_t x[kE];
+        if (KIND == 0) {
+#pragma unroll
+            for (int k = 0; k < kE; ++k) x[k] = p[(size_t)(t + T1 * k) * n2 + c];
+        } else {
+            const uint32_t srow = pl / (uint32_t)ld.group;
+            const uint64_t *sp = ld.src + ((size_t)srow << logn) + col0;
+            const uint64_t r1 = pc[prime].r1;
+            if (KIND == 1) {
+                const uint64_t qj = pc[(int)(srow % (uint32_t)ld.src_limbs)].q;
+#pragma unroll
+                for (int k = 0; k < kE; ++k) {
+                    const uint64_t v = sp[(size_t)(t + T1 * k) * n2 + c];
+                    x[k] = (!SMALL && q < qj) ? barrett_64(v, q, r1) : v;
+                }
+            } else {
+                const uint64_t P = pc[ld.special].q, h = P >> 1;
+                const uint64_t hr = (q < P) ? barrett_64(h, q, r1) : h;
+#pragma unroll
+                for (int k = 0; k < kE; ++k) {
+                    const uint64_t v = csub(sp[(size_t)(t + T1 * k) * n2 + c] + h, P);
+                    x[k] = ((!SMALL && q < P) ? barrett_64(v, q, r1) : v) + (q - hr);
+                }
+            }
+        }
+        fwd_regs_strided<SMALL>(x, W, 1, q, q2);
+#pragma unroll
+        for (int k = 0; k < kE; ++k) tile[(t + T1 * k) * C + c] = x[k];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kE; ++k) x[k] = tile[(kE * t + k) * C + c];
+        fwd_regs_blocked<T1, SMALL>(x, W, 1, t, q, q2);
+        // each thread writes back the words it alone read
+#pragma unroll
+        for (int k = 0; k < kE; ++k) tile[(kE * t + k) * C + c] = x[k];
+    }
+    cluster_barrier();
+
+    // pass 2: rows cr * R .. cr * R + R - 1, gathered from the cluster's tiles
+    const int rr = threadIdx.x / T2, t = threadIdx.x % T2;
+    const uint64_t r = (uint64_t)cr * Sh::R + rr;
+    uint64_t x[kE];
+    {
+        const uint32_t row_base = (uint32_t)__cvta_generic_to_shared(tile) + (uint32_t)(r * C) * 8u;
+#pragma unroll
+        for (int k = 0; k < kE; ++k) {
+            const int col = t + T2 * k;
+            x[k] = ld_cluster(row_base + (uint32_t)(col % C) * 8u, (uint32_t)(col / C));
+        }
+    }
+    const uint64_t B = (1ull << (logn - L2)) + r;
+    fwd_regs_strided<SMALL>(x, W, B, q, q2);
+    // every peer has read this CTA's tile: it becomes the rows exchange
+    cluster_barrier();
+    uint64_t *srow = tile + rr * S2;
+#pragma unroll
+    for (int k = 0; k < kE; ++k) srow[swx_strided<T2>(t, k)] = x[k];
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < kE; ++k) x[k] = srow[swx_blocked(t, k)];
+    fwd_regs_blocked<T2, SMALL>(x, W, B, t, q, q2);
+    if (SMALL) {
+        const uint64_t r1 = pc[prime].r1;
+        if (r1 >> 32) {
+#pragma unroll
+            for (int k = 0; k < kE; ++k) srow[swx_blocked(t, k)] = barrett_64(x[k], q, r1);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kE; ++k) srow[swx_blocked(t, k)] = barrett_64_r32(x[k], q, (uint32_t)r1);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kE; ++k) srow[swx_blocked(t, k)] = csub(csub(x[k], q2), q);
+    }
+    __syncwarp();
+    uint64_t *p = data + (lrow << logn) + r * S2;
+#pragma unroll
+    for (int k = 0; k < kE; ++k) p[t + T2 * k] = srow[swx_strided<T2>(t, k)];
+}
+
 // ---------------------------------------------------------------- inverse
 
 // Inverse pass A: rows first (undoing pass 2).  Output in [0,2q).
@@ -409,10 +563,49 @@ __global__ void __launch_bounds__(kThreads, 3) k_inv_cols(uint64_t *__restrict__
     for (int k = 0; k < kE; ++k) p[(size_t)(t + T * k) * n2 + c] = mul_shoup(x[k], P.inv_n, P.inv_n_q, q);
 }
 
+// one cluster of ClusterShape::CS CTAs per limb
+template <int L1, int L2, int KIND, bool SMALL>
+void launch_cluster_k(const Context &c, uint64_t *d, size_t limbs, LimbMap lm, NttLoader ld, cudaStream_t s)
+{
+    using Sh = ClusterShape<L1, L2>;
+    auto kern = k_fwd_cluster<L1, L2, KIND, SMALL>;
+    const size_t smem = Sh::smem_words * sizeof(uint64_t);
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        (Sh::CS > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess))
+        throw std::runtime_error("NTT cluster form: kernel attributes refused");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(limbs * Sh::CS));
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = Sh::CS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw std::runtime_error(std::string("NTT cluster form: launch failed: ") + cudaGetErrorString(e));
+    }
+    NEXUS_LAUNCHED();
+}
+
 template <int L1, int L2, bool SMALL>
 void launch_fwd_t(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cudaStream_t s, NttLoader ld)
 {
     const size_t limbs = n_polys * (size_t)lm.count;
+    if (c.tune.ntt_cluster) {
+        if (ld.kind == 1)
+            launch_cluster_k<L1, L2, 1, SMALL>(c, d, limbs, lm, ld, s);
+        else if (ld.kind == 2)
+            launch_cluster_k<L1, L2, 2, SMALL>(c, d, limbs, lm, ld, s);
+        else
+            launch_cluster_k<L1, L2, 0, SMALL>(c, d, limbs, lm, ld, s);
+        return;
+    }
     constexpr int C = kThreads / ((1 << L1) / kE);
     constexpr int R = kThreads / ((1 << L2) / kE);
     const unsigned g1 = (unsigned)(limbs * ((1u << L2) / C));

@@ -61,6 +61,8 @@ def test_lockstep_and_hoisting_entry_points_reject_null_arguments_without_gpu():
          b"null"),
         ("nexus_autotune", lambda: lib.nexus_autotune(None, 1, 1, 1, None, None, None), b"null"),
         ("nexus_set_tuning", lambda: lib.nexus_set_tuning(None, 0, 0), b"null"),
+        ("nexus_set_ntt_form", lambda: lib.nexus_set_ntt_form(None, 1), b"null"),
+        ("nexus_get_ntt_form", lambda: lib.nexus_get_ntt_form(None, None), b"null"),
     ]
     for name, call, word in cases:
         assert call() != 0, name
