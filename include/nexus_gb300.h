@@ -535,6 +535,18 @@ int nexus_bootstrapper_destroy(nexus_bootstrapper *bs);
 int nexus_bootstrapper_prepare_mod_polynomial(nexus_bootstrapper *bs, int heap_k, int heap_m, const int *node_len,
                                               const double *coeffs, double scale_inverse_coeff);
 
+/* ModularReducer::generate_inverse_sine_polynomial (ModularReducer.cpp:38-47)
+ * for inverse_deg > 1: the inverse-sine polynomial that EvalMod evaluates
+ * after the unscaled double angles (:62-73).  power holds its deg + 1
+ * power-basis coefficients (the direct forms of degree <= 3 read them,
+ * common/Polynomial.cpp:257-325); above degree 3 its odd heap
+ * (generate_poly_heap_odd, :207-210) follows in the layout of
+ * nexus_bootstrapper_prepare_mod_polynomial.  deg must equal the
+ * bootstrapper's inverse_deg; the cosine heap given to
+ * prepare_mod_polynomial is then the unscaled one. */
+int nexus_bootstrapper_set_inverse_polynomial(nexus_bootstrapper *bs, int deg, const double *power, int heap_k,
+                                              int heap_m, const int *node_len, const double *coeffs);
+
 /* Bootstrapper::addLeftRotKeys_Linear_to_vector_3 (Bootstrapper.cpp:89-184):
  * appends the missing rotation steps to steps[0..*count) (capacity entries). */
 int nexus_bootstrapper_add_rot_steps(const nexus_bootstrapper *bs, int *steps, int *count, int capacity);

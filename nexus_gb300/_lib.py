@@ -90,6 +90,8 @@ SIGNATURES = [
     ("nexus_bootstrapper_destroy", C.c_int, [C.c_void_p]),
     ("nexus_bootstrapper_prepare_mod_polynomial", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int),
                                                             C.POINTER(C.c_double), C.c_double]),
+    ("nexus_bootstrapper_set_inverse_polynomial", C.c_int,
+     [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     ("nexus_bootstrapper_add_rot_steps", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]),
     ("nexus_bootstrapper_generate_lt", C.c_int, [C.c_void_p]),
     ("nexus_lt_coefficients_3", C.c_int, [C.c_int, C.c_int, C.c_long, C.c_int, C.c_void_p, C.POINTER(C.c_int),

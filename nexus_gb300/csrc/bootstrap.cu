@@ -74,6 +74,22 @@ void ModularReducerT<EV, CT>::set_polynomial_heap(long k, long m, std::vector<st
 }
 
 template <class EV, class CT>
+void ModularReducerT<EV, CT>::set_inverse_polynomial(InversePoly p)
+{
+    const long d = (long)p.power.size() - 1;
+    if (d < 1) throw std::invalid_argument("inverse-sine polynomial: no coefficients");
+    if (d > 3) {
+        const long k = p.heap_k, m = p.heap_m;
+        if (k < 2 || m < 1 || p.heap.size() != (size_t)((1 << (m + 1)) - 1) || p.heap[0].empty())
+            throw std::invalid_argument("inverse-sine polynomial: malformed heap");
+        for (size_t i = (size_t)(1 << m) - 1; i < p.heap.size(); i++)
+            if (!p.heap[i].empty() && (p.heap[i].size() < 2 || p.heap[i].size() > (size_t)k + 1))
+                throw std::invalid_argument("inverse-sine polynomial: malformed heap");
+    }
+    inverse = std::move(p);
+}
+
+template <class EV, class CT>
 void ModularReducerT<EV, CT>::double_angle_formula(CT &cipher)
 {
     ev_->square_inplace(cipher);
@@ -100,13 +116,68 @@ void ModularReducerT<EV, CT>::double_angle_formula_scaled(CT &cipher, double sca
 template <class EV, class CT>
 void ModularReducerT<EV, CT>::homomorphic_poly_evaluation(CT &rtn, const CT &cipher)
 {
+    evaluate_heap(rtn, cipher, heap_k, heap_m, heap);
+}
+
+// The direct forms of Polynomial::homomorphic_poly_evaluation for degree
+// 1, 2 and 3 (common/Polynomial.cpp:257-325), on the power-basis
+// coefficients; a term whose coefficient is below 1 / scale is left out
+// where the reference leaves it out.
+template <class EV, class CT>
+void ModularReducerT<EV, CT>::evaluate_power(CT &rtn, const CT &cipher, const std::vector<double> &coeff)
+{
     EV &ev = *ev_;
     const double zero = 1. / cipher.scale();
-    // the reference evaluates polynomials of degree 1..3 directly on their
-    // power-basis coefficients; only the heap path is used for EvalMod
-    if ((long)heap[0].size() - 1 < 4 || heap_m < 1)
+    const size_t d = coeff.size() - 1;
+    if (d == 1) {
+        ev.multiply_const_rescale(cipher, coeff[1], rtn);
+        ev.add_const_inplace(rtn, coeff[0]);
+        return;
+    }
+    if (d == 2) {
+        CT squared;
+        ev.square(cipher, squared);
+        ev.relinearize_inplace(squared);
+        ev.rescale_to_next_inplace(squared);
+        ev.multiply_const_rescale(squared, coeff[2], squared);
+        if (std::fabs(coeff[1]) >= zero) {
+            ev.multiply_const_rescale(cipher, coeff[1], rtn);
+            ev.add_inplace_reduced_error(rtn, squared);
+        } else {
+            rtn = std::move(squared);
+        }
+        ev.add_const_inplace(rtn, coeff[0]);
+        return;
+    }
+    if (d != 3) throw std::invalid_argument("evaluate_power: degree 1, 2 or 3 expected");
+    CT squared, cubic;
+    ev.square(cipher, squared);
+    ev.relinearize_inplace(squared);
+    ev.rescale_to_next_inplace(squared);
+    ev.multiply_const_rescale(cipher, coeff[3], cubic);
+    ev.multiply_inplace_reduced_error(cubic, squared);
+    ev.rescale_to_next_inplace(cubic);
+    if (std::fabs(coeff[1]) >= zero) {
+        ev.multiply_const_rescale(cipher, coeff[1], rtn);
+        ev.add_inplace_reduced_error(rtn, cubic);
+    } else {
+        rtn = std::move(cubic);
+    }
+    if (std::fabs(coeff[2]) >= zero) {
+        ev.multiply_const_rescale(squared, coeff[2], squared);
+        ev.add_inplace_reduced_error(rtn, squared);
+    }
+    ev.add_const_inplace(rtn, coeff[0]);
+}
+
+template <class EV, class CT>
+void ModularReducerT<EV, CT>::evaluate_heap(CT &rtn, const CT &cipher, long k, long m,
+                                            const std::vector<std::vector<double>> &heap)
+{
+    EV &ev = *ev_;
+    const double zero = 1. / cipher.scale();
+    if (heap.empty() || (long)heap[0].size() - 1 < 4 || m < 1)
         throw std::invalid_argument("homomorphic_poly_evaluation: polynomial heap of degree >= 4 expected");
-    const long k = heap_k, m = heap_m;
     std::vector<CT> baby(k);
     std::vector<bool> have(k, false);
     baby[1] = cipher;
@@ -196,15 +267,24 @@ template <class EV, class CT>
 void ModularReducerT<EV, CT>::modular_reduction(CT &rtn, const CT &cipher)
 {
     if (heap.empty()) throw std::logic_error("prepare_mod_polynomial has not been called");
-    if (inverse_deg != 1) throw std::invalid_argument("only inverse_deg == 1 (scaled double angle) is supported");
     CT tmp2;
     homomorphic_poly_evaluation(tmp2, cipher);
-    double curr_scale = scale_inverse_coeff;
-    for (long i = 0; i < num_double_formula; i++) {
-        curr_scale = curr_scale * curr_scale;
-        double_angle_formula_scaled(tmp2, curr_scale);
+    if (inverse_deg == 1) {
+        double curr_scale = scale_inverse_coeff;
+        for (long i = 0; i < num_double_formula; i++) {
+            curr_scale = curr_scale * curr_scale;
+            double_angle_formula_scaled(tmp2, curr_scale);
+        }
+        rtn = std::move(tmp2);
+        return;
     }
-    rtn = std::move(tmp2);
+    if ((long)inverse.power.size() != inverse_deg + 1)
+        throw std::logic_error("the inverse-sine polynomial has not been set for this inverse_deg");
+    for (long i = 0; i < num_double_formula; i++) double_angle_formula(tmp2);
+    if (inverse_deg <= 3)
+        evaluate_power(rtn, tmp2, inverse.power);
+    else
+        evaluate_heap(rtn, tmp2, inverse.heap_k, inverse.heap_m, inverse.heap);
 }
 
 // ------------------------------------------------------------ Bootstrapper
@@ -873,7 +953,7 @@ static void evalmod_halves(ModularReducerT<Evaluator, Ciphertext> &mr, Evaluator
     BatchEvaluator bev(ev);
     ModularReducerT<BatchEvaluator, CtBatch> bmr(bev, mr.boundary_K, mr.log_width, mr.deg, mr.num_double_formula,
                                                  mr.inverse_deg);
-    bmr.set_polynomial_heap(mr.heap_k, mr.heap_m, mr.heap, mr.scale_inverse_coeff);
+    bmr.adopt_polynomials(mr);
     const size_t words = (size_t)r1.size() * r1.limbs() * c.n;
     CtBatch both, m;
     both.resize(c, 2, r1.size(), r1.limbs(), s);

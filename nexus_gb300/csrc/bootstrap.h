@@ -46,17 +46,43 @@ public:
     long inverse_deg;
     double scale_inverse_coeff = 1.0;
 
-    // Polynomial heap of the scaled cosine (generate_poly_heap): node i holds
-    // its Chebyshev coefficients; an empty node is absent.
+    // Polynomial heap of the cosine (generate_poly_heap; scaled when
+    // inverse_deg == 1): node i holds its Chebyshev coefficients; an empty
+    // node is absent.
     long heap_k = 0, heap_m = 0;
     std::vector<std::vector<double>> heap;
 
+    // The inverse-sine polynomial of inverse_deg > 1 (generate_inverse_sine_
+    // polynomial, ModularReducer.cpp:38-47): its power-basis coefficients,
+    // which the direct forms of degree <= 3 read, and above degree 3 its odd
+    // heap (generate_poly_heap_odd).
+    struct InversePoly {
+        std::vector<double> power;
+        long heap_k = 0, heap_m = 0;
+        std::vector<std::vector<double>> heap;
+    } inverse;
+
     ModularReducerT(EV &ev, long boundary_K, double log_width, long deg, long num_double_formula, long inverse_deg);
     void set_polynomial_heap(long k, long m, std::vector<std::vector<double>> nodes, double scale_inverse_coeff);
+    void set_inverse_polynomial(InversePoly p);
+    template <class EV2, class CT2>
+    void adopt_polynomials(const ModularReducerT<EV2, CT2> &o)
+    {
+        set_polynomial_heap(o.heap_k, o.heap_m, o.heap, o.scale_inverse_coeff);
+        inverse.power = o.inverse.power;
+        inverse.heap_k = o.inverse.heap_k;
+        inverse.heap_m = o.inverse.heap_m;
+        inverse.heap = o.inverse.heap;
+    }
 
     void double_angle_formula(CT &cipher);
     void double_angle_formula_scaled(CT &cipher, double scale_coeff);
+    // Polynomial::homomorphic_poly_evaluation of the cosine heap
     void homomorphic_poly_evaluation(CT &rtn, const CT &cipher);
+    // the same routine for any heap of degree >= 4 ...
+    void evaluate_heap(CT &rtn, const CT &cipher, long k, long m, const std::vector<std::vector<double>> &nodes);
+    // ... and its direct forms for degree 1-3 on power-basis coefficients
+    void evaluate_power(CT &rtn, const CT &cipher, const std::vector<double> &coeff);
     void modular_reduction(CT &rtn, const CT &cipher);
 
 private:
@@ -94,8 +120,7 @@ public:
         invfftcoeff2 = o.invfftcoeff2;
         invfftcoeff3 = o.invfftcoeff3;
         final_scale = o.final_scale;
-        mod_reducer.set_polynomial_heap(o.mod_reducer.heap_k, o.mod_reducer.heap_m, o.mod_reducer.heap,
-                                        o.mod_reducer.scale_inverse_coeff);
+        mod_reducer.adopt_polynomials(o.mod_reducer);
         cache_.clear();
     }
 

@@ -100,6 +100,36 @@ extern "C" int nexus_bootstrapper_prepare_mod_polynomial(nexus_bootstrapper *bs,
     });
 }
 
+extern "C" int nexus_bootstrapper_set_inverse_polynomial(nexus_bootstrapper *bs, int deg, const double *power,
+                                                         int heap_k, int heap_m, const int *node_len,
+                                                         const double *coeffs)
+{
+    static const char *fn = "nexus_bootstrapper_set_inverse_polynomial";
+    if (!bs || !power) return fail(fn, "null argument");
+    if (deg < 1 || deg > 255) return fail(fn, "deg out of range");
+    if (deg > 3 && (!node_len || !coeffs)) return fail(fn, "null argument");
+    if (deg > 3 && (heap_m < 1 || heap_m > 16)) return fail(fn, "heap_m out of range");
+    if (bs->bs.inverse_deg != deg) return fail(fn, "deg differs from the bootstrapper's inverse_deg");
+    return guarded(fn, [&] {
+        ModularReducerT<Evaluator, Ciphertext>::InversePoly p;
+        p.power.assign(power, power + deg + 1);
+        if (deg > 3) {
+            const int len = (1 << (heap_m + 1)) - 1;
+            p.heap_k = heap_k;
+            p.heap_m = heap_m;
+            p.heap.resize(len);
+            size_t off = 0;
+            for (int i = 0; i < len; i++) {
+                if (node_len[i] < 0) throw std::invalid_argument("negative node length");
+                p.heap[i].assign(coeffs + off, coeffs + off + node_len[i]);
+                off += (size_t)node_len[i];
+            }
+        }
+        bs->bs.mod_reducer.set_inverse_polynomial(std::move(p));
+        bs->bbs.reset();
+    });
+}
+
 extern "C" int nexus_bootstrapper_add_rot_steps(const nexus_bootstrapper *bs, int *steps, int *count, int capacity)
 {
     static const char *fn = "nexus_bootstrapper_add_rot_steps";

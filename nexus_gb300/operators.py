@@ -276,7 +276,8 @@ class Bootstrapper:
 
     def prepare_mod_polynomial(self, table: dict | None = None):
         """Load the EvalMod heap (nexus_gb300.remez.load_table for this
-        Bootstrapper's parameters unless a table is given)."""
+        Bootstrapper's parameters unless a table is given), and for
+        inverse_deg > 1 the inverse-sine polynomial."""
         from .remez import load_table
         t = table or load_table(**self.params)
         size = (1 << (t["heap_m"] + 1)) - 1
@@ -286,6 +287,20 @@ class Bootstrapper:
         check(lib().nexus_bootstrapper_prepare_mod_polynomial(self._h, t["heap_k"], t["heap_m"], lens, coeffs,
                                                               float(t["scale_inverse_coeff"])),
               "nexus_bootstrapper_prepare_mod_polynomial")
+        inv = t.get("inverse")
+        if inv is not None:
+            d = int(inv["deg"])
+            power = (C.c_double * (d + 1))(*inv["power"])
+            if d > 3:
+                isize = (1 << (inv["heap_m"] + 1)) - 1
+                ilens = (C.c_int * isize)(*[len(inv["nodes"].get(i, [])) for i in range(isize)])
+                iflat = [c for i in range(isize) for c in inv["nodes"].get(i, [])]
+                icoeffs = (C.c_double * len(iflat))(*iflat)
+                hk, hm = inv["heap_k"], inv["heap_m"]
+            else:
+                ilens, icoeffs, hk, hm = None, None, 0, 0
+            check(lib().nexus_bootstrapper_set_inverse_polynomial(self._h, d, power, hk, hm, ilens, icoeffs),
+                  "nexus_bootstrapper_set_inverse_polynomial")
 
     def addLeftRotKeys_Linear_to_vector_3(self, gal_steps_vector: list) -> None:
         cap = len(gal_steps_vector) + 256

@@ -14,10 +14,15 @@ Restates the setup NEXUS runs once per Bootstrapper in high precision
   The extrema are located by golden-section search to full working
   precision (the reference scans with a step of width/2^9.5 and refines with
   10 bisections), so the result is the minimax polynomial itself.
-* ``RemezArcsin`` (RemezArcsin.h:5-13) of degree 1 on [-w, w] with
-  w = sin(2*pi*2^-loge), whose linear coefficient becomes
-  ``scale_inverse_coeff`` after ``r`` square roots and scales the cosine
-  polynomial (ModularReducer.cpp:11-16,38-46).
+* ``RemezArcsin`` (RemezArcsin.h:5-13) of degree ``inverse_deg`` on
+  [-w, w] with w = sin(2*pi*2^-loge).  For degree 1 its linear coefficient
+  becomes ``scale_inverse_coeff`` after ``r`` square roots and scales the
+  cosine polynomial (ModularReducer.cpp:11-16,38-46); for higher degrees the
+  cosine stays unscaled and the inverse-sine polynomial is evaluated after
+  the double angles (:62-73), directly from its power-basis coefficients up
+  to degree 3 and through an odd heap (``generate_poly_heap_odd``,
+  common/Polynomial.cpp:207-210, ``oddbabycount`` common/func.cpp:95-118)
+  above.
 * ``Polynomial::generate_poly_heap`` (common/Polynomial.cpp:168-214,
   ``babycount`` common/func.cpp:120-142): the polynomial is split by
   T_{k 2^(m-1)}, ..., T_k into a heap whose leaves (degree < k) are what
@@ -56,10 +61,40 @@ def babycount(deg: int) -> tuple[int, int]:
     return mink, minm
 
 
+def oddbabycount(deg: int) -> tuple[int, int]:
+    """(k, m) of common/func.cpp:95-118 for an odd polynomial's heap: even k,
+    the split whose depth matches ceil(log2(deg)) with the fewest estimated
+    products (natural log in its ceil(log(k)) term, as written there)."""
+    mink = minm = 0
+    mind = 0
+    mineval = 100000
+    for k in range(2, deg + 1, 2):
+        m = 1
+        while (1 << m) * k < deg:
+            m += 1
+        if math.ceil(math.log(k) / math.log(2)) + m != math.ceil(math.log(deg) / math.log(2)):
+            continue
+        ev = (math.ceil(deg / k) + k // 2 - 5 + m + math.ceil(math.log(k))
+              + max(3.0 - m, math.ceil(deg / (1.5 * (1 << (m - 1)) * k))))
+        depth = math.ceil(math.log(k) / math.log(2)) + m
+        if mineval > ev:
+            mineval, mink, minm, mind = int(ev), k, m, depth
+        elif mineval == ev and mind > depth:
+            mink, minm, mind = k, m, depth
+    return mink, minm
+
+
+def _parse_heap(nodes: dict) -> dict:
+    return {int(k): [float.fromhex(c) for c in v] for k, v in nodes.items()}
+
+
 def load_table(boundary_k=25, deg=59, loge=10, double_angle=2, inverse_deg=1) -> dict:
     """The committed heap table: {"heap_k", "heap_m", "nodes": {index: [cheb coeffs]},
     "scale_inverse_coeff", ...} with every coefficient the double the
-    homomorphic evaluation encodes."""
+    homomorphic evaluation encodes.  With inverse_deg > 1 it also holds
+    "inverse": {"deg", "power": [power-basis coefficients], and for deg > 3
+    "heap_k", "heap_m", "nodes"} -- the inverse-sine polynomial evaluated
+    after the double angles."""
     path = DATA_DIR / table_name(boundary_k, deg, loge, double_angle, inverse_deg)
     if not path.exists():
         raise FileNotFoundError(f"no EvalMod table for K={boundary_k} deg={deg} loge={loge} "
@@ -67,8 +102,13 @@ def load_table(boundary_k=25, deg=59, loge=10, double_angle=2, inverse_deg=1) ->
                                 "generate it with python -m nexus_gb300.remez")
     with open(path) as f:
         t = json.load(f)
-    t["nodes"] = {int(k): [float.fromhex(c) for c in v] for k, v in t["nodes"].items()}
+    t["nodes"] = _parse_heap(t["nodes"])
     t["scale_inverse_coeff"] = float.fromhex(t["scale_inverse_coeff"])
+    inv = t.get("inverse")
+    if inv is not None:
+        inv["power"] = [float.fromhex(c) for c in inv["power"]]
+        if "nodes" in inv:
+            inv["nodes"] = _parse_heap(inv["nodes"])
     return t
 
 
@@ -336,8 +376,8 @@ def generate(boundary_k=25, deg=59, loge=10, double_angle=2, inverse_deg=1, prec
     """Run the setup and return the table dict (doubles as hex strings)."""
     import mpmath as mp
 
-    if inverse_deg != 1:
-        raise NotImplementedError("only the inverse_deg == 1 path (scaled double angle) is tabulated")
+    if inverse_deg < 1:
+        raise ValueError("inverse_deg must be at least 1")
     scale_factor = 1 << double_angle
     mp.mp.prec = remez_prec
     width = mp.mpf(2) ** (-loge)
@@ -356,27 +396,44 @@ def generate(boundary_k=25, deg=59, loge=10, double_angle=2, inverse_deg=1, prec
     def fasin(x):
         return mp.asin(x) / (2 * mp.pi)
 
-    inv_cheb, inv_err, inv_iters = remez(fasin, 1, w_inv, 1, log_width=inverse_log_width)
-    s = float(inv_cheb[1])
-    for _ in range(double_angle):
-        s = math.sqrt(s)
+    inv_cheb, inv_err, inv_iters = remez(fasin, 1, w_inv, inverse_deg, log_width=inverse_log_width)
+
+    def hexheap(heap):
+        return {str(idx): [float(c).hex() for c in node.cheb] for idx, node in sorted(heap.items())}
 
     mp.mp.prec = prec
-    scaled = [mp.mpf(c) * mp.mpf(s) for c in cheb]
     heap_k, heap_m = babycount(deg)
-    heap = poly_heap(scaled, heap_k, heap_m)
-    nodes = {}
-    for idx, node in sorted(heap.items()):
-        nodes[str(idx)] = [float(c).hex() for c in node.cheb]
-    return {
+    out = {
         "boundary_K": boundary_k, "deg": deg, "loge": loge, "double_angle": double_angle,
         "inverse_deg": inverse_deg, "heap_k": heap_k, "heap_m": heap_m,
-        "scale_inverse_coeff": s.hex(),
         "cos_cheb": [float(c).hex() for c in cheb],
         "cos_levelled_error": float(cos_err), "cos_remez_iterations": cos_iters,
         "arcsin_c1": float(inv_cheb[1]).hex(), "arcsin_levelled_error": float(inv_err),
-        "nodes": nodes,
     }
+    if inverse_deg == 1:
+        # generate_inverse_sine_polynomial (ModularReducer.cpp:38-46): the
+        # linear coefficient, square-rooted once per double angle, scales
+        # the cosine polynomial
+        s = float(inv_cheb[1])
+        for _ in range(double_angle):
+            s = math.sqrt(s)
+        scaled = [mp.mpf(c) * mp.mpf(s) for c in cheb]
+        out["scale_inverse_coeff"] = s.hex()
+        out["nodes"] = hexheap(poly_heap(scaled, heap_k, heap_m))
+        return out
+    # inverse_deg > 1: the cosine is used as it is, and the inverse-sine
+    # polynomial (power basis for the direct forms of degree <= 3, an odd
+    # heap for higher degrees) follows the unscaled double angles
+    out["scale_inverse_coeff"] = (1.0).hex()
+    out["nodes"] = hexheap(poly_heap(cheb, heap_k, heap_m))
+    inv = {"deg": inverse_deg, "power": [float(c).hex() for c in _cheb_to_power(inv_cheb)],
+           "remez_iterations": inv_iters}
+    if inverse_deg > 3:
+        ik, im = oddbabycount(inverse_deg)
+        inv["heap_k"], inv["heap_m"] = ik, im
+        inv["nodes"] = hexheap(poly_heap(inv_cheb, ik, im))
+    out["inverse"] = inv
+    return out
 
 
 def main(argv=None):

@@ -288,13 +288,16 @@ class Bootstrapper:
         self.sin_cos_deg = sin_cos_deg
         self.num_double_formula = scale_factor
         self.inverse_deg = inverse_deg
-        if inverse_deg != 1:
-            raise NotImplementedError("only inverse_deg == 1 is restated")
         if table["deg"] != sin_cos_deg or table["boundary_K"] != boundary_k or table["double_angle"] != scale_factor:
             raise ValueError("EvalMod table does not match the parameters")
+        if table.get("inverse_deg", 1) != inverse_deg:
+            raise ValueError("EvalMod table is for another inverse_deg")
         self.heap_k, self.heap_m = table["heap_k"], table["heap_m"]
         self.heap = table["nodes"]
         self.scale_inverse_coeff = table["scale_inverse_coeff"]
+        self.inverse = table.get("inverse")
+        if inverse_deg > 1 and (self.inverse is None or len(self.inverse["power"]) != inverse_deg + 1):
+            raise ValueError("EvalMod table lacks the inverse-sine polynomial")
         self.fftcoeff = self.invfftcoeff = None
 
     # -- setup ---------------------------------------------------------------
@@ -468,8 +471,38 @@ class Bootstrapper:
 
     # -- EvalMod (ModularReducer.cpp, Polynomial.cpp:255-485) -----------------
     def homomorphic_poly_evaluation(self, ct):
+        return self.evaluate_heap(ct, self.heap_k, self.heap_m, self.heap)
+
+    def evaluate_power(self, ct, coeff):
+        """Polynomial::homomorphic_poly_evaluation for degree 1-3
+        (Polynomial.cpp:257-325) on the power-basis coefficients."""
         ev = self.ev
-        k, m = self.heap_k, self.heap_m
+        zero = 1.0 / ct.scale
+        d = len(coeff) - 1
+        if d == 1:
+            return ev.add_const(ev.rescale(ev.multiply_const(ct, coeff[1])), coeff[0])
+        squared = ev.rescale(ev.relinearize(ev.square(ct)))
+        if d == 2:
+            squared = ev.rescale(ev.multiply_const(squared, coeff[2]))
+            if abs(coeff[1]) >= zero:
+                rtn = ev.add_reduced_error(ev.rescale(ev.multiply_const(ct, coeff[1])), squared)
+            else:
+                rtn = squared
+            return ev.add_const(rtn, coeff[0])
+        if d != 3:
+            raise ValueError("degree 1, 2 or 3 expected")
+        cubic = ev.rescale(ev.multiply_const(ct, coeff[3]))
+        cubic = ev.rescale(ev.multiply_reduced_error(cubic, squared))
+        if abs(coeff[1]) >= zero:
+            rtn = ev.add_reduced_error(ev.rescale(ev.multiply_const(ct, coeff[1])), cubic)
+        else:
+            rtn = cubic
+        if abs(coeff[2]) >= zero:
+            rtn = ev.add_reduced_error(rtn, ev.rescale(ev.multiply_const(squared, coeff[2])))
+        return ev.add_const(rtn, coeff[0])
+
+    def evaluate_heap(self, ct, k, m, nodes):
+        ev = self.ev
         baby = [None] * k
         baby[1] = ct
         i = 2
@@ -504,7 +537,7 @@ class Bootstrapper:
         zero = 1.0 / ct.scale
         first, last = (1 << m) - 1, (1 << (m + 1)) - 1
         for i in range(first, last):
-            coeffs = self.heap.get(i)
+            coeffs = nodes.get(i)
             if coeffs is None:
                 continue
             h = ev.rescale(ev.multiply_const(baby[1], coeffs[1]))
@@ -521,7 +554,7 @@ class Bootstrapper:
         while depth:
             depth -= 1
             for i in range((1 << depth) - 1, (1 << (depth + 1)) - 1):
-                if i not in self.heap:
+                if i not in nodes:
                     continue
                 left, right = 2 * (i + 1) - 1, 2 * (i + 1)
                 if left not in heap:
@@ -533,15 +566,25 @@ class Bootstrapper:
         return heap[0]
 
     def modular_reduction(self, ct):
-        """ModularReducer::modular_reduction (:58-78), inverse_deg == 1 branch."""
+        """ModularReducer::modular_reduction (:58-78): the cosine, then the
+        scaled double angles (inverse_deg == 1) or the plain double angles
+        and the inverse-sine polynomial (inverse_deg > 1)."""
         ev = self.ev
         t = self.homomorphic_poly_evaluation(ct)
-        s = self.scale_inverse_coeff
+        if self.inverse_deg == 1:
+            s = self.scale_inverse_coeff
+            for _ in range(self.num_double_formula):
+                s = s * s
+                t = ev.rescale(ev.relinearize(ev.square(t)))
+                t = ev.add_const(ev.add(t, t), -s)
+            return t
         for _ in range(self.num_double_formula):
-            s = s * s
             t = ev.rescale(ev.relinearize(ev.square(t)))
-            t = ev.add_const(ev.add(t, t), -s)
-        return t
+            t = ev.add_const(ev.add(t, t), -1.0)
+        inv = self.inverse
+        if self.inverse_deg <= 3:
+            return self.evaluate_power(t, inv["power"])
+        return self.evaluate_heap(t, inv["heap_k"], inv["heap_m"], inv["nodes"])
 
     # -- API ---------------------------------------------------------------------
     def bootstrap_full_3(self, ct):

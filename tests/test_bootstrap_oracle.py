@@ -149,3 +149,78 @@ def test_oracle_bootstrap_decrypts_to_input(logn):
     assert out.scale == 2.0 ** 46
     err = np.abs(s.decrypt(out.data, out.scale) - vals)
     assert err.max() < 2.0 ** -12
+
+
+def test_oddbabycount():
+    from nexus_gb300.remez import oddbabycount
+    # common/func.cpp:95-118, worked by hand for 5 and 7
+    assert oddbabycount(5) == (2, 2) and oddbabycount(7) == (4, 1)
+    assert oddbabycount(15) == (4, 2) and oddbabycount(31) == (8, 2)
+
+
+@pytest.mark.parametrize("inverse_deg", [3, 5])
+def test_evalmod_inverse_sine_tables(inverse_deg):
+    """inverse_deg > 1: the cosine stays unscaled, the inverse-sine polynomial
+    (power basis, and its odd heap above degree 3) follows the plain double
+    angles, and the composition is x - round(x)."""
+    from nexus_gb300.remez import load_table
+    tb = load_table(inverse_deg=inverse_deg)
+    inv = tb["inverse"]
+    assert inv["deg"] == inverse_deg and len(inv["power"]) == inverse_deg + 1
+    assert tb["scale_inverse_coeff"] == 1.0
+    base = load_table()
+    assert tb["cos_cheb"] == base["cos_cheb"]
+    w = 2.0 ** -tb["loge"]
+    xs = np.concatenate([np.linspace(i - w, i + w, 41) for i in range(-(K - 1), K)])
+    y = np.polynomial.chebyshev.chebval(xs / K, tb["nodes"][0])
+    assert np.abs(y - np.cos(2 * np.pi * (xs - 0.25) / 4)).max() <= tb["cos_levelled_error"] * 1.01 + 1e-15
+    for _ in range(tb["double_angle"]):
+        y = 2 * y * y - 1.0
+    p = np.polynomial.polynomial.polyval(y, inv["power"])
+    assert np.abs(p - (xs - np.round(xs))).max() < 1e-8
+    # odd polynomial: the even coefficients vanish below any ciphertext scale
+    assert all(abs(c) < 1e-60 for c in inv["power"][0::2])
+    if inverse_deg > 3:
+        k, m = inv["heap_k"], inv["heap_m"]
+        nodes = inv["nodes"]
+        first = (1 << m) - 1
+
+        def heap_value(i, g, t):
+            if i >= first:
+                return np.polynomial.chebyshev.chebval(t, nodes[i]) if i in nodes else 0.0
+            left, right = 2 * i + 1, 2 * i + 2
+            if left not in nodes:
+                return heap_value(right, g + 1, t)
+            return heap_value(left, g + 1, t) * _cheb_t((k << m) >> (g + 1), t) + heap_value(right, g + 1, t)
+
+        t = np.linspace(-0.01, 0.01, 101)
+        assert np.abs(heap_value(0, 0, t) - np.polynomial.polynomial.polyval(t, inv["power"])).max() < 1e-15
+
+
+@pytest.mark.parametrize("inverse_deg", [3, 5])
+def test_oracle_bootstrap_with_inverse_sine(inverse_deg):
+    """ModularReducer's inverse_deg > 1 branch (ModularReducer.cpp:62-73) in a
+    full-slot bootstrap with SEAL's keys: the refreshed ciphertext decrypts
+    to the input (the chain has three more bootstrapping primes for the
+    polynomial's levels)."""
+    from oracle import nexus_l3 as L
+    from oracle import pyoracle as po
+    from oracle import pyref as pr
+    from nexus_gb300.remez import load_table
+    if not pr.available():
+        pytest.skip("SEAL reference build unavailable")
+    log_n, logn = 13, 12
+    n = 1 << log_n
+    qs = po.create_coeff_modulus(n, [51] + [46] * 2 + [51] * 17 + [51])
+    steps = B.rot_key_steps_3(logn, log_n - 1)
+    s = pr.SealRef(log_n, qs, seed=9, hamming_weight=192, steps=steps)
+    ev = L.Evaluator(po.OracleContext(log_n, qs), s.relin_key(),
+                     {s.galois_elt(st): s.galois_key(s.galois_elt(st)) for st in steps})
+    bs = B.Bootstrapper(ev, 10, logn, log_n - 1, len(qs) - 2, 2.0 ** 46, K, 59, 2, inverse_deg,
+                        load_table(inverse_deg=inverse_deg))
+    bs.generate_LT_coefficient_3()
+    vals = np.random.default_rng(2).uniform(-1, 1, n // 2)
+    ct = ev.mod_switch_to(L.Ct(s.encrypt(vals, 2.0 ** 46), 2.0 ** 46), 1)
+    out = bs.bootstrap_3(ct)
+    assert out.scale == 2.0 ** 46
+    assert np.abs(s.decrypt(out.data, out.scale) - vals).max() < 2.0 ** -12
