@@ -981,6 +981,29 @@ def run_bert_gpu(args, rank, world):
     same = all(np.array_equal(a.to_numpy(), b) for a, b in zip(res[:layer.n_hid], lock_words))
     del res
 
+    # word parity at this configuration: the Q, K and V projections of the
+    # 128-token lane against the oracle's digests for the same seeds
+    parity = None
+    if rank == 0:
+        import hashlib
+        x2 = [Ciphertext.from_numpy(ctx, np.ascontiguousarray(h[:, :2, :]), BERT_SCALE) for h in host_x]
+        nh = layer.n_head
+        got = {}
+        for which, name in ((0, "q"), (1, "k"), (2, "v")):
+            y = layer.stage(NB.BERT_PROJECT, which, x2, nh, True)[:nh]
+            got[name] = [hashlib.sha256(np.ascontiguousarray(t.to_numpy(), dtype="<u8").tobytes()).hexdigest()
+                         for t in y]
+            del y
+        try:
+            want = json.loads((ROOT / "tests" / "golden" / "bench_digests.json").read_text())
+            want = want["cases"]["bert_n65536_qkv"]["sha256"]
+            parity = {"checked": "output words of the Q, K and V projections of the 128-token lane "
+                                 "(24 ciphertexts) against the oracle's digests (bert_n65536_qkv)",
+                      "words_equal_oracle": all(got[k] == want[k] for k in ("q", "k", "v"))}
+        except (KeyError, OSError, ValueError):
+            parity = None
+        del x2
+
     step_ms = total_ms / args.steps
     peak, peak_kind = _peak_hbm()
     ntt_avg_ms = ntt_ms / max(1, ntt_calls)
@@ -1000,6 +1023,7 @@ def run_bert_gpu(args, rank, world):
         "dtype": "u64",
         "data": "synthetic: weights ~ N(0,0.02), tokens ~ N(0,1), seeded; keys and encryptions from a SEAL seed",
         "config": dict(bert_config(), tuning=tuning),
+        "parity": parity,
         "throughput": {"value": world * 224 / (step_ms / 1e3), "unit": "tokens/s"},
         "accuracy": {"max_abs_err_vs_fp64_same_approx": max(errs), "mean_abs_err_vs_fp64_same_approx":
                      float(np.mean(means)), "max_abs_err_vs_fp64_exact": max(errs_exact),
@@ -1426,9 +1450,9 @@ def main():
     ap.add_argument("--impl", choices=["nexus", "reference"], default="nexus")
     ap.add_argument("--workload", choices=["bootstrap", "matmul", "ntt", "gelu", "bert", "keyswitch", "stages"],
                     default="bootstrap")
-    ap.add_argument("--ntt-form", choices=["auto", "0", "1"], default="auto",
-                    help="forward NTT form: 0 two passes, 1 one pass of thread-block clusters, auto the "
-                         "autotuner's choice (the two-pass default where no autotuner runs)")
+    ap.add_argument("--ntt-form", choices=["auto", "0", "1", "2"], default="auto",
+                    help="forward NTT form: 0 two passes, 1 one pass of thread-block clusters, 2 two passes "
+                         "with limb-grouped rows, auto the autotuner's choice (form 0 where no autotuner runs)")
     ap.add_argument("--ks-limbs", type=int, default=31, help="limbs of the keyswitch workload")
     ap.add_argument("--ks-batch", type=int, default=4, help="ciphertexts per call of the keyswitch workload")
     ap.add_argument("--cpu-depth", type=int, default=7, help="expansion-subtree depth of the MatMul CPU sample")

@@ -121,7 +121,10 @@ int nexus_get_tuning(const nexus_context *ctx, int *ntt_prefetch_waves, int *ks_
  * a rows pass, each reading and writing the limb in HBM (default); 1 = one
  * launch of thread-block clusters of N/4096 CTAs that keep a limb in their
  * distributed shared memory between the passes, so the limb crosses HBM
- * once each way.  Same words either way.
+ * once each way; 2 = the two launches with the rows pass's CTAs each taking
+ * one row of 16 (or 32, 64) limbs of one prime, whose row groups share the
+ * row's twiddles (launches of fewer polynomials keep form 0's rows pass).
+ * Same words in every form.
  */
 int nexus_set_ntt_form(nexus_context *ctx, int form);
 int nexus_get_ntt_form(const nexus_context *ctx, int *form);

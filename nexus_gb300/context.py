@@ -147,7 +147,8 @@ class Context:
 
     def set_ntt_form(self, form: int) -> None:
         """0: forward NTT in two launches (default); 1: one launch of
-        thread-block clusters holding each limb in distributed shared memory."""
+        thread-block clusters holding each limb in distributed shared memory;
+        2: two launches, the rows pass on rows of several limbs of one prime."""
         check(lib().nexus_set_ntt_form(self._h, int(form)), "nexus_set_ntt_form")
 
     def ntt_form(self) -> int:

@@ -1,5 +1,6 @@
 // Autotuner of the launch parameters (Context::Tuning): the form of the
-// forward NTT (two passes, or one pass of thread-block clusters), the L2
+// forward NTT (two passes with per-limb or limb-grouped rows, or one pass
+// of thread-block clusters), the L2
 // prefetch distance of the NTT passes and the grid of the key inner product.
 //
 // Both only change how work maps to CTAs and when tiles reach L2, never a
@@ -86,8 +87,9 @@ double autotune_keyswitch(Context &c, int l, int B, cudaStream_t s, int reps)
         return (double)ms / reps;
     };
     try {
-        for (int form = 0; form < 2; ++form) {
-            c.tune.ntt_cluster = form;
+        for (int form = 0; form < 3; ++form) {
+            c.tune.ntt_cluster = form == 1;
+            c.tune.ntt_rows_grouped = form == 2;
             if (form == 1) {
                 // the cluster form needs clusters of N/4096 CTAs; where the
                 // device refuses them the two-pass form is kept

@@ -442,15 +442,17 @@ extern "C" int nexus_set_ntt_form(nexus_context *ctx, int form)
 {
     static const char *fn = "nexus_set_ntt_form";
     if (!ctx) return fail(fn, "null context");
-    if (form != 0 && form != 1) return fail(fn, "form must be 0 (two passes) or 1 (one cluster pass)");
-    ctx->c.tune.ntt_cluster = form;
+    if (form < 0 || form > 2)
+        return fail(fn, "form must be 0 (two passes), 1 (one cluster pass) or 2 (two passes, limb-grouped rows)");
+    ctx->c.tune.ntt_cluster = form == 1;
+    ctx->c.tune.ntt_rows_grouped = form == 2;
     return 0;
 }
 
 extern "C" int nexus_get_ntt_form(const nexus_context *ctx, int *form)
 {
     if (!ctx || !form) return fail("nexus_get_ntt_form", "null argument");
-    *form = ctx->c.tune.ntt_cluster;
+    *form = ctx->c.tune.ntt_cluster ? 1 : (ctx->c.tune.ntt_rows_grouped ? 2 : 0);
     return 0;
 }
 

@@ -69,6 +69,9 @@ struct Context {
         // of thread-block clusters that keep each limb in distributed shared
         // memory between the passes
         int ntt_cluster = 0;
+        // forward NTT rows pass: 0 a CTA takes R rows of one limb, 1 one row
+        // of R limbs of one prime (the R row groups share their twiddles)
+        int ntt_rows_grouped = 0;
     } tune;
     int sm_count = 0;                // multiprocessors of `device`
 

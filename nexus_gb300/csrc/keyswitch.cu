@@ -33,25 +33,6 @@ inline unsigned grid_for(size_t n)
     return (unsigned)(g > 1048576 ? 1048576 : g);
 }
 
-// D[b][j][i'][n] = t[b][j][n] mod q(i') for i' in [0, l], q(l) = special prime;
-// rows of t are (b, j) pairs, b < batch
-__global__ void k_modup_spread(const uint64_t *__restrict__ t, uint64_t *__restrict__ D,
-                               const PrimeConst *__restrict__ pc, int l, int sp, int logn, size_t total)
-{
-    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (size_t)gridDim.x * blockDim.x) {
-        const size_t row = x >> logn;
-        const int j = (int)(row % (size_t)l);
-        const size_t n = x & (((size_t)1 << logn) - 1);
-        const uint64_t v = t[x];
-        const uint64_t qj = pc[j].q;
-        uint64_t *o = D + ((row * (l + 1)) << logn) + n;
-        for (int i = 0; i <= l; ++i) {
-            const PrimeConst P = pc[i == l ? sp : i];
-            o[(size_t)i << logn] = (P.q < qj) ? barrett_64(v, P.q, P.r1) : v;
-        }
-    }
-}
-
 // D[b][j][j] = t[b][j] for the rows of t (B*l rows, row = b*l + j): digit j's
 // own limb of the ModUp is the NTT-form target limb, as in SEAL
 __global__ void k_modup_diag(const ulonglong2 *__restrict__ t, ulonglong2 *__restrict__ D, int l, int logn,
@@ -863,7 +844,7 @@ extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l,
         set_error(std::string(fn) + ": null argument");
         return -1;
     }
-    const Context &c = ctx->c;
+    Context &c = ctx->c;
     if (l < 1 || l > c.k - 1) {
         set_error(std::string(fn) + ": limbs must be in [1, n_moduli-1]");
         return -1;
@@ -884,11 +865,9 @@ extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l,
         if (cudaGetDevice(&dev) != cudaSuccess || dev != c.device)
             throw std::runtime_error("the context's device must be current");
         uint64_t *t = noalloc_scratch_on_current_device();
-        // SEAL's key switch step by step (INTT of the target, ModUp spread, a
-        // forward NTT of every limb of every digit, inner product, ModDown),
-        // the unfused sequence whose words switch_key() reproduces with its
-        // fused kernels; every scratch word is written before it is read, so
-        // nothing needs clearing
+        // the fused sequence of switch_key_batch for one ciphertext, with its
+        // scratch t[l] | D[l][l+1] | P[2][l+1] | T[2][l] | last[2] in the
+        // fixed array instead of the context's arena
         cudaStream_t s = (cudaStream_t)stream;
         const int sp = c.k - 1;
         uint64_t *D = t + (size_t)l * N;
@@ -896,17 +875,9 @@ extern "C" int nexus_switch_key_noalloc(nexus_context *ctx, uint64_t *ct, int l,
         uint64_t *T = P + 2 * (size_t)(l + 1) * N;
         uint64_t *last = T + 2 * (size_t)l * N;
         cudaMemcpyAsync(t, target, sizeof(uint64_t) * l * N, cudaMemcpyDeviceToDevice, s);
-        ntt_inverse(c, t, 1, LimbMap{l, 0, -1}, s);
-        size_t tot = (size_t)l * N;
-        k_modup_spread<<<grid_for(tot), kBlock, 0, s>>>(t, D, c.d_pc, l, sp, c.logn, tot); NEXUS_LAUNCHED();
-        ntt_forward(c, D, l, LimbMap{l + 1, 0, sp}, s);
-        launch_ks_inner(c, D, key, P, l, 1, s);
-        cudaMemcpyAsync(last, P + (size_t)l * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
-        cudaMemcpyAsync(last + N, P + (size_t)(2 * l + 1) * N, sizeof(uint64_t) * N, cudaMemcpyDeviceToDevice, s);
-        ntt_inverse(c, last, 2, LimbMap{1, sp, -1}, s);
-        launch_round_spread(c, last, T, 2, sp, l, s);
-        ntt_forward(c, T, 2, LimbMap{l, 0, -1}, s);
-        tot = (size_t)2 * l * N;
+        ks_modup_inner(c, t, 1, l, key, D, P, s);
+        ks_moddown_terms(c, P, 1, l, T, last, s);
+        const size_t tot = (size_t)2 * l * N;
         k_moddown_finish<<<grid_for(tot), kBlock, 0, s>>>(ct, P, T, c.d_pc, c.d_inv_q + (size_t)sp * c.k, l, c.logn,
                                                            tot); NEXUS_LAUNCHED();
         cudaError_t e = cudaGetLastError();

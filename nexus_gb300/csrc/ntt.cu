@@ -268,11 +268,42 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_cols(uint64_t *__restrict__
     for (int k = 0; k < kE; ++k) p[(size_t)(kE * t + k) * n2 + c] = x[k];
 }
 
+// The rows-pass CTA of a limb-grouped launch: row r of the R launch limbs
+// (chunk*R + rr) * count + m, rr < R -- the same position m in R consecutive
+// polynomials, which use one prime (with skip_diag all but the digit whose
+// diagonal is left out), so the CTA's R row groups read the same twiddles.
+// A row group past the last polynomial repeats the chunk's first limb and
+// stores nothing.
+struct GroupedRow {
+    uint32_t pl;
+    uint64_t r;
+    bool active;
+};
+
+template <int R>
+__device__ __forceinline__ GroupedRow grouped_row(unsigned blk, int rr, int log_n1, const LimbMap &lm,
+                                                  uint32_t n_polys)
+{
+    const uint32_t chunks = (n_polys + R - 1) / R;
+    GroupedRow g;
+    g.r = blk & ((1u << log_n1) - 1);
+    const uint32_t mc = blk >> log_n1;            // m * chunks + chunk
+    const uint32_t m = mc / chunks, chunk = mc - m * chunks;
+    uint32_t poly = chunk * R + (uint32_t)rr;
+    g.active = poly < n_polys;
+    if (!g.active) poly = chunk * R;
+    g.pl = poly * (uint32_t)lm.count + m;
+    return g;
+}
+
 // Pass 2: size-2^LOGS transforms along contiguous rows, then the final
 // reduction to [0,q) (from [0,4q), or from below 2^59 on the small-prime path).
-template <int LOGS, bool SMALL>
+// GROUPED: the CTA takes one row of R limbs of one prime (grouped_row)
+// instead of R rows of one limb.
+template <int LOGS, bool SMALL, bool GROUPED>
 __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__ data, const ulonglong2 *__restrict__ tw,
-                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm, int pf)
+                                                       const PrimeConst *__restrict__ pc, int logn, LimbMap lm, int pf,
+                                                       uint32_t n_polys)
 {
     constexpr int S = 1 << LOGS, T = S / kE, R = kThreads / T, SP = S + S / 16;
     // the T threads of a row sit in one warp and share only their row's
@@ -281,9 +312,19 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
     __shared__ uint64_t sm[R * SP];
     const int log_n1 = logn - LOGS;
     const int rr = threadIdx.x / T, t = threadIdx.x % T;
-    const size_t grow = (size_t)blockIdx.x * R + rr;
-    const uint32_t pl = (uint32_t)(grow >> log_n1);
-    const uint64_t r = grow & ((1u << log_n1) - 1);
+    uint32_t pl;
+    uint64_t r;
+    bool active = true;
+    if (GROUPED) {
+        const GroupedRow g = grouped_row<R>(blockIdx.x, rr, log_n1, lm, n_polys);
+        pl = g.pl;
+        r = g.r;
+        active = g.active;
+    } else {
+        const size_t grow = (size_t)blockIdx.x * R + rr;
+        pl = (uint32_t)(grow >> log_n1);
+        r = grow & ((1u << log_n1) - 1);
+    }
     size_t lrow;
     int prime;
     lm.locate(pl, lrow, prime);
@@ -294,7 +335,17 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
     const uint64_t B = (1ull << log_n1) + r;
     if (pf) {
         const unsigned fb = blockIdx.x + (unsigned)pf * 3 * sm_count();
-        if (fb < gridDim.x) prefetch_rows_tile<S, R>(data, fb, logn, log_n1, lm);
+        if (fb < gridDim.x) {
+            if (GROUPED) {
+                const GroupedRow g = grouped_row<R>(fb, rr, log_n1, lm, n_polys);
+                size_t frow;
+                int fprime;
+                lm.locate(g.pl, frow, fprime);
+                prefetch_l2(data + (frow << logn) + g.r * S + (size_t)t * 16);
+            } else {
+                prefetch_rows_tile<S, R>(data, fb, logn, log_n1, lm);
+            }
+        }
     }
 
     uint64_t x[kE];
@@ -321,8 +372,10 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd_rows(uint64_t *__restrict__
         for (int k = 0; k < kE; ++k) srow[swz(kE * t + k)] = csub(csub(x[k], q2), q);
     }
     __syncwarp();
+    if (active) {
 #pragma unroll
-    for (int k = 0; k < kE; ++k) p[t + T * k] = srow[swz(t + T * k)];
+        for (int k = 0; k < kE; ++k) p[t + T * k] = srow[swz(t + T * k)];
+    }
 }
 
 // ------------------------------------------------- forward, one pass per cluster
@@ -617,7 +670,17 @@ void launch_fwd_t(const Context &c, uint64_t *d, size_t n_polys, LimbMap lm, cud
     else
         k_fwd_cols<L1, 0, SMALL><<<g1, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, ld);
     NEXUS_LAUNCHED();
-    k_fwd_rows<L2, SMALL><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm, c.tune.ntt_prefetch_waves);
+    if (c.tune.ntt_rows_grouped && n_polys >= (size_t)R) {
+        // one row of R limbs of one prime per CTA (the CTA reads its
+        // twiddles once); idle row groups only past the last polynomial
+        const unsigned chunks = (unsigned)((n_polys + R - 1) / R);
+        const unsigned gg = (unsigned)lm.count * chunks << (c.logn - L2);
+        k_fwd_rows<L2, SMALL, true><<<gg, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm,
+                                                             c.tune.ntt_prefetch_waves, (uint32_t)n_polys);
+    } else {
+        k_fwd_rows<L2, SMALL, false><<<g2, kThreads, 0, s>>>(d, c.d_tw_fwd, c.d_pc, c.logn, lm,
+                                                              c.tune.ntt_prefetch_waves, (uint32_t)n_polys);
+    }
     NEXUS_LAUNCHED();
 }
 

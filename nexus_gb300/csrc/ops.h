@@ -46,11 +46,6 @@ void tensor(const Context &c, const uint64_t *a, const uint64_t *b, int limbs, u
 // divide_and_round_q_last_ntt over every polynomial: [size][limbs] -> [size][limbs-1]
 void rescale(const Context &c, const uint64_t *in, int size, int limbs, uint64_t *out, cudaStream_t s);
 
-// out[p][i] = ((last[p] + h) mod q_lp) mod q_i + (q_i - h mod q_i), h = q_lp/2,
-// for i < out_limbs: the rounding step shared by rescale and ModDown
-void launch_round_spread(const Context &c, const uint64_t *last, uint64_t *out, int polys, int last_prime,
-                         int out_limbs, cudaStream_t s);
-
 // NTT-domain automorphism of [polys][limbs][N]
 void galois_permute(Context &c, const uint64_t *in, int polys, int limbs, uint32_t elt, uint64_t *out,
                     cudaStream_t s);

@@ -220,29 +220,6 @@ __global__ void k_gather_limb(const ulonglong2 *__restrict__ src, ulonglong2 *ds
     }
 }
 
-// From the inverse-transformed dropped limb x (in [0, q_last)), build for every
-// remaining prime q_i the value ((x + h) mod q_last) mod q_i + (q_i - h mod q_i)
-// with h = floor(q_last / 2): the rounding correction of
-// divide_and_round_q_last_ntt_inplace (util/rns.cpp:857-884) and of the
-// ModDown step of switch_key_inplace (evaluator.cpp:2966-2985).
-__global__ void k_round_spread(const uint64_t *__restrict__ last, uint64_t *__restrict__ out,
-                               const PrimeConst *__restrict__ pc, int last_prime, int out_limbs, int logn,
-                               size_t total)
-{
-    const uint64_t ql = pc[last_prime].q, h = ql >> 1;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
-        const size_t p = t >> logn, n = t & (((size_t)1 << logn) - 1);
-        const uint64_t x = csub(last[t] + h, ql);
-        uint64_t *o = out + (p * out_limbs << logn) + n;
-        for (int i = 0; i < out_limbs; ++i) {
-            const PrimeConst P = pc[i];
-            const uint64_t xr = (P.q < ql) ? barrett_64(x, P.q, P.r1) : x;
-            const uint64_t hr = (P.q < ql) ? barrett_64(h, P.q, P.r1) : h;
-            o[(size_t)i << logn] = xr + (P.q - hr);
-        }
-    }
-}
-
 // out[p][i] = (in[p][i] - t[p][i]) * q_last^{-1} mod q_i   (t in [0, q_i))
 __global__ void k_rescale_finish(const ulonglong2 *__restrict__ in, const ulonglong2 *__restrict__ t,
                                  ulonglong2 *out, const PrimeConst *__restrict__ pc,
@@ -467,13 +444,6 @@ void rescale_scaled(const Context &c_in, const uint64_t *in, int size, int limbs
             (const ulonglong2 *)in, (const ulonglong2 *)t, (ulonglong2 *)out, w, c.d_pc,
             c.d_inv_q + (size_t)(limbs - 1) * c.k, limbs, c.logn, pr);
     NEXUS_LAUNCHED();
-}
-
-void launch_round_spread(const Context &c, const uint64_t *last, uint64_t *out, int polys, int last_prime,
-                         int out_limbs, cudaStream_t s)
-{
-    size_t tot = (size_t)polys * c.n;
-    k_round_spread<<<grid_for(tot), kBlock, 0, s>>>(last, out, c.d_pc, last_prime, out_limbs, c.logn, tot); NEXUS_LAUNCHED();
 }
 
 void galois_permute(Context &c, const uint64_t *in, int polys, int limbs, uint32_t elt, uint64_t *out,

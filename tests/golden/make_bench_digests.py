@@ -22,7 +22,11 @@ Cases:
   bootstrap_n65536      Bootstrapper::bootstrap_3 (Bootstrapper.cpp:3489-3495)
                         full-slot at N=2^16 on 51 + 16x46 + 14x51 + 51 with
                         the sparse secret (h = 192), K = 25, degree 59, two
-                        double angles: every stage's output.
+                        double angles: every stage's output;
+  bert_n65536_qkv       the encrypted BERT-base layer's Q, K and V projections
+                        for the 128-token lane at N=2^16 on the layer chain
+                        51 + 19x46 + 14x51 + 51, from the inputs bench.py's
+                        layer receives (weights and tokens from its seeds).
 
 Digests are over the little-endian bytes of the uint64 arrays in SEAL's
 layout.  The oracle's key switch and rescale run on all host cores.
@@ -56,6 +60,7 @@ OUT = Path(__file__).parent / "bench_digests.json"
 BOOT_BITS = [51] + [46] * 16 + [51] * 14 + [51]
 GELU_BITS = [58] + [40] * 18 + [58]
 MM_BITS = [60, 40, 60]
+BERT_BITS = [51] + [46] * 19 + [51] * 14 + [51]
 
 
 def seed8(tag: int) -> list[int]:
@@ -72,6 +77,8 @@ CASES = {
     "bootstrap_n65536": dict(log_n=16, bits=BOOT_BITS, seed=seed8(400), hamming_weight=192, scale_log2=46,
                              data_seed=4096, loge=10, boundary_K=25, sin_cos_deg=59, scale_factor=2,
                              inverse_deg=1),
+    "bert_n65536_qkv": dict(log_n=16, bits=BERT_BITS, seed=seed8(600), hamming_weight=192, scale_log2=46,
+                            weight_seed=11, token_seed=12, lane=0, proj_limbs=2),
 }
 
 
@@ -284,8 +291,48 @@ def case_bootstrap(c):
     return out
 
 
+def case_bert_qkv(c):
+    """The encrypted BERT-base layer's Q, K and V projections (block-diagonal
+    BSGS transforms of the engine's BertLayerT, restated in oracle/bert.py) for
+    the lane of the 128-token request, on the ciphertexts the layer receives:
+    the packed tokens encrypted at the top level, switched down to two limbs."""
+    from nexus_gb300 import bert as NB
+    from oracle import bert as OB
+
+    class _Scale:
+        final_scale = 2.0 ** c["scale_log2"]
+
+    n = 1 << c["log_n"]
+    qs = po.create_coeff_modulus(n, c["bits"])
+    sh = NB.BertShape()
+    w = NB.random_weights(sh, np.random.default_rng(c["weight_seed"]))
+    rng = np.random.default_rng(c["token_seed"])
+    tokens = [[rng.normal(0, 1, (Lr, sh.hidden)) for (_, Lr) in lane] for lane in sh.lanes]
+    osh = OB.Shape(n // 2, sh.hidden, sh.heads, sh.head_dim, sh.ffn, sh.T, sh.lanes, sh.boot_shrink)
+    keys = SealKeys(c["log_n"], qs, c["seed"], c["hamming_weight"], keep=30)
+    keys.allow(keys.ref.galois_elt(s) for s in osh.rotation_steps())
+    scale = 2.0 ** c["scale_log2"]
+    oev = L.Evaluator(po.OracleContext(c["log_n"], qs), keys.ref.relin_key(), keys)
+    layer = OB.BertLayer(oev, _Scale(), osh, w, c["lane"])
+    top = len(qs) - 1
+    x, inputs = [], []
+    for v in NB.pack_lane(sh, n // 2, c["lane"], tokens[c["lane"]]):
+        ct = keys.ref.encrypt_ntt(oev.encode(v, scale, top).data, scale, symmetric=True)
+        inputs.append(digest(ct))
+        x.append(L.Ct(np.ascontiguousarray(ct[:, :c["proj_limbs"], :]), scale))
+    out = {"input": inputs}
+    t0 = time.time()
+    for which, name in ((0, "q"), (1, "k"), (2, "v")):
+        y = layer.project(x, which)
+        out[name] = [digest(ct.data) for ct in y]
+        out[name + "_scale"] = y[0].scale
+        out[name + "_limbs"] = y[0].limbs
+        print(f"  projection {name} done ({time.time() - t0:.0f} s, {keys.made} keys made)", flush=True)
+    return out
+
+
 RUN = {"keyswitch_n65536_l31": case_keyswitch, "gelu_n16384": case_gelu, "matmul_n65536": case_matmul,
-       "bootstrap_n65536": case_bootstrap}
+       "bootstrap_n65536": case_bootstrap, "bert_n65536_qkv": case_bert_qkv}
 
 
 def main(argv):

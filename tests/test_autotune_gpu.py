@@ -23,7 +23,7 @@ def test_autotune_choice_and_words(cuda):
     assert ctx.tuning() == {"ntt_prefetch_waves": 3, "ks_inner_ctas_per_sm": 0, "ntt_form": 0}
     t = ctx.autotune(7, 2, reps=2)
     assert t["ntt_prefetch_waves"] in (0, 1, 2, 3, 4) and t["ks_inner_ctas_per_sm"] in (0, 4, 8, 16)
-    assert t["ntt_form"] in (0, 1) and t["ms_per_call"] > 0
+    assert t["ntt_form"] in (0, 1, 2) and t["ms_per_call"] > 0
     assert ctx.tuning() == {k: t[k] for k in ("ntt_prefetch_waves", "ks_inner_ctas_per_sm", "ntt_form")}
     rng = np.random.default_rng(9)
     l = 7
@@ -32,7 +32,7 @@ def test_autotune_choice_and_words(cuda):
     key = po.random_residues(rng, (len(qs) - 1, 2, len(qs), N), qs)
     want = oc.switch_key(ct, tgt, key)
     want_ntt = oc.ntt(ct, 0, l)
-    for setting in (None, (0, 0, 0), (4, 16, 1), (1, 4, 1), (1, 4, 0)):
+    for setting in (None, (0, 0, 0), (4, 16, 1), (1, 4, 1), (1, 4, 0), (1, 0, 2), (3, 8, 2)):
         if setting is not None:
             ctx.set_tuning(*setting[:2])
             ctx.set_ntt_form(setting[2])

@@ -193,3 +193,53 @@ def test_bootstrap_n65536_stages(cuda):
     assert _digest(batch[0].to_numpy()) == d["output"]
     dec = ctx.decode(ctx.decrypt(sk, whole.to_device()), whole.scale).real
     assert np.max(np.abs(dec - vals)) < 2.0 ** -10
+
+
+def test_bert_qkv_projections(cuda):
+    """The BERT-base layer's Q, K and V projections for the 128-token lane at
+    N=2^16, on the inputs bench.py's layer receives (SEAL keys and
+    encryptions from seed 600, weights and tokens from seeds 11 and 12)."""
+    import torch
+    from nexus_gb300 import bert as NB
+    from nexus_gb300.operators import Bootstrapper, Ciphertext, Evaluator
+    if "bert_n65536_qkv" not in DOC:
+        pytest.skip("no digests for the BERT projections")
+    c = DOC["bert_n65536_qkv"]
+    d = c["sha256"]
+    ctx, qs = _ctx(c)
+    n = 1 << c["log_n"]
+    scale = 2.0 ** c["scale_log2"]
+    sk = ctx.seal_keygen_secret(_seed(c), c["hamming_weight"])
+    ev = Evaluator(ctx, scale, ctx.seal_keygen_relin(sk, _seed(c)))
+    log_nh = c["log_n"] - 1
+    bs = Bootstrapper(ev, 10, log_nh, log_nh, len(qs) - 2, scale, 25, 59, 2, 1)
+    bs.prepare_mod_polynomial()
+    bs.generate_LT_coefficient_3()
+    sh = NB.BertShape()
+    w = NB.random_weights(sh, np.random.default_rng(c["weight_seed"]))
+    rng = np.random.default_rng(c["token_seed"])
+    tokens = [[rng.normal(0, 1, (L, sh.hidden)) for (_, L) in lane] for lane in sh.lanes]
+    layer = NB.BertLayer(bs, sh, w)
+    for st in layer.rotation_steps():
+        e = ctx.galois_elt(st)
+        ev.add_galois_key(e, ctx.seal_keygen_galois(sk, e, _seed(c)))
+    top = len(qs) - 1
+    pl = c["proj_limbs"]
+    x = []
+    for lane in range(len(sh.lanes)):
+        for i, v in enumerate(NB.pack_lane(sh, n // 2, lane, tokens[lane])):
+            pt = torch.empty((top, n), dtype=torch.int64, device="cuda")
+            ctx.encode(v, scale, top, pt)
+            ct = ctx.seal_encrypt_symmetric(sk, pt, top, _seed(c))
+            if lane == c["lane"]:
+                assert _digest(ct) == d["input"][i]
+            x.append(Ciphertext.from_device(ctx, ct[:, :pl, :].contiguous(), scale))
+            del pt, ct
+    nh = layer.n_head
+    for which, name in ((0, "q"), (1, "k"), (2, "v")):
+        for lockstep in (True, False):
+            y = layer.stage(NB.BERT_PROJECT, which, x, nh, lockstep)
+            lane_y = y[c["lane"] * nh:(c["lane"] + 1) * nh]
+            assert lane_y[0].scale == d[name + "_scale"]
+            assert lane_y[0].to_numpy().shape[1] == d[name + "_limbs"]
+            assert [_digest(t.to_numpy()) for t in lane_y] == d[name], (name, lockstep)
