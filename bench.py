@@ -1329,6 +1329,79 @@ def run_keyswitch_gpu(args, rank, world):
             "gpu_launches": ng.kernel_launches() - l0}
 
 
+def run_tensor_gpu(args, rank, world):
+    """The tensor-pipe decision, measured: the dense rate of hand-written
+    tcgen05.mma (bf16 through kind::f16, e4m3 through kind::f8f6f4; one CTA per
+    SM, 128 x 256 accumulator in tensor memory) as a short burst and as a
+    loop of about a second, next to the NTT's own measured limb-NTT time at
+    N=2^16 on 51-bit primes.  The four-step tensor form of a limb-NTT runs two
+    passes of 256-point DFTs, each a 256 x 256 x 256 product per pair of
+    operand limbs: 8-bit limbs in bf16 (products below 2^16, 256-term sums
+    below 2^24, exact in the f32 accumulator), 7 x 7 pairs for a 51-bit
+    prime; 4-bit limbs in e4m3, 13 x 13 pairs.  Its MMA time alone, before
+    the limb recombination and reductions, is set against the integer-pipe
+    NTT.  int8 operands (kind::i8) do not assemble for sm_103a."""
+    import torch
+
+    import nexus_gb300 as ng
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    rates = {}
+    with ClockSampler(dev.index) as clk:
+        for name, kind in (("bf16", ng.TENSOR_BF16), ("e4m3", ng.TENSOR_E4M3)):
+            burst, burst_ms = ng.tensor_rate(kind, 20000)
+            sust, sust_ms = ng.tensor_rate(kind, 1 << 20)
+            rates[name] = {"burst_tflops": burst / 1e12, "burst_ms_per_launch": burst_ms,
+                           "sustained_tflops": sust / 1e12, "sustained_ms_per_launch": sust_ms}
+    clocks = clk.summary()
+
+    # the NTT on the integer pipes: forward, 8 ciphertexts x 2 x 31 limbs of 51-bit primes
+    log_n, n = 16, 1 << 16
+    qs = ng.create_coeff_modulus(n, [51] * 32)
+    ctx = ng.Context(log_n, qs)
+    limbs = 31
+    g = torch.Generator(device=dev).manual_seed(3)
+    qd = torch.tensor(qs[:limbs], dtype=torch.int64, device=dev)
+    x = torch.randint(0, 2 ** 62, (16, limbs, n), device=dev, dtype=torch.int64, generator=g) % qd.view(limbs, 1)
+    for _ in range(args.warmup):
+        ctx.ntt_forward(x, 0, limbs)
+    stream = torch.cuda.current_stream(dev)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(1, args.steps)
+    t0.record(stream)
+    for _ in range(reps):
+        ctx.ntt_forward(x, 0, limbs)
+    t1.record(stream)
+    torch.cuda.synchronize(dev)
+    ntt_us = t0.elapsed_time(t1) * 1e3 / (reps * 16 * limbs)
+
+    dft_macs = 256 ** 3                       # one 256-point DFT pass over a 256 x 256 limb
+    form = {}
+    for name, pairs in (("bf16", 7 * 7), ("e4m3", 13 * 13)):
+        flop = 2 * 2 * pairs * dft_macs      # two passes, 2 FLOP per multiply-add
+        us = flop / (rates[name]["burst_tflops"] * 1e12) * 1e6
+        form[name] = {"flop_per_limb_ntt": flop, "mma_us_per_limb_ntt": us,
+                      "vs_integer_ntt": us / ntt_us}
+    peak = _measured_peak("bf16_tflops")
+    return {"metric": "tensor_rate_tcgen05", "value": rates["bf16"]["burst_tflops"], "unit": "TFLOP/s",
+            "n_gpus": world, "steps": reps, "warmup": args.warmup, "higher_is_better": True, "dtype": "bf16",
+            "data": "small integers (|v| <= 2) in the operand format, fixed stream",
+            "config": {"workload": "tcgen05_mma_rate_m128_n256", "ctas": "one per SM", "k_bytes_per_mma": 32},
+            "rates": rates, "clocks": clocks,
+            "cublas_bf16_tflops_measured": peak,
+            "kind_i8": "does not assemble for sm_103a (ptxas: Feature '.kind::i8' not supported on .target "
+                       "'sm_103a')",
+            "integer_ntt_us_per_limb_ntt": ntt_us,
+            "ntt_tensor_form": form}
+
+
+def _measured_peak(key: str):
+    try:
+        return json.loads(MEASURED_PEAKS.read_text()).get(key)
+    except (OSError, ValueError):
+        return None
+
+
 def run_stages_gpu(args, rank, world):
     """The full-slot bootstrap at N=2^16 split into its stages (modulus raise,
     CoeffToSlot, EvalMod on each half, SlotToCoeff), in the single-ciphertext
@@ -1448,7 +1521,8 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["nexus", "reference"], default="nexus")
-    ap.add_argument("--workload", choices=["bootstrap", "matmul", "ntt", "gelu", "bert", "keyswitch", "stages"],
+    ap.add_argument("--workload", choices=["bootstrap", "matmul", "ntt", "gelu", "bert", "keyswitch", "stages",
+                                           "tensor"],
                     default="bootstrap")
     ap.add_argument("--ntt-form", choices=["auto", "0", "1", "2"], default="auto",
                     help="forward NTT form: 0 two passes, 1 one pass of thread-block clusters, 2 two passes "
@@ -1466,7 +1540,7 @@ def main():
     ap.add_argument("--ntt-cts", type=int, default=64,
                     help="ciphertexts per step (smaller values are for profiling captures only)")
     args = ap.parse_args()
-    if args.workload not in ("keyswitch", "stages"):
+    if args.workload not in ("keyswitch", "stages", "tensor"):
         args.warmup = max(3, args.warmup)   # the micro-benchmarks allow one cold call for a profiler
     if args.workload == "keyswitch" and not 1 <= args.ks_limbs <= len(BOOT_BITS) - 1:
         raise SystemExit(f"--ks-limbs must be in [1, {len(BOOT_BITS) - 1}]")
@@ -1476,7 +1550,8 @@ def main():
     MM_ROWS = args.mm_rows
     BOOT_CTS = args.boot_cts
     if args.steps is None:
-        args.steps = {"bootstrap": 3, "matmul": 5, "gelu": 5, "bert": 2, "keyswitch": 5, "stages": 2}.get(
+        args.steps = {"bootstrap": 3, "matmul": 5, "gelu": 5, "bert": 2, "keyswitch": 5, "stages": 2,
+                      "tensor": 5}.get(
             args.workload, 20)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1570,7 +1645,7 @@ def main():
         print(json.dumps(res), flush=True)
         return
 
-    if args.impl == "reference" and args.workload in ("keyswitch", "stages"):
+    if args.impl == "reference" and args.workload in ("keyswitch", "stages", "tensor"):
         if rank == 0:
             print(json.dumps({"impl": "reference", "unavailable": "micro-benchmark of the engine only; the CPU "
                               "reference is timed by the bootstrap, gelu, matmul, ntt and bert workloads"}))
@@ -1605,7 +1680,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
     run = {"bootstrap": run_boot_gpu, "matmul": run_mm_gpu, "ntt": run_ntt_gpu, "gelu": run_gelu_gpu,
-           "bert": run_bert_gpu, "keyswitch": run_keyswitch_gpu, "stages": run_stages_gpu}[args.workload]
+           "bert": run_bert_gpu, "keyswitch": run_keyswitch_gpu, "stages": run_stages_gpu,
+           "tensor": run_tensor_gpu}[args.workload]
     res = run(args, rank, world)
     if rank == 0:
         print(json.dumps(res), flush=True)

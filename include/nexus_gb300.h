@@ -98,6 +98,22 @@ int nexus_butterfly_rate(int mode, uint64_t q, int rounds, int blocks_per_sm, do
                          double *ms);
 
 /*
+ * Dense rate of this GPU's fifth-generation tensor cores through hand-written
+ * tcgen05.mma: one CTA per SM holds a 128 x 256 f32 accumulator in tensor
+ * memory and issues `rounds` x 4 MMAs of 128 x 256 x K from shared memory
+ * (kind 0: bf16 operands, kind::f16, K = 16; kind 1: e4m3 operands,
+ * kind::f8f6f4, K = 32), committed to an mbarrier.  Returns FLOP/s (2 per
+ * multiply-add) of the whole GPU; *ms receives one launch's duration.
+ * Synchronous.  nexus_tensor_tile runs the same kernel on one CTA and copies
+ * the accumulator out: a (128 rows) and b (256 rows) hold 128 bytes of K
+ * per row (64 bf16 or 128 e4m3 values, row-major), and d (128 x 256 f32,
+ * row-major) receives rounds * a . b^T.  Measurement aids for the tensor-pipe
+ * decision, with no counterpart in the reference.
+ */
+int nexus_tensor_rate(int kind, int rounds, double *flops_per_s, double *ms);
+int nexus_tensor_tile(int kind, int rounds, const void *a, const void *b, float *d);
+
+/*
  * Autotuner of the context's launch parameters: the L2 prefetch distance of
  * the NTT passes (in residency waves of 3 CTAs per SM, 0 = none; candidates
  * 0-4) and the grid of the key inner product (CTAs per SM of its grid-stride

@@ -123,6 +123,8 @@ SIGNATURES = [
     ("nexus_get_ntt_form", C.c_int, [C.c_void_p, C.c_void_p]),
     ("nexus_butterfly_rate", C.c_int,
      [C.c_int, C.c_uint64, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("nexus_tensor_rate", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("nexus_tensor_tile", C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nexus_bert_layer_create", C.c_int,
      [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
       C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_void_p)]),

@@ -326,3 +326,32 @@ def butterfly_rate(mode: int, q: int, rounds: int = 512, blocks_per_sm: int = 3)
     check(lib().nexus_butterfly_rate(int(mode), C.c_uint64(int(q)), int(rounds), int(blocks_per_sm), C.byref(out),
                                      C.byref(ms)), "nexus_butterfly_rate")
     return out.value
+
+
+TENSOR_BF16, TENSOR_E4M3 = 0, 1
+TENSOR_M, TENSOR_N, TENSOR_ROW_BYTES = 128, 256, 128
+
+
+def tensor_rate(kind: int, rounds: int = 20000) -> tuple[float, float]:
+    """(FLOP/s, ms per launch) of hand-written tcgen05.mma on this GPU, one
+    CTA per SM: kind 0 bf16 (kind::f16), 1 e4m3 (kind::f8f6f4)
+    (nexus_tensor_rate)."""
+    out = C.c_double()
+    ms = C.c_double()
+    check(lib().nexus_tensor_rate(int(kind), int(rounds), C.byref(out), C.byref(ms)), "nexus_tensor_rate")
+    return out.value, ms.value
+
+
+def tensor_tile(kind: int, a: np.ndarray, b: np.ndarray, rounds: int = 1) -> np.ndarray:
+    """rounds * a . b^T through the tcgen05 kernel of tensor_rate on one CTA:
+    a is 128 rows and b 256 rows of 128 operand bytes (uint16 bf16 bits or
+    uint8 e4m3 bits); returns the 128 x 256 float32 accumulator
+    (nexus_tensor_tile)."""
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    if a.nbytes != TENSOR_M * TENSOR_ROW_BYTES or b.nbytes != TENSOR_N * TENSOR_ROW_BYTES:
+        raise ValueError("a must hold 128 and b 256 rows of 128 bytes")
+    d = np.empty((TENSOR_M, TENSOR_N), dtype=np.float32)
+    check(lib().nexus_tensor_tile(int(kind), int(rounds), a.ctypes.data, b.ctypes.data, d.ctypes.data),
+          "nexus_tensor_tile")
+    return d
