@@ -597,11 +597,16 @@ def boot_config(n_keys=None):
 
 
 def run_boot_gpu(args, rank, world):
+    """The full-slot bootstrap at N=2^16, 16 ciphertexts per step.  The
+    headline form is the lockstep call (nexus_bootstrap_batch) captured once
+    as a CUDA graph and replayed per step (nexus_graph_launch); the same call
+    made directly and the single-ciphertext form are timed beside it, and
+    every form's words are checked against the direct call's."""
     import numpy as np
     import torch
 
     import nexus_gb300 as ng
-    from nexus_gb300.operators import Bootstrapper, Ciphertext, Evaluator
+    from nexus_gb300.operators import Bootstrapper, Ciphertext, Evaluator, Graph
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
@@ -613,7 +618,9 @@ def run_boot_gpu(args, rank, world):
     seed = _seal_seed(400 + rank)
     sk = ctx.seal_keygen_secret(seed, 192)
     rk = ctx.seal_keygen_relin(sk, seed)
-    ev = Evaluator(ctx, BOOT_SCALE, rk)
+    # the evaluator runs on a stream of its own: the legacy default stream cannot be captured
+    stream = torch.cuda.Stream(dev)
+    ev = Evaluator(ctx, BOOT_SCALE, rk, stream=stream)
     bs = Bootstrapper(ev, **BOOT_PARAMS)
     steps = bs.rotation_steps(BOOT_LOGN - 1)
     for st in steps:
@@ -639,9 +646,9 @@ def run_boot_gpu(args, rank, world):
         inputs.append(low)
         host_in.append(low.cpu().numpy().view(np.uint64).copy())
         del pt, ct
-    stream = torch.cuda.current_stream(dev)
+    torch.cuda.synchronize(dev)
 
-    in_cts = [Ciphertext.from_device(ctx, x, BOOT_SCALE) for x in inputs]
+    in_cts = [Ciphertext.from_device(ctx, x, BOOT_SCALE, stream) for x in inputs]
 
     def step():
         # the lockstep form: every operation once over all ciphertexts (inputs are not modified)
@@ -649,16 +656,34 @@ def run_boot_gpu(args, rank, world):
 
     def plain_step():
         # the single-ciphertext form, one bootstrap_3 per ciphertext (it raises its input in place)
-        return [bs.bootstrap_3(Ciphertext.from_device(ctx, x, BOOT_SCALE)) for x in inputs]
+        return [bs.bootstrap_3(Ciphertext.from_device(ctx, x, BOOT_SCALE, stream)) for x in inputs]
+
+    def words(xs):
+        stream.synchronize()
+        return [x.to_numpy() for x in xs]
 
     for _ in range(args.warmup):
         res = step()
-    torch.cuda.synchronize(dev)
+    ref = words(res)
     dec = ctx.decode(ctx.decrypt(sk, res[0].to_device()), res[0].scale).real
     err = float(np.max(np.abs(dec - vals[0])))
     out_limbs = res[0].info()[1]
-    parity = _digest_check("bootstrap_n65536", res[0].to_numpy()) if rank == 0 else None
+    parity = _digest_check("bootstrap_n65536", ref[0]) if rank == 0 else None
     del res
+
+    # the lockstep call captured once; its handles serve the graph alone
+    graph_in = [Ciphertext.from_device(ctx, x, BOOT_SCALE, stream) for x in inputs]
+    graph_out = [Ciphertext(ctx) for _ in inputs]
+    bs.bootstrap_batch(graph_in, graph_out)
+    stream.synchronize()
+    with Graph(stream) as graph:
+        bs.bootstrap_batch(graph_in, graph_out)
+    graph.launch()
+    graph_same = all(np.array_equal(a, b) for a, b in zip(words(graph_out), ref))
+
+    def graph_step():
+        graph.launch()
+
     barrier(world)
     l0 = ng.kernel_launches()
     # engine launches before the timed region: the -s value of a launch-list capture
@@ -669,12 +694,21 @@ def run_boot_gpu(args, rank, world):
         torch.cuda.synchronize(dev)
         t0.record(stream)
         for _ in range(args.steps):
-            res = step()
+            graph_step()
         t1.record(stream)
         torch.cuda.synchronize(dev)
     launches = ng.kernel_launches() - l0
     barrier(world)
     total_ms = max_over_ranks(t0.elapsed_time(t1), world)
+    d0 = torch.cuda.Event(enable_timing=True)
+    d1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    d0.record(stream)
+    for _ in range(args.steps):
+        res = step()
+    d1.record(stream)
+    torch.cuda.synchronize(dev)
+    direct_ms = d0.elapsed_time(d1) / args.steps
     del res
 
     ctx.ntt_timing_begin()
@@ -689,22 +723,24 @@ def run_boot_gpu(args, rank, world):
     del res
 
     # end to end through the C ABI: one-limb ciphertexts from pinned host
-    # memory, bootstrap, refreshed ciphertexts back to the host
+    # memory into the graph's input handles, one graph launch, the refreshed
+    # ciphertexts back to the host
     h_in = [torch.from_numpy(h.view(np.int64)).pin_memory() for h in host_in]
+    h_out = [torch.empty((2, out_limbs, n), dtype=torch.int64).pin_memory() for _ in graph_out]
+    sp = stream.cuda_stream
     torch.cuda.synchronize(dev)
     barrier(world)
     w0 = time.perf_counter()
-    out_bytes = 0
-    loaded = []
-    for h in h_in:
-        c = Ciphertext(ctx)
-        ng.check(ng.lib().nexus_ciphertext_load(c.handle, h.data_ptr(), 2, 1, BOOT_SCALE, 1, None), "load")
-        loaded.append(c)
-    for r in bs.bootstrap_batch(loaded):
-        out_bytes += r.to_numpy().nbytes
+    for c, h in zip(graph_in, h_in):
+        ng.check(ng.lib().nexus_ciphertext_load(c.handle, h.data_ptr(), 2, 1, BOOT_SCALE, 1, sp), "load")
+    graph.launch()
+    for r, h in zip(graph_out, h_out):
+        ng.check(ng.lib().nexus_ciphertext_store(r.handle, h.data_ptr(), 1, sp), "store")
     torch.cuda.synchronize(dev)
     e2e_s = max_over_ranks(time.perf_counter() - w0, world)
+    e2e_same = all(np.array_equal(a.numpy().view(np.uint64), b) for a, b in zip(h_out, ref))
     in_bytes = sum(h.nbytes for h in host_in)
+    out_bytes = sum(h.nbytes for h in h_out)
 
     # the single-ciphertext form on the same inputs, for comparison
     plain_step()
@@ -716,7 +752,7 @@ def run_boot_gpu(args, rank, world):
     p1.record(stream)
     torch.cuda.synchronize(dev)
     plain_ms = p0.elapsed_time(p1)
-    same = all(np.array_equal(a.to_numpy(), b.to_numpy()) for a, b in zip(res[:2], bs.bootstrap_batch(in_cts[:2])))
+    same = all(np.array_equal(a, b) for a, b in zip(words(res), ref))
     del res
 
     step_ms = total_ms / args.steps
@@ -738,8 +774,13 @@ def run_boot_gpu(args, rank, world):
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic: slots ~ U(-1,1), seeded; keys and encryptions from a SEAL seed (sparse secret h=192)",
-        "config": dict(boot_config(len(steps)), tuning=tuning),
+        "config": dict(boot_config(len(steps)), tuning=tuning,
+                       form="lockstep nexus_bootstrap_batch captured once as a CUDA graph, one "
+                            "nexus_graph_launch per step"),
         "parity": parity,
+        "graph": {"kernel_nodes": graph.info()["kernel_nodes"], "words_equal_direct": bool(graph_same)},
+        "direct_lockstep_form": {"value": world * BOOT_CTS / (direct_ms / 1e3), "unit": "bootstraps/s",
+                                 "ms_per_step": direct_ms},
         "accuracy": {"max_abs_err_vs_input": err, "precision_bits": -float(np.log2(err)),
                      "output_limbs": out_limbs},
         "roofline": {
@@ -755,7 +796,7 @@ def run_boot_gpu(args, rank, world):
             "compute_bound": _butterfly_roof(ng, qs[1], ntt_limbs, ntt_ms, BOOT_LOGN),
         },
         "e2e": {"value": world * BOOT_CTS / e2e_s, "unit": "bootstraps/s", "h2d_bytes_per_step": in_bytes,
-                "d2h_bytes_per_step": out_bytes},
+                "d2h_bytes_per_step": out_bytes, "words_equal_direct": bool(e2e_same)},
         "plain_single_ct_form": {"value": world * BOOT_CTS / (plain_ms / 1e3), "unit": "bootstraps/s",
                                  "ms_per_bootstrap": plain_ms / BOOT_CTS,
                                  "batched_words_equal_single": bool(same)},
@@ -1085,13 +1126,20 @@ def gelu_config():
 
 
 def run_gelu_gpu(args, rank, world):
+    """GELU at N=2^14 on 16 ciphertexts per step.  The headline form is the
+    lockstep call (nexus_gelu_batch) captured once as a CUDA graph and
+    replayed per step (nexus_graph_launch); the same call made directly, and
+    the single-ciphertext form (one nexus_gelu per ciphertext) made directly
+    and as a graph, are timed beside it.  Every form's words are checked
+    against the direct lockstep call's, whose first two ciphertexts are
+    checked against the oracle's digests."""
     import math
 
     import numpy as np
     import torch
 
     import nexus_gb300 as ng
-    from nexus_gb300.operators import Ciphertext, Evaluator
+    from nexus_gb300.operators import Ciphertext, Evaluator, Graph
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
@@ -1106,7 +1154,6 @@ def run_gelu_gpu(args, rank, world):
     seed = _seal_seed(200 + rank)
     sk = ctx.seal_keygen_secret(seed, 0)
     rk = ctx.seal_keygen_relin(sk, seed)
-    ev = Evaluator(ctx, GELU_SCALE, rk)
     top = len(qs) - 1
     rng = np.random.default_rng(779 + rank)
     vals, cts, host = [], [], []
@@ -1125,22 +1172,50 @@ def run_gelu_gpu(args, rank, world):
         vals.append(v)
         cts.append(ct)
         host.append(ct.cpu().numpy().view(np.uint64).copy())
-    stream = torch.cuda.current_stream(dev)
+    torch.cuda.synchronize(dev)
+    # the evaluator runs on a stream of its own: the legacy default stream cannot be captured
+    stream = torch.cuda.Stream(dev)
+    ev = Evaluator(ctx, GELU_SCALE, rk, stream=stream)
 
-    in_cts = [Ciphertext.from_device(ctx, c, GELU_SCALE) for c in cts]
+    in_cts = [Ciphertext.from_device(ctx, c, GELU_SCALE, stream) for c in cts]
+    # separate handles for the direct single form and its graph: a direct call
+    # replaces its input's buffer (the in-place mod switch), which a graph's
+    # handles must never have done to them
+    single_in = [Ciphertext(ctx) for _ in cts]
+    graph_single_in = [Ciphertext(ctx) for _ in cts]
+
+    def words(xs):
+        stream.synchronize()
+        return [x.to_numpy() for x in xs]
 
     def step():
         # the lockstep form (inputs are left unchanged)
         return ev.gelu_batch(in_cts)
 
-    def plain_step():
+    def load_single(xs=single_in):
         # GeLUEvaluator::gelu mod-switches its input in place (src/gelu.cpp), so
-        # each call gets a fresh device copy
-        return [ev.gelu(Ciphertext.from_device(ctx, c, GELU_SCALE)) for c in cts]
+        # each call gets the input words again
+        for x, c in zip(xs, cts):
+            x.load(c, GELU_SCALE, stream)
+
+    def plain_step():
+        load_single()
+        return [ev.gelu(x) for x in single_in]
+
+    def timed(f, k):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        a.record(stream)
+        for _ in range(k):
+            f()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b) / k
 
     for _ in range(args.warmup):
         res = step()
-    torch.cuda.synchronize(dev)
+        plain_step()
+    ref = words(res)
 
     def gelu_ref(x):
         return 0.5 * x * (1 + np.tanh(math.sqrt(2 / math.pi) * (x + 0.044715 * x ** 3)))
@@ -1151,12 +1226,33 @@ def run_gelu_gpu(args, rank, world):
         errs[tag] = float(np.max(np.abs(dec - gelu_ref(vals[i]))))
     parity = None
     if rank == 0:
-        c0 = _digest_check("gelu_n16384", res[0].to_numpy(), ("u-5_5", "output"))
-        c1 = _digest_check("gelu_n16384", res[1].to_numpy(), ("u-8_8", "output"))
+        c0 = _digest_check("gelu_n16384", ref[0], ("u-5_5", "output"))
+        c1 = _digest_check("gelu_n16384", ref[1], ("u-8_8", "output"))
         if c0 is not None and c1 is not None:
             parity = {"checked": "output words of ciphertexts 0 (U(-5,5)) and 1 (U(-8,8)) against the oracle's digests",
                       "words_equal_oracle": c0["words_equal_oracle"] and c1["words_equal_oracle"]}
     del res
+
+    # both forms captured once (their caches and constants exist after the warm-up)
+    graph_in = [Ciphertext.from_device(ctx, c, GELU_SCALE, stream) for c in cts]
+    with Graph(stream) as g_lock:
+        g_out = ev.gelu_batch(graph_in)
+    load_single(graph_single_in)
+    with Graph(stream) as g_single:
+        s_out = [ev.gelu(x) for x in graph_single_in]
+    g_lock.launch()
+    lock_same = all(np.array_equal(a, b) for a, b in zip(words(g_out), ref))
+
+    def graph_step():
+        g_lock.launch()
+
+    def graph_plain_step():
+        load_single(graph_single_in)
+        g_single.launch()
+
+    graph_plain_step()
+    single_same = all(np.array_equal(a, b) for a, b in zip(words(s_out), ref))
+
     barrier(world)
     l0 = ng.kernel_launches()
     print(f"engine_launches_before_timed={l0}", file=sys.stderr, flush=True)
@@ -1166,13 +1262,13 @@ def run_gelu_gpu(args, rank, world):
         torch.cuda.synchronize(dev)
         t0.record(stream)
         for _ in range(args.steps):
-            res = step()
+            graph_step()
         t1.record(stream)
         torch.cuda.synchronize(dev)
     launches = ng.kernel_launches() - l0
     barrier(world)
     total_ms = max_over_ranks(t0.elapsed_time(t1), world)
-    del res
+    direct_ms = timed(step, args.steps)
 
     ctx.ntt_timing_begin()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -1185,47 +1281,49 @@ def run_gelu_gpu(args, rank, world):
     instr_ms = e0.elapsed_time(e1)
     del res
 
+    # end to end through the C ABI: inputs from pinned host memory into the
+    # graph's input handles, one graph launch, the outputs back to the host
     h_in = [torch.from_numpy(h.view(np.int64)).pin_memory() for h in host]
+    h_out = [torch.empty((2, g_out[0].info()[1], n), dtype=torch.int64).pin_memory() for _ in g_out]
+    sp = stream.cuda_stream
     torch.cuda.synchronize(dev)
     barrier(world)
     w0 = time.perf_counter()
-    out_bytes = 0
-    loaded = []
-    for h in h_in:
-        c = Ciphertext(ctx)
-        ng.check(ng.lib().nexus_ciphertext_load(c.handle, h.data_ptr(), 2, top, GELU_SCALE, 1, None), "load")
-        loaded.append(c)
-    for r in ev.gelu_batch(loaded):
-        out_bytes += r.to_numpy().nbytes
+    for c, h in zip(graph_in, h_in):
+        ng.check(ng.lib().nexus_ciphertext_load(c.handle, h.data_ptr(), 2, top, GELU_SCALE, 1, sp), "load")
+    g_lock.launch()
+    for r, h in zip(g_out, h_out):
+        ng.check(ng.lib().nexus_ciphertext_store(r.handle, h.data_ptr(), 1, sp), "store")
     torch.cuda.synchronize(dev)
     e2e_s = max_over_ranks(time.perf_counter() - w0, world)
+    e2e_same = all(np.array_equal(a.numpy().view(np.uint64), b) for a, b in zip(h_out, ref))
     in_bytes = sum(h.nbytes for h in host)
+    out_bytes = sum(h.nbytes for h in h_out)
 
-    plain_step()
-    torch.cuda.synchronize(dev)
-    p0 = torch.cuda.Event(enable_timing=True)
-    p1 = torch.cuda.Event(enable_timing=True)
-    p0.record(stream)
+    plain_ms = timed(plain_step, 1)
     res = plain_step()
-    p1.record(stream)
-    torch.cuda.synchronize(dev)
-    plain_ms = p0.elapsed_time(p1)
-    same = all(np.array_equal(a.to_numpy(), b.to_numpy()) for a, b in zip(res[:2], ev.gelu_batch(in_cts[:2])))
+    same = all(np.array_equal(a, b) for a, b in zip(words(res), ref))
     del res
+    plain_graph_ms = timed(graph_plain_step, max(1, args.steps))
 
     value = world * args.steps * GELU_CTS / (total_ms / 1e3)
     peak, peak_kind = _peak_hbm()
     ntt_avg_ms = ntt_ms / max(1, ntt_calls)
     alg_bytes_per_call = 16.0 * n * ntt_limbs / max(1, ntt_calls)
     achieved = alg_bytes_per_call / (ntt_avg_ms / 1e3) / 1e9
+    per_s = lambda ms: world * GELU_CTS / (ms / 1e3)  # noqa: E731
     res = {
         "metric": "gelu_throughput_n16384", "value": value, "unit": "GELU/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic: slots ~ U(-5,5) and U(-8,8) (alternating ciphertexts), seeded; keys and encryptions "
                 "from a SEAL seed",
-        "config": dict(gelu_config(), tuning=tuning),
+        "config": dict(gelu_config(), tuning=tuning,
+                       form="lockstep nexus_gelu_batch captured once as a CUDA graph, one nexus_graph_launch "
+                            "per step"),
         "parity": parity,
+        "graph": {"kernel_nodes": g_lock.info()["kernel_nodes"], "words_equal_direct": bool(lock_same)},
+        "direct_lockstep_form": {"value": per_s(direct_ms), "unit": "GELU/s", "ms_per_step": direct_ms},
         "accuracy": {"max_abs_err_vs_fp64_gelu": errs},
         "roofline": {
             "kernel": "nexus NTT launches inside GELU (k_fwd/k_inv cols+rows)",
@@ -1236,9 +1334,11 @@ def run_gelu_gpu(args, rank, world):
             "traffic_source": "ncu DRAM bytes per limb-NTT of the N=2^16 capture, scaled by N and limbs per launch",
         },
         "e2e": {"value": world * GELU_CTS / e2e_s, "unit": "GELU/s", "h2d_bytes_per_step": in_bytes,
-                "d2h_bytes_per_step": out_bytes},
-        "plain_single_ct_form": {"value": world * GELU_CTS / (plain_ms / 1e3), "unit": "GELU/s",
-                                 "batched_words_equal_single": bool(same)},
+                "d2h_bytes_per_step": out_bytes, "words_equal_direct": bool(e2e_same)},
+        "plain_single_ct_form": {"value": per_s(plain_ms), "unit": "GELU/s",
+                                 "batched_words_equal_single": bool(same),
+                                 "graph_value": per_s(plain_graph_ms),
+                                 "graph_words_equal_direct": bool(single_same)},
         "clocks": clk.summary(),
         "gpu_launches": launches,
     }

@@ -716,6 +716,42 @@ int nexus_seal_ciphertext_save(const uint64_t *words, int size, int limbs, int l
 int nexus_seal_ciphertext_load(const uint8_t *bytes, size_t len, uint64_t *words, size_t capacity_words, int *size,
                                int *limbs, int *log_n, double *scale, uint64_t *parms_id, int *is_ntt_form);
 
+/* ------------------------------------------------------------------------
+ * CUDA-graph capture of engine calls
+ * ------------------------------------------------------------------------ */
+
+/*
+ * Record the engine calls a thread makes on `stream` (the stream the
+ * evaluator was created on; the legacy default stream cannot be captured)
+ * between begin and end, and replay them with one nexus_graph_launch.  The
+ * calls' host-side work (levels, scales, output sizes) happens once, while
+ * capturing; a launch repeats their device work on the same handles, so the
+ * caller reloads the captured inputs (nexus_ciphertext_load into the same
+ * handles, same size and level) and reads the captured outputs.  Run the
+ * calls once before capturing: a call that must wait on the host (an encode
+ * of a new vector constant, a cache built for the first time) invalidates
+ * the capture, and end refuses a graph that frees device memory allocated
+ * before the capture (a buffer that grew inside it), since every launch
+ * would free it again; the handles such a refused capture touched are not
+ * used again.  An output handle first sized inside the capture keeps a graph
+ * allocation that stays valid, at one address, from launch to launch.
+ * Launches of one graph must not overlap.  Between launches a captured
+ * handle is only reloaded (same size and level): a direct call that gives it
+ * a new buffer (an in-place operation outside the graph, a load of a larger
+ * size) leaves the graph pointing at freed memory, so keep separate handles
+ * for direct calls.  nexus_graph_info returns the graph's node, kernel-node
+ * and allocation-node counts.
+ * No counterpart in the reference: NEXUS's CUDA path launches every Phantom
+ * kernel on its own and synchronises its stream after rotations and at the
+ * end of bootstrap_3 (cuda/src/bootstrapping/Bootstrapper.cu:3358-3370).
+ */
+typedef struct nexus_graph nexus_graph;
+int nexus_graph_capture_begin(void *stream);
+int nexus_graph_capture_end(void *stream, nexus_graph **out);
+int nexus_graph_launch(const nexus_graph *graph, void *stream);
+int nexus_graph_info(const nexus_graph *graph, size_t *nodes, size_t *kernel_nodes, size_t *alloc_nodes);
+int nexus_graph_destroy(nexus_graph *graph);
+
 #ifdef __cplusplus
 }
 #endif

@@ -123,6 +123,12 @@ SIGNATURES = [
     ("nexus_get_ntt_form", C.c_int, [C.c_void_p, C.c_void_p]),
     ("nexus_butterfly_rate", C.c_int,
      [C.c_int, C.c_uint64, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("nexus_graph_capture_begin", C.c_int, [C.c_void_p]),
+    ("nexus_graph_capture_end", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("nexus_graph_launch", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("nexus_graph_info", C.c_int, [C.c_void_p, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t),
+                                   C.POINTER(C.c_size_t)]),
+    ("nexus_graph_destroy", C.c_int, [C.c_void_p]),
     ("nexus_tensor_rate", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("nexus_tensor_tile", C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nexus_bert_layer_create", C.c_int,

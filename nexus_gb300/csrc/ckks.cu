@@ -22,6 +22,20 @@ static void ck(cudaError_t e, const char *what)
 
 // ---------------------------------------------------------------- buffers
 
+// the id of the graph capture under way on `s`, or 0 (the legacy default
+// stream is never captured and is not queried)
+static unsigned long long capture_id(cudaStream_t s)
+{
+    if (!s) return 0;
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    unsigned long long id = 0;
+    if (cudaStreamGetCaptureInfo(s, &st, &id) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return st == cudaStreamCaptureStatusActive ? id : 0;
+}
+
 void DeviceBuffer::reserve(size_t words, cudaStream_t s)
 {
     if (words <= words_ && p_) return;
@@ -29,6 +43,7 @@ void DeviceBuffer::reserve(size_t words, cudaStream_t s)
     ck(cudaMallocAsync(&p_, words * sizeof(uint64_t), s), "cudaMallocAsync");
     words_ = words;
     s_ = s;
+    cap_ = capture_id(s);
 }
 
 void DeviceBuffer::release()
@@ -36,6 +51,37 @@ void DeviceBuffer::release()
     if (p_) cudaFreeAsync(p_, s_);
     p_ = nullptr;
     words_ = 0;
+    cap_ = 0;
+}
+
+bool DeviceBuffer::predates_capture() const
+{
+    if (!p_) return false;
+    const unsigned long long id = capture_id(s_);
+    return id != 0 && id != cap_;
+}
+
+Ciphertext &Ciphertext::operator=(Ciphertext &&o) noexcept
+{
+    if (this == &o) return *this;
+    const size_t words = (size_t)o.size_ * o.limbs_ * o.n_;
+    if (o.buf_.get() && words <= buf_.capacity() && buf_.predates_capture()) {
+        cudaMemcpyAsync(buf_.get(), o.buf_.get(), words * 8, cudaMemcpyDeviceToDevice, buf_.stream());
+        size_ = o.size_;
+        limbs_ = o.limbs_;
+        n_ = o.n_;
+        scale_ = o.scale_;
+        o.buf_.release();
+        o.size_ = o.limbs_ = 0;
+        return *this;
+    }
+    buf_ = std::move(o.buf_);
+    size_ = o.size_;
+    limbs_ = o.limbs_;
+    n_ = o.n_;
+    scale_ = o.scale_;
+    s_ = o.s_;
+    return *this;
 }
 
 void Ciphertext::resize(const Context &c, int size, int limbs, cudaStream_t s)
@@ -201,9 +247,54 @@ uint32_t Evaluator::galois_elt(int step) const
 
 // ---------------------------------------------------------------- encoding
 
+namespace {
+
+uint64_t bits_of(double v)
+{
+    uint64_t b;
+    std::memcpy(&b, &v, sizeof b);
+    return b;
+}
+
+// the value every entry of `v` holds, or false (empty, NaN or differing entries)
+template <class T>
+bool constant_value(const std::vector<T> &v, std::complex<double> &c)
+{
+    if (v.empty()) return false;
+    for (const T &x : v)
+        if (!(x == v[0])) return false;
+    c = std::complex<double>(v[0]);
+    return true;
+}
+
+// at most this many words (8 GiB) of cached constant encodings per evaluator
+constexpr size_t kConstCacheWords = (size_t)1 << 30;
+
+}  // namespace
+
+bool Evaluator::const_lookup(const ConstKey &k, Plaintext &out) const
+{
+    auto it = const_cache_.find(k);
+    if (it == const_cache_.end()) return false;
+    out = it->second;
+    return true;
+}
+
+void Evaluator::const_store(const ConstKey &k, const Plaintext &pt)
+{
+    const size_t words = (size_t)pt.limbs() * c_.n;
+    if (const_cache_words_ + words > kConstCacheWords) return;
+    const_cache_[k] = pt;
+    const_cache_words_ += words;
+}
+
 void Evaluator::encode(const std::vector<double> &values, int limbs, double scale, Plaintext &out)
 {
     if (limbs < 1 || limbs > top_limbs()) throw std::invalid_argument("parms_id is not valid for encryption parameters");
+    std::complex<double> cv;
+    const bool constant = constant_value(values, cv);
+    const ConstKey key{bits_of(cv.real()), bits_of(cv.imag()), bits_of(scale), values.size(), limbs, 0};
+    if (constant && const_lookup(key, out)) return;
     std::vector<std::complex<double>> v(values.size());
     for (size_t i = 0; i < values.size(); ++i) v[i] = values[i];
     std::vector<uint64_t> host((size_t)limbs * c_.n);
@@ -212,17 +303,23 @@ void Evaluator::encode(const std::vector<double> &values, int limbs, double scal
     ck(cudaMemcpyAsync(out.mutable_data(), host.data(), host.size() * 8, cudaMemcpyHostToDevice, s_), "upload");
     ck(cudaStreamSynchronize(s_), "encode");  // host buffer lifetime
     ntt_forward(c_, out.mutable_data(), 1, 0, limbs, s_);
+    if (constant) const_store(key, out);
 }
 
 void Evaluator::encode(const std::vector<std::complex<double>> &values, int limbs, double scale, Plaintext &out)
 {
     if (limbs < 1 || limbs > top_limbs()) throw std::invalid_argument("parms_id is not valid for encryption parameters");
+    std::complex<double> cv;
+    const bool constant = constant_value(values, cv);
+    const ConstKey key{bits_of(cv.real()), bits_of(cv.imag()), bits_of(scale), values.size(), limbs, 0};
+    if (constant && const_lookup(key, out)) return;
     std::vector<uint64_t> host((size_t)limbs * c_.n);
     enc_->encode(values.data(), values.size(), scale, limbs, host.data());
     out.set_vector(c_, limbs, scale, s_);
     ck(cudaMemcpyAsync(out.mutable_data(), host.data(), host.size() * 8, cudaMemcpyHostToDevice, s_), "upload");
     ck(cudaStreamSynchronize(s_), "encode");
     ntt_forward(c_, out.mutable_data(), 1, 0, limbs, s_);
+    if (constant) const_store(key, out);
 }
 
 void Evaluator::encode_many(const std::vector<const std::vector<std::complex<double>> *> &values, int limbs,
@@ -262,12 +359,17 @@ void Evaluator::encode_then_drop(const std::vector<std::complex<double>> &values
                                  Plaintext &out)
 {
     if (limbs < 1 || limbs > top_limbs()) throw std::invalid_argument("cannot switch to higher level modulus");
+    std::complex<double> cv;
+    const bool constant = constant_value(values, cv);
+    const ConstKey key{bits_of(cv.real()), bits_of(cv.imag()), bits_of(scale), values.size(), limbs, 1};
+    if (constant && const_lookup(key, out)) return;
     std::vector<uint64_t> host((size_t)limbs * c_.n);
     enc_->encode(values.data(), values.size(), scale, limbs, host.data(), top_limbs());
     out.set_vector(c_, limbs, scale, s_);
     ck(cudaMemcpyAsync(out.mutable_data(), host.data(), host.size() * 8, cudaMemcpyHostToDevice, s_), "upload");
     ck(cudaStreamSynchronize(s_), "encode");
     ntt_forward(c_, out.mutable_data(), 1, 0, limbs, s_);
+    if (constant) const_store(key, out);
 }
 
 void Evaluator::encode_then_drop(double value, int limbs, double scale, Plaintext &out)

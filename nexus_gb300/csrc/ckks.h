@@ -10,6 +10,7 @@
 #include <complex>
 #include <cstdint>
 #include <map>
+#include <tuple>
 #include <utility>
 #include <stdexcept>
 #include <string>
@@ -43,6 +44,11 @@ public:
     void release();
     uint64_t *get() const { return p_; }
     size_t capacity() const { return words_; }
+    cudaStream_t stream() const { return s_; }
+    // true while a CUDA-graph capture is under way on this buffer's stream
+    // and the buffer was allocated outside it: the capture may read and
+    // write it but cannot free it (a graph frees only its own allocations)
+    bool predates_capture() const;
 
 private:
     void swap(DeviceBuffer &o) noexcept
@@ -50,10 +56,12 @@ private:
         std::swap(p_, o.p_);
         std::swap(words_, o.words_);
         std::swap(s_, o.s_);
+        std::swap(cap_, o.cap_);
     }
     uint64_t *p_ = nullptr;
     size_t words_ = 0;
     cudaStream_t s_ = nullptr;
+    unsigned long long cap_ = 0;   // id of the capture the buffer was allocated in, 0 outside any
 };
 
 class Ciphertext {
@@ -62,7 +70,13 @@ public:
     Ciphertext(const Ciphertext &o);
     Ciphertext &operator=(const Ciphertext &o);
     Ciphertext(Ciphertext &&) noexcept = default;
-    Ciphertext &operator=(Ciphertext &&) noexcept = default;
+    // Takes o's words.  Outside a graph capture this moves o's buffer in.
+    // While a capture is under way on this ciphertext's stream and its
+    // buffer was allocated before the capture (a caller's handle), the
+    // buffer is kept and o's words are copied into it when they fit, so an
+    // in-place operation on a captured input leaves the handle's memory in
+    // place for the caller to reload before each launch.
+    Ciphertext &operator=(Ciphertext &&o) noexcept;
 
     // allocate for size x limbs (contents undefined)
     void resize(const Context &c, int size, int limbs, cudaStream_t s);
@@ -123,7 +137,12 @@ public:
     ~Evaluator();
     Context &context() { return c_; }
     cudaStream_t stream() const { return s_; }
-    void set_stream(cudaStream_t s) { s_ = s; }
+    void set_stream(cudaStream_t s)
+    {
+        s_ = s;
+        const_cache_.clear();   // cached encodings are copied on the stream they were made on
+        const_cache_words_ = 0;
+    }
     size_t slot_count() const { return c_.n / 2; }
     int top_limbs() const { return c_.k - 1; }
     uint64_t modulus(int i) const { return c_.q[i]; }
@@ -245,6 +264,25 @@ private:
     std::map<uint32_t, DeviceBuffer> hoist_keys_, hoist_masks_;
     std::map<std::pair<uint32_t, int>, DeviceBuffer> hoist_corrs_;
     DeviceBuffer hoist_flag_;
+    // Encodings of constant vectors (every slot the same value), the kind of
+    // vector NEXUS's operators encode on every call: the first encode of a
+    // (value, slot count, limbs, scale, form) runs the FFT and the upload,
+    // later ones copy the cached device words.  Encoding is a pure function
+    // of those, so the words are the same; it also keeps repeated operator
+    // calls free of host waits, so they can be captured in a CUDA graph.
+    struct ConstKey {
+        uint64_t re, im, scale;
+        size_t count;
+        int limbs, form;   // form 0: encode, 1: encode_then_drop
+        bool operator<(const ConstKey &o) const
+        {
+            return std::tie(re, im, scale, count, limbs, form) < std::tie(o.re, o.im, o.scale, o.count, o.limbs, o.form);
+        }
+    };
+    bool const_lookup(const ConstKey &k, Plaintext &out) const;
+    void const_store(const ConstKey &k, const Plaintext &pt);
+    std::map<ConstKey, Plaintext> const_cache_;
+    size_t const_cache_words_ = 0;
 };
 
 bool are_close(double a, double b);

@@ -45,6 +45,13 @@ class Ciphertext:
                                           _stream_ptr(stream)), "nexus_ciphertext_load")
         return ct
 
+    def load(self, t, scale: float, stream=None) -> None:
+        """Overwrite this ciphertext with the device tensor ``t``
+        [size][limbs][N] on ``stream``; a handle of at least that size keeps
+        its buffer (what a captured graph's input needs)."""
+        check(lib().nexus_ciphertext_load(self._h, t.data_ptr(), t.shape[0], t.shape[1], float(scale), 0,
+                                          _stream_ptr(stream)), "nexus_ciphertext_load")
+
     def info(self):
         size, limbs, scale, ptr = C.c_int(), C.c_int(), C.c_double(), C.c_void_p()
         check(lib().nexus_ciphertext_info(self._h, C.byref(size), C.byref(limbs), C.byref(scale), C.byref(ptr)),
@@ -327,11 +334,14 @@ class Bootstrapper:
         check(lib().nexus_bootstrap(self._h, ct.handle, rtn.handle), "nexus_bootstrap")
         return rtn
 
-    def bootstrap_batch(self, cts: list) -> list:
+    def bootstrap_batch(self, cts: list, out: list | None = None) -> list:
         """bootstrap_3 of every ciphertext, run in lockstep (one launch per
         operation for the whole batch, each key read once); the inputs are
-        left unchanged."""
-        res = [Ciphertext(self.ctx) for _ in cts]
+        left unchanged.  ``out``: ciphertexts to write (kept buffers when
+        already of the result's size), else new ones."""
+        res = out if out is not None else [Ciphertext(self.ctx) for _ in cts]
+        if len(res) != len(cts):
+            raise ValueError("one output per input")
         a = (C.c_void_p * len(cts))(*[c.handle.value for c in cts])
         r = (C.c_void_p * len(res))(*[x.handle.value for x in res])
         check(lib().nexus_bootstrap_batch(self._h, a, len(cts), r), "nexus_bootstrap_batch")
@@ -387,3 +397,48 @@ def lt_coefficients_3(logn: int, log_nh: int, boundary_k: int, which: int) -> np
     check(lib().nexus_lt_coefficients_3(logn, log_nh, boundary_k, which, out.ctypes.data, C.byref(cnt),
                                         C.byref(ln)), "nexus_lt_coefficients_3")
     return out
+
+
+class Graph:
+    """CUDA graph of the engine calls made on ``stream`` inside the ``with``
+    block (nexus_graph_capture_begin / _end); ``launch()`` replays their
+    device work on the same ciphertext handles.  Run the calls once before
+    capturing, so that caches and grown buffers already exist.  Between
+    launches only reload the captured handles (same size and level); a
+    direct call that gives one of them a new buffer leaves the graph pointing
+    at freed memory, so direct calls use handles of their own."""
+
+    def __init__(self, stream):
+        if stream is None:
+            raise ValueError("capture needs the evaluator's own stream, not the legacy default stream")
+        self.stream = stream
+        self._h = None
+
+    def __enter__(self):
+        check(lib().nexus_graph_capture_begin(_stream_ptr(self.stream)), "nexus_graph_capture_begin")
+        return self
+
+    def __exit__(self, exc_type, exc, tb):
+        h = C.c_void_p()
+        rc = lib().nexus_graph_capture_end(_stream_ptr(self.stream), C.byref(h))
+        if exc_type is not None:
+            if rc == 0:
+                lib().nexus_graph_destroy(h)
+            return False
+        check(rc, "nexus_graph_capture_end")
+        self._h = h
+        return False
+
+    def launch(self, stream=None) -> None:
+        check(lib().nexus_graph_launch(self._h, _stream_ptr(self.stream if stream is None else stream)),
+              "nexus_graph_launch")
+
+    def info(self) -> dict:
+        nodes, kernels, allocs = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        check(lib().nexus_graph_info(self._h, C.byref(nodes), C.byref(kernels), C.byref(allocs)), "nexus_graph_info")
+        return {"nodes": nodes.value, "kernel_nodes": kernels.value, "alloc_nodes": allocs.value}
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nexus_graph_destroy(self._h)
+            self._h = None
