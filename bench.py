@@ -125,6 +125,23 @@ def _ntt_compute_bound(ng, q: int, limb_ntts: int, ms: float, n: int):
             "peak_source": "measured here: nexus_butterfly_rate, the NTT's forward butterfly on register data"}
 
 
+def _int_mul_roofline(compute: dict, hbm_achieved: float, hbm_peak: float, hbm_peak_kind: str, **rest) -> dict:
+    """The roofline object of an NTT-dominated line: the binding roof is the
+    integer-multiply pipe, measured as the rate of the NTT's own butterflies
+    (achieved butterflies/s over that rate; the multiplies per butterfly are
+    fixed, so this is also the multiply-rate fraction); the HBM fraction of
+    the same launches sits beside it."""
+    out = {"bound": "int_mul", "achieved": compute["achieved"], "peak": compute["peak"], "unit": "butterflies/s",
+           "frac": compute["frac"], "peak_source": compute["peak_source"],
+           "hbm": {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_achieved / hbm_peak,
+                   "peak_source": hbm_peak_kind}}
+    for k in ("peak_forward", "peak_inverse"):
+        if k in compute:
+            out[k] = compute[k]
+    out.update(rest)
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling while the timed region runs."""
 
@@ -285,16 +302,13 @@ def run_ntt_gpu(args, rank, world):
         "data": "synthetic uniform residues (seeded)",
         "config": ntt_config(),
         "ntt_form": ctx.ntt_form(),
-        "roofline": {
-            "kernel": ("nexus_ntt_forward (k_fwd_cluster, one pass)" if ctx.ntt_form() == 1
-                       else "nexus_ntt_forward (k_fwd_cols + k_fwd_rows)"),
-            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "peak_source": peak_kind,
-            "algorithmic_bytes_per_launch": alg_bytes,
-            "traffic": _profile_traffic("ntt_forward_n65536_l24_64ct"),
-            "int_multiply_pipe": _int_pipe("ntt_forward_n65536_l24_64ct", "the 60-bit NTT passes"),
-            "compute_bound": _ntt_compute_bound(ng, qs[0], limbs, per_launch_ms, n),
-        },
+        "roofline": _int_mul_roofline(
+            _ntt_compute_bound(ng, qs[0], limbs, per_launch_ms, n), achieved, peak, peak_kind,
+            kernel=("nexus_ntt_forward (k_fwd_cluster, one pass)" if ctx.ntt_form() == 1
+                    else "nexus_ntt_forward (k_fwd_cols + k_fwd_rows)"),
+            algorithmic_bytes_per_launch=alg_bytes,
+            traffic=_profile_traffic("ntt_forward_n65536_l24_64ct"),
+            int_multiply_pipe=_int_pipe("ntt_forward_n65536_l24_64ct", "the 60-bit NTT passes")),
         "e2e": {"value": limbs * e2e_steps * world / (e2e_ms / 1e3), "unit": "limb-NTT/s",
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "clocks": clk.summary(),
@@ -480,16 +494,14 @@ def run_mm_gpu(args, rank, world):
         "config": mm_config(),
         "parity": parity,
         "accuracy": {"max_abs_err_vs_fp64": err, "rows_checked": check_rows},
-        "roofline": {
-            "kernel": "nexus NTT launches inside the MatMul (k_fwd/k_inv cols+rows)",
-            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "peak_source": peak_kind,
-            "algorithmic_bytes_per_launch": alg_bytes_per_call,
-            "avg_launch_ms": ntt_avg_ms, "launches_per_step": ntt_calls, "limb_ntts_per_step": ntt_limbs,
-            "share_of_step": ntt_ms / instr_ms,
-            "traffic": _ntt_traffic(ntt_limbs / max(1, ntt_calls)),
-            "traffic_source": "ncu DRAM bytes per limb-NTT of the N=2^16 capture x limbs per launch",
-        },
+        "roofline": _int_mul_roofline(
+            _butterfly_roof(ng, qs[0], ntt_limbs, ntt_ms, MM_LOGN), achieved, peak, peak_kind,
+            kernel="nexus NTT launches inside the MatMul (k_fwd/k_inv cols+rows)",
+            algorithmic_bytes_per_launch=alg_bytes_per_call,
+            avg_launch_ms=ntt_avg_ms, launches_per_step=ntt_calls, limb_ntts_per_step=ntt_limbs,
+            share_of_step=ntt_ms / instr_ms,
+            traffic=_ntt_traffic(ntt_limbs / max(1, ntt_calls)),
+            traffic_source="ncu DRAM bytes per limb-NTT of the N=2^16 capture x limbs per launch"),
         "e2e": {"value": world * e2e_steps / e2e_s, "unit": "matmul/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes},
         "clocks": clk.summary(),
@@ -783,18 +795,15 @@ def run_boot_gpu(args, rank, world):
                                  "ms_per_step": direct_ms},
         "accuracy": {"max_abs_err_vs_input": err, "precision_bits": -float(np.log2(err)),
                      "output_limbs": out_limbs},
-        "roofline": {
-            "kernel": "nexus NTT launches inside the bootstrap (k_fwd/k_inv cols+rows)",
-            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "peak_source": peak_kind,
-            "algorithmic_bytes_per_launch": alg_bytes_per_call,
-            "avg_launch_ms": ntt_avg_ms, "launches_per_step": ntt_calls, "limb_ntts_per_step": ntt_limbs,
-            "share_of_step": ntt_ms / instr_ms,
-            "traffic": _ntt_traffic(ntt_limbs / max(1, ntt_calls)),
-            "traffic_source": "ncu DRAM bytes per limb-NTT of the 51-bit NTT capture x limbs per launch",
-            "int_multiply_pipe": _int_pipe("keyswitch_n65536_l31_4ct", "the key switch's ModUp NTT passes"),
-            "compute_bound": _butterfly_roof(ng, qs[1], ntt_limbs, ntt_ms, BOOT_LOGN),
-        },
+        "roofline": _int_mul_roofline(
+            _butterfly_roof(ng, qs[1], ntt_limbs, ntt_ms, BOOT_LOGN), achieved, peak, peak_kind,
+            kernel="nexus NTT launches inside the bootstrap (k_fwd/k_inv cols+rows)",
+            algorithmic_bytes_per_launch=alg_bytes_per_call,
+            avg_launch_ms=ntt_avg_ms, launches_per_step=ntt_calls, limb_ntts_per_step=ntt_limbs,
+            share_of_step=ntt_ms / instr_ms,
+            traffic=_ntt_traffic(ntt_limbs / max(1, ntt_calls)),
+            traffic_source="ncu DRAM bytes per limb-NTT of the 51-bit NTT capture x limbs per launch",
+            int_multiply_pipe=_int_pipe("keyswitch_n65536_l31_4ct", "the key switch's ModUp NTT passes")),
         "e2e": {"value": world * BOOT_CTS / e2e_s, "unit": "bootstraps/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes, "words_equal_direct": bool(e2e_same)},
         "plain_single_ct_form": {"value": world * BOOT_CTS / (plain_ms / 1e3), "unit": "bootstraps/s",
@@ -1069,16 +1078,14 @@ def run_bert_gpu(args, rank, world):
         "accuracy": {"max_abs_err_vs_fp64_same_approx": max(errs), "mean_abs_err_vs_fp64_same_approx":
                      float(np.mean(means)), "max_abs_err_vs_fp64_exact": max(errs_exact),
                      "bits_vs_same_approx": -float(np.log2(max(errs)))},
-        "roofline": {
-            "kernel": "nexus NTT launches inside the layer (k_fwd/k_inv cols+rows)",
-            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg_bytes_per_call,
-            "avg_launch_ms": ntt_avg_ms, "launches_per_step": ntt_calls, "limb_ntts_per_step": ntt_limbs,
-            "share_of_step": ntt_ms / instr_ms,
-            "traffic": _ntt_traffic(ntt_limbs / max(1, ntt_calls)),
-            "traffic_source": "ncu DRAM bytes per limb-NTT of the 51-bit NTT capture x limbs per launch",
-            "compute_bound": _butterfly_roof(ng, qs[1], ntt_limbs, ntt_ms, BERT_LOGN),
-        },
+        "roofline": _int_mul_roofline(
+            _butterfly_roof(ng, qs[1], ntt_limbs, ntt_ms, BERT_LOGN), achieved, peak, peak_kind,
+            kernel="nexus NTT launches inside the layer (k_fwd/k_inv cols+rows)",
+            algorithmic_bytes_per_launch=alg_bytes_per_call,
+            avg_launch_ms=ntt_avg_ms, launches_per_step=ntt_calls, limb_ntts_per_step=ntt_limbs,
+            share_of_step=ntt_ms / instr_ms,
+            traffic=_ntt_traffic(ntt_limbs / max(1, ntt_calls)),
+            traffic_source="ncu DRAM bytes per limb-NTT of the 51-bit NTT capture x limbs per launch"),
         "e2e": {"value": e2e_s, "unit": "s per layer", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes},
         "plain_single_ct_form": {"value": plain_ms / 1e3, "unit": "s per layer",
@@ -1325,14 +1332,13 @@ def run_gelu_gpu(args, rank, world):
         "graph": {"kernel_nodes": g_lock.info()["kernel_nodes"], "words_equal_direct": bool(lock_same)},
         "direct_lockstep_form": {"value": per_s(direct_ms), "unit": "GELU/s", "ms_per_step": direct_ms},
         "accuracy": {"max_abs_err_vs_fp64_gelu": errs},
-        "roofline": {
-            "kernel": "nexus NTT launches inside GELU (k_fwd/k_inv cols+rows)",
-            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg_bytes_per_call,
-            "avg_launch_ms": ntt_avg_ms, "launches_per_step": ntt_calls, "share_of_step": ntt_ms / instr_ms,
-            "traffic": _ntt_traffic(ntt_limbs / max(1, ntt_calls), n),
-            "traffic_source": "ncu DRAM bytes per limb-NTT of the N=2^16 capture, scaled by N and limbs per launch",
-        },
+        "roofline": _int_mul_roofline(
+            _butterfly_roof(ng, qs[0], ntt_limbs, ntt_ms, GELU_LOGN), achieved, peak, peak_kind,
+            kernel="nexus NTT launches inside GELU (k_fwd/k_inv cols+rows)",
+            algorithmic_bytes_per_launch=alg_bytes_per_call,
+            avg_launch_ms=ntt_avg_ms, launches_per_step=ntt_calls, share_of_step=ntt_ms / instr_ms,
+            traffic=_ntt_traffic(ntt_limbs / max(1, ntt_calls), n),
+            traffic_source="ncu DRAM bytes per limb-NTT of the N=2^16 capture, scaled by N and limbs per launch"),
         "e2e": {"value": world * GELU_CTS / e2e_s, "unit": "GELU/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes, "words_equal_direct": bool(e2e_same)},
         "plain_single_ct_form": {"value": per_s(plain_ms), "unit": "GELU/s",
