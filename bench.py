@@ -896,12 +896,18 @@ def bert_config():
 
 
 def run_bert_gpu(args, rank, world):
+    """The encrypted BERT-base encoder layer at N=2^16 (three requests of 128,
+    32 and 64 tokens in two lanes).  The headline form is the lockstep layer
+    (nexus_bert_layer_forward) captured once as a CUDA graph and replayed per
+    step; the same call made directly and the plain form (each lane on its
+    own, one ciphertext per operation) are timed beside it, with every form's
+    words checked against the direct lockstep call's."""
     import numpy as np
     import torch
 
     import nexus_gb300 as ng
     from nexus_gb300 import bert as NB
-    from nexus_gb300.operators import Bootstrapper, Ciphertext, Evaluator
+    from nexus_gb300.operators import Bootstrapper, Ciphertext, Evaluator, Graph
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
@@ -910,7 +916,9 @@ def run_bert_gpu(args, rank, world):
     ctx = ng.Context(BERT_LOGN, qs)
     seed = _seal_seed(BERT_SEED + rank)
     sk = ctx.seal_keygen_secret(seed, 192)
-    ev = Evaluator(ctx, BERT_SCALE, ctx.seal_keygen_relin(sk, seed))
+    # the evaluator runs on a stream of its own: the legacy default stream cannot be captured
+    stream = torch.cuda.Stream(dev)
+    ev = Evaluator(ctx, BERT_SCALE, ctx.seal_keygen_relin(sk, seed), stream=stream)
     log_nh = BERT_LOGN - 1
     bs = Bootstrapper(ev, 10, log_nh, log_nh, len(qs) - 2, BERT_SCALE, 25, 59, 2, 1)
     shape = NB.BertShape()
@@ -928,19 +936,24 @@ def run_bert_gpu(args, rank, world):
         e = ctx.galois_elt(s)
         ev.add_galois_key(e, ctx.seal_keygen_galois(sk, e, seed))
     top = len(qs) - 1
-    x, host_x = [], []
+    dev_x, host_x = [], []
     for lane in range(len(shape.lanes)):
         for v in NB.pack_lane(shape, n // 2, lane, tokens[lane]):
             pt = torch.empty((top, n), dtype=torch.int64, device=dev)
             ctx.encode(v, BERT_SCALE, top, pt)
             ct = ctx.seal_encrypt_symmetric(sk, pt, top, seed)
-            x.append(Ciphertext.from_device(ctx, ct, BERT_SCALE))
+            dev_x.append(ct)
             host_x.append(ct.cpu().numpy().view(np.uint64).copy())
-            del pt, ct
-    stream = torch.cuda.current_stream(dev)
+            del pt
+    torch.cuda.synchronize(dev)
+    x = [Ciphertext.from_device(ctx, ct, BERT_SCALE, stream) for ct in dev_x]
 
     def step():
         return layer.forward(x, lockstep=True)
+
+    def words(xs):
+        stream.synchronize()
+        return [c.to_numpy() for c in xs]
 
     t_setup = time.perf_counter()
     res = step()            # the first call encodes the weights' diagonals (kept on the device)
@@ -949,6 +962,7 @@ def run_bert_gpu(args, rank, world):
     for _ in range(max(0, args.warmup - 1)):
         res = step()
     torch.cuda.synchronize(dev)
+    ref_words = words(res)
 
     # decrypted output against the FP64 layer (NEXUS's approximations, and exact)
     errs, errs_exact, means = [], [], []
@@ -963,6 +977,14 @@ def run_bert_gpu(args, rank, world):
             means.append(float(np.mean(np.abs(y - r))))
             errs_exact.append(float(np.max(np.abs(y - re))))
     del res
+
+    # the lockstep layer captured once; its handles serve the graph alone
+    graph_x = [Ciphertext.from_device(ctx, ct, BERT_SCALE, stream) for ct in dev_x]
+    with Graph(stream) as graph:
+        graph_out = layer.forward(graph_x, lockstep=True)
+    graph.launch()
+    graph_same = all(np.array_equal(a, b) for a, b in zip(words(graph_out), ref_words))
+
     barrier(world)
     l0 = ng.kernel_launches()
     print(f"engine_launches_before_timed={l0}", file=sys.stderr, flush=True)
@@ -972,12 +994,20 @@ def run_bert_gpu(args, rank, world):
         torch.cuda.synchronize(dev)
         t0.record(stream)
         for _ in range(args.steps):
-            res = step()
+            graph.launch()
         t1.record(stream)
         torch.cuda.synchronize(dev)
     launches = ng.kernel_launches() - l0
     barrier(world)
     total_ms = max_over_ranks(t0.elapsed_time(t1), world)
+    d0 = torch.cuda.Event(enable_timing=True)
+    d1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    d0.record(stream)
+    res = step()
+    d1.record(stream)
+    torch.cuda.synchronize(dev)
+    direct_ms = d0.elapsed_time(d1)
     del res
 
     ctx.ntt_timing_begin()
@@ -999,22 +1029,26 @@ def run_bert_gpu(args, rank, world):
     layer.set_timing(False)
     del res
 
-    # end to end: the encrypted inputs from pinned host memory, the layer, the
-    # outputs back to the host
+    # end to end: the encrypted inputs from pinned host memory into the
+    # graph's input handles, one graph launch, the outputs back to pinned host memory
     h_in = [torch.from_numpy(h.view(np.int64)).pin_memory() for h in host_x]
+    out_shape = graph_out[0].info()
+    h_out = [torch.empty((out_shape[0], out_shape[1], n), dtype=torch.int64).pin_memory() for _ in graph_out]
+    sp = stream.cuda_stream
     torch.cuda.synchronize(dev)
     barrier(world)
     w0 = time.perf_counter()
-    loaded = []
-    for h in h_in:
-        c = Ciphertext(ctx)
+    for c, h in zip(graph_x, h_in):
         ng.check(ng.lib().nexus_ciphertext_load(c.handle, h.data_ptr(), h.shape[0], h.shape[1], BERT_SCALE, 1,
-                                                None), "load")
-        loaded.append(c)
-    out_bytes = sum(r.to_numpy().nbytes for r in layer.forward(loaded, lockstep=True))
+                                                sp), "load")
+    graph.launch()
+    for r, h in zip(graph_out, h_out):
+        ng.check(ng.lib().nexus_ciphertext_store(r.handle, h.data_ptr(), 1, sp), "store")
     torch.cuda.synchronize(dev)
     e2e_s = max_over_ranks(time.perf_counter() - w0, world)
+    e2e_same = all(np.array_equal(a.numpy().view(np.uint64), b) for a, b in zip(h_out, ref_words))
     in_bytes = sum(h.nbytes for h in host_x)
+    out_bytes = sum(h.nbytes for h in h_out)
 
     # the plain form: each lane on its own, one ciphertext per operation
     p0 = torch.cuda.Event(enable_timing=True)
@@ -1028,7 +1062,7 @@ def run_bert_gpu(args, rank, world):
     blocks_plain = [layer.stage_times(lockstep=False, lane=l) for l in range(layer.n_lanes)]
     layer.set_timing(False)
     blocks_plain = {k: sum(b[k] for b in blocks_plain) for k in blocks_plain[0]}
-    same = all(np.array_equal(a.to_numpy(), b) for a, b in zip(res[:layer.n_hid], lock_words))
+    same = all(np.array_equal(a, b) for a, b in zip(words(res[:layer.n_hid]), lock_words))
     del res
 
     # word parity at this configuration: the Q, K and V projections of the
@@ -1037,12 +1071,13 @@ def run_bert_gpu(args, rank, world):
     if rank == 0:
         import hashlib
         x2 = [Ciphertext.from_numpy(ctx, np.ascontiguousarray(h[:, :2, :]), BERT_SCALE) for h in host_x]
+        torch.cuda.synchronize(dev)
         nh = layer.n_head
         got = {}
         for which, name in ((0, "q"), (1, "k"), (2, "v")):
             y = layer.stage(NB.BERT_PROJECT, which, x2, nh, True)[:nh]
-            got[name] = [hashlib.sha256(np.ascontiguousarray(t.to_numpy(), dtype="<u8").tobytes()).hexdigest()
-                         for t in y]
+            got[name] = [hashlib.sha256(np.ascontiguousarray(t, dtype="<u8").tobytes()).hexdigest()
+                         for t in words(y)]
             del y
         try:
             want = json.loads((ROOT / "tests" / "golden" / "bench_digests.json").read_text())
@@ -1072,8 +1107,12 @@ def run_bert_gpu(args, rank, world):
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic: weights ~ N(0,0.02), tokens ~ N(0,1), seeded; keys and encryptions from a SEAL seed",
-        "config": dict(bert_config(), tuning=tuning),
+        "config": dict(bert_config(), tuning=tuning,
+                       form="lockstep nexus_bert_layer_forward captured once as a CUDA graph, one "
+                            "nexus_graph_launch per step"),
         "parity": parity,
+        "graph": {"kernel_nodes": graph.info()["kernel_nodes"], "words_equal_direct": bool(graph_same)},
+        "direct_lockstep_form": {"value": direct_ms / 1e3, "unit": "s per layer"},
         "throughput": {"value": world * 224 / (step_ms / 1e3), "unit": "tokens/s"},
         "accuracy": {"max_abs_err_vs_fp64_same_approx": max(errs), "mean_abs_err_vs_fp64_same_approx":
                      float(np.mean(means)), "max_abs_err_vs_fp64_exact": max(errs_exact),
@@ -1087,7 +1126,7 @@ def run_bert_gpu(args, rank, world):
             traffic=_ntt_traffic(ntt_limbs / max(1, ntt_calls)),
             traffic_source="ncu DRAM bytes per limb-NTT of the 51-bit NTT capture x limbs per launch"),
         "e2e": {"value": e2e_s, "unit": "s per layer", "h2d_bytes_per_step": in_bytes,
-                "d2h_bytes_per_step": out_bytes},
+                "d2h_bytes_per_step": out_bytes, "words_equal_direct": bool(e2e_same)},
         "plain_single_ct_form": {"value": plain_ms / 1e3, "unit": "s per layer",
                                  "lockstep_speedup": plain_ms / step_ms, "words_equal_lockstep": bool(same)},
         "blocks_ms": {"lockstep": blocks_lock, "plain": blocks_plain},

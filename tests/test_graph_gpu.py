@@ -201,3 +201,60 @@ def test_gelu_graph_single_and_lockstep(gelu_env):
         g2.launch()
         for a, b in zip(_words(ys, stream), want_batch[k]):
             assert np.array_equal(a, b)
+
+
+def test_bert_layer_graph_matches_oracle(cuda):
+    """The whole lockstep encoder layer (the reduced size of
+    tests/golden/bert_digests.json: N=2^13, hidden 64, requests of 16 | 4 + 8
+    tokens) captured as one graph: replays on the captured inputs give the
+    oracle's output digests, the same as the direct call."""
+    import torch
+
+    import nexus_gb300 as ng
+    from nexus_gb300 import bert as NB
+    from nexus_gb300.operators import Bootstrapper, Ciphertext, Evaluator, Graph
+    from tests.test_bert_gpu import DOC, _lane_digests, _shape, _want
+    c = DOC
+    n = 1 << c["log_n"]
+    qs = [int(q) for q in c["moduli"]]
+    ctx = ng.Context(c["log_n"], qs)
+    seed = np.array(c["seed"], dtype=np.uint64)
+    scale = 2.0 ** c["scale_log2"]
+    sk = ctx.seal_keygen_secret(seed, c["hamming_weight"])
+    rk = ctx.seal_keygen_relin(sk, seed)
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream()
+    ev = Evaluator(ctx, scale, rk, stream=stream)
+    log_nh = c["log_n"] - 1
+    bs = Bootstrapper(ev, c["loge"], log_nh, log_nh, len(qs) - 2, scale, c["boundary_K"], c["sin_cos_deg"],
+                      c["scale_factor"], c["inverse_deg"])
+    sh = _shape()
+    w = NB.random_weights(sh, np.random.default_rng(c["weight_seed"]))
+    rng = np.random.default_rng(c["token_seed"])
+    tokens = [[rng.normal(0, 1, (L, sh.hidden)) for (_, L) in lane] for lane in sh.lanes]
+    steps = bs.rotation_steps(log_nh)
+    bs.prepare_mod_polynomial()
+    bs.generate_LT_coefficient_3()
+    layer = NB.BertLayer(bs, sh, w)
+    for s in steps + [s for s in layer.rotation_steps() if s not in steps]:
+        e = ctx.galois_elt(s)
+        ev.add_galois_key(e, ctx.seal_keygen_galois(sk, e, seed))
+    top = len(qs) - 1
+    cts = []
+    for lane in range(len(sh.lanes)):
+        for v in NB.pack_lane(sh, n // 2, lane, tokens[lane]):
+            pt = torch.empty((top, n), dtype=torch.int64, device="cuda")
+            ctx.encode(v, scale, top, pt)
+            cts.append(ctx.seal_encrypt_symmetric(sk, pt, top, seed))
+    torch.cuda.synchronize()
+    x = [Ciphertext.from_device(ctx, t, scale, stream) for t in cts]
+    direct = layer.forward(x, lockstep=True)       # also encodes and caches the layer's plaintexts
+    stream.synchronize()
+    assert _lane_digests(direct, layer.n_hid) == _want("output")
+    gx = [Ciphertext.from_device(ctx, t, scale, stream) for t in cts]
+    with Graph(stream) as g:
+        out = layer.forward(gx, lockstep=True)
+    for _ in range(2):
+        g.launch()
+        stream.synchronize()
+        assert _lane_digests(out, layer.n_hid) == _want("output")
