@@ -698,8 +698,10 @@ def run_boot_gpu(args, rank, world):
 
     barrier(world)
     l0 = ng.kernel_launches()
-    # engine launches before the timed region: the -s value of a launch-list capture
     print(f"engine_launches_before_timed={l0}", file=sys.stderr, flush=True)
+    # the counter also counted the launches recorded by the capture, which
+    # never ran: kernels actually run before the timed region (an ncu -s value)
+    print(f"engine_kernels_run_before_timed={l0 - graph.info()['kernel_nodes']}", file=sys.stderr, flush=True)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clk:
@@ -988,6 +990,9 @@ def run_bert_gpu(args, rank, world):
     barrier(world)
     l0 = ng.kernel_launches()
     print(f"engine_launches_before_timed={l0}", file=sys.stderr, flush=True)
+    # the counter also counted the launches recorded by the capture, which
+    # never ran: kernels actually run before the timed region (an ncu -s value)
+    print(f"engine_kernels_run_before_timed={l0 - graph.info()['kernel_nodes']}", file=sys.stderr, flush=True)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clk:
@@ -1302,6 +1307,10 @@ def run_gelu_gpu(args, rank, world):
     barrier(world)
     l0 = ng.kernel_launches()
     print(f"engine_launches_before_timed={l0}", file=sys.stderr, flush=True)
+    # the counter also counted the launches recorded by the capture, which
+    # never ran: kernels actually run before the timed region (an ncu -s value)
+    captured = g_lock.info()['kernel_nodes'] + g_single.info()['kernel_nodes']
+    print(f"engine_kernels_run_before_timed={l0 - captured}", file=sys.stderr, flush=True)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clk:
