@@ -76,3 +76,32 @@ def test_keyswitch_workload_rejects_a_level_outside_the_chain_without_gpu():
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--workload", "keyswitch", "--ks-limbs", "40"],
                        capture_output=True, text=True, timeout=120)
     assert r.returncode != 0 and "--ks-limbs" in r.stderr
+
+
+def test_graph_and_tensor_rate_entry_points_reject_bad_arguments_without_gpu():
+    # every check below runs before any CUDA call
+    from nexus_gb300 import _lib
+    lib = _lib.lib()
+    out = ctypes.c_void_p()
+    d = ctypes.c_double()
+    cases = [
+        ("nexus_graph_capture_begin", lambda: lib.nexus_graph_capture_begin(None), b"legacy default stream"),
+        ("nexus_graph_capture_end", lambda: lib.nexus_graph_capture_end(None, ctypes.byref(out)), b"null"),
+        ("nexus_graph_launch", lambda: lib.nexus_graph_launch(None, None), b"null graph"),
+        ("nexus_graph_info", lambda: lib.nexus_graph_info(None, None, None, None), b"null graph"),
+        ("nexus_tensor_rate", lambda: lib.nexus_tensor_rate(2, 10, ctypes.byref(d), None), b"kind"),
+        ("nexus_tensor_rate", lambda: lib.nexus_tensor_rate(0, 0, ctypes.byref(d), None), b"rounds"),
+        ("nexus_tensor_rate", lambda: lib.nexus_tensor_rate(0, 10, None, None), b"null"),
+        ("nexus_tensor_tile", lambda: lib.nexus_tensor_tile(0, 1, None, None, None), b"null"),
+    ]
+    for name, call, word in cases:
+        assert call() != 0, name
+        msg = lib.nexus_last_error()
+        assert msg.startswith(name.encode()) and word in msg, (name, msg)
+    assert lib.nexus_graph_destroy(None) == 0
+
+
+def test_graph_wrapper_needs_a_stream_without_gpu():
+    from nexus_gb300.operators import Graph
+    with pytest.raises(ValueError):
+        Graph(None)

@@ -5,8 +5,9 @@ the bootstrap test chain is run once, captured into a graph on the
 evaluator's stream, and replayed on new inputs loaded into the captured
 input handles: every replay must give exactly the words of a direct call on
 the same inputs.  Output handles first sized inside the capture keep a
-valid buffer across launches and after the graph is gone, and capture needs
-a created stream.
+valid buffer across launches and after the graph is gone, and a failing call
+inside a capture ends it cleanly.  GELU (single and lockstep) and the
+reduced-size BERT layer are replayed the same way.
 """
 import numpy as np
 import pytest
@@ -125,10 +126,21 @@ def test_outputs_first_sized_inside_the_capture(env):
     assert np.array_equal(_words(fresh, stream)[0], direct[0])   # the handle outlives the graph
 
 
-def test_capture_needs_a_stream(cuda):
-    from nexus_gb300.operators import Graph
-    with pytest.raises(ValueError):
-        Graph(None)
+def test_an_error_inside_the_capture_ends_it(env):
+    """A call that fails inside the block (here on its arguments, before any
+    device work) ends the capture and keeps no graph; the stream then runs
+    direct calls as before."""
+    from nexus_gb300 import NexusError
+    from nexus_gb300.operators import Ciphertext, Graph
+    ctx, sk, ev, bs, stream = env
+    t = _lowest_limb_ct(ctx, sk, 9)
+    ins = [Ciphertext(ctx)]
+    ins[0].load(t, SCALE, stream)
+    want = _words(bs.bootstrap_batch(ins), stream)[0]
+    with pytest.raises(NexusError, match="empty"):
+        with Graph(stream):
+            bs.bootstrap_batch([Ciphertext(ctx)])
+    assert np.array_equal(_words(bs.bootstrap_batch(ins), stream)[0], want)
 
 
 @pytest.fixture(scope="module")
