@@ -889,11 +889,17 @@ BERT_SCALE = 2.0 ** 46
 BERT_SEED = 600
 
 
-def bert_config():
+# bootstraps per layer: Q/K/V 48, softmax sums 2, residuals 12 + 12, FFN hidden
+# 48; with two ciphertexts per bootstrap 24 + 2 + 6 + 6 + 24
+BERT_BOOTSTRAPS = {False: 122, True: 62}
+
+
+def bert_config(pack: bool = True):
     return {"workload": "bert_base_layer_n65536", "N": 1 << BERT_LOGN, "hidden": 768, "heads": 12, "ffn": 3072,
             "requests": [128, 32, 64], "lanes": "[128] | [32 + 64]", "token_slots_per_block": 256,
             "moduli_bits": "51 + 19x46 + 14x51 + special 51", "hamming_weight": 192, "scale": "2^46",
-            "boot_shrink": 2, "weights": "N(0, 0.02)", "tokens": "N(0, 1)", "parallelism": "replicas",
+            "boot_shrink": 2, "boot_pack": bool(pack), "bootstraps_per_layer": BERT_BOOTSTRAPS[bool(pack)],
+            "weights": "N(0, 0.02)", "tokens": "N(0, 1)", "parallelism": "replicas",
             "l2": "keys (~110 GB), encoded weights (~60 GB) and activations far above L2, no flush"}
 
 
@@ -931,6 +937,7 @@ def run_bert_gpu(args, rank, world):
     bs.prepare_mod_polynomial()
     bs.generate_LT_coefficient_3()
     layer = NB.BertLayer(bs, shape, w)
+    layer.set_boot_pack(bool(args.bert_pack))
     tuning = ctx.autotune(20, 16)
     tuning["ntt_form"] = _apply_ntt_form(ctx, args)
     all_steps = steps + [s for s in layer.rotation_steps() if s not in steps]
@@ -1112,7 +1119,7 @@ def run_bert_gpu(args, rank, world):
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic: weights ~ N(0,0.02), tokens ~ N(0,1), seeded; keys and encryptions from a SEAL seed",
-        "config": dict(bert_config(), tuning=tuning,
+        "config": dict(bert_config(bool(args.bert_pack)), tuning=tuning,
                        form="lockstep nexus_bert_layer_forward captured once as a CUDA graph, one "
                             "nexus_graph_launch per step"),
         "parity": parity,
@@ -1139,23 +1146,25 @@ def run_bert_gpu(args, rank, world):
                   "cached_plaintexts": layer.cached_plaintexts()},
         "clocks": clk.summary(),
         "gpu_launches": launches,
-        "cpu_baseline": cpu_bert_sample(os.cpu_count() or 1) if rank == 0 and world == 1 else None,
+        "cpu_baseline": cpu_bert_sample(os.cpu_count() or 1, bool(args.bert_pack)) if rank == 0 and world == 1
+        else None,
     }
 
 
-BERT_BOOTSTRAPS = 122   # per layer: Q/K/V 48, softmax sums 2, residuals 12 + 12, FFN hidden 48
 
 
-def cpu_bert_sample(threads: int):
+def cpu_bert_sample(threads: int, pack: bool = True):
     """A lower bound of the layer on the oracle port: one full bootstrap on the
-    layer's chain, timed, times the layer's 122 bootstraps (projections,
-    attention, GELU and LayerNorm left out)."""
+    layer's chain, timed, times the layer's bootstraps (122, or 62 with two
+    ciphertexts per bootstrap; projections, attention, GELU, LayerNorm and the
+    packing's conjugations left out)."""
     cb = CpuBootstrap(threads, BERT_BITS)
     t = cb.bootstrap()
-    total = BERT_BOOTSTRAPS * t
+    n_boot = BERT_BOOTSTRAPS[bool(pack)]
+    total = n_boot * t
     return {"value": total, "unit": "s per layer", "cores": threads, "kind": "port",
             "sample": f"one full-slot bootstrap_3 on the layer chain (51 + 19x46 + 14x51 + 51) with the oracle port "
-                      f"timed at {t:.1f} s on {threads} threads, times the layer's {BERT_BOOTSTRAPS} bootstraps: a "
+                      f"timed at {t:.1f} s on {threads} threads, times the layer's {n_boot} bootstraps: a "
                       f"lower bound (the linear maps, attention, GELU and LayerNorm are not counted)"
                       + _calibration_note()}
 
@@ -1691,6 +1700,8 @@ def main():
                     help="prime size of the NTT workload (other values are for profiling captures only)")
     ap.add_argument("--boot-cts", type=int, default=16,
                     help="ciphertexts per bootstrap step (smaller values are for profiling captures only)")
+    ap.add_argument("--bert-pack", type=int, choices=[0, 1], default=1,
+                    help="BERT layer: refresh two ciphertexts per bootstrap (c0 + i c1; 0: one each)")
     ap.add_argument("--ntt-cts", type=int, default=64,
                     help="ciphertexts per step (smaller values are for profiling captures only)")
     args = ap.parse_args()
@@ -1789,12 +1800,12 @@ def main():
         if rank != 0:
             return
         threads = max(1, os.cpu_count() or 1)
-        r = cpu_bert_sample(threads)
+        r = cpu_bert_sample(threads, bool(args.bert_pack))
         res = {"impl": "reference", "metric": "bert_base_layer_latency_n65536", "value": r["value"],
                "unit": r["unit"], "n_gpus": world, "steps": 1, "steps_requested": args.steps, "warmup": 0,
                "ms_per_step": r["value"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
                "dtype": "u64", "data": "synthetic (uniform random residues; the cost does not depend on them)",
-               "config": bert_config(), "cpu_baseline": r,
+               "config": bert_config(bool(args.bert_pack)), "cpu_baseline": r,
                "e2e": {"value": r["value"], "unit": r["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(res), flush=True)
         return

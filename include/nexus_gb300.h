@@ -695,6 +695,13 @@ int nexus_bert_layer_stage(nexus_bert_layer *layer, int lockstep, int stage, int
  * (lockstep form, or lane `lane` of the single form) in ms[], their names in
  * `names` separated by newlines; ms = NULL only counts them. */
 int nexus_bert_layer_set_timing(nexus_bert_layer *layer, int enable);
+/* With boot_pack on, each bootstrap of the layer refreshes two ciphertexts:
+ * z = c0 + X^(N/2) c1 holds c0 + i c1, its scale doubled, and after
+ * bootstrap_3 c0 = z + conj(z), c1 = (conj(z) - z) X^(N/2) (a trailing odd
+ * ciphertext is refreshed alone).  Half the bootstraps, one conjugation per
+ * pair, the same error per output.  On by default; no counterpart in the
+ * reference (NEXUS has no layer). */
+int nexus_bert_layer_set_boot_pack(nexus_bert_layer *layer, int enable);
 int nexus_bert_layer_stage_times(nexus_bert_layer *layer, int lockstep, int lane, double *ms, char *names,
                                  size_t names_capacity, int *count, int capacity);
 

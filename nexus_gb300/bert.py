@@ -34,6 +34,8 @@ class BertShape:
     # per lane, requests as (first token slot, tokens)
     lanes: list = field(default_factory=lambda: [[(0, 128)], [(0, 32), (64, 64)]])
     boot_shrink: float = 2.0
+    # two ciphertexts per bootstrap (c0 + i c1, separated by a conjugation)
+    boot_pack: bool = True
 
     def blocks(self, slots: int) -> int:
         return slots // self.T
@@ -220,6 +222,7 @@ class BertLayer:
         check(lib().nexus_bert_layer_info(self._h, *[C.byref(i) for i in info], C.byref(cached)),
               "nexus_bert_layer_info")
         self.n_lanes, self.n_hid, self.n_head, self.n_ffn = [i.value for i in info]
+        self.set_boot_pack(shape.boot_pack)
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -241,6 +244,10 @@ class BertLayer:
 
     def set_timing(self, enable: bool) -> None:
         check(lib().nexus_bert_layer_set_timing(self._h, 1 if enable else 0), "nexus_bert_layer_set_timing")
+
+    def set_boot_pack(self, enable: bool) -> None:
+        """Two ciphertexts per bootstrap (nexus_bert_layer_set_boot_pack)."""
+        check(lib().nexus_bert_layer_set_boot_pack(self._h, 1 if enable else 0), "nexus_bert_layer_set_boot_pack")
 
     def stage_times(self, lockstep: bool = True, lane: int = 0) -> dict:
         """Device ms of each block of the last forward with timing on."""

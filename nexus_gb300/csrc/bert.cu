@@ -315,10 +315,7 @@ void BertLayerT<EV, CT>::encode_diagonals(int which, int limbs, double scale)
                 const BertPlaintexts::DKey key{which, a, b, d, limbs, sb};
                 if (!pt_->diag.count(key) && diag_nonzero(which, a, b, d)) keys.push_back(key);
             }
-    Evaluator &base = [&]() -> Evaluator & {
-        if constexpr (std::is_same<EV, Evaluator>::value) return *ev_;
-        else return ev_->base();
-    }();
+    Evaluator &base = base_evaluator();
     // host FFTs on every core, in chunks that bound the host staging memory;
     // a chunk enters the cache only once all of it is encoded
     const size_t chunk = 256;
@@ -490,18 +487,53 @@ void BertLayerT<EV, CT>::project(const std::vector<CT> &x, int which, std::vecto
 }
 
 template <class EV, class CT>
+Evaluator &BertLayerT<EV, CT>::base_evaluator()
+{
+    if constexpr (std::is_same<EV, Evaluator>::value) return *ev_;
+    else return ev_->base();
+}
+
+template <class EV, class CT>
 void BertLayerT<EV, CT>::bootstrap_all(std::vector<CT> &cts)
 {
-    std::vector<CT *> p;
-    for (auto &c : cts) {
-        ev_->mod_switch_to_inplace(c, 1);
-        p.push_back(&c);
+    EV &ev = *ev_;
+    for (auto &c : cts) ev.mod_switch_to_inplace(c, 1);
+    auto refresh = [&](std::vector<CT> &v) {
+        std::vector<CT *> p;
+        for (auto &c : v) p.push_back(&c);
+        each(ev, p, 16, [&](CT &c) {
+            CT r;
+            bs_->bootstrap_3(r, c);
+            c = std::move(r);
+        });
+    };
+    if (!sh_.boot_pack) {
+        refresh(cts);
+        return;
     }
-    each(*ev_, p, 16, [&](CT &c) {
-        CT r;
-        bs_->bootstrap_3(r, c);
-        c = std::move(r);
-    });
+    // pairs (2i, 2i + 1) share a bootstrap (see bert.h); a trailing odd one
+    // is refreshed alone
+    Evaluator &base = base_evaluator();
+    const int half = (int)(base.context().n / 2);
+    const size_t pairs = cts.size() / 2;
+    std::vector<CT> z(pairs), rest;
+    for (size_t i = 0; i < pairs; ++i) {
+        CT t;
+        ev.multiply_plain(cts[2 * i + 1], base.monomial(half, 1), t);
+        ev.add(cts[2 * i], t, z[i]);
+        z[i].scale() *= 2.0;
+    }
+    for (size_t i = 2 * pairs; i < cts.size(); ++i) rest.push_back(std::move(cts[i]));
+    refresh(z);
+    refresh(rest);
+    for (size_t i = 0; i < pairs; ++i) {
+        CT conj = z[i];
+        ev.complex_conjugate_inplace(conj);
+        ev.add(z[i], conj, cts[2 * i]);
+        ev.sub(conj, z[i], cts[2 * i + 1]);
+        ev.multiply_plain_inplace(cts[2 * i + 1], base.monomial(half, cts[2 * i + 1].limbs()));
+    }
+    for (size_t i = 0; i < rest.size(); ++i) cts[2 * pairs + i] = std::move(rest[i]);
 }
 
 template <class EV, class CT>

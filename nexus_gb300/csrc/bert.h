@@ -45,6 +45,14 @@
 // are constant over many slots (the softmax row sums, for one) concentrate in
 // few coefficients and leave EvalMod's intervals otherwise.  The bootstrap's
 // own error grows with the factor (about 2e-4 times it at N = 2^16), hence 2.
+//
+// With boot_pack, two ciphertexts share one bootstrap.  The values are real,
+// and the full-slot bootstrap refreshes complex slots: z = c0 + X^(N/2) c1
+// holds c0 + i c1 (X^(N/2) multiplies every slot by i, exactly, at no
+// level), its scale is doubled so that the refreshed z holds (c0 + i c1) / 2,
+// and c0 = z + conj(z), c1 = (conj(z) - z) X^(N/2) afterwards (one
+// conjugation).  The words EvalMod sees are the two messages' sum, and the
+// error of each output is that of an unpacked bootstrap.
 #pragma once
 #include <cstdint>
 #include <map>
@@ -67,6 +75,9 @@ struct BertShape {
     // per lane, each request as (first token slot, tokens)
     std::vector<std::vector<std::pair<int, int>>> lanes;
     double boot_shrink = 2.0;
+    // refresh two ciphertexts with one bootstrap (c0 + i c1, separated by a
+    // conjugation afterwards)
+    bool boot_pack = true;
 
     // derived by derive()
     int S = 0, NB = 0, H2 = 0, KB = 0, n_head = 0, n_hid = 0, n_ffn = 0, Lmax = 0, G = 0, Glt = 0;
@@ -123,6 +134,7 @@ public:
     double delta() const { return delta_; }
     size_t cached_plaintexts() const { return pt_->count(); }
     const BertShape &shape() const { return sh_; }
+    void set_boot_pack(bool on) { sh_.boot_pack = on; }
 
 private:
     int in_count(int which) const;
@@ -144,6 +156,7 @@ private:
     void begin_marks();
     void mark(const char *name);
     void exact_scale_const(CT &ct, double value, double target_scale);
+    Evaluator &base_evaluator();
 
     EV *ev_;
     BootstrapperT<EV, CT> *bs_;

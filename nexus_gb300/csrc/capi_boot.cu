@@ -619,6 +619,15 @@ extern "C" int nexus_bert_layer_set_timing(nexus_bert_layer *layer, int enable)
     return 0;
 }
 
+extern "C" int nexus_bert_layer_set_boot_pack(nexus_bert_layer *layer, int enable)
+{
+    if (!layer) return fail("nexus_bert_layer_set_boot_pack", "null argument");
+    layer->shape.boot_pack = enable != 0;
+    for (auto &l : layer->single) l->set_boot_pack(enable != 0);
+    if (layer->lockstep) layer->lockstep->set_boot_pack(enable != 0);
+    return 0;
+}
+
 extern "C" int nexus_bert_layer_stage_times(nexus_bert_layer *layer, int lockstep, int lane, double *ms, char *names,
                                             size_t names_capacity, int *count, int capacity)
 {

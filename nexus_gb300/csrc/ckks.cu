@@ -834,6 +834,23 @@ void Evaluator::rotate_vector(const Ciphertext &ct, int steps, Ciphertext &dest)
 
 void Evaluator::complex_conjugate_inplace(Ciphertext &ct) { apply_galois_inplace(ct, galois_elt(0)); }
 
+const Plaintext &Evaluator::monomial(int power, int limbs)
+{
+    if (power < 0 || power >= (int)c_.n) throw std::invalid_argument("monomial: power out of range");
+    if (limbs < 1 || limbs > top_limbs()) throw std::invalid_argument("monomial: limbs out of range");
+    const auto key = std::make_pair(power, limbs);
+    auto it = monomials_.find(key);
+    if (it != monomials_.end()) return it->second;
+    std::vector<uint64_t> host((size_t)limbs * c_.n, 0);
+    for (int l = 0; l < limbs; ++l) host[(size_t)l * c_.n + (size_t)power] = 1;
+    Plaintext p;
+    p.set_vector(c_, limbs, 1.0, s_);
+    ck(cudaMemcpyAsync(p.mutable_data(), host.data(), host.size() * 8, cudaMemcpyHostToDevice, s_), "upload");
+    ck(cudaStreamSynchronize(s_), "monomial");  // host buffer lifetime
+    ntt_forward(c_, p.mutable_data(), 1, 0, limbs, s_);
+    return monomials_.emplace(key, std::move(p)).first->second;
+}
+
 // ------------------------------------------------------- hoisted rotations
 
 void Evaluator::set_galois_key(uint32_t elt, const uint64_t *key)

@@ -142,6 +142,7 @@ public:
         s_ = s;
         const_cache_.clear();   // cached encodings are copied on the stream they were made on
         const_cache_words_ = 0;
+        monomials_.clear();
     }
     size_t slot_count() const { return c_.n / 2; }
     int top_limbs() const { return c_.k - 1; }
@@ -225,6 +226,10 @@ public:
     void rotate_vector_inplace(Ciphertext &ct, int steps);
     void rotate_vector(const Ciphertext &ct, int steps, Ciphertext &dest);
     void complex_conjugate_inplace(Ciphertext &ct);
+    // the NTT form of the monomial X^power at `limbs` limbs, scale 1 (made
+    // once per evaluator, then cached): multiply_plain by it multiplies the
+    // message by X^power exactly and leaves the scale and level as they are
+    const Plaintext &monomial(int power, int limbs);
     uint32_t galois_elt(int step) const;
     // outs[i] = rotate_vector(ct, steps[i]) for every i, word for word; the
     // steps that have their own Galois key share one ModUp of c1 (hoisted
@@ -283,6 +288,7 @@ private:
     void const_store(const ConstKey &k, const Plaintext &pt);
     std::map<ConstKey, Plaintext> const_cache_;
     size_t const_cache_words_ = 0;
+    std::map<std::pair<int, int>, Plaintext> monomials_;
 };
 
 bool are_close(double a, double b);

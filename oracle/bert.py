@@ -35,10 +35,11 @@ def _pow2_ceil(v):
 
 
 class Shape:
-    def __init__(self, slots, hidden, heads, head_dim, ffn, T, lanes, boot_shrink):
+    def __init__(self, slots, hidden, heads, head_dim, ffn, T, lanes, boot_shrink, boot_pack=True):
         self.S, self.hidden, self.heads, self.head_dim, self.ffn, self.T = slots, hidden, heads, head_dim, ffn, T
         self.lanes = [list(l) for l in lanes]
         self.boot_shrink = float(boot_shrink)
+        self.boot_pack = bool(boot_pack)
         self.NB = slots // T
         self.H2 = _pow2_ceil(heads)
         self.KB = self.NB // self.H2
@@ -87,6 +88,7 @@ class BertLayer:
         self.ev, self.bs, self.sh, self.w, self.lane = ev, bs, shape, w, lane
         self.delta = float(bs.final_scale)
         self.ck = L.CKKSEvaluator(ev, self.delta)
+        self._mono = {}
 
     # -- linear maps -----------------------------------------------------------
     def _in_count(self, which):
@@ -192,8 +194,39 @@ class BertLayer:
             out.append(c)
         return out
 
+    def _monomial(self, power, limbs):
+        """The NTT form of X^power at `limbs` limbs, scale 1 (Evaluator::monomial)."""
+        key = (power, limbs)
+        if key not in self._mono:
+            oc = self.ev.oc
+            x = np.zeros((limbs, oc.n), dtype=np.uint64)
+            x[:, power] = 1
+            self._mono[key] = L.Pt(1.0, data=oc.ntt(x, 0, limbs))
+        return self._mono[key]
+
     def bootstrap_all(self, cts):
-        return [self.bs.bootstrap_3(self.ev.mod_switch_to(c, 1)) for c in cts]
+        """BertLayerT::bootstrap_all: every ciphertext refreshed at one limb;
+        with boot_pack, ciphertexts 2i and 2i + 1 share one bootstrap of
+        z = c0 + X^(N/2) c1 (scale doubled), then c0 = z + conj(z) and
+        c1 = (conj(z) - z) X^(N/2); a trailing odd one is refreshed alone."""
+        ev = self.ev
+        cts = [ev.mod_switch_to(c, 1) for c in cts]
+        if not self.sh.boot_pack:
+            return [self.bs.bootstrap_3(c) for c in cts]
+        half = ev.oc.n // 2
+        pairs = len(cts) // 2
+        z = []
+        for i in range(pairs):
+            s = ev.add(cts[2 * i], ev.multiply_plain(cts[2 * i + 1], self._monomial(half, 1)))
+            s.scale *= 2.0
+            z.append(self.bs.bootstrap_3(s))
+        rest = [self.bs.bootstrap_3(c) for c in cts[2 * pairs:]]
+        out = []
+        for zi in z:
+            conj = ev.conjugate(zi)
+            out.append(ev.add(zi, conj))
+            out.append(ev.multiply_plain(ev.sub(conj, zi), self._monomial(half, zi.limbs)))
+        return out + rest
 
     def _mask(self, delta, kind, limbs, scale):
         sh = self.sh

@@ -3,7 +3,7 @@ words at every stage of the encrypted BERT encoder layer (oracle/bert.py) at
 a reduced size: N = 2^13, 32 token slots per feature block, hidden 64 =
 2 heads x 32, FFN 128, two lanes with requests of 16 | 4 + 8 tokens, on
 the chain 51 + 19x46 + 14x51 + special 51 with the sparse secret
-(h = 192).  Keys and encryptions come from the real SEAL-4.1-bs with one
+(h = 192), two ciphertexts per bootstrap (boot_pack).  Keys and encryptions come from the real SEAL-4.1-bs with one
 seeded Blake2xbPRNG factory, so the engine can make them again on the GPU
 from the seed (tests/test_bert_gpu.py).
 
@@ -38,7 +38,7 @@ OUT = Path(__file__).parent / "bert_digests.json"
 CASE = dict(log_n=13, bits=[51] + [46] * 19 + [51] * 14 + [51], seed=seed8(500), hamming_weight=192,
             scale_log2=46, loge=10, boundary_K=25, sin_cos_deg=59, scale_factor=2, inverse_deg=1,
             hidden=64, heads=2, head_dim=32, ffn=128, T=32, lanes=[[[0, 16]], [[0, 4], [8, 8]]],
-            boot_shrink=2.0, weight_seed=7, token_seed=8)
+            boot_shrink=2.0, boot_pack=True, weight_seed=7, token_seed=8)
 
 
 def digest(a) -> str:
@@ -47,7 +47,8 @@ def digest(a) -> str:
 
 def shape_of(c):
     return NB.BertShape(hidden=c["hidden"], heads=c["heads"], head_dim=c["head_dim"], ffn=c["ffn"], T=c["T"],
-                        lanes=[[tuple(r) for r in lane] for lane in c["lanes"]], boot_shrink=c["boot_shrink"])
+                        lanes=[[tuple(r) for r in lane] for lane in c["lanes"]], boot_shrink=c["boot_shrink"],
+                        boot_pack=c["boot_pack"])
 
 
 def inputs(c):
@@ -68,7 +69,7 @@ def main():
     qs = po.create_coeff_modulus(n, c["bits"])
     log_nh = c["log_n"] - 1
     sh, w, tokens = inputs(c)
-    osh = OB.Shape(n // 2, sh.hidden, sh.heads, sh.head_dim, sh.ffn, sh.T, sh.lanes, sh.boot_shrink)
+    osh = OB.Shape(n // 2, sh.hidden, sh.heads, sh.head_dim, sh.ffn, sh.T, sh.lanes, sh.boot_shrink, sh.boot_pack)
     keys = SealKeys(c["log_n"], qs, c["seed"], c["hamming_weight"], keep=1000)
     steps = B.rot_key_steps_3(log_nh, log_nh)
     for s in osh.rotation_steps():

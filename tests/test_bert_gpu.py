@@ -2,9 +2,10 @@
 word for word, at the reduced size of tests/golden/bert_digests.json (N = 2^13,
 hidden 64, 2 heads, FFN 128, requests of 16 | 4 + 8 tokens in two lanes):
 the Q/K/V projections, their bootstrap, the attention block and the whole
-layer in its single-lane and lockstep forms, with keys and encryptions made
-from the same SEAL seed; plus the decrypted output against the FP64 layer
-with NEXUS's approximations."""
+layer in its single-lane and lockstep forms (two ciphertexts per bootstrap,
+the default), with keys and encryptions made from the same SEAL seed; plus
+the decrypted output against the FP64 layer with NEXUS's approximations, in
+both bootstrap forms."""
 import hashlib
 import json
 from pathlib import Path
@@ -27,7 +28,8 @@ def _shape():
     from nexus_gb300 import bert as NB
     c = DOC
     return NB.BertShape(hidden=c["hidden"], heads=c["heads"], head_dim=c["head_dim"], ffn=c["ffn"], T=c["T"],
-                        lanes=[[tuple(r) for r in lane] for lane in c["lanes"]], boot_shrink=c["boot_shrink"])
+                        lanes=[[tuple(r) for r in lane] for lane in c["lanes"]], boot_shrink=c["boot_shrink"],
+                        boot_pack=c["boot_pack"])
 
 
 @pytest.fixture(scope="module")
@@ -111,6 +113,29 @@ def test_layer_matches_oracle(env, lockstep):
     for lane in range(layer.n_lanes):
         cts = out[lane * layer.n_hid:(lane + 1) * layer.n_hid]
         assert cts[0].scale == DOC["lanes_out"][lane]["output_scale"]
+        dec = np.stack([ctx.decode(ctx.decrypt(env["sk"], c.to_device()), c.scale).real for c in cts])
+        ys = NB.unpack_lane(sh, n // 2, lane, dec)
+        ref = NB.layer_reference(sh, env["w"], env["tokens"][lane])
+        err = max(float(np.max(np.abs(y - r))) for y, r in zip(ys, ref))
+        assert err < 2.0 ** -7, err
+
+
+def test_unpacked_bootstraps_keep_the_layer_within_its_error(env):
+    """With one ciphertext per bootstrap (boot_pack off) the layer's lockstep
+    and single-lane forms agree word for word, and the decrypted output stays
+    within the packed layer's error bound against the FP64 layer."""
+    from nexus_gb300 import bert as NB
+    layer, ctx, sh, n = env["layer"], env["ctx"], env["sh"], env["n"]
+    layer.set_boot_pack(False)
+    try:
+        lock = layer.forward(env["x"], True)
+        single = layer.forward(env["x"], False)
+    finally:
+        layer.set_boot_pack(True)
+    for a, b in zip(lock, single):
+        assert np.array_equal(a.to_numpy(), b.to_numpy())
+    for lane in range(layer.n_lanes):
+        cts = lock[lane * layer.n_hid:(lane + 1) * layer.n_hid]
         dec = np.stack([ctx.decode(ctx.decrypt(env["sk"], c.to_device()), c.scale).real for c in cts])
         ys = NB.unpack_lane(sh, n // 2, lane, dec)
         ref = NB.layer_reference(sh, env["w"], env["tokens"][lane])
