@@ -593,6 +593,17 @@ int nexus_bootstrap(nexus_bootstrapper *bs, nexus_ciphertext *ct, nexus_cipherte
  * (it bootstraps one ciphertext per call). */
 int nexus_bootstrap_batch(nexus_bootstrapper *bs, nexus_ciphertext *const *cts, int count,
                           nexus_ciphertext *const *rtn);
+/* The ciphertexts of a batch refreshed two per bootstrap, for real slot
+ * values: cts[2i] and cts[2i+1] share one lockstep bootstrap_3 of
+ * z = cts[2i] + X^(N/2) cts[2i+1] (X^(N/2) multiplies every slot by i) with
+ * z's scale doubled, and come back as z + conj(z) and (conj(z) - z) X^(N/2)
+ * (one conjugation per pair); an odd last one is refreshed alone.  Each
+ * output decrypts to its input's values within an unpacked bootstrap's
+ * error, at half the bootstraps; the words are those of that sequence, not
+ * of bootstrap_3 on each ciphertext.  Same input rules as
+ * nexus_bootstrap_batch.  No counterpart in the reference. */
+int nexus_bootstrap_real_batch(nexus_bootstrapper *bs, nexus_ciphertext *const *cts, int count,
+                               nexus_ciphertext *const *rtn);
 
 /* The stages of bootstrap_full_3 (Bootstrapper.cpp:3224-3244), for
  * stage-wise checking: MODRAISE a in place (modraise_inplace :2937-2991);

@@ -99,6 +99,7 @@ SIGNATURES = [
     ("nexus_bootstrap", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nexus_argmax", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("nexus_bootstrap_batch", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("nexus_bootstrap_real_batch", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("nexus_bootstrapper_stage", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nexus_rotate_vector_many", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("nexus_rotate_vector_many_batch", C.c_int,

@@ -271,6 +271,77 @@ extern "C" int nexus_argmax_batch(nexus_bootstrapper *bs, nexus_ciphertext *cons
     });
 }
 
+extern "C" int nexus_bootstrap_real_batch(nexus_bootstrapper *bs, nexus_ciphertext *const *cts, int count,
+                                          nexus_ciphertext *const *rtn)
+{
+    static const char *fn = "nexus_bootstrap_real_batch";
+    if (!bs || !cts || !rtn || count < 1) return fail(fn, "null argument");
+    for (int b = 0; b < count; ++b) {
+        if (!cts[b] || !rtn[b]) return fail(fn, "null ciphertext");
+        if (const char *e = input_problem(bs->ev->ctx, cts[b])) return fail(fn, e);
+        for (int j = 0; j < count; ++j)
+            if (rtn[b] == cts[j]) return fail(fn, "rtn must not alias an input");
+    }
+    return guarded(fn, [&] {
+        BatchBootstrapper &BB = lockstep_form(bs);
+        BatchEvaluator &ev = *bs->bev;
+        const Ciphertext &first = cts[0]->ct;
+        for (int b = 0; b < count; ++b) {
+            const Ciphertext &c = cts[b]->ct;
+            if (c.size() != 2) throw std::invalid_argument("Ciphertexts of size 2 are supported only!");
+            if (c.limbs() != 1) throw std::invalid_argument("Ciphertexts in the lowest level are supported only!");
+            if (c.scale() != first.scale()) throw std::invalid_argument("the ciphertexts of a batch must share one scale");
+        }
+        Context &ctx = bs->ev->ctx->c;
+        cudaStream_t s = bs->ev->ev.stream();
+        const int pairs = count / 2, odd = count % 2;
+        auto gather = [&](CtBatch &dst, int first_index, int step, int n) {
+            dst.resize(ctx, n, 2, 1, s);
+            dst.scale() = first.scale();
+            for (int b = 0; b < n; ++b)
+                if (cudaMemcpyAsync(dst.ct(b), cts[first_index + step * b]->ct.data(), dst.words_per_ct() * 8,
+                                    cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+                    throw std::runtime_error("copy failed");
+        };
+        auto scatter = [&](const CtBatch &src, int first_index, int step) {
+            for (int b = 0; b < src.batch(); ++b) {
+                Ciphertext &r = rtn[first_index + step * b]->ct;
+                r.resize(ctx, src.size(), src.limbs(), s);
+                r.scale() = src.scale();
+                if (cudaMemcpyAsync(r.data(), src.ct(b), src.words_per_ct() * 8, cudaMemcpyDeviceToDevice, s) !=
+                    cudaSuccess)
+                    throw std::runtime_error("copy failed");
+            }
+        };
+        Evaluator &base = bs->ev->ev;
+        const int half = (int)(ctx.n / 2);
+        if (pairs) {
+            // z = c0 + X^(N/2) c1 holds c0 + i c1; its scale doubled, the
+            // refreshed z holds (c0 + i c1) / 2
+            CtBatch c0, c1, t, z, out;
+            gather(c0, 0, 2, pairs);
+            gather(c1, 1, 2, pairs);
+            ev.multiply_plain(c1, base.monomial(half, 1), t);
+            ev.add(c0, t, z);
+            z.scale() *= 2.0;
+            BB.bootstrap_3(out, z);
+            CtBatch conj = out, re, im;
+            ev.complex_conjugate_inplace(conj);
+            ev.add(out, conj, re);
+            ev.sub(conj, out, im);
+            ev.multiply_plain_inplace(im, base.monomial(half, im.limbs()));
+            scatter(re, 0, 2);
+            scatter(im, 1, 2);
+        }
+        if (odd) {
+            CtBatch one, out;
+            gather(one, count - 1, 1, 1);
+            BB.bootstrap_3(out, one);
+            scatter(out, count - 1, 1);
+        }
+    });
+}
+
 extern "C" int nexus_bootstrapper_stage(nexus_bootstrapper *bs, int stage, nexus_ciphertext *a,
                                         const nexus_ciphertext *b, nexus_ciphertext *r1, nexus_ciphertext *r2)
 {

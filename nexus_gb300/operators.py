@@ -347,6 +347,18 @@ class Bootstrapper:
         check(lib().nexus_bootstrap_batch(self._h, a, len(cts), r), "nexus_bootstrap_batch")
         return res
 
+    def bootstrap_real_batch(self, cts: list, out: list | None = None) -> list:
+        """Refresh ciphertexts of real slot values two per bootstrap
+        (nexus_bootstrap_real_batch): pairs share one bootstrap_3 of
+        c0 + X^(N/2) c1 and are split by a conjugation."""
+        res = out if out is not None else [Ciphertext(self.ctx) for _ in cts]
+        if len(res) != len(cts):
+            raise ValueError("one output per input")
+        a = (C.c_void_p * len(cts))(*[c.handle.value for c in cts])
+        r = (C.c_void_p * len(res))(*[x.handle.value for x in res])
+        check(lib().nexus_bootstrap_real_batch(self._h, a, len(cts), r), "nexus_bootstrap_real_batch")
+        return res
+
     def argmax(self, x: Ciphertext, length: int) -> Ciphertext:
         """ArgmaxEvaluator::argmax (src/argmax.cpp) over slots 0..length-1 of x
         (x is updated in place as in the reference)."""

@@ -22,6 +22,7 @@ import math
 
 import numpy as np
 
+from . import bootstrap as B
 from . import nexus_l3 as L
 
 LT_Q, LT_K, LT_V, LT_O, LT_1, LT_2 = range(6)
@@ -88,7 +89,6 @@ class BertLayer:
         self.ev, self.bs, self.sh, self.w, self.lane = ev, bs, shape, w, lane
         self.delta = float(bs.final_scale)
         self.ck = L.CKKSEvaluator(ev, self.delta)
-        self._mono = {}
 
     # -- linear maps -----------------------------------------------------------
     def _in_count(self, which):
@@ -194,39 +194,18 @@ class BertLayer:
             out.append(c)
         return out
 
-    def _monomial(self, power, limbs):
-        """The NTT form of X^power at `limbs` limbs, scale 1 (Evaluator::monomial)."""
-        key = (power, limbs)
-        if key not in self._mono:
-            oc = self.ev.oc
-            x = np.zeros((limbs, oc.n), dtype=np.uint64)
-            x[:, power] = 1
-            self._mono[key] = L.Pt(1.0, data=oc.ntt(x, 0, limbs))
-        return self._mono[key]
-
     def bootstrap_all(self, cts):
         """BertLayerT::bootstrap_all: every ciphertext refreshed at one limb;
-        with boot_pack, ciphertexts 2i and 2i + 1 share one bootstrap of
-        z = c0 + X^(N/2) c1 (scale doubled), then c0 = z + conj(z) and
-        c1 = (conj(z) - z) X^(N/2); a trailing odd one is refreshed alone."""
-        ev = self.ev
-        cts = [ev.mod_switch_to(c, 1) for c in cts]
+        with boot_pack, ciphertexts 2i and 2i + 1 share one bootstrap
+        (bootstrap.bootstrap_real_pair); a trailing odd one is refreshed alone."""
+        cts = [self.ev.mod_switch_to(c, 1) for c in cts]
         if not self.sh.boot_pack:
             return [self.bs.bootstrap_3(c) for c in cts]
-        half = ev.oc.n // 2
         pairs = len(cts) // 2
-        z = []
-        for i in range(pairs):
-            s = ev.add(cts[2 * i], ev.multiply_plain(cts[2 * i + 1], self._monomial(half, 1)))
-            s.scale *= 2.0
-            z.append(self.bs.bootstrap_3(s))
-        rest = [self.bs.bootstrap_3(c) for c in cts[2 * pairs:]]
         out = []
-        for zi in z:
-            conj = ev.conjugate(zi)
-            out.append(ev.add(zi, conj))
-            out.append(ev.multiply_plain(ev.sub(conj, zi), self._monomial(half, zi.limbs)))
-        return out + rest
+        for i in range(pairs):
+            out.extend(B.bootstrap_real_pair(self.bs, cts[2 * i], cts[2 * i + 1]))
+        return out + [self.bs.bootstrap_3(c) for c in cts[2 * pairs:]]
 
     def _mask(self, delta, kind, limbs, scale):
         sh = self.sh

@@ -631,3 +631,25 @@ class Bootstrapper:
         if self.logn == self.log_nh:
             return self.bootstrap_full_3(ct)
         return self.bootstrap_sparse_3(ct)
+
+
+def monomial(ev: l3.Evaluator, power: int, limbs: int) -> l3.Pt:
+    """The NTT form of X^power at `limbs` limbs, scale 1 (Evaluator::monomial
+    of the engine): multiply_plain by it multiplies the message by X^power."""
+    x = np.zeros((limbs, ev.oc.n), dtype=np.uint64)
+    x[:, power] = 1
+    return l3.Pt(1.0, data=ev.oc.ntt(x, 0, limbs))
+
+
+def bootstrap_real_pair(bs: Bootstrapper, c0, c1):
+    """Two ciphertexts of real slot values refreshed by one bootstrap_3
+    (nexus_bootstrap_real_batch and the BERT layer's boot_pack): z = c0 +
+    X^(N/2) c1 holds c0 + i c1, its scale doubled so that the refreshed z
+    holds (c0 + i c1) / 2; then c0 = z + conj(z), c1 = (conj(z) - z) X^(N/2)."""
+    ev = bs.ev
+    half = ev.oc.n // 2
+    z = ev.add(c0, ev.multiply_plain(c1, monomial(ev, half, 1)))
+    z.scale *= 2.0
+    r = bs.bootstrap_3(z)
+    conj = ev.conjugate(r)
+    return ev.add(r, conj), ev.multiply_plain(ev.sub(conj, r), monomial(ev, half, r.limbs))

@@ -171,6 +171,25 @@ def test_bootstrap_matches_oracle_and_refreshes(env):
     assert err.max() < 2.0 ** -12, err.max()
 
 
+def test_real_pairs_match_oracle_and_refresh(env):
+    """nexus_bootstrap_real_batch on three ciphertexts: the first two share
+    one bootstrap (c0 + X^(N/2) c1, split by a conjugation) and the third is
+    refreshed alone; every word equals the oracle's restatement
+    (oracle/bootstrap.py::bootstrap_real_pair) and every output decrypts to
+    its own input within a single bootstrap's error."""
+    from oracle import bootstrap as OBS
+    ctx, sk, bs, obs, _ = env
+    ins = [_input(ctx, sk, 40 + i) for i in range(3)]
+    before = [_decrypt(ctx, sk, x) for _, x, _ in ins]
+    outs = bs.bootstrap_real_batch([x for _, x, _ in ins])
+    want = list(OBS.bootstrap_real_pair(obs, ins[0][2].copy(), ins[1][2].copy())) + [obs.bootstrap_3(ins[2][2].copy())]
+    for got, o in zip(outs, want):
+        _same(got, o)
+    for b, out in zip(before, outs):
+        err = np.abs(_decrypt(ctx, sk, out) - b)
+        assert err.max() < 2.0 ** -12, err.max()
+
+
 def test_second_bootstrap_reuses_encoded_diagonals(env):
     ctx, sk, bs, obs, _ = env
     _, x1, _ = _input(ctx, sk, 9)
