@@ -1083,7 +1083,8 @@ def run_bert_gpu(args, rank, world):
     in_bytes = sum(h.nbytes for h in host_x)
     out_bytes = sum(h.nbytes for h in h_out)
 
-    # the plain form: each lane on its own, one ciphertext per operation
+    # each lane on its own, one ciphertext per operation, with the bootstraps
+    # in the lockstep form's setting (words equal to the lockstep form's)
     p0 = torch.cuda.Event(enable_timing=True)
     p1 = torch.cuda.Event(enable_timing=True)
     layer.set_timing(True)
@@ -1091,12 +1092,36 @@ def run_bert_gpu(args, rank, world):
     res = layer.forward(x, lockstep=False)
     p1.record(stream)
     torch.cuda.synchronize(dev)
-    plain_ms = p0.elapsed_time(p1)
+    lanes_ms = p0.elapsed_time(p1)
     blocks_plain = [layer.stage_times(lockstep=False, lane=l) for l in range(layer.n_lanes)]
     layer.set_timing(False)
     blocks_plain = {k: sum(b[k] for b in blocks_plain) for k in blocks_plain[0]}
     same = all(np.array_equal(a, b) for a, b in zip(words(res[:layer.n_hid]), lock_words))
     del res
+    # the plain single-ciphertext form: each lane on its own, one ciphertext
+    # per operation and one per bootstrap
+    plain_err = None
+    if args.bert_pack:
+        layer.set_boot_pack(False)
+        res = layer.forward(x, lockstep=False)   # warm: the unpacked bootstraps' own encoded diagonals
+        del res
+        torch.cuda.synchronize(dev)
+        p0.record(stream)
+        res = layer.forward(x, lockstep=False)
+        p1.record(stream)
+        torch.cuda.synchronize(dev)
+        plain_ms = p0.elapsed_time(p1)
+        layer.set_boot_pack(True)
+        errs_plain = []
+        for lane in range(layer.n_lanes):
+            cts = res[lane * layer.n_hid:(lane + 1) * layer.n_hid]
+            dec = np.stack([ctx.decode(ctx.decrypt(sk, c.to_device()), c.scale).real for c in cts])
+            for y, r in zip(NB.unpack_lane(shape, n // 2, lane, dec), NB.layer_reference(shape, w, tokens[lane])):
+                errs_plain.append(float(np.max(np.abs(y - r))))
+        plain_err = max(errs_plain)
+        del res
+    else:
+        plain_ms = lanes_ms
 
     # word parity at this configuration: the Q, K and V projections of the
     # 128-token lane against the oracle's digests for the same seeds
@@ -1161,8 +1186,14 @@ def run_bert_gpu(args, rank, world):
         "e2e": {"value": e2e_s, "unit": "s per layer", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes, "words_equal_direct": bool(e2e_same)},
         "plain_single_ct_form": {"value": plain_ms / 1e3, "unit": "s per layer",
-                                 "lockstep_speedup": plain_ms / step_ms, "words_equal_lockstep": bool(same)},
-        "blocks_ms": {"lockstep": blocks_lock, "plain": blocks_plain},
+                                 "what": "each lane on its own, one ciphertext per operation and per bootstrap",
+                                 "lockstep_speedup": plain_ms / step_ms,
+                                 "max_abs_err_vs_fp64_same_approx": plain_err},
+        "lanes_one_by_one_form": {"value": lanes_ms / 1e3, "unit": "s per layer",
+                                  "what": "each lane on its own, one ciphertext per operation, bootstraps as in "
+                                          "the lockstep form (two ciphertexts each when boot_pack)",
+                                  "lockstep_speedup": lanes_ms / step_ms, "words_equal_lockstep": bool(same)},
+        "blocks_ms": {"lockstep": blocks_lock, "lanes_one_by_one": blocks_plain},
         "setup": {"first_call_s": setup_s, "galois_keys": len(all_steps),
                   "cached_plaintexts": layer.cached_plaintexts()},
         "clocks": clk.summary(),
