@@ -910,9 +910,10 @@ BERT_SCALE = 2.0 ** 46
 BERT_SEED = 600
 
 
-# bootstraps per layer: Q/K/V 48, softmax sums 2, residuals 12 + 12, FFN hidden
-# 48; with two ciphertexts per bootstrap 24 + 2 + 6 + 6 + 24
-BERT_BOOTSTRAPS = {False: 122, True: 62}
+# bootstraps per layer: Q/K 32 (V is projected at the attention's level and
+# not refreshed), softmax sums 2, residuals 12 + 12, FFN hidden 48; with two
+# ciphertexts per bootstrap 16 + 2 + 6 + 6 + 24
+BERT_BOOTSTRAPS = {False: 106, True: 54}
 
 
 def bert_config(pack: bool = True):
@@ -1207,7 +1208,7 @@ def run_bert_gpu(args, rank, world):
 
 def cpu_bert_sample(threads: int, pack: bool = True):
     """A lower bound of the layer on the oracle port: one full bootstrap on the
-    layer's chain, timed, times the layer's bootstraps (122, or 62 with two
+    layer's chain, timed, times the layer's bootstraps (106, or 54 with two
     ciphertexts per bootstrap; projections, attention, GELU, LayerNorm and the
     packing's conjugations left out)."""
     cb = CpuBootstrap(threads, BERT_BITS)

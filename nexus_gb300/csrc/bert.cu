@@ -544,6 +544,7 @@ void BertLayerT<EV, CT>::attention(std::vector<CT> &q, std::vector<CT> &k, std::
     // levels, counted back from the output projection (2 limbs): PV 1,
     // P = E * I 1, exp 8 (constant + 7 squarings), mask 1, Q.K 1
     const int e_limbs = 4, qk_limbs = e_limbs + 10, v_limbs = e_limbs - 1;
+    static_assert(kVInLimbs - 1 == 3, "the V projection lands at the attention's V level");
     for (auto &c : q) ev.mod_switch_to_inplace(c, qk_limbs);
     for (auto &c : k) ev.mod_switch_to_inplace(c, qk_limbs);
     for (auto &c : v) ev.mod_switch_to_inplace(c, v_limbs);
@@ -734,33 +735,34 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
     if ((int)x_in.size() != sh_.n_hid) throw std::invalid_argument("forward: wrong number of input ciphertexts");
     for (auto &c : x_in)
         if (batch_of(c) != (int)lanes_.size()) throw std::invalid_argument("forward: batch does not match the lanes");
-    if (x_in[0].limbs() < 3) throw std::invalid_argument("forward: the input needs at least 3 limbs");
+    if (x_in[0].limbs() < kVInLimbs) throw std::invalid_argument("forward: the input needs at least 4 limbs");
     begin_marks();
     // the residual branch: x / boot_shrink at one limb
     std::vector<CT> x_res = x_in;
     shrink_for_bootstrap(x_res);
     for (auto &c : x_res) ev.mod_switch_to_inplace(c, 1);
-    // Q, K, V at one limb, refreshed
-    std::vector<CT> x2 = x_in;
+    // Q and K at one limb, refreshed; V from the input at 4 limbs lands at
+    // the 3 limbs the attention reads it at, so it needs no bootstrap
+    std::vector<CT> x2 = x_in, x4 = x_in;
     for (auto &c : x2) ev.mod_switch_to_inplace(c, 2);
+    for (auto &c : x4) ev.mod_switch_to_inplace(c, kVInLimbs);
     std::vector<CT> q, k, v;
     project(x2, LT_Q, q);
     project(x2, LT_K, k);
-    project(x2, LT_V, v);
+    project(x4, LT_V, v);
     mark("qkv projections");
     {
         std::vector<CT> all;
-        for (auto *t : {&q, &k, &v})
+        for (auto *t : {&q, &k})
             for (auto &c : *t) all.push_back(std::move(c));
         bootstrap_all(all);
         const int nh = sh_.n_head;
         for (int i = 0; i < nh; ++i) {
             q[i] = std::move(all[i]);
             k[i] = std::move(all[nh + i]);
-            v[i] = std::move(all[2 * nh + i]);
         }
     }
-    mark("qkv bootstraps");
+    mark("qk bootstraps");
     std::vector<CT> o, a;
     attention(q, k, v, o);
     mark("attention");

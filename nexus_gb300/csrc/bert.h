@@ -5,7 +5,8 @@
 // defines both.  One layer: Q/K/V projections, attention (QK^T / sqrt(d_h),
 // softmax, .V), output projection, residual + LayerNorm, FFN (W1, GELU, W2),
 // residual + LayerNorm, with bootstraps (Bootstrapper::bootstrap_3) between
-// the blocks.  The nonlinearities are NEXUS's: CKKSEvaluator::exp and
+// the blocks (Q and K are refreshed; V is projected from the input two levels
+// higher, at the level the attention uses it, and is not).  The nonlinearities are NEXUS's: CKKSEvaluator::exp and
 // ::inverse inside the softmax (src/softmax.cpp:6-42 call sequence, with the
 // row sum taken over diagonals, below), CKKSEvaluator::invert_sqrt inside the
 // LayerNorm (src/layer_norm.cpp:6-33, the feature sum taken over blocks), and
@@ -68,6 +69,10 @@
 #include "nexus_ops.h"
 
 namespace nexus {
+
+// the level the V projection reads its input at: its output (one level
+// lower) is the level the attention's P.V products take V at
+constexpr int kVInLimbs = 4;
 
 struct BertShape {
     int hidden = 768, heads = 12, head_dim = 64, ffn = 3072;

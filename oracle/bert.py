@@ -26,6 +26,9 @@ from . import bootstrap as B
 from . import nexus_l3 as L
 
 LT_Q, LT_K, LT_V, LT_O, LT_1, LT_2 = range(6)
+# the V projection reads its input at 4 limbs and lands at the 3 limbs the
+# attention takes V at: Q and K are refreshed, V is not (kVInLimbs, bert.h)
+V_IN_LIMBS = 4
 
 
 def _pow2_ceil(v):
@@ -297,12 +300,13 @@ class BertLayer:
         rec = (lambda k, v: trace.__setitem__(k, v)) if trace is not None else (lambda k, v: None)
         x_res = [ev.mod_switch_to(c, 1) for c in self.shrink_for_bootstrap(x)]
         x2 = [ev.mod_switch_to(c, 2) for c in x]
-        q, k, v = self.project(x2, LT_Q), self.project(x2, LT_K), self.project(x2, LT_V)
+        x4 = [ev.mod_switch_to(c, V_IN_LIMBS) for c in x]
+        q, k, v = self.project(x2, LT_Q), self.project(x2, LT_K), self.project(x4, LT_V)
         rec("qkv", q + k + v)
-        qkv = self.bootstrap_all(q + k + v)
+        qk = self.bootstrap_all(q + k)
         nh = sh.n_head
-        q, k, v = qkv[:nh], qkv[nh:2 * nh], qkv[2 * nh:]
-        rec("qkv_boot", qkv)
+        q, k = qk[:nh], qk[nh:]
+        rec("qkv_boot", qk + v)
         o = self.attention(q, k, v)
         rec("attention", o)
         a = self.project(o, LT_O)

@@ -89,17 +89,20 @@ def test_qkv_and_attention_stages(env, lockstep):
     from nexus_gb300.operators import Ciphertext
     layer, ctx = env["layer"], env["ctx"]
     nl, nh, nhid = layer.n_lanes, layer.n_head, layer.n_hid
-    x2 = []
-    for c in env["x"]:
-        a = c.to_numpy()[:, :2, :].copy()
-        x2.append(Ciphertext.from_numpy(ctx, a, c.scale))
-    proj = [layer.stage(BERT_PROJECT, w, x2, nh, lockstep) for w in (0, 1, 2)]
+
+    def at(limbs):
+        return [Ciphertext.from_numpy(ctx, c.to_numpy()[:, :limbs, :].copy(), c.scale) for c in env["x"]]
+    # Q and K from the input at 2 limbs, V at 4 (it lands at the attention's level unrefreshed)
+    x2, x4 = at(2), at(4)
+    proj = [layer.stage(BERT_PROJECT, w, x, nh, lockstep) for w, x in ((0, x2), (1, x2), (2, x4))]
     # lane-major q | k | v per lane
     qkv = [proj[t][l * nh + i] for l in range(nl) for t in range(3) for i in range(nh)]
     assert _lane_digests(qkv, 3 * nh) == _want("qkv")
-    boot = layer.stage(BERT_BOOTSTRAP, 0, qkv, 3 * nh, lockstep)
-    assert _lane_digests(boot, 3 * nh) == _want("qkv_boot")
-    att = layer.stage(BERT_ATTENTION, 0, boot, nh, lockstep)
+    qk = [proj[t][l * nh + i] for l in range(nl) for t in range(2) for i in range(nh)]
+    boot = layer.stage(BERT_BOOTSTRAP, 0, qk, 2 * nh, lockstep)
+    att_in = [c for l in range(nl) for c in boot[l * 2 * nh:(l + 1) * 2 * nh] + proj[2][l * nh:(l + 1) * nh]]
+    assert _lane_digests(att_in, 3 * nh) == _want("qkv_boot")
+    att = layer.stage(BERT_ATTENTION, 0, att_in, nh, lockstep)
     assert _lane_digests(att, nh) == _want("attention")
 
 
