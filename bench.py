@@ -1086,6 +1086,9 @@ def run_bert_gpu(args, rank, world):
 
     # each lane on its own, one ciphertext per operation, with the bootstraps
     # in the lockstep form's setting (words equal to the lockstep form's)
+    res = layer.forward(x, lockstep=False)   # warm: the single-lane bootstrapper's encoded diagonals
+    del res
+    torch.cuda.synchronize(dev)
     p0 = torch.cuda.Event(enable_timing=True)
     p1 = torch.cuda.Event(enable_timing=True)
     layer.set_timing(True)
