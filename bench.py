@@ -916,11 +916,11 @@ BERT_SEED = 600
 BERT_BOOTSTRAPS = {False: 106, True: 54}
 
 
-def bert_config(pack: bool = True):
+def bert_config(pack: bool = True, shrink: float = 1.0):
     return {"workload": "bert_base_layer_n65536", "N": 1 << BERT_LOGN, "hidden": 768, "heads": 12, "ffn": 3072,
             "requests": [128, 32, 64], "lanes": "[128] | [32 + 64]", "token_slots_per_block": 256,
             "moduli_bits": "51 + 19x46 + 14x51 + special 51", "hamming_weight": 192, "scale": "2^46",
-            "boot_shrink": 2, "boot_pack": bool(pack), "bootstraps_per_layer": BERT_BOOTSTRAPS[bool(pack)],
+            "boot_shrink": shrink, "rowsum_shrink": 2, "boot_pack": bool(pack), "bootstraps_per_layer": BERT_BOOTSTRAPS[bool(pack)],
             "weights": "N(0, 0.02)", "tokens": "N(0, 1)", "parallelism": "replicas",
             "l2": "keys (~110 GB), encoded weights (~60 GB) and activations far above L2, no flush"}
 
@@ -951,7 +951,7 @@ def run_bert_gpu(args, rank, world):
     ev = Evaluator(ctx, BERT_SCALE, ctx.seal_keygen_relin(sk, seed), stream=stream)
     log_nh = BERT_LOGN - 1
     bs = Bootstrapper(ev, 10, log_nh, log_nh, len(qs) - 2, BERT_SCALE, 25, 59, 2, 1)
-    shape = NB.BertShape()
+    shape = NB.BertShape(boot_shrink=args.bert_shrink)
     w = NB.random_weights(shape, np.random.default_rng(11 + rank))
     rng = np.random.default_rng(12 + rank)
     tokens = [[rng.normal(0, 1, (L, shape.hidden)) for (_, L) in lane] for lane in shape.lanes]
@@ -1169,7 +1169,7 @@ def run_bert_gpu(args, rank, world):
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic: weights ~ N(0,0.02), tokens ~ N(0,1), seeded; keys and encryptions from a SEAL seed",
-        "config": dict(bert_config(bool(args.bert_pack)), tuning=tuning,
+        "config": dict(bert_config(bool(args.bert_pack), args.bert_shrink), tuning=tuning,
                        form="lockstep nexus_bert_layer_forward captured once as a CUDA graph, one "
                             "nexus_graph_launch per step"),
         "parity": parity,
@@ -1756,6 +1756,8 @@ def main():
                     help="prime size of the NTT workload (other values are for profiling captures only)")
     ap.add_argument("--boot-cts", type=int, default=16,
                     help="ciphertexts per bootstrap step (smaller values are for profiling captures only)")
+    ap.add_argument("--bert-shrink", type=float, default=1.0,
+                    help="BERT layer: the factor values are divided by before each bootstrap")
     ap.add_argument("--bert-pack", type=int, choices=[0, 1], default=1,
                     help="BERT layer: refresh two ciphertexts per bootstrap (c0 + i c1; 0: one each)")
     ap.add_argument("--ntt-cts", type=int, default=64,
@@ -1861,7 +1863,7 @@ def main():
                "unit": r["unit"], "n_gpus": world, "steps": 1, "steps_requested": args.steps, "warmup": 0,
                "ms_per_step": r["value"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
                "dtype": "u64", "data": "synthetic (uniform random residues; the cost does not depend on them)",
-               "config": bert_config(bool(args.bert_pack)), "cpu_baseline": r,
+               "config": bert_config(bool(args.bert_pack), args.bert_shrink), "cpu_baseline": r,
                "e2e": {"value": r["value"], "unit": r["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(res), flush=True)
         return

@@ -33,7 +33,7 @@ class BertShape:
     T: int = 256
     # per lane, requests as (first token slot, tokens)
     lanes: list = field(default_factory=lambda: [[(0, 128)], [(0, 32), (64, 64)]])
-    boot_shrink: float = 2.0
+    boot_shrink: float = 1.0
     # two ciphertexts per bootstrap (c0 + i c1, separated by a conjugation)
     boot_pack: bool = True
 

@@ -624,10 +624,10 @@ void BertLayerT<EV, CT>::attention(std::vector<CT> &q, std::vector<CT> &k, std::
     for (int d = 1; d < L; ++d) ev.add_inplace(sum, e[d]);
     {
         Plaintext delta;
-        ev.encode(0.01 / sh_.boot_shrink, sum.limbs(), sum.scale(), delta);
+        ev.encode(0.01 / sh_.rowsum_shrink, sum.limbs(), sum.scale(), delta);
         ev.multiply_plain_inplace(sum, delta);
         ev.rescale_to_next_inplace(sum);
-        sum.scale() /= sh_.boot_shrink;
+        sum.scale() /= sh_.rowsum_shrink;
     }
     std::vector<CT> one{std::move(sum)};
     bootstrap_all(one);

@@ -39,13 +39,14 @@
 // Pairs with delta >= L_r are masked to -128 before NEXUS's exp, which
 // (1 + x/128)^128 maps to 0.
 //
-// Every value about to be bootstrapped is first scaled down by boot_shrink
-// (folded into the preceding linear map or constant product) and its scale
-// divided by the same factor, so the refreshed ciphertext holds the value
-// itself while the bootstrap's EvalMod sees a smaller message: values that
-// are constant over many slots (the softmax row sums, for one) concentrate in
-// few coefficients and leave EvalMod's intervals otherwise.  The bootstrap's
-// own error grows with the factor (about 2e-4 times it at N = 2^16), hence 2.
+// Every value about to be bootstrapped may first be scaled down by
+// boot_shrink (folded into the preceding linear map or constant product) and
+// its scale divided by the same factor, so the refreshed ciphertext holds the
+// value itself while the bootstrap's EvalMod sees a smaller message.  The
+// bootstrap's own error grows with the factor (about 2e-4 times it at
+// N = 2^16), so it is 1 by default; the softmax row sums, constant over a
+// request's token slots (their message concentrates in few coefficients,
+// which leave EvalMod's intervals sooner), take rowsum_shrink = 2.
 //
 // With boot_pack, two ciphertexts share one bootstrap.  The values are real,
 // and the full-slot bootstrap refreshes complex slots: z = c0 + X^(N/2) c1
@@ -79,7 +80,10 @@ struct BertShape {
     int T = 256;  // token slots per feature block
     // per lane, each request as (first token slot, tokens)
     std::vector<std::vector<std::pair<int, int>>> lanes;
-    double boot_shrink = 2.0;
+    double boot_shrink = 1.0;
+    // the softmax row sums, constant over a request's token slots (their
+    // message piles onto few coefficients), are divided by this instead
+    double rowsum_shrink = 2.0;
     // refresh two ciphertexts with one bootstrap (c0 + i c1, separated by a
     // conjugation afterwards)
     bool boot_pack = true;

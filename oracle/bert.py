@@ -39,10 +39,11 @@ def _pow2_ceil(v):
 
 
 class Shape:
-    def __init__(self, slots, hidden, heads, head_dim, ffn, T, lanes, boot_shrink, boot_pack=True):
+    def __init__(self, slots, hidden, heads, head_dim, ffn, T, lanes, boot_shrink, boot_pack=True, rowsum_shrink=2.0):
         self.S, self.hidden, self.heads, self.head_dim, self.ffn, self.T = slots, hidden, heads, head_dim, ffn, T
         self.lanes = [list(l) for l in lanes]
         self.boot_shrink = float(boot_shrink)
+        self.rowsum_shrink = float(rowsum_shrink)
         self.boot_pack = bool(boot_pack)
         self.NB = slots // T
         self.H2 = _pow2_ceil(heads)
@@ -255,9 +256,9 @@ class BertLayer:
         total = e[0]
         for d in range(1, Lm):
             total = ev.add(total, e[d])
-        total = ev.rescale(ev.multiply_plain(total, ev.encode_scalar(0.01 / sh.boot_shrink, total.scale,
+        total = ev.rescale(ev.multiply_plain(total, ev.encode_scalar(0.01 / sh.rowsum_shrink, total.scale,
                                                                      total.limbs)))
-        total.scale /= sh.boot_shrink
+        total.scale /= sh.rowsum_shrink
         inv = ck.inverse(self.bootstrap_all([total])[0])
         inv = ev.rescale(ev.multiply_plain(inv, ev.encode_scalar(0.01, inv.scale, inv.limbs)))
         inv = ev.mod_switch_to(inv, e[0].limbs)

@@ -38,7 +38,7 @@ OUT = Path(__file__).parent / "bert_digests.json"
 CASE = dict(log_n=13, bits=[51] + [46] * 19 + [51] * 14 + [51], seed=seed8(500), hamming_weight=192,
             scale_log2=46, loge=10, boundary_K=25, sin_cos_deg=59, scale_factor=2, inverse_deg=1,
             hidden=64, heads=2, head_dim=32, ffn=128, T=32, lanes=[[[0, 16]], [[0, 4], [8, 8]]],
-            boot_shrink=2.0, boot_pack=True, weight_seed=7, token_seed=8)
+            boot_shrink=1.0, boot_pack=True, weight_seed=7, token_seed=8)
 
 
 def digest(a) -> str:
