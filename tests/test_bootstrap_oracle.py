@@ -151,6 +151,36 @@ def test_oracle_bootstrap_decrypts_to_input(logn):
     assert err.max() < 2.0 ** -12
 
 
+def test_oracle_real_pair_bootstrap_decrypts_to_both_inputs():
+    """Two ciphertexts of real values refreshed by one full-slot bootstrap_3
+    of c0 + X^(N/2) c1 (scale doubled), split by a conjugation
+    (bootstrap_real_pair): with SEAL's keys each output decrypts to its own
+    input within a single bootstrap's error."""
+    from oracle import nexus_l3 as L
+    from oracle import pyoracle as po
+    from oracle import pyref as pr
+    from nexus_gb300.remez import load_table
+    if not pr.available():
+        pytest.skip("SEAL reference build unavailable")
+    log_n = 13
+    n = 1 << log_n
+    qs = po.create_coeff_modulus(n, [51] + [46] * 2 + [51] * 14 + [51])
+    steps = B.rot_key_steps_3(log_n - 1, log_n - 1)
+    s = pr.SealRef(log_n, qs, seed=9, hamming_weight=192, steps=steps)
+    ev = L.Evaluator(po.OracleContext(log_n, qs), s.relin_key(),
+                     {s.galois_elt(st): s.galois_key(s.galois_elt(st)) for st in steps})
+    bs = B.Bootstrapper(ev, 10, log_n - 1, log_n - 1, len(qs) - 2, 2.0 ** 46, K, 59, 2, 1, load_table())
+    bs.generate_LT_coefficient_3()
+    rng = np.random.default_rng(3)
+    vals = [rng.uniform(-1, 1, n // 2) for _ in range(2)]
+    cts = [ev.mod_switch_to(L.Ct(s.encrypt(v, 2.0 ** 46), 2.0 ** 46), 1) for v in vals]
+    outs = B.bootstrap_real_pair(bs, cts[0], cts[1])
+    for v, out in zip(vals, outs):
+        assert out.scale == 2.0 ** 46
+        err = np.abs(s.decrypt(out.data, out.scale) - v)
+        assert err.max() < 2.0 ** -12, err.max()
+
+
 def test_oddbabycount():
     from nexus_gb300.remez import oddbabycount
     # common/func.cpp:95-118, worked by hand for 5 and 7
