@@ -77,7 +77,7 @@ def test_ntt_edge_values(cuda, bits):
 
 
 def test_ntt_full_size_round_trip(cuda):
-    """BASELINE NTT shape (N=2^16, 24 x 60-bit primes), 64 ciphertexts x 2 polys:
+    """The benchmarked NTT shape (N=2^16, 24 x 60-bit primes), 64 ciphertexts x 2 polys:
     INTT(NTT(x)) == x everywhere plus oracle agreement on sampled limbs."""
     import torch
     from nexus_gb300 import Context
