@@ -925,17 +925,22 @@ BERT_SCALE = 2.0 ** 46
 BERT_SEED = 600
 
 
-# bootstraps per layer: Q/K 32 (V is projected at the attention's level and
-# not refreshed), softmax sums 2, residuals 12 + 12, FFN hidden 48; with two
-# ciphertexts per bootstrap 16 + 2 + 6 + 6 + 24
-BERT_BOOTSTRAPS = {False: 106, True: 54}
+def bert_bootstraps(pack: bool = True, fold: bool = True) -> int:
+    """Bootstraps per layer: Q/K 32 ciphertexts (V is projected at the
+    attention's level and not refreshed), the softmax row sums 2 (one per
+    lane, refreshed alone), the residuals 12 + 12 and the FFN hidden
+    activations 48 (24 folded two per ciphertext); two ciphertexts per
+    bootstrap with pack: 16 + 2 + 6 + 6 + 24 (12 folded)."""
+    ffn = 24 if fold else 48
+    return (32 + 24 + ffn) // 2 + 2 if pack else 32 + 2 + 24 + ffn
 
 
-def bert_config(pack: bool = True, shrink: float = 1.0):
+def bert_config(pack: bool = True, shrink: float = 1.0, fold: bool = True):
     return {"workload": "bert_base_layer_n65536", "N": 1 << BERT_LOGN, "hidden": 768, "heads": 12, "ffn": 3072,
             "requests": [128, 32, 64], "lanes": "[128] | [32 + 64]", "token_slots_per_block": 256,
             "moduli_bits": "51 + 19x46 + 14x51 + special 51", "hamming_weight": 192, "scale": "2^46",
-            "boot_shrink": shrink, "rowsum_shrink": 2, "boot_pack": bool(pack), "bootstraps_per_layer": BERT_BOOTSTRAPS[bool(pack)],
+            "boot_shrink": shrink, "rowsum_shrink": 2, "boot_pack": bool(pack), "ffn_fold": bool(fold),
+            "bootstraps_per_layer": bert_bootstraps(pack, fold),
             "weights": "N(0, 0.02)", "tokens": "N(0, 1)", "parallelism": "replicas",
             "l2": "keys (~110 GB), encoded weights (~60 GB) and activations far above L2, no flush"}
 
@@ -975,6 +980,7 @@ def run_bert_gpu(args, rank, world):
     bs.generate_LT_coefficient_3()
     layer = NB.BertLayer(bs, shape, w)
     layer.set_boot_pack(bool(args.bert_pack))
+    layer.set_ffn_fold(bool(args.bert_fold))
     tuning = ctx.autotune(20, 16)
     tuning["ntt_form"] = _apply_ntt_form(ctx, args)
     all_steps = steps + [s for s in layer.rotation_steps() if s not in steps]
@@ -1136,11 +1142,12 @@ def run_bert_gpu(args, rank, world):
     same = all(np.array_equal(a, b) for a, b in zip(words(res[:layer.n_hid]), lock_words))
     del res
     # the plain single-ciphertext form: each lane on its own, one ciphertext
-    # per operation and one per bootstrap
+    # per operation and one per bootstrap, the FFN unfolded
     plain_err = None
-    if args.bert_pack:
+    if args.bert_pack or args.bert_fold:
         layer.set_boot_pack(False)
-        res = layer.forward(x, lockstep=False)   # warm: the unpacked bootstraps' own encoded diagonals
+        layer.set_ffn_fold(False)
+        res = layer.forward(x, lockstep=False)   # warm: the unpacked bootstraps' and unfolded FFN1's encodings
         del res
         torch.cuda.synchronize(dev)
         p0.record(stream)
@@ -1148,7 +1155,8 @@ def run_bert_gpu(args, rank, world):
         p1.record(stream)
         torch.cuda.synchronize(dev)
         plain_ms = p0.elapsed_time(p1)
-        layer.set_boot_pack(True)
+        layer.set_boot_pack(bool(args.bert_pack))
+        layer.set_ffn_fold(bool(args.bert_fold))
         errs_plain = []
         for lane in range(layer.n_lanes):
             cts = res[lane * layer.n_hid:(lane + 1) * layer.n_hid]
@@ -1185,6 +1193,8 @@ def run_bert_gpu(args, rank, world):
         del x2
 
     step_ms = total_ms / args.steps
+    free_b, total_b = torch.cuda.mem_get_info(dev)
+    mem_used = total_b - free_b
     peak, peak_kind = _peak_hbm()
     ntt_avg_ms = ntt_ms / max(1, ntt_calls)
     alg_bytes_per_call = 16.0 * n * ntt_limbs / max(1, ntt_calls)
@@ -1202,7 +1212,7 @@ def run_bert_gpu(args, rank, world):
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic: weights ~ N(0,0.02), tokens ~ N(0,1), seeded; keys and encryptions from a SEAL seed",
-        "config": dict(bert_config(bool(args.bert_pack), args.bert_shrink), tuning=tuning,
+        "config": dict(bert_config(bool(args.bert_pack), args.bert_shrink, bool(args.bert_fold)), tuning=tuning,
                        form=("lockstep nexus_bert_layer_forward captured once as a CUDA graph, one "
                              "nexus_graph_launch per step" if graph is not None
                              else "lockstep nexus_bert_layer_forward, direct calls")),
@@ -1225,33 +1235,36 @@ def run_bert_gpu(args, rank, world):
         "e2e": {"value": e2e_s, "unit": "s per layer", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes, "words_equal_direct": bool(e2e_same)},
         "plain_single_ct_form": {"value": plain_ms / 1e3, "unit": "s per layer",
-                                 "what": "each lane on its own, one ciphertext per operation and per bootstrap",
+                                 "what": "each lane on its own, one ciphertext per operation and per bootstrap, "
+                                         "the FFN unfolded",
                                  "lockstep_speedup": plain_ms / step_ms,
                                  "max_abs_err_vs_fp64_same_approx": plain_err},
         "lanes_one_by_one_form": {"value": lanes_ms / 1e3, "unit": "s per layer",
                                   "what": "each lane on its own, one ciphertext per operation, bootstraps as in "
-                                          "the lockstep form (two ciphertexts each when boot_pack)",
+                                          "the lockstep form (two ciphertexts each when boot_pack), the FFN "
+                                          "folded as in it",
                                   "lockstep_speedup": lanes_ms / step_ms, "words_equal_lockstep": bool(same)},
         "blocks_ms": {"lockstep": blocks_lock, "lanes_one_by_one": blocks_plain},
         "setup": {"first_call_s": setup_s, "galois_keys": len(all_steps),
-                  "cached_plaintexts": layer.cached_plaintexts()},
+                  "cached_plaintexts": layer.cached_plaintexts(), "device_memory_in_use_gb": mem_used / 1e9},
         "clocks": clk.summary(),
         "gpu_launches": launches,
-        "cpu_baseline": cpu_bert_sample(os.cpu_count() or 1, bool(args.bert_pack)) if rank == 0 and world == 1
+        "cpu_baseline": cpu_bert_sample(os.cpu_count() or 1, bool(args.bert_pack), bool(args.bert_fold))
+        if rank == 0 and world == 1
         else None,
     }
 
 
 
 
-def cpu_bert_sample(threads: int, pack: bool = True):
+def cpu_bert_sample(threads: int, pack: bool = True, fold: bool = True):
     """A lower bound of the layer on the oracle port: one full bootstrap on the
-    layer's chain, timed, times the layer's bootstraps (106, or 54 with two
-    ciphertexts per bootstrap; projections, attention, GELU, LayerNorm and the
-    packing's conjugations left out)."""
+    layer's chain, timed, times the layer's bootstraps (bert_bootstraps:
+    42 with two ciphertexts per bootstrap and the FFN folded; projections,
+    attention, GELU, LayerNorm and the packing's conjugations left out)."""
     cb = CpuBootstrap(threads, BERT_BITS)
     t = cb.bootstrap()
-    n_boot = BERT_BOOTSTRAPS[bool(pack)]
+    n_boot = bert_bootstraps(pack, fold)
     total = n_boot * t
     return {"value": total, "unit": "s per layer", "cores": threads, "kind": "port",
             "sample": f"one full-slot bootstrap_3 on the layer chain (51 + 19x46 + 14x51 + 51) with the oracle port "
@@ -1821,6 +1834,8 @@ def main():
                     help="BERT layer: the factor values are divided by before each bootstrap")
     ap.add_argument("--bert-pack", type=int, choices=[0, 1], default=1,
                     help="BERT layer: refresh two ciphertexts per bootstrap (c0 + i c1; 0: one each)")
+    ap.add_argument("--bert-fold", type=int, choices=[0, 1], default=1,
+                    help="BERT layer: FFN hidden activations of two ciphertexts folded into one (0: unfolded)")
     ap.add_argument("--ntt-cts", type=int, default=64,
                     help="ciphertexts per step (smaller values are for profiling captures only)")
     args = ap.parse_args()
@@ -1919,12 +1934,13 @@ def main():
         if rank != 0:
             return
         threads = max(1, os.cpu_count() or 1)
-        r = cpu_bert_sample(threads, bool(args.bert_pack))
+        r = cpu_bert_sample(threads, bool(args.bert_pack), bool(args.bert_fold))
         res = {"impl": "reference", "metric": "bert_base_layer_latency_n65536", "value": r["value"],
                "unit": r["unit"], "n_gpus": world, "steps": 1, "steps_requested": args.steps, "warmup": 0,
                "ms_per_step": r["value"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
                "dtype": "u64", "data": "synthetic (uniform random residues; the cost does not depend on them)",
-               "config": bert_config(bool(args.bert_pack), args.bert_shrink), "cpu_baseline": r,
+               "config": bert_config(bool(args.bert_pack), args.bert_shrink, bool(args.bert_fold)),
+               "cpu_baseline": r,
                "e2e": {"value": r["value"], "unit": r["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(res), flush=True)
         return

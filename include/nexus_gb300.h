@@ -685,7 +685,8 @@ int nexus_bert_layer_info(const nexus_bert_layer *layer, int *n_lanes, int *n_hi
 /* the slot rotations the layer performs (steps = NULL only counts them) */
 int nexus_bert_layer_rotation_steps(const nexus_bert_layer *layer, int *steps, int *count, int capacity);
 /* out[l * n_hidden_cts + c] = the layer applied to x[l * n_hidden_cts + c]
- * (lane-major; x at 3 or more limbs, both token copies filled); lockstep = 0
+ * (lane-major; x at 4 or more limbs, both token copies filled; the
+ * outputs' first token copies hold the result); lockstep = 0
  * runs each lane on its own, one ciphertext at a time (the plain form),
  * lockstep = 1 runs every lane together and bootstraps and evaluates the
  * nonlinearities over all ciphertexts of a step at once, with the same words. */
@@ -713,6 +714,16 @@ int nexus_bert_layer_set_timing(nexus_bert_layer *layer, int enable);
  * pair, the same error per output.  On by default; no counterpart in the
  * reference (NEXUS has no layer). */
 int nexus_bert_layer_set_boot_pack(nexus_bert_layer *layer, int enable);
+/* With ffn_fold on, and when every request's tokens lie in token slots
+ * [0, T/2) and the FFN takes two or more ciphertexts, the FFN hidden
+ * activations of ciphertexts 2i and 2i+1 share one ciphertext, the second's
+ * tokens in the upper half of every token block: W1 writes the lower half
+ * only, its outputs are folded by one rotation of -T/2, refreshed and passed
+ * through GELU, and W2 reads ciphertext 2i+1 as the folded one rotated by
+ * T/2.  Half the FFN bootstraps and GELUs; the rotation steps include +-T/2
+ * whenever the fold applies.  On by default; no counterpart in the
+ * reference (NEXUS has no layer). */
+int nexus_bert_layer_set_ffn_fold(nexus_bert_layer *layer, int enable);
 int nexus_bert_layer_stage_times(nexus_bert_layer *layer, int lockstep, int lane, double *ms, char *names,
                                  size_t names_capacity, int *count, int capacity);
 

@@ -144,6 +144,7 @@ SIGNATURES = [
      [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     ("nexus_bert_layer_set_timing", C.c_int, [C.c_void_p, C.c_int]),
     ("nexus_bert_layer_set_boot_pack", C.c_int, [C.c_void_p, C.c_int]),
+    ("nexus_bert_layer_set_ffn_fold", C.c_int, [C.c_void_p, C.c_int]),
     ("nexus_bert_layer_stage_times", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_char_p,
                                                C.c_size_t, C.POINTER(C.c_int), C.c_int]),
 ]

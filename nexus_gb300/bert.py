@@ -36,6 +36,9 @@ class BertShape:
     boot_shrink: float = 1.0
     # two ciphertexts per bootstrap (c0 + i c1, separated by a conjugation)
     boot_pack: bool = True
+    # the FFN hidden activations of two ciphertexts in one (the halves of
+    # each token block), when every request's tokens lie in [0, T/2)
+    ffn_fold: bool = True
 
     def blocks(self, slots: int) -> int:
         return slots // self.T
@@ -223,6 +226,7 @@ class BertLayer:
               "nexus_bert_layer_info")
         self.n_lanes, self.n_hid, self.n_head, self.n_ffn = [i.value for i in info]
         self.set_boot_pack(shape.boot_pack)
+        self.set_ffn_fold(shape.ffn_fold)
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -248,6 +252,10 @@ class BertLayer:
     def set_boot_pack(self, enable: bool) -> None:
         """Two ciphertexts per bootstrap (nexus_bert_layer_set_boot_pack)."""
         check(lib().nexus_bert_layer_set_boot_pack(self._h, 1 if enable else 0), "nexus_bert_layer_set_boot_pack")
+
+    def set_ffn_fold(self, enable: bool) -> None:
+        """Two FFN hidden ciphertexts folded into one (nexus_bert_layer_set_ffn_fold)."""
+        check(lib().nexus_bert_layer_set_ffn_fold(self._h, 1 if enable else 0), "nexus_bert_layer_set_ffn_fold")
 
     def stage_times(self, lockstep: bool = True, lane: int = 0) -> dict:
         """Device ms of each block of the last forward with timing on."""

@@ -148,6 +148,10 @@ void BertShape::derive(size_t slots)
     G = (int)std::ceil(std::sqrt((double)Lmax));
     Glt = (int)std::ceil(std::sqrt((double)NB));
     if (!(boot_shrink >= 1.0)) throw std::invalid_argument("boot_shrink must be >= 1");
+    fold_ok = n_ffn >= 2;
+    for (auto &lane : lanes)
+        for (auto &q : lane)
+            if (q.first + q.second > T / 2) fold_ok = false;
 }
 
 std::vector<int> BertShape::rotation_steps() const
@@ -166,6 +170,10 @@ std::vector<int> BertShape::rotation_steps() const
     }
     for (int m = 1; m < KB; m <<= 1) push(H2 * T * m);
     for (int m = 1; m < NB; m <<= 1) push(T * m);
+    if (fold_ok) {
+        push(T / 2);
+        push(-T / 2);
+    }
     return v;
 }
 
@@ -285,19 +293,21 @@ bool BertLayerT<EV, CT>::diag_nonzero(int which, int a, int b, int d) const
 
 // diagonal d of the (a -> b) block of map `which`, scaled by 1/boot_shrink,
 // rotated right by pre_rotate_blocks blocks: slot s holds the entry of block
-// (s / T - pre_rotate_blocks) mod NB
+// (s / T - pre_rotate_blocks) mod NB (on the lower half of each block only
+// when lower_half)
 template <class EV, class CT>
-std::vector<double> BertLayerT<EV, CT>::diag_vector(int which, int a, int b, int d, int pre_rotate_blocks) const
+std::vector<double> BertLayerT<EV, CT>::diag_vector(int which, int a, int b, int d, int pre_rotate_blocks,
+                                                    bool lower_half) const
 {
     const auto &W = weights(which);
-    const int nout = out_features(which), NB = sh_.NB, T = sh_.T;
+    const int nout = out_features(which), NB = sh_.NB, T = sh_.T, span = lower_half ? T / 2 : T;
     std::vector<double> v((size_t)sh_.S, 0.0);
     for (int j = 0; j < NB; ++j) {
         const int fo = out_feature(which, b, j), fi = in_feature(which, a, (j + d) % NB);
         if (fo < 0 || fi < 0) continue;
         const double x = W[(size_t)fi * nout + fo] / sh_.boot_shrink;
         const int dst = (j + pre_rotate_blocks) % NB;
-        std::fill(v.begin() + (size_t)dst * T, v.begin() + (size_t)(dst + 1) * T, x);
+        std::fill(v.begin() + (size_t)dst * T, v.begin() + (size_t)dst * T + span, x);
     }
     return v;
 }
@@ -305,14 +315,15 @@ std::vector<double> BertLayerT<EV, CT>::diag_vector(int which, int a, int b, int
 // encode every nonzero diagonal of map `which` at (limbs, scale) that is not
 // cached yet: host FFTs on all cores, one NTT launch per plaintext
 template <class EV, class CT>
-void BertLayerT<EV, CT>::encode_diagonals(int which, int limbs, double scale)
+void BertLayerT<EV, CT>::encode_diagonals(int which, int limbs, double scale, bool lower_half)
 {
     std::vector<BertPlaintexts::DKey> keys;
     const uint64_t sb = bits_of(scale);
+    const int tag = which + (lower_half ? LT_COUNT : 0);
     for (int a = 0; a < in_count(which); ++a)
         for (int b = 0; b < out_count(which); ++b)
             for (int d = 0; d < sh_.NB; ++d) {
-                const BertPlaintexts::DKey key{which, a, b, d, limbs, sb};
+                const BertPlaintexts::DKey key{tag, a, b, d, limbs, sb};
                 if (!pt_->diag.count(key) && diag_nonzero(which, a, b, d)) keys.push_back(key);
             }
     Evaluator &base = base_evaluator();
@@ -327,7 +338,7 @@ void BertLayerT<EV, CT>::encode_diagonals(int which, int limbs, double scale)
         std::vector<Plaintext *> outs;
         for (size_t i = lo; i < hi; ++i) {
             const int a = std::get<1>(keys[i]), b = std::get<2>(keys[i]), d = std::get<3>(keys[i]);
-            const std::vector<double> v = diag_vector(which, a, b, d, (d / sh_.Glt) * sh_.Glt);
+            const std::vector<double> v = diag_vector(which, a, b, d, (d / sh_.Glt) * sh_.Glt, lower_half);
             vecs[i - lo].assign(v.begin(), v.end());
             vp.push_back(&vecs[i - lo]);
             outs.push_back(&plains[i - lo]);
@@ -338,23 +349,24 @@ void BertLayerT<EV, CT>::encode_diagonals(int which, int limbs, double scale)
 }
 
 template <class EV, class CT>
-const Plaintext &BertLayerT<EV, CT>::diag(int which, int a, int b, int d, int limbs, double scale)
+const Plaintext &BertLayerT<EV, CT>::diag(int which, int a, int b, int d, int limbs, double scale, bool lower_half)
 {
-    const BertPlaintexts::DKey key{which, a, b, d, limbs, bits_of(scale)};
+    const BertPlaintexts::DKey key{which + (lower_half ? LT_COUNT : 0), a, b, d, limbs, bits_of(scale)};
     auto it = pt_->diag.find(key);
     if (it == pt_->diag.end()) {
-        encode_diagonals(which, limbs, scale);
+        encode_diagonals(which, limbs, scale, lower_half);
         it = pt_->diag.find(key);
         if (it == pt_->diag.end()) throw std::logic_error("diagonal missing after encoding");
     }
     return it->second;
 }
 
-// bias of map `which` for output ciphertext ct: b[f] on every token slot of f's block
+// bias of map `which` for output ciphertext ct: b[f] on every token slot of
+// f's block (on the lower half only when lower_half)
 template <class EV, class CT>
-const Plaintext &BertLayerT<EV, CT>::bias_plain(int which, int ct, int limbs, double scale)
+const Plaintext &BertLayerT<EV, CT>::bias_plain(int which, int ct, int limbs, double scale, bool lower_half)
 {
-    const auto key = std::make_tuple(which, ct, limbs, bits_of(scale));
+    const auto key = std::make_tuple(which + (lower_half ? LT_COUNT : 0), ct, limbs, bits_of(scale));
     auto it = pt_->bias.find(key);
     if (it != pt_->bias.end()) return it->second;
     const auto &bv = bias(which);
@@ -362,7 +374,7 @@ const Plaintext &BertLayerT<EV, CT>::bias_plain(int which, int ct, int limbs, do
     for (int j = 0; j < sh_.NB; ++j) {
         const int f = out_feature(which, ct, j);
         if (f < 0) continue;
-        for (int t = 0; t < sh_.T; ++t) v[(size_t)j * sh_.T + t] = bv[f];
+        for (int t = 0; t < (lower_half ? sh_.T / 2 : sh_.T); ++t) v[(size_t)j * sh_.T + t] = bv[f];
     }
     Plaintext p;
     ev_->encode(v, limbs, scale, p);
@@ -424,7 +436,7 @@ void BertLayerT<EV, CT>::exact_scale_const(CT &ct, double value, double target_s
 
 // y = map(x) + bias, x at >= 2 limbs: y at x.limbs - 1 at scale delta / boot_shrink
 template <class EV, class CT>
-void BertLayerT<EV, CT>::project(const std::vector<CT> &x, int which, std::vector<CT> &y)
+void BertLayerT<EV, CT>::project(const std::vector<CT> &x, int which, std::vector<CT> &y, bool lower_half)
 {
     EV &ev = *ev_;
     const int n_in = in_count(which), n_out = out_count(which);
@@ -436,7 +448,7 @@ void BertLayerT<EV, CT>::project(const std::vector<CT> &x, int which, std::vecto
         if (c.limbs() != l || c.scale() != in_scale) throw std::invalid_argument("project: inputs differ");
     // diagonals at a scale that brings the product back to delta after the rescale
     const double dscale = (double)ev.modulus(l - 1) * delta_ / in_scale;
-    encode_diagonals(which, l, dscale);
+    encode_diagonals(which, l, dscale, lower_half);
     const int Glt = sh_.Glt, T = sh_.T, NB = sh_.NB;
     std::vector<std::vector<CT>> baby(n_in);
     std::vector<int> steps;
@@ -462,7 +474,7 @@ void BertLayerT<EV, CT>::project(const std::vector<CT> &x, int which, std::vecto
                     const int d = g * Glt + bb;
                     if (!diag_nonzero(which, a, b, d)) continue;
                     terms.push_back(&baby[a][bb]);
-                    pts.push_back(&diag(which, a, b, d, l, dscale));
+                    pts.push_back(&diag(which, a, b, d, l, dscale, lower_half));
                 }
             if (terms.empty()) continue;
             ev.multiply_plain_accumulate(terms, pts, giant);
@@ -481,9 +493,42 @@ void BertLayerT<EV, CT>::project(const std::vector<CT> &x, int which, std::vecto
         if (!have) throw std::logic_error("project: an output ciphertext has no diagonal");
         ev.rescale_to_next_inplace(acc);
         acc.scale() = delta_ / sh_.boot_shrink;
-        ev.add_plain_inplace(acc, bias_plain(which, b, acc.limbs(), acc.scale()));
+        ev.add_plain_inplace(acc, bias_plain(which, b, acc.limbs(), acc.scale(), lower_half));
         y[b] = std::move(acc);
     }
+}
+
+// out[i] = x[2i] + rot(x[2i+1], -T/2) (x[2i] alone for an odd last one); the
+// inputs hold values on the lower half of each token block only
+template <class EV, class CT>
+void BertLayerT<EV, CT>::fold_halves(std::vector<CT> &x)
+{
+    EV &ev = *ev_;
+    std::vector<CT> out((x.size() + 1) / 2);
+    for (size_t i = 0; i < out.size(); ++i) {
+        if (2 * i + 1 < x.size()) {
+            CT t;
+            ev.rotate_vector(x[2 * i + 1], sh_.S - sh_.T / 2, t);
+            ev.add(x[2 * i], t, out[i]);
+        } else {
+            out[i] = std::move(x[2 * i]);
+        }
+    }
+    x = std::move(out);
+}
+
+// inverse of fold_halves on the lower half: out[2i] = x[i], out[2i+1] = rot(x[i], T/2)
+template <class EV, class CT>
+void BertLayerT<EV, CT>::unfold_halves(std::vector<CT> &x, int count)
+{
+    EV &ev = *ev_;
+    if ((int)x.size() != (count + 1) / 2) throw std::logic_error("unfold_halves: wrong number of ciphertexts");
+    std::vector<CT> out(count);
+    for (int i = 0; i < count; ++i) {
+        if (i % 2) ev.rotate_vector(x[i / 2], sh_.T / 2, out[i]);
+        else out[i] = x[i / 2];
+    }
+    x = std::move(out);
 }
 
 template <class EV, class CT>
@@ -783,7 +828,9 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
     for (auto &c : y_res) ev.mod_switch_to_inplace(c, 1);
     for (auto &c : a) ev.mod_switch_to_inplace(c, 2);
     std::vector<CT> h, f;
-    project(a, LT_1, h);
+    const bool fold = sh_.folding();
+    project(a, LT_1, h, fold);
+    if (fold) fold_halves(h);
     mark("ffn1 projection");
     bootstrap_all(h);
     mark("ffn hidden bootstraps");
@@ -798,6 +845,7 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
         });
     }
     mark("gelu");
+    if (fold) unfold_halves(h, sh_.n_ffn);
     project(h, LT_2, f);
     for (int c = 0; c < sh_.n_hid; ++c) {
         f[c].scale() = y_res[c].scale();

@@ -55,6 +55,18 @@
 // and c0 = z + conj(z), c1 = (conj(z) - z) X^(N/2) afterwards (one
 // conjugation).  The words EvalMod sees are the two messages' sum, and the
 // error of each output is that of an unpacked bootstrap.
+//
+// With ffn_fold, the FFN hidden activations take half the ciphertexts.  Past
+// the attention only the first token copies matter and every op but the
+// linear maps' block rotations acts on one token slot; when every request's
+// tokens lie in the lower half of the token block ([0, T/2)), FFN1 writes
+// only that half (its diagonals and bias are zero on the upper half), and
+// ciphertexts 2i and 2i+1 of its output become one: h_2i + rot(h_2i+1, -T/2)
+// holds the second's tokens in the upper half of every block.  Those are
+// refreshed and passed through GELU, and FFN2 reads ciphertext 2i as the
+// folded one itself and 2i+1 as its rotation by T/2 (each token slot of the
+// lower half then holds the right feature; the upper half, not read for the
+// first copies, holds other tokens' values of the same magnitude).
 #pragma once
 #include <cstdint>
 #include <map>
@@ -87,10 +99,16 @@ struct BertShape {
     // refresh two ciphertexts with one bootstrap (c0 + i c1, separated by a
     // conjugation afterwards)
     bool boot_pack = true;
+    // fold two FFN hidden ciphertexts into one (the halves of each token
+    // block) when the requests allow it (fold_ok)
+    bool ffn_fold = true;
 
     // derived by derive()
     int S = 0, NB = 0, H2 = 0, KB = 0, n_head = 0, n_hid = 0, n_ffn = 0, Lmax = 0, G = 0, Glt = 0;
+    // every request's tokens in [0, T/2) and at least two FFN ciphertexts
+    bool fold_ok = false;
     void derive(size_t slots);
+    bool folding() const { return ffn_fold && fold_ok; }
     // every rotation step the layer uses (the bootstrapper's are separate)
     std::vector<int> rotation_steps() const;
 };
@@ -125,7 +143,8 @@ public:
     void forward(const std::vector<CT> &x, std::vector<CT> &out);
 
     // the stages of forward(), public for tests and profiling
-    void project(const std::vector<CT> &x, int which, std::vector<CT> &y);       // linear map + bias
+    // linear map + bias; lower_half: written on token slots [0, T/2) only
+    void project(const std::vector<CT> &x, int which, std::vector<CT> &y, bool lower_half = false);
     void attention(std::vector<CT> &q, std::vector<CT> &k, std::vector<CT> &v, std::vector<CT> &o);
     void layer_norm(std::vector<CT> &x);
     void bootstrap_all(std::vector<CT> &cts);
@@ -144,6 +163,7 @@ public:
     size_t cached_plaintexts() const { return pt_->count(); }
     const BertShape &shape() const { return sh_; }
     void set_boot_pack(bool on) { sh_.boot_pack = on; }
+    void set_ffn_fold(bool on) { sh_.ffn_fold = on; }
 
 private:
     int in_count(int which) const;
@@ -156,10 +176,13 @@ private:
     int in_feature(int which, int ct, int block) const;
     int out_feature(int which, int ct, int block) const;
     bool diag_nonzero(int which, int a, int b, int d) const;
-    std::vector<double> diag_vector(int which, int a, int b, int d, int pre_rotate_blocks) const;
-    const Plaintext &diag(int which, int a, int b, int d, int limbs, double scale);
-    void encode_diagonals(int which, int limbs, double scale);
-    const Plaintext &bias_plain(int which, int ct, int limbs, double scale);
+    std::vector<double> diag_vector(int which, int a, int b, int d, int pre_rotate_blocks, bool lower_half) const;
+    const Plaintext &diag(int which, int a, int b, int d, int limbs, double scale, bool lower_half);
+    void encode_diagonals(int which, int limbs, double scale, bool lower_half);
+    const Plaintext &bias_plain(int which, int ct, int limbs, double scale, bool lower_half);
+    // ciphertexts 2i, 2i+1 (lower-half layout) -> one; and back to `count`
+    void fold_halves(std::vector<CT> &x);
+    void unfold_halves(std::vector<CT> &x, int count);
     void masks(int delta, int kind, int limbs, double scale, std::vector<const Plaintext *> &out);
     void shrink_for_bootstrap(std::vector<CT> &cts);
     void begin_marks();

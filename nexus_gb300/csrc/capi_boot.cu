@@ -699,6 +699,15 @@ extern "C" int nexus_bert_layer_set_boot_pack(nexus_bert_layer *layer, int enabl
     return 0;
 }
 
+extern "C" int nexus_bert_layer_set_ffn_fold(nexus_bert_layer *layer, int enable)
+{
+    if (!layer) return fail("nexus_bert_layer_set_ffn_fold", "null argument");
+    layer->shape.ffn_fold = enable != 0;
+    for (auto &l : layer->single) l->set_ffn_fold(enable != 0);
+    if (layer->lockstep) layer->lockstep->set_ffn_fold(enable != 0);
+    return 0;
+}
+
 extern "C" int nexus_bert_layer_stage_times(nexus_bert_layer *layer, int lockstep, int lane, double *ms, char *names,
                                             size_t names_capacity, int *count, int capacity)
 {

@@ -15,6 +15,9 @@ Packing (the engine's): slot j*T + t of a ciphertext is feature block j at
 token slot t; a lane packs requests (o_r, L_r) with tokens at o_r + i and
 o_r + L_r + i.  std layout: feature f in ciphertext f // NB, block f % NB;
 head layout: feature h*dh + k in ciphertext k // KB, block (k % KB)*H2 + h.
+With the FFN fold (BertShape::ffn_fold), FFN1 writes the lower half of each
+token block only and its outputs 2i, 2i+1 become h_2i + rot(h_2i+1, -T/2);
+FFN2 reads them back as the folded ciphertext and its rotation by T/2.
 """
 from __future__ import annotations
 
@@ -39,7 +42,8 @@ def _pow2_ceil(v):
 
 
 class Shape:
-    def __init__(self, slots, hidden, heads, head_dim, ffn, T, lanes, boot_shrink, boot_pack=True, rowsum_shrink=2.0):
+    def __init__(self, slots, hidden, heads, head_dim, ffn, T, lanes, boot_shrink, boot_pack=True, rowsum_shrink=2.0,
+                 ffn_fold=True):
         self.S, self.hidden, self.heads, self.head_dim, self.ffn, self.T = slots, hidden, heads, head_dim, ffn, T
         self.lanes = [list(l) for l in lanes]
         self.boot_shrink = float(boot_shrink)
@@ -54,6 +58,13 @@ class Shape:
         self.Lmax = max(Lr for lane in lanes for (_, Lr) in lane)
         self.G = int(math.ceil(math.sqrt(self.Lmax)))
         self.Glt = int(math.ceil(math.sqrt(self.NB)))
+        # BertShape::derive: the fold needs every request's tokens in [0, T/2)
+        self.ffn_fold = bool(ffn_fold)
+        self.fold_ok = self.n_ffn >= 2 and all(o + Lr <= T // 2 for lane in lanes for (o, Lr) in lane)
+
+    @property
+    def folding(self):
+        return self.ffn_fold and self.fold_ok
 
     def rotation_steps(self):
         v = []
@@ -83,6 +94,9 @@ class Shape:
         while m < self.NB:
             push(self.T * m)
             m <<= 1
+        if self.fold_ok:
+            push(self.T // 2)
+            push(-self.T // 2)
         return v
 
 
@@ -126,8 +140,9 @@ class BertLayer:
     def _bias(self, which):
         return self.w[("bq", "bk", "bv", "bo", "b1", "b2")[which]]
 
-    def _diag(self, which, a, b, d):
-        """diagonal d of block (a -> b), divided by boot_shrink, or None when zero"""
+    def _diag(self, which, a, b, d, lower_half=False):
+        """diagonal d of block (a -> b), divided by boot_shrink, or None when
+        zero; lower_half: on token slots [0, T/2) of each block only"""
         sh = self.sh
         W = self._weights(which)
         vals = np.zeros(sh.NB)
@@ -141,9 +156,17 @@ class BertLayer:
             return None
         g = d // sh.Glt
         vals = np.roll(vals, g * sh.Glt)       # pre-rotated by the giant step
-        return np.repeat(vals, sh.T)
+        return self._spread(vals, lower_half)
 
-    def project(self, x, which):
+    def _spread(self, per_block, lower_half):
+        """one value per block on every token slot of it (the lower half only)"""
+        sh = self.sh
+        v = np.repeat(per_block, sh.T).reshape(sh.NB, sh.T)
+        if lower_half:
+            v[:, sh.T // 2:] = 0.0
+        return v.ravel()
+
+    def project(self, x, which, lower_half=False):
         ev, sh = self.ev, self.sh
         l = x[0].limbs
         in_scale = x[0].scale
@@ -160,7 +183,7 @@ class BertLayer:
                         d = g * sh.Glt + bb
                         if d >= sh.NB:
                             break
-                        v = self._diag(which, a, b, d)
+                        v = self._diag(which, a, b, d, lower_half)
                         if v is None:
                             continue
                         t = ev.multiply_plain(baby[a][bb], ev.encode(v, dscale, l))
@@ -171,15 +194,28 @@ class BertLayer:
                 g += 1
             acc = ev.rescale(acc)
             acc.scale = self.delta / sh.boot_shrink
-            bias = np.zeros(sh.S)
+            per_block = np.zeros(sh.NB)
             bv = self._bias(which)
             for j in range(sh.NB):
                 f = self._out_feature(which, b, j)
                 if f >= 0:
-                    bias[j * sh.T:(j + 1) * sh.T] = bv[f]
-            acc = ev.add_plain(acc, ev.encode(bias, acc.scale, acc.limbs))
+                    per_block[j] = bv[f]
+            acc = ev.add_plain(acc, ev.encode(self._spread(per_block, lower_half), acc.scale, acc.limbs))
             y.append(acc)
         return y
+
+    def fold_halves(self, x):
+        """BertLayerT::fold_halves: x[2i] + rot(x[2i+1], -T/2), an odd last one alone."""
+        ev, sh = self.ev, self.sh
+        out = []
+        for i in range(0, len(x), 2):
+            out.append(ev.add(x[i], ev.rotate(x[i + 1], sh.S - sh.T // 2)) if i + 1 < len(x) else x[i])
+        return out
+
+    def unfold_halves(self, x, count):
+        """BertLayerT::unfold_halves: ciphertext 2i is x[i], 2i+1 is rot(x[i], T/2)."""
+        assert len(x) == (count + 1) // 2
+        return [x[i // 2] if i % 2 == 0 else self.ev.rotate(x[i // 2], self.sh.T // 2) for i in range(count)]
 
     # -- helpers ------------------------------------------------------------------
     def exact_scale_const(self, ct, value, target):
@@ -320,10 +356,16 @@ class BertLayer:
         rec("ln1", a)
         y_res = [ev.mod_switch_to(c, 1) for c in self.shrink_for_bootstrap(a)]
         a2 = [ev.mod_switch_to(c, 2) for c in a]
-        h = self.bootstrap_all(self.project(a2, LT_1))
+        fold = sh.folding
+        h = self.project(a2, LT_1, fold)
+        if fold:
+            h = self.fold_halves(h)
+        h = self.bootstrap_all(h)
         rec("ffn1_boot", h)
         h = [L.gelu(self.ck, c) for c in h]
         rec("gelu", h)
+        if fold:
+            h = self.unfold_halves(h, sh.n_ffn)
         f = self.project(h, LT_2)
         for c in range(sh.n_hid):
             f[c].scale = y_res[c].scale

@@ -1,11 +1,11 @@
 """Encrypted BERT encoder layer on the GPU against the oracle (oracle/bert.py),
 word for word, at the reduced size of tests/golden/bert_digests.json (N = 2^13,
-hidden 64, 2 heads, FFN 128, requests of 16 | 4 + 8 tokens in two lanes):
-the Q/K/V projections, their bootstrap, the attention block and the whole
-layer in its single-lane and lockstep forms (two ciphertexts per bootstrap,
-the default), with keys and encryptions made from the same SEAL seed; plus
-the decrypted output against the FP64 layer with NEXUS's approximations, in
-both bootstrap forms."""
+128 token slots per block, hidden 64, 2 heads, FFN 160, requests of 16 | 4 + 8
+tokens in two lanes): the Q/K/V projections, their bootstrap, the attention
+block and the whole layer in its single-lane and lockstep forms (two
+ciphertexts per bootstrap and the FFN fold, the defaults), with keys and
+encryptions made from the same SEAL seed; plus the decrypted output against
+the FP64 layer with NEXUS's approximations, with and without the packing."""
 import hashlib
 import json
 from pathlib import Path
@@ -29,7 +29,7 @@ def _shape():
     c = DOC
     return NB.BertShape(hidden=c["hidden"], heads=c["heads"], head_dim=c["head_dim"], ffn=c["ffn"], T=c["T"],
                         lanes=[[tuple(r) for r in lane] for lane in c["lanes"]], boot_shrink=c["boot_shrink"],
-                        boot_pack=c["boot_pack"])
+                        boot_pack=c["boot_pack"], ffn_fold=c["ffn_fold"])
 
 
 @pytest.fixture(scope="module")
@@ -123,18 +123,22 @@ def test_layer_matches_oracle(env, lockstep):
         assert err < 2.0 ** -7, err
 
 
-def test_unpacked_bootstraps_keep_the_layer_within_its_error(env):
-    """With one ciphertext per bootstrap (boot_pack off) the layer's lockstep
-    and single-lane forms agree word for word, and the decrypted output stays
-    within the packed layer's error bound against the FP64 layer."""
+@pytest.mark.parametrize("pack,fold", [(False, False), (True, False), (False, True)])
+def test_other_packings_keep_the_layer_within_its_error(env, pack, fold):
+    """With one ciphertext per bootstrap (boot_pack off), the FFN unfolded
+    (ffn_fold off), or both (the plain form), the layer's lockstep and
+    single-lane forms agree word for word, and the decrypted output stays
+    within the default layer's error bound against the FP64 layer."""
     from nexus_gb300 import bert as NB
     layer, ctx, sh, n = env["layer"], env["ctx"], env["sh"], env["n"]
-    layer.set_boot_pack(False)
+    layer.set_boot_pack(pack)
+    layer.set_ffn_fold(fold)
     try:
         lock = layer.forward(env["x"], True)
         single = layer.forward(env["x"], False)
     finally:
         layer.set_boot_pack(True)
+        layer.set_ffn_fold(True)
     for a, b in zip(lock, single):
         assert np.array_equal(a.to_numpy(), b.to_numpy())
     for lane in range(layer.n_lanes):

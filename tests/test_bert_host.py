@@ -78,3 +78,75 @@ def test_layer_abi_rejects_null_arguments_without_gpu():
     assert lib.nexus_bert_layer_stage(None, 1, 0, 0, None, 0, None, 0) != 0
     n = ctypes.c_int()
     assert lib.nexus_bert_layer_rotation_steps(None, None, ctypes.byref(n), 0) != 0
+
+
+class _Slots:
+    """A plaintext stand-in for the oracle's ciphertexts: slot values only."""
+
+    def __init__(self, v, limbs=3, scale=1.0):
+        self.v, self.limbs, self.scale = np.asarray(v, dtype=float), limbs, scale
+
+
+class _SlotEvaluator:
+    """The oracle evaluator's interface over slot vectors: rotate(x, k) moves
+    slot i + k to slot i (CKKS rotate_vector), rescale drops a limb."""
+
+    q = [2.0 ** 40] * 8
+
+    def rotate(self, x, k):
+        return _Slots(np.roll(x.v, -k), x.limbs, x.scale)
+
+    def add(self, a, b):
+        return _Slots(a.v + b.v, a.limbs, a.scale)
+
+    def add_plain(self, a, p):
+        return _Slots(a.v + p, a.limbs, a.scale)
+
+    def multiply_plain(self, a, p):
+        return _Slots(a.v * p, a.limbs, a.scale)
+
+    def encode(self, v, scale, limbs):
+        return np.asarray(v, dtype=float)
+
+    def rescale(self, a):
+        return _Slots(a.v, a.limbs - 1, a.scale)
+
+
+def test_ffn_fold_slot_algebra():
+    """The fold of BertLayerT (restated in oracle/bert.py): FFN1 on the lower
+    half, h_2i + rot(h_2i+1, -T/2), an element-wise function, the unfold
+    (2i+1 = rot(folded, T/2)) and FFN2 give the unfolded FFN's values on every
+    lower-half token slot, which hold the numpy FFN of each token."""
+    from oracle import bert as OB
+    S, T, hidden, ffn = 256, 16, 16, 40
+    lanes = [[(0, 4)], [(0, 2), (4, 3)]]
+    osh = OB.Shape(S, hidden, 2, 8, ffn, T, lanes, 1.0)
+    assert osh.fold_ok and osh.n_ffn == 3 and osh.n_hid == 1
+    assert (T // 2) in osh.rotation_steps() and (S - T // 2) in osh.rotation_steps()
+    rng = np.random.default_rng(5)
+    w = {k: rng.normal(0, 0.5, s) for k, s in (("w1", (hidden, ffn)), ("w2", (ffn, hidden)), ("b1", ffn),
+                                                ("b2", hidden))}
+    layer = OB.BertLayer.__new__(OB.BertLayer)
+    layer.ev, layer.sh, layer.w, layer.delta = _SlotEvaluator(), osh, w, 1.0
+    X = rng.normal(size=(T, hidden))              # token slot t of every block holds token t
+    x = [_Slots(np.concatenate([X[:, c * osh.NB + j] if c * osh.NB + j < hidden else np.zeros(T)
+                                for j in range(osh.NB)])) for c in range(osh.n_hid)]
+
+    def act(cts):
+        return [_Slots(np.tanh(c.v), c.limbs, c.scale) for c in cts]
+
+    plain = layer.project(act(layer.project(x, OB.LT_1)), OB.LT_2)
+    folded_h = layer.fold_halves(layer.project(x, OB.LT_1, lower_half=True))
+    assert len(folded_h) == 2
+    folded = layer.project(layer.unfold_halves(act(folded_h), osh.n_ffn), OB.LT_2)
+    want = np.tanh(X @ w["w1"] + w["b1"]) @ w["w2"] + w["b2"]          # [T][hidden]
+    for c in range(osh.n_hid):
+        for j in range(osh.NB):
+            f = c * osh.NB + j
+            if f >= hidden:
+                continue
+            blk = slice(j * T, (j + 1) * T)
+            assert np.allclose(plain[c].v[blk], want[:, f])
+            assert np.allclose(folded[c].v[blk][:T // 2], want[:T // 2, f])
+    # requests reaching into the upper half turn the fold off
+    assert not OB.Shape(S, hidden, 2, 8, ffn, T, [[(0, 9)]], 1.0).fold_ok
