@@ -926,20 +926,20 @@ BERT_SEED = 600
 
 
 def bert_bootstraps(pack: bool = True, fold: bool = True) -> int:
-    """Bootstraps per layer: Q/K 32 ciphertexts (V is projected at the
-    attention's level and not refreshed), the softmax row sums 2 (one per
-    lane, refreshed alone), the residuals 12 + 12 and the FFN hidden
-    activations 48 (24 folded two per ciphertext); two ciphertexts per
-    bootstrap with pack: 16 + 2 + 6 + 6 + 24 (12 folded)."""
-    ffn = 24 if fold else 48
-    return (32 + 24 + ffn) // 2 + 2 if pack else 32 + 2 + 24 + ffn
+    """Bootstraps per layer: Q and K 32 ciphertexts (24 with Q folded two per
+    ciphertext; V is projected at the attention's level and not refreshed),
+    the softmax row sums 2 (one per lane, refreshed alone), the residuals
+    12 + 12 and the FFN hidden activations 48 (24 folded); two ciphertexts
+    per bootstrap with pack: 12 + 2 + 6 + 6 + 12 = 38 folded, 54 not."""
+    qk, ffn = (24, 24) if fold else (32, 48)
+    return (qk + 24 + ffn) // 2 + 2 if pack else qk + 2 + 24 + ffn
 
 
 def bert_config(pack: bool = True, shrink: float = 1.0, fold: bool = True):
     return {"workload": "bert_base_layer_n65536", "N": 1 << BERT_LOGN, "hidden": 768, "heads": 12, "ffn": 3072,
             "requests": [128, 32, 64], "lanes": "[128] | [32 + 64]", "token_slots_per_block": 256,
             "moduli_bits": "51 + 19x46 + 14x51 + special 51", "hamming_weight": 192, "scale": "2^46",
-            "boot_shrink": shrink, "rowsum_shrink": 2, "boot_pack": bool(pack), "ffn_fold": bool(fold),
+            "boot_shrink": shrink, "rowsum_shrink": 2, "boot_pack": bool(pack), "token_fold": bool(fold),
             "bootstraps_per_layer": bert_bootstraps(pack, fold),
             "weights": "N(0, 0.02)", "tokens": "N(0, 1)", "parallelism": "replicas",
             "l2": "keys (~110 GB), encoded weights (~60 GB) and activations far above L2, no flush"}
@@ -980,7 +980,7 @@ def run_bert_gpu(args, rank, world):
     bs.generate_LT_coefficient_3()
     layer = NB.BertLayer(bs, shape, w)
     layer.set_boot_pack(bool(args.bert_pack))
-    layer.set_ffn_fold(bool(args.bert_fold))
+    layer.set_token_fold(bool(args.bert_fold))
     tuning = ctx.autotune(20, 16)
     tuning["ntt_form"] = _apply_ntt_form(ctx, args)
     all_steps = steps + [s for s in layer.rotation_steps() if s not in steps]
@@ -1142,12 +1142,16 @@ def run_bert_gpu(args, rank, world):
     same = all(np.array_equal(a, b) for a, b in zip(words(res[:layer.n_hid]), lock_words))
     del res
     # the plain single-ciphertext form: each lane on its own, one ciphertext
-    # per operation and one per bootstrap, the FFN unfolded
+    # per operation and one per bootstrap, nothing folded
     plain_err = None
     if args.bert_pack or args.bert_fold:
         layer.set_boot_pack(False)
-        layer.set_ffn_fold(False)
-        res = layer.forward(x, lockstep=False)   # warm: the unpacked bootstraps' and unfolded FFN1's encodings
+        layer.set_token_fold(False)
+        # the unpacked bootstraps and the unmasked maps add encodings of their
+        # own: hand the pool's cached free blocks back first
+        torch.cuda.empty_cache()
+        ng.memory_trim()
+        res = layer.forward(x, lockstep=False)   # warm: the unpacked bootstraps' and unmasked maps' encodings
         del res
         torch.cuda.synchronize(dev)
         p0.record(stream)
@@ -1156,7 +1160,7 @@ def run_bert_gpu(args, rank, world):
         torch.cuda.synchronize(dev)
         plain_ms = p0.elapsed_time(p1)
         layer.set_boot_pack(bool(args.bert_pack))
-        layer.set_ffn_fold(bool(args.bert_fold))
+        layer.set_token_fold(bool(args.bert_fold))
         errs_plain = []
         for lane in range(layer.n_lanes):
             cts = res[lane * layer.n_hid:(lane + 1) * layer.n_hid]
@@ -1195,6 +1199,7 @@ def run_bert_gpu(args, rank, world):
     step_ms = total_ms / args.steps
     free_b, total_b = torch.cuda.mem_get_info(dev)
     mem_used = total_b - free_b
+    mem = ng.memory_info()
     peak, peak_kind = _peak_hbm()
     ntt_avg_ms = ntt_ms / max(1, ntt_calls)
     alg_bytes_per_call = 16.0 * n * ntt_limbs / max(1, ntt_calls)
@@ -1236,17 +1241,25 @@ def run_bert_gpu(args, rank, world):
                 "d2h_bytes_per_step": out_bytes, "words_equal_direct": bool(e2e_same)},
         "plain_single_ct_form": {"value": plain_ms / 1e3, "unit": "s per layer",
                                  "what": "each lane on its own, one ciphertext per operation and per bootstrap, "
-                                         "the FFN unfolded",
+                                         "nothing folded",
                                  "lockstep_speedup": plain_ms / step_ms,
                                  "max_abs_err_vs_fp64_same_approx": plain_err},
         "lanes_one_by_one_form": {"value": lanes_ms / 1e3, "unit": "s per layer",
                                   "what": "each lane on its own, one ciphertext per operation, bootstraps as in "
-                                          "the lockstep form (two ciphertexts each when boot_pack), the FFN "
-                                          "folded as in it",
+                                          "the lockstep form (two ciphertexts each when boot_pack), Q and the "
+                                          "FFN folded as in it",
                                   "lockstep_speedup": lanes_ms / step_ms, "words_equal_lockstep": bool(same)},
         "blocks_ms": {"lockstep": blocks_lock, "lanes_one_by_one": blocks_plain},
         "setup": {"first_call_s": setup_s, "galois_keys": len(all_steps),
-                  "cached_plaintexts": layer.cached_plaintexts(), "device_memory_in_use_gb": mem_used / 1e9},
+                  "cached_plaintexts": layer.cached_plaintexts(),
+                  "device_memory_gb": {"engine_live": mem["pool_used"] / 1e9,
+                                       "engine_peak": mem["pool_used_high"] / 1e9,
+                                       "engine_pool_held": mem["pool_reserved"] / 1e9,
+                                       "graph_held": mem["graph_reserved"] / 1e9,
+                                       "process_held": mem_used / 1e9,
+                                       "note": "live and peak: the engine's allocations outside graphs; pool "
+                                               "held: also the freed blocks its pool keeps for reuse; graph held: "
+                                               "the captured layer's temporaries, kept between launches"}},
         "clocks": clk.summary(),
         "gpu_launches": launches,
         "cpu_baseline": cpu_bert_sample(os.cpu_count() or 1, bool(args.bert_pack), bool(args.bert_fold))
@@ -1260,7 +1273,7 @@ def run_bert_gpu(args, rank, world):
 def cpu_bert_sample(threads: int, pack: bool = True, fold: bool = True):
     """A lower bound of the layer on the oracle port: one full bootstrap on the
     layer's chain, timed, times the layer's bootstraps (bert_bootstraps:
-    42 with two ciphertexts per bootstrap and the FFN folded; projections,
+    38 with two ciphertexts per bootstrap and the token fold; projections,
     attention, GELU, LayerNorm and the packing's conjugations left out)."""
     cb = CpuBootstrap(threads, BERT_BITS)
     t = cb.bootstrap()
@@ -1835,7 +1848,7 @@ def main():
     ap.add_argument("--bert-pack", type=int, choices=[0, 1], default=1,
                     help="BERT layer: refresh two ciphertexts per bootstrap (c0 + i c1; 0: one each)")
     ap.add_argument("--bert-fold", type=int, choices=[0, 1], default=1,
-                    help="BERT layer: FFN hidden activations of two ciphertexts folded into one (0: unfolded)")
+                    help="BERT layer: Q and the FFN hidden activations folded two ciphertexts in one (0: unfolded)")
     ap.add_argument("--ntt-cts", type=int, default=64,
                     help="ciphertexts per step (smaller values are for profiling captures only)")
     args = ap.parse_args()

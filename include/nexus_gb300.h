@@ -31,6 +31,21 @@ const char *nexus_last_error(void);
  * the reference. */
 uint64_t nexus_kernel_launches(void);
 
+/* Device memory of the current device's stream-ordered pool, which every
+ * engine buffer (keys, plaintexts, ciphertexts, temporaries) comes from
+ * outside CUDA graphs: bytes in live allocations now, their peak since the
+ * process started, and bytes the pool holds (freed blocks stay in the pool
+ * for reuse; its release threshold is set to the maximum); and the bytes the
+ * device holds for the allocations of instantiated graphs (a graph keeps
+ * the memory of its temporaries between launches).  Any pointer may be
+ * NULL.  No counterpart in the reference. */
+int nexus_memory_info(uint64_t *pool_used, uint64_t *pool_used_high, uint64_t *pool_reserved,
+                      uint64_t *graph_reserved);
+/* Return the pool's free blocks, and graph memory no instantiated graph
+ * uses, to the device (cudaMemPoolTrimTo(pool, 0), cudaDeviceGraphMemTrim);
+ * live allocations are untouched.  No counterpart in the reference. */
+int nexus_memory_trim(void);
+
 /*
  * Primes for a coefficient modulus: out[i] is a prime of bit_sizes[i] bits,
  * congruent to 1 mod 2*poly_degree, chosen exactly as SEAL chooses them.
@@ -694,12 +709,19 @@ int nexus_bert_layer_forward(nexus_bert_layer *layer, int lockstep, nexus_cipher
                              nexus_ciphertext *const *out);
 /* One stage of the layer on lane-major ciphertexts, for stage-wise checking:
  * PROJECT linear map `which` (0 Q, 1 K, 2 V, 3 output, 4 W1, 5 W2) plus its
- * bias; ATTENTION q, k, v (head layout, in that order) -> the attention
- * output; LAYER_NORM and BOOTSTRAP return their inputs transformed. */
+ * bias, written on token slots [0, T/2) only when `which` also carries
+ * NEXUS_BERT_LOWER_HALF; ATTENTION q, k, v (head layout, in that order) ->
+ * the attention output; LAYER_NORM and BOOTSTRAP return their inputs
+ * transformed; FOLD maps count_in ciphertexts to (count_in + 1) / 2 (2i and
+ * 2i+1 -> x_2i + rot(x_2i+1, -T/2)), UNFOLD maps (count_out + 1) / 2 back to
+ * count_out (2i -> x_i, 2i+1 -> rot(x_i, T/2)); see set_token_fold. */
 #define NEXUS_BERT_PROJECT 0
 #define NEXUS_BERT_ATTENTION 1
 #define NEXUS_BERT_LAYER_NORM 2
 #define NEXUS_BERT_BOOTSTRAP 3
+#define NEXUS_BERT_FOLD 4
+#define NEXUS_BERT_UNFOLD 5
+#define NEXUS_BERT_LOWER_HALF 16
 int nexus_bert_layer_stage(nexus_bert_layer *layer, int lockstep, int stage, int which, nexus_ciphertext *const *in,
                            int count_in, nexus_ciphertext *const *out, int count_out);
 /* With timing on, forward records a CUDA event after each of its blocks;
@@ -714,16 +736,17 @@ int nexus_bert_layer_set_timing(nexus_bert_layer *layer, int enable);
  * pair, the same error per output.  On by default; no counterpart in the
  * reference (NEXUS has no layer). */
 int nexus_bert_layer_set_boot_pack(nexus_bert_layer *layer, int enable);
-/* With ffn_fold on, and when every request's tokens lie in token slots
- * [0, T/2) and the FFN takes two or more ciphertexts, the FFN hidden
- * activations of ciphertexts 2i and 2i+1 share one ciphertext, the second's
- * tokens in the upper half of every token block: W1 writes the lower half
- * only, its outputs are folded by one rotation of -T/2, refreshed and passed
- * through GELU, and W2 reads ciphertext 2i+1 as the folded one rotated by
- * T/2.  Half the FFN bootstraps and GELUs; the rotation steps include +-T/2
- * whenever the fold applies.  On by default; no counterpart in the
- * reference (NEXUS has no layer). */
-int nexus_bert_layer_set_ffn_fold(nexus_bert_layer *layer, int enable);
+/* With token_fold on, and when every request's tokens lie in token slots
+ * [0, T/2), Q and the FFN hidden activations go through their bootstraps
+ * (and the FFN through GELU) two ciphertexts in one, the second's tokens in
+ * the upper half of every token block: the Q and W1 maps write the lower
+ * half only, their outputs are folded by one rotation of -T/2 and unfolded
+ * afterwards (ciphertext 2i+1 is the folded one rotated by T/2; Q at the
+ * attention's level).  A quarter fewer Q/K bootstraps, half the FFN
+ * bootstraps and GELUs; the rotation steps include +-T/2 whenever the fold
+ * applies.  On by default; no counterpart in the reference (NEXUS has no
+ * layer). */
+int nexus_bert_layer_set_token_fold(nexus_bert_layer *layer, int enable);
 int nexus_bert_layer_stage_times(nexus_bert_layer *layer, int lockstep, int lane, double *ms, char *names,
                                  size_t names_capacity, int *count, int capacity);
 

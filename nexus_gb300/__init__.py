@@ -7,5 +7,6 @@ ctypes layer used by the tests and the benchmark.
 """
 from ._lib import NexusError, check, lib  # noqa: F401
 from .context import (SEAL_CBD, SEAL_SPARSE_TERNARY, SEAL_TERNARY, SEAL_UNIFORM, Context,  # noqa: F401
-                      butterfly_rate, create_coeff_modulus, kernel_launches, seal_prng_bytes, seal_sample_poly, seal_seed,
+                      butterfly_rate, create_coeff_modulus, kernel_launches, memory_info, memory_trim, seal_prng_bytes,
+                      seal_sample_poly, seal_seed,
                       TENSOR_BF16, TENSOR_E4M3, tensor_rate, tensor_tile)

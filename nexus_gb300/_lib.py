@@ -17,6 +17,8 @@ u64p = C.POINTER(C.c_uint64)
 SIGNATURES = [
     ("nexus_last_error", C.c_char_p, []),
     ("nexus_kernel_launches", C.c_uint64, []),
+    ("nexus_memory_info", C.c_int, [C.POINTER(C.c_uint64)] * 4),
+    ("nexus_memory_trim", C.c_int, []),
     ("nexus_create_coeff_modulus", C.c_int, [C.c_uint64, C.POINTER(C.c_int), C.c_int, u64p]),
     ("nexus_context_create", C.c_int, [C.c_int, u64p, C.c_int, C.POINTER(C.c_void_p)]),
     ("nexus_context_destroy", C.c_int, [C.c_void_p]),
@@ -144,7 +146,7 @@ SIGNATURES = [
      [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     ("nexus_bert_layer_set_timing", C.c_int, [C.c_void_p, C.c_int]),
     ("nexus_bert_layer_set_boot_pack", C.c_int, [C.c_void_p, C.c_int]),
-    ("nexus_bert_layer_set_ffn_fold", C.c_int, [C.c_void_p, C.c_int]),
+    ("nexus_bert_layer_set_token_fold", C.c_int, [C.c_void_p, C.c_int]),
     ("nexus_bert_layer_stage_times", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_char_p,
                                                C.c_size_t, C.POINTER(C.c_int), C.c_int]),
 ]

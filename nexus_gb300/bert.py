@@ -36,9 +36,10 @@ class BertShape:
     boot_shrink: float = 1.0
     # two ciphertexts per bootstrap (c0 + i c1, separated by a conjugation)
     boot_pack: bool = True
-    # the FFN hidden activations of two ciphertexts in one (the halves of
-    # each token block), when every request's tokens lie in [0, T/2)
-    ffn_fold: bool = True
+    # Q and the FFN hidden activations two ciphertexts in one through their
+    # bootstraps (the halves of each token block), when every request's
+    # tokens lie in [0, T/2)
+    token_fold: bool = True
 
     def blocks(self, slots: int) -> int:
         return slots // self.T
@@ -226,7 +227,7 @@ class BertLayer:
               "nexus_bert_layer_info")
         self.n_lanes, self.n_hid, self.n_head, self.n_ffn = [i.value for i in info]
         self.set_boot_pack(shape.boot_pack)
-        self.set_ffn_fold(shape.ffn_fold)
+        self.set_token_fold(shape.token_fold)
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -253,9 +254,10 @@ class BertLayer:
         """Two ciphertexts per bootstrap (nexus_bert_layer_set_boot_pack)."""
         check(lib().nexus_bert_layer_set_boot_pack(self._h, 1 if enable else 0), "nexus_bert_layer_set_boot_pack")
 
-    def set_ffn_fold(self, enable: bool) -> None:
-        """Two FFN hidden ciphertexts folded into one (nexus_bert_layer_set_ffn_fold)."""
-        check(lib().nexus_bert_layer_set_ffn_fold(self._h, 1 if enable else 0), "nexus_bert_layer_set_ffn_fold")
+    def set_token_fold(self, enable: bool) -> None:
+        """Q and the FFN hidden activations folded two ciphertexts in one
+        (nexus_bert_layer_set_token_fold)."""
+        check(lib().nexus_bert_layer_set_token_fold(self._h, 1 if enable else 0), "nexus_bert_layer_set_token_fold")
 
     def stage_times(self, lockstep: bool = True, lane: int = 0) -> dict:
         """Device ms of each block of the last forward with timing on."""
@@ -289,4 +291,6 @@ class BertLayer:
         return out
 
 
-BERT_PROJECT, BERT_ATTENTION, BERT_LAYER_NORM, BERT_BOOTSTRAP = 0, 1, 2, 3
+BERT_PROJECT, BERT_ATTENTION, BERT_LAYER_NORM, BERT_BOOTSTRAP, BERT_FOLD, BERT_UNFOLD = 0, 1, 2, 3, 4, 5
+# OR-ed into a BERT_PROJECT map: written on the lower half of each token block only
+BERT_LOWER_HALF = 16

@@ -317,6 +317,21 @@ def kernel_launches() -> int:
     return int(lib().nexus_kernel_launches())
 
 
+def memory_info() -> dict:
+    """Bytes of the engine's device memory pool (nexus_memory_info): live
+    allocations now, their peak, what the pool holds, and what instantiated
+    graphs hold for their allocations."""
+    v = [C.c_uint64() for _ in range(4)]
+    check(lib().nexus_memory_info(*[C.byref(x) for x in v]), "nexus_memory_info")
+    return {"pool_used": v[0].value, "pool_used_high": v[1].value, "pool_reserved": v[2].value,
+            "graph_reserved": v[3].value}
+
+
+def memory_trim() -> None:
+    """Return the engine pool's free blocks to the device (nexus_memory_trim)."""
+    check(lib().nexus_memory_trim(), "nexus_memory_trim")
+
+
 def butterfly_rate(mode: int, q: int, rounds: int = 512, blocks_per_sm: int = 3) -> float:
     """Butterflies per second of the NTT's own butterfly on this GPU (mode 0
     forward, 1 forward for primes below 2^52, 2 inverse): the compute ceiling

@@ -148,7 +148,7 @@ void BertShape::derive(size_t slots)
     G = (int)std::ceil(std::sqrt((double)Lmax));
     Glt = (int)std::ceil(std::sqrt((double)NB));
     if (!(boot_shrink >= 1.0)) throw std::invalid_argument("boot_shrink must be >= 1");
-    fold_ok = n_ffn >= 2;
+    fold_ok = true;
     for (auto &lane : lanes)
         for (auto &q : lane)
             if (q.first + q.second > T / 2) fold_ok = false;
@@ -522,7 +522,8 @@ template <class EV, class CT>
 void BertLayerT<EV, CT>::unfold_halves(std::vector<CT> &x, int count)
 {
     EV &ev = *ev_;
-    if ((int)x.size() != (count + 1) / 2) throw std::logic_error("unfold_halves: wrong number of ciphertexts");
+    if (count < 1 || (int)x.size() != (count + 1) / 2)
+        throw std::invalid_argument("unfold_halves: wrong number of ciphertexts");
     std::vector<CT> out(count);
     for (int i = 0; i < count; ++i) {
         if (i % 2) ev.rotate_vector(x[i / 2], sh_.T / 2, out[i]);
@@ -588,8 +589,8 @@ void BertLayerT<EV, CT>::attention(std::vector<CT> &q, std::vector<CT> &k, std::
     const int nh = sh_.n_head, G = sh_.G, L = sh_.Lmax, S = sh_.S;
     // levels, counted back from the output projection (2 limbs): PV 1,
     // P = E * I 1, exp 8 (constant + 7 squarings), mask 1, Q.K 1
-    const int e_limbs = 4, qk_limbs = e_limbs + 10, v_limbs = e_limbs - 1;
-    static_assert(kVInLimbs - 1 == 3, "the V projection lands at the attention's V level");
+    const int e_limbs = 4, qk_limbs = kQKLimbs, v_limbs = e_limbs - 1;
+    static_assert(kVInLimbs - 1 == 3 && kQKLimbs == 14, "the levels the projections and bootstraps leave");
     for (auto &c : q) ev.mod_switch_to_inplace(c, qk_limbs);
     for (auto &c : k) ev.mod_switch_to_inplace(c, qk_limbs);
     for (auto &c : v) ev.mod_switch_to_inplace(c, v_limbs);
@@ -791,20 +792,26 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
     std::vector<CT> x2 = x_in, x4 = x_in;
     for (auto &c : x2) ev.mod_switch_to_inplace(c, 2);
     for (auto &c : x4) ev.mod_switch_to_inplace(c, kVInLimbs);
+    const bool fold = sh_.folding();
     std::vector<CT> q, k, v;
-    project(x2, LT_Q, q);
+    project(x2, LT_Q, q, fold);
     project(x2, LT_K, k);
     project(x4, LT_V, v);
     mark("qkv projections");
     {
+        // Q folded two per ciphertext through the bootstrap (bert.h), unfolded
+        // at the attention's level
+        if (fold) fold_halves(q);
+        const size_t nq = q.size();
         std::vector<CT> all;
         for (auto *t : {&q, &k})
             for (auto &c : *t) all.push_back(std::move(c));
         bootstrap_all(all);
-        const int nh = sh_.n_head;
-        for (int i = 0; i < nh; ++i) {
-            q[i] = std::move(all[i]);
-            k[i] = std::move(all[nh + i]);
+        for (size_t i = 0; i < nq; ++i) q[i] = std::move(all[i]);
+        for (size_t i = 0; i < k.size(); ++i) k[i] = std::move(all[nq + i]);
+        if (fold) {
+            for (auto &c : q) ev.mod_switch_to_inplace(c, kQKLimbs);
+            unfold_halves(q, sh_.n_head);
         }
     }
     mark("qk bootstraps");
@@ -828,7 +835,6 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
     for (auto &c : y_res) ev.mod_switch_to_inplace(c, 1);
     for (auto &c : a) ev.mod_switch_to_inplace(c, 2);
     std::vector<CT> h, f;
-    const bool fold = sh_.folding();
     project(a, LT_1, h, fold);
     if (fold) fold_halves(h);
     mark("ffn1 projection");

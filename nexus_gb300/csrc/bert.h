@@ -56,17 +56,20 @@
 // conjugation).  The words EvalMod sees are the two messages' sum, and the
 // error of each output is that of an unpacked bootstrap.
 //
-// With ffn_fold, the FFN hidden activations take half the ciphertexts.  Past
-// the attention only the first token copies matter and every op but the
-// linear maps' block rotations acts on one token slot; when every request's
-// tokens lie in the lower half of the token block ([0, T/2)), FFN1 writes
-// only that half (its diagonals and bias are zero on the upper half), and
-// ciphertexts 2i and 2i+1 of its output become one: h_2i + rot(h_2i+1, -T/2)
-// holds the second's tokens in the upper half of every block.  Those are
-// refreshed and passed through GELU, and FFN2 reads ciphertext 2i as the
-// folded one itself and 2i+1 as its rotation by T/2 (each token slot of the
-// lower half then holds the right feature; the upper half, not read for the
-// first copies, holds other tokens' values of the same magnitude).
+// With token_fold, Q and the FFN hidden activations take half the
+// ciphertexts through their bootstraps.  Only the first token copies of Q
+// are read (the scores' mask zeroes every other slot), and past the
+// attention only the first copies matter at all, while every op but the
+// linear maps' block rotations acts on one token slot.  So when every
+// request's tokens lie in the lower half of the token block ([0, T/2)), the
+// Q and FFN1 maps write only that half (their diagonals and biases are zero
+// on the upper half), and ciphertexts 2i and 2i+1 of their outputs become
+// one: y_2i + rot(y_2i+1, -T/2) holds the second's tokens in the upper half
+// of every block.  Those are refreshed (and, for the FFN, passed through
+// GELU); then ciphertext 2i is the folded one itself and 2i+1 its rotation
+// by T/2 (each token slot of the lower half holds the right feature; the
+// upper half, never read for a first copy, holds other tokens' values of the
+// same magnitude).
 #pragma once
 #include <cstdint>
 #include <map>
@@ -86,6 +89,9 @@ namespace nexus {
 // the level the V projection reads its input at: its output (one level
 // lower) is the level the attention's P.V products take V at
 constexpr int kVInLimbs = 4;
+// the level the attention takes Q and K at (scores 1, mask 1, exp 8, P 1,
+// P.V 1, above the output projection's 2 limbs)
+constexpr int kQKLimbs = 14;
 
 struct BertShape {
     int hidden = 768, heads = 12, head_dim = 64, ffn = 3072;
@@ -99,16 +105,17 @@ struct BertShape {
     // refresh two ciphertexts with one bootstrap (c0 + i c1, separated by a
     // conjugation afterwards)
     bool boot_pack = true;
-    // fold two FFN hidden ciphertexts into one (the halves of each token
-    // block) when the requests allow it (fold_ok)
-    bool ffn_fold = true;
+    // fold two Q, and two FFN hidden, ciphertexts into one through their
+    // bootstraps (the halves of each token block) when the requests allow
+    // it (fold_ok)
+    bool token_fold = true;
 
     // derived by derive()
     int S = 0, NB = 0, H2 = 0, KB = 0, n_head = 0, n_hid = 0, n_ffn = 0, Lmax = 0, G = 0, Glt = 0;
-    // every request's tokens in [0, T/2) and at least two FFN ciphertexts
+    // every request's tokens in [0, T/2)
     bool fold_ok = false;
     void derive(size_t slots);
-    bool folding() const { return ffn_fold && fold_ok; }
+    bool folding() const { return token_fold && fold_ok; }
     // every rotation step the layer uses (the bootstrapper's are separate)
     std::vector<int> rotation_steps() const;
 };
@@ -148,6 +155,9 @@ public:
     void attention(std::vector<CT> &q, std::vector<CT> &k, std::vector<CT> &v, std::vector<CT> &o);
     void layer_norm(std::vector<CT> &x);
     void bootstrap_all(std::vector<CT> &cts);
+    // ciphertexts 2i, 2i+1 (lower-half layout) -> one; and back to `count`
+    void fold_halves(std::vector<CT> &x);
+    void unfold_halves(std::vector<CT> &x, int count);
 
     ~BertLayerT();
     BertLayerT(const BertLayerT &) = delete;
@@ -163,7 +173,7 @@ public:
     size_t cached_plaintexts() const { return pt_->count(); }
     const BertShape &shape() const { return sh_; }
     void set_boot_pack(bool on) { sh_.boot_pack = on; }
-    void set_ffn_fold(bool on) { sh_.ffn_fold = on; }
+    void set_token_fold(bool on) { sh_.token_fold = on; }
 
 private:
     int in_count(int which) const;
@@ -180,9 +190,6 @@ private:
     const Plaintext &diag(int which, int a, int b, int d, int limbs, double scale, bool lower_half);
     void encode_diagonals(int which, int limbs, double scale, bool lower_half);
     const Plaintext &bias_plain(int which, int ct, int limbs, double scale, bool lower_half);
-    // ciphertexts 2i, 2i+1 (lower-half layout) -> one; and back to `count`
-    void fold_halves(std::vector<CT> &x);
-    void unfold_halves(std::vector<CT> &x, int count);
     void masks(int delta, int kind, int limbs, double scale, std::vector<const Plaintext *> &out);
     void shrink_for_bootstrap(std::vector<CT> &cts);
     void begin_marks();

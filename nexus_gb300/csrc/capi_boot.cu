@@ -623,14 +623,39 @@ extern "C" int nexus_bert_layer_stage(nexus_bert_layer *layer, int lockstep, int
         const BertShape &sh = layer->shape;
         switch (stage) {
         case NEXUS_BERT_PROJECT: {
-            if (which < 0 || which > 5) throw std::invalid_argument("unknown linear map");
-            const int n_in = which == 3 ? sh.n_head : which == 5 ? sh.n_ffn : sh.n_hid;
-            const int n_out = which <= 2 ? sh.n_head : which == 4 ? sh.n_ffn : sh.n_hid;
+            const bool lower = (which & NEXUS_BERT_LOWER_HALF) != 0;
+            const int map = which & ~NEXUS_BERT_LOWER_HALF;
+            if (map < 0 || map > 5) throw std::invalid_argument("unknown linear map");
+            const int n_in = map == 3 ? sh.n_head : map == 5 ? sh.n_ffn : sh.n_hid;
+            const int n_out = map <= 2 ? sh.n_head : map == 4 ? sh.n_ffn : sh.n_hid;
             if (count_in != n_in || count_out != n_out) throw std::invalid_argument("wrong ciphertext count");
             bert_run(
                 layer, lockstep, in, n_in, out, n_out,
-                [&](BertLayer &L, std::vector<Ciphertext> &a, std::vector<Ciphertext> &b) { L.project(a, which, b); },
-                [&](BatchBertLayer &L, std::vector<CtBatch> &a, std::vector<CtBatch> &b) { L.project(a, which, b); });
+                [&](BertLayer &L, std::vector<Ciphertext> &a, std::vector<Ciphertext> &b) {
+                    L.project(a, map, b, lower);
+                },
+                [&](BatchBertLayer &L, std::vector<CtBatch> &a, std::vector<CtBatch> &b) {
+                    L.project(a, map, b, lower);
+                });
+            break;
+        }
+        case NEXUS_BERT_FOLD:
+        case NEXUS_BERT_UNFOLD: {
+            const bool fold = stage == NEXUS_BERT_FOLD;
+            const int halves = fold ? count_in : count_out, folded = fold ? count_out : count_in;
+            if (halves < 1 || folded != (halves + 1) / 2) throw std::invalid_argument("wrong ciphertext count");
+            bert_run(
+                layer, lockstep, in, count_in, out, count_out,
+                [&](BertLayer &L, std::vector<Ciphertext> &a, std::vector<Ciphertext> &b) {
+                    if (fold) L.fold_halves(a);
+                    else L.unfold_halves(a, count_out);
+                    b = std::move(a);
+                },
+                [&](BatchBertLayer &L, std::vector<CtBatch> &a, std::vector<CtBatch> &b) {
+                    if (fold) L.fold_halves(a);
+                    else L.unfold_halves(a, count_out);
+                    b = std::move(a);
+                });
             break;
         }
         case NEXUS_BERT_ATTENTION: {
@@ -699,12 +724,12 @@ extern "C" int nexus_bert_layer_set_boot_pack(nexus_bert_layer *layer, int enabl
     return 0;
 }
 
-extern "C" int nexus_bert_layer_set_ffn_fold(nexus_bert_layer *layer, int enable)
+extern "C" int nexus_bert_layer_set_token_fold(nexus_bert_layer *layer, int enable)
 {
-    if (!layer) return fail("nexus_bert_layer_set_ffn_fold", "null argument");
-    layer->shape.ffn_fold = enable != 0;
-    for (auto &l : layer->single) l->set_ffn_fold(enable != 0);
-    if (layer->lockstep) layer->lockstep->set_ffn_fold(enable != 0);
+    if (!layer) return fail("nexus_bert_layer_set_token_fold", "null argument");
+    layer->shape.token_fold = enable != 0;
+    for (auto &l : layer->single) l->set_token_fold(enable != 0);
+    if (layer->lockstep) layer->lockstep->set_token_fold(enable != 0);
     return 0;
 }
 

@@ -143,6 +143,50 @@ extern "C" const char *nexus_last_error(void) { return nexus::g_last_error.c_str
 
 extern "C" uint64_t nexus_kernel_launches(void) { return nexus::g_kernel_launches.load(); }
 
+extern "C" int nexus_memory_info(uint64_t *pool_used, uint64_t *pool_used_high, uint64_t *pool_reserved,
+                                 uint64_t *graph_reserved)
+{
+    int dev = 0;
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, dev);
+    const cudaMemPoolAttr attr[3] = {cudaMemPoolAttrUsedMemCurrent, cudaMemPoolAttrUsedMemHigh,
+                                     cudaMemPoolAttrReservedMemCurrent};
+    uint64_t *dst[3] = {pool_used, pool_used_high, pool_reserved};
+    for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
+        uint64_t v = 0;  // the byte-count attributes are 64-bit
+        e = cudaMemPoolGetAttribute(pool, attr[i], &v);
+        if (e == cudaSuccess && dst[i]) *dst[i] = v;
+    }
+    if (e == cudaSuccess) {
+        uint64_t v = 0;
+        e = cudaDeviceGetGraphMemAttribute(dev, cudaGraphMemAttrReservedMemCurrent, &v);
+        if (e == cudaSuccess && graph_reserved) *graph_reserved = v;
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error(std::string("nexus_memory_info: ") + cudaGetErrorString(e));
+        return -1;
+    }
+    return 0;
+}
+
+extern "C" int nexus_memory_trim(void)
+{
+    int dev = 0;
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, dev);
+    if (e == cudaSuccess) e = cudaMemPoolTrimTo(pool, 0);
+    if (e == cudaSuccess) e = cudaDeviceGraphMemTrim(dev);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error(std::string("nexus_memory_trim: ") + cudaGetErrorString(e));
+        return -1;
+    }
+    return 0;
+}
+
 extern "C" int nexus_context_create(int log_n, const uint64_t *moduli, int n_moduli, nexus_context **out)
 {
     if (!out || !moduli) {

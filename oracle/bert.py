@@ -15,9 +15,10 @@ Packing (the engine's): slot j*T + t of a ciphertext is feature block j at
 token slot t; a lane packs requests (o_r, L_r) with tokens at o_r + i and
 o_r + L_r + i.  std layout: feature f in ciphertext f // NB, block f % NB;
 head layout: feature h*dh + k in ciphertext k // KB, block (k % KB)*H2 + h.
-With the FFN fold (BertShape::ffn_fold), FFN1 writes the lower half of each
-token block only and its outputs 2i, 2i+1 become h_2i + rot(h_2i+1, -T/2);
-FFN2 reads them back as the folded ciphertext and its rotation by T/2.
+With the token fold (BertShape::token_fold), the Q and FFN1 maps write the
+lower half of each token block only and their outputs 2i, 2i+1 become
+y_2i + rot(y_2i+1, -T/2) through the bootstrap (and GELU); ciphertext 2i is
+then the folded one and 2i+1 its rotation by T/2 (Q at QK_LIMBS).
 """
 from __future__ import annotations
 
@@ -32,6 +33,8 @@ LT_Q, LT_K, LT_V, LT_O, LT_1, LT_2 = range(6)
 # the V projection reads its input at 4 limbs and lands at the 3 limbs the
 # attention takes V at: Q and K are refreshed, V is not (kVInLimbs, bert.h)
 V_IN_LIMBS = 4
+# the level the attention takes Q and K at (kQKLimbs, bert.h)
+QK_LIMBS = 14
 
 
 def _pow2_ceil(v):
@@ -43,7 +46,7 @@ def _pow2_ceil(v):
 
 class Shape:
     def __init__(self, slots, hidden, heads, head_dim, ffn, T, lanes, boot_shrink, boot_pack=True, rowsum_shrink=2.0,
-                 ffn_fold=True):
+                 token_fold=True):
         self.S, self.hidden, self.heads, self.head_dim, self.ffn, self.T = slots, hidden, heads, head_dim, ffn, T
         self.lanes = [list(l) for l in lanes]
         self.boot_shrink = float(boot_shrink)
@@ -59,12 +62,12 @@ class Shape:
         self.G = int(math.ceil(math.sqrt(self.Lmax)))
         self.Glt = int(math.ceil(math.sqrt(self.NB)))
         # BertShape::derive: the fold needs every request's tokens in [0, T/2)
-        self.ffn_fold = bool(ffn_fold)
+        self.token_fold = bool(token_fold)
         self.fold_ok = self.n_ffn >= 2 and all(o + Lr <= T // 2 for lane in lanes for (o, Lr) in lane)
 
     @property
     def folding(self):
-        return self.ffn_fold and self.fold_ok
+        return self.token_fold and self.fold_ok
 
     def rotation_steps(self):
         v = []
@@ -265,8 +268,8 @@ class BertLayer:
         ev, sh, ck = self.ev, self.sh, self.ck
         nh, G, Lm, S = sh.n_head, sh.G, sh.Lmax, sh.S
         e_limbs = 4
-        q = [ev.mod_switch_to(c, e_limbs + 10) for c in q]
-        k = [ev.mod_switch_to(c, e_limbs + 10) for c in k]
+        q = [ev.mod_switch_to(c, QK_LIMBS) for c in q]
+        k = [ev.mod_switch_to(c, QK_LIMBS) for c in k]
         v = [ev.mod_switch_to(c, e_limbs - 1) for c in v]
         n_g = -(-Lm // G)
         kb = [[c] + [ev.rotate(c, b) for b in range(1, G)] for c in k]
@@ -338,12 +341,18 @@ class BertLayer:
         x_res = [ev.mod_switch_to(c, 1) for c in self.shrink_for_bootstrap(x)]
         x2 = [ev.mod_switch_to(c, 2) for c in x]
         x4 = [ev.mod_switch_to(c, V_IN_LIMBS) for c in x]
-        q, k, v = self.project(x2, LT_Q), self.project(x2, LT_K), self.project(x4, LT_V)
+        fold = sh.folding
+        q, k, v = self.project(x2, LT_Q, fold), self.project(x2, LT_K), self.project(x4, LT_V)
         rec("qkv", q + k + v)
+        if fold:
+            q = self.fold_halves(q)
+        nq = len(q)
         qk = self.bootstrap_all(q + k)
-        nh = sh.n_head
-        q, k = qk[:nh], qk[nh:]
-        rec("qkv_boot", qk + v)
+        rec("qk_boot", qk)
+        q, k = qk[:nq], qk[nq:]
+        if fold:
+            q = self.unfold_halves([ev.mod_switch_to(c, QK_LIMBS) for c in q], sh.n_head)
+        rec("qkv_boot", q + k + v)
         o = self.attention(q, k, v)
         rec("attention", o)
         a = self.project(o, LT_O)

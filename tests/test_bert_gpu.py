@@ -29,7 +29,7 @@ def _shape():
     c = DOC
     return NB.BertShape(hidden=c["hidden"], heads=c["heads"], head_dim=c["head_dim"], ffn=c["ffn"], T=c["T"],
                         lanes=[[tuple(r) for r in lane] for lane in c["lanes"]], boot_shrink=c["boot_shrink"],
-                        boot_pack=c["boot_pack"], ffn_fold=c["ffn_fold"])
+                        boot_pack=c["boot_pack"], token_fold=c["token_fold"])
 
 
 @pytest.fixture(scope="module")
@@ -83,27 +83,51 @@ def _want(stage):
     return [lane["stages"][stage] for lane in DOC["lanes_out"]]
 
 
+def _truncate(ctx, cts, limbs):
+    from nexus_gb300.operators import Ciphertext
+    return [Ciphertext.from_numpy(ctx, c.to_numpy()[:, :limbs, :].copy(), c.scale) for c in cts]
+
+
 @pytest.mark.parametrize("lockstep", [False, True])
 def test_qkv_and_attention_stages(env, lockstep):
-    from nexus_gb300.bert import BERT_ATTENTION, BERT_BOOTSTRAP, BERT_PROJECT
-    from nexus_gb300.operators import Ciphertext
+    """The forward's first blocks stage by stage: Q on the lower half of each
+    token block, K, V; Q folded two per ciphertext (token fold), refreshed
+    with K, unfolded at the attention's level (14 limbs); the attention."""
+    from nexus_gb300.bert import (BERT_ATTENTION, BERT_BOOTSTRAP, BERT_FOLD, BERT_LOWER_HALF, BERT_PROJECT,
+                                  BERT_UNFOLD)
     layer, ctx = env["layer"], env["ctx"]
-    nl, nh, nhid = layer.n_lanes, layer.n_head, layer.n_hid
-
-    def at(limbs):
-        return [Ciphertext.from_numpy(ctx, c.to_numpy()[:, :limbs, :].copy(), c.scale) for c in env["x"]]
+    nl, nh = layer.n_lanes, layer.n_head
+    assert DOC["token_fold"] and nh == 2
+    nq = (nh + 1) // 2
     # Q and K from the input at 2 limbs, V at 4 (it lands at the attention's level unrefreshed)
-    x2, x4 = at(2), at(4)
-    proj = [layer.stage(BERT_PROJECT, w, x, nh, lockstep) for w, x in ((0, x2), (1, x2), (2, x4))]
+    x2, x4 = _truncate(ctx, env["x"], 2), _truncate(ctx, env["x"], 4)
+    proj = [layer.stage(BERT_PROJECT, w, x, nh, lockstep)
+            for w, x in ((0 | BERT_LOWER_HALF, x2), (1, x2), (2, x4))]
     # lane-major q | k | v per lane
     qkv = [proj[t][l * nh + i] for l in range(nl) for t in range(3) for i in range(nh)]
     assert _lane_digests(qkv, 3 * nh) == _want("qkv")
-    qk = [proj[t][l * nh + i] for l in range(nl) for t in range(2) for i in range(nh)]
-    boot = layer.stage(BERT_BOOTSTRAP, 0, qk, 2 * nh, lockstep)
-    att_in = [c for l in range(nl) for c in boot[l * 2 * nh:(l + 1) * 2 * nh] + proj[2][l * nh:(l + 1) * nh]]
+    qf = layer.stage(BERT_FOLD, 0, proj[0], nq, lockstep)
+    qk = [c for l in range(nl) for c in qf[l * nq:(l + 1) * nq] + proj[1][l * nh:(l + 1) * nh]]
+    boot = layer.stage(BERT_BOOTSTRAP, 0, qk, nq + nh, lockstep)
+    assert _lane_digests(boot, nq + nh) == _want("qk_boot")
+    q14 = _truncate(ctx, [boot[l * (nq + nh) + i] for l in range(nl) for i in range(nq)], 14)
+    q = layer.stage(BERT_UNFOLD, 0, q14, nh, lockstep)
+    att_in = [c for l in range(nl) for c in q[l * nh:(l + 1) * nh] + boot[l * (nq + nh) + nq:(l + 1) * (nq + nh)]
+              + proj[2][l * nh:(l + 1) * nh]]
     assert _lane_digests(att_in, 3 * nh) == _want("qkv_boot")
     att = layer.stage(BERT_ATTENTION, 0, att_in, nh, lockstep)
     assert _lane_digests(att, nh) == _want("attention")
+
+
+def test_fold_stages_reject_wrong_counts(env):
+    from nexus_gb300 import NexusError
+    from nexus_gb300.bert import BERT_FOLD, BERT_UNFOLD
+    layer = env["layer"]
+    x = env["x"]                                  # 2 per lane
+    with pytest.raises(NexusError, match="count"):
+        layer.stage(BERT_FOLD, 0, x, 2, True)      # 2 -> 1, not 2
+    with pytest.raises(NexusError, match="count"):
+        layer.stage(BERT_UNFOLD, 0, x, 2, True)    # 2 unfold to 3 or 4, not 2
 
 
 @pytest.mark.parametrize("lockstep", [False, True])
@@ -126,19 +150,19 @@ def test_layer_matches_oracle(env, lockstep):
 @pytest.mark.parametrize("pack,fold", [(False, False), (True, False), (False, True)])
 def test_other_packings_keep_the_layer_within_its_error(env, pack, fold):
     """With one ciphertext per bootstrap (boot_pack off), the FFN unfolded
-    (ffn_fold off), or both (the plain form), the layer's lockstep and
+    (token_fold off), or both (the plain form), the layer's lockstep and
     single-lane forms agree word for word, and the decrypted output stays
     within the default layer's error bound against the FP64 layer."""
     from nexus_gb300 import bert as NB
     layer, ctx, sh, n = env["layer"], env["ctx"], env["sh"], env["n"]
     layer.set_boot_pack(pack)
-    layer.set_ffn_fold(fold)
+    layer.set_token_fold(fold)
     try:
         lock = layer.forward(env["x"], True)
         single = layer.forward(env["x"], False)
     finally:
         layer.set_boot_pack(True)
-        layer.set_ffn_fold(True)
+        layer.set_token_fold(True)
     for a, b in zip(lock, single):
         assert np.array_equal(a.to_numpy(), b.to_numpy())
     for lane in range(layer.n_lanes):

@@ -112,7 +112,7 @@ class _SlotEvaluator:
         return _Slots(a.v, a.limbs - 1, a.scale)
 
 
-def test_ffn_fold_slot_algebra():
+def test_token_fold_slot_algebra():
     """The fold of BertLayerT (restated in oracle/bert.py): FFN1 on the lower
     half, h_2i + rot(h_2i+1, -T/2), an element-wise function, the unfold
     (2i+1 = rot(folded, T/2)) and FFN2 give the unfolded FFN's values on every

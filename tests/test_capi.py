@@ -105,3 +105,12 @@ def test_graph_wrapper_needs_a_stream_without_gpu():
     from nexus_gb300.operators import Graph
     with pytest.raises(ValueError):
         Graph(None)
+
+
+def test_memory_info_reports_an_error_without_a_device():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    import nexus_gb300 as ng
+    with pytest.raises(ng.NexusError, match="nexus_memory_info"):
+        ng.memory_info()

@@ -270,3 +270,18 @@ def test_bert_layer_graph_matches_oracle(cuda):
         g.launch()
         stream.synchronize()
         assert _lane_digests(out, layer.n_hid) == _want("output")
+
+
+def test_memory_info_counts_the_engine_buffers(env):
+    """Keys, LT coefficients and ciphertexts live in the engine's pool: its
+    live bytes are nonzero, at most their peak and at most what it holds."""
+    import torch
+
+    import nexus_gb300 as ng
+    torch.cuda.synchronize()
+    m = ng.memory_info()
+    assert 0 < m["pool_used"] <= m["pool_used_high"]
+    assert m["pool_used"] <= m["pool_reserved"]
+    ng.memory_trim()
+    t = ng.memory_info()
+    assert t["pool_used"] == m["pool_used"] and t["pool_reserved"] <= m["pool_reserved"]
