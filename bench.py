@@ -926,13 +926,16 @@ BERT_SEED = 600
 
 
 def bert_bootstraps(pack: bool = True, fold: bool = True) -> int:
-    """Bootstraps per layer: Q and K 32 ciphertexts (24 with Q folded two per
-    ciphertext; V is projected at the attention's level and not refreshed),
-    the softmax row sums 2 (one per lane, refreshed alone), the residuals
-    12 + 12 and the FFN hidden activations 48 (24 folded); two ciphertexts
-    per bootstrap with pack: 12 + 2 + 6 + 6 + 12 = 38 folded, 54 not."""
-    qk, ffn = (24, 24) if fold else (32, 48)
-    return (qk + 24 + ffn) // 2 + 2 if pack else qk + 2 + 24 + ffn
+    """Bootstraps per layer, over its two lanes: per lane Q and K 16
+    ciphertexts (12 with Q folded two per ciphertext; V is projected at the
+    attention's level and not refreshed), the softmax row sum 1, the two
+    residuals 6 each (3 folded) and the FFN hidden activations 24 (12
+    folded); with pack two per bootstrap, an odd one alone: 2 x (6 + 1 + 2 +
+    2 + 6) = 34 folded, 54 not."""
+    qk, res, ffn = (12, 3, 12) if fold else (16, 6, 24)
+    if pack:
+        return 2 * ((qk + 1) // 2 + 1 + 2 * ((res + 1) // 2) + (ffn + 1) // 2)
+    return 2 * (qk + 1 + 2 * res + ffn)
 
 
 def bert_config(pack: bool = True, shrink: float = 1.0, fold: bool = True):
@@ -1200,6 +1203,7 @@ def run_bert_gpu(args, rank, world):
     free_b, total_b = torch.cuda.mem_get_info(dev)
     mem_used = total_b - free_b
     mem = ng.memory_info()
+    torch_bytes = torch.cuda.memory_allocated(dev)
     peak, peak_kind = _peak_hbm()
     ntt_avg_ms = ntt_ms / max(1, ntt_calls)
     alg_bytes_per_call = 16.0 * n * ntt_limbs / max(1, ntt_calls)
@@ -1246,8 +1250,8 @@ def run_bert_gpu(args, rank, world):
                                  "max_abs_err_vs_fp64_same_approx": plain_err},
         "lanes_one_by_one_form": {"value": lanes_ms / 1e3, "unit": "s per layer",
                                   "what": "each lane on its own, one ciphertext per operation, bootstraps as in "
-                                          "the lockstep form (two ciphertexts each when boot_pack), Q and the "
-                                          "FFN folded as in it",
+                                          "the lockstep form (two ciphertexts each when boot_pack), folded as "
+                                          "in it",
                                   "lockstep_speedup": lanes_ms / step_ms, "words_equal_lockstep": bool(same)},
         "blocks_ms": {"lockstep": blocks_lock, "lanes_one_by_one": blocks_plain},
         "setup": {"first_call_s": setup_s, "galois_keys": len(all_steps),
@@ -1256,10 +1260,14 @@ def run_bert_gpu(args, rank, world):
                                        "engine_peak": mem["pool_used_high"] / 1e9,
                                        "engine_pool_held": mem["pool_reserved"] / 1e9,
                                        "graph_held": mem["graph_reserved"] / 1e9,
+                                       "torch_allocated": torch_bytes / 1e9,
                                        "process_held": mem_used / 1e9,
                                        "note": "live and peak: the engine's allocations outside graphs; pool "
                                                "held: also the freed blocks its pool keeps for reuse; graph held: "
-                                               "the captured layer's temporaries, kept between launches"}},
+                                               "the captured layer's temporaries, kept between launches; torch: "
+                                               "the keys (made as torch tensors the evaluator references) and "
+                                               "the encrypted inputs; process held: the device's total minus "
+                                               "its free memory"}},
         "clocks": clk.summary(),
         "gpu_launches": launches,
         "cpu_baseline": cpu_bert_sample(os.cpu_count() or 1, bool(args.bert_pack), bool(args.bert_fold))
@@ -1273,7 +1281,7 @@ def run_bert_gpu(args, rank, world):
 def cpu_bert_sample(threads: int, pack: bool = True, fold: bool = True):
     """A lower bound of the layer on the oracle port: one full bootstrap on the
     layer's chain, timed, times the layer's bootstraps (bert_bootstraps:
-    38 with two ciphertexts per bootstrap and the token fold; projections,
+    34 with two ciphertexts per bootstrap and the token fold; projections,
     attention, GELU, LayerNorm and the packing's conjugations left out)."""
     cb = CpuBootstrap(threads, BERT_BITS)
     t = cb.bootstrap()

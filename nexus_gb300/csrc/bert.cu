@@ -421,15 +421,33 @@ void BertLayerT<EV, CT>::masks(int delta, int kind, int limbs, double scale, std
 }
 
 // ct *= value with the constant encoded so that, after the rescale, the
-// scale is target_scale (set exactly)
+// scale is target_scale (set exactly); with lower_half the value is on the
+// lower half of each token block and 0 on the upper half
 template <class EV, class CT>
-void BertLayerT<EV, CT>::exact_scale_const(CT &ct, double value, double target_scale)
+void BertLayerT<EV, CT>::exact_scale_const(CT &ct, double value, double target_scale, bool lower_half)
 {
     const int l = ct.limbs();
     const double q = (double)ev_->modulus(l - 1);
-    Plaintext p;
-    ev_->encode(value, l, q * target_scale / ct.scale(), p);
-    ev_->multiply_plain_inplace(ct, p);
+    const double sc = q * target_scale / ct.scale();
+    Plaintext scalar;
+    const Plaintext *p = &scalar;
+    if (lower_half) {
+        // encoded once per level and scale (a graph replays no host encode)
+        const auto key = std::make_tuple(bits_of(value), l, bits_of(sc));
+        auto it = pt_->half.find(key);
+        if (it == pt_->half.end()) {
+            std::vector<double> v((size_t)sh_.S, 0.0);
+            for (int j = 0; j < sh_.NB; ++j)
+                std::fill(v.begin() + (size_t)j * sh_.T, v.begin() + (size_t)j * sh_.T + sh_.T / 2, value);
+            Plaintext e;
+            ev_->encode(v, l, sc, e);
+            it = pt_->half.emplace(key, std::move(e)).first;
+        }
+        p = &it->second;
+    } else {
+        ev_->encode(value, l, sc, scalar);
+    }
+    ev_->multiply_plain_inplace(ct, *p);
     ev_->rescale_to_next_inplace(ct);
     ct.scale() = target_scale;
 }
@@ -558,28 +576,32 @@ void BertLayerT<EV, CT>::bootstrap_all(std::vector<CT> &cts)
         return;
     }
     // pairs (2i, 2i + 1) share a bootstrap (see bert.h); a trailing odd one
-    // is refreshed alone
+    // is a pair whose second member is zero, so that every z goes through
+    // the same lockstep group
     Evaluator &base = base_evaluator();
     const int half = (int)(base.context().n / 2);
-    const size_t pairs = cts.size() / 2;
-    std::vector<CT> z(pairs), rest;
+    const size_t pairs = (cts.size() + 1) / 2;
+    std::vector<CT> z(pairs);
     for (size_t i = 0; i < pairs; ++i) {
-        CT t;
-        ev.multiply_plain(cts[2 * i + 1], base.monomial(half, 1), t);
-        ev.add(cts[2 * i], t, z[i]);
+        if (2 * i + 1 < cts.size()) {
+            CT t;
+            ev.multiply_plain(cts[2 * i + 1], base.monomial(half, 1), t);
+            ev.add(cts[2 * i], t, z[i]);
+        } else {
+            z[i] = std::move(cts[2 * i]);
+        }
         z[i].scale() *= 2.0;
     }
-    for (size_t i = 2 * pairs; i < cts.size(); ++i) rest.push_back(std::move(cts[i]));
     refresh(z);
-    refresh(rest);
     for (size_t i = 0; i < pairs; ++i) {
         CT conj = z[i];
         ev.complex_conjugate_inplace(conj);
         ev.add(z[i], conj, cts[2 * i]);
-        ev.sub(conj, z[i], cts[2 * i + 1]);
-        ev.multiply_plain_inplace(cts[2 * i + 1], base.monomial(half, cts[2 * i + 1].limbs()));
+        if (2 * i + 1 < cts.size()) {
+            ev.sub(conj, z[i], cts[2 * i + 1]);
+            ev.multiply_plain_inplace(cts[2 * i + 1], base.monomial(half, cts[2 * i + 1].limbs()));
+        }
     }
-    for (size_t i = 0; i < rest.size(); ++i) cts[2 * pairs + i] = std::move(rest[i]);
 }
 
 template <class EV, class CT>
@@ -737,7 +759,7 @@ void BertLayerT<EV, CT>::attention(std::vector<CT> &q, std::vector<CT> &k, std::
 // LayerNorm of NEXUS (layer_norm.cpp:6-33): the sum of squares over the
 // features is a sum over ciphertexts and a fold over the NB blocks
 template <class EV, class CT>
-void BertLayerT<EV, CT>::layer_norm(std::vector<CT> &x)
+void BertLayerT<EV, CT>::layer_norm(std::vector<CT> &x, bool folded)
 {
     EV &ev = *ev_;
     CT sum, t;
@@ -750,6 +772,12 @@ void BertLayerT<EV, CT>::layer_norm(std::vector<CT> &x)
     }
     for (int m = 1; m < sh_.NB; m <<= 1) {
         ev.rotate_vector(sum, sh_.T * m, t);
+        ev.add_inplace(sum, t);
+    }
+    if (folded) {
+        // every block now holds the same sums; the two halves hold two
+        // feature sets of the same tokens
+        ev.rotate_vector(sum, sh_.T / 2, t);
         ev.add_inplace(sum, t);
     }
     Plaintext delta;
@@ -766,10 +794,10 @@ void BertLayerT<EV, CT>::layer_norm(std::vector<CT> &x)
 }
 
 template <class EV, class CT>
-void BertLayerT<EV, CT>::shrink_for_bootstrap(std::vector<CT> &cts)
+void BertLayerT<EV, CT>::shrink_for_bootstrap(std::vector<CT> &cts, bool lower_half)
 {
     for (auto &c : cts) {
-        exact_scale_const(c, 1.0 / sh_.boot_shrink, delta_);
+        exact_scale_const(c, 1.0 / sh_.boot_shrink, delta_, lower_half);
         c.scale() = delta_ / sh_.boot_shrink;
     }
 }
@@ -783,16 +811,17 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
         if (batch_of(c) != (int)lanes_.size()) throw std::invalid_argument("forward: batch does not match the lanes");
     if (x_in[0].limbs() < kVInLimbs) throw std::invalid_argument("forward: the input needs at least 4 limbs");
     begin_marks();
-    // the residual branch: x / boot_shrink at one limb
+    const bool fold = sh_.folding();
+    // the residual branch: x / boot_shrink at one limb (on the lower half of
+    // each token block when folding)
     std::vector<CT> x_res = x_in;
-    shrink_for_bootstrap(x_res);
+    shrink_for_bootstrap(x_res, fold);
     for (auto &c : x_res) ev.mod_switch_to_inplace(c, 1);
     // Q and K at one limb, refreshed; V from the input at 4 limbs lands at
     // the 3 limbs the attention reads it at, so it needs no bootstrap
     std::vector<CT> x2 = x_in, x4 = x_in;
     for (auto &c : x2) ev.mod_switch_to_inplace(c, 2);
     for (auto &c : x4) ev.mod_switch_to_inplace(c, kVInLimbs);
-    const bool fold = sh_.folding();
     std::vector<CT> q, k, v;
     project(x2, LT_Q, q, fold);
     project(x2, LT_K, k);
@@ -818,22 +847,25 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
     std::vector<CT> o, a;
     attention(q, k, v, o);
     mark("attention");
-    project(o, LT_O, a);
-    // residual + LayerNorm
+    project(o, LT_O, a, fold);
+    // residual + LayerNorm (two hidden ciphertexts folded in one from here
+    // to the layer's output when folding)
     for (int c = 0; c < sh_.n_hid; ++c) {
         a[c].scale() = x_res[c].scale();
         ev.add_inplace(a[c], x_res[c]);
     }
+    if (fold) fold_halves(a);
     mark("output projection + residual");
     bootstrap_all(a);
     mark("residual bootstraps 1");
-    layer_norm(a);
+    layer_norm(a, fold);
     mark("layer norm 1");
     // FFN
     std::vector<CT> y_res = a;
     shrink_for_bootstrap(y_res);
     for (auto &c : y_res) ev.mod_switch_to_inplace(c, 1);
     for (auto &c : a) ev.mod_switch_to_inplace(c, 2);
+    if (fold) unfold_halves(a, sh_.n_hid);
     std::vector<CT> h, f;
     project(a, LT_1, h, fold);
     if (fold) fold_halves(h);
@@ -852,15 +884,17 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
     }
     mark("gelu");
     if (fold) unfold_halves(h, sh_.n_ffn);
-    project(h, LT_2, f);
-    for (int c = 0; c < sh_.n_hid; ++c) {
+    project(h, LT_2, f, fold);
+    if (fold) fold_halves(f);
+    for (size_t c = 0; c < f.size(); ++c) {
         f[c].scale() = y_res[c].scale();
         ev.add_inplace(f[c], y_res[c]);
     }
     mark("ffn2 projection + residual");
     bootstrap_all(f);
     mark("residual bootstraps 2");
-    layer_norm(f);
+    layer_norm(f, fold);
+    if (fold) unfold_halves(f, sh_.n_hid);
     mark("layer norm 2");
     out = std::move(f);
 }

@@ -133,7 +133,9 @@ struct BertPlaintexts {
     std::map<DKey, Plaintext> diag;
     std::map<std::tuple<int, int, int, uint64_t, int>, Plaintext> mask;
     std::map<std::tuple<int, int, int, uint64_t>, Plaintext> bias;
-    size_t count() const { return diag.size() + mask.size() + bias.size(); }
+    // a value on the lower half of every token block: (value bits, limbs, scale bits)
+    std::map<std::tuple<uint64_t, int, uint64_t>, Plaintext> half;
+    size_t count() const { return diag.size() + mask.size() + bias.size() + half.size(); }
 };
 
 // one layer over ciphertexts that each hold one lane (Evaluator, Ciphertext)
@@ -153,7 +155,8 @@ public:
     // linear map + bias; lower_half: written on token slots [0, T/2) only
     void project(const std::vector<CT> &x, int which, std::vector<CT> &y, bool lower_half = false);
     void attention(std::vector<CT> &q, std::vector<CT> &k, std::vector<CT> &v, std::vector<CT> &o);
-    void layer_norm(std::vector<CT> &x);
+    // folded: x holds two feature sets per ciphertext (the block halves)
+    void layer_norm(std::vector<CT> &x, bool folded = false);
     void bootstrap_all(std::vector<CT> &cts);
     // ciphertexts 2i, 2i+1 (lower-half layout) -> one; and back to `count`
     void fold_halves(std::vector<CT> &x);
@@ -191,10 +194,10 @@ private:
     void encode_diagonals(int which, int limbs, double scale, bool lower_half);
     const Plaintext &bias_plain(int which, int ct, int limbs, double scale, bool lower_half);
     void masks(int delta, int kind, int limbs, double scale, std::vector<const Plaintext *> &out);
-    void shrink_for_bootstrap(std::vector<CT> &cts);
+    void shrink_for_bootstrap(std::vector<CT> &cts, bool lower_half = false);
     void begin_marks();
     void mark(const char *name);
-    void exact_scale_const(CT &ct, double value, double target_scale);
+    void exact_scale_const(CT &ct, double value, double target_scale, bool lower_half = false);
     Evaluator &base_evaluator();
 
     EV *ev_;

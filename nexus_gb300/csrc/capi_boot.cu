@@ -686,15 +686,16 @@ extern "C" int nexus_bert_layer_stage(nexus_bert_layer *layer, int lockstep, int
         case NEXUS_BERT_BOOTSTRAP: {
             if (count_in != count_out || count_in < 1) throw std::invalid_argument("wrong ciphertext count");
             const bool ln = stage == NEXUS_BERT_LAYER_NORM;
+            if (ln && which != 0 && which != 1) throw std::invalid_argument("LAYER_NORM takes which = 0 or 1");
             bert_run(
                 layer, lockstep, in, count_in, out, count_out,
                 [&](BertLayer &L, std::vector<Ciphertext> &a, std::vector<Ciphertext> &b) {
-                    if (ln) L.layer_norm(a);
+                    if (ln) L.layer_norm(a, which == 1);
                     else L.bootstrap_all(a);
                     b = std::move(a);
                 },
                 [&](BatchBertLayer &L, std::vector<CtBatch> &a, std::vector<CtBatch> &b) {
-                    if (ln) L.layer_norm(a);
+                    if (ln) L.layer_norm(a, which == 1);
                     else L.bootstrap_all(a);
                     b = std::move(a);
                 });

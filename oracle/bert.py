@@ -15,10 +15,13 @@ Packing (the engine's): slot j*T + t of a ciphertext is feature block j at
 token slot t; a lane packs requests (o_r, L_r) with tokens at o_r + i and
 o_r + L_r + i.  std layout: feature f in ciphertext f // NB, block f % NB;
 head layout: feature h*dh + k in ciphertext k // KB, block (k % KB)*H2 + h.
-With the token fold (BertShape::token_fold), the Q and FFN1 maps write the
-lower half of each token block only and their outputs 2i, 2i+1 become
-y_2i + rot(y_2i+1, -T/2) through the bootstrap (and GELU); ciphertext 2i is
-then the folded one and 2i+1 its rotation by T/2 (Q at QK_LIMBS).
+With the token fold (BertShape::token_fold), the Q, output, FFN1 and FFN2
+maps and the residual input write the lower half of each token block only,
+and two ciphertexts 2i, 2i+1 become y_2i + rot(y_2i+1, -T/2): Q through its
+bootstrap, the hidden and FFN activations from the output projection to the
+layer's output; an unfold gives 2i as the folded one and 2i+1 as its
+rotation by T/2 (Q at QK_LIMBS), and LayerNorm on folded ciphertexts adds
+the halves' sums with one more rotation.
 """
 from __future__ import annotations
 
@@ -221,18 +224,22 @@ class BertLayer:
         return [x[i // 2] if i % 2 == 0 else self.ev.rotate(x[i // 2], self.sh.T // 2) for i in range(count)]
 
     # -- helpers ------------------------------------------------------------------
-    def exact_scale_const(self, ct, value, target):
+    def exact_scale_const(self, ct, value, target, lower_half=False):
         ev = self.ev
         q = float(ev.q[ct.limbs - 1])
-        p = ev.encode_scalar(value, q * target / ct.scale, ct.limbs)
+        sc = q * target / ct.scale
+        if lower_half:
+            p = ev.encode(self._spread(np.full(self.sh.NB, value), True), sc, ct.limbs)
+        else:
+            p = ev.encode_scalar(value, sc, ct.limbs)
         ct = ev.rescale(ev.multiply_plain(ct, p))
         ct.scale = target
         return ct
 
-    def shrink_for_bootstrap(self, cts):
+    def shrink_for_bootstrap(self, cts, lower_half=False):
         out = []
         for c in cts:
-            c = self.exact_scale_const(c, 1.0 / self.sh.boot_shrink, self.delta)
+            c = self.exact_scale_const(c, 1.0 / self.sh.boot_shrink, self.delta, lower_half)
             c.scale = self.delta / self.sh.boot_shrink
             out.append(c)
         return out
@@ -240,15 +247,20 @@ class BertLayer:
     def bootstrap_all(self, cts):
         """BertLayerT::bootstrap_all: every ciphertext refreshed at one limb;
         with boot_pack, ciphertexts 2i and 2i + 1 share one bootstrap
-        (bootstrap.bootstrap_real_pair); a trailing odd one is refreshed alone."""
-        cts = [self.ev.mod_switch_to(c, 1) for c in cts]
+        (bootstrap.bootstrap_real_pair); a trailing odd one is a pair whose
+        second member is zero (its scale doubled, then z + conj(z))."""
+        ev = self.ev
+        cts = [ev.mod_switch_to(c, 1) for c in cts]
         if not self.sh.boot_pack:
             return [self.bs.bootstrap_3(c) for c in cts]
-        pairs = len(cts) // 2
         out = []
-        for i in range(pairs):
-            out.extend(B.bootstrap_real_pair(self.bs, cts[2 * i], cts[2 * i + 1]))
-        return out + [self.bs.bootstrap_3(c) for c in cts[2 * pairs:]]
+        for i in range(0, len(cts) - 1, 2):
+            out.extend(B.bootstrap_real_pair(self.bs, cts[i], cts[i + 1]))
+        if len(cts) % 2:
+            z = L.Ct(cts[-1].data, cts[-1].scale * 2.0)
+            r = self.bs.bootstrap_3(z)
+            out.append(ev.add(r, ev.conjugate(r)))
+        return out
 
     def _mask(self, delta, kind, limbs, scale):
         sh = self.sh
@@ -319,7 +331,7 @@ class BertLayer:
             o.append(acc)
         return o
 
-    def layer_norm(self, x):
+    def layer_norm(self, x, folded=False):
         ev, sh = self.ev, self.sh
         total = None
         for c in x:
@@ -329,6 +341,8 @@ class BertLayer:
         while m < sh.NB:
             total = ev.add(total, ev.rotate(total, sh.T * m))
             m <<= 1
+        if folded:
+            total = ev.add(total, ev.rotate(total, sh.T // 2))
         total = ev.rescale(ev.multiply_plain(total, ev.encode_scalar(1.0 / sh.hidden, total.scale, total.limbs)))
         r = self.ck.invert_sqrt(total, 4, 2)
         return [ev.rescale(ev.relinearize(ev.multiply(ev.mod_switch_to(c, r.limbs), r))) for c in x]
@@ -338,10 +352,10 @@ class BertLayer:
         trace, a dict, receives every stage's ciphertexts."""
         ev, sh = self.ev, self.sh
         rec = (lambda k, v: trace.__setitem__(k, v)) if trace is not None else (lambda k, v: None)
-        x_res = [ev.mod_switch_to(c, 1) for c in self.shrink_for_bootstrap(x)]
+        fold = sh.folding
+        x_res = [ev.mod_switch_to(c, 1) for c in self.shrink_for_bootstrap(x, fold)]
         x2 = [ev.mod_switch_to(c, 2) for c in x]
         x4 = [ev.mod_switch_to(c, V_IN_LIMBS) for c in x]
-        fold = sh.folding
         q, k, v = self.project(x2, LT_Q, fold), self.project(x2, LT_K), self.project(x4, LT_V)
         rec("qkv", q + k + v)
         if fold:
@@ -355,17 +369,20 @@ class BertLayer:
         rec("qkv_boot", q + k + v)
         o = self.attention(q, k, v)
         rec("attention", o)
-        a = self.project(o, LT_O)
+        a = self.project(o, LT_O, fold)
         for c in range(sh.n_hid):
             a[c].scale = x_res[c].scale
             a[c] = ev.add(a[c], x_res[c])
+        if fold:
+            a = self.fold_halves(a)
         a = self.bootstrap_all(a)
         rec("residual1_boot", a)
-        a = self.layer_norm(a)
+        a = self.layer_norm(a, fold)
         rec("ln1", a)
         y_res = [ev.mod_switch_to(c, 1) for c in self.shrink_for_bootstrap(a)]
         a2 = [ev.mod_switch_to(c, 2) for c in a]
-        fold = sh.folding
+        if fold:
+            a2 = self.unfold_halves(a2, sh.n_hid)
         h = self.project(a2, LT_1, fold)
         if fold:
             h = self.fold_halves(h)
@@ -375,12 +392,16 @@ class BertLayer:
         rec("gelu", h)
         if fold:
             h = self.unfold_halves(h, sh.n_ffn)
-        f = self.project(h, LT_2)
-        for c in range(sh.n_hid):
+        f = self.project(h, LT_2, fold)
+        if fold:
+            f = self.fold_halves(f)
+        for c in range(len(f)):
             f[c].scale = y_res[c].scale
             f[c] = ev.add(f[c], y_res[c])
         f = self.bootstrap_all(f)
         rec("residual2_boot", f)
-        out = self.layer_norm(f)
+        out = self.layer_norm(f, fold)
+        if fold:
+            out = self.unfold_halves(out, sh.n_hid)
         rec("output", out)
         return out
