@@ -927,12 +927,12 @@ BERT_SEED = 600
 
 def bert_bootstraps(pack: bool = True, fold: bool = True) -> int:
     """Bootstraps per layer, over its two lanes: per lane Q and K 16
-    ciphertexts (12 with Q folded two per ciphertext; V is projected at the
-    attention's level and not refreshed), the softmax row sum 1, the two
-    residuals 6 each (3 folded) and the FFN hidden activations 24 (12
-    folded); with pack two per bootstrap, an odd one alone: 2 x (6 + 1 + 2 +
-    2 + 6) = 34 folded, 54 not."""
-    qk, res, ffn = (12, 3, 12) if fold else (16, 6, 24)
+    ciphertexts (8 with the token fold; V is projected at the attention's
+    level and not refreshed), the softmax row sum 1, the two residuals 6
+    each (3 folded) and the FFN hidden activations 24 (12 folded); with pack
+    two per bootstrap, an odd one alone: 2 x (4 + 1 + 2 + 2 + 6) = 30
+    folded, 54 not."""
+    qk, res, ffn = (8, 3, 12) if fold else (16, 6, 24)
     if pack:
         return 2 * ((qk + 1) // 2 + 1 + 2 * ((res + 1) // 2) + (ffn + 1) // 2)
     return 2 * (qk + 1 + 2 * res + ffn)
@@ -1281,7 +1281,7 @@ def run_bert_gpu(args, rank, world):
 def cpu_bert_sample(threads: int, pack: bool = True, fold: bool = True):
     """A lower bound of the layer on the oracle port: one full bootstrap on the
     layer's chain, timed, times the layer's bootstraps (bert_bootstraps:
-    34 with two ciphertexts per bootstrap and the token fold; projections,
+    30 with two ciphertexts per bootstrap and the token fold; projections,
     attention, GELU, LayerNorm and the packing's conjugations left out)."""
     cb = CpuBootstrap(threads, BERT_BITS)
     t = cb.bootstrap()
@@ -1856,7 +1856,8 @@ def main():
     ap.add_argument("--bert-pack", type=int, choices=[0, 1], default=1,
                     help="BERT layer: refresh two ciphertexts per bootstrap (c0 + i c1; 0: one each)")
     ap.add_argument("--bert-fold", type=int, choices=[0, 1], default=1,
-                    help="BERT layer: Q and the FFN hidden activations folded two ciphertexts in one (0: unfolded)")
+                    help="BERT layer: Q, K and the activations after the attention folded two ciphertexts in one "
+                         "(0: unfolded)")
     ap.add_argument("--ntt-cts", type=int, default=64,
                     help="ciphertexts per step (smaller values are for profiling captures only)")
     args = ap.parse_args()

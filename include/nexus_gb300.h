@@ -715,8 +715,9 @@ int nexus_bert_layer_forward(nexus_bert_layer *layer, int lockstep, nexus_cipher
  * feature sets in the halves of each token block) and BOOTSTRAP return
  * their inputs transformed; FOLD maps count_in ciphertexts to
  * (count_in + 1) / 2 (2i and 2i+1 -> x_2i + rot(x_2i+1, -T/2)), UNFOLD maps
- * (count_out + 1) / 2 back to count_out (2i -> x_i, 2i+1 -> rot(x_i, T/2));
- * see set_token_fold. */
+ * (count_out + 1) / 2 back to count_out (2i -> x_i, 2i+1 -> rot(x_i, T/2);
+ * which = 1: also rebuilds every request's second token copy where it lies
+ * in the upper half, one level down, as K is); see set_token_fold. */
 #define NEXUS_BERT_PROJECT 0
 #define NEXUS_BERT_ATTENTION 1
 #define NEXUS_BERT_LAYER_NORM 2
@@ -740,16 +741,18 @@ int nexus_bert_layer_set_timing(nexus_bert_layer *layer, int enable);
 int nexus_bert_layer_set_boot_pack(nexus_bert_layer *layer, int enable);
 /* With token_fold on, and when every request's tokens lie in token slots
  * [0, T/2), two ciphertexts share one, the second's tokens in the upper half
- * of every token block: Q through its bootstrap, and the hidden and FFN
+ * of every token block: Q and K through their bootstrap (K's second token
+ * copies rebuilt by masked rotations when unfolded), and the hidden and FFN
  * activations from the output projection to the layer's output (both
  * residual bootstraps and LayerNorms, the FFN's bootstraps and GELU).  The
- * maps feeding a fold (Q, output, W1, W2) and the residual input write the
+ * maps feeding a fold (Q, K, output, W1, W2) and the residual input write the
  * lower half only; a fold is one rotation of -T/2, an unfold gives
  * ciphertext 2i+1 as the folded one rotated by T/2 (Q at the attention's
  * level), and LayerNorm adds the two halves' feature sums with one more
- * rotation.  34 bootstraps per BERT-base layer instead of 54, half the
- * GELUs and LayerNorm products; the rotation steps include +-T/2 whenever
- * the fold applies.  On by default; no counterpart in the reference (NEXUS
+ * rotation.  30 bootstraps per BERT-base layer instead of 54, half the
+ * GELUs and LayerNorm products; the rotation steps include +-T/2 and the
+ * copy shifts (-L for every request length L whose second copy reaches the
+ * upper half) whenever the fold applies.  On by default; no counterpart in the reference (NEXUS
  * has no layer). */
 int nexus_bert_layer_set_token_fold(nexus_bert_layer *layer, int enable);
 int nexus_bert_layer_stage_times(nexus_bert_layer *layer, int lockstep, int lane, double *ms, char *names,

@@ -36,9 +36,9 @@ class BertShape:
     boot_shrink: float = 1.0
     # two ciphertexts per bootstrap (c0 + i c1, separated by a conjugation)
     boot_pack: bool = True
-    # Q and the FFN hidden activations two ciphertexts in one through their
-    # bootstraps (the halves of each token block), when every request's
-    # tokens lie in [0, T/2)
+    # two ciphertexts in one (the halves of each token block) for Q and K
+    # through their bootstrap and for the activations after the attention,
+    # when every request's tokens lie in [0, T/2)
     token_fold: bool = True
 
     def blocks(self, slots: int) -> int:
@@ -255,8 +255,8 @@ class BertLayer:
         check(lib().nexus_bert_layer_set_boot_pack(self._h, 1 if enable else 0), "nexus_bert_layer_set_boot_pack")
 
     def set_token_fold(self, enable: bool) -> None:
-        """Q and the FFN hidden activations folded two ciphertexts in one
-        (nexus_bert_layer_set_token_fold)."""
+        """Q, K and the activations after the attention folded two
+        ciphertexts in one (nexus_bert_layer_set_token_fold)."""
         check(lib().nexus_bert_layer_set_token_fold(self._h, 1 if enable else 0), "nexus_bert_layer_set_token_fold")
 
     def stage_times(self, lockstep: bool = True, lane: int = 0) -> dict:

@@ -149,9 +149,15 @@ void BertShape::derive(size_t slots)
     Glt = (int)std::ceil(std::sqrt((double)NB));
     if (!(boot_shrink >= 1.0)) throw std::invalid_argument("boot_shrink must be >= 1");
     fold_ok = true;
+    copy_shifts.clear();
     for (auto &lane : lanes)
-        for (auto &q : lane)
+        for (auto &q : lane) {
             if (q.first + q.second > T / 2) fold_ok = false;
+            if (q.first + 2 * q.second > T / 2 &&
+                std::find(copy_shifts.begin(), copy_shifts.end(), q.second) == copy_shifts.end())
+                copy_shifts.push_back(q.second);
+        }
+    std::sort(copy_shifts.begin(), copy_shifts.end());
 }
 
 std::vector<int> BertShape::rotation_steps() const
@@ -173,6 +179,7 @@ std::vector<int> BertShape::rotation_steps() const
     if (fold_ok) {
         push(T / 2);
         push(-T / 2);
+        for (int s : copy_shifts) push(-s);
     }
     return v;
 }
@@ -420,6 +427,37 @@ void BertLayerT<EV, CT>::masks(int delta, int kind, int limbs, double scale, std
     }
 }
 
+// copy-rebuild masks of unfold_copies, per lane element: shift 0 keeps the
+// lower half of every block; shift s > 0 selects the token slots of the
+// requests of length s whose copy (s slots on) lies in the upper half
+template <class EV, class CT>
+void BertLayerT<EV, CT>::copy_masks(int shift, int limbs, std::vector<const Plaintext *> &out)
+{
+    out.clear();
+    const double sc = (double)ev_->modulus(limbs - 1);
+    const int T = sh_.T, half = T / 2;
+    for (int lane : lanes_) {
+        const auto key = std::make_tuple(lane, shift, limbs, bits_of(sc), 2);
+        auto it = pt_->mask.find(key);
+        if (it == pt_->mask.end()) {
+            std::vector<double> block((size_t)T, 0.0);
+            if (shift == 0) {
+                std::fill(block.begin(), block.begin() + half, 1.0);
+            } else {
+                for (auto &r : sh_.lanes[lane])
+                    if (r.second == shift)
+                        for (int t = std::max(r.first, half - shift); t < r.first + r.second; ++t) block[t] = 1.0;
+            }
+            std::vector<double> v((size_t)sh_.S);
+            for (int j = 0; j < sh_.NB; ++j) std::copy(block.begin(), block.end(), v.begin() + (size_t)j * T);
+            Plaintext p;
+            ev_->encode(v, limbs, sc, p);
+            it = pt_->mask.emplace(key, std::move(p)).first;
+        }
+        out.push_back(&it->second);
+    }
+}
+
 // ct *= value with the constant encoded so that, after the rescale, the
 // scale is target_scale (set exactly); with lower_half the value is on the
 // lower half of each token block and 0 on the upper half
@@ -546,6 +584,41 @@ void BertLayerT<EV, CT>::unfold_halves(std::vector<CT> &x, int count)
     for (int i = 0; i < count; ++i) {
         if (i % 2) ev.rotate_vector(x[i / 2], sh_.T / 2, out[i]);
         else out[i] = x[i / 2];
+    }
+    x = std::move(out);
+}
+
+// unfold_halves, then on each half: its lower half kept, and for every copy
+// shift s the tokens whose second copy lies in the upper half rotated s slots
+// on (masks per lane, each product rescaled once: the output is one level
+// below the input)
+template <class EV, class CT>
+void BertLayerT<EV, CT>::unfold_copies(std::vector<CT> &x, int count)
+{
+    EV &ev = *ev_;
+    if (count < 1 || (int)x.size() != (count + 1) / 2)
+        throw std::invalid_argument("unfold_copies: wrong number of ciphertexts");
+    const int l = x[0].limbs();
+    if (l < 2) throw std::invalid_argument("unfold_copies: the input needs a level to spend");
+    std::vector<const Plaintext *> keep, mp;
+    copy_masks(0, l, keep);
+    std::vector<CT> out(count);
+    for (int i = 0; i < count; ++i) {
+        CT h;
+        if (i % 2) ev.rotate_vector(x[i / 2], sh_.T / 2, h);
+        else h = x[i / 2];
+        CT acc = h;
+        mul_plain_each(ev, acc, keep);
+        ev.rescale_to_next_inplace(acc);
+        for (int s : sh_.copy_shifts) {
+            CT t = h, r;
+            copy_masks(s, l, mp);
+            mul_plain_each(ev, t, mp);
+            ev.rescale_to_next_inplace(t);
+            ev.rotate_vector(t, sh_.S - s, r);
+            ev.add_inplace(acc, r);
+        }
+        out[i] = std::move(acc);
     }
     x = std::move(out);
 }
@@ -824,13 +897,17 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
     for (auto &c : x4) ev.mod_switch_to_inplace(c, kVInLimbs);
     std::vector<CT> q, k, v;
     project(x2, LT_Q, q, fold);
-    project(x2, LT_K, k);
+    project(x2, LT_K, k, fold);
     project(x4, LT_V, v);
     mark("qkv projections");
     {
-        // Q folded two per ciphertext through the bootstrap (bert.h), unfolded
-        // at the attention's level
-        if (fold) fold_halves(q);
+        // Q and K folded two per ciphertext through the bootstrap (bert.h),
+        // unfolded at the attention's level (K with its token copies rebuilt,
+        // one level above it)
+        if (fold) {
+            fold_halves(q);
+            fold_halves(k);
+        }
         const size_t nq = q.size();
         std::vector<CT> all;
         for (auto *t : {&q, &k})
@@ -841,6 +918,8 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
         if (fold) {
             for (auto &c : q) ev.mod_switch_to_inplace(c, kQKLimbs);
             unfold_halves(q, sh_.n_head);
+            for (auto &c : k) ev.mod_switch_to_inplace(c, kQKLimbs + 1);
+            unfold_copies(k, sh_.n_head);
         }
     }
     mark("qk bootstraps");

@@ -56,20 +56,24 @@
 // conjugation).  The words EvalMod sees are the two messages' sum, and the
 // error of each output is that of an unpacked bootstrap.
 //
-// With token_fold, Q and the FFN hidden activations take half the
-// ciphertexts through their bootstraps.  Only the first token copies of Q
+// With token_fold, two ciphertexts travel as one wherever the upper half of
+// the token block carries nothing needed.  Every op but the linear maps'
+// block rotations acts on one token slot; only the first token copies of Q
 // are read (the scores' mask zeroes every other slot), and past the
-// attention only the first copies matter at all, while every op but the
-// linear maps' block rotations acts on one token slot.  So when every
-// request's tokens lie in the lower half of the token block ([0, T/2)), the
-// Q and FFN1 maps write only that half (their diagonals and biases are zero
-// on the upper half), and ciphertexts 2i and 2i+1 of their outputs become
-// one: y_2i + rot(y_2i+1, -T/2) holds the second's tokens in the upper half
-// of every block.  Those are refreshed (and, for the FFN, passed through
-// GELU); then ciphertext 2i is the folded one itself and 2i+1 its rotation
-// by T/2 (each token slot of the lower half holds the right feature; the
-// upper half, never read for a first copy, holds other tokens' values of the
-// same magnitude).
+// attention only the first copies matter at all.  So when every request's
+// tokens lie in the lower half of the token block ([0, T/2)), a map feeding
+// a fold writes only that half (its diagonals and bias are zero on the upper
+// half; the residual input is masked in the constant product it already
+// takes), and ciphertexts 2i and 2i+1 become one: y_2i + rot(y_2i+1, -T/2)
+// holds the second's tokens in the upper half of every block.  Unfolding
+// gives ciphertext 2i as the folded one itself and 2i+1 as its rotation by
+// T/2; each token slot of the lower half then holds the right feature, and
+// the upper half, never read for a first copy, holds other tokens' values of
+// the same magnitude.  Folded: Q and K through their bootstrap (K, read at
+// both token copies, is unfolded with the copies that reach the upper half
+// rebuilt from its tokens by masked rotations, one level), and the hidden
+// and FFN activations from the output projection to the layer's output
+// (LayerNorm adds the two halves' feature sums with one more rotation).
 #pragma once
 #include <cstdint>
 #include <map>
@@ -114,6 +118,10 @@ struct BertShape {
     int S = 0, NB = 0, H2 = 0, KB = 0, n_head = 0, n_hid = 0, n_ffn = 0, Lmax = 0, G = 0, Glt = 0;
     // every request's tokens in [0, T/2)
     bool fold_ok = false;
+    // the distinct lengths of the requests whose second token copy reaches
+    // the upper half of the block (o + 2L > T/2): the shifts that rebuild it
+    // when K is unfolded
+    std::vector<int> copy_shifts;
     void derive(size_t slots);
     bool folding() const { return token_fold && fold_ok; }
     // every rotation step the layer uses (the bootstrapper's are separate)
@@ -161,6 +169,10 @@ public:
     // ciphertexts 2i, 2i+1 (lower-half layout) -> one; and back to `count`
     void fold_halves(std::vector<CT> &x);
     void unfold_halves(std::vector<CT> &x, int count);
+    // unfold_halves with every request's second token copy rebuilt from its
+    // tokens (masks per lane, one rescale): for K, which the attention reads
+    // at both copies
+    void unfold_copies(std::vector<CT> &x, int count);
 
     ~BertLayerT();
     BertLayerT(const BertLayerT &) = delete;
@@ -194,6 +206,10 @@ private:
     void encode_diagonals(int which, int limbs, double scale, bool lower_half);
     const Plaintext &bias_plain(int which, int ct, int limbs, double scale, bool lower_half);
     void masks(int delta, int kind, int limbs, double scale, std::vector<const Plaintext *> &out);
+    // per lane: the lower half of the block (shift 0), or the tokens whose
+    // copy lies `shift` slots on in the upper half; encoded at the scale of
+    // the prime the rescale drops
+    void copy_masks(int shift, int limbs, std::vector<const Plaintext *> &out);
     void shrink_for_bootstrap(std::vector<CT> &cts, bool lower_half = false);
     void begin_marks();
     void mark(const char *name);

@@ -644,15 +644,19 @@ extern "C" int nexus_bert_layer_stage(nexus_bert_layer *layer, int lockstep, int
             const bool fold = stage == NEXUS_BERT_FOLD;
             const int halves = fold ? count_in : count_out, folded = fold ? count_out : count_in;
             if (halves < 1 || folded != (halves + 1) / 2) throw std::invalid_argument("wrong ciphertext count");
+            if (which != 0 && (fold || which != 1)) throw std::invalid_argument("FOLD takes which = 0, UNFOLD 0 or 1");
+            const bool copies = which == 1;
             bert_run(
                 layer, lockstep, in, count_in, out, count_out,
                 [&](BertLayer &L, std::vector<Ciphertext> &a, std::vector<Ciphertext> &b) {
                     if (fold) L.fold_halves(a);
+                    else if (copies) L.unfold_copies(a, count_out);
                     else L.unfold_halves(a, count_out);
                     b = std::move(a);
                 },
                 [&](BatchBertLayer &L, std::vector<CtBatch> &a, std::vector<CtBatch> &b) {
                     if (fold) L.fold_halves(a);
+                    else if (copies) L.unfold_copies(a, count_out);
                     else L.unfold_halves(a, count_out);
                     b = std::move(a);
                 });

@@ -15,13 +15,15 @@ Packing (the engine's): slot j*T + t of a ciphertext is feature block j at
 token slot t; a lane packs requests (o_r, L_r) with tokens at o_r + i and
 o_r + L_r + i.  std layout: feature f in ciphertext f // NB, block f % NB;
 head layout: feature h*dh + k in ciphertext k // KB, block (k % KB)*H2 + h.
-With the token fold (BertShape::token_fold), the Q, output, FFN1 and FFN2
+With the token fold (BertShape::token_fold), the Q, K, output, FFN1 and FFN2
 maps and the residual input write the lower half of each token block only,
-and two ciphertexts 2i, 2i+1 become y_2i + rot(y_2i+1, -T/2): Q through its
-bootstrap, the hidden and FFN activations from the output projection to the
-layer's output; an unfold gives 2i as the folded one and 2i+1 as its
-rotation by T/2 (Q at QK_LIMBS), and LayerNorm on folded ciphertexts adds
-the halves' sums with one more rotation.
+and two ciphertexts 2i, 2i+1 become y_2i + rot(y_2i+1, -T/2): Q and K
+through their bootstrap, the hidden and FFN activations from the output
+projection to the layer's output; an unfold gives 2i as the folded one and
+2i+1 as its rotation by T/2 (Q at QK_LIMBS; K one level above it, with every
+request's second token copy in the upper half rebuilt by masked rotations),
+and LayerNorm on folded ciphertexts adds the halves' sums with one more
+rotation.
 """
 from __future__ import annotations
 
@@ -66,7 +68,9 @@ class Shape:
         self.Glt = int(math.ceil(math.sqrt(self.NB)))
         # BertShape::derive: the fold needs every request's tokens in [0, T/2)
         self.token_fold = bool(token_fold)
-        self.fold_ok = self.n_ffn >= 2 and all(o + Lr <= T // 2 for lane in lanes for (o, Lr) in lane)
+        self.fold_ok = all(o + Lr <= T // 2 for lane in lanes for (o, Lr) in lane)
+        # lengths of the requests whose second token copy reaches the upper half
+        self.copy_shifts = sorted({Lr for lane in lanes for (o, Lr) in lane if o + 2 * Lr > T // 2})
 
     @property
     def folding(self):
@@ -103,6 +107,8 @@ class Shape:
         if self.fold_ok:
             push(self.T // 2)
             push(-self.T // 2)
+            for s in self.copy_shifts:
+                push(-s)
         return v
 
 
@@ -222,6 +228,37 @@ class BertLayer:
         """BertLayerT::unfold_halves: ciphertext 2i is x[i], 2i+1 is rot(x[i], T/2)."""
         assert len(x) == (count + 1) // 2
         return [x[i // 2] if i % 2 == 0 else self.ev.rotate(x[i // 2], self.sh.T // 2) for i in range(count)]
+
+    def _copy_mask(self, shift, limbs):
+        """BertLayerT::copy_masks for this lane: the lower half of every block
+        (shift 0), or the tokens of the requests of length `shift` whose copy
+        lies in the upper half; at the scale of the prime the rescale drops."""
+        sh = self.sh
+        half = sh.T // 2
+        block = np.zeros(sh.T)
+        if shift == 0:
+            block[:half] = 1.0
+        else:
+            for (o, Lr) in sh.lanes[self.lane]:
+                if Lr == shift:
+                    block[max(o, half - shift):o + Lr] = 1.0
+        return self.ev.encode(np.tile(block, sh.NB), float(self.ev.q[limbs - 1]), limbs)
+
+    def unfold_copies(self, x, count):
+        """BertLayerT::unfold_copies: unfold_halves with every request's
+        second token copy in the upper half rebuilt from its tokens."""
+        ev, sh = self.ev, self.sh
+        assert len(x) == (count + 1) // 2
+        limbs = x[0].limbs
+        out = []
+        for i in range(count):
+            h = ev.rotate(x[i // 2], sh.T // 2) if i % 2 else x[i // 2]
+            acc = ev.rescale(ev.multiply_plain(h, self._copy_mask(0, limbs)))
+            for s in sh.copy_shifts:
+                t = ev.rescale(ev.multiply_plain(h, self._copy_mask(s, limbs)))
+                acc = ev.add(acc, ev.rotate(t, sh.S - s))
+            out.append(acc)
+        return out
 
     # -- helpers ------------------------------------------------------------------
     def exact_scale_const(self, ct, value, target, lower_half=False):
@@ -356,16 +393,17 @@ class BertLayer:
         x_res = [ev.mod_switch_to(c, 1) for c in self.shrink_for_bootstrap(x, fold)]
         x2 = [ev.mod_switch_to(c, 2) for c in x]
         x4 = [ev.mod_switch_to(c, V_IN_LIMBS) for c in x]
-        q, k, v = self.project(x2, LT_Q, fold), self.project(x2, LT_K), self.project(x4, LT_V)
+        q, k, v = self.project(x2, LT_Q, fold), self.project(x2, LT_K, fold), self.project(x4, LT_V)
         rec("qkv", q + k + v)
         if fold:
-            q = self.fold_halves(q)
+            q, k = self.fold_halves(q), self.fold_halves(k)
         nq = len(q)
         qk = self.bootstrap_all(q + k)
         rec("qk_boot", qk)
         q, k = qk[:nq], qk[nq:]
         if fold:
             q = self.unfold_halves([ev.mod_switch_to(c, QK_LIMBS) for c in q], sh.n_head)
+            k = self.unfold_copies([ev.mod_switch_to(c, QK_LIMBS + 1) for c in k], sh.n_head)
         rec("qkv_boot", q + k + v)
         o = self.attention(q, k, v)
         rec("attention", o)

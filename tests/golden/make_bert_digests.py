@@ -2,10 +2,11 @@
 words at every stage of the encrypted BERT encoder layer (oracle/bert.py) at
 a reduced size: N = 2^13, 128 token slots per feature block (32 blocks per
 ciphertext: 2 hidden, 2 head-layout and 5 FFN ciphertexts), hidden 64 =
-2 heads x 32, FFN 160, two lanes with requests of 16 | 4 + 8 tokens, on
-the chain 51 + 19x46 + 14x51 + special 51 with the sparse secret
-(h = 192), two ciphertexts per bootstrap (boot_pack) and the FFN hidden
-activations folded two per ciphertext (token_fold: 5 -> 3).  Keys and encryptions come from the real SEAL-4.1-bs with one
+2 heads x 32, FFN 160, two lanes with requests of 40 | 8 + 32 tokens (the
+second copies of the 40- and 32-token requests reach the upper half of the
+block), on the chain 51 + 19x46 + 14x51 + special 51 with the sparse secret
+(h = 192), two ciphertexts per bootstrap (boot_pack) and the token fold
+(Q, K and the post-attention activations two per ciphertext).  Keys and encryptions come from the real SEAL-4.1-bs with one
 seeded Blake2xbPRNG factory, so the engine can make them again on the GPU
 from the seed (tests/test_bert_gpu.py).
 
@@ -39,7 +40,7 @@ OUT = Path(__file__).parent / "bert_digests.json"
 
 CASE = dict(log_n=13, bits=[51] + [46] * 19 + [51] * 14 + [51], seed=seed8(500), hamming_weight=192,
             scale_log2=46, loge=10, boundary_K=25, sin_cos_deg=59, scale_factor=2, inverse_deg=1,
-            hidden=64, heads=2, head_dim=32, ffn=160, T=128, lanes=[[[0, 16]], [[0, 4], [8, 8]]],
+            hidden=64, heads=2, head_dim=32, ffn=160, T=128, lanes=[[[0, 40]], [[0, 8], [16, 32]]],
             boot_shrink=1.0, boot_pack=True, token_fold=True, weight_seed=7, token_seed=8)
 
 
@@ -73,7 +74,7 @@ def main():
     sh, w, tokens = inputs(c)
     osh = OB.Shape(n // 2, sh.hidden, sh.heads, sh.head_dim, sh.ffn, sh.T, sh.lanes, sh.boot_shrink, sh.boot_pack,
                    token_fold=sh.token_fold)
-    assert osh.folding and (osh.n_hid, osh.n_head, osh.n_ffn) == (2, 2, 5)
+    assert osh.folding and (osh.n_hid, osh.n_head, osh.n_ffn) == (2, 2, 5) and osh.copy_shifts == [32, 40]
     keys = SealKeys(c["log_n"], qs, c["seed"], c["hamming_weight"], keep=1000)
     steps = B.rot_key_steps_3(log_nh, log_nh)
     for s in osh.rotation_steps():

@@ -1,6 +1,6 @@
 """Encrypted BERT encoder layer on the GPU against the oracle (oracle/bert.py),
 word for word, at the reduced size of tests/golden/bert_digests.json (N = 2^13,
-128 token slots per block, hidden 64, 2 heads, FFN 160, requests of 16 | 4 + 8
+128 token slots per block, hidden 64, 2 heads, FFN 160, requests of 40 | 8 + 32
 tokens in two lanes): the Q/K/V projections, their bootstrap, the attention
 block and the whole layer in its single-lane and lockstep forms (two
 ciphertexts per bootstrap and the FFN fold, the defaults), with keys and
@@ -90,9 +90,10 @@ def _truncate(ctx, cts, limbs):
 
 @pytest.mark.parametrize("lockstep", [False, True])
 def test_qkv_and_attention_stages(env, lockstep):
-    """The forward's first blocks stage by stage: Q on the lower half of each
-    token block, K, V; Q folded two per ciphertext (token fold), refreshed
-    with K, unfolded at the attention's level (14 limbs); the attention."""
+    """The forward's first blocks stage by stage: Q and K on the lower half of
+    each token block, V; Q and K folded two per ciphertext (token fold),
+    refreshed together, Q unfolded at the attention's level (14 limbs) and K
+    one level above it with its second token copies rebuilt; the attention."""
     from nexus_gb300.bert import (BERT_ATTENTION, BERT_BOOTSTRAP, BERT_FOLD, BERT_LOWER_HALF, BERT_PROJECT,
                                   BERT_UNFOLD)
     layer, ctx = env["layer"], env["ctx"]
@@ -102,17 +103,19 @@ def test_qkv_and_attention_stages(env, lockstep):
     # Q and K from the input at 2 limbs, V at 4 (it lands at the attention's level unrefreshed)
     x2, x4 = _truncate(ctx, env["x"], 2), _truncate(ctx, env["x"], 4)
     proj = [layer.stage(BERT_PROJECT, w, x, nh, lockstep)
-            for w, x in ((0 | BERT_LOWER_HALF, x2), (1, x2), (2, x4))]
+            for w, x in ((0 | BERT_LOWER_HALF, x2), (1 | BERT_LOWER_HALF, x2), (2, x4))]
     # lane-major q | k | v per lane
     qkv = [proj[t][l * nh + i] for l in range(nl) for t in range(3) for i in range(nh)]
     assert _lane_digests(qkv, 3 * nh) == _want("qkv")
-    qf = layer.stage(BERT_FOLD, 0, proj[0], nq, lockstep)
-    qk = [c for l in range(nl) for c in qf[l * nq:(l + 1) * nq] + proj[1][l * nh:(l + 1) * nh]]
-    boot = layer.stage(BERT_BOOTSTRAP, 0, qk, nq + nh, lockstep)
-    assert _lane_digests(boot, nq + nh) == _want("qk_boot")
-    q14 = _truncate(ctx, [boot[l * (nq + nh) + i] for l in range(nl) for i in range(nq)], 14)
+    qf, kf = (layer.stage(BERT_FOLD, 0, proj[t], nq, lockstep) for t in (0, 1))
+    qk = [c for l in range(nl) for c in qf[l * nq:(l + 1) * nq] + kf[l * nq:(l + 1) * nq]]
+    boot = layer.stage(BERT_BOOTSTRAP, 0, qk, 2 * nq, lockstep)
+    assert _lane_digests(boot, 2 * nq) == _want("qk_boot")
+    q14 = _truncate(ctx, [boot[l * 2 * nq + i] for l in range(nl) for i in range(nq)], 14)
+    k15 = _truncate(ctx, [boot[l * 2 * nq + nq + i] for l in range(nl) for i in range(nq)], 15)
     q = layer.stage(BERT_UNFOLD, 0, q14, nh, lockstep)
-    att_in = [c for l in range(nl) for c in q[l * nh:(l + 1) * nh] + boot[l * (nq + nh) + nq:(l + 1) * (nq + nh)]
+    k = layer.stage(BERT_UNFOLD, 1, k15, nh, lockstep)
+    att_in = [c for l in range(nl) for c in q[l * nh:(l + 1) * nh] + k[l * nh:(l + 1) * nh]
               + proj[2][l * nh:(l + 1) * nh]]
     assert _lane_digests(att_in, 3 * nh) == _want("qkv_boot")
     att = layer.stage(BERT_ATTENTION, 0, att_in, nh, lockstep)

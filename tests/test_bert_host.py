@@ -150,3 +150,38 @@ def test_token_fold_slot_algebra():
             assert np.allclose(folded[c].v[blk][:T // 2], want[:T // 2, f])
     # requests reaching into the upper half turn the fold off
     assert not OB.Shape(S, hidden, 2, 8, ffn, T, [[(0, 9)]], 1.0).fold_ok
+
+
+def test_unfold_copies_rebuilds_the_second_token_copies():
+    """K's unfold (BertLayerT::unfold_copies, restated in oracle/bert.py):
+    three ciphertexts written on the lower half of each token block, folded
+    two per ciphertext, come back with every request's tokens and both token
+    copies, including the copies that reach the upper half (rebuilt by one
+    masked rotation per request length)."""
+    from oracle import bert as OB
+    S, T = 256, 32
+    lanes = [[(0, 10)], [(0, 2), (4, 7)]]           # copies reaching slot 16 and up: lengths 10 and 7
+    osh = OB.Shape(S, 16, 2, 8, 40, T, lanes, 1.0)
+    assert osh.fold_ok and osh.copy_shifts == [7, 10]
+    assert all((S - s) in osh.rotation_steps() for s in (7, 10, T // 2))
+    rng = np.random.default_rng(9)
+    for lane, reqs in enumerate(lanes):
+        layer = OB.BertLayer.__new__(OB.BertLayer)
+        layer.ev, layer.sh, layer.lane = _SlotEvaluator(), osh, lane
+        full = []
+        for _ in range(3):
+            v = np.zeros(S)
+            for j in range(S // T):
+                for (o, L) in reqs:
+                    tok = rng.normal(size=L)
+                    v[j * T + o:j * T + o + L] = tok
+                    v[j * T + o + L:j * T + o + 2 * L] = tok
+            full.append(v)
+        lower = [_Slots(np.where(np.arange(S) % T < T // 2, v, 0.0)) for v in full]
+        out = layer.unfold_copies(layer.fold_halves(lower), 3)
+        assert len(out) == 3 and out[0].limbs == lower[0].limbs - 1
+        for got, want in zip(out, full):
+            for j in range(S // T):
+                for (o, L) in reqs:
+                    sl = slice(j * T + o, j * T + o + 2 * L)
+                    assert np.allclose(got.v[sl], want[sl])

@@ -217,7 +217,7 @@ def test_gelu_graph_single_and_lockstep(gelu_env):
 
 def test_bert_layer_graph_matches_oracle(cuda):
     """The whole lockstep encoder layer (the reduced size of
-    tests/golden/bert_digests.json: N=2^13, hidden 64, requests of 16 | 4 + 8
+    tests/golden/bert_digests.json: N=2^13, hidden 64, requests of 40 | 8 + 32
     tokens) captured as one graph: replays on the captured inputs give the
     oracle's output digests, the same as the direct call."""
     import torch
