@@ -458,6 +458,65 @@ void BertLayerT<EV, CT>::copy_masks(int shift, int limbs, std::vector<const Plai
     }
 }
 
+// the kind-1 masks of offsets 2 pair and 2 pair + 1 in the two halves of
+// every block (all -128 in the upper half past the last offset)
+template <class EV, class CT>
+void BertLayerT<EV, CT>::fold_masks(int pair, int limbs, double scale, std::vector<const Plaintext *> &out)
+{
+    out.clear();
+    const int T = sh_.T, half = T / 2, d0 = 2 * pair, d1 = 2 * pair + 1;
+    for (int lane : lanes_) {
+        const auto &reqs = sh_.lanes[lane];
+        auto sig_of = [&](int delta) {
+            int sig = 0;
+            for (size_t r = 0; r < reqs.size(); ++r)
+                if (delta < reqs[r].second) sig |= 1 << r;
+            return sig;
+        };
+        const int s0 = sig_of(d0), s1 = d1 < sh_.Lmax ? sig_of(d1) : 0;
+        const auto key = std::make_tuple(lane, s0 * 65536 + s1, limbs, bits_of(scale), 3);
+        auto it = pt_->mask.find(key);
+        if (it == pt_->mask.end()) {
+            std::vector<std::complex<double>> v((size_t)sh_.S, 0.0);
+            for (int j = 0; j < sh_.NB; ++j) {
+                const bool head_ok = (j % sh_.H2) < sh_.heads;
+                for (int t = 0; t < T; ++t) {
+                    const int sig = t < half ? s0 : s1, tt = t < half ? t : t - half;
+                    bool ok = false;
+                    if (head_ok)
+                        for (size_t r = 0; r < reqs.size(); ++r)
+                            if ((sig >> r & 1) && tt >= reqs[r].first && tt < reqs[r].first + reqs[r].second) ok = true;
+                    v[(size_t)j * T + t] = ok ? 0.0 : -128.0;
+                }
+            }
+            Plaintext p;
+            ev_->encode(v, limbs, scale, p);
+            it = pt_->mask.emplace(key, std::move(p)).first;
+        }
+        out.push_back(&it->second);
+    }
+}
+
+// encoded once per level and scale (a graph replays no host encode)
+template <class EV, class CT>
+const Plaintext &BertLayerT<EV, CT>::half_plain(double value, bool upper, int limbs, double scale)
+{
+    const auto key = std::make_tuple(bits_of(value), limbs, bits_of(scale), upper ? 1 : 0);
+    auto it = pt_->half.find(key);
+    if (it == pt_->half.end()) {
+        const int half = sh_.T / 2;
+        std::vector<double> v((size_t)sh_.S, 0.0);
+        for (int j = 0; j < sh_.NB; ++j) {
+            const auto b = v.begin() + (size_t)j * sh_.T + (upper ? half : 0);
+            std::fill(b, b + half, value);
+        }
+        Plaintext e;
+        ev_->encode(v, limbs, scale, e);
+        it = pt_->half.emplace(key, std::move(e)).first;
+    }
+    return it->second;
+}
+
 // ct *= value with the constant encoded so that, after the rescale, the
 // scale is target_scale (set exactly); with lower_half the value is on the
 // lower half of each token block and 0 on the upper half
@@ -469,22 +528,8 @@ void BertLayerT<EV, CT>::exact_scale_const(CT &ct, double value, double target_s
     const double sc = q * target_scale / ct.scale();
     Plaintext scalar;
     const Plaintext *p = &scalar;
-    if (lower_half) {
-        // encoded once per level and scale (a graph replays no host encode)
-        const auto key = std::make_tuple(bits_of(value), l, bits_of(sc));
-        auto it = pt_->half.find(key);
-        if (it == pt_->half.end()) {
-            std::vector<double> v((size_t)sh_.S, 0.0);
-            for (int j = 0; j < sh_.NB; ++j)
-                std::fill(v.begin() + (size_t)j * sh_.T, v.begin() + (size_t)j * sh_.T + sh_.T / 2, value);
-            Plaintext e;
-            ev_->encode(v, l, sc, e);
-            it = pt_->half.emplace(key, std::move(e)).first;
-        }
-        p = &it->second;
-    } else {
-        ev_->encode(value, l, sc, scalar);
-    }
+    if (lower_half) p = &half_plain(value, false, l, sc);
+    else ev_->encode(value, l, sc, scalar);
     ev_->multiply_plain_inplace(ct, *p);
     ev_->rescale_to_next_inplace(ct);
     ct.scale() = target_scale;
@@ -726,7 +771,10 @@ void BertLayerT<EV, CT>::attention(std::vector<CT> &q, std::vector<CT> &k, std::
         for (int g = 1; g < n_g; ++g) qg[c][g] = std::move(r[g - 1]);
     }
 
-    // scores S_delta, masked and passed through exp
+    // scores S_delta, masked and passed through exp (offsets 2p and 2p+1
+    // folded in one ciphertext when folding: the valid slots are first token
+    // copies, all in the lower half)
+    const bool fold = sh_.folding();
     std::vector<CT> e(L);
     std::vector<const Plaintext *> mp;
     for (int d = 0; d < L; ++d) {
@@ -750,23 +798,48 @@ void BertLayerT<EV, CT>::attention(std::vector<CT> &q, std::vector<CT> &k, std::
         masks(d, 0, acc.limbs(), acc.scale(), mp);
         mul_plain_each(ev, acc, mp);
         ev.rescale_to_next_inplace(acc);
-        masks(d, 1, acc.limbs(), acc.scale(), mp);
-        add_plain_each(ev, acc, mp);
+        if (!fold) {
+            masks(d, 1, acc.limbs(), acc.scale(), mp);
+            add_plain_each(ev, acc, mp);
+        }
         e[d] = std::move(acc);
     }
+    if (fold) {
+        fold_halves(e);
+        for (size_t p = 0; p < e.size(); ++p) {
+            fold_masks((int)p, e[p].limbs(), e[p].scale(), mp);
+            add_plain_each(ev, e[p], mp);
+        }
+    }
+    mark("attention scores");
     {
         std::vector<CT *> p;
         for (auto &x : e) p.push_back(&x);
         each(ev, p, 64, [&](CT &x) { x = ck_.exp(x); });
     }
+    mark("attention exp");
 
     // row sums over delta, the inverse after a bootstrap (softmax.cpp:24-35)
     CT sum = e[0];
-    for (int d = 1; d < L; ++d) ev.add_inplace(sum, e[d]);
+    for (size_t d = 1; d < e.size(); ++d) ev.add_inplace(sum, e[d]);
     {
+        const double c = 0.01 / sh_.rowsum_shrink;
         Plaintext delta;
-        ev.encode(0.01 / sh_.rowsum_shrink, sum.limbs(), sum.scale(), delta);
-        ev.multiply_plain_inplace(sum, delta);
+        ev.encode(c, sum.limbs(), sum.scale(), delta);
+        if (fold) {
+            // each half adds the other half of its own block (masked in the
+            // constant product the sum takes anyway)
+            CT up, down;
+            ev.rotate_vector(sum, sh_.T / 2, up);
+            ev.rotate_vector(sum, sh_.S - sh_.T / 2, down);
+            ev.multiply_plain_inplace(up, half_plain(c, false, up.limbs(), sum.scale()));
+            ev.multiply_plain_inplace(down, half_plain(c, true, down.limbs(), sum.scale()));
+            ev.multiply_plain_inplace(sum, delta);
+            ev.add_inplace(sum, up);
+            ev.add_inplace(sum, down);
+        } else {
+            ev.multiply_plain_inplace(sum, delta);
+        }
         ev.rescale_to_next_inplace(sum);
         sum.scale() /= sh_.rowsum_shrink;
     }
@@ -780,12 +853,15 @@ void BertLayerT<EV, CT>::attention(std::vector<CT> &q, std::vector<CT> &k, std::
         ev.rescale_to_next_inplace(inv);
     }
     ev.mod_switch_to_inplace(inv, e[0].limbs());
+    mark("attention row sums");
     // P_delta = exp(S_delta) * inverse(sum) (softmax.cpp:37-40)
-    for (int d = 0; d < L; ++d) {
-        ev.multiply_inplace(e[d], inv);
-        ev.relinearize_inplace(e[d]);
-        ev.rescale_to_next_inplace(e[d]);
+    for (auto &x : e) {
+        ev.multiply_inplace(x, inv);
+        ev.relinearize_inplace(x);
+        ev.rescale_to_next_inplace(x);
     }
+    if (fold) unfold_halves(e, L);
+    mark("attention probabilities");
 
     // O_c = sum_g rot(sum_b rot(P_{G g + b}, -G g) * rot(V_c, b), G g)
     o.assign(nh, CT());
@@ -925,7 +1001,7 @@ void BertLayerT<EV, CT>::forward(const std::vector<CT> &x_in, std::vector<CT> &o
     mark("qk bootstraps");
     std::vector<CT> o, a;
     attention(q, k, v, o);
-    mark("attention");
+    mark("attention values");
     project(o, LT_O, a, fold);
     // residual + LayerNorm (two hidden ciphertexts folded in one from here
     // to the layer's output when folding)

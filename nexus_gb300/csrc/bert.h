@@ -71,9 +71,12 @@
 // the upper half, never read for a first copy, holds other tokens' values of
 // the same magnitude.  Folded: Q and K through their bootstrap (K, read at
 // both token copies, is unfolded with the copies that reach the upper half
-// rebuilt from its tokens by masked rotations, one level), and the hidden
-// and FFN activations from the output projection to the layer's output
-// (LayerNorm adds the two halves' feature sums with one more rotation).
+// rebuilt from its tokens by masked rotations, one level); the attention's
+// scores of offsets 2p and 2p+1 through their exp and the probabilities
+// (P is read at the first copies only; each half's row sum takes the other
+// half of its own block); and the hidden and FFN activations from the
+// output projection to the layer's output (LayerNorm adds the two halves'
+// feature sums with one more rotation).
 #pragma once
 #include <cstdint>
 #include <map>
@@ -141,8 +144,9 @@ struct BertPlaintexts {
     std::map<DKey, Plaintext> diag;
     std::map<std::tuple<int, int, int, uint64_t, int>, Plaintext> mask;
     std::map<std::tuple<int, int, int, uint64_t>, Plaintext> bias;
-    // a value on the lower half of every token block: (value bits, limbs, scale bits)
-    std::map<std::tuple<uint64_t, int, uint64_t>, Plaintext> half;
+    // a value on the lower or upper half of every token block:
+    // (value bits, limbs, scale bits, upper)
+    std::map<std::tuple<uint64_t, int, uint64_t, int>, Plaintext> half;
     size_t count() const { return diag.size() + mask.size() + bias.size() + half.size(); }
 };
 
@@ -206,6 +210,11 @@ private:
     void encode_diagonals(int which, int limbs, double scale, bool lower_half);
     const Plaintext &bias_plain(int which, int ct, int limbs, double scale, bool lower_half);
     void masks(int delta, int kind, int limbs, double scale, std::vector<const Plaintext *> &out);
+    // the -128 masks of two offsets folded in one ciphertext (offset 2 pair in
+    // the lower half, 2 pair + 1 in the upper), per lane element
+    void fold_masks(int pair, int limbs, double scale, std::vector<const Plaintext *> &out);
+    // `value` on the lower (or upper) half of every token block, 0 elsewhere
+    const Plaintext &half_plain(double value, bool upper, int limbs, double scale);
     // per lane: the lower half of the block (shift 0), or the tokens whose
     // copy lies `shift` slots on in the upper half; encoded at the scale of
     // the prime the rescale drops

@@ -22,8 +22,10 @@ through their bootstrap, the hidden and FFN activations from the output
 projection to the layer's output; an unfold gives 2i as the folded one and
 2i+1 as its rotation by T/2 (Q at QK_LIMBS; K one level above it, with every
 request's second token copy in the upper half rebuilt by masked rotations),
-and LayerNorm on folded ciphertexts adds the halves' sums with one more
-rotation.
+the attention's scores of offsets 2p and 2p + 1 go folded through their exp
+and the probabilities (each half's row sum adds the other half of its own
+block), and LayerNorm on folded ciphertexts adds the halves' sums with one
+more rotation.
 """
 from __future__ import annotations
 
@@ -312,6 +314,29 @@ class BertLayer:
         sc = float(self.ev.q[limbs - 1]) if kind == 0 else scale
         return self.ev.encode(v, sc, limbs)
 
+    def _fold_mask(self, pair, limbs, scale):
+        """BertLayerT::fold_masks for this lane: the -128 masks of offsets
+        2 pair (lower half) and 2 pair + 1 (upper half) in one plaintext."""
+        sh = self.sh
+        reqs = sh.lanes[self.lane]
+        half = sh.T // 2
+        v = np.zeros(sh.S)
+        for j in range(sh.NB):
+            head_ok = (j % sh.H2) < sh.heads
+            for t in range(sh.T):
+                d, tt = (2 * pair, t) if t < half else (2 * pair + 1, t - half)
+                ok = head_ok and d < sh.Lmax and any(d < Lr and o <= tt < o + Lr for (o, Lr) in reqs)
+                v[j * sh.T + t] = 0.0 if ok else -128.0
+        return self.ev.encode(v, scale, limbs)
+
+    def _half(self, value, upper, limbs, scale):
+        """BertLayerT::half_plain: value on one half of every token block."""
+        sh = self.sh
+        block = np.zeros(sh.T)
+        block[sh.T // 2:] = value if upper else 0.0
+        block[:sh.T // 2] = 0.0 if upper else value
+        return self.ev.encode(np.tile(block, sh.NB), scale, limbs)
+
     # -- blocks -----------------------------------------------------------------
     def attention(self, q, k, v):
         ev, sh, ck = self.ev, self.sh, self.ck
@@ -339,18 +364,35 @@ class BertLayer:
             if g:
                 acc = ev.rotate(acc, g * G)
             acc = ev.rescale(ev.multiply_plain(acc, self._mask(d, 0, acc.limbs, acc.scale)))
-            acc = ev.add_plain(acc, self._mask(d, 1, acc.limbs, acc.scale))
-            e.append(ck.exp(acc))
+            if not sh.folding:
+                acc = ev.add_plain(acc, self._mask(d, 1, acc.limbs, acc.scale))
+            e.append(acc)
+        if sh.folding:
+            # offsets 2p and 2p + 1 in the two halves of one ciphertext
+            e = self.fold_halves(e)
+            e = [ev.add_plain(c, self._fold_mask(p, c.limbs, c.scale)) for p, c in enumerate(e)]
+        e = [ck.exp(c) for c in e]
         total = e[0]
-        for d in range(1, Lm):
-            total = ev.add(total, e[d])
-        total = ev.rescale(ev.multiply_plain(total, ev.encode_scalar(0.01 / sh.rowsum_shrink, total.scale,
-                                                                     total.limbs)))
+        for c in e[1:]:
+            total = ev.add(total, c)
+        cst = 0.01 / sh.rowsum_shrink
+        delta = ev.encode_scalar(cst, total.scale, total.limbs)
+        if sh.folding:
+            # each half adds the other half of its own block
+            up = ev.multiply_plain(ev.rotate(total, sh.T // 2), self._half(cst, False, total.limbs, total.scale))
+            down = ev.multiply_plain(ev.rotate(total, S - sh.T // 2),
+                                     self._half(cst, True, total.limbs, total.scale))
+            total = ev.add(ev.add(ev.multiply_plain(total, delta), up), down)
+        else:
+            total = ev.multiply_plain(total, delta)
+        total = ev.rescale(total)
         total.scale /= sh.rowsum_shrink
         inv = ck.inverse(self.bootstrap_all([total])[0])
         inv = ev.rescale(ev.multiply_plain(inv, ev.encode_scalar(0.01, inv.scale, inv.limbs)))
         inv = ev.mod_switch_to(inv, e[0].limbs)
         p = [ev.rescale(ev.relinearize(ev.multiply(ed, inv))) for ed in e]
+        if sh.folding:
+            p = self.unfold_halves(p, Lm)
         pg = [[(ev.rotate(p[g * G + b], S - g * G) if g else p[b]) for b in range(G) if g * G + b < Lm]
               for g in range(n_g)]
         o = []
