@@ -787,10 +787,6 @@ void BertLayerT<EV, CT>::attention(std::vector<CT> &q, std::vector<CT> &k, std::
         }
         ev.relinearize_inplace(acc);
         ev.rescale_to_next_inplace(acc);
-        for (int m = 1; m < sh_.KB; m <<= 1) {
-            ev.rotate_vector(acc, sh_.H2 * sh_.T * m, t);
-            ev.add_inplace(acc, t);
-        }
         if (g) {
             ev.rotate_vector(acc, g * G, t);
             acc = std::move(t);
@@ -798,18 +794,21 @@ void BertLayerT<EV, CT>::attention(std::vector<CT> &q, std::vector<CT> &k, std::
         masks(d, 0, acc.limbs(), acc.scale(), mp);
         mul_plain_each(ev, acc, mp);
         ev.rescale_to_next_inplace(acc);
-        if (!fold) {
-            masks(d, 1, acc.limbs(), acc.scale(), mp);
-            add_plain_each(ev, acc, mp);
-        }
         e[d] = std::move(acc);
     }
-    if (fold) {
-        fold_halves(e);
-        for (size_t p = 0; p < e.size(); ++p) {
-            fold_masks((int)p, e[p].limbs(), e[p].scale(), mp);
-            add_plain_each(ev, e[p], mp);
+    // the sum over the KB blocks of each head commutes with the zeroing mask
+    // (the same on every block of a head) and with the fold, so it is taken
+    // once per ciphertext after both; then the -128 masks
+    if (fold) fold_halves(e);
+    for (size_t p = 0; p < e.size(); ++p) {
+        CT t;
+        for (int m = 1; m < sh_.KB; m <<= 1) {
+            ev.rotate_vector(e[p], sh_.H2 * sh_.T * m, t);
+            ev.add_inplace(e[p], t);
         }
+        if (fold) fold_masks((int)p, e[p].limbs(), e[p].scale(), mp);
+        else masks((int)p, 1, e[p].limbs(), e[p].scale(), mp);
+        add_plain_each(ev, e[p], mp);
     }
     mark("attention scores");
     {

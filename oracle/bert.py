@@ -357,21 +357,24 @@ class BertLayer:
                 t = ev.multiply(qg[c][g], kb[c][b])
                 acc = t if acc is None else ev.add(acc, t)
             acc = ev.rescale(ev.relinearize(acc))
-            m = 1
-            while m < sh.KB:
-                acc = ev.add(acc, ev.rotate(acc, sh.H2 * sh.T * m))
-                m <<= 1
             if g:
                 acc = ev.rotate(acc, g * G)
             acc = ev.rescale(ev.multiply_plain(acc, self._mask(d, 0, acc.limbs, acc.scale)))
-            if not sh.folding:
-                acc = ev.add_plain(acc, self._mask(d, 1, acc.limbs, acc.scale))
             e.append(acc)
         if sh.folding:
             # offsets 2p and 2p + 1 in the two halves of one ciphertext
             e = self.fold_halves(e)
-            e = [ev.add_plain(c, self._fold_mask(p, c.limbs, c.scale)) for p, c in enumerate(e)]
-        e = [ck.exp(c) for c in e]
+        # the sum over the KB blocks of each head, once per ciphertext after
+        # the zeroing mask and the fold (it commutes with both), then -128
+        summed = []
+        for p, c in enumerate(e):
+            m = 1
+            while m < sh.KB:
+                c = ev.add(c, ev.rotate(c, sh.H2 * sh.T * m))
+                m <<= 1
+            mask = self._fold_mask(p, c.limbs, c.scale) if sh.folding else self._mask(p, 1, c.limbs, c.scale)
+            summed.append(ev.add_plain(c, mask))
+        e = [ck.exp(c) for c in summed]
         total = e[0]
         for c in e[1:]:
             total = ev.add(total, c)
