@@ -742,7 +742,9 @@ int nexus_bert_layer_set_boot_pack(nexus_bert_layer *layer, int enable);
 /* With token_fold on, and when every request's tokens lie in token slots
  * [0, T/2), two ciphertexts share one, the second's tokens in the upper half
  * of every token block: Q and K through their bootstrap (K's second token
- * copies rebuilt by masked rotations when unfolded), and the hidden and FFN
+ * copies rebuilt by masked rotations when unfolded), the attention's scores
+ * of offsets 2p and 2p+1 through their exp and the probabilities, and the
+ * hidden and FFN
  * activations from the output projection to the layer's output (both
  * residual bootstraps and LayerNorms, the FFN's bootstraps and GELU).  The
  * maps feeding a fold (Q, K, output, W1, W2) and the residual input write the
