@@ -744,18 +744,17 @@ int nexus_bert_layer_set_boot_pack(nexus_bert_layer *layer, int enable);
  * of every token block: Q and K through their bootstrap (K's second token
  * copies rebuilt by masked rotations when unfolded), the attention's scores
  * of offsets 2p and 2p+1 through their exp and the probabilities, and the
- * hidden and FFN
- * activations from the output projection to the layer's output (both
- * residual bootstraps and LayerNorms, the FFN's bootstraps and GELU).  The
- * maps feeding a fold (Q, K, output, W1, W2) and the residual input write the
- * lower half only; a fold is one rotation of -T/2, an unfold gives
- * ciphertext 2i+1 as the folded one rotated by T/2 (Q at the attention's
- * level), and LayerNorm adds the two halves' feature sums with one more
- * rotation.  30 bootstraps per BERT-base layer instead of 54, half the
- * GELUs and LayerNorm products; the rotation steps include +-T/2 and the
- * copy shifts (-L for every request length L whose second copy reaches the
- * upper half) whenever the fold applies.  On by default; no counterpart in the reference (NEXUS
- * has no layer). */
+ * hidden and FFN activations from the output projection to the layer's
+ * output (both residual bootstraps and LayerNorms, the FFN's bootstraps and
+ * GELU).  The maps feeding a fold (Q, K, output, W1, W2) and the residual
+ * input write the lower half only; a fold is one rotation of -T/2, an
+ * unfold gives ciphertext 2i+1 as the folded one rotated by T/2 (Q at the
+ * attention's level), and LayerNorm adds the two halves' feature sums with
+ * one more rotation.  30 bootstraps per BERT-base layer instead of 54, half
+ * the exps, GELUs and LayerNorm products; the rotation steps include +-T/2
+ * and the copy shifts (-L for every request length L whose second copy
+ * reaches the upper half) whenever the fold applies.  On by default; no
+ * counterpart in the reference (NEXUS has no layer). */
 int nexus_bert_layer_set_token_fold(nexus_bert_layer *layer, int enable);
 int nexus_bert_layer_stage_times(nexus_bert_layer *layer, int lockstep, int lane, double *ms, char *names,
                                  size_t names_capacity, int *count, int capacity);
