@@ -135,6 +135,8 @@ void BertShape::derive(size_t slots)
     Lmax = 0;
     for (auto &lane : lanes) {
         if (lane.empty()) throw std::invalid_argument("empty lane");
+        // the attention's masks key a lane's requests as bits of one 16-bit field
+        if (lane.size() > 16) throw std::invalid_argument("more than 16 requests in a lane");
         std::vector<std::pair<int, int>> r = lane;
         std::sort(r.begin(), r.end());
         int end = 0;
