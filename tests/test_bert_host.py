@@ -185,3 +185,25 @@ def test_unfold_copies_rebuilds_the_second_token_copies():
                 for (o, L) in reqs:
                     sl = slice(j * T + o, j * T + o + 2 * L)
                     assert np.allclose(got.v[sl], want[sl])
+
+
+def test_bench_bootstrap_count_follows_the_layer_shape():
+    """bench.py's bootstraps per layer (the CPU lower bound's multiplier) is the
+    count the layer's shape gives: per lane, Q and K folded two per ciphertext
+    and refreshed in pairs, the row sum alone, each folded residual and the
+    folded FFN hidden activations in pairs (an odd one alone)."""
+    import bench
+    from oracle import bert as OB
+
+    def pairs(n):
+        return (n + 1) // 2
+    sh = NB.BertShape()                       # BERT-base, 128 | 32 + 64 tokens
+    slots = 1 << 15
+    osh = OB.Shape(slots, sh.hidden, sh.heads, sh.head_dim, sh.ffn, sh.T, sh.lanes, sh.boot_shrink)
+    assert osh.folding and (osh.n_head, osh.n_hid, osh.n_ffn) == (8, 6, 24)
+    for pack in (True, False):
+        for fold in (True, False):
+            f = pairs if fold else (lambda n: n)
+            refresh = pairs if pack else (lambda n: n)
+            per_lane = (refresh(2 * f(osh.n_head)) + 1 + 2 * refresh(f(osh.n_hid)) + refresh(f(osh.n_ffn)))
+            assert bench.bert_bootstraps(pack, fold) == len(sh.lanes) * per_lane, (pack, fold)
