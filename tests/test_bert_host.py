@@ -207,3 +207,120 @@ def test_bench_bootstrap_count_follows_the_layer_shape():
             refresh = pairs if pack else (lambda n: n)
             per_lane = (refresh(2 * f(osh.n_head)) + 1 + 2 * refresh(f(osh.n_hid)) + refresh(f(osh.n_ffn)))
             assert bench.bert_bootstraps(pack, fold) == len(sh.lanes) * per_lane, (pack, fold)
+
+
+class _Enc:
+    """A stand-in ciphertext that keeps CKKS's encoded slot values m (the
+    decoded value is m / scale), so that scale bookkeeping (rescale by the
+    dropped prime, a scale reinterpreted by hand) means what it does on real
+    ciphertexts."""
+
+    def __init__(self, m, limbs, scale):
+        self.m, self.limbs, self.scale = np.asarray(m, dtype=float), limbs, scale
+
+    def value(self):
+        return self.m / self.scale
+
+
+class _EncPlain:
+    def __init__(self, m, scale):
+        self.m, self.scale = m, scale
+
+
+class _EncEvaluator:
+    """The oracle evaluator's interface on _Enc values (exact arithmetic on
+    the encoded slot values, no noise)."""
+
+    q = [float(2 ** 40 + 2 * i + 1) for i in range(32)]
+
+    def rotate(self, x, k):
+        return _Enc(np.roll(x.m, -k), x.limbs, x.scale)
+
+    def add(self, a, b):
+        assert np.isclose(a.scale, b.scale, rtol=1e-9)
+        return _Enc(a.m + b.m, a.limbs, a.scale)
+
+    def multiply(self, a, b):
+        return _Enc(a.m * b.m, min(a.limbs, b.limbs), a.scale * b.scale)
+
+    def relinearize(self, x):
+        return x
+
+    def rescale(self, x):
+        qd = self.q[x.limbs - 1]
+        return _Enc(x.m / qd, x.limbs - 1, x.scale / qd)
+
+    def mod_switch_to(self, x, limbs):
+        return _Enc(x.m, limbs, x.scale)
+
+    def encode(self, v, scale, limbs):
+        return _EncPlain(np.asarray(v, dtype=float) * scale, scale)
+
+    def encode_scalar(self, value, scale, limbs):
+        return _EncPlain(value * scale, scale)
+
+    def multiply_plain(self, a, p):
+        return _Enc(a.m * p.m, a.limbs, a.scale * p.scale)
+
+    def add_plain(self, a, p):
+        assert np.isclose(a.scale, p.scale, rtol=1e-9)
+        return _Enc(a.m + p.m, a.limbs, a.scale)
+
+
+class _EncCkks:
+    """NEXUS's exp and inverse on decoded values (the oracle's CKKSEvaluator
+    restates their ciphertext sequences; here only the layer's use of them
+    is under test)."""
+
+    def exp(self, x):
+        return _Enc(NB.nexus_exp(x.value()) * x.scale, x.limbs - 8, x.scale)
+
+    def inverse(self, x):
+        return _Enc(NB.nexus_inverse(x.value()) * x.scale, x.limbs - 8, x.scale)
+
+
+def test_attention_fold_slot_algebra():
+    """The oracle's attention block (BertLayerT::attention) on exact encoded
+    slot values, with the token fold on and off: scores of offsets 2p and
+    2p+1 folded after their zeroing mask, the head block sums per folded
+    pair, the folded -128 masks, the row sums that add the other half of
+    their own block (and take the 0.01 / 2 constant with the scale
+    reinterpreted), P unfolded for the values.  Both give, on every first
+    token copy, NEXUS's softmax attention of each request computed in numpy."""
+    from oracle import bert as OB
+    S, T, heads, dh = 512, 32, 2, 16
+    lanes = [[(0, 6)], [(0, 3), (8, 5)]]
+    delta = 2.0 ** 30
+    rng = np.random.default_rng(21)
+    for fold in (True, False):
+        osh = OB.Shape(S, heads * dh, heads, dh, 64, T, lanes, 1.0, token_fold=fold)
+        assert osh.folding == fold and osh.n_head == 2 and osh.KB == 8
+        for lane, reqs in enumerate(lanes):
+            layer = OB.BertLayer.__new__(OB.BertLayer)
+            layer.ev, layer.sh, layer.lane, layer.delta, layer.ck = _EncEvaluator(), osh, lane, delta, _EncCkks()
+            layer.bootstrap_all = lambda cts: [_Enc(c.value() * delta, 20, delta) for c in cts]
+            toks = {name: [rng.normal(0, 0.5, (L, heads * dh)) for (_, L) in reqs] for name in "qkv"}
+
+            def pack(x):
+                # head layout: feature h*dh + k in ciphertext k // KB, block (k % KB) * H2 + h
+                out = np.zeros((osh.n_head, S))
+                for (o, L), xr in zip(reqs, x):
+                    for h in range(heads):
+                        for k in range(dh):
+                            c, blk = k // osh.KB, (k % osh.KB) * osh.H2 + h
+                            out[c, blk * T + o:blk * T + o + L] = xr[:, h * dh + k]
+                            out[c, blk * T + o + L:blk * T + o + 2 * L] = xr[:, h * dh + k]
+                return [_Enc(v * delta, 20, delta) for v in out]
+            o = layer.attention(pack(toks["q"]), pack(toks["k"]), pack(toks["v"]))
+            got = [c.value() for c in o]
+            for r, (o_r, L) in enumerate(reqs):
+                for h in range(heads):
+                    sl = slice(h * dh, (h + 1) * dh)
+                    s = toks["q"][r][:, sl] @ toks["k"][r][:, sl].T / np.sqrt(dh)
+                    e = NB.nexus_exp(s)
+                    p = e * (NB.nexus_inverse(0.01 * e.sum(axis=1, keepdims=True)) * 0.01)
+                    want = p @ toks["v"][r][:, sl]
+                    for k in range(dh):
+                        c, blk = k // osh.KB, (k % osh.KB) * osh.H2 + h
+                        assert np.allclose(got[c][blk * T + o_r:blk * T + o_r + L], want[:, k], rtol=1e-6,
+                                           atol=1e-9), (fold, lane, r, h, k)
