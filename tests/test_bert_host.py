@@ -246,6 +246,9 @@ class _EncEvaluator:
     def relinearize(self, x):
         return x
 
+    def square(self, x):
+        return self.multiply(x, x)
+
     def rescale(self, x):
         qd = self.q[x.limbs - 1]
         return _Enc(x.m / qd, x.limbs - 1, x.scale / qd)
@@ -277,6 +280,9 @@ class _EncCkks:
 
     def inverse(self, x):
         return _Enc(NB.nexus_inverse(x.value()) * x.scale, x.limbs - 8, x.scale)
+
+    def invert_sqrt(self, x, d_newt, d_gold):
+        return _Enc(NB.nexus_invert_sqrt(x.value(), d_newt, d_gold) * x.scale, x.limbs - 17, x.scale)
 
 
 def test_attention_fold_slot_algebra():
@@ -324,3 +330,36 @@ def test_attention_fold_slot_algebra():
                         c, blk = k // osh.KB, (k % osh.KB) * osh.H2 + h
                         assert np.allclose(got[c][blk * T + o_r:blk * T + o_r + L], want[:, k], rtol=1e-6,
                                            atol=1e-9), (fold, lane, r, h, k)
+
+
+def test_layer_forward_slot_algebra(monkeypatch):
+    """The oracle's whole layer (BertLayerT::forward) on exact encoded slot
+    values, with the token fold on and off: the masked residual input, Q and
+    K folded and unfolded (K's copies rebuilt), the attention, the folded
+    residual bootstraps and LayerNorms (the halves' feature sums), the folded
+    FFN and the output unfold.  Bootstraps keep the value; exp, inverse,
+    invert_sqrt and GELU are NEXUS's approximations on decoded values.  The
+    first token copies of the output equal the FP64 layer with the same
+    approximations (nexus_gb300.bert.layer_reference)."""
+    from oracle import bert as OB
+    S = 512
+    sh = NB.BertShape(hidden=32, heads=2, head_dim=16, ffn=64, T=32, lanes=[[(0, 10)], [(0, 3), (6, 7)]])
+    w = NB.random_weights(sh, np.random.default_rng(3), std=0.2)
+    delta = 2.0 ** 30
+    monkeypatch.setattr(OB.L, "gelu", lambda ck, c: _Enc(NB.nexus_gelu(c.value()) * c.scale, c.limbs - 18, c.scale))
+    rng = np.random.default_rng(4)
+    tokens = [[rng.normal(0, 1, (L, sh.hidden)) for (_, L) in lane] for lane in sh.lanes]
+    for fold in (True, False):
+        osh = OB.Shape(S, sh.hidden, sh.heads, sh.head_dim, sh.ffn, sh.T, sh.lanes, 1.0, token_fold=fold)
+        assert osh.folding == fold and (osh.n_hid, osh.n_head, osh.n_ffn) == (2, 2, 4)
+        assert osh.copy_shifts == [7, 10]
+        for lane in range(len(sh.lanes)):
+            layer = OB.BertLayer.__new__(OB.BertLayer)
+            layer.ev, layer.sh, layer.w, layer.lane, layer.delta = _EncEvaluator(), osh, w, lane, delta
+            layer.ck = _EncCkks()
+            layer.bootstrap_all = lambda cts: [_Enc(c.value() * delta, 20, delta) for c in cts]
+            x = [_Enc(v * delta, 20, delta) for v in NB.pack_lane(sh, S, lane, tokens[lane])]
+            out = layer.forward(x)
+            got = NB.unpack_lane(sh, S, lane, np.stack([c.value() for c in out]))
+            for g, r in zip(got, NB.layer_reference(sh, w, tokens[lane])):
+                assert np.allclose(g, r, rtol=1e-6, atol=1e-8), (fold, lane, float(np.max(np.abs(g - r))))
